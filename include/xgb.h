@@ -1,0 +1,176 @@
+/*
+ * xgb.h -- C-ABI of the GB300 block-sparse tensor backend (kernel level).
+ *
+ * This is the plugin boundary an Xped storage/matrix backend binds: every
+ * entry point takes plain device pointers, element offsets and sizes, and
+ * processes ALL sector blocks of one tensor operation in one grouped launch.
+ * Each replaces a per-block loop of the reference (paths relative to the
+ * Xped source tree):
+ *
+ *   xgb_grouped_gemm   TensorBase::operator*  (src/Core/TensorBase.cpp:237-288),
+ *                      PlainInterface::prod  (src/Interfaces/MatrixInterface_Eigen_impl.cpp:156-160),
+ *                      AdjointOp operands    (include/Xped/Core/AdjointOp.hpp:49-59)
+ *   xgb_permute        Tensor::permute_impl  (src/Core/Tensor.cpp:83-214):
+ *                      subBlock + shuffle + add_to_block_from_tensor
+ *                      (src/Interfaces/PlainInterface_Eigen_impl.cpp:32-42,68-79)
+ *   xgb_batched_svd    full_svd_impl / PlainInterface::svd (src/Core/Tensor.cpp:494-521,
+ *                      src/Interfaces/PlainInterface_Eigen_impl.cpp:114-127)
+ *   xgb_truncate       cutoff_matrices       (src/Core/Tensor.cpp:523-633)
+ *   xgb_batched_qr     Tensor::tQR / MatrixInterface::qr (src/Core/Tensor.cpp:757-780,
+ *                      src/Interfaces/MatrixInterface_Eigen_impl.cpp:250-256)
+ *   xgb_absmax,
+ *   xgb_scale_by_inv_absmax  TensorBase::maxNorm + T*(1/maxNorm) (src/Core/TensorBase.cpp:48-56,
+ *                      src/PEPS/CTM.cpp:1372,1383,1405)
+ *   xgb_diag_apply     TensorBase::diag_sqrt / diag_inv (src/Core/TensorBase.cpp:191-201)
+ *   xgb_copy2d_batched block slicing in cutoff_matrices (src/Core/Tensor.cpp:609-630)
+ *
+ * Conventions: all matrices are column-major FP64 inside one flat buffer per
+ * tensor; offsets and leading dimensions are in elements.  Descriptor arrays
+ * live in HOST memory and are copied by the call.  Every call is
+ * stream-ordered on the library's stream (or `stream` when non-NULL) and
+ * returns 0 on success or a negative XGB_E_* code; xgb_last_error() gives
+ * the message.  No call allocates caller-visible memory except xgb_malloc.
+ */
+#ifndef XGB_H_
+#define XGB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  XGB_OK = 0,
+  XGB_E_CUDA = -1,      /* a CUDA runtime call failed */
+  XGB_E_OOM = -2,       /* device allocation failed */
+  XGB_E_BADPLAN = -3,   /* inconsistent descriptors or sizes */
+  XGB_E_TIMEOUT = -4,   /* a bounded device wait gave up */
+  XGB_E_NONFINITE = -5, /* NaN/Inf met where a finite value is required */
+  XGB_E_NOINIT = -6,    /* xgb_init was not called */
+  XGB_E_UNSUPPORTED = -7
+};
+
+/* precision forms of the block GEMM */
+enum { XGB_PREC_FP64 = 0, XGB_PREC_3XTF32 = 1, XGB_PREC_BF16X9 = 2 };
+
+/* ---------------------------------------------------------------- runtime */
+int xgb_init(int device);
+int xgb_shutdown(void);
+const char* xgb_last_error(void);
+int xgb_synchronize(void);
+int xgb_malloc(void** ptr, size_t bytes);
+int xgb_free(void* ptr);
+int xgb_memcpy_h2d(void* dst, const void* src, size_t bytes);
+int xgb_memcpy_d2h(void* dst, const void* src, size_t bytes);
+int xgb_memset_zero(void* dst, size_t bytes);
+/* number of kernels this library launched since xgb_init */
+int64_t xgb_launch_count(void);
+/* the library's CUDA stream (cudaStream_t) for callers that order work with it */
+void* xgb_stream_handle(void);
+/* Instrumentation: with profiling enabled every launch is bracketed by CUDA
+   events on the library stream.  kind: 0 gemm, 1 permute, 2 svd, 3 truncate,
+   4 qr, 5 absmax, 6 scale, 7 copy2d, 8 diag, 9 tensor-core gemm.  work is the
+   algorithmic flop count (GEMMs) or bytes moved (everything else). */
+int xgb_profile_enable(int on);
+int xgb_profile_reset(void);
+int xgb_profile_read(int kind, int64_t* launches, double* ms, double* work);
+/* 16 user event slots recorded on the library stream */
+int xgb_event_record(int slot);
+double xgb_event_elapsed_ms(int a, int b);
+
+/* ------------------------------------------------------- grouped block GEMM */
+typedef struct xgb_gemm_desc {
+  int64_t m, n, k;        /* C_g is m x n, inner dimension k (k == 0 writes beta*C) */
+  int64_t a_off, lda;     /* op(A_g) = trans_a ? A^T : A, A stored lda-strided */
+  int64_t b_off, ldb;
+  int64_t c_off, ldc;
+  int32_t trans_a, trans_b;
+} xgb_gemm_desc;
+
+/* C_g = alpha * op(A_g) op(B_g) + beta * C_g for every group g, one launch. */
+int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, const double* A, const double* B,
+                     double* C, double alpha, double beta, void* stream);
+
+/* ------------------------------------------------------------------ permute */
+#define XGB_MAX_LEGS 8
+typedef struct xgb_perm_task {
+  int64_t dst_base;                   /* element offset of the output sub-block origin */
+  int64_t nelem;                      /* prod(dims) */
+  int32_t rank;                       /* legs of the sub-tensor (<= XGB_MAX_LEGS) */
+  int32_t n_contrib;                  /* number of source sub-blocks that add into it */
+  int32_t contrib0;                   /* first entry in the contribution array */
+  int32_t pad;
+  int32_t dims[XGB_MAX_LEGS];         /* output sub-tensor extents, leg 0 fastest */
+  int64_t dst_stride[XGB_MAX_LEGS];   /* element stride in dst per output leg */
+} xgb_perm_task;
+
+typedef struct xgb_perm_contrib {
+  int64_t src_base;                   /* element offset of the source sub-block origin */
+  double coeff;                       /* recoupling coefficient (1, +-1, or SU(2) value) */
+  int64_t src_stride[XGB_MAX_LEGS];   /* element stride in src per OUTPUT leg */
+} xgb_perm_contrib;
+
+/* dst[task elements] = sum_c coeff_c * src[...]; tasks must tile disjoint
+   regions of dst.  Elements of dst not covered by a task are left untouched. */
+int xgb_permute(int n_tasks, const xgb_perm_task* tasks, int n_contrib, const xgb_perm_contrib* contribs,
+                const double* src, double* dst, void* stream);
+
+/* -------------------------------------------------------------- batched SVD */
+typedef struct xgb_svd_desc {
+  int64_t m, n;           /* block is m x n, k = min(m, n) singular triplets */
+  int64_t a_off;          /* A block, ld = m */
+  int64_t u_off;          /* U block m x k, ld = m */
+  int64_t s_off;          /* k singular values, descending */
+  int64_t vt_off;         /* V^T block k x n, ld = k */
+} xgb_svd_desc;
+
+/* Thin SVD of every block (FP64, one-sided Jacobi).  Singular vectors are
+   sign-normalised: the entry of largest magnitude of each u_j is positive.
+   `work` must hold xgb_svd_workspace_bytes(...) bytes. */
+size_t xgb_svd_workspace_bytes(int n, const xgb_svd_desc* descs);
+int xgb_batched_svd(int n, const xgb_svd_desc* descs, const double* A, double* U, double* S, double* Vt, void* work,
+                    void* stream);
+
+/* ---------------------------------------------------------------- truncation */
+/* Global truncation over all sectors' singular values (cutoff_matrices):
+   s holds every sector's values back to back (descending within a sector),
+   sector g owning [s_begin[g], s_begin[g+1]).  Writes keep[g] and
+   out2[0] = truncated weight, out2[1] = entropy (device pointers). */
+int xgb_truncate(int n_sectors, const int64_t* s_begin_host, const int32_t* degeneracy_host, const double* s,
+                 int64_t max_keep, double eps_svd, int preserve_multiplets, int32_t* keep_dev, double* out2_dev,
+                 void* stream);
+
+/* ------------------------------------------------------------ batched QR */
+typedef struct xgb_qr_desc {
+  int64_t m, n;           /* block m x n */
+  int64_t a_off;          /* ld = m */
+  int64_t q_off, q_cols;  /* Q block m x q_cols (ld = m), zero padded past min(m,n) */
+  int64_t r_off, r_rows;  /* R block r_rows x n (ld = r_rows), zero padded past min(m,n) */
+} xgb_qr_desc;
+size_t xgb_qr_workspace_bytes(int n, const xgb_qr_desc* descs);
+int xgb_batched_qr(int n, const xgb_qr_desc* descs, const double* A, double* Q, double* R, void* work, void* stream);
+
+/* ------------------------------------------------------------ elementwise */
+/* out_dev[0] = max |x_i| over n elements (0 for n == 0) */
+int xgb_absmax(const double* x, int64_t n, double* out_dev, void* stream);
+/* x *= 1 / max|x| computed on the device (x unchanged if max == 0) */
+int xgb_scale_by_inv_absmax(double* x, int64_t n, double* scratch_dev, void* stream);
+int xgb_scale(double* x, int64_t n, double alpha, void* stream);
+
+enum { XGB_DIAG_SQRT = 0, XGB_DIAG_INV = 1, XGB_DIAG_INV_SQRT = 2 };
+typedef struct xgb_copy2d_desc {
+  int64_t src_off, src_ld, dst_off, dst_ld, rows, cols;
+} xgb_copy2d_desc;
+/* dst block = src block, column-major, for every descriptor */
+int xgb_copy2d_batched(int n, const xgb_copy2d_desc* descs, const double* src, double* dst, void* stream);
+/* dst = diag(f(src_vec)) as k x k blocks: descs use src_off (vector), dst_off, rows = cols = k */
+int xgb_diag_from_vec(int n, const xgb_copy2d_desc* descs, int fn, const double* src, double* dst, void* stream);
+/* in-place f() on the diagonal of k x k blocks (off-diagonal zeroed) */
+int xgb_diag_apply(int n, const xgb_copy2d_desc* descs, int fn, double* x, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XGB_H_ */

@@ -1,0 +1,114 @@
+/*
+ * xgb_tensor.h -- C-ABI of the GB300 backend at the Tensor-operation level.
+ *
+ * Opaque handles to leg bases, device-resident block-sparse tensors and a
+ * 1x1-cell CTM environment.  These are the calls an Xped storage backend
+ * (XPED_STORAGE=Device) makes from the Tensor core in place of its per-block
+ * loops; each replaces the reference function named beside it (paths relative
+ * to the Xped source tree).  All functions return 0 / a valid handle on
+ * success, a negative XGB_E_* code / NULL on failure (xgb_last_error()).
+ * Handles are owned by the caller and released with the matching *_release.
+ */
+#ifndef XGB_TENSOR_H_
+#define XGB_TENSOR_H_
+
+#include <stdint.h>
+
+#include "xgb.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct xgb_basis_s* xgb_basis;
+typedef struct xgb_tensor_s* xgb_tensor;
+typedef struct xgb_ctm_s* xgb_ctm;
+
+/* symmetry kinds */
+enum { XGB_SYM_U1 = 0, XGB_SYM_U1_FERMIONIC = 1, XGB_SYM_Z2 = 2, XGB_SYM_Z2_FERMIONIC = 3, XGB_SYM_SU2 = 4 };
+
+/* ------------------------------------------------------------------ bases */
+/* Qbasis::push_back per (q, dim) pair, then Qbasis::sort when sort != 0
+   (src/Core/Qbasis.cpp:34-73, 306-331). */
+xgb_basis xgb_basis_create(int sym, int n, const int32_t* qs, const int64_t* dims, int sort);
+xgb_basis xgb_basis_conj(xgb_basis b);                      /* Qbasis::conj (Qbasis.cpp:418-439) */
+xgb_basis xgb_basis_combine(xgb_basis a, xgb_basis b);      /* Qbasis::combine (Qbasis.cpp:441-495) */
+xgb_basis xgb_basis_forget_history(xgb_basis b);            /* Qbasis::forgetHistory (Qbasis.cpp:410-416) */
+/* number of irreps; fills qs/dims (may be NULL) in storage order */
+int xgb_basis_info(xgb_basis b, int32_t* qs, int64_t* dims, int* conj_flag, int* depth);
+/* fusion trees of irrep index i: per tree rank, qc, dual mask, qu[rank], dims[rank], qi[rank-2] packed into
+   `out` (int64 entries, 3 + 2*rank + max(rank-2,0) per tree); returns the number of trees, or the number of
+   int64 entries needed when out == NULL. */
+int xgb_basis_trees(xgb_basis b, int i, int64_t* out, int cap);
+void xgb_basis_release(xgb_basis b);
+
+/* ---------------------------------------------------------------- tensors */
+/* Tensor(basis_domain, basis_codomain) + setZero (include/Xped/Core/Tensor.hpp:106-110) */
+xgb_tensor xgb_tensor_zeros(int rank, const xgb_basis* dom, int corank, const xgb_basis* cod);
+/* Tensor::Identity (Tensor.hpp:229-236) */
+xgb_tensor xgb_tensor_identity(int rank, const xgb_basis* dom, int corank, const xgb_basis* cod);
+/* sectors in storage order: returns count, fills qs/rows/cols (may be NULL) */
+int xgb_tensor_sectors(xgb_tensor t, int32_t* qs, int64_t* rows, int64_t* cols);
+int64_t xgb_tensor_size(xgb_tensor t);                      /* Tensor::plainSize */
+int xgb_tensor_rank(xgb_tensor t, int* rank, int* corank);
+xgb_basis xgb_tensor_leg(xgb_tensor t, int leg);            /* uncoupled basis of leg (domain legs first) */
+xgb_basis xgb_tensor_coupled(xgb_tensor t, int codomain);   /* coupledDomain / coupledCodomain */
+/* Tensor::set_data / data(): flat column-major blocks in sector order (host buffers) */
+int xgb_tensor_upload(xgb_tensor t, const double* host, int64_t n);
+int xgb_tensor_download(xgb_tensor t, double* host, int64_t n);
+/* device pointer of the block data (after pending twists are applied) */
+double* xgb_tensor_device_data(xgb_tensor t);
+
+xgb_tensor xgb_tensor_permute(xgb_tensor t, int shift, const int32_t* p, int n);   /* Tensor::permute (Tensor.cpp:335-355) */
+xgb_tensor xgb_tensor_twist(xgb_tensor t, int leg);                                /* Tensor::twist (Tensor.cpp:357-377) */
+xgb_tensor xgb_tensor_adjoint(xgb_tensor t);                                       /* adjoint().eval() */
+xgb_tensor xgb_tensor_matmul(xgb_tensor a, xgb_tensor b, int adj_a, int adj_b);    /* operator* (TensorBase.cpp:237-288) */
+/* Tensor::contract<a1, a2, rankres> (Tensor.hpp:328-351) */
+xgb_tensor xgb_tensor_contract(xgb_tensor a, xgb_tensor b, const int32_t* a1, int n1, const int32_t* a2, int n2,
+                               int rankres);
+xgb_tensor xgb_tensor_scale(xgb_tensor t, double s);
+double xgb_tensor_max_norm(xgb_tensor t);                                          /* TensorBase::maxNorm */
+xgb_tensor xgb_tensor_normalize_max(xgb_tensor t);                                 /* t * (1/maxNorm) */
+/* Tensor::tSVD (Tensor.cpp:478-633); keep[] (may be NULL, one per input sector) gets kept counts */
+int xgb_tensor_tsvd(xgb_tensor t, int64_t max_keep, double eps_svd, int preserve_multiplets, xgb_tensor* U,
+                    xgb_tensor* S, xgb_tensor* Vdag, double* trunc_weight, double* entropy, int32_t* keep);
+int xgb_tensor_tqr(xgb_tensor t, xgb_tensor* Q, xgb_tensor* R);                    /* Tensor::tQR (Tensor.cpp:757-780) */
+/* decompose (src/PEPS/PEPSContractions.cpp:16-43) */
+int xgb_decompose(xgb_tensor t1, xgb_tensor t2, int64_t max_nsv, xgb_tensor* P1, xgb_tensor* P2);
+void xgb_tensor_release(xgb_tensor t);
+
+/* -------------------------------------------------------------------- CTM */
+/* CTM<double, Sym, 2, false> on a 1x1 unit cell with site tensor A: Tensor<2,3>
+   (src/PEPS/CTM.cpp). which: 0..3 = C1..C4, 4..7 = T1..T4, 8 = A, 9 = Adag. */
+xgb_ctm xgb_ctm_create(xgb_tensor A, int64_t chi);
+int xgb_ctm_init(xgb_ctm c);                                /* CTM::init, FROM_A (CTM.cpp:161-212) */
+int xgb_ctm_grow_all(xgb_ctm c);                            /* CTM::grow_all (CTM.cpp:385-398) */
+int xgb_ctm_move(xgb_ctm c, char dir);                      /* 'L','R','T','B' moves (CTM.cpp:924-1183) */
+xgb_tensor xgb_ctm_get(xgb_ctm c, int which);
+int xgb_ctm_set(xgb_ctm c, int which, xgb_tensor t);
+void xgb_ctm_release(xgb_ctm c);
+
+/* ------------------------------------------------- host-only planning */
+/* Metadata-only tensor (no device memory): sectors, blocks and the plans below
+   can be inspected without a GPU. */
+xgb_tensor xgb_tensor_meta(int rank, const xgb_basis* dom, int corank, const xgb_basis* cod);
+/* The permute plan the device kernel would run for permute<shift>(p) with
+   pending twists `twist_mask`; counts always written, arrays when non-NULL. */
+int xgb_permute_plan_host(xgb_tensor t, int shift, const int32_t* p, int n, uint32_t twist_mask, int* n_tasks,
+                          int* n_contrib, xgb_perm_task* tasks, int task_cap, xgb_perm_contrib* contribs,
+                          int contrib_cap, xgb_tensor* out_meta);
+/* The grouped-GEMM descriptors of operator*(a, b) (with adjoint operands). */
+int xgb_gemm_plan_host(xgb_tensor a, int adj_a, xgb_tensor b, int adj_b, int* n, xgb_gemm_desc* descs, int cap,
+                       xgb_tensor* out_meta);
+/* get_permutations (include/Xped/Util/Constfct.hpp:55-109): writes
+   p1[n1], shift1, p2[n2], shift2, pres[nres], shiftres into out; returns nres. */
+int xgb_contract_perms(const int32_t* a1, int n1, int rank1, const int32_t* a2, int n2, int rank2, int rankres,
+                       int32_t* out);
+
+/* plan-cache counters: perm hits, perm misses, gemm hits, gemm misses */
+int xgb_plan_cache_stats(int64_t* out4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XGB_TENSOR_H_ */

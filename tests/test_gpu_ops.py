@@ -1,0 +1,163 @@
+"""GPU parity of the tensor operations against the CPU oracle, through the C-ABI.
+
+Tolerances: permute/twist/adjoint are pure data movement with coefficients
++-1 (abelian) -> bit-exact; SU(2) coefficients are computed independently on
+both sides -> 1e-13.  FP64 GEMM: 1e-12 relative to the block scale.  SVD:
+gauge-normalised singular vectors and values to 1e-10 relative.
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle.tensor import decompose as o_decompose
+from helpers import assert_same, pair_basis, random_pairs, to_native
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair_tensors(symname, pairsB, pairsC, seed=0):
+    rng = np.random.default_rng(seed)
+    s, oB, nB = pair_basis(symname, pairsB)
+    _, oC, nC = pair_basis(symname, pairsC)
+    ot = oracle.Tensor(s, [oB, oC], [oB, oC]).set_random(rng)
+    nt = to_native(ot, [nB, nC], [nB, nC])
+    return s, (oB, oC), (nB, nC), ot, nt
+
+
+CASES = [
+    ("u1", [(2, 2), (0, 1), (-1, 1), (-3, 1)], [(-2, 2), (1, 3)]),
+    ("u1", [(-2, 2), (-1, 4), (0, 6), (1, 4), (2, 2)], [(-2, 2), (-1, 4), (0, 6), (1, 4), (2, 2)]),
+    ("fu1", [(-1, 2), (0, 1), (1, 2), (2, 1)], [(0, 2), (1, 1), (-1, 1)]),
+    ("fz2", [(0, 2), (1, 3)], [(1, 2), (0, 1)]),
+    ("su2", [(1, 2), (2, 1), (3, 1)], [(1, 1), (2, 2)]),
+]
+
+
+@pytest.mark.parametrize("symname,pB,pC", CASES)
+def test_permute_all(symname, pB, pC):
+    s, ob, nb, ot, nt = _pair_tensors(symname, pB, pC)
+    tol = 1e-13 if symname == "su2" else 0.0
+    for p in itertools.permutations(range(4)):
+        for shift in range(-2, 3):
+            ref = ot.permute(shift, list(p))
+            got = nt.permute(shift, list(p))
+            assert_same(got, ref, rtol=tol, atol=tol)
+
+
+def test_twist_then_permute():
+    s, ob, nb, ot, nt = _pair_tensors("fu1", *CASES[2][1:])
+    for mask in range(16):
+        o2, n2 = ot, nt
+        for l in range(4):
+            if mask >> l & 1:
+                o2, n2 = o2.twist(l), n2.twist(l)
+        assert_same(n2.permute(1, [0, 2, 3, 1]), o2.permute(1, [0, 2, 3, 1]), 0, 0)
+        assert_same(n2, o2, 0, 0)  # download materialises pending twists
+
+
+def test_adjoint():
+    for symname, pB, pC in CASES:
+        s, ob, nb, ot, nt = _pair_tensors(symname, pB, pC)
+        assert_same(nt.adjoint(), ot.adjoint(), 0, 0)
+
+
+def test_matmul_and_adjoint_operands():
+    rng = np.random.default_rng(3)
+    s, oB, nB = pair_basis("u1", [(-2, 2), (-1, 4), (0, 6), (1, 4), (2, 2)])
+    _, oC, nC = pair_basis("u1", [(-1, 3), (0, 5), (1, 2), (3, 1)])
+    oT1 = oracle.Tensor(s, [oB, oB], [oC, oB]).set_random(rng)
+    oT2 = oracle.Tensor(s, [oC, oB], [oB, oC]).set_random(rng)
+    nT1 = to_native(oT1, [nB, nB], [nC, nB])
+    nT2 = to_native(oT2, [nC, nB], [nB, nC])
+    assert_same(nT1 * nT2, oT1 * oT2, 1e-12, 1e-12)
+    # adjoint operands without materialising the transpose
+    assert_same(nT1.matmul(nT1, adj_b=True), oT1 * oT1.adjoint(), 1e-12, 1e-12)
+    assert_same(nT2.matmul(nT2, adj_a=True), oT2.adjoint() * oT2, 1e-12, 1e-12)
+
+
+def test_config1_contract_permute_tsvd():
+    """BASELINE config 1: U(1) Tensor<2,2>, legs q=-2..2 deg [2,4,6,4,2];
+    T1*T2 -> permute<0>(0,2,1,3) -> tSVD(chi=16, eps=1e-10)."""
+    pairs = [(-2, 2), (-1, 4), (0, 6), (1, 4), (2, 2)]
+    for seed in range(3):
+        rng = np.random.default_rng(seed)
+        s, oB, nB = pair_basis("u1", pairs, sort=True)
+        o1 = oracle.Tensor(s, [oB, oB], [oB, oB]).set_random(rng)
+        o2 = oracle.Tensor(s, [oB, oB], [oB, oB]).set_random(rng)
+        n1 = to_native(o1, [nB, nB], [nB, nB])
+        n2 = to_native(o2, [nB, nB], [nB, nB])
+        oprod = o1 * o2
+        nprod = n1 * n2
+        assert_same(nprod, oprod, 1e-12, 1e-12)
+        operm = oprod.permute(0, [0, 2, 1, 3])
+        nperm = nprod.permute(0, [0, 2, 1, 3])
+        assert_same(nperm, operm, 1e-12, 1e-12)
+        oU, oS, oV, otw, oent = operm.tsvd(16, 1e-10)
+        nU, nS, nV, ntw, nent, keep = nperm.tSVD(16, 1e-10)
+        assert_same(nS, oS, 1e-10, 1e-12)
+        assert_same(nU, oU, 1e-9, 1e-9)
+        assert_same(nV, oV, 1e-9, 1e-9)
+        assert abs(ntw - otw) <= 1e-10 * max(1.0, otw)
+        assert abs(nent - oent) <= 1e-10 * max(1.0, abs(oent))
+
+
+def test_contract_labels():
+    rng = np.random.default_rng(5)
+    s, oB, nB = pair_basis("u1", [(-1, 1), (0, 2), (1, 1)], sort=True)
+    _, oP, nP = pair_basis("u1", [(-1, 1), (1, 1)], sort=True)
+    oA = oracle.Tensor(s, [oB, oB], [oB, oB, oP]).set_random(rng)
+    nA = to_native(oA, [nB, nB], [nB, nB, nP])
+    oAd = oA.adjoint().permute(0, [3, 4, 2, 0, 1])
+    nAd = nA.adjoint().permute(0, [3, 4, 2, 0, 1])
+    assert_same(nAd, oAd, 0, 0)
+    for a1, a2, r in [([1, 2, -1, -2, 3], [1, 2, 3, -3, -4], 2), ([-1, 1, -2, -3, 2], [-4, 1, 2, -5, -6], 3),
+                      ([-1, -2, 1, 2, 3], [-3, -4, 3, 1, 2], 2)]:
+        assert_same(nA.contract(nAd, a1, a2, r), oA.contract(oAd, a1, a2, r), 1e-12, 1e-12)
+
+
+def test_maxnorm_normalize():
+    s, ob, nb, ot, nt = _pair_tensors(*CASES[1])
+    assert nt.maxNorm() == ot.max_norm()
+    assert_same(nt.normalize_max(), ot.normalize_max(), 0, 0)
+
+
+def test_tsvd_truncation_edge_cases():
+    rng = np.random.default_rng(11)
+    s, oB, nB = pair_basis("u1", [(-1, 3), (0, 5), (1, 2)], sort=True)
+    ot = oracle.Tensor(s, [oB, oB], [oB, oB]).set_random(rng)
+    nt = to_native(ot, [nB, nB], [nB, nB])
+    for keep, eps in [(1, 0.0), (7, 1e-10), (1000, 0.0), (1000, 1e-10), (40, 5.0), (3, 1e9)]:
+        oU, oS, oV, otw, oent = ot.tsvd(keep, eps)
+        nU, nS, nV, ntw, nent, _ = nt.tSVD(keep, eps)
+        assert nS.sectors() == (oS.sectors, [b.shape[0] for b in oS.blocks], [b.shape[1] for b in oS.blocks])
+        assert_same(nS, oS, 1e-10, 1e-12)
+        assert_same(nU, oU, 1e-9, 1e-9)
+        assert_same(nV, oV, 1e-9, 1e-9)
+
+
+def test_tqr():
+    rng = np.random.default_rng(2)
+    s, oB, nB = pair_basis("u1", [(-1, 3), (0, 5), (1, 2)], sort=True)
+    _, oC, nC = pair_basis("u1", [(-1, 1), (0, 2), (1, 1)], sort=True)
+    ot = oracle.Tensor(s, [oB, oB], [oC]).set_random(rng)  # tall blocks: middle = codomain
+    nt = to_native(ot, [nB, nB], [nC])
+    oQ, oR = ot.tqr()
+    nQ, nR = nt.tQR()
+    assert_same(nQ, oQ, 1e-11, 1e-11)
+    assert_same(nR, oR, 1e-11, 1e-11)
+
+
+def test_decompose_projectors():
+    rng = np.random.default_rng(4)
+    s, oB, nB = pair_basis("u1", [(-1, 2), (0, 3), (1, 2)], sort=True)
+    o1 = oracle.Tensor(s, [oB, oB], [oB, oB]).set_random(rng)
+    o2 = oracle.Tensor(s, [oB, oB], [oB, oB]).set_random(rng)
+    n1 = to_native(o1, [nB, nB], [nB, nB])
+    n2 = to_native(o2, [nB, nB], [nB, nB])
+    oP1, oP2 = o_decompose(o1, o2, 12)
+    from xped_gb300 import decompose
+    nP1, nP2 = decompose(n1, n2, 12)
+    assert_same(nP1, oP1, 1e-9, 1e-9)
+    assert_same(nP2, oP2, 1e-9, 1e-9)

@@ -1,0 +1,186 @@
+"""Pins the CPU oracle to the reference's own test properties (no golden
+vectors exist upstream; tests/tensor_tests.hpp, tests/tree_tests.hpp and
+tests/ad.cpp assert identities, restated here) plus exact SU(2) 6j values."""
+import itertools
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle.basis import Qbasis, decompose_permutation, inverse_permutation, treepair_permute
+from oracle.sym import wigner6j_twice
+from oracle.tensor import get_permutations, decompose
+
+
+def _rand_basis(rng, sym, n, qrange):
+    b = Qbasis(sym, 1)
+    while b.fullDim() < n:
+        q = int(rng.integers(*qrange))
+        d = int(rng.integers(1, 3))
+        if b.fullDim() + sym.degeneracy(q) * d <= n:
+            b.push_back(q, d)
+    return b
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_permute_equals_dense_shuffle_u1(seed):
+    """tests/tensor_tests.hpp:1-48 over all 24 permutations and shifts -2..2
+    (tests/tensor.cpp:188-227), U(1), unsorted random bases of size 5."""
+    rng = np.random.default_rng(seed)
+    s = oracle.U1()
+    B, C = _rand_basis(rng, s, 5, (-3, 4)), _rand_basis(rng, s, 5, (-3, 4))
+    t = oracle.Tensor(s, [B, C], [B, C]).set_random(rng)
+    P = t.plain_tensor()
+    for p in itertools.permutations(range(4)):
+        for shift in range(-2, 3):
+            tp = t.permute(shift, list(p))
+            assert np.array_equal(tp.plain_tensor(), np.transpose(P, p))
+
+
+def test_permute_within_domain_codomain_rank4():
+    """Within-domain permutations of Tensor<4,0> / <0,4> (tensor_tests.hpp:111-303)."""
+    rng = np.random.default_rng(9)
+    s = oracle.U1()
+    Bs = [_rand_basis(rng, s, 4, (-2, 3)) for _ in range(4)]
+    t = oracle.Tensor(s, Bs, []).set_random(rng)
+    P = t.plain_tensor()
+    for p in itertools.permutations(range(4)):
+        assert np.array_equal(t.permute(0, list(p)).plain_tensor(), np.transpose(P, p))
+    t2 = oracle.Tensor(s, [], Bs).set_random(rng)
+    P2 = t2.plain_tensor()
+    for p in itertools.permutations(range(4)):
+        assert np.array_equal(t2.permute(0, list(p)).plain_tensor(), np.transpose(P2, p))
+
+
+@pytest.mark.parametrize("symname,pairs", [("fu1", [(-1, 2), (0, 1), (1, 2), (2, 1)]), ("fz2", [(0, 2), (1, 3)]),
+                                           ("su2", [(1, 2), (2, 1), (3, 1)])])
+def test_permute_round_trip_and_norm(symname, pairs):
+    rng = np.random.default_rng(4)
+    s = oracle.make_symmetry(symname)
+    B = Qbasis.from_pairs(s, pairs, sort=False)
+    C = Qbasis.from_pairs(s, pairs[::-1], sort=False)
+    t = oracle.Tensor(s, [B, C], [B, C]).set_random(rng)
+    for p in itertools.permutations(range(4)):
+        for shift in range(-2, 3):
+            tp = t.permute(shift, list(p))
+            back = tp.permute(-shift, inverse_permutation(p))
+            for q in t.sectors:
+                assert np.allclose(back.block(q), t.block(q), atol=1e-13)
+            assert abs(tp.squared_norm() - t.squared_norm()) < 1e-11 * t.squared_norm()
+
+
+@pytest.mark.parametrize("symname", ["u1", "fu1", "su2"])
+def test_tree_swap_and_permute_round_trips(symname):
+    """tests/tree_tests.hpp:1-167: swap(pos) twice and permute(p) then p^-1
+    give coefficient 1 on the original tree and 0 elsewhere."""
+    s = oracle.make_symmetry(symname)
+    if symname == "su2":
+        B = Qbasis.from_pairs(s, [(1, 1), (2, 1), (3, 1)])
+    else:
+        B = Qbasis.from_pairs(s, [(-1, 1), (0, 1), (1, 1)])
+    BCDE = B.combine(B).combine(B).combine(B)
+    for q in BCDE.qs:
+        for tree in BCDE.trees[q]:
+            for pos in range(3):
+                acc = {}
+                for t2, c in tree.swap(s, pos).items():
+                    for t3, c2 in t2.swap(s, pos).items():
+                        acc[t3] = acc.get(t3, 0.0) + c * c2
+                for t3, c in acc.items():
+                    assert abs(c - (1.0 if t3 == tree else 0.0)) < 1e-12
+            for p in itertools.permutations(range(4)):
+                acc = {}
+                for t2, c in tree.permute(s, list(p)).items():
+                    for t3, c2 in t2.permute(s, inverse_permutation(p)).items():
+                        acc[t3] = acc.get(t3, 0.0) + c * c2
+                for t3, c in acc.items():
+                    assert abs(c - (1.0 if t3 == tree else 0.0)) < 1e-12
+
+
+def test_treepair_permute_round_trip_su2():
+    """treepair::permute<shift> round trip (tests/tree.cpp:48-215)."""
+    s = oracle.SU2()
+    B = Qbasis.from_pairs(s, [(1, 1), (2, 1), (3, 1)])
+    dom = B.combine(B)
+    cod = B.combine(B)
+    for q in dom.qs:
+        if not cod.IS_PRESENT(q):
+            continue
+        for f1 in dom.trees[q]:
+            for f2 in cod.trees[q]:
+                for p in itertools.permutations(range(4)):
+                    for shift in (-1, 0, 1):
+                        acc = {}
+                        for (g1, g2), c in treepair_permute(s, shift, f1, f2, list(p)).items():
+                            for (h1, h2), c2 in treepair_permute(s, -shift, g1, g2, inverse_permutation(p)).items():
+                                acc[(h1, h2)] = acc.get((h1, h2), 0.0) + c * c2
+                        for k, c in acc.items():
+                            assert abs(c - (1.0 if k == (f1, f2) else 0.0)) < 1e-12
+
+
+def test_su2_6j_against_sympy():
+    sympy = pytest.importorskip("sympy")
+    from sympy.physics.wigner import wigner_6j
+    rng = np.random.default_rng(0)
+    n = 0
+    tri = lambda x, y, z: (x + y + z) % 2 == 0 and abs(x - y) <= z <= x + y
+    valid = [t for t in itertools.product(range(6), repeat=6)
+             if tri(t[0], t[1], t[2]) and tri(t[0], t[4], t[5]) and tri(t[3], t[1], t[5]) and tri(t[3], t[4], t[2])]
+    picks = [valid[i] for i in rng.choice(len(valid), size=250, replace=False)]
+    picks += [tuple(int(x) for x in rng.integers(0, 7, size=6)) for _ in range(100)]
+    for two in picks:
+        try:
+            ref = float(wigner_6j(*[sympy.Rational(t, 2) for t in two]))
+        except ValueError:  # sympy rejects non-triangular arguments; the value is 0
+            ref = 0.0
+        assert abs(wigner6j_twice(*two) - ref) < 1e-14
+        n += ref != 0.0
+    assert n > 20
+
+
+def test_permutation_decompose():
+    for p in itertools.permutations(range(5)):
+        a = list(range(5))
+        for j in decompose_permutation(list(p)):
+            a[j], a[j + 1] = a[j + 1], a[j]
+        assert a == list(p)
+
+
+def test_get_permutations_known_answers():
+    # corner contraction C1T1 = C1.contract<{-1,1},{1,-2,-3,-4},1>(T1)  (CTM.cpp:1668)
+    assert get_permutations([-1, 1], 0, [1, -2, -3, -4], 1, 1) == ([0, 1], -1, [0, 1, 2, 3], 0, [0, 1, 2, 3], 0)
+    p1, s1, p2, s2, pres, sres = get_permutations([1, 2, -1, -2, 3], 2, [1, 2, 3, -3, -4], 3, 2)
+    # A: Tensor<2,3> -> domain = open legs (2,3), codomain = contracted legs (0,1,4); shift 2-5+3 = 0
+    assert (p1, s1, p2, s2, pres, sres) == ([2, 3, 0, 1, 4], 0, [0, 1, 2, 3, 4], 0, [0, 1, 2, 3], 0)
+
+
+def test_tsvd_reconstruction_and_cutoff():
+    rng = np.random.default_rng(1)
+    s = oracle.U1()
+    B = Qbasis.from_pairs(s, [(-2, 2), (-1, 4), (0, 6), (1, 4), (2, 2)])
+    t = oracle.Tensor(s, [B, B], [B, B]).set_random(rng)
+    U, S, V, tw, ent = t.tsvd(10000, 0.0)
+    rec = (U * S) * V
+    for q in t.sectors:
+        assert np.allclose(rec.block(q), t.block(q), atol=1e-12)
+    U, S, V, tw, ent = t.tsvd(16, 1e-10)
+    assert sum(b.shape[0] for b in S.blocks) == 16
+    allsv = sorted(np.concatenate([np.linalg.svd(b, compute_uv=False) for b in t.blocks]), reverse=True)
+    assert abs(tw - sum(x * x for x in allsv[16:])) < 1e-10 * tw
+    kept = allsv[:16]
+    assert abs(ent - sum(-x * x * np.log(x * x) for x in kept)) < 1e-10 * abs(ent)
+
+
+def test_decompose_projector_identity():
+    """P1 P2 is the identity on the kept space when nothing is truncated
+    (decompose, PEPSContractions.cpp:16-43)."""
+    rng = np.random.default_rng(2)
+    s = oracle.U1()
+    B = Qbasis.from_pairs(s, [(-1, 2), (0, 3), (1, 2)])
+    t1 = oracle.Tensor(s, [B, B], [B, B]).set_random(rng)
+    t2 = oracle.Tensor(s, [B, B], [B, B]).set_random(rng)
+    P1, P2 = decompose(t1, t2, 10000)
+    I = P1 * P2
+    for q, b in zip(I.sectors, I.blocks):
+        assert np.allclose(b, np.eye(b.shape[0]), atol=1e-9)

@@ -1,0 +1,322 @@
+// Tensor-level C-ABI (include/xgb_tensor.h) over the C++ host layer.
+// No exception crosses the boundary: failures map to XGB_E_* / NULL.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <new>
+#include <stdexcept>
+
+#include "../../include/xgb_tensor.h"
+#include "tensor.hpp"
+
+struct xgb_basis_s { xgb::BasisPtr b; };
+struct xgb_tensor_s { xgb::Tensor t; };
+struct xgb_ctm_s { std::unique_ptr<xgb::CTM> c; };
+
+using namespace xgb;
+
+namespace {
+Sym sym_of(int kind) {
+  Sym s;
+  s.kind = kind;
+  s.N = 2;
+  return s;
+}
+xgb_tensor wrap(Tensor t) { return new xgb_tensor_s{std::move(t)}; }
+xgb_basis wrapb(BasisPtr b) { return new xgb_basis_s{std::move(b)}; }
+}  // namespace
+
+#define GUARD(fail, ...)                               \
+  try {                                                \
+    __VA_ARGS__                                        \
+  } catch (const std::bad_alloc&) {                    \
+    set_error(XGB_E_OOM, "device allocation failed");  \
+    return fail;                                       \
+  } catch (const std::exception& e) {                  \
+    set_error(XGB_E_BADPLAN, e.what());                \
+    return fail;                                       \
+  }
+
+extern "C" {
+
+xgb_basis xgb_basis_create(int sym, int n, const int32_t* qs, const int64_t* dims, int sort) {
+  GUARD(nullptr, {
+    if (sym < 0 || sym > XGB_SYM_SU2) throw std::runtime_error("unknown symmetry kind");
+    std::vector<std::pair<int, int64_t>> pairs;
+    for (int i = 0; i < n; ++i) pairs.push_back({qs[i], dims[i]});
+    return wrapb(basis_from_pairs(sym_of(sym), pairs, sort != 0));
+  })
+}
+xgb_basis xgb_basis_conj(xgb_basis b) { GUARD(nullptr, { return wrapb(basis_conj(b->b)); }) }
+xgb_basis xgb_basis_combine(xgb_basis a, xgb_basis b) { GUARD(nullptr, { return wrapb(basis_combine(a->b, b->b)); }) }
+xgb_basis xgb_basis_forget_history(xgb_basis b) { GUARD(nullptr, { return wrapb(basis_forget_history(b->b)); }) }
+
+int xgb_basis_info(xgb_basis b, int32_t* qs, int64_t* dims, int* conj_flag, int* depth) {
+  const Qbasis& B = *b->b;
+  for (size_t i = 0; i < B.qs.size(); ++i) {
+    if (qs) qs[i] = B.qs[i];
+    if (dims) dims[i] = B.dims[i];
+  }
+  if (conj_flag) *conj_flag = B.conj_flag;
+  if (depth) *depth = B.depth;
+  return int(B.qs.size());
+}
+
+int xgb_basis_trees(xgb_basis b, int i, int64_t* out, int cap) {
+  const Qbasis& B = *b->b;
+  if (i < 0 || i >= int(B.qs.size())) return set_error(XGB_E_BADPLAN, "irrep index out of range");
+  int need = 0;
+  for (const auto& t : B.trees[i]) need += 3 + 2 * t.rank + t.nqi();
+  if (!out) return need;
+  if (cap < need) return set_error(XGB_E_BADPLAN, "buffer too small");
+  int64_t* o = out;
+  for (const auto& t : B.trees[i]) {
+    *o++ = t.rank;
+    *o++ = t.qc;
+    *o++ = t.dual;
+    for (int k = 0; k < t.rank; ++k) *o++ = t.qu[k];
+    for (int k = 0; k < t.rank; ++k) *o++ = t.dims[k];
+    for (int k = 0; k < t.nqi(); ++k) *o++ = t.qi[k];
+  }
+  return int(B.trees[i].size());
+}
+
+void xgb_basis_release(xgb_basis b) { delete b; }
+
+static std::vector<BasisPtr> legs(int n, const xgb_basis* b) {
+  std::vector<BasisPtr> v;
+  for (int i = 0; i < n; ++i) v.push_back(b[i]->b);
+  return v;
+}
+
+static Sym sym_from_legs(int rank, const xgb_basis* dom, int corank, const xgb_basis* cod) {
+  if (rank > 0) return dom[0]->b->sym;
+  if (corank > 0) return cod[0]->b->sym;
+  throw std::runtime_error("tensor needs at least one leg");
+}
+
+xgb_tensor xgb_tensor_zeros(int rank, const xgb_basis* dom, int corank, const xgb_basis* cod) {
+  GUARD(nullptr, {
+    Sym s = sym_from_legs(rank, dom, corank, cod);
+    return wrap(zeros(make_meta(s, legs(rank, dom), legs(corank, cod))));
+  })
+}
+
+xgb_tensor xgb_tensor_identity(int rank, const xgb_basis* dom, int corank, const xgb_basis* cod) {
+  GUARD(nullptr, {
+    Sym s = sym_from_legs(rank, dom, corank, cod);
+    return wrap(identity(s, legs(rank, dom), legs(corank, cod)));
+  })
+}
+
+int xgb_tensor_sectors(xgb_tensor t, int32_t* qs, int64_t* rows, int64_t* cols) {
+  const TensorMeta& m = *t->t.meta;
+  for (size_t i = 0; i < m.sectors.size(); ++i) {
+    if (qs) qs[i] = m.sectors[i];
+    if (rows) rows[i] = m.rows[i];
+    if (cols) cols[i] = m.cols[i];
+  }
+  return int(m.sectors.size());
+}
+
+int64_t xgb_tensor_size(xgb_tensor t) { return t->t.size(); }
+
+int xgb_tensor_rank(xgb_tensor t, int* rank, int* corank) {
+  *rank = t->t.meta->rank();
+  *corank = t->t.meta->corank();
+  return XGB_OK;
+}
+
+xgb_basis xgb_tensor_leg(xgb_tensor t, int leg) {
+  const TensorMeta& m = *t->t.meta;
+  if (leg < 0 || leg >= m.rank() + m.corank()) { set_error(XGB_E_BADPLAN, "leg out of range"); return nullptr; }
+  return wrapb(leg < m.rank() ? m.dom[leg] : m.cod[leg - m.rank()]);
+}
+
+xgb_basis xgb_tensor_coupled(xgb_tensor t, int codomain) { return wrapb(codomain ? t->t.meta->ccod : t->t.meta->cdom); }
+
+int xgb_tensor_upload(xgb_tensor t, const double* host, int64_t n) {
+  if (n != t->t.size()) return set_error(XGB_E_BADPLAN, "upload: size mismatch");
+  GUARD(XGB_E_CUDA, {
+    t->t.twist_mask = 0;
+    if (t->t.buf.use_count() > 1) t->t.buf = std::make_shared<DevBuf>(n);
+    if (n) {
+      cudaError_t e = cudaMemcpyAsync(t->t.data(), host, sizeof(double) * n, cudaMemcpyHostToDevice, stream());
+      if (e == cudaSuccess) e = cudaStreamSynchronize(stream());
+      if (e != cudaSuccess) return set_error(XGB_E_CUDA, cudaGetErrorString(e));
+    }
+    return XGB_OK;
+  })
+}
+
+int xgb_tensor_download(xgb_tensor t, double* host, int64_t n) {
+  if (n != t->t.size()) return set_error(XGB_E_BADPLAN, "download: size mismatch");
+  GUARD(XGB_E_CUDA, {
+    Tensor m = materialize(t->t);
+    if (n) {
+      cudaError_t e = cudaMemcpyAsync(host, m.data(), sizeof(double) * n, cudaMemcpyDeviceToHost, stream());
+      if (e == cudaSuccess) e = cudaStreamSynchronize(stream());
+      if (e != cudaSuccess) return set_error(XGB_E_CUDA, cudaGetErrorString(e));
+    }
+    return XGB_OK;
+  })
+}
+
+double* xgb_tensor_device_data(xgb_tensor t) {
+  GUARD(nullptr, {
+    t->t = materialize(t->t);
+    return t->t.data();
+  })
+}
+
+xgb_tensor xgb_tensor_permute(xgb_tensor t, int shift, const int32_t* p, int n) {
+  GUARD(nullptr, { return wrap(permute(t->t, shift, std::vector<int>(p, p + n))); })
+}
+xgb_tensor xgb_tensor_twist(xgb_tensor t, int leg) { GUARD(nullptr, { return wrap(twist(t->t, leg)); }) }
+xgb_tensor xgb_tensor_adjoint(xgb_tensor t) { GUARD(nullptr, { return wrap(adjoint(t->t)); }) }
+xgb_tensor xgb_tensor_matmul(xgb_tensor a, xgb_tensor b, int adj_a, int adj_b) {
+  GUARD(nullptr, { return wrap(matmul(a->t, b->t, adj_a != 0, adj_b != 0)); })
+}
+xgb_tensor xgb_tensor_contract(xgb_tensor a, xgb_tensor b, const int32_t* a1, int n1, const int32_t* a2, int n2,
+                               int rankres) {
+  GUARD(nullptr, {
+    return wrap(contract(a->t, b->t, std::vector<int>(a1, a1 + n1), std::vector<int>(a2, a2 + n2), rankres));
+  })
+}
+xgb_tensor xgb_tensor_scale(xgb_tensor t, double s) { GUARD(nullptr, { return wrap(scale(t->t, s)); }) }
+double xgb_tensor_max_norm(xgb_tensor t) { GUARD(-1.0, { return max_norm(t->t); }) }
+xgb_tensor xgb_tensor_normalize_max(xgb_tensor t) { GUARD(nullptr, { return wrap(normalize_max(t->t)); }) }
+
+int xgb_tensor_tsvd(xgb_tensor t, int64_t max_keep, double eps_svd, int preserve_multiplets, xgb_tensor* U,
+                    xgb_tensor* S, xgb_tensor* Vdag, double* trunc_weight, double* entropy, int32_t* keep) {
+  GUARD(XGB_E_BADPLAN, {
+    SVDResult r = tsvd(t->t, max_keep, eps_svd, preserve_multiplets != 0);
+    if (U) *U = wrap(r.U);
+    if (S) *S = wrap(r.S);
+    if (Vdag) *Vdag = wrap(r.Vdag);
+    if (trunc_weight) *trunc_weight = r.trunc_weight;
+    if (entropy) *entropy = r.entropy;
+    if (keep) for (size_t i = 0; i < r.keep.size(); ++i) keep[i] = r.keep[i];
+    return XGB_OK;
+  })
+}
+
+int xgb_tensor_tqr(xgb_tensor t, xgb_tensor* Q, xgb_tensor* R) {
+  GUARD(XGB_E_BADPLAN, {
+    auto [q, r] = tqr(t->t);
+    *Q = wrap(q);
+    *R = wrap(r);
+    return XGB_OK;
+  })
+}
+
+int xgb_decompose(xgb_tensor t1, xgb_tensor t2, int64_t max_nsv, xgb_tensor* P1, xgb_tensor* P2) {
+  GUARD(XGB_E_BADPLAN, {
+    auto [a, b] = decompose(t1->t, t2->t, max_nsv);
+    *P1 = wrap(a);
+    *P2 = wrap(b);
+    return XGB_OK;
+  })
+}
+
+void xgb_tensor_release(xgb_tensor t) { delete t; }
+
+xgb_ctm xgb_ctm_create(xgb_tensor A, int64_t chi) {
+  GUARD(nullptr, { return new xgb_ctm_s{std::make_unique<CTM>(A->t, chi)}; })
+}
+int xgb_ctm_init(xgb_ctm c) { GUARD(XGB_E_BADPLAN, { c->c->init(); return XGB_OK; }) }
+int xgb_ctm_grow_all(xgb_ctm c) { GUARD(XGB_E_BADPLAN, { c->c->grow_all(); return XGB_OK; }) }
+int xgb_ctm_move(xgb_ctm c, char dir) { GUARD(XGB_E_BADPLAN, { c->c->move(dir); return XGB_OK; }) }
+xgb_tensor xgb_ctm_get(xgb_ctm c, int which) {
+  GUARD(nullptr, {
+    if (which < 0 || which > 9) throw std::runtime_error("ctm slot out of range");
+    Tensor& t = c->c->slot(which);
+    if (!t.valid()) throw std::runtime_error("ctm slot is empty (call xgb_ctm_init)");
+    return wrap(t);
+  })
+}
+int xgb_ctm_set(xgb_ctm c, int which, xgb_tensor t) {
+  GUARD(XGB_E_BADPLAN, {
+    if (which < 0 || which > 7) throw std::runtime_error("ctm slot out of range");
+    c->c->slot(which) = t->t;
+    return XGB_OK;
+  })
+}
+void xgb_ctm_release(xgb_ctm c) { delete c; }
+
+xgb_tensor xgb_tensor_meta(int rank, const xgb_basis* dom, int corank, const xgb_basis* cod) {
+  GUARD(nullptr, {
+    Sym s = sym_from_legs(rank, dom, corank, cod);
+    Tensor t;
+    t.meta = make_meta(s, legs(rank, dom), legs(corank, cod));
+    return wrap(t);
+  })
+}
+
+static xgb_tensor meta_handle(const MetaPtr& m) {
+  Tensor t;
+  t.meta = m;
+  return wrap(t);
+}
+
+int xgb_permute_plan_host(xgb_tensor t, int shift, const int32_t* p, int n, uint32_t twist_mask, int* n_tasks,
+                          int* n_contrib, xgb_perm_task* tasks, int task_cap, xgb_perm_contrib* contribs,
+                          int contrib_cap, xgb_tensor* out_meta) {
+  GUARD(XGB_E_BADPLAN, {
+    const TensorMeta& m = *t->t.meta;
+    if (n != m.rank() + m.corank()) throw std::runtime_error("permutation length mismatch");
+    PermTables pt = build_perm_tables(m, twist_mask, shift, std::vector<int>(p, p + n));
+    *n_tasks = int(pt.tasks.size());
+    *n_contrib = int(pt.contribs.size());
+    if (tasks) {
+      if (task_cap < *n_tasks) throw std::runtime_error("task buffer too small");
+      std::memcpy(tasks, pt.tasks.data(), sizeof(xgb_perm_task) * pt.tasks.size());
+    }
+    if (contribs) {
+      if (contrib_cap < *n_contrib) throw std::runtime_error("contribution buffer too small");
+      std::memcpy(contribs, pt.contribs.data(), sizeof(xgb_perm_contrib) * pt.contribs.size());
+    }
+    if (out_meta) *out_meta = meta_handle(pt.out);
+    return XGB_OK;
+  })
+}
+
+int xgb_gemm_plan_host(xgb_tensor a, int adj_a, xgb_tensor b, int adj_b, int* n, xgb_gemm_desc* descs, int cap,
+                       xgb_tensor* out_meta) {
+  GUARD(XGB_E_BADPLAN, {
+    GemmTables gt = build_gemm_tables(*a->t.meta, adj_a != 0, *b->t.meta, adj_b != 0);
+    *n = int(gt.descs.size());
+    if (descs) {
+      if (cap < *n) throw std::runtime_error("descriptor buffer too small");
+      std::memcpy(descs, gt.descs.data(), sizeof(xgb_gemm_desc) * gt.descs.size());
+    }
+    if (out_meta) *out_meta = meta_handle(gt.out);
+    return XGB_OK;
+  })
+}
+
+int xgb_contract_perms(const int32_t* a1, int n1, int rank1, const int32_t* a2, int n2, int rank2, int rankres,
+                       int32_t* out) {
+  GUARD(XGB_E_BADPLAN, {
+    ContractPerms cp = get_permutations(std::vector<int>(a1, a1 + n1), rank1, std::vector<int>(a2, a2 + n2), rank2, rankres);
+    int k = 0;
+    for (int x : cp.p1) out[k++] = x;
+    out[k++] = cp.shift1;
+    for (int x : cp.p2) out[k++] = x;
+    out[k++] = cp.shift2;
+    for (int x : cp.pres) out[k++] = x;
+    out[k++] = cp.shiftres;
+    return int(cp.pres.size());
+  })
+}
+
+int xgb_plan_cache_stats(int64_t* out4) {
+  CacheStats s = cache_stats();
+  out4[0] = s.perm_hits;
+  out4[1] = s.perm_misses;
+  out4[2] = s.gemm_hits;
+  out4[3] = s.gemm_misses;
+  return XGB_OK;
+}
+
+}  // extern "C"

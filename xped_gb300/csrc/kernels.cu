@@ -1,0 +1,1047 @@
+// CUDA kernels of the GB300 block-sparse tensor backend (sm_103a) and the
+// kernel-level C-ABI declared in include/xgb.h.
+//
+// Data layout: one flat column-major FP64 buffer per tensor, one block per
+// coupled sector at a known element offset (the reference's contiguous
+// storage, include/Xped/Core/storage/StorageType_contiguous.hpp:79-122).
+// Every kernel processes all sectors of one tensor operation in a single
+// launch driven by a descriptor table.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kernels.hpp"
+
+namespace xgb {
+
+// ======================================================================= runtime
+namespace {
+struct Runtime {
+  bool ready = false;
+  int device = 0;
+  int sms = 152;
+  cudaStream_t stream = nullptr;
+  double* scratch = nullptr;  // 64 doubles of device scratch
+};
+Runtime g_rt;
+std::atomic<int64_t> g_launches{0};
+thread_local std::string g_err;
+}  // namespace
+
+cudaStream_t stream() { return g_rt.stream; }
+int num_sms() { return g_rt.sms; }
+double* scalar_scratch() { return g_rt.scratch; }
+void count_launch(int n) { g_launches += n; }
+
+int set_error(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int check_cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return XGB_OK;
+  return set_error(e == cudaErrorMemoryAllocation ? XGB_E_OOM : XGB_E_CUDA,
+                   std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void* dev_alloc(size_t bytes) {
+  if (bytes == 0) bytes = 8;
+  void* p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, bytes, g_rt.stream);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    set_error(XGB_E_OOM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+    throw std::bad_alloc();
+  }
+  return p;
+}
+
+void dev_free(void* p) {
+  if (p && g_rt.ready) cudaFreeAsync(p, g_rt.stream);
+}
+
+// ======================================================================= instrumentation
+namespace {
+struct ProfEvent {
+  int kind;
+  cudaEvent_t a, b;
+  double work;
+};
+bool g_prof_on = false;
+std::vector<ProfEvent> g_prof_events;
+std::vector<cudaEvent_t> g_event_pool;
+int64_t g_prof_launches[K_COUNT] = {0};
+double g_prof_work[K_COUNT] = {0};
+double g_prof_ms[K_COUNT] = {0};
+cudaEvent_t g_pending_a[K_COUNT] = {nullptr};
+cudaEvent_t g_user_events[16] = {nullptr};
+
+cudaEvent_t pool_event() {
+  if (!g_event_pool.empty()) {
+    cudaEvent_t e = g_event_pool.back();
+    g_event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void prof_drain() {
+  for (auto& ev : g_prof_events) {
+    float ms = 0.f;
+    cudaEventSynchronize(ev.b);
+    cudaEventElapsedTime(&ms, ev.a, ev.b);
+    g_prof_ms[ev.kind] += ms;
+    g_event_pool.push_back(ev.a);
+    g_event_pool.push_back(ev.b);
+  }
+  g_prof_events.clear();
+}
+}  // namespace
+
+void prof_begin(int kind, cudaStream_t s) {
+  if (!g_prof_on) return;
+  g_pending_a[kind] = pool_event();
+  cudaEventRecord(g_pending_a[kind], s);
+}
+
+void prof_end(int kind, cudaStream_t s, double work) {
+  g_prof_launches[kind] += 1;
+  g_prof_work[kind] += work;
+  if (!g_prof_on || !g_pending_a[kind]) return;
+  cudaEvent_t b = pool_event();
+  cudaEventRecord(b, s);
+  g_prof_events.push_back({kind, g_pending_a[kind], b, work});
+  g_pending_a[kind] = nullptr;
+  if (g_prof_events.size() > 4096) prof_drain();
+}
+
+// ======================================================================= GEMM
+// FP64 grouped GEMM: C_g = alpha*op(A_g)op(B_g) + beta*C_g.  One CTA per
+// TILE x TILE output tile of one group; 256 threads, each owning a
+// (TILE/16)^2 micro-tile.  FP64 on GB300 runs on the narrow DFMA pipe, so the
+// host picks the tile edge that spreads the work over the most SMs.
+template <int TILE>
+__global__ void __launch_bounds__(256) gemm_f64_kernel(const xgb_gemm_desc* __restrict__ descs,
+                                                       const GemmTile* __restrict__ tiles, const double* __restrict__ A,
+                                                       const double* __restrict__ B, double* __restrict__ C, double alpha,
+                                                       double beta) {
+  constexpr int BK = 16;
+  constexpr int R = TILE / 16;
+  __shared__ double As[BK][TILE + 1];
+  __shared__ double Bs[BK][TILE + 1];
+  const GemmTile t = tiles[blockIdx.x];
+  const xgb_gemm_desc d = descs[t.g];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int64_t row0 = int64_t(t.tm) * TILE, col0 = int64_t(t.tn) * TILE;
+  double acc[R][R];
+#pragma unroll
+  for (int i = 0; i < R; ++i)
+#pragma unroll
+    for (int j = 0; j < R; ++j) acc[i][j] = 0.0;
+
+  for (int64_t k0 = 0; k0 < d.k; k0 += BK) {
+    // A tile: TILE rows x BK
+    for (int e = tid; e < TILE * BK; e += 256) {
+      int i, kk;
+      if (d.trans_a) { kk = e % BK; i = e / BK; } else { i = e % TILE; kk = e / TILE; }
+      int64_t gi = row0 + i, gk = k0 + kk;
+      double v = 0.0;
+      if (gi < d.m && gk < d.k) v = d.trans_a ? A[d.a_off + gk + gi * d.lda] : A[d.a_off + gi + gk * d.lda];
+      As[kk][i] = v;
+    }
+    for (int e = tid; e < TILE * BK; e += 256) {
+      int j, kk;
+      if (d.trans_b) { j = e % TILE; kk = e / TILE; } else { kk = e % BK; j = e / BK; }
+      int64_t gj = col0 + j, gk = k0 + kk;
+      double v = 0.0;
+      if (gj < d.n && gk < d.k) v = d.trans_b ? B[d.b_off + gj + gk * d.ldb] : B[d.b_off + gk + gj * d.ldb];
+      Bs[kk][j] = v;
+    }
+    __syncthreads();
+    const int kmax = (d.k - k0) < BK ? int(d.k - k0) : BK;
+    for (int kk = 0; kk < kmax; ++kk) {
+      double a[R], b[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) a[r] = As[kk][tx + 16 * r];
+#pragma unroll
+      for (int c = 0; c < R; ++c) b[c] = Bs[kk][ty + 16 * c];
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int c = 0; c < R; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int c = 0; c < R; ++c) {
+      int64_t i = row0 + tx + 16 * r, j = col0 + ty + 16 * c;
+      if (i < d.m && j < d.n) {
+        double* p = C + d.c_off + i + j * d.ldc;
+        double v = alpha * acc[r][c];
+        if (beta != 0.0) v += beta * (*p);
+        *p = v;
+      }
+    }
+}
+
+void launch_gemm_f64(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
+                     const double* B, double* C, double alpha, double beta, cudaStream_t s) {
+  if (n_tiles <= 0) return;
+  if (tile == 64) gemm_f64_kernel<64><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
+  else if (tile == 32) gemm_f64_kernel<32><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
+  else gemm_f64_kernel<16><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
+  count_launch();
+}
+
+int choose_gemm_tile(const xgb_gemm_desc* descs, int n) {
+  // Largest tile edge that still yields >= 2 CTAs per SM; FP64 throughput is
+  // per SM, so spreading tiles over SMs beats bigger tiles' reuse here.
+  const int target = 2 * (g_rt.sms > 0 ? g_rt.sms : 152);
+  for (int tile : {64, 32}) {
+    int64_t cnt = 0;
+    for (int g = 0; g < n; ++g) cnt += ((descs[g].m + tile - 1) / tile) * ((descs[g].n + tile - 1) / tile);
+    if (cnt >= target) return tile;
+  }
+  return 16;
+}
+
+// ======================================================================= permute
+// Gather-permute with recoupling coefficients.  The flat element space of all
+// output sub-blocks is walked in output memory order (leg 0 fastest), so the
+// stores of a warp are contiguous within a sub-block row; the loads gather
+// through the permuted strides.
+__global__ void __launch_bounds__(256) permute_kernel(const xgb_perm_task* __restrict__ tasks,
+                                                      const int64_t* __restrict__ start, int n_tasks, int64_t total,
+                                                      const xgb_perm_contrib* __restrict__ contribs,
+                                                      const double* __restrict__ src, double* __restrict__ dst) {
+  constexpr int EPT = 4;
+  int64_t g = int64_t(blockIdx.x) * blockDim.x * EPT + threadIdx.x;
+  int cached = -1;
+  for (int e = 0; e < EPT; ++e, g += blockDim.x) {
+    if (g >= total) return;
+    int ti;
+    if (cached >= 0 && g >= start[cached] && g < start[cached + 1]) {
+      ti = cached;
+    } else {
+      int lo = 0, hi = n_tasks - 1;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= g) lo = mid; else hi = mid - 1;
+      }
+      ti = lo;
+      cached = ti;
+    }
+    const xgb_perm_task& t = tasks[ti];
+    int64_t rem = g - start[ti];
+    int idx[XGB_MAX_LEGS];
+    int64_t dofs = t.dst_base;
+    for (int k = 0; k < t.rank; ++k) {
+      int dk = t.dims[k];
+      int64_t q = rem / dk;
+      idx[k] = int(rem - q * dk);
+      rem = q;
+      dofs += idx[k] * t.dst_stride[k];
+    }
+    double v = 0.0;
+    for (int c = 0; c < t.n_contrib; ++c) {
+      const xgb_perm_contrib& cc = contribs[t.contrib0 + c];
+      int64_t so = cc.src_base;
+      for (int k = 0; k < t.rank; ++k) so += idx[k] * cc.src_stride[k];
+      v = fma(cc.coeff, src[so], v);
+    }
+    dst[dofs] = v;
+  }
+}
+
+void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_task_start, int n_tasks, int64_t total,
+                    const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s) {
+  if (total <= 0 || n_tasks <= 0) return;
+  int64_t per_block = 256 * 4;
+  int64_t blocks = (total + per_block - 1) / per_block;
+  permute_kernel<<<unsigned(blocks), 256, 0, s>>>(d_tasks, d_task_start, n_tasks, total, d_contribs, src, dst);
+  count_launch();
+}
+
+// ======================================================================= SVD
+// Batched one-sided (Hestenes) Jacobi SVD in FP64, one CTA per block.  For an
+// m x n block with m >= n the columns of W = A are orthogonalised by plane
+// rotations (accumulated into V); for m < n the same is done on A^T.  Pairs
+// follow the round-robin (circle) ordering, n/2 disjoint rotations per round
+// spread over the warps.  Converged when no pair has
+// |w_p.w_q| > tol*|w_p||w_q|.  Afterwards the singular values are sorted
+// descending (ties by column index) and every pair (u_j, v_j) is sign
+// normalised so that the largest-magnitude entry of u_j is positive.
+constexpr int kSvdThreads = 256;
+constexpr int kSvdMaxSweeps = 60;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ void rr_pair(int round, int k, int N, int& p, int& q) {
+  // circle method over N (even) slots; slot 0 fixed, slots 1..N-1 rotate
+  auto pos = [&](int i) { return (round + i) % (N - 1) + 1; };
+  if (k == 0) { p = 0; q = pos(0); }
+  else { p = pos(k); q = pos(N - 1 - k); }
+}
+
+__global__ void __launch_bounds__(kSvdThreads) svd_jacobi_kernel(const xgb_svd_desc* __restrict__ descs,
+                                                                 const int64_t* __restrict__ work_off,
+                                                                 const double* __restrict__ A, double* __restrict__ U,
+                                                                 double* __restrict__ S, double* __restrict__ Vt,
+                                                                 double* __restrict__ work) {
+  extern __shared__ unsigned char smem_raw[];
+  const xgb_svd_desc d = descs[blockIdx.x];
+  const bool tr = d.m < d.n;
+  const int64_t mm = tr ? d.n : d.m;  // rows of W
+  const int nn = int(tr ? d.m : d.n); // columns of W (= k)
+  if (nn == 0) return;
+  double* W = work + work_off[blockIdx.x];
+  double* V = W + mm * nn;
+  double* sval = reinterpret_cast<double*>(smem_raw);
+  int* order = reinterpret_cast<int*>(sval + nn);
+  __shared__ int rotated;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = kSvdThreads / 32;
+  // W = A or A^T, V = I
+  for (int64_t e = tid; e < mm * nn; e += kSvdThreads) {
+    int64_t i = e % mm, j = e / mm;
+    W[e] = tr ? A[d.a_off + j + i * d.m] : A[d.a_off + i + j * d.m];
+  }
+  for (int64_t e = tid; e < int64_t(nn) * nn; e += kSvdThreads) V[e] = ((e % nn) == (e / nn)) ? 1.0 : 0.0;
+  __syncthreads();
+
+  const double tol = 1.0e-15 * sqrt(double(mm));
+  const int N = nn + (nn & 1);
+  for (int sweep = 0; sweep < kSvdMaxSweeps && nn > 1; ++sweep) {
+    if (tid == 0) rotated = 0;
+    __syncthreads();
+    for (int round = 0; round < N - 1; ++round) {
+      for (int k = warp; k < N / 2; k += nw) {
+        int p, q;
+        rr_pair(round, k, N, p, q);
+        if (p >= nn || q >= nn) continue;
+        double* wp = W + int64_t(p) * mm;
+        double* wq = W + int64_t(q) * mm;
+        double al = 0, be = 0, ga = 0;
+        for (int64_t i = lane; i < mm; i += 32) {
+          double x = wp[i], y = wq[i];
+          al = fma(x, x, al);
+          be = fma(y, y, be);
+          ga = fma(x, y, ga);
+        }
+        al = warp_sum(al);
+        be = warp_sum(be);
+        ga = warp_sum(ga);
+        if (al == 0.0 || be == 0.0) continue;
+        if (fabs(ga) <= tol * sqrt(al) * sqrt(be)) continue;
+        double zeta = (be - al) / (2.0 * ga);
+        double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + hypot(1.0, zeta));
+        double c = 1.0 / sqrt(1.0 + t * t);
+        double s = c * t;
+        for (int64_t i = lane; i < mm; i += 32) {
+          double x = wp[i], y = wq[i];
+          wp[i] = c * x - s * y;
+          wq[i] = s * x + c * y;
+        }
+        double* vp = V + int64_t(p) * nn;
+        double* vq = V + int64_t(q) * nn;
+        for (int i = lane; i < nn; i += 32) {
+          double x = vp[i], y = vq[i];
+          vp[i] = c * x - s * y;
+          vq[i] = s * x + c * y;
+        }
+        if (lane == 0) rotated = 1;
+      }
+      __syncthreads();
+    }
+    if (rotated == 0) break;
+    __syncthreads();
+  }
+  // singular values = column norms
+  for (int j = warp; j < nn; j += nw) {
+    const double* wj = W + int64_t(j) * mm;
+    double acc = 0;
+    for (int64_t i = lane; i < mm; i += 32) acc = fma(wj[i], wj[i], acc);
+    acc = warp_sum(acc);
+    if (lane == 0) sval[j] = sqrt(acc);
+  }
+  __syncthreads();
+  for (int j = tid; j < nn; j += kSvdThreads) {
+    double sj = sval[j];
+    int r = 0;
+    for (int i = 0; i < nn; ++i) {
+      double si = sval[i];
+      r += (si > sj) || (si == sj && i < j);
+    }
+    order[r] = j;
+  }
+  __syncthreads();
+  const int64_t k = nn;
+  for (int r = warp; r < nn; r += nw) {
+    const int j = order[r];
+    const double sj = sval[j];
+    const double inv = sj > 0 ? 1.0 / sj : 0.0;
+    // left vector u = (tr ? V[:,j] : W[:,j]/s), right vector v = (tr ? W[:,j]/s : V[:,j])
+    const double* ucol = tr ? V + int64_t(j) * nn : W + int64_t(j) * mm;
+    const double uscale = tr ? 1.0 : inv;
+    const int64_t ulen = tr ? nn : mm;
+    // sign: largest |u_i| positive (first index on ties)
+    double best = -1.0, bval = 0.0;
+    int64_t bidx = 0;
+    for (int64_t i = lane; i < ulen; i += 32) {
+      double a = fabs(ucol[i]);
+      if (a > best) { best = a; bval = ucol[i]; bidx = i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      double ov = __shfl_xor_sync(0xffffffffu, bval, o);
+      int64_t oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+      if (ob > best || (ob == best && oi < bidx)) { best = ob; bval = ov; bidx = oi; }
+    }
+    const double sg = (bval < 0) ? -1.0 : 1.0;
+    for (int64_t i = lane; i < ulen; i += 32) U[d.u_off + i + r * d.m] = sg * uscale * ucol[i];
+    const double* vcol = tr ? W + int64_t(j) * mm : V + int64_t(j) * nn;
+    const double vscale = tr ? inv : 1.0;
+    const int64_t vlen = tr ? mm : nn;
+    for (int64_t c = lane; c < vlen; c += 32) Vt[d.vt_off + r + c * k] = sg * vscale * vcol[c];
+    if (lane == 0) S[d.s_off + r] = sj;
+  }
+}
+
+size_t svd_work_elems(int64_t m, int64_t n) {
+  int64_t mm = std::max(m, n), nn = std::min(m, n);
+  return size_t(mm * nn + nn * nn);
+}
+
+void launch_svd(const xgb_svd_desc* d_descs, const int64_t* d_work_off, int n, int64_t max_k, const double* A, double* U,
+                double* S, double* Vt, double* work, cudaStream_t s) {
+  if (n <= 0) return;
+  size_t smem = size_t(std::max<int64_t>(max_k, 1)) * (sizeof(double) + sizeof(int));
+  if (smem > 48 * 1024) cudaFuncSetAttribute(svd_jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  svd_jacobi_kernel<<<n, kSvdThreads, smem, s>>>(d_descs, d_work_off, A, U, S, Vt, work);
+  count_launch();
+}
+
+// ======================================================================= truncation
+// cutoff_matrices on the device: rank every singular value in the global
+// descending order (ties by position), keep rank < max_keep with s >= eps,
+// optionally cut the last multiplet, fall back to the first entry when
+// nothing survives, and count kept values per sector.  One CTA.
+__global__ void __launch_bounds__(1024) truncate_kernel(int n_sectors, const int64_t* __restrict__ s_begin,
+                                                        const int32_t* __restrict__ deg, const double* __restrict__ s,
+                                                        int64_t total, int64_t max_keep, double eps, int preserve,
+                                                        int32_t* __restrict__ keep, double* __restrict__ out2,
+                                                        int64_t* __restrict__ rank_buf, double* __restrict__ sorted) {
+  __shared__ double red_w[32], red_e[32];
+  __shared__ int64_t n_keep_sh;
+  __shared__ int64_t cut_sh;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int g = tid; g < n_sectors; g += blockDim.x) keep[g] = 0;
+  // global rank of each value
+  for (int64_t i = tid; i < total; i += blockDim.x) {
+    double si = s[i];
+    int64_t r = 0;
+    for (int64_t j = 0; j < total; ++j) {
+      double sj = s[j];
+      r += (sj > si) || (sj == si && j < i);
+    }
+    rank_buf[i] = r;
+    sorted[r] = si;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int64_t nk = total < max_keep ? total : max_keep;
+    if (eps > 0.0) {
+      // values are sorted descending, so "s < eps" removes a suffix
+      int64_t c = 0;
+      while (c < nk && !(sorted[c] < eps)) ++c;
+      nk = c;
+    }
+    if (preserve) {
+      int64_t end = -1;
+      for (int64_t i = nk - 1; i > 0; --i) {
+        double rel = 2.0 * (sorted[i - 1] - sorted[i]) / (sorted[i - 1] + sorted[i]);
+        if (rel > 0.1) { end = i; break; }
+      }
+      if (end != -1) nk = end;
+    }
+    n_keep_sh = nk;
+    cut_sh = (total < max_keep ? total : max_keep);
+  }
+  __syncthreads();
+  const int64_t nk = n_keep_sh, cut = cut_sh;
+  double wsum = 0.0, esum = 0.0;
+  for (int64_t i = tid; i < total; i += blockDim.x) {
+    // sector of i
+    int lo = 0, hi = n_sectors - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (s_begin[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    const double v = s[i];
+    const int64_t r = rank_buf[i];
+    if (r >= max_keep) wsum += deg[lo] * v * v;
+    bool kept = (nk > 0) ? (r < nk) : (i == 0);  // empty -> first entry (first value of first sector)
+    if (kept) {
+      atomicAdd(&keep[lo], 1);
+      esum += -deg[lo] * v * v * log(v * v);
+    }
+  }
+  (void)cut;
+  wsum = warp_sum(wsum);
+  esum = warp_sum(esum);
+  if (lane == 0) { red_w[warp] = wsum; red_e[warp] = esum; }
+  __syncthreads();
+  if (tid == 0) {
+    double a = 0, b = 0;
+    for (int w = 0; w < int(blockDim.x + 31) / 32; ++w) { a += red_w[w]; b += red_e[w]; }
+    out2[0] = a;
+    out2[1] = b;
+  }
+}
+
+void launch_truncate(int n_sectors, const int64_t* d_s_begin, const int32_t* d_deg, const double* s, int64_t total,
+                     int64_t max_keep, double eps, int preserve, int32_t* keep, double* out2, cudaStream_t st) {
+  int64_t* rank_buf = static_cast<int64_t*>(dev_alloc(sizeof(int64_t) * std::max<int64_t>(total, 1)));
+  double* sorted = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(total, 1)));
+  truncate_kernel<<<1, 1024, 0, st>>>(n_sectors, d_s_begin, d_deg, s, total, max_keep, eps, preserve, keep, out2, rank_buf,
+                                      sorted);
+  count_launch();
+  dev_free(rank_buf);
+  dev_free(sorted);
+}
+
+// ======================================================================= QR
+// Batched Householder QR in FP64 with LAPACK's dlarfg sign convention
+// (beta = -sign(alpha)*||x||), so Q and R agree with dgeqrf/dorgqr.
+__global__ void __launch_bounds__(256) qr_kernel(const xgb_qr_desc* __restrict__ descs, const int64_t* __restrict__ work_off,
+                                                 const double* __restrict__ A, double* __restrict__ Q,
+                                                 double* __restrict__ R, double* __restrict__ work) {
+  const xgb_qr_desc d = descs[blockIdx.x];
+  const int64_t m = d.m, n = d.n, kk = m < n ? m : n;
+  double* W = work + work_off[blockIdx.x];  // m x n working copy (Householder vectors below diagonal)
+  double* tau = W + m * n;                  // kk
+  double* Qw = tau + kk;                    // m x m accumulation
+  __shared__ double red[8];
+  __shared__ double bcast[2];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int64_t e = tid; e < m * n; e += 256) W[e] = A[d.a_off + e];
+  __syncthreads();
+  auto block_sum = [&](double v) {
+    v = warp_sum(v);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double r = 0;
+    if (tid == 0) { for (int w = 0; w < 8; ++w) r += red[w]; bcast[0] = r; }
+    __syncthreads();
+    r = bcast[0];
+    __syncthreads();
+    return r;
+  };
+  for (int64_t j = 0; j < kk; ++j) {
+    double* col = W + j * m;
+    double part = 0;
+    for (int64_t i = j + 1 + tid; i < m; i += 256) part = fma(col[i], col[i], part);
+    double xnorm2 = block_sum(part);
+    double alpha = col[j];
+    double t = 0.0, beta = alpha;
+    if (xnorm2 > 0.0) {
+      beta = -copysign(sqrt(alpha * alpha + xnorm2), alpha);
+      t = (beta - alpha) / beta;
+      double scal = 1.0 / (alpha - beta);
+      for (int64_t i = j + 1 + tid; i < m; i += 256) col[i] *= scal;
+    }
+    __syncthreads();
+    if (tid == 0) { tau[j] = t; col[j] = beta; }
+    __syncthreads();
+    if (t != 0.0) {
+      for (int64_t c = j + 1 + warp; c < n; c += 8) {
+        double* cc = W + c * m;
+        double w = (lane == 0) ? cc[j] : 0.0;
+        for (int64_t i = j + 1 + lane; i < m; i += 32) w = fma(col[i], cc[i], w);
+        w = warp_sum(w) * t;
+        if (lane == 0) cc[j] -= w;
+        for (int64_t i = j + 1 + lane; i < m; i += 32) cc[i] -= w * col[i];
+      }
+    }
+    __syncthreads();
+  }
+  // R (r_rows x n): upper triangle of W in the first kk rows
+  for (int64_t e = tid; e < d.r_rows * n; e += 256) {
+    int64_t i = e % d.r_rows, c = e / d.r_rows;
+    R[d.r_off + e] = (i < kk && i <= c) ? W[i + c * m] : 0.0;
+  }
+  // Q = H_0 H_1 ... H_{kk-1} applied to the first q_cols columns of I (backward accumulation)
+  const int64_t qc = d.q_cols < m ? d.q_cols : m;
+  for (int64_t e = tid; e < m * qc; e += 256) Qw[e] = ((e % m) == (e / m)) ? 1.0 : 0.0;
+  __syncthreads();
+  for (int64_t j = kk - 1; j >= 0; --j) {
+    const double t = tau[j];
+    if (t == 0.0) continue;
+    const double* v = W + j * m;
+    for (int64_t c = warp; c < qc; c += 8) {
+      double* cc = Qw + c * m;
+      double w = (lane == 0) ? cc[j] : 0.0;
+      for (int64_t i = j + 1 + lane; i < m; i += 32) w = fma(v[i], cc[i], w);
+      w = warp_sum(w) * t;
+      if (lane == 0) cc[j] -= w;
+      for (int64_t i = j + 1 + lane; i < m; i += 32) cc[i] -= w * v[i];
+    }
+    __syncthreads();
+  }
+  for (int64_t e = tid; e < m * d.q_cols; e += 256) {
+    int64_t c = e / m;
+    Q[d.q_off + e] = (c < qc && c < kk) ? Qw[e] : 0.0;
+  }
+}
+
+size_t qr_work_elems(int64_t m, int64_t n) { return size_t(m * n + std::min(m, n) + m * m); }
+
+void launch_qr(const xgb_qr_desc* d_descs, const int64_t* d_work_off, int n, const double* A, double* Q, double* R,
+               double* work, cudaStream_t s) {
+  if (n <= 0) return;
+  qr_kernel<<<n, 256, 0, s>>>(d_descs, d_work_off, A, Q, R, work);
+  count_launch();
+}
+
+// ======================================================================= elementwise
+__global__ void absmax_kernel(const double* __restrict__ x, int64_t n, unsigned long long* __restrict__ out) {
+  double m = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    m = fmax(m, fabs(x[i]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  // non-negative doubles order like their bit patterns
+  if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(out, __double_as_longlong(m));
+}
+
+void launch_absmax(const double* x, int64_t n, double* out, cudaStream_t s) {
+  cudaMemsetAsync(out, 0, sizeof(double), s);
+  if (n <= 0) return;
+  int blocks = int(std::min<int64_t>((n + 255) / 256, int64_t(num_sms()) * 8));
+  absmax_kernel<<<blocks, 256, 0, s>>>(x, n, reinterpret_cast<unsigned long long*>(out));
+  count_launch();
+}
+
+__global__ void scale_by_inv_kernel(double* __restrict__ x, int64_t n, const double* __restrict__ m) {
+  const double mv = *m;
+  if (mv == 0.0) return;
+  const double inv = 1.0 / mv;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) x[i] *= inv;
+}
+
+void launch_scale_by_inv(double* x, int64_t n, const double* m, cudaStream_t s) {
+  if (n <= 0) return;
+  int blocks = int(std::min<int64_t>((n + 255) / 256, int64_t(num_sms()) * 8));
+  scale_by_inv_kernel<<<blocks, 256, 0, s>>>(x, n, m);
+  count_launch();
+}
+
+__global__ void scale_kernel(double* __restrict__ x, int64_t n, double a) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) x[i] *= a;
+}
+
+void launch_scale(double* x, int64_t n, double alpha, cudaStream_t s) {
+  if (n <= 0) return;
+  int blocks = int(std::min<int64_t>((n + 255) / 256, int64_t(num_sms()) * 8));
+  scale_kernel<<<blocks, 256, 0, s>>>(x, n, alpha);
+  count_launch();
+}
+
+__global__ void copy2d_kernel(const xgb_copy2d_desc* __restrict__ descs, const double* __restrict__ src,
+                              double* __restrict__ dst) {
+  const xgb_copy2d_desc d = descs[blockIdx.y];
+  const int64_t ne = d.rows * d.cols;
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < ne; e += int64_t(gridDim.x) * blockDim.x) {
+    int64_t i = e % d.rows, j = e / d.rows;
+    dst[d.dst_off + i + j * d.dst_ld] = src[d.src_off + i + j * d.src_ld];
+  }
+}
+
+void launch_copy2d(const xgb_copy2d_desc* d_descs, int n, int64_t max_elems, const double* src, double* dst, cudaStream_t s) {
+  if (n <= 0 || max_elems <= 0) return;
+  dim3 grid(unsigned(std::min<int64_t>((max_elems + 255) / 256, 1024)), unsigned(n));
+  copy2d_kernel<<<grid, 256, 0, s>>>(d_descs, src, dst);
+  count_launch();
+}
+
+__device__ __forceinline__ double diag_fn(int fn, double x) {
+  switch (fn) {
+    case XGB_DIAG_SQRT: return sqrt(x);
+    case XGB_DIAG_INV: return 1.0 / x;
+    default: return 1.0 / sqrt(x);
+  }
+}
+
+__global__ void diag_from_vec_kernel(const xgb_copy2d_desc* __restrict__ descs, int fn, const double* __restrict__ src,
+                                     double* __restrict__ dst) {
+  const xgb_copy2d_desc d = descs[blockIdx.y];
+  const int64_t k = d.rows;
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < k * k; e += int64_t(gridDim.x) * blockDim.x) {
+    int64_t i = e % k, j = e / k;
+    dst[d.dst_off + e] = (i == j) ? (fn < 0 ? src[d.src_off + i] : diag_fn(fn, src[d.src_off + i])) : 0.0;
+  }
+}
+
+void launch_diag_from_vec(const xgb_copy2d_desc* d_descs, int n, int64_t max_k, int fn, const double* src, double* dst,
+                          cudaStream_t s) {
+  if (n <= 0 || max_k <= 0) return;
+  dim3 grid(unsigned(std::min<int64_t>((max_k * max_k + 255) / 256, 1024)), unsigned(n));
+  diag_from_vec_kernel<<<grid, 256, 0, s>>>(d_descs, fn, src, dst);
+  count_launch();
+}
+
+__global__ void diag_apply_kernel(const xgb_copy2d_desc* __restrict__ descs, int fn, double* __restrict__ x) {
+  const xgb_copy2d_desc d = descs[blockIdx.y];
+  const int64_t r = d.rows, c = d.cols;
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < r * c; e += int64_t(gridDim.x) * blockDim.x) {
+    int64_t i = e % r, j = e / r;
+    double* p = x + d.dst_off + i + j * d.dst_ld;
+    *p = (i == j) ? diag_fn(fn, *p) : 0.0;
+  }
+}
+
+void launch_diag_apply(const xgb_copy2d_desc* d_descs, int n, int64_t max_k, int fn, double* x, cudaStream_t s) {
+  if (n <= 0 || max_k <= 0) return;
+  dim3 grid(unsigned(std::min<int64_t>((max_k * max_k + 255) / 256, 1024)), unsigned(n));
+  diag_apply_kernel<<<grid, 256, 0, s>>>(d_descs, fn, x);
+  count_launch();
+}
+
+// ======================================================================= C-ABI helpers
+namespace {
+template <class T>
+T* upload(const T* host, size_t n, cudaStream_t s) {
+  T* d = static_cast<T*>(dev_alloc(sizeof(T) * std::max<size_t>(n, 1)));
+  if (n) cudaMemcpyAsync(d, host, sizeof(T) * n, cudaMemcpyHostToDevice, s);
+  return d;
+}
+cudaStream_t pick(void* s) { return s ? static_cast<cudaStream_t>(s) : g_rt.stream; }
+#define XGB_REQUIRE_INIT() \
+  if (!g_rt.ready) return set_error(XGB_E_NOINIT, "xgb_init was not called")
+#define XGB_GUARD_BEGIN try {
+#define XGB_GUARD_END                                                         \
+  }                                                                           \
+  catch (const std::bad_alloc&) {                                             \
+    return XGB_E_OOM;                                                         \
+  }                                                                           \
+  catch (const std::exception& ex) {                                          \
+    return set_error(XGB_E_BADPLAN, ex.what());                               \
+  }
+}  // namespace
+
+}  // namespace xgb
+
+using namespace xgb;
+
+extern "C" {
+
+int xgb_init(int device) {
+  if (g_rt.ready) return XGB_OK;
+  int rc = check_cuda(cudaSetDevice(device), "cudaSetDevice");
+  if (rc) return rc;
+  cudaDeviceProp prop{};
+  if ((rc = check_cuda(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties"))) return rc;
+  g_rt.sms = prop.multiProcessorCount;
+  g_rt.device = device;
+  if ((rc = check_cuda(cudaStreamCreateWithFlags(&g_rt.stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  if ((rc = check_cuda(cudaMalloc(&g_rt.scratch, 64 * sizeof(double)), "cudaMalloc scratch"))) return rc;
+  g_rt.ready = true;
+  return XGB_OK;
+}
+
+int xgb_shutdown(void) {
+  if (!g_rt.ready) return XGB_OK;
+  cudaStreamSynchronize(g_rt.stream);
+  cudaFree(g_rt.scratch);
+  cudaStreamDestroy(g_rt.stream);
+  g_rt = Runtime{};
+  return XGB_OK;
+}
+
+const char* xgb_last_error(void) { return g_err.c_str(); }
+
+int xgb_synchronize(void) {
+  XGB_REQUIRE_INIT();
+  return check_cuda(cudaStreamSynchronize(g_rt.stream), "cudaStreamSynchronize");
+}
+
+int64_t xgb_launch_count(void) { return g_launches.load(); }
+
+int xgb_profile_enable(int on) {
+  XGB_REQUIRE_INIT();
+  if (!on) prof_drain();
+  g_prof_on = on != 0;
+  return XGB_OK;
+}
+
+int xgb_profile_reset(void) {
+  XGB_REQUIRE_INIT();
+  cudaStreamSynchronize(g_rt.stream);
+  prof_drain();
+  for (int k = 0; k < K_COUNT; ++k) { g_prof_launches[k] = 0; g_prof_work[k] = 0; g_prof_ms[k] = 0; }
+  return XGB_OK;
+}
+
+int xgb_profile_read(int kind, int64_t* launches, double* ms, double* work) {
+  XGB_REQUIRE_INIT();
+  if (kind < 0 || kind >= K_COUNT) return set_error(XGB_E_BADPLAN, "kernel kind out of range");
+  cudaStreamSynchronize(g_rt.stream);
+  prof_drain();
+  *launches = g_prof_launches[kind];
+  *ms = g_prof_ms[kind];
+  *work = g_prof_work[kind];
+  return XGB_OK;
+}
+
+int xgb_event_record(int slot) {
+  XGB_REQUIRE_INIT();
+  if (slot < 0 || slot >= 16) return set_error(XGB_E_BADPLAN, "event slot out of range");
+  if (!g_user_events[slot]) cudaEventCreate(&g_user_events[slot]);
+  return check_cuda(cudaEventRecord(g_user_events[slot], g_rt.stream), "cudaEventRecord");
+}
+
+double xgb_event_elapsed_ms(int a, int b) {
+  if (a < 0 || a >= 16 || b < 0 || b >= 16 || !g_user_events[a] || !g_user_events[b]) return -1.0;
+  cudaEventSynchronize(g_user_events[b]);
+  float ms = -1.f;
+  if (cudaEventElapsedTime(&ms, g_user_events[a], g_user_events[b]) != cudaSuccess) return -1.0;
+  return ms;
+}
+
+void* xgb_stream_handle(void) { return g_rt.stream; }
+
+int xgb_malloc(void** ptr, size_t bytes) {
+  XGB_REQUIRE_INIT();
+  return check_cuda(cudaMalloc(ptr, bytes ? bytes : 8), "cudaMalloc");
+}
+int xgb_free(void* ptr) {
+  XGB_REQUIRE_INIT();
+  cudaStreamSynchronize(g_rt.stream);
+  return check_cuda(cudaFree(ptr), "cudaFree");
+}
+int xgb_memcpy_h2d(void* dst, const void* src, size_t bytes) {
+  XGB_REQUIRE_INIT();
+  int rc = check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, g_rt.stream), "h2d");
+  if (rc) return rc;
+  return check_cuda(cudaStreamSynchronize(g_rt.stream), "h2d sync");
+}
+int xgb_memcpy_d2h(void* dst, const void* src, size_t bytes) {
+  XGB_REQUIRE_INIT();
+  int rc = check_cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, g_rt.stream), "d2h");
+  if (rc) return rc;
+  return check_cuda(cudaStreamSynchronize(g_rt.stream), "d2h sync");
+}
+int xgb_memset_zero(void* dst, size_t bytes) {
+  XGB_REQUIRE_INIT();
+  return check_cuda(cudaMemsetAsync(dst, 0, bytes, g_rt.stream), "memset");
+}
+
+int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, const double* A, const double* B,
+                     double* C, double alpha, double beta, void* stream_) {
+  XGB_REQUIRE_INIT();
+  if (precision != XGB_PREC_FP64) return set_error(XGB_E_UNSUPPORTED, "precision form not available through this entry");
+  if (n_groups < 0) return set_error(XGB_E_BADPLAN, "n_groups < 0");
+  XGB_GUARD_BEGIN
+  cudaStream_t s = pick(stream_);
+  for (int g = 0; g < n_groups; ++g)
+    if (descs[g].m < 0 || descs[g].n < 0 || descs[g].k < 0) return set_error(XGB_E_BADPLAN, "negative GEMM extent");
+  const int tile = choose_gemm_tile(descs, n_groups);
+  std::vector<GemmTile> tiles;
+  for (int g = 0; g < n_groups; ++g) {
+    int64_t tm = (descs[g].m + tile - 1) / tile, tn = (descs[g].n + tile - 1) / tile;
+    for (int64_t j = 0; j < tn; ++j)
+      for (int64_t i = 0; i < tm; ++i) tiles.push_back({g, int32_t(i), int32_t(j), tile});
+  }
+  if (tiles.empty()) return XGB_OK;
+  auto* dd = upload(descs, size_t(n_groups), s);
+  auto* dt = upload(tiles.data(), tiles.size(), s);
+  launch_gemm_f64(dd, dt, int(tiles.size()), tile, A, B, C, alpha, beta, s);
+  dev_free(dd);
+  dev_free(dt);
+  return check_cuda(cudaGetLastError(), "gemm launch");
+  XGB_GUARD_END
+}
+
+int xgb_permute(int n_tasks, const xgb_perm_task* tasks, int n_contrib, const xgb_perm_contrib* contribs,
+                const double* src, double* dst, void* stream_) {
+  XGB_REQUIRE_INIT();
+  XGB_GUARD_BEGIN
+  cudaStream_t s = pick(stream_);
+  std::vector<int64_t> start(size_t(n_tasks) + 1, 0);
+  for (int t = 0; t < n_tasks; ++t) {
+    if (tasks[t].rank < 0 || tasks[t].rank > XGB_MAX_LEGS) return set_error(XGB_E_BADPLAN, "task rank out of range");
+    if (tasks[t].contrib0 < 0 || tasks[t].contrib0 + tasks[t].n_contrib > n_contrib)
+      return set_error(XGB_E_BADPLAN, "contribution index out of range");
+    start[t + 1] = start[t] + tasks[t].nelem;
+  }
+  if (n_tasks == 0 || start.back() == 0) return XGB_OK;
+  auto* dt = upload(tasks, size_t(n_tasks), s);
+  auto* ds = upload(start.data(), start.size(), s);
+  auto* dc = upload(contribs, size_t(n_contrib), s);
+  launch_permute(dt, ds, n_tasks, start.back(), dc, src, dst, s);
+  dev_free(dt);
+  dev_free(ds);
+  dev_free(dc);
+  return check_cuda(cudaGetLastError(), "permute launch");
+  XGB_GUARD_END
+}
+
+size_t xgb_svd_workspace_bytes(int n, const xgb_svd_desc* descs) {
+  size_t e = 0;
+  for (int i = 0; i < n; ++i) e += svd_work_elems(descs[i].m, descs[i].n);
+  return e * sizeof(double);
+}
+
+int xgb_batched_svd(int n, const xgb_svd_desc* descs, const double* A, double* U, double* S, double* Vt, void* work,
+                    void* stream_) {
+  XGB_REQUIRE_INIT();
+  XGB_GUARD_BEGIN
+  cudaStream_t s = pick(stream_);
+  std::vector<int64_t> off(size_t(std::max(n, 0)), 0);
+  int64_t acc = 0, maxk = 0;
+  for (int i = 0; i < n; ++i) {
+    if (descs[i].m < 0 || descs[i].n < 0) return set_error(XGB_E_BADPLAN, "negative SVD extent");
+    off[i] = acc;
+    acc += int64_t(svd_work_elems(descs[i].m, descs[i].n));
+    maxk = std::max(maxk, std::min(descs[i].m, descs[i].n));
+  }
+  if (maxk > 8192) return set_error(XGB_E_UNSUPPORTED, "SVD block larger than 8192 columns");
+  if (n == 0) return XGB_OK;
+  auto* dd = upload(descs, size_t(n), s);
+  auto* dof = upload(off.data(), off.size(), s);
+  launch_svd(dd, dof, n, maxk, A, U, S, Vt, static_cast<double*>(work), s);
+  dev_free(dd);
+  dev_free(dof);
+  return check_cuda(cudaGetLastError(), "svd launch");
+  XGB_GUARD_END
+}
+
+int xgb_truncate(int n_sectors, const int64_t* s_begin_host, const int32_t* degeneracy_host, const double* s,
+                 int64_t max_keep, double eps_svd, int preserve_multiplets, int32_t* keep_dev, double* out2_dev,
+                 void* stream_) {
+  XGB_REQUIRE_INIT();
+  XGB_GUARD_BEGIN
+  if (n_sectors <= 0) return set_error(XGB_E_BADPLAN, "truncation needs at least one sector");
+  cudaStream_t st = pick(stream_);
+  const int64_t total = s_begin_host[n_sectors];
+  if (total <= 0) return set_error(XGB_E_BADPLAN, "no singular values");
+  auto* db = upload(s_begin_host, size_t(n_sectors) + 1, st);
+  auto* dg = upload(degeneracy_host, size_t(n_sectors), st);
+  launch_truncate(n_sectors, db, dg, s, total, max_keep, eps_svd, preserve_multiplets, keep_dev, out2_dev, st);
+  dev_free(db);
+  dev_free(dg);
+  return check_cuda(cudaGetLastError(), "truncate launch");
+  XGB_GUARD_END
+}
+
+size_t xgb_qr_workspace_bytes(int n, const xgb_qr_desc* descs) {
+  size_t e = 0;
+  for (int i = 0; i < n; ++i) e += qr_work_elems(descs[i].m, descs[i].n);
+  return e * sizeof(double);
+}
+
+int xgb_batched_qr(int n, const xgb_qr_desc* descs, const double* A, double* Q, double* R, void* work, void* stream_) {
+  XGB_REQUIRE_INIT();
+  XGB_GUARD_BEGIN
+  cudaStream_t s = pick(stream_);
+  std::vector<int64_t> off(size_t(std::max(n, 0)), 0);
+  int64_t acc = 0;
+  for (int i = 0; i < n; ++i) {
+    off[i] = acc;
+    acc += int64_t(qr_work_elems(descs[i].m, descs[i].n));
+  }
+  if (n == 0) return XGB_OK;
+  auto* dd = upload(descs, size_t(n), s);
+  auto* dof = upload(off.data(), off.size(), s);
+  launch_qr(dd, dof, n, A, Q, R, static_cast<double*>(work), s);
+  dev_free(dd);
+  dev_free(dof);
+  return check_cuda(cudaGetLastError(), "qr launch");
+  XGB_GUARD_END
+}
+
+int xgb_absmax(const double* x, int64_t n, double* out_dev, void* stream_) {
+  XGB_REQUIRE_INIT();
+  launch_absmax(x, n, out_dev, pick(stream_));
+  return check_cuda(cudaGetLastError(), "absmax launch");
+}
+
+int xgb_scale_by_inv_absmax(double* x, int64_t n, double* scratch_dev, void* stream_) {
+  XGB_REQUIRE_INIT();
+  cudaStream_t s = pick(stream_);
+  launch_absmax(x, n, scratch_dev, s);
+  launch_scale_by_inv(x, n, scratch_dev, s);
+  return check_cuda(cudaGetLastError(), "scale launch");
+}
+
+int xgb_scale(double* x, int64_t n, double alpha, void* stream_) {
+  XGB_REQUIRE_INIT();
+  launch_scale(x, n, alpha, pick(stream_));
+  return check_cuda(cudaGetLastError(), "scale launch");
+}
+
+int xgb_copy2d_batched(int n, const xgb_copy2d_desc* descs, const double* src, double* dst, void* stream_) {
+  XGB_REQUIRE_INIT();
+  XGB_GUARD_BEGIN
+  if (n <= 0) return XGB_OK;
+  cudaStream_t s = pick(stream_);
+  int64_t mx = 0;
+  for (int i = 0; i < n; ++i) mx = std::max(mx, descs[i].rows * descs[i].cols);
+  auto* dd = upload(descs, size_t(n), s);
+  launch_copy2d(dd, n, mx, src, dst, s);
+  dev_free(dd);
+  return check_cuda(cudaGetLastError(), "copy2d launch");
+  XGB_GUARD_END
+}
+
+int xgb_diag_from_vec(int n, const xgb_copy2d_desc* descs, int fn, const double* src, double* dst, void* stream_) {
+  XGB_REQUIRE_INIT();
+  XGB_GUARD_BEGIN
+  if (n <= 0) return XGB_OK;
+  cudaStream_t s = pick(stream_);
+  int64_t mx = 0;
+  for (int i = 0; i < n; ++i) mx = std::max(mx, descs[i].rows);
+  auto* dd = upload(descs, size_t(n), s);
+  launch_diag_from_vec(dd, n, mx, fn, src, dst, s);
+  dev_free(dd);
+  return check_cuda(cudaGetLastError(), "diag launch");
+  XGB_GUARD_END
+}
+
+int xgb_diag_apply(int n, const xgb_copy2d_desc* descs, int fn, double* x, void* stream_) {
+  XGB_REQUIRE_INIT();
+  XGB_GUARD_BEGIN
+  if (n <= 0) return XGB_OK;
+  cudaStream_t s = pick(stream_);
+  int64_t mx = 0;
+  for (int i = 0; i < n; ++i) mx = std::max(mx, std::max(descs[i].rows, descs[i].cols));
+  auto* dd = upload(descs, size_t(n), s);
+  launch_diag_apply(dd, n, mx, fn, x, s);
+  dev_free(dd);
+  return check_cuda(cudaGetLastError(), "diag launch");
+  XGB_GUARD_END
+}
+
+}  // extern "C"

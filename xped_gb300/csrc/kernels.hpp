@@ -1,0 +1,60 @@
+// Internal launch interface shared by the host layer and the CUDA kernels.
+// The host layer keeps its descriptor tables resident on the device (plans
+// are cached), so these launchers take DEVICE descriptor pointers; the public
+// xgb_* entry points in include/xgb.h upload host descriptors and call them.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/xgb.h"
+
+namespace xgb {
+
+struct GemmTile { int32_t g, tm, tn, tile; };  // tile = edge length (16/32/64)
+
+// runtime ------------------------------------------------------------------------
+cudaStream_t stream();
+int set_error(int code, const std::string& msg);
+int check_cuda(cudaError_t e, const char* what);
+void* dev_alloc(size_t bytes);          // stream-ordered; throws std::bad_alloc on failure
+void dev_free(void* p);
+void count_launch(int n = 1);
+int num_sms();
+
+// device scratch for small results (absmax, truncation outputs)
+double* scalar_scratch();
+
+// launchers (descriptor arrays are device pointers) -----------------------------------
+void launch_gemm_f64(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
+                     const double* B, double* C, double alpha, double beta, cudaStream_t s);
+void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_task_start, int n_tasks, int64_t total,
+                    const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s);
+void launch_svd(const xgb_svd_desc* d_descs, const int64_t* d_work_off, int n, int64_t max_k, const double* A, double* U,
+                double* S, double* Vt, double* work, cudaStream_t s);
+void launch_truncate(int n_sectors, const int64_t* d_s_begin, const int32_t* d_deg, const double* sv, int64_t total,
+                     int64_t max_keep, double eps, int preserve, int32_t* keep, double* out2, cudaStream_t s);
+void launch_qr(const xgb_qr_desc* d_descs, const int64_t* d_work_off, int n, const double* A, double* Q, double* R,
+               double* work, cudaStream_t s);
+void launch_absmax(const double* x, int64_t n, double* out, cudaStream_t s);
+void launch_scale_by_inv(double* x, int64_t n, const double* m, cudaStream_t s);
+void launch_scale(double* x, int64_t n, double alpha, cudaStream_t s);
+void launch_copy2d(const xgb_copy2d_desc* d_descs, int n, int64_t max_elems, const double* src, double* dst, cudaStream_t s);
+void launch_diag_from_vec(const xgb_copy2d_desc* d_descs, int n, int64_t max_k, int fn, const double* src, double* dst,
+                          cudaStream_t s);
+void launch_diag_apply(const xgb_copy2d_desc* d_descs, int n, int64_t max_k, int fn, double* x, cudaStream_t s);
+
+// per-kernel-kind instrumentation (CUDA events around each launch when enabled;
+// algorithmic work - flops for GEMMs, bytes for data movement - always counted)
+enum KernelKind { K_GEMM = 0, K_PERMUTE, K_SVD, K_TRUNC, K_QR, K_ABSMAX, K_SCALE, K_COPY2D, K_DIAG, K_GEMM_TC, K_COUNT };
+void prof_begin(int kind, cudaStream_t s);
+void prof_end(int kind, cudaStream_t s, double work);
+
+// helpers
+size_t svd_work_elems(int64_t m, int64_t n);
+size_t qr_work_elems(int64_t m, int64_t n);
+int choose_gemm_tile(const xgb_gemm_desc* descs, int n);  // host-side tile heuristic
+
+}  // namespace xgb

@@ -1,0 +1,1007 @@
+// Device tensor operations: plan building (host) + grouped launches (device).
+// Every function cites the reference routine whose semantics it follows.
+#include "tensor.hpp"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <sstream>
+#include <stdexcept>
+
+namespace xgb {
+
+static constexpr double kCoeffCut = 1.0e-10;  // src/Core/Tensor.cpp:127,193
+
+static void cuda_ok(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    set_error(XGB_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+// persistent device copy of a host table (plans live as long as the cache)
+template <class T>
+static T* dev_table(const std::vector<T>& v) {
+  T* d = nullptr;
+  size_t bytes = sizeof(T) * std::max<size_t>(v.size(), 1);
+  cuda_ok(cudaMalloc(&d, bytes), "cudaMalloc(plan)");
+  if (!v.empty()) cuda_ok(cudaMemcpy(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice), "plan upload");
+  return d;
+}
+
+// ======================================================================= meta
+namespace {
+std::mutex g_meta_mu;
+std::unordered_map<std::string, std::shared_ptr<const TensorMeta>> g_metas;  // metas are small; keep them for plan reuse
+uint64_t g_meta_next = 1;
+}  // namespace
+
+static MetaPtr finish_meta(TensorMeta&& m) {
+  std::ostringstream os;
+  os << m.sym.kind << ':' << m.sym.N << '|';
+  for (auto& b : m.dom) os << b->id << ',';
+  os << '|';
+  for (auto& b : m.cod) os << b->id << ',';
+  os << '|';
+  for (int q : m.sectors) os << q << ',';
+  std::string key = os.str();
+  std::lock_guard<std::mutex> lk(g_meta_mu);
+  auto it = g_metas.find(key);
+  if (it != g_metas.end()) return it->second;
+  m.id = g_meta_next++;
+  auto sp = std::make_shared<const TensorMeta>(std::move(m));
+  g_metas[key] = sp;
+  return sp;
+}
+
+static void fill_blocks(TensorMeta& m) {
+  m.rows.clear(); m.cols.clear(); m.offset.clear(); m.dict.clear();
+  int64_t cur = 0;
+  for (size_t i = 0; i < m.sectors.size(); ++i) {
+    int q = m.sectors[i];
+    m.dict[q] = int(i);
+    m.rows.push_back(m.cdom->inner_dim(q));
+    m.cols.push_back(m.ccod->inner_dim(q));
+    m.offset.push_back(cur);
+    cur += m.rows.back() * m.cols.back();
+  }
+  m.size = cur;
+}
+
+MetaPtr make_meta(const Sym& s, const std::vector<BasisPtr>& dom, const std::vector<BasisPtr>& cod) {
+  if (dom.size() + cod.size() > kMaxRank) throw std::runtime_error("tensor rank exceeds 8 legs");
+  TensorMeta m;
+  m.sym = s;
+  m.dom = dom;
+  m.cod = cod;
+  m.cdom = build_fusion_tree(s, dom);
+  m.ccod = build_fusion_tree(s, cod);
+  for (int q : m.cdom->qs)
+    if (m.ccod->index(q) >= 0) m.sectors.push_back(q);  // StorageType_contiguous.hpp:79-97
+  fill_blocks(m);
+  return finish_meta(std::move(m));
+}
+
+MetaPtr make_meta_ordered(const Sym& s, const std::vector<BasisPtr>& dom, const std::vector<BasisPtr>& cod,
+                          const std::vector<int>& sectors) {
+  TensorMeta m;
+  m.sym = s;
+  m.dom = dom;
+  m.cod = cod;
+  m.cdom = build_fusion_tree(s, dom);
+  m.ccod = build_fusion_tree(s, cod);
+  m.sectors = sectors;
+  fill_blocks(m);
+  return finish_meta(std::move(m));
+}
+
+DevBuf::DevBuf(int64_t n_) : n(n_) { p = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(n_, 1))); }
+DevBuf::~DevBuf() { dev_free(p); }
+
+Tensor empty_like_meta(const MetaPtr& m) {
+  Tensor t;
+  t.meta = m;
+  t.buf = std::make_shared<DevBuf>(m->size);
+  return t;
+}
+
+Tensor zeros(const MetaPtr& m) {
+  Tensor t = empty_like_meta(m);
+  if (m->size) cuda_ok(cudaMemsetAsync(t.data(), 0, sizeof(double) * m->size, stream()), "memset");
+  return t;
+}
+
+// ======================================================================= permute plans
+namespace {
+struct PermPlan {
+  MetaPtr out;
+  bool needs_zero = false;
+  int n_tasks = 0;
+  int64_t total = 0;
+  xgb_perm_task* d_tasks = nullptr;
+  int64_t* d_start = nullptr;
+  xgb_perm_contrib* d_contribs = nullptr;
+  double bytes = 0;  // algorithmic: every output written once, every contribution read once
+};
+struct GemmPlan {
+  MetaPtr out;
+  double flops = 0;  // useful 2*m*n*k summed over groups
+  int n_tiles = 0, tile = 16;
+  xgb_gemm_desc* d_descs = nullptr;
+  GemmTile* d_tiles = nullptr;
+};
+std::shared_ptr<PermPlan> upload_tables(const PermTables& t) {
+  auto plan = std::make_shared<PermPlan>();
+  plan->out = t.out;
+  plan->n_tasks = int(t.tasks.size());
+  plan->total = t.start.back();
+  plan->needs_zero = t.needs_zero;
+  plan->d_tasks = dev_table(t.tasks);
+  plan->d_start = dev_table(t.start);
+  plan->d_contribs = dev_table(t.contribs);
+  for (const auto& task : t.tasks) plan->bytes += 8.0 * double(task.nelem) * (1 + task.n_contrib);
+  return plan;
+}
+std::mutex g_plan_mu;
+std::unordered_map<std::string, std::shared_ptr<PermPlan>> g_perm_plans;
+std::unordered_map<std::string, std::shared_ptr<GemmPlan>> g_gemm_plans;
+CacheStats g_stats;
+
+struct TaskBuilder {
+  std::map<int64_t, int> by_dst;  // dst_base -> task
+  std::vector<xgb_perm_task> tasks;
+  std::vector<std::vector<xgb_perm_contrib>> contribs;
+
+  void add(int64_t dst_base, int rank, const int32_t* dims, const int64_t* dst_stride, int64_t src_base,
+           const int64_t* src_stride, double coeff) {
+    auto it = by_dst.find(dst_base);
+    int ti;
+    if (it == by_dst.end()) {
+      xgb_perm_task t{};
+      t.dst_base = dst_base;
+      t.rank = rank;
+      t.nelem = 1;
+      for (int k = 0; k < rank; ++k) {
+        t.dims[k] = dims[k];
+        t.dst_stride[k] = dst_stride[k];
+        t.nelem *= dims[k];
+      }
+      ti = int(tasks.size());
+      tasks.push_back(t);
+      contribs.emplace_back();
+      by_dst.emplace(dst_base, ti);
+    } else {
+      ti = it->second;
+      for (int k = 0; k < rank; ++k)
+        if (tasks[ti].dims[k] != dims[k]) throw std::runtime_error("permute plan: inconsistent sub-block shapes");
+    }
+    xgb_perm_contrib c{};
+    c.src_base = src_base;
+    c.coeff = coeff;
+    for (int k = 0; k < rank; ++k) c.src_stride[k] = src_stride[k];
+    contribs[ti].push_back(c);
+  }
+
+  PermTables tables(const MetaPtr& out) const {
+    PermTables t;
+    t.out = out;
+    t.start.push_back(0);
+    for (const auto& [dst, ti] : by_dst) {
+      xgb_perm_task task = tasks[ti];
+      task.contrib0 = int32_t(t.contribs.size());
+      task.n_contrib = int32_t(contribs[ti].size());
+      for (const auto& c : contribs[ti]) t.contribs.push_back(c);
+      t.tasks.push_back(task);
+      t.start.push_back(t.start.back() + task.nelem);
+    }
+    t.needs_zero = t.start.back() < out->size;
+    return t;
+  }
+
+  std::shared_ptr<PermPlan> finish(const MetaPtr& out) const { return upload_tables(tables(out)); }
+};
+
+// column-major strides of a sub-tensor with the given leg dims; codomain
+// legs are additionally scaled by the block's leading dimension.
+void sub_strides(const FusionTree& f1, const FusionTree& f2, int64_t ld, int64_t* st) {
+  int64_t acc = 1;
+  for (int m = 0; m < f1.rank; ++m) { st[m] = acc; acc *= f1.dims[m]; }
+  acc = ld;
+  for (int m = 0; m < f2.rank; ++m) { st[f1.rank + m] = acc; acc *= f2.dims[m]; }
+}
+
+double twist_coeff(const Sym& s, uint32_t mask, const FusionTree& f1, const FusionTree& f2) {
+  double c = 1.0;
+  if (!mask) return c;
+  for (int l = 0; l < f1.rank + f2.rank; ++l)
+    if ((mask >> l) & 1u) c *= (l < f1.rank) ? s.coeff_twist(f1.qu[l]) : s.coeff_twist(f2.qu[l - f1.rank]);
+  return c;
+}
+
+}  // namespace
+
+PermTables build_perm_tables(const TensorMeta& in, uint32_t mask, int shift, const std::vector<int>& p) {
+  const Sym& s = in.sym;
+  const int R = in.rank(), C = in.corank(), N = R + C;
+  const int newR = R - shift, newC = C + shift;
+  std::vector<int> pd(p.begin(), p.begin() + newR), pc(p.begin() + newR, p.end());
+  const bool identity = (shift == 0) && [&] {
+    for (int i = 0; i < N; ++i) if (p[i] != i) return false;
+    return true;
+  }();
+  const bool within = !identity && shift == 0 && std::all_of(pd.begin(), pd.end(), [&](int x) { return x < R; }) &&
+                      std::all_of(pc.begin(), pc.end(), [&](int x) { return x >= R; });
+  // output bases (Tensor.cpp:100-106 for the within path, 157-176 otherwise)
+  std::vector<BasisPtr> nd, nc;
+  if (identity) {
+    nd = in.dom;
+    nc = in.cod;
+  } else if (within) {
+    for (int x : pd) nd.push_back(in.dom[x]);
+    for (int x : pc) nc.push_back(in.cod[x - R]);
+  } else {
+    for (int i = 0; i < newR; ++i) nd.push_back((p[i] > R - 1 || R == 0) ? in.cod[p[i] - R] : in.dom[p[i]]);
+    for (int i = 0; i < newR; ++i) if (p[i] > R - 1 || R == 0) nd[i] = basis_conj(nd[i]);
+    for (int i = 0; i < newC; ++i) {
+      int x = p[i + newR];
+      nc.push_back((x > R - 1 || R == 0) ? in.cod[x - R] : basis_conj(in.dom[x]));
+    }
+  }
+  MetaPtr out = identity ? make_meta_ordered(s, nd, nc, in.sectors) : make_meta(s, nd, nc);
+  std::vector<int> pdd, pcc;
+  for (int x : pd) pdd.push_back(x);
+  for (int x : pc) pcc.push_back(x - R);
+
+  TaskBuilder tb;
+  int64_t ist[kMaxRank], ost[kMaxRank], sst[kMaxRank];
+  int32_t odims[kMaxRank];
+  for (size_t si = 0; si < in.sectors.size(); ++si) {
+    const int q = in.sectors[si];
+    const int dq = in.cdom->index(q), cq = in.ccod->index(q);
+    for (const auto& f1 : in.cdom->trees[dq]) {
+      for (const auto& f2 : in.ccod->trees[cq]) {
+        const double tw = twist_coeff(s, mask, f1, f2);
+        const int64_t src_base = in.offset[si] + in.cdom->left_offset(f1) + in.ccod->left_offset(f2) * in.rows[si];
+        sub_strides(f1, f2, in.rows[si], ist);
+        auto emit = [&](const FusionTree& g1, const FusionTree& g2, double coeff, const std::vector<int>& ptot) {
+          const int oq = out->index(g1.qc);
+          if (oq < 0) throw std::runtime_error("permute plan: output sector missing");
+          const int64_t dst_base = out->offset[oq] + out->cdom->left_offset(g1) + out->ccod->left_offset(g2) * out->rows[oq];
+          sub_strides(g1, g2, out->rows[oq], ost);
+          for (int k = 0; k < N; ++k) {
+            odims[k] = (k < g1.rank) ? g1.dims[k] : g2.dims[k - g1.rank];
+            sst[k] = ist[ptot[k]];
+          }
+          tb.add(dst_base, N, odims, ost, src_base, sst, coeff * tw);
+        };
+        if (identity) {
+          std::vector<int> ptot(N);
+          std::iota(ptot.begin(), ptot.end(), 0);
+          emit(f1, f2, 1.0, ptot);
+        } else if (within) {
+          // permute_impl(pd, pc) (Tensor.cpp:83-146)
+          TreeMap a = tree_permute(s, f1, pdd), b = tree_permute(s, f2, pcc);
+          std::vector<int> ptot = p;
+          for (const auto& [g1, c1] : a)
+            for (const auto& [g2, c2] : b) {
+              if (std::abs(c1 * c2) < kCoeffCut) continue;
+              emit(g1, g2, c1 * c2, ptot);
+            }
+        } else {
+          // permute_impl<shift>(p) (Tensor.cpp:148-214)
+          for (const auto& [pr, c] : treepair_permute(s, shift, f1, f2, p)) {
+            if (std::abs(c) < kCoeffCut) continue;
+            emit(pr.first, pr.second, c, p);
+          }
+        }
+      }
+    }
+  }
+  return tb.tables(out);
+}
+
+namespace {
+std::string perm_key(const TensorMeta& m, uint32_t mask, int shift, const std::vector<int>& p) {
+  std::ostringstream os;
+  os << m.id << '|' << mask << '|' << shift << '|';
+  for (int x : p) os << x << ',';
+  return os.str();
+}
+
+std::shared_ptr<PermPlan> get_perm_plan(const TensorMeta& m, uint32_t mask, int shift, const std::vector<int>& p) {
+  std::string key = perm_key(m, mask, shift, p);
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    auto it = g_perm_plans.find(key);
+    if (it != g_perm_plans.end()) { ++g_stats.perm_hits; return it->second; }
+  }
+  auto plan = upload_tables(build_perm_tables(m, mask, shift, p));
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  ++g_stats.perm_misses;
+  g_perm_plans[key] = plan;
+  return plan;
+}
+
+Tensor run_perm_plan(const PermPlan& plan, const Tensor& src) {
+  Tensor out = plan.needs_zero ? zeros(plan.out) : empty_like_meta(plan.out);
+  prof_begin(K_PERMUTE, stream());
+  launch_permute(plan.d_tasks, plan.d_start, plan.n_tasks, plan.total, plan.d_contribs, src.data(), out.data(), stream());
+  prof_end(K_PERMUTE, stream(), plan.bytes);
+  return out;
+}
+}  // namespace
+
+CacheStats cache_stats() { return g_stats; }
+
+void clear_plan_caches() {
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  cudaStreamSynchronize(stream());
+  for (auto& [k, p] : g_perm_plans) { cudaFree(p->d_tasks); cudaFree(p->d_start); cudaFree(p->d_contribs); }
+  for (auto& [k, p] : g_gemm_plans) { cudaFree(p->d_descs); cudaFree(p->d_tiles); }
+  g_perm_plans.clear();
+  g_gemm_plans.clear();
+}
+
+Tensor materialize(const Tensor& t) {
+  if (!t.twist_mask) return t;
+  const int N = t.meta->rank() + t.meta->corank();
+  std::vector<int> id(N);
+  std::iota(id.begin(), id.end(), 0);
+  auto plan = get_perm_plan(*t.meta, t.twist_mask, 0, id);
+  return run_perm_plan(*plan, t);
+}
+
+Tensor permute(const Tensor& t, int shift, const std::vector<int>& p) {
+  // Tensor::permute dispatcher (Tensor.cpp:335-355)
+  const int R = t.meta->rank(), C = t.meta->corank();
+  if (int(p.size()) != R + C) throw std::runtime_error("permute: permutation length mismatch");
+  if (shift > R || -shift > C) throw std::runtime_error("permute: invalid shift");
+  bool id = shift == 0;
+  for (int i = 0; i < R + C && id; ++i) id = (p[i] == i);
+  if (id) return materialize(t);
+  auto plan = get_perm_plan(*t.meta, t.twist_mask, shift, p);
+  return run_perm_plan(*plan, t);
+}
+
+Tensor twist(const Tensor& t, int leg) {
+  // Tensor::twist (Tensor.cpp:357-377): a +-1 per sub-block for abelian
+  // fermionic charges; kept pending and folded into the next permute.
+  if (!t.meta->sym.fermionic()) return t;
+  if (leg < 0 || leg >= t.meta->rank() + t.meta->corank()) throw std::runtime_error("twist: leg out of range");
+  Tensor out = t;
+  out.twist_mask ^= (1u << leg);
+  return out;
+}
+
+Tensor adjoint(const Tensor& t0) {
+  // AdjointOp evaluated (AdjointOp.hpp:49-59, Tensor.hpp:446-453): blocks
+  // transposed, domain <-> codomain, sectors kept in the original order.
+  Tensor t = materialize(t0);
+  const TensorMeta& m = *t.meta;
+  MetaPtr out = make_meta_ordered(m.sym, m.cod, m.dom, m.sectors);
+  std::string key = "adj|" + std::to_string(m.id);
+  std::shared_ptr<PermPlan> plan;
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    auto it = g_perm_plans.find(key);
+    if (it != g_perm_plans.end()) plan = it->second;
+  }
+  if (!plan) {
+    TaskBuilder tb;
+    for (size_t i = 0; i < m.sectors.size(); ++i) {
+      const int64_t r = m.rows[i], c = m.cols[i];
+      if (r * c == 0) continue;
+      int32_t dims[2] = {int32_t(c), int32_t(r)};
+      int64_t dst[2] = {1, c};
+      int64_t src[2] = {r, 1};
+      tb.add(out->offset[i], 2, dims, dst, m.offset[i], src, 1.0);
+    }
+    plan = tb.finish(out);
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    g_perm_plans[key] = plan;
+  }
+  return run_perm_plan(*plan, t);
+}
+
+// ======================================================================= GEMM
+GemmTables build_gemm_tables(const TensorMeta& A, bool adj_a, const TensorMeta& B, bool adj_b) {
+  const auto& adom = adj_a ? A.cod : A.dom;
+  const auto& acod = adj_a ? A.dom : A.cod;
+  const auto& bdom = adj_b ? B.cod : B.dom;
+  const auto& bcod = adj_b ? B.dom : B.cod;
+  if (acod.size() != bdom.size()) throw std::runtime_error("operator*: CoRank of left != Rank of right");
+  GemmTables gt;
+  gt.out = make_meta(A.sym, adom, bcod);
+  const TensorMeta& O = *gt.out;
+  std::vector<char> covered(O.sectors.size(), 0);
+  for (size_t i = 0; i < A.sectors.size(); ++i) {
+    const int q = A.sectors[i];
+    const int j = B.index(q);
+    if (j < 0) continue;
+    const int o = O.index(q);
+    if (o < 0) throw std::runtime_error("operator*: output sector missing");
+    xgb_gemm_desc d{};
+    d.m = adj_a ? A.cols[i] : A.rows[i];
+    d.k = adj_a ? A.rows[i] : A.cols[i];
+    const int64_t kb = adj_b ? B.cols[j] : B.rows[j];
+    d.n = adj_b ? B.rows[j] : B.cols[j];
+    if (kb != d.k || d.m != O.rows[o] || d.n != O.cols[o])
+      throw std::runtime_error("operator*: block shapes do not match (coupled codomain != coupled domain)");
+    d.a_off = A.offset[i]; d.lda = A.rows[i];
+    d.b_off = B.offset[j]; d.ldb = B.rows[j];
+    d.c_off = O.offset[o]; d.ldc = O.rows[o];
+    d.trans_a = adj_a; d.trans_b = adj_b;
+    gt.descs.push_back(d);
+    covered[o] = 1;
+  }
+  // sectors of the output with no partner stay zero (Tout.setZero(), TensorBase.cpp:256-258): k = 0 groups
+  for (size_t o = 0; o < O.sectors.size(); ++o) {
+    if (covered[o] || O.rows[o] * O.cols[o] == 0) continue;
+    xgb_gemm_desc d{};
+    d.m = O.rows[o]; d.n = O.cols[o]; d.k = 0;
+    d.lda = 1; d.ldb = 1;
+    d.c_off = O.offset[o]; d.ldc = O.rows[o];
+    gt.descs.push_back(d);
+  }
+  return gt;
+}
+
+Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
+  // TensorBase::operator* (TensorBase.cpp:237-288), with AdjointOp operands
+  // handled as transposed GEMM operands (no materialised transpose).
+  Tensor a = materialize(a0), b = materialize(b0);
+  const TensorMeta& A = *a.meta;
+  const TensorMeta& B = *b.meta;
+  std::ostringstream os;
+  os << A.id << (adj_a ? 'T' : 'N') << '|' << B.id << (adj_b ? 'T' : 'N');
+  const std::string key = os.str();
+  std::shared_ptr<GemmPlan> plan;
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    auto it = g_gemm_plans.find(key);
+    if (it != g_gemm_plans.end()) { plan = it->second; ++g_stats.gemm_hits; }
+  }
+  if (!plan) {
+    GemmTables gt = build_gemm_tables(A, adj_a, B, adj_b);
+    plan = std::make_shared<GemmPlan>();
+    plan->out = gt.out;
+    const std::vector<xgb_gemm_desc>& descs = gt.descs;
+    plan->tile = choose_gemm_tile(descs.data(), int(descs.size()));
+    std::vector<GemmTile> tiles;
+    for (size_t g = 0; g < descs.size(); ++g) {
+      int64_t tm = (descs[g].m + plan->tile - 1) / plan->tile, tn = (descs[g].n + plan->tile - 1) / plan->tile;
+      for (int64_t y = 0; y < tn; ++y)
+        for (int64_t x = 0; x < tm; ++x) tiles.push_back({int32_t(g), int32_t(x), int32_t(y), plan->tile});
+    }
+    plan->n_tiles = int(tiles.size());
+    plan->d_descs = dev_table(descs);
+    plan->d_tiles = dev_table(tiles);
+    for (const auto& d : descs) plan->flops += 2.0 * double(d.m) * double(d.n) * double(d.k);
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    ++g_stats.gemm_misses;
+    g_gemm_plans[key] = plan;
+  }
+  Tensor out = empty_like_meta(plan->out);
+  prof_begin(K_GEMM, stream());
+  launch_gemm_f64(plan->d_descs, plan->d_tiles, plan->n_tiles, plan->tile, a.data(), b.data(), out.data(), 1.0, 0.0, stream());
+  prof_end(K_GEMM, stream(), plan->flops);
+  return out;
+}
+
+// ======================================================================= contract
+ContractPerms get_permutations(const std::vector<int>& a1, int rank1, const std::vector<int>& a2, int rank2, int rankres) {
+  ContractPerms r;
+  const int r1 = int(a1.size()), r2 = int(a2.size());
+  int max1 = 0, max2 = 0;
+  for (int x : a1) max1 = std::max(max1, x);
+  for (int x : a2) max2 = std::max(max2, x);
+  if (max1 != max2) throw std::runtime_error("contract: label sets do not match");
+  auto pos = [](const std::vector<int>& a, int v) {
+    auto it = std::find(a.begin(), a.end(), v);
+    if (it == a.end()) throw std::runtime_error("contract: missing label");
+    return int(it - a.begin());
+  };
+  r.p2.assign(r2, 0);
+  std::vector<int> found2(r2, -1);
+  for (int ind = 0; ind < max2; ++ind) { int v = pos(a2, ind + 1); found2[ind] = v; r.p2[ind] = v; }
+  for (int ind = max2; ind < r2; ++ind) {
+    int v = 0;
+    while (std::find(found2.begin(), found2.end(), v) != found2.end()) ++v;
+    found2[ind] = v;
+    r.p2[ind] = v;
+  }
+  r.p1.assign(r1, 0);
+  std::vector<int> found1(r1, -1);
+  for (int ind = 0; ind < max1; ++ind) { int v = pos(a1, ind + 1); found1[ind] = v; r.p1[r1 - max1 + ind] = v; }
+  for (int ind = max1, k = 0; ind < r1; ++ind, ++k) {
+    int v = 0;
+    while (std::find(found1.begin(), found1.end(), v) != found1.end()) ++v;
+    found1[ind] = v;
+    r.p1[k] = v;
+  }
+  std::vector<int> tmp;
+  for (int x : a1) if (x < 0) tmp.push_back(x);
+  for (int x : a2) if (x < 0) tmp.push_back(x);
+  r.pres.resize(tmp.size());
+  std::iota(r.pres.begin(), r.pres.end(), 0);
+  std::stable_sort(r.pres.begin(), r.pres.end(), [&](int i, int j) { return tmp[i] > tmp[j]; });
+  r.shift1 = rank1 - r1 + max1;
+  r.shift2 = rank2 - max2;
+  r.shiftres = r1 - max1 - rankres;
+  return r;
+}
+
+Tensor contract(const Tensor& a, const Tensor& b, const std::vector<int>& a1, const std::vector<int>& a2, int rankres) {
+  // Tensor::contract (Tensor.hpp:328-351): permute, operator*, permute
+  ContractPerms cp = get_permutations(a1, a.meta->rank(), a2, b.meta->rank(), rankres);
+  Tensor l = permute(a, cp.shift1, cp.p1);
+  Tensor r = permute(b, cp.shift2, cp.p2);
+  return permute(matmul(l, r), cp.shiftres, cp.pres);
+}
+
+// ======================================================================= scalar ops
+Tensor scale(const Tensor& t0, double s) {
+  Tensor t = materialize(t0);
+  Tensor out = empty_like_meta(t.meta);
+  if (t.size()) {
+    cuda_ok(cudaMemcpyAsync(out.data(), t.data(), sizeof(double) * t.size(), cudaMemcpyDeviceToDevice, stream()), "copy");
+    launch_scale(out.data(), t.size(), s, stream());
+  }
+  return out;
+}
+
+double max_norm(const Tensor& t) {
+  // TensorBase::maxNorm (TensorBase.cpp:48-56); twists do not change |x|
+  double* sc = scalar_scratch();
+  launch_absmax(t.data(), t.size(), sc, stream());
+  double h = 0;
+  cuda_ok(cudaMemcpyAsync(&h, sc, sizeof(double), cudaMemcpyDeviceToHost, stream()), "d2h");
+  cuda_ok(cudaStreamSynchronize(stream()), "sync");
+  return h;
+}
+
+Tensor normalize_max(const Tensor& t0) {
+  // T * (1. / T.maxNorm()) entirely on the device (CTM.cpp:1372,1383,1405)
+  Tensor t = materialize(t0);
+  Tensor out;
+  if (t.buf.use_count() == 1) {
+    out = t;
+  } else {
+    out = empty_like_meta(t.meta);
+    if (t.size())
+      cuda_ok(cudaMemcpyAsync(out.data(), t.data(), sizeof(double) * t.size(), cudaMemcpyDeviceToDevice, stream()), "copy");
+  }
+  double* sc = scalar_scratch();
+  prof_begin(K_ABSMAX, stream());
+  launch_absmax(out.data(), out.size(), sc, stream());
+  prof_end(K_ABSMAX, stream(), 8.0 * out.size());
+  prof_begin(K_SCALE, stream());
+  launch_scale_by_inv(out.data(), out.size(), sc, stream());
+  prof_end(K_SCALE, stream(), 16.0 * out.size());
+  return out;
+}
+
+Tensor identity(const Sym& s, const std::vector<BasisPtr>& dom, const std::vector<BasisPtr>& cod) {
+  // Tensor::Identity / setIdentity: ones on each block's main diagonal
+  MetaPtr m = make_meta(s, dom, cod);
+  Tensor t = zeros(m);
+  std::vector<double> ones;
+  std::vector<xgb_copy2d_desc> descs;
+  int64_t mx = 0;
+  for (size_t i = 0; i < m->sectors.size(); ++i) {
+    int64_t k = std::min(m->rows[i], m->cols[i]);
+    if (!k) continue;
+    xgb_copy2d_desc d{};
+    d.src_off = int64_t(ones.size());
+    d.src_ld = 1;
+    d.dst_off = m->offset[i];
+    d.dst_ld = m->rows[i] + 1;  // walk the diagonal
+    d.rows = 1;
+    d.cols = k;
+    descs.push_back(d);
+    ones.insert(ones.end(), size_t(k), 1.0);
+    mx = std::max(mx, k);
+  }
+  if (!descs.empty()) {
+    double* dones = static_cast<double*>(dev_alloc(sizeof(double) * ones.size()));
+    auto* dd = static_cast<xgb_copy2d_desc*>(dev_alloc(sizeof(xgb_copy2d_desc) * descs.size()));
+    cuda_ok(cudaMemcpyAsync(dones, ones.data(), sizeof(double) * ones.size(), cudaMemcpyHostToDevice, stream()), "h2d");
+    cuda_ok(cudaMemcpyAsync(dd, descs.data(), sizeof(xgb_copy2d_desc) * descs.size(), cudaMemcpyHostToDevice, stream()), "h2d");
+    launch_copy2d(dd, int(descs.size()), mx, dones, t.data(), stream());
+    cuda_ok(cudaStreamSynchronize(stream()), "sync");
+    dev_free(dones);
+    dev_free(dd);
+  }
+  return t;
+}
+
+// ======================================================================= SVD / truncation
+namespace {
+struct SvdPlan {
+  int n = 0;
+  int64_t u_total = 0, s_total = 0, v_total = 0, work_total = 0, maxk = 0;
+  std::vector<int64_t> s_begin;  // per sector prefix (host), size n+1
+  std::vector<int64_t> u_off, s_off, v_off, kfull;
+  xgb_svd_desc* d_descs = nullptr;
+  int64_t* d_work_off = nullptr;
+  int64_t* d_s_begin = nullptr;
+  int32_t* d_deg = nullptr;
+};
+std::unordered_map<uint64_t, std::shared_ptr<SvdPlan>> g_svd_plans;
+int32_t* g_keep_host = nullptr;  // pinned
+double* g_out2_host = nullptr;
+int g_keep_cap = 0;
+
+std::shared_ptr<SvdPlan> get_svd_plan(const TensorMeta& m) {
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    auto it = g_svd_plans.find(m.id);
+    if (it != g_svd_plans.end()) return it->second;
+  }
+  auto p = std::make_shared<SvdPlan>();
+  p->n = int(m.sectors.size());
+  std::vector<xgb_svd_desc> descs;
+  std::vector<int64_t> woff;
+  std::vector<int32_t> deg;
+  p->s_begin.push_back(0);
+  for (int i = 0; i < p->n; ++i) {
+    int64_t r = m.rows[i], c = m.cols[i], k = std::min(r, c);
+    xgb_svd_desc d{};
+    d.m = r; d.n = c; d.a_off = m.offset[i];
+    d.u_off = p->u_total; d.s_off = p->s_total; d.vt_off = p->v_total;
+    p->u_off.push_back(p->u_total); p->s_off.push_back(p->s_total); p->v_off.push_back(p->v_total); p->kfull.push_back(k);
+    p->u_total += r * k; p->s_total += k; p->v_total += k * c;
+    woff.push_back(p->work_total);
+    p->work_total += int64_t(svd_work_elems(r, c));
+    p->maxk = std::max(p->maxk, k);
+    descs.push_back(d);
+    deg.push_back(m.sym.deg(m.sectors[i]));
+    p->s_begin.push_back(p->s_total);
+  }
+  if (p->maxk > 8192) throw std::runtime_error("tSVD: sector block larger than 8192 columns");
+  p->d_descs = dev_table(descs);
+  p->d_work_off = dev_table(woff);
+  p->d_s_begin = dev_table(p->s_begin);
+  p->d_deg = dev_table(deg);
+  std::lock_guard<std::mutex> lk(g_plan_mu);
+  g_svd_plans[m.id] = p;
+  return p;
+}
+}  // namespace
+
+SVDResult tsvd(const Tensor& t0, int64_t max_keep, double eps_svd, bool preserve_multiplets) {
+  // Tensor::tSVD = full_svd_impl + cutoff_matrices (Tensor.cpp:478-633)
+  Tensor t = materialize(t0);
+  const TensorMeta& m = *t.meta;
+  if (m.sectors.empty()) throw std::runtime_error("tSVD of a tensor without sectors");
+  auto plan = get_svd_plan(m);
+  cudaStream_t st = stream();
+  double* U = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->u_total, 1)));
+  double* S = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->s_total, 1)));
+  double* V = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->v_total, 1)));
+  double* W = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->work_total, 1)));
+  prof_begin(K_SVD, st);
+  launch_svd(plan->d_descs, plan->d_work_off, plan->n, plan->maxk, t.data(), U, S, V, W, st);
+  prof_end(K_SVD, st, 8.0 * double(m.size + plan->u_total + plan->s_total + plan->v_total));
+  dev_free(W);
+  if (plan->s_total == 0) throw std::runtime_error("tSVD: no singular values");
+  int32_t* keep_d = static_cast<int32_t*>(dev_alloc(sizeof(int32_t) * plan->n));
+  double* out2_d = scalar_scratch() + 8;
+  prof_begin(K_TRUNC, st);
+  launch_truncate(plan->n, plan->d_s_begin, plan->d_deg, S, plan->s_total, max_keep, eps_svd, preserve_multiplets ? 1 : 0,
+                  keep_d, out2_d, st);
+  prof_end(K_TRUNC, st, 8.0 * double(plan->s_total));
+  if (g_keep_cap < plan->n) {
+    if (g_keep_host) cudaFreeHost(g_keep_host);
+    cuda_ok(cudaMallocHost(&g_keep_host, sizeof(int32_t) * plan->n), "pinned");
+    g_keep_cap = plan->n;
+    if (!g_out2_host) cuda_ok(cudaMallocHost(&g_out2_host, sizeof(double) * 2), "pinned");
+  }
+  cuda_ok(cudaMemcpyAsync(g_keep_host, keep_d, sizeof(int32_t) * plan->n, cudaMemcpyDeviceToHost, st), "d2h");
+  cuda_ok(cudaMemcpyAsync(g_out2_host, out2_d, sizeof(double) * 2, cudaMemcpyDeviceToHost, st), "d2h");
+  cuda_ok(cudaStreamSynchronize(st), "sync");
+  dev_free(keep_d);
+
+  SVDResult res;
+  res.trunc_weight = g_out2_host[0];
+  res.entropy = g_out2_host[1];
+  res.keep.assign(g_keep_host, g_keep_host + plan->n);
+  // truncated basis: charges with kept values in ascending order (std::map, Tensor.cpp:592-598)
+  std::vector<std::pair<int, int>> kept;  // (q, sector index)
+  for (int i = 0; i < plan->n; ++i)
+    if (res.keep[i] > 0) kept.push_back({m.sectors[i], i});
+  std::sort(kept.begin(), kept.end());
+  std::vector<std::pair<int, int64_t>> pairs;
+  std::vector<int> qs;
+  for (auto& [q, i] : kept) { pairs.push_back({q, res.keep[i]}); qs.push_back(q); }
+  BasisPtr trunc = basis_from_pairs(m.sym, pairs, false);
+  MetaPtr mu = make_meta_ordered(m.sym, m.dom, {trunc}, qs);
+  MetaPtr ms = make_meta_ordered(m.sym, {trunc}, {trunc}, qs);
+  MetaPtr mv = make_meta_ordered(m.sym, {trunc}, m.cod, qs);
+  res.U = empty_like_meta(mu);
+  res.S = empty_like_meta(ms);
+  res.Vdag = empty_like_meta(mv);
+  std::vector<xgb_copy2d_desc> du, dv, ds;
+  int64_t mxu = 0, mxv = 0, mxs = 0;
+  for (size_t a = 0; a < kept.size(); ++a) {
+    const int i = kept[a].second;
+    const int64_t k = res.keep[i], r = m.rows[i], c = m.cols[i], kf = plan->kfull[i];
+    du.push_back({plan->u_off[i], r, mu->offset[a], r, r, k});
+    dv.push_back({plan->v_off[i], kf, mv->offset[a], k, k, c});
+    ds.push_back({plan->s_off[i], 1, ms->offset[a], k, k, k});
+    mxu = std::max(mxu, r * k);
+    mxv = std::max(mxv, k * c);
+    mxs = std::max(mxs, k);
+  }
+  const size_t nb = du.size();
+  auto* dd = static_cast<xgb_copy2d_desc*>(dev_alloc(sizeof(xgb_copy2d_desc) * 3 * std::max<size_t>(nb, 1)));
+  std::vector<xgb_copy2d_desc> all;
+  all.insert(all.end(), du.begin(), du.end());
+  all.insert(all.end(), dv.begin(), dv.end());
+  all.insert(all.end(), ds.begin(), ds.end());
+  cuda_ok(cudaMemcpyAsync(dd, all.data(), sizeof(xgb_copy2d_desc) * all.size(), cudaMemcpyHostToDevice, st), "h2d");
+  prof_begin(K_COPY2D, st);
+  launch_copy2d(dd, int(nb), mxu, U, res.U.data(), st);
+  launch_copy2d(dd + nb, int(nb), mxv, V, res.Vdag.data(), st);
+  launch_diag_from_vec(dd + 2 * nb, int(nb), mxs, -1, S, res.S.data(), st);
+  prof_end(K_COPY2D, st, 16.0 * double(res.U.size() + res.Vdag.size() + res.S.size()));
+  cuda_ok(cudaStreamSynchronize(st), "sync");  // descriptors are pageable host memory
+  dev_free(dd);
+  dev_free(U);
+  dev_free(S);
+  dev_free(V);
+  return res;
+}
+
+std::pair<Tensor, Tensor> tqr(const Tensor& t0) {
+  // Tensor::tQR (Tensor.cpp:757-780): middle basis = coupled codomain when
+  // the domain is larger, else the coupled domain (forgetHistory).
+  Tensor t = materialize(t0);
+  const TensorMeta& m = *t.meta;
+  BasisPtr middle = (m.cdom->dim() > m.ccod->dim()) ? basis_forget_history(m.ccod) : basis_forget_history(m.cdom);
+  MetaPtr mq = make_meta_ordered(m.sym, m.dom, {middle}, m.sectors);
+  MetaPtr mr = make_meta_ordered(m.sym, {middle}, m.cod, m.sectors);
+  Tensor Q = empty_like_meta(mq), R = empty_like_meta(mr);
+  std::vector<xgb_qr_desc> descs;
+  std::vector<int64_t> woff;
+  int64_t wt = 0;
+  for (size_t i = 0; i < m.sectors.size(); ++i) {
+    xgb_qr_desc d{};
+    d.m = m.rows[i]; d.n = m.cols[i]; d.a_off = m.offset[i];
+    d.q_off = mq->offset[i]; d.q_cols = mq->cols[i];
+    d.r_off = mr->offset[i]; d.r_rows = mr->rows[i];
+    descs.push_back(d);
+    woff.push_back(wt);
+    wt += int64_t(qr_work_elems(d.m, d.n));
+  }
+  if (!descs.empty()) {
+    cudaStream_t st = stream();
+    auto* dd = static_cast<xgb_qr_desc*>(dev_alloc(sizeof(xgb_qr_desc) * descs.size()));
+    auto* dw = static_cast<int64_t*>(dev_alloc(sizeof(int64_t) * woff.size()));
+    double* W = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(wt, 1)));
+    cuda_ok(cudaMemcpyAsync(dd, descs.data(), sizeof(xgb_qr_desc) * descs.size(), cudaMemcpyHostToDevice, st), "h2d");
+    cuda_ok(cudaMemcpyAsync(dw, woff.data(), sizeof(int64_t) * woff.size(), cudaMemcpyHostToDevice, st), "h2d");
+    launch_qr(dd, dw, int(descs.size()), t.data(), Q.data(), R.data(), W, st);
+    cuda_ok(cudaStreamSynchronize(st), "sync");
+    dev_free(dd);
+    dev_free(dw);
+    dev_free(W);
+  }
+  return {Q, R};
+}
+
+std::pair<Tensor, Tensor> decompose(const Tensor& t1, const Tensor& t2, int64_t max_nsv) {
+  // decompose (src/PEPS/PEPSContractions.cpp:16-43)
+  Tensor prod = matmul(t1, t2);
+  SVDResult r = tsvd(prod, max_nsv, 1.0e-10, false);
+  // isqrtS = S.diag_sqrt().diag_inv(): 1/sqrt(s) on the diagonal
+  Tensor isq = empty_like_meta(r.S.meta);
+  {
+    const TensorMeta& ms = *r.S.meta;
+    std::vector<xgb_copy2d_desc> descs;
+    int64_t mx = 0;
+    for (size_t i = 0; i < ms.sectors.size(); ++i) {
+      descs.push_back({ms.offset[i], ms.rows[i], ms.offset[i], ms.rows[i], ms.rows[i], ms.cols[i]});
+      mx = std::max(mx, std::max(ms.rows[i], ms.cols[i]));
+    }
+    cuda_ok(cudaMemcpyAsync(isq.data(), r.S.data(), sizeof(double) * ms.size, cudaMemcpyDeviceToDevice, stream()), "copy");
+    auto* dd = static_cast<xgb_copy2d_desc*>(dev_alloc(sizeof(xgb_copy2d_desc) * std::max<size_t>(descs.size(), 1)));
+    cuda_ok(cudaMemcpyAsync(dd, descs.data(), sizeof(xgb_copy2d_desc) * descs.size(), cudaMemcpyHostToDevice, stream()), "h2d");
+    launch_diag_apply(dd, int(descs.size()), mx, XGB_DIAG_SQRT, isq.data(), stream());
+    launch_diag_apply(dd, int(descs.size()), mx, XGB_DIAG_INV, isq.data(), stream());
+    cuda_ok(cudaStreamSynchronize(stream()), "sync");
+    dev_free(dd);
+  }
+  Tensor P1 = matmul(matmul(isq, r.U, false, true), t1);      // isqrtS * U.adjoint() * T1
+  Tensor P2 = matmul(matmul(t2, r.Vdag, false, true), isq);   // T2 * Vdag.adjoint() * isqrtS
+  return {P1, P2};
+}
+
+// ======================================================================= CTM
+static Tensor tw(const Tensor& t, std::initializer_list<int> legs) {
+  Tensor o = t;
+  for (int l : legs) o = twist(o, l);
+  return o;
+}
+
+CTM::CTM(const Tensor& A_, int64_t chi_) : chi(chi_), A(materialize(A_)) {
+  if (A.meta->rank() != 2 || A.meta->corank() != 3) throw std::runtime_error("CTM: site tensor must be Tensor<2,3>");
+  // Adags = As.adjoint().eval().permute<0, 3, 4, 2, 0, 1>()  (src/PEPS/iPEPS.cpp:210)
+  Ad = permute(adjoint(A), 0, {3, 4, 2, 0, 1});
+}
+
+Tensor& CTM::slot(int which) {
+  switch (which) {
+    case 0: return C1; case 1: return C2; case 2: return C3; case 3: return C4;
+    case 4: return T1; case 5: return T2; case 6: return T3; case 7: return T4;
+    case 8: return A; default: return Ad;
+  }
+}
+
+void CTM::init() {
+  // CTM::init, FROM_A, TRank == 2, not ALL_OUT_LEGS (src/PEPS/CTM.cpp:161-212)
+  const Sym s = A.meta->sym;
+  auto ket = [&](char l) -> BasisPtr {
+    switch (l) { case 'L': return A.meta->dom[0]; case 'T': return A.meta->dom[1]; case 'R': return A.meta->cod[0];
+      case 'B': return A.meta->cod[1]; default: return A.meta->cod[2]; }
+  };
+  auto bra = [&](char l) -> BasisPtr {
+    switch (l) { case 'L': return Ad.meta->dom[0]; case 'T': return Ad.meta->dom[1]; case 'R': return Ad.meta->cod[0];
+      case 'B': return Ad.meta->cod[1]; default: return Ad.meta->dom[2]; }
+  };
+  auto fused = [&](char l) { return basis_forget_history(basis_combine(ket(l), bra(l))); };
+  Tensor fuse_ll = identity(s, {fused('L')}, {ket('L'), bra('L')});
+  Tensor fuse_uu = identity(s, {fused('T')}, {ket('T'), bra('T')});
+  Tensor fuse_rr = identity(s, {ket('R'), bra('R')}, {fused('R')});
+  Tensor fuse_dd = identity(s, {ket('B'), bra('B')}, {fused('B')});
+  C1 = contract(contract(contract(A, tw(Ad, {3, 4}), {1, 2, -1, -2, 3}, {1, 2, 3, -3, -4}, 2), fuse_rr, {1, -1, 2, -2}, {1, 2, -3}, 2),
+                fuse_dd, {1, 2, -2}, {1, 2, -1}, 0);
+  C2 = contract(contract(contract(A, tw(Ad, {4}), {-1, 1, 2, -2, 3}, {-3, 1, 3, 2, -4}, 2), tw(fuse_ll, {1, 2}), {1, -1, 2, -2},
+                         {-3, 1, 2}, 2),
+                fuse_dd, {1, 2, -1}, {1, 2, -2}, 1);
+  C3 = contract(contract(contract(A, Ad, {-1, -2, 1, 2, 3}, {-3, -4, 3, 1, 2}, 2), tw(fuse_ll, {1, 2}), {1, -1, 2, -2}, {-3, 1, 2}, 2),
+                tw(fuse_uu, {1, 2}), {1, 2, -2}, {-1, 1, 2}, 2);
+  C4 = contract(contract(contract(A, tw(Ad, {3}), {1, -1, -2, 2, 3}, {1, -3, 3, -4, 2}, 2), tw(fuse_uu, {1, 2}), {1, -1, 2, -2},
+                         {-3, 1, 2}, 2),
+                fuse_rr, {1, 2, -1}, {1, 2, -2}, 1);
+  T1 = contract(contract(contract(A, tw(Ad, {3, 4}), {-1, 1, -2, -3, 2}, {-4, 1, 2, -5, -6}, 3), tw(fuse_ll, {1, 2}),
+                         {1, -1, -2, 2, -3, -4}, {-5, 1, 2}, 4),
+                fuse_rr, {1, -3, 2, -4, -1}, {1, 2, -2}, 1);
+  T2 = contract(contract(contract(A, tw(Ad, {4}), {-1, -2, 1, -3, 2}, {-4, -5, 2, 1, -6}, 3), tw(fuse_uu, {1, 2}),
+                         {-1, 1, -2, -3, 2, -4}, {-5, 1, 2}, 4),
+                fuse_dd, {-1, 1, -2, 2, -3}, {1, 2, -4}, 3);
+  T3 = contract(contract(contract(A, tw(Ad, {3}), {-1, -2, -3, 1, 2}, {-4, -5, 2, -6, 1}, 3), tw(fuse_ll, {1, 2}),
+                         {1, -1, -2, 2, -3, -4}, {-5, 1, 2}, 4),
+                fuse_rr, {-1, 1, -2, 2, -3}, {1, 2, -4}, 3);
+  T4 = contract(contract(contract(A, tw(Ad, {3, 4}), {1, -1, -2, -3, 2}, {1, -4, 2, -5, -6}, 3), tw(fuse_uu, {1, 2}),
+                         {1, -1, -2, 2, -3, -4}, {-5, 1, 2}, 4),
+                fuse_dd, {-3, 1, -4, 2, -1}, {1, 2, -2}, 1);
+}
+
+Tensor CTM::contract_corner(const char* corner) {
+  // contractCorner, TRank == 2 (src/PEPS/CTM.cpp:1667-1738)
+  const std::string c(corner);
+  if (c == "UL") {
+    Tensor C1T1 = contract(C1, T1, {-1, 1}, {1, -2, -3, -4}, 1);
+    Tensor T4C1T1 = contract(T4, tw(C1T1, {0}), {1, -1, -2, -3}, {1, -4, -5, -6}, 3);
+    Tensor T4C1T1A = contract(T4C1T1, A, {-1, 1, -2, -3, 2, -4}, {1, 2, -5, -6, -7}, 4);
+    return contract(T4C1T1A, tw(Ad, {3, 4}), {-1, 1, -4, 2, -5, -2, 3}, {1, 2, 3, -6, -3}, 3);
+  }
+  if (c == "LL") {
+    Tensor C4T3 = contract(C4, T3, {-1, 1}, {-2, -3, 1, -4}, 1);
+    Tensor T4C4T3 = contract(T4, C4T3, {-1, 1, -2, -3}, {1, -4, -5, -6}, 3);
+    Tensor T4C4T3A = contract(T4C4T3, tw(A, {3}), {-1, 1, -2, 2, -3, -4}, {1, -5, -6, 2, -7}, 4);
+    return contract(T4C4T3A, tw(Ad, {3}), {-4, 1, 2, -1, -5, -2, 3}, {1, -6, 3, -3, 2}, 3);
+  }
+  if (c == "UR") {
+    Tensor T1C2 = contract(T1, C2, {-1, 1, -2, -3}, {1, -4}, 3);
+    Tensor T1C2T2 = contract(T1C2, T2, {-1, -2, -3, 1}, {-4, -5, 1, -6}, 3);
+    Tensor T1C2T2A = contract(T1C2T2, tw(A, {2}), {-1, 1, -2, 2, -3, -4}, {-5, 1, 2, -6, -7}, 4);
+    return contract(T1C2T2A, tw(Ad, {4}), {-1, 1, 2, -4, -2, -5, 3}, {-3, 1, 3, 2, -6}, 3);
+  }
+  if (c == "LR") {
+    Tensor C3T3 = contract(tw(C3, {1}), T3, {-1, 1}, {-2, -3, -4, 1}, 1);
+    Tensor T2C3T3 = contract(T2, C3T3, {-1, -2, -3, 1}, {1, -4, -5, -6}, 3);
+    Tensor T2C3T3A = contract(T2C3T3, tw(A, {2, 3}), {1, -1, -2, 2, -3, -4}, {-5, -6, 1, 2, -7}, 4);
+    return contract(T2C3T3A, Ad, {1, -1, 2, -4, -5, -2, 3}, {-6, -3, 3, 1, 2}, 3);
+  }
+  throw std::runtime_error("contract_corner: unknown corner");
+}
+
+std::pair<Tensor, Tensor> CTM::get_projectors(char dir) {
+  // get_projectors, PROJECTION::CORNER (src/PEPS/CTM.cpp:1195-1326)
+  switch (dir) {
+    case 'L': {
+      Tensor Q1 = contract_corner("UL");
+      Tensor Q4 = tw(contract_corner("LL"), {3, 4, 5});
+      return decompose(Q4, Q1, chi);
+    }
+    case 'R': {
+      Tensor Q2 = contract_corner("UR");
+      Tensor Q3 = contract_corner("LR");
+      return decompose(Q2, Q3, chi);
+    }
+    case 'T': {
+      Tensor Q1 = contract_corner("UL");
+      Tensor Q2 = contract_corner("UR");
+      return decompose(Q1, Q2, chi);
+    }
+    default: {
+      Tensor Q4 = tw(contract_corner("LL"), {0, 1, 2});
+      Tensor Q3 = contract_corner("LR");
+      return decompose(Q3, Q4, chi);
+    }
+  }
+}
+
+std::tuple<Tensor, Tensor, Tensor> CTM::renormalize(char dir, const Tensor& P1, const Tensor& P2) {
+  // renormalize_left/right/top/bottom, TRank == 2 (src/PEPS/CTM.cpp:1358-1627)
+  if (dir == 'L') {
+    Tensor C1T1 = contract(C1, T1, {-1, 1}, {1, -4, -2, -3}, 3);
+    Tensor C1n = contract(tw(P1, {1, 2, 3}), C1T1, {-1, 1, 2, 3}, {1, 2, 3, -2}, 0);
+    Tensor C4T3 = contract(C4, T3, {-2, 1}, {-3, -4, 1, -1}, 1);
+    Tensor C4n = contract(C4T3, tw(P2, {0, 1, 2}), {-2, 1, 2, 3}, {1, 2, 3, -1}, 1);
+    Tensor P1T4 = contract(tw(P1, {1, 2, 3}), T4, {-1, 1, -2, -3}, {-4, 1, -5, -6}, 3);
+    Tensor P1T4A = contract(P1T4, A, {-1, 2, -2, -3, 1, -4}, {1, -5, -6, 2, -7}, 4);
+    Tensor P1T4AAd = contract(P1T4A, tw(Ad, {3, 4}), {-1, 2, -4, 1, -5, -2, 3}, {1, -6, 3, -3, 2}, 3);
+    Tensor T4n = contract(P1T4AAd, tw(P2, {0, 1, 2}), {-2, -3, -4, 1, 2, 3}, {1, 2, 3, -1}, 1);
+    return {normalize_max(C1n), normalize_max(T4n), normalize_max(C4n)};
+  }
+  if (dir == 'R') {
+    Tensor T1C2 = contract(T1, C2, {-1, 1, -3, -4}, {1, -2}, 1);
+    Tensor C2n = contract(T1C2, P2, {-1, 1, 2, 3}, {1, 2, 3, -2}, 1);
+    Tensor C3T3 = contract(tw(C3, {1}), T3, {-1, 1}, {-2, -3, -4, 1}, 3);
+    Tensor C3n = contract(P1, C3T3, {-1, 1, 2, 3}, {1, 2, 3, -2}, 2);
+    Tensor P1T2 = contract(P1, T2, {-1, 1, -2, -3}, {-4, -5, 1, -6}, 3);
+    Tensor P1T2A = contract(P1T2, tw(A, {2}), {-1, 1, -2, 2, -3, -4}, {-5, 1, 2, -6, -7}, 4);
+    Tensor P1T2AAd = contract(P1T2A, tw(Ad, {4}), {-1, 1, 2, -4, -2, -5, 3}, {-3, 1, 3, 2, -6}, 3);
+    Tensor T2n = contract(P1T2AAd, P2, {-3, -1, -2, 1, 2, 3}, {1, 2, 3, -4}, 3);
+    return {normalize_max(C2n), normalize_max(T2n), normalize_max(C3n)};
+  }
+  if (dir == 'T') {
+    Tensor T4C1 = contract(T4, tw(C1, {0}), {1, -1, -3, -4}, {1, -2}, 1);
+    Tensor C1n = contract(T4C1, P2, {-1, 1, 2, 3}, {1, 2, 3, -2}, 0);
+    Tensor C2T2 = contract(C2, T2, {-1, 1}, {-2, -3, 1, -4}, 3);
+    Tensor C2n = contract(P1, C2T2, {-1, 1, 2, 3}, {1, 2, 3, -2}, 1);
+    Tensor P1T1 = contract(P1, T1, {-1, 1, -2, -3}, {1, -4, -5, -6}, 3);
+    Tensor P1T1A = contract(P1T1, A, {-1, 1, -2, -3, 2, -4}, {1, 2, -5, -6, -7}, 4);
+    Tensor P1T1AAd = contract(P1T1A, tw(Ad, {3, 4}), {-1, 1, -4, 2, -5, -2, 3}, {1, 2, 3, -6, -3}, 3);
+    Tensor T1n = contract(P1T1AAd, P2, {-1, -3, -4, 1, 2, 3}, {1, 2, 3, -2}, 1);
+    return {normalize_max(C1n), normalize_max(T1n), normalize_max(C2n)};
+  }
+  Tensor T4C4 = contract(T4, C4, {-4, 1, -2, -3}, {1, -1}, 3);
+  Tensor C4n = contract(tw(P1, {1, 2, 3}), T4C4, {-2, 1, 2, 3}, {1, 2, 3, -1}, 1);
+  Tensor T2C3 = contract(T2, C3, {-3, -4, -1, 1}, {1, -2}, 1);
+  Tensor C3n = contract(T2C3, tw(P2, {0, 1, 2}), {-1, 1, 2, 3}, {1, 2, 3, -2}, 2);
+  Tensor P1T3 = contract(tw(P1, {1, 2, 3}), tw(T3, {0}), {-1, 1, -2, -3}, {-4, -5, -6, 1}, 3);
+  Tensor P1T3A = contract(P1T3, A, {-1, 1, -2, 2, -3, -4}, {-5, -6, 1, 2, -7}, 4);
+  Tensor P1T3AAd = contract(P1T3A, tw(Ad, {3}), {-1, 1, 2, -4, -5, -2, 3}, {-6, -3, 3, 1, 2}, 3);
+  Tensor T3n = contract(P1T3AAd, tw(P2, {0, 1, 2}), {-4, -1, -2, 1, 2, 3}, {1, 2, 3, -3}, 3);
+  return {normalize_max(C4n), normalize_max(T3n), normalize_max(C3n)};
+}
+
+void CTM::move(char dir) {
+  auto [P1, P2] = get_projectors(dir);
+  auto [a, b, c] = renormalize(dir, P1, P2);
+  switch (dir) {
+    case 'L': C1 = a; T4 = b; C4 = c; break;
+    case 'R': C2 = a; T2 = b; C3 = c; break;
+    case 'T': C1 = a; T1 = b; C2 = c; break;
+    default: C4 = a; T3 = b; C3 = c; break;
+  }
+}
+
+void CTM::grow_all() {
+  // CTM::grow_all (src/PEPS/CTM.cpp:385-398)
+  move('L');
+  move('R');
+  move('T');
+  move('B');
+}
+
+}  // namespace xgb

@@ -1,0 +1,308 @@
+"""Python mirror of Xped's Tensor interface over the native GB300 backend.
+
+Every operation is one call through the C-ABI (include/xgb_tensor.h); the
+data stays in HBM.  Names and argument meaning follow the reference
+(include/Xped/Core/Tensor.hpp): ``permute(shift, p)``, ``twist(leg)``,
+``contract(other, a1, a2, rankres)``, ``tSVD(maxKeep, eps)``, ``tQR()``,
+``maxNorm()``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, List, Sequence, Tuple
+
+import numpy as np
+
+from ._lib import (PermContrib, PermTask, GemmDesc, check, check_handle, ensure_device, lib)
+
+SYM_IDS = {"U1": 0, "fU1": 1, "Z2": 2, "fZ2": 3, "SU2": 4}
+
+
+def _i32(seq):
+    arr = (C.c_int32 * max(len(seq), 1))(*seq)
+    return arr
+
+
+def _i64(seq):
+    return (C.c_int64 * max(len(seq), 1))(*seq)
+
+
+class Basis:
+    """Qbasis<Symmetry, depth> (include/Xped/Core/Qbasis.hpp)."""
+
+    def __init__(self, handle):
+        self._h = check_handle(handle, "basis")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().xgb_basis_release(h)
+            self._h = None
+
+    @classmethod
+    def from_pairs(cls, sym: str, pairs: Sequence[Tuple[int, int]], sort: bool = True) -> "Basis":
+        qs = [int(q) for q, _ in pairs]
+        ds = [int(d) for _, d in pairs]
+        return cls(lib().xgb_basis_create(SYM_IDS[sym], len(qs), _i32(qs), _i64(ds), 1 if sort else 0))
+
+    def conj(self) -> "Basis":
+        return Basis(lib().xgb_basis_conj(self._h))
+
+    def combine(self, other: "Basis") -> "Basis":
+        return Basis(lib().xgb_basis_combine(self._h, other._h))
+
+    def forget_history(self) -> "Basis":
+        return Basis(lib().xgb_basis_forget_history(self._h))
+
+    def info(self):
+        n = lib().xgb_basis_info(self._h, None, None, None, None)
+        qs = (C.c_int32 * max(n, 1))()
+        ds = (C.c_int64 * max(n, 1))()
+        cj = C.c_int()
+        dp = C.c_int()
+        lib().xgb_basis_info(self._h, qs, ds, C.byref(cj), C.byref(dp))
+        return list(qs[:n]), list(ds[:n]), bool(cj.value), dp.value
+
+    @property
+    def qs(self):
+        return self.info()[0]
+
+    @property
+    def dims(self):
+        return self.info()[1]
+
+    def trees(self, i: int):
+        """Fusion trees of irrep index i as tuples (qu, qi, qc, dims, dual_mask)."""
+        need = check(lib().xgb_basis_trees(self._h, i, None, 0), "basis_trees")
+        buf = (C.c_int64 * max(need, 1))()
+        n = check(lib().xgb_basis_trees(self._h, i, buf, need), "basis_trees")
+        out, k = [], 0
+        for _ in range(n):
+            r, qc, dual = buf[k], buf[k + 1], buf[k + 2]
+            k += 3
+            qu = tuple(buf[k:k + r]); k += r
+            dims = tuple(buf[k:k + r]); k += r
+            nqi = max(r - 2, 0)
+            qi = tuple(buf[k:k + nqi]); k += nqi
+            out.append((qu, qi, qc, dims, dual))
+        return out
+
+
+def _handles(bases):
+    arr = (C.c_void_p * max(len(bases), 1))(*[b._h for b in bases])
+    return arr
+
+
+class Tensor:
+    """Tensor<double, Rank, CoRank, Symmetry> with device-resident blocks."""
+
+    def __init__(self, handle):
+        self._h = check_handle(handle, "tensor")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().xgb_tensor_release(h)
+            self._h = None
+
+    # -- construction ---------------------------------------------------------
+    @classmethod
+    def zeros(cls, dom: List[Basis], cod: List[Basis]) -> "Tensor":
+        ensure_device()
+        return cls(lib().xgb_tensor_zeros(len(dom), _handles(dom), len(cod), _handles(cod)))
+
+    @classmethod
+    def identity(cls, dom: List[Basis], cod: List[Basis]) -> "Tensor":
+        ensure_device()
+        return cls(lib().xgb_tensor_identity(len(dom), _handles(dom), len(cod), _handles(cod)))
+
+    @classmethod
+    def meta(cls, dom: List[Basis], cod: List[Basis]) -> "Tensor":
+        """Metadata only, no device memory (usable without a GPU)."""
+        return cls(lib().xgb_tensor_meta(len(dom), _handles(dom), len(cod), _handles(cod)))
+
+    @classmethod
+    def from_blocks(cls, dom, cod, blocks: Dict[int, np.ndarray]) -> "Tensor":
+        t = cls.zeros(dom, cod)
+        t.set_blocks(blocks)
+        return t
+
+    # -- metadata ----------------------------------------------------------------
+    def sectors(self):
+        n = lib().xgb_tensor_sectors(self._h, None, None, None)
+        qs = (C.c_int32 * max(n, 1))()
+        rs = (C.c_int64 * max(n, 1))()
+        cs = (C.c_int64 * max(n, 1))()
+        lib().xgb_tensor_sectors(self._h, qs, rs, cs)
+        return list(qs[:n]), list(rs[:n]), list(cs[:n])
+
+    @property
+    def size(self) -> int:
+        return int(lib().xgb_tensor_size(self._h))
+
+    @property
+    def rank(self):
+        r, c = C.c_int(), C.c_int()
+        lib().xgb_tensor_rank(self._h, C.byref(r), C.byref(c))
+        return r.value, c.value
+
+    def leg(self, i) -> Basis:
+        return Basis(lib().xgb_tensor_leg(self._h, i))
+
+    def coupled(self, codomain: bool) -> Basis:
+        return Basis(lib().xgb_tensor_coupled(self._h, 1 if codomain else 0))
+
+    # -- data ------------------------------------------------------------------------
+    def data(self) -> np.ndarray:
+        n = self.size
+        out = np.empty(n, dtype=np.float64)
+        check(lib().xgb_tensor_download(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), n), "download")
+        return out
+
+    def set_data(self, flat: np.ndarray):
+        flat = np.ascontiguousarray(flat, dtype=np.float64)
+        check(lib().xgb_tensor_upload(self._h, flat.ctypes.data_as(C.POINTER(C.c_double)), flat.size), "upload")
+
+    def blocks(self) -> Dict[int, np.ndarray]:
+        qs, rs, cs = self.sectors()
+        flat = self.data()
+        out, off = {}, 0
+        for q, r, c in zip(qs, rs, cs):
+            out[q] = flat[off:off + r * c].reshape((r, c), order="F").copy()
+            off += r * c
+        return out
+
+    def set_blocks(self, blocks: Dict[int, np.ndarray]):
+        qs, rs, cs = self.sectors()
+        parts = []
+        for q, r, c in zip(qs, rs, cs):
+            b = np.asarray(blocks[q], dtype=np.float64)
+            if b.shape != (r, c):
+                raise ValueError(f"block {q}: shape {b.shape} != {(r, c)}")
+            parts.append(b.ravel(order="F"))
+        self.set_data(np.concatenate(parts) if parts else np.zeros(0))
+
+    # -- operations ---------------------------------------------------------------------
+    def permute(self, shift: int, p: Sequence[int]) -> "Tensor":
+        return Tensor(lib().xgb_tensor_permute(self._h, int(shift), _i32(list(p)), len(p)))
+
+    def twist(self, leg: int) -> "Tensor":
+        return Tensor(lib().xgb_tensor_twist(self._h, int(leg)))
+
+    def adjoint(self) -> "Tensor":
+        return Tensor(lib().xgb_tensor_adjoint(self._h))
+
+    def matmul(self, other: "Tensor", adj_a=False, adj_b=False) -> "Tensor":
+        return Tensor(lib().xgb_tensor_matmul(self._h, other._h, int(adj_a), int(adj_b)))
+
+    def __mul__(self, other):
+        if isinstance(other, Tensor):
+            return self.matmul(other)
+        return Tensor(lib().xgb_tensor_scale(self._h, float(other)))
+
+    def contract(self, other: "Tensor", a1: Sequence[int], a2: Sequence[int], rankres: int) -> "Tensor":
+        return Tensor(lib().xgb_tensor_contract(self._h, other._h, _i32(list(a1)), len(a1), _i32(list(a2)), len(a2),
+                                                int(rankres)))
+
+    def maxNorm(self) -> float:
+        v = lib().xgb_tensor_max_norm(self._h)
+        if v < 0:
+            check(-3, "maxNorm")
+        return v
+
+    def normalize_max(self) -> "Tensor":
+        return Tensor(lib().xgb_tensor_normalize_max(self._h))
+
+    def tSVD(self, max_keep: int, eps_svd: float, preserve_multiplets: bool = False):
+        U, S, V = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        tw, ent = C.c_double(), C.c_double()
+        n = len(self.sectors()[0])
+        keep = (C.c_int32 * max(n, 1))()
+        check(lib().xgb_tensor_tsvd(self._h, int(max_keep), float(eps_svd), int(preserve_multiplets), C.byref(U),
+                                    C.byref(S), C.byref(V), C.byref(tw), C.byref(ent), keep), "tSVD")
+        return Tensor(U.value), Tensor(S.value), Tensor(V.value), tw.value, ent.value, list(keep[:n])
+
+    def tQR(self):
+        Q, R = C.c_void_p(), C.c_void_p()
+        check(lib().xgb_tensor_tqr(self._h, C.byref(Q), C.byref(R)), "tQR")
+        return Tensor(Q.value), Tensor(R.value)
+
+    # -- host-only planning -----------------------------------------------------------------
+    def permute_plan(self, shift: int, p: Sequence[int], twist_mask: int = 0):
+        nt, nc = C.c_int(), C.c_int()
+        pp = _i32(list(p))
+        check(lib().xgb_permute_plan_host(self._h, int(shift), pp, len(p), twist_mask, C.byref(nt), C.byref(nc), None,
+                                          0, None, 0, None), "permute_plan")
+        tasks = (PermTask * max(nt.value, 1))()
+        contribs = (PermContrib * max(nc.value, 1))()
+        out = C.c_void_p()
+        check(lib().xgb_permute_plan_host(self._h, int(shift), pp, len(p), twist_mask, C.byref(nt), C.byref(nc), tasks,
+                                          nt.value, contribs, nc.value, C.byref(out)), "permute_plan")
+        return list(tasks[:nt.value]), list(contribs[:nc.value]), Tensor(out.value)
+
+    def gemm_plan(self, other: "Tensor", adj_a=False, adj_b=False):
+        n = C.c_int()
+        check(lib().xgb_gemm_plan_host(self._h, int(adj_a), other._h, int(adj_b), C.byref(n), None, 0, None), "gemm_plan")
+        descs = (GemmDesc * max(n.value, 1))()
+        out = C.c_void_p()
+        check(lib().xgb_gemm_plan_host(self._h, int(adj_a), other._h, int(adj_b), C.byref(n), descs, n.value,
+                                       C.byref(out)), "gemm_plan")
+        return list(descs[:n.value]), Tensor(out.value)
+
+
+def decompose(T1: Tensor, T2: Tensor, max_nsv: int):
+    """decompose (src/PEPS/PEPSContractions.cpp:16-43)."""
+    P1, P2 = C.c_void_p(), C.c_void_p()
+    check(lib().xgb_decompose(T1._h, T2._h, int(max_nsv), C.byref(P1), C.byref(P2)), "decompose")
+    return Tensor(P1.value), Tensor(P2.value)
+
+
+def contract_perms(a1, rank1, a2, rank2, rankres):
+    out = (C.c_int32 * (len(a1) + len(a2) + 16))()
+    nres = check(lib().xgb_contract_perms(_i32(list(a1)), len(a1), rank1, _i32(list(a2)), len(a2), rank2, rankres, out),
+                 "contract_perms")
+    v = list(out)
+    k = 0
+    p1 = v[k:k + len(a1)]; k += len(a1)
+    s1 = v[k]; k += 1
+    p2 = v[k:k + len(a2)]; k += len(a2)
+    s2 = v[k]; k += 1
+    pres = v[k:k + nres]; k += nres
+    sres = v[k]
+    return p1, s1, p2, s2, pres, sres
+
+
+class CTM:
+    """CTM<double, Sym, TRank=2, ALL_OUT_LEGS=false> on a 1x1 unit cell
+    (src/PEPS/CTM.cpp), all tensor work on the GPU."""
+
+    SLOTS = {"C1": 0, "C2": 1, "C3": 2, "C4": 3, "T1": 4, "T2": 5, "T3": 6, "T4": 7, "A": 8, "Adag": 9}
+
+    def __init__(self, A: Tensor, chi: int):
+        self._h = check_handle(lib().xgb_ctm_create(A._h, int(chi)), "ctm_create")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().xgb_ctm_release(h)
+            self._h = None
+
+    def init(self):
+        check(lib().xgb_ctm_init(self._h), "ctm_init")
+        return self
+
+    def grow_all(self):
+        check(lib().xgb_ctm_grow_all(self._h), "grow_all")
+        return self
+
+    def move(self, d: str):
+        check(lib().xgb_ctm_move(self._h, d.encode()), "ctm_move")
+
+    def get(self, name: str) -> Tensor:
+        return Tensor(lib().xgb_ctm_get(self._h, self.SLOTS[name]))
+
+    def set(self, name: str, t: Tensor):
+        check(lib().xgb_ctm_set(self._h, self.SLOTS[name], t._h), "ctm_set")
+
+    def env(self):
+        return {k: self.get(k) for k in ("C1", "C2", "C3", "C4", "T1", "T2", "T3", "T4")}
