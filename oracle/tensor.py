@@ -415,14 +415,39 @@ def matmul(left: Tensor, right: Tensor) -> Tensor:
     return out
 
 
+TIE_RTOL = 1.0e-12
+
+
+def tie_tolerant_order(values):
+    """Global descending order of singular values used for truncation.
+
+    The reference sorts with std::sort (unstable, Tensor.cpp:543-547), so the
+    order of equal values - and hence which of two degenerate values survives
+    the chi cut - is unspecified.  Here the order is made deterministic and
+    insensitive to last-bit differences between LAPACK and the GPU kernel:
+    values are sorted descending, consecutive values within TIE_RTOL
+    (relative) form a tie group, and inside a group entries keep their
+    (sector, index) position order."""
+    n = len(values)
+    exact = sorted(range(n), key=lambda i: (-values[i], i))
+    groups = []
+    for pos, i in enumerate(exact):
+        if pos == 0 or values[exact[pos - 1]] - values[i] > TIE_RTOL * values[exact[pos - 1]]:
+            groups.append([])
+        groups[-1].append(i)
+    out = []
+    for g in groups:
+        out.extend(sorted(g))
+    return out
+
+
 def cutoff_matrices(T, U, S, Vd, allsv, max_keep, eps_svd, preserve_multiplets, return_spec):
     """Tensor::cutoff_matrices (Tensor.cpp:523-633)."""
     sym = T.sym
     n = len(allsv)
     assert n > 0
     first_entry = allsv[0]
-    order = sorted(range(n), key=lambda i: -allsv[i][1])  # stable: ties keep (sector, index) order
-    allsv = [allsv[i] for i in order]
+    allsv = [allsv[i] for i in tie_tolerant_order([v for _, v in allsv])]
     trunc_weight = 0.0
     for i in range(max_keep, len(allsv)):
         trunc_weight += sym.degeneracy(allsv[i][0]) * abs(allsv[i][1]) ** 2

@@ -275,235 +275,103 @@ void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_task_start, i
   count_launch();
 }
 
-// ======================================================================= SVD
-// Batched one-sided (Hestenes) Jacobi SVD in FP64, one CTA per block.  For an
-// m x n block with m >= n the columns of W = A are orthogonalised by plane
-// rotations (accumulated into V); for m < n the same is done on A^T.  Pairs
-// follow the round-robin (circle) ordering, n/2 disjoint rotations per round
-// spread over the warps.  Converged when no pair has
-// |w_p.w_q| > tol*|w_p||w_q|.  Afterwards the singular values are sorted
-// descending (ties by column index) and every pair (u_j, v_j) is sign
-// normalised so that the largest-magnitude entry of u_j is positive.
-constexpr int kSvdThreads = 256;
-constexpr int kSvdMaxSweeps = 60;
-
+// ======================================================================= shared helpers
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
-__device__ __forceinline__ void rr_pair(int round, int k, int N, int& p, int& q) {
-  // circle method over N (even) slots; slot 0 fixed, slots 1..N-1 rotate
-  auto pos = [&](int i) { return (round + i) % (N - 1) + 1; };
-  if (k == 0) { p = 0; q = pos(0); }
-  else { p = pos(k); q = pos(N - 1 - k); }
-}
-
-__global__ void __launch_bounds__(kSvdThreads) svd_jacobi_kernel(const xgb_svd_desc* __restrict__ descs,
-                                                                 const int64_t* __restrict__ work_off,
-                                                                 const double* __restrict__ A, double* __restrict__ U,
-                                                                 double* __restrict__ S, double* __restrict__ Vt,
-                                                                 double* __restrict__ work) {
-  extern __shared__ unsigned char smem_raw[];
-  const xgb_svd_desc d = descs[blockIdx.x];
-  const bool tr = d.m < d.n;
-  const int64_t mm = tr ? d.n : d.m;  // rows of W
-  const int nn = int(tr ? d.m : d.n); // columns of W (= k)
-  if (nn == 0) return;
-  double* W = work + work_off[blockIdx.x];
-  double* V = W + mm * nn;
-  double* sval = reinterpret_cast<double*>(smem_raw);
-  int* order = reinterpret_cast<int*>(sval + nn);
-  __shared__ int rotated;
-
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = kSvdThreads / 32;
-  // W = A or A^T, V = I
-  for (int64_t e = tid; e < mm * nn; e += kSvdThreads) {
-    int64_t i = e % mm, j = e / mm;
-    W[e] = tr ? A[d.a_off + j + i * d.m] : A[d.a_off + i + j * d.m];
-  }
-  for (int64_t e = tid; e < int64_t(nn) * nn; e += kSvdThreads) V[e] = ((e % nn) == (e / nn)) ? 1.0 : 0.0;
-  __syncthreads();
-
-  const double tol = 1.0e-15 * sqrt(double(mm));
-  const int N = nn + (nn & 1);
-  for (int sweep = 0; sweep < kSvdMaxSweeps && nn > 1; ++sweep) {
-    if (tid == 0) rotated = 0;
-    __syncthreads();
-    for (int round = 0; round < N - 1; ++round) {
-      for (int k = warp; k < N / 2; k += nw) {
-        int p, q;
-        rr_pair(round, k, N, p, q);
-        if (p >= nn || q >= nn) continue;
-        double* wp = W + int64_t(p) * mm;
-        double* wq = W + int64_t(q) * mm;
-        double al = 0, be = 0, ga = 0;
-        for (int64_t i = lane; i < mm; i += 32) {
-          double x = wp[i], y = wq[i];
-          al = fma(x, x, al);
-          be = fma(y, y, be);
-          ga = fma(x, y, ga);
-        }
-        al = warp_sum(al);
-        be = warp_sum(be);
-        ga = warp_sum(ga);
-        if (al == 0.0 || be == 0.0) continue;
-        if (fabs(ga) <= tol * sqrt(al) * sqrt(be)) continue;
-        double zeta = (be - al) / (2.0 * ga);
-        double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + hypot(1.0, zeta));
-        double c = 1.0 / sqrt(1.0 + t * t);
-        double s = c * t;
-        for (int64_t i = lane; i < mm; i += 32) {
-          double x = wp[i], y = wq[i];
-          wp[i] = c * x - s * y;
-          wq[i] = s * x + c * y;
-        }
-        double* vp = V + int64_t(p) * nn;
-        double* vq = V + int64_t(q) * nn;
-        for (int i = lane; i < nn; i += 32) {
-          double x = vp[i], y = vq[i];
-          vp[i] = c * x - s * y;
-          vq[i] = s * x + c * y;
-        }
-        if (lane == 0) rotated = 1;
-      }
-      __syncthreads();
-    }
-    if (rotated == 0) break;
-    __syncthreads();
-  }
-  // singular values = column norms
-  for (int j = warp; j < nn; j += nw) {
-    const double* wj = W + int64_t(j) * mm;
-    double acc = 0;
-    for (int64_t i = lane; i < mm; i += 32) acc = fma(wj[i], wj[i], acc);
-    acc = warp_sum(acc);
-    if (lane == 0) sval[j] = sqrt(acc);
-  }
-  __syncthreads();
-  for (int j = tid; j < nn; j += kSvdThreads) {
-    double sj = sval[j];
-    int r = 0;
-    for (int i = 0; i < nn; ++i) {
-      double si = sval[i];
-      r += (si > sj) || (si == sj && i < j);
-    }
-    order[r] = j;
-  }
-  __syncthreads();
-  const int64_t k = nn;
-  for (int r = warp; r < nn; r += nw) {
-    const int j = order[r];
-    const double sj = sval[j];
-    const double inv = sj > 0 ? 1.0 / sj : 0.0;
-    // left vector u = (tr ? V[:,j] : W[:,j]/s), right vector v = (tr ? W[:,j]/s : V[:,j])
-    const double* ucol = tr ? V + int64_t(j) * nn : W + int64_t(j) * mm;
-    const double uscale = tr ? 1.0 : inv;
-    const int64_t ulen = tr ? nn : mm;
-    // sign: largest |u_i| positive (first index on ties)
-    double best = -1.0, bval = 0.0;
-    int64_t bidx = 0;
-    for (int64_t i = lane; i < ulen; i += 32) {
-      double a = fabs(ucol[i]);
-      if (a > best) { best = a; bval = ucol[i]; bidx = i; }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      double ob = __shfl_xor_sync(0xffffffffu, best, o);
-      double ov = __shfl_xor_sync(0xffffffffu, bval, o);
-      int64_t oi = __shfl_xor_sync(0xffffffffu, bidx, o);
-      if (ob > best || (ob == best && oi < bidx)) { best = ob; bval = ov; bidx = oi; }
-    }
-    const double sg = (bval < 0) ? -1.0 : 1.0;
-    for (int64_t i = lane; i < ulen; i += 32) U[d.u_off + i + r * d.m] = sg * uscale * ucol[i];
-    const double* vcol = tr ? W + int64_t(j) * mm : V + int64_t(j) * nn;
-    const double vscale = tr ? inv : 1.0;
-    const int64_t vlen = tr ? mm : nn;
-    for (int64_t c = lane; c < vlen; c += 32) Vt[d.vt_off + r + c * k] = sg * vscale * vcol[c];
-    if (lane == 0) S[d.s_off + r] = sj;
-  }
-}
-
-size_t svd_work_elems(int64_t m, int64_t n) {
-  int64_t mm = std::max(m, n), nn = std::min(m, n);
-  return size_t(mm * nn + nn * nn);
-}
-
-void launch_svd(const xgb_svd_desc* d_descs, const int64_t* d_work_off, int n, int64_t max_k, const double* A, double* U,
-                double* S, double* Vt, double* work, cudaStream_t s) {
-  if (n <= 0) return;
-  size_t smem = size_t(std::max<int64_t>(max_k, 1)) * (sizeof(double) + sizeof(int));
-  if (smem > 48 * 1024) cudaFuncSetAttribute(svd_jacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  svd_jacobi_kernel<<<n, kSvdThreads, smem, s>>>(d_descs, d_work_off, A, U, S, Vt, work);
-  count_launch();
-}
-
 // ======================================================================= truncation
-// cutoff_matrices on the device: rank every singular value in the global
-// descending order (ties by position), keep rank < max_keep with s >= eps,
-// optionally cut the last multiplet, fall back to the first entry when
-// nothing survives, and count kept values per sector.  One CTA.
+// cutoff_matrices on the device (src/Core/Tensor.cpp:523-633).  The global
+// descending order of all singular values is made deterministic and robust
+// to last-bit differences: values are ranked exactly (ties by position),
+// consecutive values within kTieRtol (relative) form a tie group, and inside
+// a group entries keep their (sector, index) position order.  Then: keep the
+// first max_keep, drop values < eps, optionally cut the last multiplet, fall
+// back to the first value of the first sector when nothing survives, and
+// count kept values per sector.  One CTA; n is the number of singular values
+// of one tensor (thousands at most).
+constexpr double kTieRtol = 1.0e-12;
+
 __global__ void __launch_bounds__(1024) truncate_kernel(int n_sectors, const int64_t* __restrict__ s_begin,
                                                         const int32_t* __restrict__ deg, const double* __restrict__ s,
                                                         int64_t total, int64_t max_keep, double eps, int preserve,
                                                         int32_t* __restrict__ keep, double* __restrict__ out2,
-                                                        int64_t* __restrict__ rank_buf, double* __restrict__ sorted) {
+                                                        int64_t* __restrict__ ws) {
   __shared__ double red_w[32], red_e[32];
-  __shared__ int64_t n_keep_sh;
-  __shared__ int64_t cut_sh;
+  int64_t* exact = ws;                 // exact[r] = index with exact rank r
+  int64_t* gstart = ws + total;        // group start position for each exact position
+  int64_t* order = ws + 2 * total;     // order[f] = index at final position f
+  int64_t* flag = ws + 3 * total;      // flag[i] = 1 kept, 0 dropped; fpos stored in gstart reuse below
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int g = tid; g < n_sectors; g += blockDim.x) keep[g] = 0;
-  // global rank of each value
   for (int64_t i = tid; i < total; i += blockDim.x) {
-    double si = s[i];
+    const double si = s[i];
     int64_t r = 0;
     for (int64_t j = 0; j < total; ++j) {
-      double sj = s[j];
+      const double sj = s[j];
       r += (sj > si) || (sj == si && j < i);
     }
-    rank_buf[i] = r;
-    sorted[r] = si;
+    exact[r] = i;
+    flag[i] = 0;
   }
   __syncthreads();
   if (tid == 0) {
-    int64_t nk = total < max_keep ? total : max_keep;
-    if (eps > 0.0) {
-      // values are sorted descending, so "s < eps" removes a suffix
-      int64_t c = 0;
-      while (c < nk && !(sorted[c] < eps)) ++c;
-      nk = c;
+    int64_t start = 0;
+    for (int64_t p = 0; p < total; ++p) {
+      if (p > 0) {
+        const double prev = s[exact[p - 1]], cur = s[exact[p]];
+        if (prev - cur > kTieRtol * prev) start = p;
+      }
+      gstart[p] = start;
+    }
+  }
+  __syncthreads();
+  for (int64_t p = tid; p < total; p += blockDim.x) {
+    const int64_t i = exact[p], g0 = gstart[p];
+    int64_t f = g0;
+    for (int64_t q = g0; q < total && gstart[q] == g0; ++q) f += (exact[q] < i);
+    order[f] = i;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const int64_t lim = total < max_keep ? total : max_keep;
+    // kept list in final order, stored compactly at the front of `exact`
+    int64_t nk = 0;
+    for (int64_t f = 0; f < lim; ++f) {
+      const int64_t i = order[f];
+      if (eps > 0.0 && s[i] < eps) continue;
+      exact[nk++] = i;
     }
     if (preserve) {
       int64_t end = -1;
-      for (int64_t i = nk - 1; i > 0; --i) {
-        double rel = 2.0 * (sorted[i - 1] - sorted[i]) / (sorted[i - 1] + sorted[i]);
-        if (rel > 0.1) { end = i; break; }
+      for (int64_t k = nk - 1; k > 0; --k) {
+        const double a = s[exact[k - 1]], b = s[exact[k]];
+        if (2.0 * (a - b) / (a + b) > 0.1) { end = k; break; }
       }
       if (end != -1) nk = end;
     }
-    n_keep_sh = nk;
-    cut_sh = (total < max_keep ? total : max_keep);
+    if (nk == 0) { exact[0] = 0; nk = 1; }  // first entry: first value of the first sector
+    for (int64_t k = 0; k < nk; ++k) flag[exact[k]] = 1;
+    // positions >= max_keep contribute to the truncated weight
+    for (int64_t f = lim; f < total; ++f) flag[order[f]] |= 2;
   }
   __syncthreads();
-  const int64_t nk = n_keep_sh, cut = cut_sh;
   double wsum = 0.0, esum = 0.0;
   for (int64_t i = tid; i < total; i += blockDim.x) {
-    // sector of i
     int lo = 0, hi = n_sectors - 1;
     while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
+      const int mid = (lo + hi + 1) >> 1;
       if (s_begin[mid] <= i) lo = mid; else hi = mid - 1;
     }
     const double v = s[i];
-    const int64_t r = rank_buf[i];
-    if (r >= max_keep) wsum += deg[lo] * v * v;
-    bool kept = (nk > 0) ? (r < nk) : (i == 0);  // empty -> first entry (first value of first sector)
-    if (kept) {
+    if (flag[i] & 2) wsum += deg[lo] * v * v;
+    if (flag[i] & 1) {
       atomicAdd(&keep[lo], 1);
       esum += -deg[lo] * v * v * log(v * v);
     }
   }
-  (void)cut;
   wsum = warp_sum(wsum);
   esum = warp_sum(esum);
   if (lane == 0) { red_w[warp] = wsum; red_e[warp] = esum; }
@@ -518,13 +386,10 @@ __global__ void __launch_bounds__(1024) truncate_kernel(int n_sectors, const int
 
 void launch_truncate(int n_sectors, const int64_t* d_s_begin, const int32_t* d_deg, const double* s, int64_t total,
                      int64_t max_keep, double eps, int preserve, int32_t* keep, double* out2, cudaStream_t st) {
-  int64_t* rank_buf = static_cast<int64_t*>(dev_alloc(sizeof(int64_t) * std::max<int64_t>(total, 1)));
-  double* sorted = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(total, 1)));
-  truncate_kernel<<<1, 1024, 0, st>>>(n_sectors, d_s_begin, d_deg, s, total, max_keep, eps, preserve, keep, out2, rank_buf,
-                                      sorted);
+  int64_t* ws = static_cast<int64_t*>(dev_alloc(sizeof(int64_t) * 4 * std::max<int64_t>(total, 1)));
+  truncate_kernel<<<1, 1024, 0, st>>>(n_sectors, d_s_begin, d_deg, s, total, max_keep, eps, preserve, keep, out2, ws);
   count_launch();
-  dev_free(rank_buf);
-  dev_free(sorted);
+  dev_free(ws);
 }
 
 // ======================================================================= QR
