@@ -391,12 +391,25 @@ class Tensor:
 
 
 def fix_svd_signs(u, vt):
-    """Flip (u_j, v_j) so that the first largest-|.| entry of u_j is positive."""
+    """Gauge convention shared with the GPU kernel: flip (u_j, v_j) so that
+    r.u_j > 0 for the fixed generic vector r_i = frac((i+1)*0.7548776662466927)
+    + 0.25; when r.u_j is negligible (|r.u| <= 1e-8 sum r_i|u_i|) the first
+    largest-magnitude entry of u_j is made positive instead.  Structured
+    inputs (e.g. ket-bra fused environments) have singular vectors with
+    entries of exactly equal magnitude, for which a largest-entry rule alone
+    is decided by rounding."""
     u = u.copy()
     vt = vt.copy()
+    y = np.arange(1, u.shape[0] + 1, dtype=np.float64) * 0.7548776662466927
+    r = (y - np.floor(y)) + 0.25
     for j in range(u.shape[1]):
-        i = int(np.argmax(np.abs(u[:, j])))
-        if u[i, j] < 0:
+        dot = float(r @ u[:, j])
+        mag = float(r @ np.abs(u[:, j]))
+        if abs(dot) > 1.0e-8 * mag:
+            neg = dot < 0
+        else:
+            neg = u[int(np.argmax(np.abs(u[:, j]))), j] < 0
+        if neg:
             u[:, j] *= -1.0
             vt[j, :] *= -1.0
     return u, vt

@@ -180,6 +180,7 @@ PROTOS_EXTRA = [
     ("xgb_profile_read", C.c_int, [C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("xgb_event_record", C.c_int, [C.c_int]),
     ("xgb_event_elapsed_ms", C.c_double, [C.c_int, C.c_int]),
+    ("xgb_svd_last_sweeps", C.c_int, [i32p, C.c_int]),
 ]
 PROTOS.extend(PROTOS_EXTRA)
 

@@ -3,24 +3,29 @@
 // Replaces the per-sector LAPACK/Eigen SVD of full_svd_impl
 // (src/Core/Tensor.cpp:494-521, src/Interfaces/PlainInterface_Eigen_impl.cpp:114-127).
 //
-// Algorithm: one-sided (Hestenes) Jacobi, mixed precision, one thread-block
-// CLUSTER per sector block.  GB300 executes FP64 on a narrow pipe (about two
-// DFMA per clock per SM), so the FP64 work is (a) cut by first converging in
-// FP32 and (b) spread over the SMs of a cluster:
-//   1. W32 = op(A) in FP32, V32 = I; FP32 Jacobi sweeps until the columns of W32
-//      are orthogonal to FP32 accuracy.
-//   2. V64 = classical Gram-Schmidt of V32 in FP64 (V32 is orthogonal to ~1e-6,
-//      so one pass gives FP64 orthogonality), W64 = op(A) V64 in FP64.
-//   3. FP64 Jacobi sweeps on (W64, V64) until |w_p.w_q| <= tol |w_p||w_q|;
-//      starting from nearly orthogonal columns this takes two or three sweeps.
-//   4. sigma_j = |w_j|, sorted descending (ties by column), u_j = w_j/sigma_j,
-//      v_j = V64[:, j]; each pair sign-normalised so the largest |u_ij| > 0.
-// op(A) = A when m >= n, else A^T (then U and V swap roles).
-// All CTAs of a cluster share W/V/norms in global memory (L2-resident, read
-// and written with .cg so every SM sees the L2 copy); rounds of disjoint
-// rotation pairs are separated by cluster barriers.  Every loop has a fixed
-// bound (max sweeps), and all CTAs of a cluster take identical control flow,
-// so every barrier is reached by all of them.
+// Algorithm: one-sided (Hestenes) BLOCK Jacobi, mixed precision, one
+// thread-block cluster (8 CTAs on 8 SMs) per sector block.  GB300 executes
+// FP64 on a narrow pipe (about two DFMA per clock per SM), so the FP64 work is
+// cut by converging in FP32 first and is spread over the SMs of the cluster.
+//   1. W32 = op(A) in FP32, V32 = I; FP32 block-Jacobi sweeps.
+//   2. V = V32 in FP64, re-orthonormalised by the second-order polar
+//      correction V <- V (I - E/2 + 3E^2/8), E = V^T V - I (|E| ~ 1e-6, so the
+//      result is orthogonal to FP64 rounding); W64 = op(A) V.
+//   3. FP64 block-Jacobi sweeps on (W64, V) until every pair satisfies
+//      |w_p.w_q| <= tol |w_p||w_q| (two or three sweeps from step 2).
+//   4. sigma_j = |w_j| sorted descending (ties by column), u_j = w_j / sigma_j,
+//      v_j = V[:, j]; every pair sign-normalised (see sign rule below).
+// op(A) = A when m >= n, else A^T (U and V swap roles).
+//
+// Block schedule: the nn columns form 2P blocks (P = cluster size).  In each
+// outer round every CTA owns one pair of blocks (circle method over the 2P
+// blocks), stages their W/V columns and norms in shared memory, applies the
+// rotations of all cross pairs (and, in round 0, of the pairs inside each of
+// its blocks), writes them back and meets the other CTAs at a cluster
+// barrier.  A sweep therefore visits every column pair exactly once in 2P-1
+// barrier-separated rounds.  W/V live in global memory (L2 resident) and are
+// moved with .cg loads/stores so every SM sees the L2 copy.  All CTAs of a
+// cluster follow identical control flow and every loop has a fixed bound.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -35,9 +40,12 @@ namespace xgb {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
 constexpr int kCluster = 8;
+constexpr int kBlocks = 2 * kCluster;
 constexpr int kMaxSweeps32 = 30;
 constexpr int kMaxSweeps64 = 20;
+constexpr int kSmemLimit = 200 * 1024;
 
 template <class T>
 __device__ __forceinline__ T wsum(T v) {
@@ -53,86 +61,227 @@ __device__ __forceinline__ void rr_pair(int round, int k, int N, int& p, int& q)
   else { p = pos(k); q = pos(N - 1 - k); }
 }
 
-__device__ __forceinline__ float ld(const float* p) { return __ldcg(p); }
-__device__ __forceinline__ double ld(const double* p) { return __ldcg(p); }
-__device__ __forceinline__ void st(float* p, float v) { __stcg(p, v); }
-__device__ __forceinline__ void st(double* p, double v) { __stcg(p, v); }
-
+__device__ __forceinline__ float ldg(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ double ldg(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ void stg(float* p, float v) { __stcg(p, v); }
+__device__ __forceinline__ void stg(double* p, double v) { __stcg(p, v); }
 __device__ __forceinline__ float tsqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double tsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float thypot(float a, float b) { return hypotf(a, b); }
 __device__ __forceinline__ double thypot(double a, double b) { return hypot(a, b); }
 
+// shared-memory or global (L1-bypassing) element access
+template <class T, bool G>
+__device__ __forceinline__ T ld(const T* p) { if constexpr (G) return ldg(p); else return *p; }
+template <class T, bool G>
+__device__ __forceinline__ void st(T* p, T v) { if constexpr (G) stg(p, v); else *p = v; }
+
 struct Ctx {
-  int tid, lane, warp, gw, gnw, gtid, gnt;
+  int tid, lane, warp, rank, gw, gnw, gtid, gnt;
 };
 
-// Jacobi sweeps over the columns of W (mm x nn) with V (nn x nn) accumulated.
-// norms[nn] and flag live in global memory shared by the cluster.
+// One plane rotation between columns p and q (warp-cooperative).  Returns
+// true if a rotation was applied.
+template <class T, bool G>
+__device__ bool rotate(T* wp, T* wq, T* vp, T* vq, T* np, T* nq, int64_t mm, int nn, T tol, int lane) {
+  const T al = ld<T, G>(np), be = ld<T, G>(nq);
+  if (!(al > T(0)) || !(be > T(0))) return false;
+  T ga = 0;
+  for (int64_t i = lane; i < mm; i += 32) ga = fma(ld<T, G>(wp + i), ld<T, G>(wq + i), ga);
+  ga = wsum(ga);
+  if (fabs(ga) <= tol * tsqrt(al) * tsqrt(be)) return false;
+  const T zeta = (be - al) / (T(2) * ga);
+  const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + thypot(T(1), zeta));
+  const T cs = T(1) / tsqrt(T(1) + t * t);
+  const T sn = cs * t;
+  for (int64_t i = lane; i < mm; i += 32) {
+    const T x = ld<T, G>(wp + i), y = ld<T, G>(wq + i);
+    st<T, G>(wp + i, cs * x - sn * y);
+    st<T, G>(wq + i, sn * x + cs * y);
+  }
+  for (int i = lane; i < nn; i += 32) {
+    const T x = ld<T, G>(vp + i), y = ld<T, G>(vq + i);
+    st<T, G>(vp + i, cs * x - sn * y);
+    st<T, G>(vq + i, sn * x + cs * y);
+  }
+  __syncwarp();
+  if (lane == 0) {
+    st<T, G>(np, al - t * ga);
+    st<T, G>(nq, be + t * ga);
+  }
+  __syncwarp();
+  return true;
+}
+
+// Rotations of one outer round for the CTA's block pair.  Column c of the
+// pair (c < 2b) lives at W + c*ldw, V + c*ldv, N + c; columns [0, la) form
+// block A and [b, b+lb) block B.
+template <class T, bool G>
+__device__ bool round_rotations(const Ctx& c, T* W, int64_t ldw, T* V, int64_t ldv, T* N, int b, int la, int lb,
+                                bool inner, int64_t mm, int nn, T tol) {
+  bool any = false;
+  if (inner) {
+    // pairs inside block A and inside block B: circle method over each block
+    const int pa = la + (la & 1), pb = lb + (lb & 1);
+    const int rounds = max(pa, pb) - 1;
+    for (int r = 0; r < rounds; ++r) {
+      const int na = r < pa - 1 ? pa / 2 : 0, nb = r < pb - 1 ? pb / 2 : 0;
+      for (int k = c.warp; k < na + nb; k += kWarps) {
+        int p, q, base;
+        if (k < na) { rr_pair(r, k, pa, p, q); base = 0; if (p >= la || q >= la) continue; }
+        else { rr_pair(r, k - na, pb, p, q); base = b; if (p >= lb || q >= lb) continue; }
+        p += base;
+        q += base;
+        any |= rotate<T, G>(W + p * ldw, W + q * ldw, V + p * ldv, V + q * ldv, N + p, N + q, mm, nn, tol, c.lane);
+      }
+      __syncthreads();
+    }
+  }
+  // cross pairs (i, (i + r) mod b), i in A, j in B
+  for (int r = 0; r < b; ++r) {
+    for (int i = c.warp; i < b; i += kWarps) {
+      const int j = (i + r) % b;
+      if (i >= la || j >= lb) continue;
+      const int p = i, q = b + j;
+      any |= rotate<T, G>(W + p * ldw, W + q * ldw, V + p * ldv, V + q * ldv, N + p, N + q, mm, nn, tol, c.lane);
+    }
+    __syncthreads();
+  }
+  return any;
+}
+
 template <class T>
-__device__ int jacobi_sweeps(cg::cluster_group& cl, const Ctx& c, T* W, T* V, T* norms, int* flag, int64_t mm, int nn,
-                             T tol, int max_sweeps) {
-  const int N = nn + (nn & 1);
+__device__ int block_jacobi(cg::cluster_group& cl, const Ctx& c, T* W, T* V, T* norms, int* flag, int64_t mm, int nn,
+                            T tol, int max_sweeps, T* smem, bool staged) {
+  const int b = (nn + kBlocks - 1) / kBlocks;
   int sweeps = 0;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     for (int j = c.gw; j < nn; j += c.gnw) {
       const T* w = W + int64_t(j) * mm;
       T a = 0;
-      for (int64_t i = c.lane; i < mm; i += 32) { const T x = ld(w + i); a = fma(x, x, a); }
+      for (int64_t i = c.lane; i < mm; i += 32) { const T x = ldg(w + i); a = fma(x, x, a); }
       a = wsum(a);
-      if (c.lane == 0) st(norms + j, a);
+      if (c.lane == 0) stg(norms + j, a);
     }
-    if (cl.block_rank() == 0 && c.tid == 0) atomicExch(flag, 0);
+    if (c.rank == 0 && c.tid == 0) atomicExch(flag, 0);
     cl.sync();
-    for (int round = 0; round < N - 1; ++round) {
-      for (int k = c.gw; k < N / 2; k += c.gnw) {
-        int p, q;
-        rr_pair(round, k, N, p, q);
-        if (p >= nn || q >= nn) continue;
-        const T al = ld(norms + p), be = ld(norms + q);
-        if (!(al > T(0)) || !(be > T(0))) continue;
-        T* wp = W + int64_t(p) * mm;
-        T* wq = W + int64_t(q) * mm;
-        T ga = 0;
-        for (int64_t i = c.lane; i < mm; i += 32) ga = fma(ld(wp + i), ld(wq + i), ga);
-        ga = wsum(ga);
-        if (fabs(ga) <= tol * tsqrt(al) * tsqrt(be)) continue;
-        const T zeta = (be - al) / (T(2) * ga);
-        const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + thypot(T(1), zeta));
-        const T cs = T(1) / tsqrt(T(1) + t * t);
-        const T sn = cs * t;
-        for (int64_t i = c.lane; i < mm; i += 32) {
-          const T x = ld(wp + i), y = ld(wq + i);
-          st(wp + i, cs * x - sn * y);
-          st(wq + i, sn * x + cs * y);
+    for (int round = 0; round < kBlocks - 1; ++round) {
+      int ba, bb;
+      rr_pair(round, c.rank, kBlocks, ba, bb);
+      const int ca = ba * b, cb = bb * b;
+      const int la = max(0, min(b, nn - ca)), lb = max(0, min(b, nn - cb));
+      bool any = false;
+      if (staged) {
+        T* sW = smem;                        // 2b columns of mm
+        T* sV = sW + int64_t(2 * b) * mm;    // 2b columns of nn
+        T* sN = sV + int64_t(2 * b) * nn;    // 2b norms
+        for (int64_t e = c.tid; e < int64_t(2 * b) * mm; e += kThreads) {
+          const int col = int(e / mm);
+          const int64_t row = e % mm;
+          const int g = col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1);
+          sW[e] = g >= 0 ? ldg(W + int64_t(g) * mm + row) : T(0);
         }
-        T* vp = V + int64_t(p) * nn;
-        T* vq = V + int64_t(q) * nn;
-        for (int i = c.lane; i < nn; i += 32) {
-          const T x = ld(vp + i), y = ld(vq + i);
-          st(vp + i, cs * x - sn * y);
-          st(vq + i, sn * x + cs * y);
+        for (int64_t e = c.tid; e < int64_t(2 * b) * nn; e += kThreads) {
+          const int col = int(e / nn);
+          const int64_t row = e % nn;
+          const int g = col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1);
+          sV[e] = g >= 0 ? ldg(V + int64_t(g) * nn + row) : T(0);
         }
-        if (c.lane == 0) {
-          st(norms + p, al - t * ga);
-          st(norms + q, be + t * ga);
-          atomicExch(flag, 1);
+        for (int col = c.tid; col < 2 * b; col += kThreads) {
+          const int g = col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1);
+          sN[col] = g >= 0 ? ldg(norms + g) : T(0);
+        }
+        __syncthreads();
+        any = round_rotations<T, false>(c, sW, mm, sV, nn, sN, b, la, lb, round == 0, mm, nn, tol);
+        for (int64_t e = c.tid; e < int64_t(2 * b) * mm; e += kThreads) {
+          const int col = int(e / mm);
+          const int g = col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1);
+          if (g >= 0) stg(W + int64_t(g) * mm + e % mm, sW[e]);
+        }
+        for (int64_t e = c.tid; e < int64_t(2 * b) * nn; e += kThreads) {
+          const int col = int(e / nn);
+          const int g = col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1);
+          if (g >= 0) stg(V + int64_t(g) * nn + e % nn, sV[e]);
+        }
+        for (int col = c.tid; col < 2 * b; col += kThreads) {
+          const int g = col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1);
+          if (g >= 0) stg(norms + g, sN[col]);
+        }
+      } else {
+        // staging does not fit: rotate the columns in place in L2, with
+        // per-pair pointers (the two blocks are not adjacent in memory)
+        if (round == 0) {
+          const int pa = la + (la & 1), pb = lb + (lb & 1);
+          const int rounds = max(pa, pb) - 1;
+          for (int r = 0; r < rounds; ++r) {
+            const int na = r < pa - 1 ? pa / 2 : 0, nb = r < pb - 1 ? pb / 2 : 0;
+            for (int k = c.warp; k < na + nb; k += kWarps) {
+              int p, q, base;
+              if (k < na) { rr_pair(r, k, pa, p, q); base = ca; if (p >= la || q >= la) continue; }
+              else { rr_pair(r, k - na, pb, p, q); base = cb; if (p >= lb || q >= lb) continue; }
+              p += base;
+              q += base;
+              any |= rotate<T, true>(W + int64_t(p) * mm, W + int64_t(q) * mm, V + int64_t(p) * nn, V + int64_t(q) * nn,
+                                     norms + p, norms + q, mm, nn, tol, c.lane);
+            }
+            __syncthreads();
+          }
+        }
+        for (int r = 0; r < b; ++r) {
+          for (int i = c.warp; i < b; i += kWarps) {
+            const int j = (i + r) % b;
+            if (i >= la || j >= lb) continue;
+            const int p = ca + i, q = cb + j;
+            any |= rotate<T, true>(W + int64_t(p) * mm, W + int64_t(q) * mm, V + int64_t(p) * nn, V + int64_t(q) * nn,
+                                   norms + p, norms + q, mm, nn, tol, c.lane);
+          }
+          __syncthreads();
         }
       }
+      if (any && c.lane == 0) atomicExch(flag, 1);
       cl.sync();
     }
     ++sweeps;
     const int any = atomicAdd(flag, 0);
-    cl.sync();  // everybody has read the flag before the next sweep resets it
+    cl.sync();  // every CTA has read the flag before the next sweep resets it
     if (!any) break;
   }
   return sweeps;
 }
 
+// Sign rule shared with the CPU oracle: s = sign(r . u) with the fixed
+// generic vector r_i = frac((i+1) * 0.7548776662466927) + 0.25; if r.u is
+// negligible against sum_i r_i |u_i| (u nearly orthogonal to r), the sign
+// of the first largest-magnitude entry is used instead.
+__device__ double sign_of(const double* u, int64_t len, double scale, int lane) {
+  double dot = 0, mag = 0, best = -1, bval = 0;
+  long long bidx = 0;
+  for (int64_t i = lane; i < len; i += 32) {
+    const double x = ldg(u + i) * scale;
+    const double y = double(i + 1) * 0.7548776662466927;
+    const double r = (y - floor(y)) + 0.25;
+    dot = fma(r, x, dot);
+    mag = fma(r, fabs(x), mag);
+    if (fabs(x) > best) { best = fabs(x); bval = x; bidx = i; }
+  }
+  dot = wsum(dot);
+  mag = wsum(mag);
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const double ov = __shfl_xor_sync(0xffffffffu, bval, o);
+    const long long oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+    if (ob > best || (ob == best && oi < bidx)) { best = ob; bval = ov; bidx = oi; }
+  }
+  if (fabs(dot) > 1.0e-8 * mag) return dot < 0 ? -1.0 : 1.0;
+  return bval < 0 ? -1.0 : 1.0;
+}
+
 __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
     svd_cluster_kernel(const xgb_svd_desc* __restrict__ descs, const int64_t* __restrict__ work_off,
                        const double* __restrict__ A, double* __restrict__ U, double* __restrict__ S,
-                       double* __restrict__ Vt, double* __restrict__ work, int* __restrict__ sweep_stats) {
+                       double* __restrict__ Vt, double* __restrict__ work, int* __restrict__ sweep_stats,
+                       int smem_bytes) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cl = cg::this_cluster();
   const int sector = blockIdx.x / kCluster;
   const xgb_svd_desc d = descs[sector];
@@ -145,134 +294,157 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
   c.tid = threadIdx.x;
   c.lane = c.tid & 31;
   c.warp = c.tid >> 5;
-  const int nw = kThreads / 32;
-  c.gw = int(cl.block_rank()) * nw + c.warp;
-  c.gnw = kCluster * nw;
-  c.gtid = int(cl.block_rank()) * kThreads + c.tid;
+  c.rank = int(cl.block_rank());
+  c.gw = c.rank * kWarps + c.warp;
+  c.gnw = kCluster * kWarps;
+  c.gtid = c.rank * kThreads + c.tid;
   c.gnt = kCluster * kThreads;
 
-  // workspace layout (doubles): W64 mm*nn | V64 nn*nn | norms64 nn | misc 8 | then floats W32 mm*nn | V32 nn*nn | norms32 nn
+  // workspace (doubles): W64 mm*nn | V64 nn*nn | T1 nn*nn | T2 nn*nn | n64 nn | flag 8 | floats: W32 | V32 | n32
+  const int64_t nn2 = int64_t(nn) * nn;
   double* W64 = work + work_off[sector];
   double* V64 = W64 + mm * nn;
-  double* n64 = V64 + int64_t(nn) * nn;
+  double* T1 = V64 + nn2;
+  double* T2 = T1 + nn2;
+  double* n64 = T2 + nn2;
   int* flag = reinterpret_cast<int*>(n64 + nn);
   float* W32 = reinterpret_cast<float*>(n64 + nn + 8);
   float* V32 = W32 + mm * nn;
-  float* n32 = V32 + int64_t(nn) * nn;
+  float* n32 = V32 + nn2;
 
   auto opA = [&](int64_t i, int64_t j) { return tr ? A[d.a_off + j + i * d.m] : A[d.a_off + i + j * d.m]; };
+  const int b = (nn + kBlocks - 1) / kBlocks;
+  const bool staged32 = int64_t(2 * b) * (mm + nn + 1) * 4 <= smem_bytes;
+  const bool staged64 = int64_t(2 * b) * (mm + nn + 1) * 8 <= smem_bytes;
 
-  // ---- phase 1: FP32 Jacobi
-  for (int64_t e = c.gtid; e < mm * nn; e += c.gnt) st(W32 + e, float(opA(e % mm, e / mm)));
-  for (int64_t e = c.gtid; e < int64_t(nn) * nn; e += c.gnt) st(V32 + e, (e % nn) == (e / nn) ? 1.f : 0.f);
+  // ---- phase 1: FP32 block Jacobi
+  for (int64_t e = c.gtid; e < mm * nn; e += c.gnt) stg(W32 + e, float(opA(e % mm, e / mm)));
+  for (int64_t e = c.gtid; e < nn2; e += c.gnt) stg(V32 + e, (e % nn) == (e / nn) ? 1.f : 0.f);
   cl.sync();
   const float tol32 = 8.0f * sqrtf(float(mm)) * 6.0e-8f;
-  int sw32 = nn > 1 ? jacobi_sweeps<float>(cl, c, W32, V32, n32, flag, mm, nn, tol32, kMaxSweeps32) : 0;
+  const int sw32 = nn > 1 ? block_jacobi<float>(cl, c, W32, V32, n32, flag, mm, nn, tol32, kMaxSweeps32,
+                                                reinterpret_cast<float*>(smem_raw), staged32)
+                          : 0;
 
-  // ---- phase 2: V64 = Gram-Schmidt(V32), W64 = op(A) V64
-  for (int64_t e = c.gtid; e < int64_t(nn) * nn; e += c.gnt) st(V64 + e, double(ld(V32 + e)));
+  // ---- phase 2: V = V32 (I - E/2 + 3E^2/8), E = V32^T V32 - I;  W64 = op(A) V
+  for (int64_t e = c.gtid; e < nn2; e += c.gnt) stg(V64 + e, double(ldg(V32 + e)));
   cl.sync();
-  for (int j = 0; j < nn; ++j) {
-    double* vj = V64 + int64_t(j) * nn;
-    for (int i = c.gw; i < j; i += c.gnw) {  // d_i = <v_i, v_j>
-      const double* vi = V64 + int64_t(i) * nn;
-      double a = 0;
-      for (int r = c.lane; r < nn; r += 32) a = fma(ld(vi + r), ld(vj + r), a);
-      a = wsum(a);
-      if (c.lane == 0) st(n64 + i, a);
-    }
-    cl.sync();
-    for (int r = c.gtid; r < nn; r += c.gnt) {
-      double x = ld(vj + r);
-      for (int i = 0; i < j; ++i) x = fma(-ld(n64 + i), ld(V64 + int64_t(i) * nn + r), x);
-      st(vj + r, x);
-    }
-    cl.sync();
-    // normalise v_j (every CTA computes the same norm redundantly: no extra barrier)
-    double a = 0;
-    for (int r = c.lane; r < nn; r += 32) { const double x = ld(vj + r); a = fma(x, x, a); }
-    a = wsum(a);
-    const double inv = a > 0 ? 1.0 / sqrt(a) : 0.0;
-    cl.sync();
-    for (int r = c.gtid; r < nn; r += c.gnt) st(vj + r, ld(vj + r) * inv);
-    cl.sync();
+  for (int64_t e = c.gtid; e < nn2; e += c.gnt) {  // T1 = E
+    const int64_t i = e % nn, j = e / nn;
+    double acc = 0;
+    for (int r = 0; r < nn; ++r) acc = fma(ldg(V64 + i * nn + r), ldg(V64 + j * nn + r), acc);
+    stg(T1 + e, acc - (i == j ? 1.0 : 0.0));
   }
+  cl.sync();
+  for (int64_t e = c.gtid; e < nn2; e += c.gnt) {  // T2 = I - E/2 + 3/8 E^2
+    const int64_t i = e % nn, j = e / nn;
+    double acc = 0;
+    for (int r = 0; r < nn; ++r) acc = fma(ldg(T1 + i + int64_t(r) * nn), ldg(T1 + r + j * nn), acc);
+    stg(T2 + e, (i == j ? 1.0 : 0.0) - 0.5 * ldg(T1 + e) + 0.375 * acc);
+  }
+  cl.sync();
+  for (int64_t e = c.gtid; e < nn2; e += c.gnt) {  // T1 = V T2
+    const int64_t i = e % nn, j = e / nn;
+    double acc = 0;
+    for (int r = 0; r < nn; ++r) acc = fma(ldg(V64 + i + int64_t(r) * nn), ldg(T2 + r + j * nn), acc);
+    stg(T1 + e, acc);
+  }
+  cl.sync();
+  double* V = T1;
   for (int64_t e = c.gtid; e < mm * nn; e += c.gnt) {
     const int64_t i = e % mm, j = e / mm;
-    const double* vj = V64 + j * nn;
+    const double* vj = V + j * nn;
     double acc = 0;
-    for (int l = 0; l < nn; ++l) acc = fma(opA(i, l), ld(vj + l), acc);
-    st(W64 + e, acc);
+    for (int l = 0; l < nn; ++l) acc = fma(opA(i, l), ldg(vj + l), acc);
+    stg(W64 + e, acc);
   }
   cl.sync();
 
-  // ---- phase 3: FP64 Jacobi polish
+  // ---- phase 3: FP64 block Jacobi polish
   const double tol64 = 1.0e-13;
-  int sw64 = nn > 1 ? jacobi_sweeps<double>(cl, c, W64, V64, n64, flag, mm, nn, tol64, kMaxSweeps64) : 0;
+  const int sw64 = nn > 1 ? block_jacobi<double>(cl, c, W64, V, n64, flag, mm, nn, tol64, kMaxSweeps64,
+                                                 reinterpret_cast<double*>(smem_raw), staged64)
+                          : 0;
 
   // ---- phase 4: sort, sign, write
-  double* sval = n64;  // reuse: exact column norms
+  double* sval = n64;
   for (int j = c.gw; j < nn; j += c.gnw) {
     const double* w = W64 + int64_t(j) * mm;
     double a = 0;
-    for (int64_t i = c.lane; i < mm; i += 32) { const double x = ld(w + i); a = fma(x, x, a); }
+    for (int64_t i = c.lane; i < mm; i += 32) { const double x = ldg(w + i); a = fma(x, x, a); }
     a = wsum(a);
-    if (c.lane == 0) st(sval + j, sqrt(a));
+    if (c.lane == 0) stg(sval + j, sqrt(a));
   }
   cl.sync();
   const int64_t k = nn;
   for (int j = c.gw; j < nn; j += c.gnw) {
-    const double sj = ld(sval + j);
+    const double sj = ldg(sval + j);
     int r = 0;
     for (int i = c.lane; i < nn; i += 32) {
-      const double si = ld(sval + i);
+      const double si = ldg(sval + i);
       r += (si > sj) || (si == sj && i < j);
     }
     r = wsum(r);
     const double inv = sj > 0 ? 1.0 / sj : 0.0;
-    const double* ucol = tr ? V64 + int64_t(j) * nn : W64 + int64_t(j) * mm;
+    const double* ucol = tr ? V + int64_t(j) * nn : W64 + int64_t(j) * mm;
     const double uscale = tr ? 1.0 : inv;
     const int64_t ulen = tr ? nn : mm;
-    double best = -1.0, bval = 0.0;
-    long long bidx = 0;
-    for (int64_t i = c.lane; i < ulen; i += 32) {
-      const double x = ld(ucol + i), a = fabs(x);
-      if (a > best) { best = a; bval = x; bidx = i; }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-      const double ov = __shfl_xor_sync(0xffffffffu, bval, o);
-      const long long oi = __shfl_xor_sync(0xffffffffu, bidx, o);
-      if (ob > best || (ob == best && oi < bidx)) { best = ob; bval = ov; bidx = oi; }
-    }
-    const double sg = (bval < 0) ? -1.0 : 1.0;
-    for (int64_t i = c.lane; i < ulen; i += 32) U[d.u_off + i + int64_t(r) * d.m] = sg * uscale * ld(ucol + i);
-    const double* vcol = tr ? W64 + int64_t(j) * mm : V64 + int64_t(j) * nn;
+    const double sg = sign_of(ucol, ulen, uscale, c.lane);
+    for (int64_t i = c.lane; i < ulen; i += 32) U[d.u_off + i + int64_t(r) * d.m] = sg * uscale * ldg(ucol + i);
+    const double* vcol = tr ? W64 + int64_t(j) * mm : V + int64_t(j) * nn;
     const double vscale = tr ? inv : 1.0;
     const int64_t vlen = tr ? mm : nn;
-    for (int64_t cc = c.lane; cc < vlen; cc += 32) Vt[d.vt_off + r + cc * k] = sg * vscale * ld(vcol + cc);
+    for (int64_t cc = c.lane; cc < vlen; cc += 32) Vt[d.vt_off + r + cc * k] = sg * vscale * ldg(vcol + cc);
     if (c.lane == 0) S[d.s_off + r] = sj;
   }
-  if (sweep_stats && cl.block_rank() == 0 && c.tid == 0) {
+  if (sweep_stats && c.rank == 0 && c.tid == 0) {
     sweep_stats[2 * sector] = sw32;
     sweep_stats[2 * sector + 1] = sw64;
   }
 }
 
+int* g_stats_dev = nullptr;
+int g_stats_cap = 0;
+int g_stats_n = 0;
+
 }  // namespace
 
 size_t svd_work_elems(int64_t m, int64_t n) {
   const int64_t mm = std::max(m, n), nn = std::min(m, n);
-  const int64_t doubles = mm * nn + nn * nn + nn + 8;
+  const int64_t doubles = mm * nn + 3 * nn * nn + nn + 8;
   const int64_t floats = mm * nn + nn * nn + nn;
   return size_t(doubles + (floats + 1) / 2 + 2);
 }
 
-void launch_svd(const xgb_svd_desc* d_descs, const int64_t* d_work_off, int n, int64_t /*max_k*/, const double* A,
+void launch_svd(const xgb_svd_desc* d_descs, const int64_t* d_work_off, int n, int64_t max_k, const double* A,
                 double* U, double* S, double* Vt, double* work, cudaStream_t s) {
   if (n <= 0) return;
-  svd_cluster_kernel<<<n * kCluster, kThreads, 0, s>>>(d_descs, d_work_off, A, U, S, Vt, work, nullptr);
+  if (g_stats_cap < n) {
+    if (g_stats_dev) cudaFree(g_stats_dev);
+    cudaMalloc(&g_stats_dev, sizeof(int) * 2 * n);
+    g_stats_cap = n;
+  }
+  g_stats_n = n;
+  // Every CTA gets the full staging budget (one CTA per SM); each block
+  // checks whether its 2b staged columns fit and otherwise rotates in L2.
+  (void)max_k;
+  const int smem = kSmemLimit;
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(svd_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+    configured = true;
+  }
+  svd_cluster_kernel<<<n * kCluster, kThreads, smem, s>>>(d_descs, d_work_off, A, U, S, Vt, work, g_stats_dev, smem);
   count_launch();
 }
 
 }  // namespace xgb
+
+extern "C" int xgb_svd_last_sweeps(int32_t* out, int cap) {
+  using namespace xgb;
+  if (!g_stats_dev || g_stats_n == 0) return 0;
+  const int n = std::min(cap / 2, g_stats_n);
+  cudaStreamSynchronize(stream());
+  cudaMemcpy(out, g_stats_dev, sizeof(int) * 2 * n, cudaMemcpyDeviceToHost);
+  return n;
+}
