@@ -133,8 +133,10 @@ size_t xgb_svd_workspace_bytes(int n, const xgb_svd_desc* descs);
 int xgb_batched_svd(int n, const xgb_svd_desc* descs, const double* A, double* U, double* S, double* Vt, void* work,
                     void* stream);
 
-/* FP32 / FP64 Jacobi sweep counts of the blocks of the last batched SVD
-   (pairs per block); returns the number of blocks written */
+/* Diagnostics of the last batched SVD, 6 ints per block: FP32 sweeps, FP64
+   sweeps, then the cycles/1024 spent in the FP32 sweeps, the FP64
+   re-orthonormalisation, the FP64 sweeps and the output stage; returns the
+   number of blocks written */
 int xgb_svd_last_sweeps(int32_t* out, int cap);
 
 /* ---------------------------------------------------------------- truncation */

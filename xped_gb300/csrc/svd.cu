@@ -4,17 +4,24 @@
 // (src/Core/Tensor.cpp:494-521, src/Interfaces/PlainInterface_Eigen_impl.cpp:114-127).
 //
 // Algorithm: one-sided (Hestenes) BLOCK Jacobi, mixed precision, one
-// thread-block cluster (8 CTAs on 8 SMs) per sector block.  GB300 executes
-// FP64 on a narrow pipe (about two DFMA per clock per SM), so the FP64 work is
-// cut by converging in FP32 first and is spread over the SMs of the cluster.
+// thread-block cluster (8 CTAs on 8 SMs) per sector block.  On GB300 a
+// warp-wide FP64 instruction occupies the SM sub-partition's FP64 pipe for
+// about 64 cycles, so FP64 work is (a) cut by converging in FP32 first,
+// (b) kept to the vector updates (rotation angles are found in FP32 and only
+// the rotation itself is formed in FP64), and (c) spread over the cluster:
+//   0. A is scaled by a power of two (exact) so its largest entry is O(1),
+//      keeping the FP32 squares inside the FP32 range.
 //   1. W32 = op(A) in FP32, V32 = I; FP32 block-Jacobi sweeps.
 //   2. V = V32 in FP64, re-orthonormalised by the second-order polar
 //      correction V <- V (I - E/2 + 3E^2/8), E = V^T V - I (|E| ~ 1e-6, so the
-//      result is orthogonal to FP64 rounding); W64 = op(A) V.
+//      result is orthogonal to FP64 rounding); W64 = op(A) V (unscaled A).
 //   3. FP64 block-Jacobi sweeps on (W64, V) until every pair satisfies
-//      |w_p.w_q| <= tol |w_p||w_q| (two or three sweeps from step 2).
+//      |w_p.w_q| <= tol |w_p||w_q|.  Each rotation is exactly orthogonal in
+//      FP64 (c = 1/sqrt(1+t^2) refined by Newton steps, s = c t), its angle t
+//      comes from FP32 arithmetic on exactly rescaled inputs: an FP32 angle
+//      shrinks |w_p.w_q| by ~1e-7 per visit, ample from the ~1e-6 start.
 //   4. sigma_j = |w_j| sorted descending (ties by column), u_j = w_j / sigma_j,
-//      v_j = V[:, j]; every pair sign-normalised (see sign rule below).
+//      v_j = V[:, j]; every pair sign-normalised (sign rule below).
 // op(A) = A when m >= n, else A^T (U and V swap roles).
 //
 // Block schedule: the nn columns form 2P blocks (P = cluster size).  In each
@@ -39,13 +46,14 @@ namespace cg = cooperative_groups;
 namespace xgb {
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kCluster = 8;
 constexpr int kBlocks = 2 * kCluster;
 constexpr int kMaxSweeps32 = 30;
 constexpr int kMaxSweeps64 = 20;
 constexpr int kSmemLimit = 200 * 1024;
+constexpr int kCgemmCols = 16;
 
 template <class T>
 __device__ __forceinline__ T wsum(T v) {
@@ -65,10 +73,6 @@ __device__ __forceinline__ float ldg(const float* p) { return __ldcg(p); }
 __device__ __forceinline__ double ldg(const double* p) { return __ldcg(p); }
 __device__ __forceinline__ void stg(float* p, float v) { __stcg(p, v); }
 __device__ __forceinline__ void stg(double* p, double v) { __stcg(p, v); }
-__device__ __forceinline__ float tsqrt(float x) { return sqrtf(x); }
-__device__ __forceinline__ double tsqrt(double x) { return sqrt(x); }
-__device__ __forceinline__ float thypot(float a, float b) { return hypotf(a, b); }
-__device__ __forceinline__ double thypot(double a, double b) { return hypot(a, b); }
 
 // shared-memory or global (L1-bypassing) element access
 template <class T, bool G>
@@ -76,9 +80,20 @@ __device__ __forceinline__ T ld(const T* p) { if constexpr (G) return ldg(p); el
 template <class T, bool G>
 __device__ __forceinline__ void st(T* p, T v) { if constexpr (G) stg(p, v); else *p = v; }
 
+// exact power of two 2^e as a double (|e| < 1000)
+__device__ __forceinline__ double pow2(int e) { return __longlong_as_double((long long)(e + 1023) << 52); }
+__device__ __forceinline__ int exponent_of(double x) { return int((__double_as_longlong(x) >> 52) & 0x7ff) - 1023; }
+
 struct Ctx {
   int tid, lane, warp, rank, gw, gnw, gtid, gnt;
 };
+
+// FP32 rotation angle t = tan(theta) that zeroes w_p.w_q (Rutishauser's
+// formula), from norms al, be and dot ga that are already scaled into [~1e-?, 4].
+__device__ __forceinline__ float angle32(float al, float be, float ga) {
+  const float zeta = (be - al) / (2.0f * ga);
+  return copysignf(1.0f, zeta) / (fabsf(zeta) + hypotf(1.0f, zeta));
+}
 
 // One plane rotation between columns p and q (warp-cooperative).  Returns
 // true if a rotation was applied.
@@ -89,11 +104,23 @@ __device__ bool rotate(T* wp, T* wq, T* vp, T* vq, T* np, T* nq, int64_t mm, int
   T ga = 0;
   for (int64_t i = lane; i < mm; i += 32) ga = fma(ld<T, G>(wp + i), ld<T, G>(wq + i), ga);
   ga = wsum(ga);
-  if (fabs(ga) <= tol * tsqrt(al) * tsqrt(be)) return false;
-  const T zeta = (be - al) / (T(2) * ga);
-  const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + thypot(T(1), zeta));
-  const T cs = T(1) / tsqrt(T(1) + t * t);
-  const T sn = cs * t;
+  if (ga * ga <= tol * tol * al * be) return false;
+  T cs, sn, t;
+  if constexpr (sizeof(T) == 4) {
+    t = angle32(al, be, ga);
+    cs = rsqrtf(1.0f + t * t);
+    sn = cs * t;
+  } else {
+    // exact rescaling by a power of two brings al, be, ga into FP32 range
+    const double sc = pow2(-exponent_of(fmax(al, be)));
+    t = double(angle32(float(al * sc), float(be * sc), float(ga * sc)));
+    const double x = 1.0 + t * t;
+    double r = double(rsqrtf(float(x)));
+    r = r * (1.5 - 0.5 * x * r * r);
+    r = r * (1.5 - 0.5 * x * r * r);
+    cs = r;
+    sn = r * t;
+  }
   for (int64_t i = lane; i < mm; i += 32) {
     const T x = ld<T, G>(wp + i), y = ld<T, G>(wq + i);
     st<T, G>(wp + i, cs * x - sn * y);
@@ -113,12 +140,12 @@ __device__ bool rotate(T* wp, T* wq, T* vp, T* vq, T* np, T* nq, int64_t mm, int
   return true;
 }
 
-// Rotations of one outer round for the CTA's block pair.  Column c of the
-// pair (c < 2b) lives at W + c*ldw, V + c*ldv, N + c; columns [0, la) form
-// block A and [b, b+lb) block B.
-template <class T, bool G>
-__device__ bool round_rotations(const Ctx& c, T* W, int64_t ldw, T* V, int64_t ldv, T* N, int b, int la, int lb,
-                                bool inner, int64_t mm, int nn, T tol) {
+// Rotations of one outer round for the CTA's block pair, columns staged in
+// shared memory: column c (< 2b) at W + c*mm, V + c*nn, N + c; block A is
+// [0, la), block B is [b, b+lb).
+template <class T>
+__device__ bool round_rotations(const Ctx& c, T* W, T* V, T* N, int b, int la, int lb, bool inner, int64_t mm, int nn,
+                                T tol) {
   bool any = false;
   if (inner) {
     // pairs inside block A and inside block B: circle method over each block
@@ -132,7 +159,7 @@ __device__ bool round_rotations(const Ctx& c, T* W, int64_t ldw, T* V, int64_t l
         else { rr_pair(r, k - na, pb, p, q); base = b; if (p >= lb || q >= lb) continue; }
         p += base;
         q += base;
-        any |= rotate<T, G>(W + p * ldw, W + q * ldw, V + p * ldv, V + q * ldv, N + p, N + q, mm, nn, tol, c.lane);
+        any |= rotate<T, false>(W + p * mm, W + q * mm, V + p * nn, V + q * nn, N + p, N + q, mm, nn, tol, c.lane);
       }
       __syncthreads();
     }
@@ -143,7 +170,7 @@ __device__ bool round_rotations(const Ctx& c, T* W, int64_t ldw, T* V, int64_t l
       const int j = (i + r) % b;
       if (i >= la || j >= lb) continue;
       const int p = i, q = b + j;
-      any |= rotate<T, G>(W + p * ldw, W + q * ldw, V + p * ldv, V + q * ldv, N + p, N + q, mm, nn, tol, c.lane);
+      any |= rotate<T, false>(W + p * mm, W + q * mm, V + p * nn, V + q * nn, N + p, N + q, mm, nn, tol, c.lane);
     }
     __syncthreads();
   }
@@ -170,45 +197,29 @@ __device__ int block_jacobi(cg::cluster_group& cl, const Ctx& c, T* W, T* V, T* 
       rr_pair(round, c.rank, kBlocks, ba, bb);
       const int ca = ba * b, cb = bb * b;
       const int la = max(0, min(b, nn - ca)), lb = max(0, min(b, nn - cb));
+      auto gcol = [&](int col) { return col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1); };
       bool any = false;
       if (staged) {
         T* sW = smem;                        // 2b columns of mm
         T* sV = sW + int64_t(2 * b) * mm;    // 2b columns of nn
         T* sN = sV + int64_t(2 * b) * nn;    // 2b norms
-        for (int64_t e = c.tid; e < int64_t(2 * b) * mm; e += kThreads) {
-          const int col = int(e / mm);
-          const int64_t row = e % mm;
-          const int g = col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1);
-          sW[e] = g >= 0 ? ldg(W + int64_t(g) * mm + row) : T(0);
-        }
-        for (int64_t e = c.tid; e < int64_t(2 * b) * nn; e += kThreads) {
-          const int col = int(e / nn);
-          const int64_t row = e % nn;
-          const int g = col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1);
-          sV[e] = g >= 0 ? ldg(V + int64_t(g) * nn + row) : T(0);
-        }
-        for (int col = c.tid; col < 2 * b; col += kThreads) {
-          const int g = col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1);
-          sN[col] = g >= 0 ? ldg(norms + g) : T(0);
+        for (int col = c.warp; col < 2 * b; col += kWarps) {
+          const int g = gcol(col);
+          for (int64_t i = c.lane; i < mm; i += 32) sW[col * mm + i] = g >= 0 ? ldg(W + int64_t(g) * mm + i) : T(0);
+          for (int i = c.lane; i < nn; i += 32) sV[col * nn + i] = g >= 0 ? ldg(V + int64_t(g) * nn + i) : T(0);
+          if (c.lane == 0) sN[col] = g >= 0 ? ldg(norms + g) : T(0);
         }
         __syncthreads();
-        any = round_rotations<T, false>(c, sW, mm, sV, nn, sN, b, la, lb, round == 0, mm, nn, tol);
-        for (int64_t e = c.tid; e < int64_t(2 * b) * mm; e += kThreads) {
-          const int col = int(e / mm);
-          const int g = col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1);
-          if (g >= 0) stg(W + int64_t(g) * mm + e % mm, sW[e]);
-        }
-        for (int64_t e = c.tid; e < int64_t(2 * b) * nn; e += kThreads) {
-          const int col = int(e / nn);
-          const int g = col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1);
-          if (g >= 0) stg(V + int64_t(g) * nn + e % nn, sV[e]);
-        }
-        for (int col = c.tid; col < 2 * b; col += kThreads) {
-          const int g = col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1);
-          if (g >= 0) stg(norms + g, sN[col]);
+        any = round_rotations<T>(c, sW, sV, sN, b, la, lb, round == 0, mm, nn, tol);
+        for (int col = c.warp; col < 2 * b; col += kWarps) {
+          const int g = gcol(col);
+          if (g < 0) continue;
+          for (int64_t i = c.lane; i < mm; i += 32) stg(W + int64_t(g) * mm + i, sW[col * mm + i]);
+          for (int i = c.lane; i < nn; i += 32) stg(V + int64_t(g) * nn + i, sV[col * nn + i]);
+          if (c.lane == 0) stg(norms + g, sN[col]);
         }
       } else {
-        // staging does not fit: rotate the columns in place in L2, with
+        // staging does not fit: rotate the columns in place in L2 with
         // per-pair pointers (the two blocks are not adjacent in memory)
         if (round == 0) {
           const int pa = la + (la & 1), pb = lb + (lb & 1);
@@ -247,6 +258,49 @@ __device__ int block_jacobi(cg::cluster_group& cl, const Ctx& c, T* W, T* V, T* 
     if (!any) break;
   }
   return sweeps;
+}
+
+// Small FP64 GEMM over the cluster: C (M x N) = op(A) (M x K) * B (K x N),
+// op(A)[i,l] = trans ? A[l + i*lda] : A[i + l*lda].  Output columns are split
+// over the CTAs; each CTA stages its columns of B in shared memory and every
+// thread accumulates one row of its column block in registers, so each A
+// element read from L2 feeds up to kCgemmCols FMAs.  post(i, j, acc) gives
+// the stored value.  Requires ceil(N / cluster) <= kCgemmCols.
+template <class F>
+__device__ void cgemm(const Ctx& c, int64_t M, int N, int K, const double* A, int64_t lda, bool trans, const double* B,
+                      int64_t ldb, double* C, int64_t ldc, double* sB, F post) {
+  const int cb = (N + kCluster - 1) / kCluster;
+  const int j0 = c.rank * cb;
+  const int nj = max(0, min(cb, N - j0));
+  for (int jj = c.warp; jj < nj; jj += kWarps)
+    for (int l = c.lane; l < K; l += 32) sB[l + jj * K] = ldg(B + l + int64_t(j0 + jj) * ldb);
+  __syncthreads();
+  for (int64_t i = c.tid; i < M; i += kThreads) {
+    double acc[kCgemmCols];
+#pragma unroll
+    for (int jj = 0; jj < kCgemmCols; ++jj) acc[jj] = 0.0;
+    int l = 0;
+    for (; l + 4 <= K; l += 4) {
+      double a[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = trans ? ldg(A + (l + u) + i * lda) : ldg(A + i + int64_t(l + u) * lda);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int jj = 0; jj < kCgemmCols; ++jj)
+          if (jj < nj) acc[jj] = fma(a[u], sB[l + u + jj * K], acc[jj]);
+    }
+    for (; l < K; ++l) {
+      const double a = trans ? ldg(A + l + i * lda) : ldg(A + i + int64_t(l) * lda);
+#pragma unroll
+      for (int jj = 0; jj < kCgemmCols; ++jj)
+        if (jj < nj) acc[jj] = fma(a, sB[l + jj * K], acc[jj]);
+    }
+#pragma unroll
+    for (int jj = 0; jj < kCgemmCols; ++jj)
+      if (jj < nj) stg(C + i + int64_t(j0 + jj) * ldc, post(i, j0 + jj, acc[jj]));
+  }
+  __syncthreads();
 }
 
 // Sign rule shared with the CPU oracle: s = sign(r . u) with the fixed
@@ -300,7 +354,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
   c.gtid = c.rank * kThreads + c.tid;
   c.gnt = kCluster * kThreads;
 
-  // workspace (doubles): W64 mm*nn | V64 nn*nn | T1 nn*nn | T2 nn*nn | n64 nn | flag 8 | floats: W32 | V32 | n32
+  // workspace (doubles): W64 mm*nn | V64 nn*nn | T1 nn*nn | T2 nn*nn | n64 nn | misc 8 | floats: W32 | V32 | n32
   const int64_t nn2 = int64_t(nn) * nn;
   double* W64 = work + work_off[sector];
   double* V64 = W64 + mm * nn;
@@ -308,6 +362,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
   double* T2 = T1 + nn2;
   double* n64 = T2 + nn2;
   int* flag = reinterpret_cast<int*>(n64 + nn);
+  unsigned long long* amax = reinterpret_cast<unsigned long long*>(n64 + nn + 1);
   float* W32 = reinterpret_cast<float*>(n64 + nn + 8);
   float* V32 = W32 + mm * nn;
   float* n32 = V32 + nn2;
@@ -316,55 +371,91 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
   const int b = (nn + kBlocks - 1) / kBlocks;
   const bool staged32 = int64_t(2 * b) * (mm + nn + 1) * 4 <= smem_bytes;
   const bool staged64 = int64_t(2 * b) * (mm + nn + 1) * 8 <= smem_bytes;
+  const long long t0 = clock64();
 
-  // ---- phase 1: FP32 block Jacobi
-  for (int64_t e = c.gtid; e < mm * nn; e += c.gnt) stg(W32 + e, float(opA(e % mm, e / mm)));
-  for (int64_t e = c.gtid; e < nn2; e += c.gnt) stg(V32 + e, (e % nn) == (e / nn) ? 1.f : 0.f);
+  // ---- phase 0: power-of-two scale for the FP32 copy
+  if (c.rank == 0 && c.tid == 0) atomicExch(amax, 0ull);
+  cl.sync();
+  {
+    double m = 0.0;
+    for (int j = c.gw; j < nn; j += c.gnw)
+      for (int64_t i = c.lane; i < mm; i += 32) m = fmax(m, fabs(opA(i, j)));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (c.lane == 0 && m > 0.0) atomicMax(amax, (unsigned long long)__double_as_longlong(m));
+  }
+  cl.sync();
+  const double amaxv = __longlong_as_double((long long)atomicAdd(amax, 0ull));
+  const double scale = amaxv > 0.0 ? pow2(-exponent_of(amaxv)) : 1.0;
+
+  // ---- phase 1: FP32 block Jacobi on the scaled copy
+  for (int j = c.gw; j < nn; j += c.gnw) {
+    for (int64_t i = c.lane; i < mm; i += 32) stg(W32 + int64_t(j) * mm + i, float(opA(i, j) * scale));
+    for (int i = c.lane; i < nn; i += 32) stg(V32 + int64_t(j) * nn + i, i == j ? 1.f : 0.f);
+  }
   cl.sync();
   const float tol32 = 8.0f * sqrtf(float(mm)) * 6.0e-8f;
   const int sw32 = nn > 1 ? block_jacobi<float>(cl, c, W32, V32, n32, flag, mm, nn, tol32, kMaxSweeps32,
                                                 reinterpret_cast<float*>(smem_raw), staged32)
                           : 0;
+  const long long t1 = clock64();
 
   // ---- phase 2: V = V32 (I - E/2 + 3E^2/8), E = V32^T V32 - I;  W64 = op(A) V
-  for (int64_t e = c.gtid; e < nn2; e += c.gnt) stg(V64 + e, double(ldg(V32 + e)));
-  cl.sync();
-  for (int64_t e = c.gtid; e < nn2; e += c.gnt) {  // T1 = E
-    const int64_t i = e % nn, j = e / nn;
-    double acc = 0;
-    for (int r = 0; r < nn; ++r) acc = fma(ldg(V64 + i * nn + r), ldg(V64 + j * nn + r), acc);
-    stg(T1 + e, acc - (i == j ? 1.0 : 0.0));
-  }
-  cl.sync();
-  for (int64_t e = c.gtid; e < nn2; e += c.gnt) {  // T2 = I - E/2 + 3/8 E^2
-    const int64_t i = e % nn, j = e / nn;
-    double acc = 0;
-    for (int r = 0; r < nn; ++r) acc = fma(ldg(T1 + i + int64_t(r) * nn), ldg(T1 + r + j * nn), acc);
-    stg(T2 + e, (i == j ? 1.0 : 0.0) - 0.5 * ldg(T1 + e) + 0.375 * acc);
-  }
-  cl.sync();
-  for (int64_t e = c.gtid; e < nn2; e += c.gnt) {  // T1 = V T2
-    const int64_t i = e % nn, j = e / nn;
-    double acc = 0;
-    for (int r = 0; r < nn; ++r) acc = fma(ldg(V64 + i + int64_t(r) * nn), ldg(T2 + r + j * nn), acc);
-    stg(T1 + e, acc);
-  }
+  for (int j = c.gw; j < nn; j += c.gnw)
+    for (int i = c.lane; i < nn; i += 32) stg(V64 + int64_t(j) * nn + i, double(ldg(V32 + int64_t(j) * nn + i)));
   cl.sync();
   double* V = T1;
-  for (int64_t e = c.gtid; e < mm * nn; e += c.gnt) {
-    const int64_t i = e % mm, j = e / mm;
-    const double* vj = V + j * nn;
-    double acc = 0;
-    for (int l = 0; l < nn; ++l) acc = fma(opA(i, l), ldg(vj + l), acc);
-    stg(W64 + e, acc);
+  double* sB = reinterpret_cast<double*>(smem_raw);
+  if (nn <= kCluster * kCgemmCols && int64_t(nn) * kCgemmCols * 8 <= smem_bytes) {
+    cgemm(c, nn, nn, nn, V64, nn, true, V64, nn, T1, nn, sB,
+          [&](int64_t i, int64_t j, double acc) { return acc - (i == j ? 1.0 : 0.0); });
+    cl.sync();
+    cgemm(c, nn, nn, nn, T1, nn, false, T1, nn, T2, nn, sB, [&](int64_t i, int64_t j, double acc) {
+      return (i == j ? 1.0 : 0.0) - 0.5 * ldg(T1 + i + j * nn) + 0.375 * acc;
+    });
+    cl.sync();
+    cgemm(c, nn, nn, nn, V64, nn, false, T2, nn, T1, nn, sB, [](int64_t, int64_t, double acc) { return acc; });
+    cl.sync();
+    cgemm(c, mm, nn, nn, A + d.a_off, d.m, tr, T1, nn, W64, mm, sB, [](int64_t, int64_t, double acc) { return acc; });
+    cl.sync();
+  } else {
+    for (int j = c.gw; j < nn; j += c.gnw)  // T1 = E
+      for (int i = c.lane; i < nn; i += 32) {
+        double acc = 0;
+        for (int r = 0; r < nn; ++r) acc = fma(ldg(V64 + int64_t(i) * nn + r), ldg(V64 + int64_t(j) * nn + r), acc);
+        stg(T1 + i + int64_t(j) * nn, acc - (i == j ? 1.0 : 0.0));
+      }
+    cl.sync();
+    for (int j = c.gw; j < nn; j += c.gnw)  // T2 = I - E/2 + 3/8 E^2
+      for (int i = c.lane; i < nn; i += 32) {
+        double acc = 0;
+        for (int r = 0; r < nn; ++r) acc = fma(ldg(T1 + i + int64_t(r) * nn), ldg(T1 + r + int64_t(j) * nn), acc);
+        stg(T2 + i + int64_t(j) * nn, (i == j ? 1.0 : 0.0) - 0.5 * ldg(T1 + i + int64_t(j) * nn) + 0.375 * acc);
+      }
+    cl.sync();
+    for (int j = c.gw; j < nn; j += c.gnw)  // T1 = V T2
+      for (int i = c.lane; i < nn; i += 32) {
+        double acc = 0;
+        for (int r = 0; r < nn; ++r) acc = fma(ldg(V64 + i + int64_t(r) * nn), ldg(T2 + r + int64_t(j) * nn), acc);
+        stg(T1 + i + int64_t(j) * nn, acc);
+      }
+    cl.sync();
+    for (int j = c.gw; j < nn; j += c.gnw)
+      for (int64_t i = c.lane; i < mm; i += 32) {
+        double acc = 0;
+        for (int l = 0; l < nn; ++l) acc = fma(opA(i, l), ldg(V + int64_t(j) * nn + l), acc);
+        stg(W64 + i + int64_t(j) * mm, acc);
+      }
+    cl.sync();
   }
-  cl.sync();
+  const long long t2 = clock64();
 
   // ---- phase 3: FP64 block Jacobi polish
   const double tol64 = 1.0e-13;
   const int sw64 = nn > 1 ? block_jacobi<double>(cl, c, W64, V, n64, flag, mm, nn, tol64, kMaxSweeps64,
                                                  reinterpret_cast<double*>(smem_raw), staged64)
                           : 0;
+  const long long t3 = clock64();
 
   // ---- phase 4: sort, sign, write
   double* sval = n64;
@@ -398,8 +489,13 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
     if (c.lane == 0) S[d.s_off + r] = sj;
   }
   if (sweep_stats && c.rank == 0 && c.tid == 0) {
-    sweep_stats[2 * sector] = sw32;
-    sweep_stats[2 * sector + 1] = sw64;
+    int* st6 = sweep_stats + 6 * sector;
+    st6[0] = sw32;
+    st6[1] = sw64;
+    st6[2] = int((t1 - t0) >> 10);  // phase cycles / 1024 on CTA 0's SM
+    st6[3] = int((t2 - t1) >> 10);
+    st6[4] = int((t3 - t2) >> 10);
+    st6[5] = int((clock64() - t3) >> 10);
   }
 }
 
@@ -421,7 +517,7 @@ void launch_svd(const xgb_svd_desc* d_descs, const int64_t* d_work_off, int n, i
   if (n <= 0) return;
   if (g_stats_cap < n) {
     if (g_stats_dev) cudaFree(g_stats_dev);
-    cudaMalloc(&g_stats_dev, sizeof(int) * 2 * n);
+    cudaMalloc(&g_stats_dev, sizeof(int) * 6 * n);
     g_stats_cap = n;
   }
   g_stats_n = n;
@@ -443,8 +539,8 @@ void launch_svd(const xgb_svd_desc* d_descs, const int64_t* d_work_off, int n, i
 extern "C" int xgb_svd_last_sweeps(int32_t* out, int cap) {
   using namespace xgb;
   if (!g_stats_dev || g_stats_n == 0) return 0;
-  const int n = std::min(cap / 2, g_stats_n);
+  const int n = std::min(cap / 6, g_stats_n);
   cudaStreamSynchronize(stream());
-  cudaMemcpy(out, g_stats_dev, sizeof(int) * 2 * n, cudaMemcpyDeviceToHost);
+  cudaMemcpy(out, g_stats_dev, sizeof(int) * 6 * n, cudaMemcpyDeviceToHost);
   return n;
 }
