@@ -133,6 +133,21 @@ size_t xgb_svd_workspace_bytes(int n, const xgb_svd_desc* descs);
 int xgb_batched_svd(int n, const xgb_svd_desc* descs, const double* A, double* U, double* S, double* Vt, void* work,
                     void* stream);
 
+/* xgb_batched_svd for callers that cannot allocate device memory (a plugin
+   whose host framework owns all device allocations, or a service with a
+   fixed device-memory budget).  No counterpart in the reference: it exists
+   only for embedders of this library.  Same descriptors and outputs as
+   xgb_batched_svd, but the workspace comes from one fixed 16 MiB device
+   array per GPU (xgb_batched_svd_noalloc_capacity_bytes()) that the library
+   holds until exit; batches needing more return XGB_E_UNSUPPORTED.  The
+   array's address is looked up on the first call on each device, so make
+   that first call before any stream capture.  All calls share the array:
+   calls that overlap on the GPU race and must be serialised by the caller.
+   Calls no cudaMalloc/cudaFree and returns after the stream has finished. */
+int xgb_batched_svd_noalloc(int n, const xgb_svd_desc* descs, const double* A, double* U, double* S, double* Vt,
+                            void* stream);
+size_t xgb_batched_svd_noalloc_capacity_bytes(void);
+
 /* Diagnostics of the last batched SVD, 6 ints per block: FP32 sweeps, FP64
    sweeps, then the cycles/1024 spent in the FP32 sweeps, the FP64
    re-orthonormalisation, the FP64 sweeps and the output stage; returns the

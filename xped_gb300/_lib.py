@@ -181,6 +181,8 @@ PROTOS_EXTRA = [
     ("xgb_event_record", C.c_int, [C.c_int]),
     ("xgb_event_elapsed_ms", C.c_double, [C.c_int, C.c_int]),
     ("xgb_svd_last_sweeps", C.c_int, [i32p, C.c_int]),
+    ("xgb_batched_svd_noalloc", C.c_int, [C.c_int, C.POINTER(SvdDesc), P, P, P, P, P]),
+    ("xgb_batched_svd_noalloc_capacity_bytes", C.c_size_t, []),
 ]
 PROTOS.extend(PROTOS_EXTRA)
 

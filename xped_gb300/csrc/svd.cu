@@ -38,6 +38,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <string>
+#include <vector>
 
 #include "kernels.hpp"
 
@@ -535,6 +537,83 @@ void launch_svd(const xgb_svd_desc* d_descs, const int64_t* d_work_off, int n, i
 }
 
 }  // namespace xgb
+
+// ---------------------------------------------------------------------------
+// Batched SVD for callers that cannot allocate device memory.
+//
+// Some embedders of this library may not call cudaMalloc at all: a plugin
+// whose host framework owns every device allocation through its own memory
+// pool, or a service that fixes its device-memory budget up front and
+// forbids allocations on the request path.  For them the SVD workspace (and the small
+// descriptor tables) live in one file-scope device array of kNoAllocDoubles
+// doubles (16 MiB) that every GPU loading the library keeps until exit.  The
+// array's device address is looked up once per device with
+// cudaGetSymbolAddress on that device's first call (make that first call
+// before any stream capture begins).  All calls share the array and it keeps
+// the previous call's contents; the kernel overwrites every workspace entry
+// it reads, so nothing needs clearing between calls.  Two calls whose work
+// overlaps on the GPU (different streams, or concurrent host threads) race on
+// the array and must be serialised by the caller.
+namespace xgb {
+namespace {
+constexpr size_t kNoAllocDoubles = size_t(2) << 20;  // 16 MiB
+__device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+double* g_noalloc_ptr[64] = {nullptr};
+}  // namespace
+}  // namespace xgb
+
+extern "C" size_t xgb_batched_svd_noalloc_capacity_bytes(void) { return xgb::kNoAllocDoubles * sizeof(double); }
+
+extern "C" int xgb_batched_svd_noalloc(int n, const xgb_svd_desc* descs, const double* A, double* U, double* S,
+                                       double* Vt, void* stream_) {
+  using namespace xgb;
+  if (n <= 0) return XGB_OK;
+  if (!descs) return set_error(XGB_E_BADPLAN, "xgb_batched_svd_noalloc: descriptor array is NULL");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return set_error(XGB_E_CUDA, "xgb_batched_svd_noalloc: no current CUDA device");
+  // bytes needed: descriptors, work offsets, then the per-block workspaces
+  const size_t desc_doubles = (sizeof(xgb_svd_desc) * size_t(n) + 255) / 256 * 32;
+  const size_t off_doubles = (sizeof(int64_t) * size_t(n) + 255) / 256 * 32;
+  std::vector<int64_t> off(static_cast<size_t>(n));
+  size_t work = 0;
+  for (int i = 0; i < n; ++i) {
+    if (descs[i].m < 0 || descs[i].n < 0) return set_error(XGB_E_BADPLAN, "xgb_batched_svd_noalloc: negative extent");
+    off[i] = int64_t(work);
+    work += svd_work_elems(descs[i].m, descs[i].n);
+  }
+  const size_t need = desc_doubles + off_doubles + work;
+  if (need > kNoAllocDoubles)
+    return set_error(XGB_E_UNSUPPORTED,
+                     "xgb_batched_svd_noalloc: the batch needs " + std::to_string(need * 8) +
+                         " bytes of workspace, above the fixed capacity of " + std::to_string(kNoAllocDoubles * 8) +
+                         " bytes; use xgb_batched_svd with caller-provided workspace");
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return set_error(XGB_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  double* base = g_noalloc_ptr[dev];
+  auto* d_descs = reinterpret_cast<xgb_svd_desc*>(base);
+  auto* d_off = reinterpret_cast<int64_t*>(base + desc_doubles);
+  double* d_work = base + desc_doubles + off_doubles;
+  cudaStream_t s = stream_ ? static_cast<cudaStream_t>(stream_) : stream();
+  cudaError_t e = cudaMemcpyAsync(d_descs, descs, sizeof(xgb_svd_desc) * size_t(n), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, off.data(), sizeof(int64_t) * size_t(n), cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return set_error(XGB_E_CUDA, std::string("descriptor copy: ") + cudaGetErrorString(e));
+  cudaFuncSetAttribute(svd_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+  svd_cluster_kernel<<<n * kCluster, kThreads, kSmemLimit, s>>>(d_descs, d_off, A, U, S, Vt, d_work, nullptr,
+                                                                kSmemLimit);
+  count_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(XGB_E_CUDA, std::string("svd launch: ") + cudaGetErrorString(e));
+  // the descriptor copies read pageable host memory that the caller may free
+  // on return, so wait for them (and the kernel) before returning
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return set_error(XGB_E_CUDA, std::string("svd: ") + cudaGetErrorString(e));
+  return XGB_OK;
+}
 
 extern "C" int xgb_svd_last_sweeps(int32_t* out, int cap) {
   using namespace xgb;
