@@ -208,11 +208,13 @@ def roofline(prof, steps):
     n, ms, work = kinds[dom]
     per_launch_ms = ms / n
     per_launch_work = work / n
-    if dom.startswith("gemm"):
-        # FP64 runs on the DFMA pipe; GB300's nominal dense FP64 rate is 1.25 TFLOP/s
+    if dom in ("gemm_f64", "svd_jacobi", "qr"):
+        # FP64 runs on the DFMA pipe; GB300's nominal dense FP64 rate is 1.25 TFLOP/s.
+        # SVD work is counted as LAPACK dgesvd-equivalent flops (4m^2n + 8mn^2 + 9n^3, m >= n).
         achieved = per_launch_work / (per_launch_ms * 1e-3) / 1e12
         out = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
-               "peak_source": "nominal GB300 FP64 (not in MEASURED_PEAKS.json)"}
+               "peak_source": "nominal GB300 FP64 rate (MEASURED_PEAKS.json has no FP64 figure)",
+               "work": "LAPACK-equivalent flops" if dom == "svd_jacobi" else "useful flops"}
     else:
         achieved = per_launch_work / (per_launch_ms * 1e-3) / 1e9
         out = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",

@@ -625,6 +625,7 @@ namespace {
 struct SvdPlan {
   int n = 0;
   int64_t u_total = 0, s_total = 0, v_total = 0, work_total = 0, maxk = 0;
+  double lapack_flops = 0;  // dgesvd-equivalent work: 4m^2n + 8mn^2 + 9n^3 (m >= n)
   std::vector<int64_t> s_begin;  // per sector prefix (host), size n+1
   std::vector<int64_t> u_off, s_off, v_off, kfull;
   xgb_svd_desc* d_descs = nullptr;
@@ -659,6 +660,10 @@ std::shared_ptr<SvdPlan> get_svd_plan(const TensorMeta& m) {
     woff.push_back(p->work_total);
     p->work_total += int64_t(svd_work_elems(r, c));
     p->maxk = std::max(p->maxk, k);
+    {
+      const double M = double(std::max(r, c)), N = double(std::min(r, c));
+      p->lapack_flops += 4.0 * M * M * N + 8.0 * M * N * N + 9.0 * N * N * N;
+    }
     descs.push_back(d);
     deg.push_back(m.sym.deg(m.sectors[i]));
     p->s_begin.push_back(p->s_total);
@@ -687,7 +692,7 @@ SVDResult tsvd(const Tensor& t0, int64_t max_keep, double eps_svd, bool preserve
   double* W = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->work_total, 1)));
   prof_begin(K_SVD, st);
   launch_svd(plan->d_descs, plan->d_work_off, plan->n, plan->maxk, t.data(), U, S, V, W, st);
-  prof_end(K_SVD, st, 8.0 * double(m.size + plan->u_total + plan->s_total + plan->v_total));
+  prof_end(K_SVD, st, plan->lapack_flops);
   dev_free(W);
   if (plan->s_total == 0) throw std::runtime_error("tSVD: no singular values");
   int32_t* keep_d = static_cast<int32_t*>(dev_alloc(sizeof(int32_t) * plan->n));
