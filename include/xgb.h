@@ -71,7 +71,8 @@ int64_t xgb_launch_count(void);
 void* xgb_stream_handle(void);
 /* Instrumentation: with profiling enabled every launch is bracketed by CUDA
    events on the library stream.  kind: 0 gemm, 1 permute, 2 svd, 3 truncate,
-   4 qr, 5 absmax, 6 scale, 7 copy2d, 8 diag, 9 tensor-core gemm.  work is the
+   4 qr, 5 absmax, 6 scale, 7 copy2d, 8 diag, 9 tensor-core gemm, 10 sketch
+   (Gaussian test matrices, sign fixing), 11 rank-predictor MLP.  work is the
    algorithmic flop count (GEMMs) or bytes moved (everything else). */
 int xgb_profile_enable(int on);
 int xgb_profile_reset(void);
@@ -89,9 +90,15 @@ typedef struct xgb_gemm_desc {
   int32_t trans_a, trans_b;
 } xgb_gemm_desc;
 
-/* C_g = alpha * op(A_g) op(B_g) + beta * C_g for every group g, one launch. */
+/* C_g = alpha * op(A_g) op(B_g) + beta * C_g for every group g, one launch.
+   precision XGB_PREC_FP64: FP64 FMA; XGB_PREC_3XTF32: FP64 in and out, products
+   as three TF32 tensor-core products (hi*hi + hi*lo + lo*hi) accumulated in FP32
+   (about 1e-6 relative); XGB_PREC_BF16X9 is not available (XGB_E_UNSUPPORTED). */
 int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, const double* A, const double* B,
                      double* C, double alpha, double beta, void* stream);
+/* Synchronises and reports whether a tensor-core GEMM CTA gave up on a bounded
+   wait since the last call (XGB_E_TIMEOUT) - no counterpart in the reference. */
+int xgb_gemm_tc_status(void);
 
 /* ------------------------------------------------------------------ permute */
 #define XGB_MAX_LEGS 8

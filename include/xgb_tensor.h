@@ -23,6 +23,7 @@ extern "C" {
 typedef struct xgb_basis_s* xgb_basis;
 typedef struct xgb_tensor_s* xgb_tensor;
 typedef struct xgb_ctm_s* xgb_ctm;
+typedef struct xgb_rank_model_s* xgb_rank_model;
 
 /* symmetry kinds */
 enum { XGB_SYM_U1 = 0, XGB_SYM_U1_FERMIONIC = 1, XGB_SYM_Z2 = 2, XGB_SYM_Z2_FERMIONIC = 3, XGB_SYM_SU2 = 4 };
@@ -72,6 +73,17 @@ xgb_tensor xgb_tensor_normalize_max(xgb_tensor t);                              
 /* Tensor::tSVD (Tensor.cpp:478-633); keep[] (may be NULL, one per input sector) gets kept counts */
 int xgb_tensor_tsvd(xgb_tensor t, int64_t max_keep, double eps_svd, int preserve_multiplets, xgb_tensor* U,
                     xgb_tensor* S, xgb_tensor* Vdag, double* trunc_weight, double* entropy, int32_t* keep);
+/* Randomized blockwise tSVD with per-sector sketch widths (no counterpart in the
+   reference; its results follow Tensor::tSVD's cutoff_matrices semantics).
+   sketch[i] <= 0 or 2*sketch[i] >= min(rows, cols) decomposes sector i exactly;
+   power_iters subspace iterations; Gaussian test matrices from `seed`.  A sketched
+   sector that keeps all of its sketch is redone exactly (n_saturated counts them).
+   keep[] and width[] (may be NULL) get, per input sector, the kept count and the
+   sketch width used (min(rows, cols) for exact sectors). */
+int xgb_tensor_tsvd_randomized(xgb_tensor t, int64_t max_keep, double eps_svd, int n_sectors, const int64_t* sketch,
+                               int power_iters, uint64_t seed, xgb_tensor* U, xgb_tensor* S, xgb_tensor* Vdag,
+                               double* trunc_weight, double* entropy, int32_t* keep, int64_t* width,
+                               int32_t* n_saturated);
 int xgb_tensor_tqr(xgb_tensor t, xgb_tensor* Q, xgb_tensor* R);                    /* Tensor::tQR (Tensor.cpp:757-780) */
 /* decompose (src/PEPS/PEPSContractions.cpp:16-43) */
 int xgb_decompose(xgb_tensor t1, xgb_tensor t2, int64_t max_nsv, xgb_tensor* P1, xgb_tensor* P2);
@@ -87,6 +99,48 @@ int xgb_ctm_move(xgb_ctm c, char dir);                      /* 'L','R','T','B' m
 xgb_tensor xgb_ctm_get(xgb_ctm c, int which);
 int xgb_ctm_set(xgb_ctm c, int which, xgb_tensor t);
 void xgb_ctm_release(xgb_ctm c);
+/* Projector SVD form of the moves (no counterpart in the reference, which always
+   runs the full tSVD): mode 0 exact FP64 tSVD, mode 1 randomized tSVD whose sketch
+   widths are the direction's last kept counts + max(oversample, growth * kept)
+   (exact for sectors not seen before); power_iters subspace iterations. */
+int xgb_ctm_set_svd(xgb_ctm c, int mode, int power_iters, uint64_t seed, int64_t oversample, double growth);
+/* out5: decompositions, sketched sectors, exact sectors, sketch redos, sketch columns */
+int xgb_ctm_stats(xgb_ctm c, int64_t* out5);
+/* Decomposition log for learning sketch widths (features of the rank predictor,
+   kept counts, widths, min(rows, cols), full computed spectra). on = 0 clears it. */
+int xgb_ctm_record(xgb_ctm c, int on);
+int xgb_ctm_record_count(xgb_ctm c);
+int xgb_ctm_record_get(xgb_ctm c, int i, int* dir, int* n_sectors, int64_t* n_spectrum, int32_t* sectors,
+                       float* features, int64_t* keep, int64_t* width, int64_t* kmin, double* spectrum,
+                       int64_t* spec_begin);
+/* computeRDM_h (vertical = 0) / computeRDM_v (vertical = 1), normalised
+   (src/PEPS/CTM.cpp:583-627, 756-790) */
+xgb_tensor xgb_ctm_rdm(xgb_ctm c, int vertical);
+/* Learned sketch widths (no counterpart in the reference).  A small MLP
+   (xgb_rank_model_num_features() inputs per sector -> 3 x 64 ReLU -> 2 outputs,
+   FP32) predicts log2(1 + kept count) and log2(1 + oversampling) of each sector of
+   a projector decomposition from its shape and the direction's last spectrum;
+   forward, backward and Adam run on the device.  Parameters are packed W1, b1,
+   W2, b2, W3, b3, W4, b4 with row-major W[out][in]; loss = mean over samples of
+   half the squared error summed over both outputs.  X is n x features, T and Y
+   n x 2, row-major host arrays. */
+int xgb_rank_model_num_params(void);
+int xgb_rank_model_num_features(void);
+xgb_rank_model xgb_rank_model_create(uint64_t seed);
+void xgb_rank_model_release(xgb_rank_model m);
+int xgb_rank_model_get_params(xgb_rank_model m, float* out, int cap);
+int xgb_rank_model_set_params(xgb_rank_model m, const float* in, int n);  /* also resets the Adam state */
+int xgb_rank_model_predict(xgb_rank_model m, const float* X, int64_t n, float* Y);
+int xgb_rank_model_gradient(xgb_rank_model m, const float* X, const float* T, int64_t n, float* grad, double* loss);
+/* steps full-batch Adam steps (beta 0.9 / 0.999, eps 1e-8); loss before the last step */
+int xgb_rank_model_train(xgb_rank_model m, const float* X, const float* T, int64_t n, int steps, float lr,
+                         double* loss);
+/* Switch the CTM to the randomized projector SVD with model-predicted widths:
+   ceil(k * (1 + margin)) + max(min_oversample, ceil(p)) columns per sector. */
+int xgb_ctm_set_rank_model(xgb_ctm c, xgb_rank_model m, double margin, int64_t min_oversample, int power_iters,
+                           uint64_t seed);
+/* avg of a two-site operator on a bond RDM (src/PEPS/LinearAlgebra.cpp:58-64) */
+int xgb_tensor_bond_expectation(xgb_tensor rho, xgb_tensor op, double* out);
 
 /* ------------------------------------------------- host-only planning */
 /* Metadata-only tensor (no device memory): sectors, blocks and the plans below

@@ -10,6 +10,8 @@ PROJECTION::CORNER.  References:
   renormalize_*:         src/PEPS/CTM.cpp:1339-1641
   contractCorner:        src/PEPS/CTM.cpp:1643-1760
   decompose:             src/PEPS/PEPSContractions.cpp:16-43
+  computeRDM_h / _v:     src/PEPS/CTM.cpp:530-698, 700-876 (TRank == 2 branch)
+  avg (two-site op):     src/PEPS/LinearAlgebra.cpp:36-80
 On a 1x1 cell every (x +- 1, y +- 1) index refers to the same site tensors.
 """
 from __future__ import annotations
@@ -205,9 +207,94 @@ class CTM:
             self.move(d)
         return self
 
+    # -- reduced density matrices and bond energies ---------------------------------
+    def rdm_h(self):
+        """computeRDM_h, TRank == 2 (CTM.cpp:583-619): rho_h Tensor<2,2>
+        (left phys, right phys | left phys', right phys'), normalised."""
+        A, Ad = self.peps.A, self.peps.Adag
+        C1T1 = self.C1.contract(self.T1, [-1, 1], [1, -2, -3, -4], 1)
+        T4C1T1 = self.T4.contract(C1T1.twist(0), [1, -1, -2, -3], [1, -4, -5, -6], 3)
+        T4C1T1A = T4C1T1.contract(A, [-1, 1, -2, -3, 2, -4], [1, 2, -5, -6, -7], 4)
+        C4T3 = self.C4.contract(self.T3, [-1, 1], [-2, -3, 1, -4], 1)
+        C4T3Ad = C4T3.contract(Ad.twist(3), [-1, -2, 1, -3], [-4, -5, -6, -7, 1], 3)
+        left = T4C1T1A.contract(C4T3Ad, [1, 2, -1, 3, -2, 4, -3], [1, 4, -4, 2, 3, -5, -6], 3)
+        T1C2 = self.T1.contract(self.C2, [-1, 1, -2, -3], [1, -4], 3)
+        T1C2T2 = T1C2.contract(self.T2, [-1, -2, -3, 1], [-4, -5, 1, -6], 3)
+        AT1C2T2 = A.twist(1).contract(T1C2T2, [-1, 1, 2, -2, -3], [-4, 1, -5, 2, -6, -7], 3)
+        T3C3 = self.T3.contract(self.C3, [-1, -2, -3, 1], [-4, 1], 3)
+        T3C3Ad = T3C3.contract(Ad, [-1, 1, -2, -3], [-4, -5, -6, -7, 1], 3)
+        right = AT1C2T2.contract(T3C3Ad, [-1, 1, -2, -3, 2, 3, 4], [1, -4, 4, -5, 2, -6, 3], 3)
+        rho = left.contract(right, [1, 2, -3, 3, -1, 4], [2, -4, 1, 3, 4, -2], 2)
+        return _normalise_rdm(rho)
+
+    def rdm_v(self):
+        """computeRDM_v, TRank == 2 (CTM.cpp:756-781): rho_v Tensor<2,2>
+        (upper phys, lower phys | upper phys', lower phys'), normalised."""
+        A, Ad = self.peps.A, self.peps.Adag
+        C1T1 = self.C1.contract(self.T1, [-1, 1], [1, -2, -3, -4], 1)
+        T4C1T1 = self.T4.contract(C1T1.twist(0), [1, -1, -2, -3], [1, -4, -5, -6], 3)
+        T4C1T1A = T4C1T1.contract(A, [-1, 1, -2, -3, 2, -4], [1, 2, -5, -6, -7], 4)
+        C2T2 = self.C2.contract(self.T2, [-1, 1], [-2, -3, 1, -4], 1)
+        AdC2T2 = Ad.twist(3).twist(4).contract(C2T2, [-1, -2, -3, 1, -4], [-5, -6, 1, -7], 4)
+        upper = T4C1T1A.contract(AdC2T2, [-1, 1, 2, 3, 4, -2, -3], [1, 3, -4, -5, 2, 4, -6], 3)
+        C4T3 = self.C4.contract(self.T3, [-1, 1], [-2, -3, 1, -4], 1)
+        T4C4T3 = self.T4.contract(C4T3, [-1, 1, -2, -3], [1, -4, -5, -6], 3)
+        AT4C4T3 = A.twist(0).contract(T4C4T3, [1, -1, -2, 2, -3], [-4, 1, -5, 2, -6, -7], 3)
+        T2C3 = self.T2.contract(self.C3, [-1, -2, -3, 1], [1, -4], 3)
+        T2C3Ad = T2C3.contract(Ad, [-1, 1, -2, -3], [-4, -5, -6, 1, -7], 3)
+        lower = AT4C4T3.contract(T2C3Ad, [-1, 1, -2, -3, 2, 3, 4], [1, -4, 4, 2, -5, -6, 3], 3)
+        rho = upper.contract(lower, [1, 2, -3, -1, 3, 4], [2, -4, 1, 4, 3, -2], 2)
+        return _normalise_rdm(rho)
+
     def env(self):
         return dict(C1=self.C1, C2=self.C2, C3=self.C3, C4=self.C4,
                     T1=self.T1, T2=self.T2, T3=self.T3, T4=self.T4)
+
+
+def _normalise_rdm(rho):
+    """rho / tr(rho Id2.twist(0).twist(1)) (CTM.cpp:620-627)."""
+    Id2 = Tensor.identity(rho.sym, rho.cod, rho.dom)
+    norm = rho.contract(Id2.twist(0).twist(1), [1, 2, 3, 4], [3, 4, 1, 2], 0).trace()
+    return rho.scale(1.0 / norm)
+
+
+def bond_expectation(rho, op):
+    """avg for a two-site operator (LinearAlgebra.cpp:58-64):
+    tr(rho.twist(0).twist(1) contracted with op)."""
+    return rho.twist(0).twist(1).contract(op, [1, 2, 3, 4], [3, 4, 1, 2], 0).trace()
+
+
+def heisenberg_u1(sym, phys: Qbasis, J=1.0):
+    """Spin-1/2 Heisenberg bond J (Sz Sz + (S+ S- + S- S+)/2) as a U(1)
+    Tensor<2,2>({phys, phys}, {phys, phys}); phys charges are 2 Sz = -1, +1
+    with degeneracy 1.  Built from its dense 4x4 matrix in the product basis
+    |s1 s2> (s1 fastest) by projecting onto each coupled sector."""
+    sz = {-1: -0.5, 1: 0.5}
+    H = Tensor(sym, [phys, phys], [phys, phys])
+    for i, q in enumerate(H.sectors):
+        rows = _product_states(H.cdom, q)
+        cols = _product_states(H.ccod, q)
+        blk = np.zeros((len(rows), len(cols)))
+        for r, (a1, a2) in enumerate(rows):
+            for c, (b1, b2) in enumerate(cols):
+                v = 0.0
+                if (a1, a2) == (b1, b2):
+                    v += sz[a1] * sz[a2]
+                if a1 == b2 and a2 == b1 and a1 != a2:
+                    v += 0.5
+                blk[r, c] = J * v
+        H.blocks[i] = blk
+    return H
+
+
+def _product_states(cbasis, q):
+    """(q1, q2) of each row of coupled sector q, in the sector's fusion-tree
+    order (every degeneracy is 1 for the spin-1/2 leg)."""
+    out = []
+    for t in cbasis.trees[q]:
+        assert all(d == 1 for d in t.dims)
+        out.append(tuple(t.qu))
+    return out
 
 
 def _twists(T, legs):

@@ -1,0 +1,113 @@
+"""Randomized blockwise tSVD restated in numpy (test infrastructure only).
+
+The randomized form has no counterpart in the reference; its contract is
+the reference's Tensor::tSVD (src/Core/Tensor.cpp:478-633): the same
+truncation (cutoff_matrices, Tensor.cpp:523-633) applied to per-sector
+spectra that come from a sketch instead of a full SVD.  This module follows
+the device algorithm step by step so both can be compared on the same
+seeded test matrices:
+
+  Omega_i = N(0,1) from (seed, stream i)          n_i x l_i
+  Q = orth(A Omega)                               left singular vectors
+  repeat p times: Q = orth(A orth(A^T Q))
+  B = Q^T A = U_B S V^T ,  U = Q U_B ,  sign convention of fix_svd_signs
+
+A sector is decomposed exactly if l_i <= 0 or 2 l_i >= min(m_i, n_i); a
+sketched sector that keeps all l_i of its values is redone with 2 l_i
+columns (the same Gaussian stream, extended), exactly after the third
+doubling.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.linalg as sla
+
+from .basis import Qbasis
+from .tensor import Tensor, cutoff_matrices, fix_svd_signs
+
+
+
+MAX_RETRIES = 3
+
+
+def _mix64(z):
+    """splitmix64 finaliser on uint64 arrays (wrapping arithmetic)."""
+    with np.errstate(over="ignore"):
+        z = z + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def gaussian(seed: int, stream: int, count: int) -> np.ndarray:
+    """Counter-based N(0,1) numbers: Box-Muller on hashed uniforms
+    u1 = ((h1 >> 11) + 1) 2^-53 in (0, 1], u2 = (h2 >> 11) 2^-53."""
+    base = _mix64(np.uint64(seed) ^ _mix64(np.array([stream], dtype=np.uint64)))[0]
+    e = np.arange(count, dtype=np.uint64)
+    h1 = _mix64(base ^ (np.uint64(2) * e))
+    h2 = _mix64(base ^ (np.uint64(2) * e + np.uint64(1)))
+    u1 = ((h1 >> np.uint64(11)).astype(np.float64) + 1.0) * 2.0 ** -53
+    u2 = (h2 >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+    return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+
+
+def _orth(Y):
+    return np.linalg.svd(Y, full_matrices=False)[0]
+
+
+def sketch_svd(A, l, power_iters, seed, stream):
+    """Rank-l randomized SVD of one block (U m x l, s l, Vt l x n), sign-fixed."""
+    m, n = A.shape
+    Om = gaussian(seed, stream, n * l).reshape((n, l), order="F")
+    Q = _orth(A @ Om)
+    for _ in range(power_iters):
+        Q = _orth(A @ _orth(A.T @ Q))
+    ub, s, vt = np.linalg.svd(Q.T @ A, full_matrices=False)
+    u, vt = fix_svd_signs(Q @ ub, vt)
+    return u, s, vt
+
+
+def tsvd_randomized(T: Tensor, max_keep, eps_svd, sketch, power_iters=1, seed=0):
+    """Returns (U, S, Vdag, truncWeight, entropy, keep, width, n_saturated)."""
+    n = len(T.sectors)
+    assert len(sketch) == n
+    exact = [False] * n
+    want = [int(x) for x in sketch]
+    saturated = 0
+    for rnd in range(MAX_RETRIES + 1):
+        width = []
+        for i, b in enumerate(T.blocks):
+            kmin = min(b.shape)
+            l = want[i]
+            if exact[i] or l <= 0 or 2 * l >= kmin:
+                exact[i] = True
+                l = kmin
+            width.append(l)
+        sym = T.sym
+        middle = Qbasis(sym, 1)
+        for q, l in zip(T.sectors, width):
+            middle.push_back(q, l)
+        U = Tensor(sym, T.dom, [middle], fill=False)
+        S = Tensor(sym, [middle], [middle], fill=False)
+        Vd = Tensor(sym, [middle], T.cod, fill=False)
+        allsv = []
+        for i, (q, b) in enumerate(zip(T.sectors, T.blocks)):
+            if exact[i]:
+                u, s, vt = sla.svd(b, full_matrices=False, lapack_driver="gesvd")
+                u, vt = fix_svd_signs(u, vt)
+            else:
+                u, s, vt = sketch_svd(b, width[i], power_iters, seed, i)
+            allsv.extend((q, float(v)) for v in s)
+            U.push_back(q, u)
+            S.push_back(q, np.diag(s))
+            Vd.push_back(q, vt)
+        oU, oS, oV, tw, ent = cutoff_matrices(T, U, S, Vd, allsv, max_keep, eps_svd, False, False)
+        keep = [oS.block(q).shape[0] if q in oS._dict else 0 for q in T.sectors]
+        sat = [i for i in range(n) if not exact[i] and keep[i] >= width[i]]
+        if not sat:
+            return oU, oS, oV, tw, ent, keep, width, saturated
+        for i in sat:
+            want[i] = 2 * width[i]
+            if rnd + 1 >= MAX_RETRIES:
+                exact[i] = True
+        saturated += len(sat)

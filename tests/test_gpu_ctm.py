@@ -63,3 +63,46 @@ def test_ctm_fermionic_z2():
         oc.grow_all()
         nc.grow_all()
     _compare(oc, nc, 1e-8)
+
+
+def test_rdm_and_energy_match_oracle():
+    """computeRDM_h / computeRDM_v and the Heisenberg bond energies after three steps."""
+    from oracle.ctm import bond_expectation as obond
+    from oracle.ctm import heisenberg_u1
+    from xped_gb300 import bond_expectation
+    from xped_gb300.observables import heisenberg_bond
+    oc, nc = _setup("u1", [(-1, 1), (0, 2), (1, 1)], [(-1, 1), (1, 1)], 12, 0)
+    for _ in range(3):
+        oc.grow_all()
+        nc.grow_all()
+    s = oracle.make_symmetry("u1")
+    oH = heisenberg_u1(s, oc.peps.A.cod[2])
+    nH = heisenberg_bond(nc.get("A").leg(4))
+    assert_same(nH, oH, 0, 0)
+    for orho, nrho in ((oc.rdm_h(), nc.rdm_h()), (oc.rdm_v(), nc.rdm_v())):
+        assert_same(nrho, orho, 1e-8, 1e-10)
+        assert abs(bond_expectation(nrho, nH) - obond(orho, oH)) < 1e-10
+
+
+def test_randomized_projectors_keep_the_energy():
+    """Chosen form (randomized projector SVD with history widths: three
+    subspace iterations, last kept + max(16, 50 %) columns) against the exact
+    FP64 tSVD on the GPU: same kept counts every step and the same energy per
+    site to 1e-8."""
+    from xped_gb300.observables import energy, heisenberg_bond
+    _, ex = _setup("u1", [(-1, 1), (0, 2), (1, 1)], [(-1, 1), (1, 1)], 32, 7)
+    _, rz = _setup("u1", [(-1, 1), (0, 2), (1, 1)], [(-1, 1), (1, 1)], 32, 7)
+    rz.set_svd("randomized", power_iters=3, oversample=16, growth=0.5)
+    ex.record(True)
+    rz.record(True)
+    for _ in range(6):
+        ex.grow_all()
+        rz.grow_all()
+    H = heisenberg_bond(ex.get("A").leg(4))
+    e_ex, e_rz = energy(ex, H), energy(rz, H)
+    assert abs(e_ex - e_rz) < 1e-8, (e_ex, e_rz)
+    st = rz.stats()
+    assert st["sketched_sectors"] > 0
+    for a, b in zip(ex.records(), rz.records()):
+        assert a["sectors"] == b["sectors"]
+        assert list(a["keep"]) == list(b["keep"])

@@ -48,6 +48,7 @@ P = C.c_void_p
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
 dblp = C.POINTER(C.c_double)
+fltp = C.POINTER(C.c_float)
 
 # (name, restype, argtypes)
 PROTOS = [
@@ -104,12 +105,32 @@ PROTOS = [
     ("xgb_tensor_normalize_max", P, [P]),
     ("xgb_tensor_tsvd", C.c_int, [P, C.c_int64, C.c_double, C.c_int, C.POINTER(P), C.POINTER(P), C.POINTER(P),
                                   dblp, dblp, i32p]),
+    ("xgb_tensor_tsvd_randomized", C.c_int, [P, C.c_int64, C.c_double, C.c_int, i64p, C.c_int, C.c_uint64,
+                                             C.POINTER(P), C.POINTER(P), C.POINTER(P), dblp, dblp, i32p, i64p, i32p]),
     ("xgb_tensor_tqr", C.c_int, [P, C.POINTER(P), C.POINTER(P)]),
     ("xgb_decompose", C.c_int, [P, P, C.c_int64, C.POINTER(P), C.POINTER(P)]),
     ("xgb_tensor_release", None, [P]),
     ("xgb_ctm_create", P, [P, C.c_int64]),
     ("xgb_ctm_init", C.c_int, [P]),
     ("xgb_ctm_grow_all", C.c_int, [P]),
+    ("xgb_ctm_set_svd", C.c_int, [P, C.c_int, C.c_int, C.c_uint64, C.c_int64, C.c_double]),
+    ("xgb_ctm_stats", C.c_int, [P, i64p]),
+    ("xgb_ctm_record", C.c_int, [P, C.c_int]),
+    ("xgb_ctm_record_count", C.c_int, [P]),
+    ("xgb_ctm_record_get", C.c_int, [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), i64p, i32p,
+                                     C.POINTER(C.c_float), i64p, i64p, i64p, dblp, i64p]),
+    ("xgb_ctm_rdm", P, [P, C.c_int]),
+    ("xgb_rank_model_num_params", C.c_int, []),
+    ("xgb_rank_model_num_features", C.c_int, []),
+    ("xgb_rank_model_create", P, [C.c_uint64]),
+    ("xgb_rank_model_release", None, [P]),
+    ("xgb_rank_model_get_params", C.c_int, [P, fltp, C.c_int]),
+    ("xgb_rank_model_set_params", C.c_int, [P, fltp, C.c_int]),
+    ("xgb_rank_model_predict", C.c_int, [P, fltp, C.c_int64, fltp]),
+    ("xgb_rank_model_gradient", C.c_int, [P, fltp, fltp, C.c_int64, fltp, dblp]),
+    ("xgb_rank_model_train", C.c_int, [P, fltp, fltp, C.c_int64, C.c_int, C.c_float, dblp]),
+    ("xgb_ctm_set_rank_model", C.c_int, [P, P, C.c_double, C.c_int64, C.c_int, C.c_uint64]),
+    ("xgb_tensor_bond_expectation", C.c_int, [P, P, dblp]),
     ("xgb_ctm_move", C.c_int, [P, C.c_char]),
     ("xgb_ctm_get", P, [P, C.c_int]),
     ("xgb_ctm_set", C.c_int, [P, C.c_int, P]),
@@ -175,6 +196,7 @@ def ensure_device(device: int = 0):
 
 PROTOS_EXTRA = [
     ("xgb_stream_handle", C.c_void_p, []),
+    ("xgb_gemm_tc_status", C.c_int, []),
     ("xgb_profile_enable", C.c_int, [C.c_int]),
     ("xgb_profile_reset", C.c_int, []),
     ("xgb_profile_read", C.c_int, [C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -186,7 +208,7 @@ PROTOS_EXTRA = [
 ]
 PROTOS.extend(PROTOS_EXTRA)
 
-KERNEL_KINDS = ["gemm_f64", "permute", "svd_jacobi", "truncate", "qr", "absmax", "scale", "copy2d", "diag", "gemm_tc"]
+KERNEL_KINDS = ["gemm_f64", "permute", "svd_jacobi", "truncate", "qr", "absmax", "scale", "copy2d", "diag", "gemm_tc", "sketch", "mlp"]
 
 
 def profile_read():

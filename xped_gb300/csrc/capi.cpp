@@ -7,6 +7,7 @@
 #include <stdexcept>
 
 #include "../../include/xgb_tensor.h"
+#include "rank_model.hpp"
 #include "tensor.hpp"
 
 struct xgb_basis_s { xgb::BasisPtr b; };
@@ -201,6 +202,28 @@ int xgb_tensor_tsvd(xgb_tensor t, int64_t max_keep, double eps_svd, int preserve
   })
 }
 
+int xgb_tensor_tsvd_randomized(xgb_tensor t, int64_t max_keep, double eps_svd, int n_sectors, const int64_t* sketch,
+                               int power_iters, uint64_t seed, xgb_tensor* U, xgb_tensor* S, xgb_tensor* Vdag,
+                               double* trunc_weight, double* entropy, int32_t* keep, int64_t* width,
+                               int32_t* n_saturated) {
+  GUARD(XGB_E_BADPLAN, {
+    if (n_sectors != int(t->t.meta->sectors.size()) || (n_sectors > 0 && !sketch))
+      return set_error(XGB_E_BADPLAN, "randomized tSVD: one sketch width per sector required");
+    RsvdInfo info;
+    SVDResult r = tsvd_randomized(t->t, max_keep, eps_svd, std::vector<int64_t>(sketch, sketch + n_sectors),
+                                  power_iters, seed, &info);
+    if (U) *U = wrap(r.U);
+    if (S) *S = wrap(r.S);
+    if (Vdag) *Vdag = wrap(r.Vdag);
+    if (trunc_weight) *trunc_weight = r.trunc_weight;
+    if (entropy) *entropy = r.entropy;
+    if (keep) for (size_t i = 0; i < r.keep.size(); ++i) keep[i] = r.keep[i];
+    if (width) for (size_t i = 0; i < info.width.size(); ++i) width[i] = info.width[i];
+    if (n_saturated) *n_saturated = int32_t(info.saturated.size());
+    return XGB_OK;
+  })
+}
+
 int xgb_tensor_tqr(xgb_tensor t, xgb_tensor* Q, xgb_tensor* R) {
   GUARD(XGB_E_BADPLAN, {
     auto [q, r] = tqr(t->t);
@@ -243,6 +266,141 @@ int xgb_ctm_set(xgb_ctm c, int which, xgb_tensor t) {
   })
 }
 void xgb_ctm_release(xgb_ctm c) { delete c; }
+
+int xgb_ctm_set_svd(xgb_ctm c, int mode, int power_iters, uint64_t seed, int64_t oversample, double growth) {
+  GUARD(XGB_E_BADPLAN, {
+    if (mode != 0 && mode != 1) throw std::runtime_error("svd mode must be 0 (exact) or 1 (randomized)");
+    if (power_iters < 0 || oversample < 0 || growth < 0) throw std::runtime_error("negative randomized tSVD parameter");
+    CTM& m = *c->c;
+    m.svd_mode = mode;
+    m.power_iters = power_iters;
+    m.seed = seed;
+    auto hp = std::make_shared<HistoryPolicy>();
+    hp->oversample = oversample;
+    hp->growth = growth;
+    m.policy = hp;
+    return XGB_OK;
+  })
+}
+
+int xgb_ctm_stats(xgb_ctm c, int64_t* out5) {
+  GUARD(XGB_E_BADPLAN, {
+    const CTMStats& s = c->c->stats;
+    out5[0] = s.decompositions;
+    out5[1] = s.sketched_sectors;
+    out5[2] = s.exact_sectors;
+    out5[3] = s.redo;
+    out5[4] = s.sketch_cols;
+    return XGB_OK;
+  })
+}
+
+int xgb_ctm_record(xgb_ctm c, int on) {
+  GUARD(XGB_E_BADPLAN, {
+    c->c->record = on != 0;
+    if (!on) c->c->records.clear();
+    return XGB_OK;
+  })
+}
+
+int xgb_ctm_record_count(xgb_ctm c) { GUARD(XGB_E_BADPLAN, { return int(c->c->records.size()); }) }
+
+int xgb_ctm_record_get(xgb_ctm c, int i, int* dir, int* n_sectors, int64_t* n_spectrum, int32_t* sectors,
+                       float* features, int64_t* keep, int64_t* width, int64_t* kmin, double* spectrum,
+                       int64_t* spec_begin) {
+  GUARD(XGB_E_BADPLAN, {
+    const auto& R = c->c->records;
+    if (i < 0 || i >= int(R.size())) throw std::runtime_error("record index out of range");
+    const DecompRecord& r = R[size_t(i)];
+    const size_t n = r.sectors.size();
+    if (dir) *dir = r.dir;
+    if (n_sectors) *n_sectors = int(n);
+    if (n_spectrum) *n_spectrum = int64_t(r.spectrum.size());
+    for (size_t a = 0; a < n; ++a) {
+      if (sectors) sectors[a] = r.sectors[a];
+      if (keep) keep[a] = r.keep[a];
+      if (width) width[a] = r.width[a];
+      if (kmin) kmin[a] = r.kmin[a];
+    }
+    if (features) std::memcpy(features, r.features.data(), sizeof(float) * r.features.size());
+    if (spectrum) std::memcpy(spectrum, r.spectrum.data(), sizeof(double) * r.spectrum.size());
+    if (spec_begin) std::memcpy(spec_begin, r.spec_begin.data(), sizeof(int64_t) * r.spec_begin.size());
+    return XGB_OK;
+  })
+}
+
+struct xgb_rank_model_s {
+  std::shared_ptr<RankModel> m;
+};
+
+int xgb_rank_model_num_params(void) { return kMlpParams; }
+int xgb_rank_model_num_features(void) { return kMlpIn; }
+
+xgb_rank_model xgb_rank_model_create(uint64_t seed) {
+  GUARD(nullptr, { return new xgb_rank_model_s{std::make_shared<RankModel>(seed)}; })
+}
+void xgb_rank_model_release(xgb_rank_model m) { delete m; }
+
+int xgb_rank_model_get_params(xgb_rank_model m, float* out, int cap) {
+  GUARD(XGB_E_BADPLAN, {
+    if (cap < kMlpParams) throw std::runtime_error("parameter buffer too small");
+    m->m->get_params(out);
+    return XGB_OK;
+  })
+}
+int xgb_rank_model_set_params(xgb_rank_model m, const float* in, int n) {
+  GUARD(XGB_E_BADPLAN, {
+    if (n != kMlpParams) throw std::runtime_error("wrong parameter count");
+    m->m->set_params(in);
+    return XGB_OK;
+  })
+}
+int xgb_rank_model_predict(xgb_rank_model m, const float* X, int64_t n, float* Y) {
+  GUARD(XGB_E_BADPLAN, {
+    m->m->predict(X, n, Y);
+    return XGB_OK;
+  })
+}
+int xgb_rank_model_gradient(xgb_rank_model m, const float* X, const float* T, int64_t n, float* grad, double* loss) {
+  GUARD(XGB_E_BADPLAN, {
+    const double l = m->m->gradient(X, T, n, grad);
+    if (loss) *loss = l;
+    return XGB_OK;
+  })
+}
+int xgb_rank_model_train(xgb_rank_model m, const float* X, const float* T, int64_t n, int steps, float lr,
+                         double* loss) {
+  GUARD(XGB_E_BADPLAN, {
+    const double l = m->m->train(X, T, n, steps, lr);
+    if (loss) *loss = l;
+    return XGB_OK;
+  })
+}
+int xgb_ctm_set_rank_model(xgb_ctm c, xgb_rank_model m, double margin, int64_t min_oversample, int power_iters,
+                           uint64_t seed) {
+  GUARD(XGB_E_BADPLAN, {
+    if (margin < 0 || min_oversample < 0 || power_iters < 0) throw std::runtime_error("negative width parameter");
+    auto pol = std::make_shared<MlpPolicy>();
+    pol->model = m->m;
+    pol->margin = margin;
+    pol->min_oversample = min_oversample;
+    CTM& t = *c->c;
+    t.policy = pol;
+    t.svd_mode = 1;
+    t.power_iters = power_iters;
+    t.seed = seed;
+    return XGB_OK;
+  })
+}
+
+xgb_tensor xgb_ctm_rdm(xgb_ctm c, int vertical) { GUARD(nullptr, { return wrap(c->c->rdm(vertical != 0)); }) }
+
+int xgb_tensor_bond_expectation(xgb_tensor rho, xgb_tensor op, double* out) {
+  GUARD(XGB_E_BADPLAN, {
+    *out = bond_expectation(rho->t, op->t);
+    return XGB_OK;
+  })
+}
 
 xgb_tensor xgb_tensor_meta(int rank, const xgb_basis* dom, int corank, const xgb_basis* cod) {
   GUARD(nullptr, {

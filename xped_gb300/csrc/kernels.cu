@@ -726,12 +726,33 @@ int xgb_memset_zero(void* dst, size_t bytes) {
 int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, const double* A, const double* B,
                      double* C, double alpha, double beta, void* stream_) {
   XGB_REQUIRE_INIT();
-  if (precision != XGB_PREC_FP64) return set_error(XGB_E_UNSUPPORTED, "precision form not available through this entry");
+  if (precision != XGB_PREC_FP64 && precision != XGB_PREC_3XTF32)
+    return set_error(XGB_E_UNSUPPORTED, "precision form not available through this entry");
   if (n_groups < 0) return set_error(XGB_E_BADPLAN, "n_groups < 0");
   XGB_GUARD_BEGIN
   cudaStream_t s = pick(stream_);
   for (int g = 0; g < n_groups; ++g)
     if (descs[g].m < 0 || descs[g].n < 0 || descs[g].k < 0) return set_error(XGB_E_BADPLAN, "negative GEMM extent");
+  if (precision == XGB_PREC_3XTF32) {
+    const int tile = gemm_tc_tile();
+    std::vector<GemmTile> tiles;
+    double flops = 0;
+    for (int g = 0; g < n_groups; ++g) {
+      int64_t tm = (descs[g].m + tile - 1) / tile, tn = (descs[g].n + tile - 1) / tile;
+      for (int64_t j = 0; j < tn; ++j)
+        for (int64_t i = 0; i < tm; ++i) tiles.push_back({g, int32_t(i), int32_t(j), tile});
+      flops += 2.0 * double(descs[g].m) * double(descs[g].n) * double(descs[g].k);
+    }
+    if (tiles.empty()) return XGB_OK;
+    auto* dd = upload(descs, size_t(n_groups), s);
+    auto* dt = upload(tiles.data(), tiles.size(), s);
+    prof_begin(K_GEMM_TC, s);
+    launch_gemm_tc(dd, dt, int(tiles.size()), A, B, C, alpha, beta, s);
+    prof_end(K_GEMM_TC, s, flops);
+    dev_free(dd);
+    dev_free(dt);
+    return check_cuda(cudaGetLastError(), "tensor-core gemm launch");
+  }
   const int tile = choose_gemm_tile(descs, n_groups);
   std::vector<GemmTile> tiles;
   for (int g = 0; g < n_groups; ++g) {
@@ -746,6 +767,14 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
   dev_free(dd);
   dev_free(dt);
   return check_cuda(cudaGetLastError(), "gemm launch");
+  XGB_GUARD_END
+}
+
+int xgb_gemm_tc_status(void) {
+  XGB_REQUIRE_INIT();
+  XGB_GUARD_BEGIN
+  cudaStreamSynchronize(stream());
+  return gemm_tc_error(true) ? set_error(XGB_E_TIMEOUT, "tensor-core GEMM: a CTA gave up waiting for its MMAs") : XGB_OK;
   XGB_GUARD_END
 }
 

@@ -46,9 +46,34 @@ void launch_diag_from_vec(const xgb_copy2d_desc* d_descs, int n, int64_t max_k, 
                           cudaStream_t s);
 void launch_diag_apply(const xgb_copy2d_desc* d_descs, int n, int64_t max_k, int fn, double* x, cudaStream_t s);
 
+// split-precision (3xTF32) tensor-core grouped GEMM (gemm_tc.cu): 128 x 128 tiles
+int gemm_tc_tile();
+void launch_gemm_tc(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, const double* A,
+                    const double* B, double* C, double alpha, double beta, cudaStream_t s);
+int gemm_tc_error(bool reset);  // 1 if a tensor-core GEMM CTA gave up waiting (synchronous read)
+
+// randomized tSVD helpers (rsvd.cu)
+struct GaussBlock { int64_t offset, count, stream; };       // fill out[offset .. offset+count) from stream
+struct SignFixDesc { int64_t m, n, k, u_off, v_off; };      // U m x k (ld m), V^T k x n (ld k)
+void launch_gauss_fill(const GaussBlock* d_blocks, int n_blocks, int64_t max_count, uint64_t seed, double* out,
+                       cudaStream_t s);
+void launch_sign_fix(const SignFixDesc* d_descs, int n, int64_t max_k, double* U, double* Vt, cudaStream_t s);
+
+// rank-predictor MLP (mlp.cu): kMlpIn -> kMlpHidden x 3 (ReLU) -> kMlpOut, FP32,
+// parameters packed as W1, b1, W2, b2, W3, b3, W4, b4 with row-major W[out][in]
+constexpr int kMlpIn = 8, kMlpHidden = 64, kMlpOut = 2;
+constexpr int kMlpParams = kMlpHidden * kMlpIn + kMlpHidden + 2 * (kMlpHidden * kMlpHidden + kMlpHidden) +
+                           kMlpOut * kMlpHidden + kMlpOut;
+int mlp_grad_slots(int64_t n);  // per-CTA gradient slots used by launch_mlp_grad for n samples
+void launch_mlp_forward(const float* params, const float* X, int64_t n, float* Y, cudaStream_t s);
+void launch_mlp_grad(const float* params, const float* X, const float* T, int64_t n, float* gpart, float* lpart,
+                     cudaStream_t s);
+void launch_mlp_reduce_adam(float* params, float* mom, float* vel, const float* gpart, int slots, float* grad_out,
+                            int adam, float lr, float b1, float b2, float eps, int step, cudaStream_t s);
+
 // per-kernel-kind instrumentation (CUDA events around each launch when enabled;
 // algorithmic work - flops for GEMMs, bytes for data movement - always counted)
-enum KernelKind { K_GEMM = 0, K_PERMUTE, K_SVD, K_TRUNC, K_QR, K_ABSMAX, K_SCALE, K_COPY2D, K_DIAG, K_GEMM_TC, K_COUNT };
+enum KernelKind { K_GEMM = 0, K_PERMUTE, K_SVD, K_TRUNC, K_QR, K_ABSMAX, K_SCALE, K_COPY2D, K_DIAG, K_GEMM_TC, K_SKETCH, K_MLP, K_COUNT };
 void prof_begin(int kind, cudaStream_t s);
 void prof_end(int kind, cudaStream_t s, double work);
 

@@ -1,0 +1,307 @@
+// Randomized blockwise truncated SVD (host orchestration).
+//
+// Every stage is one grouped launch over all sketched sectors: the Gaussian
+// test matrices, the sketch GEMMs (A Omega, A^T Q, Q^T A, Q U_B), the
+// orthonormalisations (thin SVD of the tall sketch, whose left factor is
+// orthonormal to FP64 round-off even when the sketch is rank deficient), the
+// small exact SVD of B = Q^T A together with the exactly decomposed sectors,
+// and the sign convention.  Truncation is the shared cutoff_matrices step
+// (src/Core/Tensor.cpp:523-633) on the resulting per-sector spectra.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "tensor.hpp"
+
+namespace xgb {
+namespace {
+
+void ok(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Host tables packed into one device allocation and uploaded with one copy;
+// the allocation is released in stream order when the object goes away.
+class Staging {
+ public:
+  template <class T>
+  size_t add(const std::vector<T>& v) {
+    const size_t off = (host_.size() + 255) & ~size_t(255);
+    host_.resize(off + sizeof(T) * v.size());
+    if (!v.empty()) std::memcpy(host_.data() + off, v.data(), sizeof(T) * v.size());
+    return off;
+  }
+  void upload(cudaStream_t s) {
+    dev_ = static_cast<char*>(dev_alloc(std::max<size_t>(host_.size(), 256)));
+    if (!host_.empty()) ok(cudaMemcpyAsync(dev_, host_.data(), host_.size(), cudaMemcpyHostToDevice, s), "h2d tables");
+  }
+  template <class T>
+  T* at(size_t off) const { return reinterpret_cast<T*>(dev_ + off); }
+  ~Staging() { if (dev_) dev_free(dev_); }
+
+ private:
+  std::vector<char> host_;
+  char* dev_ = nullptr;
+};
+
+double* alloc_d(int64_t n) { return static_cast<double*>(dev_alloc(sizeof(double) * size_t(std::max<int64_t>(n, 1)))); }
+
+void grouped_gemm(const std::vector<xgb_gemm_desc>& d, const double* A, const double* B, double* C, cudaStream_t s) {
+  if (d.empty()) return;
+  const int tile = choose_gemm_tile(d.data(), int(d.size()));
+  std::vector<GemmTile> tiles;
+  double flops = 0;
+  for (size_t g = 0; g < d.size(); ++g) {
+    const int64_t tm = (d[g].m + tile - 1) / tile, tn = (d[g].n + tile - 1) / tile;
+    for (int64_t y = 0; y < tn; ++y)
+      for (int64_t x = 0; x < tm; ++x) tiles.push_back({int32_t(g), int32_t(x), int32_t(y), tile});
+    flops += 2.0 * double(d[g].m) * double(d[g].n) * double(d[g].k);
+  }
+  Staging st;
+  const size_t od = st.add(d), ot = st.add(tiles);
+  st.upload(s);
+  prof_begin(K_GEMM, s);
+  launch_gemm_f64(st.at<xgb_gemm_desc>(od), st.at<GemmTile>(ot), int(tiles.size()), tile, A, B, C, 1.0, 0.0, s);
+  prof_end(K_GEMM, s, flops);
+}
+
+// Batched thin SVD through the cluster Jacobi kernel (work counted as LAPACK dgesvd flops).
+void batched_svd(const std::vector<xgb_svd_desc>& d, const double* A, double* U, double* S, double* Vt, cudaStream_t s) {
+  if (d.empty()) return;
+  std::vector<int64_t> woff(d.size());
+  int64_t wt = 0, maxk = 0;
+  double flops = 0;
+  for (size_t i = 0; i < d.size(); ++i) {
+    woff[i] = wt;
+    wt += int64_t(svd_work_elems(d[i].m, d[i].n));
+    const double mm = double(std::max(d[i].m, d[i].n)), nn = double(std::min(d[i].m, d[i].n));
+    maxk = std::max(maxk, std::min(d[i].m, d[i].n));
+    flops += 4 * mm * mm * nn + 8 * mm * nn * nn + 9 * nn * nn * nn;
+  }
+  Staging st;
+  const size_t od = st.add(d), ow = st.add(woff);
+  st.upload(s);
+  double* W = alloc_d(wt);
+  prof_begin(K_SVD, s);
+  launch_svd(st.at<xgb_svd_desc>(od), st.at<int64_t>(ow), int(d.size()), maxk, A, U, S, Vt, W, s);
+  prof_end(K_SVD, s, flops);
+  dev_free(W);
+}
+
+// Orthonormal basis of each tall m x l block of Y (left singular vectors) into Q.
+void orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64_t>& cols, const std::vector<int64_t>& y_off,
+                    const double* Y, double* Q, cudaStream_t s) {
+  std::vector<xgb_svd_desc> d;
+  int64_t so = 0, vo = 0;
+  for (size_t i = 0; i < rows.size(); ++i) {
+    d.push_back({rows[i], cols[i], y_off[i], y_off[i], so, vo});
+    so += cols[i];
+    vo += cols[i] * cols[i];
+  }
+  double* Ss = alloc_d(so);
+  double* Vs = alloc_d(vo);
+  batched_svd(d, Y, Q, Ss, Vs, s);
+  dev_free(Ss);
+  dev_free(Vs);
+}
+
+constexpr int kMaxRetries = 3;
+
+}  // namespace
+
+SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, const std::vector<int64_t>& sketch,
+                          int power_iters, uint64_t seed, RsvdInfo* info) {
+  Tensor t = materialize(t0);
+  const TensorMeta& m = *t.meta;
+  const int n = int(m.sectors.size());
+  if (n == 0) throw std::runtime_error("tSVD of a tensor without sectors");
+  if (int(sketch.size()) != n) throw std::runtime_error("randomized tSVD: one sketch width per sector required");
+  if (power_iters < 0) throw std::runtime_error("randomized tSVD: negative number of power iterations");
+  cudaStream_t st = stream();
+  std::vector<char> exact(n, 0);
+  std::vector<int64_t> want(sketch);
+  std::vector<int> saturated;
+  for (int round = 0;; ++round) {
+    // ---- widths and layout
+    std::vector<int64_t> width(n);
+    std::vector<int> R, E;  // sketched / exact sector indices
+    for (int i = 0; i < n; ++i) {
+      const int64_t kmin = std::min(m.rows[i], m.cols[i]);
+      int64_t l = want[i];
+      if (exact[i] || l <= 0 || 2 * l >= kmin) { exact[i] = 1; l = kmin; }
+      width[i] = l;
+      (exact[i] ? E : R).push_back(i);
+    }
+    Spectra sp;
+    sp.k = width;
+    sp.u_off.assign(n, 0);
+    sp.v_off.assign(n, 0);
+    sp.s_begin.assign(n + 1, 0);
+    int64_t ut = 0, vt = 0;
+    for (int i = 0; i < n; ++i) {
+      sp.u_off[i] = ut;
+      ut += m.rows[i] * width[i];
+      sp.v_off[i] = vt;
+      vt += width[i] * m.cols[i];
+      sp.s_begin[i + 1] = sp.s_begin[i] + width[i];
+    }
+    // per sketched sector: Omega (n x l), Y (m x l), Q (m x l), Z / Qz (n x l), U_B (l x l)
+    const int nr = int(R.size());
+    std::vector<int64_t> rr(nr), rc(nr), rl(nr), om(nr), yo(nr), zo(nr), ub(nr), bo(n, 0);
+    int64_t omt = 0, yt = 0, zt = 0, ubt = 0, bt = 0;
+    for (int a = 0; a < nr; ++a) {
+      const int i = R[a];
+      rr[a] = m.rows[i];
+      rc[a] = m.cols[i];
+      rl[a] = width[i];
+      om[a] = omt;
+      omt += rc[a] * rl[a];
+      yo[a] = yt;
+      yt += rr[a] * rl[a];
+      zo[a] = zt;
+      zt += rc[a] * rl[a];
+      ub[a] = ut + ubt;  // U_B lives behind the spectra's U blocks in the same buffer
+      ubt += rl[a] * rl[a];
+    }
+    for (int i = 0; i < n; ++i) {
+      bo[i] = bt;
+      bt += exact[i] ? m.rows[i] * m.cols[i] : width[i] * m.cols[i];
+    }
+    sp.U = alloc_d(ut + ubt);
+    sp.S = alloc_d(sp.s_begin.back());
+    sp.V = alloc_d(vt);
+    double* Bb = alloc_d(bt);
+    double* Q = nr ? alloc_d(yt) : nullptr;
+
+    if (nr) {
+      double* Om = alloc_d(std::max(omt, zt));
+      double* Y = alloc_d(yt);
+      // ---- Omega
+      {
+        std::vector<GaussBlock> gb;
+        int64_t mx = 0;
+        for (int a = 0; a < nr; ++a) {
+          gb.push_back({om[a], rc[a] * rl[a], int64_t(R[a])});
+          mx = std::max(mx, rc[a] * rl[a]);
+        }
+        Staging sg;
+        const size_t o = sg.add(gb);
+        sg.upload(st);
+        prof_begin(K_SKETCH, st);
+        launch_gauss_fill(sg.at<GaussBlock>(o), nr, mx, seed, Om, st);
+        prof_end(K_SKETCH, st, 8.0 * double(omt));
+      }
+      // ---- Y = A Omega, Q = orth(Y)
+      std::vector<xgb_gemm_desc> g;
+      for (int a = 0; a < nr; ++a)
+        g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], om[a], rc[a], yo[a], rr[a], 0, 0});
+      grouped_gemm(g, t.data(), Om, Y, st);
+      orthonormalise(rr, rl, yo, Y, Q, st);
+      // ---- subspace iterations: Z = A^T Q, Qz = orth(Z), Y = A Qz, Q = orth(Y)
+      if (power_iters > 0) {
+        double* Z = alloc_d(zt);
+        double* Qz = Om;  // Omega is no longer needed
+        for (int p = 0; p < power_iters; ++p) {
+          g.clear();
+          for (int a = 0; a < nr; ++a)
+            g.push_back({rc[a], rl[a], rr[a], m.offset[R[a]], rr[a], yo[a], rr[a], zo[a], rc[a], 1, 0});
+          grouped_gemm(g, t.data(), Q, Z, st);
+          orthonormalise(rc, rl, zo, Z, Qz, st);
+          g.clear();
+          for (int a = 0; a < nr; ++a)
+            g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], zo[a], rc[a], yo[a], rr[a], 0, 0});
+          grouped_gemm(g, t.data(), Qz, Y, st);
+          orthonormalise(rr, rl, yo, Y, Q, st);
+        }
+        dev_free(Z);
+      }
+      // ---- B = Q^T A (l x n)
+      g.clear();
+      for (int a = 0; a < nr; ++a)
+        g.push_back({rl[a], rc[a], rr[a], yo[a], rr[a], m.offset[R[a]], rr[a], bo[R[a]], rl[a], 1, 0});
+      grouped_gemm(g, Q, t.data(), Bb, st);
+      dev_free(Y);
+      dev_free(Om);
+    }
+    // ---- exact sectors: their blocks join the final batched SVD
+    if (!E.empty()) {
+      std::vector<xgb_copy2d_desc> cd;
+      int64_t mx = 0;
+      for (int i : E) {
+        cd.push_back({m.offset[i], m.rows[i], bo[i], m.rows[i], m.rows[i], m.cols[i]});
+        mx = std::max(mx, m.rows[i] * m.cols[i]);
+      }
+      Staging sc;
+      const size_t o = sc.add(cd);
+      sc.upload(st);
+      prof_begin(K_COPY2D, st);
+      launch_copy2d(sc.at<xgb_copy2d_desc>(o), int(cd.size()), mx, t.data(), Bb, st);
+      prof_end(K_COPY2D, st, 16.0 * double(bt));
+    }
+    // ---- one batched SVD: exact sectors (largest first) and the sketched B blocks
+    {
+      std::vector<xgb_svd_desc> d;
+      std::vector<int> order(E.begin(), E.end());
+      std::sort(order.begin(), order.end(), [&](int x, int y) {
+        return m.rows[x] * m.cols[x] * std::min(m.rows[x], m.cols[x]) > m.rows[y] * m.cols[y] * std::min(m.rows[y], m.cols[y]);
+      });
+      for (int i : order) d.push_back({m.rows[i], m.cols[i], bo[i], sp.u_off[i], sp.s_begin[i], sp.v_off[i]});
+      for (int a = 0; a < nr; ++a) {
+        const int i = R[a];
+        d.push_back({rl[a], rc[a], bo[i], ub[a], sp.s_begin[i], sp.v_off[i]});
+      }
+      batched_svd(d, Bb, sp.U, sp.S, sp.V, st);
+    }
+    dev_free(Bb);
+    if (nr) {
+      // ---- U = Q U_B, then the sign convention on the lifted vectors
+      std::vector<xgb_gemm_desc> g;
+      std::vector<SignFixDesc> sf;
+      int64_t mx = 0;
+      for (int a = 0; a < nr; ++a) {
+        const int i = R[a];
+        g.push_back({rr[a], rl[a], rl[a], yo[a], rr[a], ub[a], rl[a], sp.u_off[i], rr[a], 0, 0});
+        sf.push_back({rr[a], rc[a], rl[a], sp.u_off[i], sp.v_off[i]});
+        mx = std::max(mx, rl[a]);
+      }
+      grouped_gemm(g, Q, sp.U, sp.U, st);
+      Staging ss;
+      const size_t o = ss.add(sf);
+      ss.upload(st);
+      prof_begin(K_SKETCH, st);
+      launch_sign_fix(ss.at<SignFixDesc>(o), nr, mx, sp.U, sp.V, st);
+      prof_end(K_SKETCH, st, 16.0 * double(yt + vt));
+      dev_free(Q);
+    }
+    SVDResult res = truncate_spectra(m, sp, max_keep, eps_svd, false);
+    dev_free(sp.U);
+    dev_free(sp.S);
+    dev_free(sp.V);
+    std::vector<int> sat;
+    for (int i : R)
+      if (res.keep[i] >= width[i]) sat.push_back(i);
+    if (sat.empty()) {
+      if (info) {
+        info->width = width;
+        info->saturated = saturated;
+        info->sketch_cols = 0;
+        for (int i : R) info->sketch_cols += width[i];
+        info->exact_sectors = int(E.size());
+      }
+      return res;
+    }
+    // saturated sectors: double the sketch (the new columns extend the same
+    // Gaussian stream); after kMaxRetries doublings they are decomposed exactly
+    for (int i : sat) {
+      want[i] = 2 * width[i];
+      if (round + 1 >= kMaxRetries) exact[i] = 1;
+      saturated.push_back(i);
+    }
+  }
+}
+
+}  // namespace xgb

@@ -1,0 +1,96 @@
+// Kernels of the randomized blockwise tSVD: the seeded Gaussian test
+// matrices and the singular-vector sign convention applied after the
+// sketch-space singular vectors are lifted back (U = Q U_B).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.hpp"
+
+namespace xgb {
+namespace {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  // splitmix64 finaliser (Steele, Lea, Flood 2014)
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// Standard normal number `e` of stream `stream` under `seed`: Box-Muller on
+// two counter-hashed uniforms u1 in (0, 1], u2 in [0, 1).
+__device__ double gauss_at(uint64_t seed, uint64_t stream, uint64_t e) {
+  const uint64_t base = mix64(seed ^ mix64(stream));
+  const uint64_t h1 = mix64(base ^ (2 * e)), h2 = mix64(base ^ (2 * e + 1));
+  const double u1 = double((h1 >> 11) + 1) * 0x1.0p-53;
+  const double u2 = double(h2 >> 11) * 0x1.0p-53;
+  return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+}
+
+__global__ void gauss_fill_kernel(const GaussBlock* __restrict__ blocks, int n_blocks, uint64_t seed,
+                                  double* __restrict__ out) {
+  const GaussBlock b = blocks[blockIdx.y];
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < b.count; e += int64_t(gridDim.x) * blockDim.x)
+    out[b.offset + e] = gauss_at(seed, uint64_t(b.stream), uint64_t(e));
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Same rule as the batched SVD kernel: s = sign(r . u) with
+// r_i = frac((i+1) * 0.7548776662466927) + 0.25, or the sign of the first
+// largest-magnitude entry when |r . u| <= 1e-8 sum_i r_i |u_i|.
+__global__ void sign_fix_kernel(const SignFixDesc* __restrict__ descs, double* __restrict__ U, double* __restrict__ Vt) {
+  const SignFixDesc d = descs[blockIdx.y];
+  const int lane = threadIdx.x & 31;
+  const int64_t j = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (j >= d.k) return;
+  double* u = U + d.u_off + j * d.m;
+  double dot = 0, mag = 0, best = -1, bval = 0;
+  long long bidx = 0;
+  for (int64_t i = lane; i < d.m; i += 32) {
+    const double x = u[i];
+    const double y = double(i + 1) * 0.7548776662466927;
+    const double r = (y - floor(y)) + 0.25;
+    dot = fma(r, x, dot);
+    mag = fma(r, fabs(x), mag);
+    if (fabs(x) > best) { best = fabs(x); bval = x; bidx = i; }
+  }
+  dot = warp_sum_d(dot);
+  mag = warp_sum_d(mag);
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const double ov = __shfl_xor_sync(0xffffffffu, bval, o);
+    const long long oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+    if (ob > best || (ob == best && oi < bidx)) { best = ob; bval = ov; bidx = oi; }
+  }
+  const bool neg = fabs(dot) > 1.0e-8 * mag ? dot < 0 : bval < 0;
+  if (!neg) return;
+  for (int64_t i = lane; i < d.m; i += 32) u[i] = -u[i];
+  double* v = Vt + d.v_off + j;
+  for (int64_t c = lane; c < d.n; c += 32) v[c * d.k] = -v[c * d.k];
+}
+
+}  // namespace
+
+void launch_gauss_fill(const GaussBlock* d_blocks, int n_blocks, int64_t max_count, uint64_t seed, double* out,
+                       cudaStream_t s) {
+  if (n_blocks <= 0 || max_count <= 0) return;
+  const int64_t want = (max_count + 255) / 256;
+  dim3 grid(unsigned(want < 1024 ? want : 1024), unsigned(n_blocks));
+  gauss_fill_kernel<<<grid, 256, 0, s>>>(d_blocks, n_blocks, seed, out);
+  count_launch();
+}
+
+void launch_sign_fix(const SignFixDesc* d_descs, int n, int64_t max_k, double* U, double* Vt, cudaStream_t s) {
+  if (n <= 0 || max_k <= 0) return;
+  dim3 grid(unsigned((max_k + 7) / 8), unsigned(n));
+  sign_fix_kernel<<<grid, 256, 0, s>>>(d_descs, U, Vt);
+  count_launch();
+}
+
+}  // namespace xgb

@@ -679,46 +679,56 @@ std::shared_ptr<SvdPlan> get_svd_plan(const TensorMeta& m) {
 }
 }  // namespace
 
-SVDResult tsvd(const Tensor& t0, int64_t max_keep, double eps_svd, bool preserve_multiplets) {
-  // Tensor::tSVD = full_svd_impl + cutoff_matrices (Tensor.cpp:478-633)
-  Tensor t = materialize(t0);
-  const TensorMeta& m = *t.meta;
-  if (m.sectors.empty()) throw std::runtime_error("tSVD of a tensor without sectors");
-  auto plan = get_svd_plan(m);
+SVDResult truncate_spectra(const TensorMeta& m, const Spectra& sp, int64_t max_keep, double eps_svd,
+                           bool preserve_multiplets) {
+  // cutoff_matrices (Tensor.cpp:523-633) on per-sector spectra: global
+  // truncation on the device, then U[:, :k], S[:k, :k], V^T[:k, :] per kept sector.
   cudaStream_t st = stream();
-  double* U = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->u_total, 1)));
-  double* S = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->s_total, 1)));
-  double* V = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->v_total, 1)));
-  double* W = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->work_total, 1)));
-  prof_begin(K_SVD, st);
-  launch_svd(plan->d_descs, plan->d_work_off, plan->n, plan->maxk, t.data(), U, S, V, W, st);
-  prof_end(K_SVD, st, plan->lapack_flops);
-  dev_free(W);
-  if (plan->s_total == 0) throw std::runtime_error("tSVD: no singular values");
-  int32_t* keep_d = static_cast<int32_t*>(dev_alloc(sizeof(int32_t) * plan->n));
+  const int n = int(m.sectors.size());
+  const int64_t s_total = sp.s_begin.back();
+  if (s_total == 0) throw std::runtime_error("tSVD: no singular values");
+  int64_t* d_sb = sp.d_s_begin;
+  int32_t* d_deg = sp.d_deg;
+  bool own_tables = false;
+  if (!d_sb || !d_deg) {
+    std::vector<int32_t> deg;
+    for (int q : m.sectors) deg.push_back(m.sym.deg(q));
+    d_sb = static_cast<int64_t*>(dev_alloc(sizeof(int64_t) * sp.s_begin.size()));
+    d_deg = static_cast<int32_t*>(dev_alloc(sizeof(int32_t) * std::max<size_t>(deg.size(), 1)));
+    cuda_ok(cudaMemcpyAsync(d_sb, sp.s_begin.data(), sizeof(int64_t) * sp.s_begin.size(), cudaMemcpyHostToDevice, st), "h2d");
+    cuda_ok(cudaMemcpyAsync(d_deg, deg.data(), sizeof(int32_t) * deg.size(), cudaMemcpyHostToDevice, st), "h2d");
+    own_tables = true;
+  }
+  int32_t* keep_d = static_cast<int32_t*>(dev_alloc(sizeof(int32_t) * n));
   double* out2_d = scalar_scratch() + 8;
   prof_begin(K_TRUNC, st);
-  launch_truncate(plan->n, plan->d_s_begin, plan->d_deg, S, plan->s_total, max_keep, eps_svd, preserve_multiplets ? 1 : 0,
-                  keep_d, out2_d, st);
-  prof_end(K_TRUNC, st, 8.0 * double(plan->s_total));
-  if (g_keep_cap < plan->n) {
+  launch_truncate(n, d_sb, d_deg, sp.S, s_total, max_keep, eps_svd, preserve_multiplets ? 1 : 0, keep_d, out2_d, st);
+  prof_end(K_TRUNC, st, 8.0 * double(s_total));
+  if (g_keep_cap < n) {
     if (g_keep_host) cudaFreeHost(g_keep_host);
-    cuda_ok(cudaMallocHost(&g_keep_host, sizeof(int32_t) * plan->n), "pinned");
-    g_keep_cap = plan->n;
+    cuda_ok(cudaMallocHost(&g_keep_host, sizeof(int32_t) * n), "pinned");
+    g_keep_cap = n;
     if (!g_out2_host) cuda_ok(cudaMallocHost(&g_out2_host, sizeof(double) * 2), "pinned");
   }
-  cuda_ok(cudaMemcpyAsync(g_keep_host, keep_d, sizeof(int32_t) * plan->n, cudaMemcpyDeviceToHost, st), "d2h");
+  cuda_ok(cudaMemcpyAsync(g_keep_host, keep_d, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st), "d2h");
   cuda_ok(cudaMemcpyAsync(g_out2_host, out2_d, sizeof(double) * 2, cudaMemcpyDeviceToHost, st), "d2h");
+  SVDResult res;
+  res.spectrum.resize(size_t(s_total));
+  res.spec_begin = sp.s_begin;
+  cuda_ok(cudaMemcpyAsync(res.spectrum.data(), sp.S, sizeof(double) * size_t(s_total), cudaMemcpyDeviceToHost, st), "d2h");
   cuda_ok(cudaStreamSynchronize(st), "sync");
   dev_free(keep_d);
+  if (own_tables) {
+    dev_free(d_sb);
+    dev_free(d_deg);
+  }
 
-  SVDResult res;
   res.trunc_weight = g_out2_host[0];
   res.entropy = g_out2_host[1];
-  res.keep.assign(g_keep_host, g_keep_host + plan->n);
+  res.keep.assign(g_keep_host, g_keep_host + n);
   // truncated basis: charges with kept values in ascending order (std::map, Tensor.cpp:592-598)
   std::vector<std::pair<int, int>> kept;  // (q, sector index)
-  for (int i = 0; i < plan->n; ++i)
+  for (int i = 0; i < n; ++i)
     if (res.keep[i] > 0) kept.push_back({m.sectors[i], i});
   std::sort(kept.begin(), kept.end());
   std::vector<std::pair<int, int64_t>> pairs;
@@ -735,10 +745,10 @@ SVDResult tsvd(const Tensor& t0, int64_t max_keep, double eps_svd, bool preserve
   int64_t mxu = 0, mxv = 0, mxs = 0;
   for (size_t a = 0; a < kept.size(); ++a) {
     const int i = kept[a].second;
-    const int64_t k = res.keep[i], r = m.rows[i], c = m.cols[i], kf = plan->kfull[i];
-    du.push_back({plan->u_off[i], r, mu->offset[a], r, r, k});
-    dv.push_back({plan->v_off[i], kf, mv->offset[a], k, k, c});
-    ds.push_back({plan->s_off[i], 1, ms->offset[a], k, k, k});
+    const int64_t k = res.keep[i], r = m.rows[i], c = m.cols[i], kf = sp.k[i];
+    du.push_back({sp.u_off[i], r, mu->offset[a], r, r, k});
+    dv.push_back({sp.v_off[i], kf, mv->offset[a], k, k, c});
+    ds.push_back({sp.s_begin[i], 1, ms->offset[a], k, k, k});
     mxu = std::max(mxu, r * k);
     mxv = std::max(mxv, k * c);
     mxs = std::max(mxs, k);
@@ -751,15 +761,41 @@ SVDResult tsvd(const Tensor& t0, int64_t max_keep, double eps_svd, bool preserve
   all.insert(all.end(), ds.begin(), ds.end());
   cuda_ok(cudaMemcpyAsync(dd, all.data(), sizeof(xgb_copy2d_desc) * all.size(), cudaMemcpyHostToDevice, st), "h2d");
   prof_begin(K_COPY2D, st);
-  launch_copy2d(dd, int(nb), mxu, U, res.U.data(), st);
-  launch_copy2d(dd + nb, int(nb), mxv, V, res.Vdag.data(), st);
-  launch_diag_from_vec(dd + 2 * nb, int(nb), mxs, -1, S, res.S.data(), st);
+  launch_copy2d(dd, int(nb), mxu, sp.U, res.U.data(), st);
+  launch_copy2d(dd + nb, int(nb), mxv, sp.V, res.Vdag.data(), st);
+  launch_diag_from_vec(dd + 2 * nb, int(nb), mxs, -1, sp.S, res.S.data(), st);
   prof_end(K_COPY2D, st, 16.0 * double(res.U.size() + res.Vdag.size() + res.S.size()));
   cuda_ok(cudaStreamSynchronize(st), "sync");  // descriptors are pageable host memory
   dev_free(dd);
-  dev_free(U);
-  dev_free(S);
-  dev_free(V);
+  return res;
+}
+
+SVDResult tsvd(const Tensor& t0, int64_t max_keep, double eps_svd, bool preserve_multiplets) {
+  // Tensor::tSVD = full_svd_impl + cutoff_matrices (Tensor.cpp:478-633)
+  Tensor t = materialize(t0);
+  const TensorMeta& m = *t.meta;
+  if (m.sectors.empty()) throw std::runtime_error("tSVD of a tensor without sectors");
+  auto plan = get_svd_plan(m);
+  cudaStream_t st = stream();
+  Spectra sp;
+  sp.U = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->u_total, 1)));
+  sp.S = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->s_total, 1)));
+  sp.V = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->v_total, 1)));
+  double* W = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->work_total, 1)));
+  prof_begin(K_SVD, st);
+  launch_svd(plan->d_descs, plan->d_work_off, plan->n, plan->maxk, t.data(), sp.U, sp.S, sp.V, W, st);
+  prof_end(K_SVD, st, plan->lapack_flops);
+  dev_free(W);
+  sp.k = plan->kfull;
+  sp.u_off = plan->u_off;
+  sp.v_off = plan->v_off;
+  sp.s_begin = plan->s_begin;
+  sp.d_s_begin = plan->d_s_begin;
+  sp.d_deg = plan->d_deg;
+  SVDResult res = truncate_spectra(m, sp, max_keep, eps_svd, preserve_multiplets);
+  dev_free(sp.U);
+  dev_free(sp.S);
+  dev_free(sp.V);
   return res;
 }
 
@@ -800,10 +836,7 @@ std::pair<Tensor, Tensor> tqr(const Tensor& t0) {
   return {Q, R};
 }
 
-std::pair<Tensor, Tensor> decompose(const Tensor& t1, const Tensor& t2, int64_t max_nsv) {
-  // decompose (src/PEPS/PEPSContractions.cpp:16-43)
-  Tensor prod = matmul(t1, t2);
-  SVDResult r = tsvd(prod, max_nsv, 1.0e-10, false);
+std::pair<Tensor, Tensor> projectors_from_svd(const SVDResult& r, const Tensor& t1, const Tensor& t2) {
   // isqrtS = S.diag_sqrt().diag_inv(): 1/sqrt(s) on the diagonal
   Tensor isq = empty_like_meta(r.S.meta);
   {
@@ -827,6 +860,46 @@ std::pair<Tensor, Tensor> decompose(const Tensor& t1, const Tensor& t2, int64_t 
   return {P1, P2};
 }
 
+std::pair<Tensor, Tensor> decompose(const Tensor& t1, const Tensor& t2, int64_t max_nsv) {
+  // decompose (src/PEPS/PEPSContractions.cpp:16-43)
+  Tensor prod = matmul(t1, t2);
+  SVDResult r = tsvd(prod, max_nsv, 1.0e-10, false);
+  return projectors_from_svd(r, t1, t2);
+}
+
+// ======================================================================= width policies
+std::vector<int64_t> HistoryPolicy::widths(const TensorMeta& m, const History& last, int64_t chi) {
+  std::vector<int64_t> w(m.sectors.size(), 0);
+  for (size_t i = 0; i < m.sectors.size(); ++i) {
+    auto it = last.find(m.sectors[i]);
+    if (it == last.end()) continue;  // never seen: exact
+    const int64_t k = it->second.keep;
+    w[i] = std::min<int64_t>(chi, k) + std::max<int64_t>(oversample, int64_t(std::ceil(growth * double(k))));
+  }
+  return w;
+}
+
+void sector_features(const TensorMeta& m, const History& last, int64_t chi, std::vector<float>& out) {
+  const size_t n = m.sectors.size();
+  out.assign(n * kFeatures, 0.0f);
+  auto lg10 = [](double x, double floor_) { return x > 0 ? std::max(std::log10(x), floor_) : floor_; };
+  for (size_t i = 0; i < n; ++i) {
+    float* f = out.data() + i * kFeatures;
+    f[0] = float(std::log2(1.0 + double(m.rows[i])) / 12.0);
+    f[1] = float(std::log2(1.0 + double(m.cols[i])) / 12.0);
+    f[7] = float(std::log2(1.0 + double(chi)) / 8.0);
+    auto it = last.find(m.sectors[i]);
+    if (it == last.end()) continue;
+    const SectorHistory& h = it->second;
+    const double smax = h.s_max > 0 ? h.s_max : 1.0;
+    f[2] = 1.0f;
+    f[3] = float(std::log2(1.0 + double(h.keep)) / 8.0);
+    f[4] = float(lg10(h.s_first / smax, -16.0) / 16.0);
+    f[5] = float(lg10(h.s_last / smax, -16.0) / 16.0);
+    f[6] = float((h.keep > 0 && h.s_next > 0 ? lg10(h.s_next / std::max(h.s_last, 1e-300), -8.0) : -8.0) / 8.0);
+  }
+}
+
 // ======================================================================= CTM
 static Tensor tw(const Tensor& t, std::initializer_list<int> legs) {
   Tensor o = t;
@@ -834,7 +907,7 @@ static Tensor tw(const Tensor& t, std::initializer_list<int> legs) {
   return o;
 }
 
-CTM::CTM(const Tensor& A_, int64_t chi_) : chi(chi_), A(materialize(A_)) {
+CTM::CTM(const Tensor& A_, int64_t chi_) : chi(chi_), policy(std::make_shared<HistoryPolicy>()), A(materialize(A_)) {
   if (A.meta->rank() != 2 || A.meta->corank() != 3) throw std::runtime_error("CTM: site tensor must be Tensor<2,3>");
   // Adags = As.adjoint().eval().permute<0, 3, 4, 2, 0, 1>()  (src/PEPS/iPEPS.cpp:210)
   Ad = permute(adjoint(A), 0, {3, 4, 2, 0, 1});
@@ -918,28 +991,139 @@ Tensor CTM::contract_corner(const char* corner) {
   throw std::runtime_error("contract_corner: unknown corner");
 }
 
+std::pair<Tensor, Tensor> CTM::decompose_dir(int d, const Tensor& t1, const Tensor& t2) {
+  // decompose (src/PEPS/PEPSContractions.cpp:16-43) with the configured SVD form
+  Tensor prod = matmul(t1, t2);
+  const TensorMeta& m = *prod.meta;
+  const size_t n = m.sectors.size();
+  DecompRecord rec;
+  if (record) {
+    rec.dir = d;
+    rec.sectors = m.sectors;
+    sector_features(m, hist[d], chi, rec.features);
+  }
+  SVDResult r;
+  std::vector<int64_t> width(n);
+  if (svd_mode == 0) {
+    r = tsvd(prod, chi, 1.0e-10, false);
+    for (size_t i = 0; i < n; ++i) width[i] = std::min(m.rows[i], m.cols[i]);
+    stats.exact_sectors += int64_t(n);
+  } else {
+    if (!policy) throw std::runtime_error("CTM: randomized projector SVD without a width policy");
+    std::vector<int64_t> want = policy->widths(m, hist[d], chi);
+    RsvdInfo info;
+    r = tsvd_randomized(prod, chi, 1.0e-10, want, power_iters, seed + uint64_t(stats.decompositions), &info);
+    width = info.width;
+    stats.exact_sectors += info.exact_sectors;
+    stats.sketched_sectors += int64_t(n) - info.exact_sectors;
+    stats.redo += int64_t(info.saturated.size());
+    stats.sketch_cols += info.sketch_cols;
+  }
+  ++stats.decompositions;
+  // history for the next decomposition of this direction
+  History h;
+  double smax = 0;
+  for (double v : r.spectrum) smax = std::max(smax, v);
+  for (size_t i = 0; i < n; ++i) {
+    SectorHistory e;
+    e.rows = m.rows[i];
+    e.cols = m.cols[i];
+    e.keep = r.keep[i];
+    e.width = width[i];
+    const int64_t b = r.spec_begin[i], len = r.spec_begin[i + 1] - b;
+    e.s_first = len > 0 ? r.spectrum[size_t(b)] : 0.0;
+    e.s_last = e.keep > 0 ? r.spectrum[size_t(b + e.keep - 1)] : 0.0;
+    e.s_next = e.keep < len ? r.spectrum[size_t(b + e.keep)] : 0.0;
+    e.s_max = smax;
+    h[m.sectors[i]] = e;
+  }
+  hist[d] = std::move(h);
+  if (record) {
+    rec.keep.assign(r.keep.begin(), r.keep.end());
+    rec.width = width;
+    for (size_t i = 0; i < n; ++i) rec.kmin.push_back(std::min(m.rows[i], m.cols[i]));
+    rec.spectrum = r.spectrum;
+    rec.spec_begin = r.spec_begin;
+    records.push_back(std::move(rec));
+  }
+  return projectors_from_svd(r, t1, t2);
+}
+
+Tensor CTM::rdm(bool vertical) {
+  if (!vertical) {
+    // computeRDM_h, TRank == 2 (src/PEPS/CTM.cpp:583-619)
+    Tensor C1T1 = contract(C1, T1, {-1, 1}, {1, -2, -3, -4}, 1);
+    Tensor T4C1T1 = contract(T4, twist(C1T1, 0), {1, -1, -2, -3}, {1, -4, -5, -6}, 3);
+    Tensor T4C1T1A = contract(T4C1T1, A, {-1, 1, -2, -3, 2, -4}, {1, 2, -5, -6, -7}, 4);
+    Tensor C4T3 = contract(C4, T3, {-1, 1}, {-2, -3, 1, -4}, 1);
+    Tensor C4T3Ad = contract(C4T3, twist(Ad, 3), {-1, -2, 1, -3}, {-4, -5, -6, -7, 1}, 3);
+    Tensor left = contract(T4C1T1A, C4T3Ad, {1, 2, -1, 3, -2, 4, -3}, {1, 4, -4, 2, 3, -5, -6}, 3);
+    Tensor T1C2 = contract(T1, C2, {-1, 1, -2, -3}, {1, -4}, 3);
+    Tensor T1C2T2 = contract(T1C2, T2, {-1, -2, -3, 1}, {-4, -5, 1, -6}, 3);
+    Tensor AT1C2T2 = contract(twist(A, 1), T1C2T2, {-1, 1, 2, -2, -3}, {-4, 1, -5, 2, -6, -7}, 3);
+    Tensor T3C3 = contract(T3, C3, {-1, -2, -3, 1}, {-4, 1}, 3);
+    Tensor T3C3Ad = contract(T3C3, Ad, {-1, 1, -2, -3}, {-4, -5, -6, -7, 1}, 3);
+    Tensor right = contract(AT1C2T2, T3C3Ad, {-1, 1, -2, -3, 2, 3, 4}, {1, -4, 4, -5, 2, -6, 3}, 3);
+    Tensor rho = contract(left, right, {1, 2, -3, 3, -1, 4}, {2, -4, 1, 3, 4, -2}, 2);
+    Tensor id2 = identity(rho.meta->sym, rho.meta->cod, rho.meta->dom);
+    const double norm = scalar_value(contract(rho, twist(twist(id2, 0), 1), {1, 2, 3, 4}, {3, 4, 1, 2}, 0));
+    return scale(rho, 1.0 / norm);
+  }
+  // computeRDM_v, TRank == 2 (src/PEPS/CTM.cpp:756-781)
+  Tensor C1T1 = contract(C1, T1, {-1, 1}, {1, -2, -3, -4}, 1);
+  Tensor T4C1T1 = contract(T4, twist(C1T1, 0), {1, -1, -2, -3}, {1, -4, -5, -6}, 3);
+  Tensor T4C1T1A = contract(T4C1T1, A, {-1, 1, -2, -3, 2, -4}, {1, 2, -5, -6, -7}, 4);
+  Tensor C2T2 = contract(C2, T2, {-1, 1}, {-2, -3, 1, -4}, 1);
+  Tensor AdC2T2 = contract(twist(twist(Ad, 3), 4), C2T2, {-1, -2, -3, 1, -4}, {-5, -6, 1, -7}, 4);
+  Tensor upper = contract(T4C1T1A, AdC2T2, {-1, 1, 2, 3, 4, -2, -3}, {1, 3, -4, -5, 2, 4, -6}, 3);
+  Tensor C4T3 = contract(C4, T3, {-1, 1}, {-2, -3, 1, -4}, 1);
+  Tensor T4C4T3 = contract(T4, C4T3, {-1, 1, -2, -3}, {1, -4, -5, -6}, 3);
+  Tensor AT4C4T3 = contract(twist(A, 0), T4C4T3, {1, -1, -2, 2, -3}, {-4, 1, -5, 2, -6, -7}, 3);
+  Tensor T2C3 = contract(T2, C3, {-1, -2, -3, 1}, {1, -4}, 3);
+  Tensor T2C3Ad = contract(T2C3, Ad, {-1, 1, -2, -3}, {-4, -5, -6, 1, -7}, 3);
+  Tensor lower = contract(AT4C4T3, T2C3Ad, {-1, 1, -2, -3, 2, 3, 4}, {1, -4, 4, 2, -5, -6, 3}, 3);
+  Tensor rho = contract(upper, lower, {1, 2, -3, -1, 3, 4}, {2, -4, 1, 4, 3, -2}, 2);
+  Tensor id2 = identity(rho.meta->sym, rho.meta->cod, rho.meta->dom);
+  const double norm = scalar_value(contract(rho, twist(twist(id2, 0), 1), {1, 2, 3, 4}, {3, 4, 1, 2}, 0));
+  return scale(rho, 1.0 / norm);
+}
+
+double scalar_value(const Tensor& t0) {
+  Tensor t = materialize(t0);
+  if (t.meta->size == 0) return 0.0;
+  if (t.meta->size != 1) throw std::runtime_error("scalar_value: tensor holds more than one entry");
+  double v = 0;
+  cuda_ok(cudaMemcpyAsync(&v, t.data(), sizeof(double), cudaMemcpyDeviceToHost, stream()), "d2h");
+  cuda_ok(cudaStreamSynchronize(stream()), "sync");
+  return v;
+}
+
+double bond_expectation(const Tensor& rho, const Tensor& op) {
+  return scalar_value(contract(twist(twist(rho, 0), 1), op, {1, 2, 3, 4}, {3, 4, 1, 2}, 0));
+}
+
 std::pair<Tensor, Tensor> CTM::get_projectors(char dir) {
   // get_projectors, PROJECTION::CORNER (src/PEPS/CTM.cpp:1195-1326)
   switch (dir) {
     case 'L': {
       Tensor Q1 = contract_corner("UL");
       Tensor Q4 = tw(contract_corner("LL"), {3, 4, 5});
-      return decompose(Q4, Q1, chi);
+      return decompose_dir(0, Q4, Q1);
     }
     case 'R': {
       Tensor Q2 = contract_corner("UR");
       Tensor Q3 = contract_corner("LR");
-      return decompose(Q2, Q3, chi);
+      return decompose_dir(1, Q2, Q3);
     }
     case 'T': {
       Tensor Q1 = contract_corner("UL");
       Tensor Q2 = contract_corner("UR");
-      return decompose(Q1, Q2, chi);
+      return decompose_dir(2, Q1, Q2);
     }
     default: {
       Tensor Q4 = tw(contract_corner("LL"), {0, 1, 2});
       Tensor Q3 = contract_corner("LR");
-      return decompose(Q3, Q4, chi);
+      return decompose_dir(3, Q3, Q4);
     }
   }
 }

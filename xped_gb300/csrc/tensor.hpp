@@ -11,6 +11,7 @@
 #include <cstdint>
 #include <memory>
 #include <string>
+#include <map>
 #include <tuple>
 #include <unordered_map>
 #include <vector>
@@ -82,9 +83,44 @@ struct SVDResult {
   Tensor U, S, Vdag;
   double trunc_weight = 0.0, entropy = 0.0;
   std::vector<int> keep;  // kept singular values per input sector
-  // full spectrum of the input (device), for the learned-rank path
+  // every computed singular value of the input (host copy, descending per
+  // sector): sector i owns spectrum[spec_begin[i] .. spec_begin[i+1])
+  std::vector<double> spectrum;
+  std::vector<int64_t> spec_begin;
 };
 SVDResult tsvd(const Tensor& t, int64_t max_keep, double eps_svd, bool preserve_multiplets);
+
+// Per-sector singular triplets of one tensor in flat device buffers: sector i
+// owns k[i] values S[s_begin[i] .. s_begin[i+1]), U block rows(i) x k[i] at
+// u_off[i] (ld rows(i)) and V^T block k[i] x cols(i) at v_off[i] (ld k[i]),
+// values descending within a sector.
+struct Spectra {
+  double *U = nullptr, *S = nullptr, *V = nullptr;
+  std::vector<int64_t> k, u_off, v_off, s_begin;
+  int64_t* d_s_begin = nullptr;  // optional cached device copies
+  int32_t* d_deg = nullptr;
+};
+// cutoff_matrices on given spectra (shared by the exact and randomized tSVD)
+SVDResult truncate_spectra(const TensorMeta& m, const Spectra& sp, int64_t max_keep, double eps_svd,
+                           bool preserve_multiplets);
+
+// Randomized blockwise tSVD (the chosen form).  Sector i is sketched with
+// sketch[i] seeded Gaussian columns (stream i of `seed`), refined by
+// `power_iters` subspace iterations, and decomposed exactly in the sketch
+// space: Q = orth(A Omega), B = Q^T A = U_B S V^T, U = Q U_B.  Sectors with
+// sketch[i] <= 0 or 2 sketch[i] >= min(rows, cols) are decomposed exactly.
+// A sketched sector that keeps all of its sketch columns (its next value was
+// never seen) is redone with twice the columns, exactly after the third
+// doubling, so the kept set is the one of the exact tSVD whenever the sketch
+// resolves the kept values.
+struct RsvdInfo {
+  std::vector<int64_t> width;  // columns used per sector (min(rows, cols) for exact sectors)
+  std::vector<int> saturated;  // sector indices, once per redo
+  int64_t sketch_cols = 0;     // sum of widths over sketched sectors
+  int exact_sectors = 0;
+};
+SVDResult tsvd_randomized(const Tensor& t, int64_t max_keep, double eps_svd, const std::vector<int64_t>& sketch,
+                          int power_iters, uint64_t seed, RsvdInfo* info = nullptr);
 std::pair<Tensor, Tensor> tqr(const Tensor& t);
 std::pair<Tensor, Tensor> decompose(const Tensor& t1, const Tensor& t2, int64_t max_nsv);
 
@@ -94,6 +130,51 @@ struct ContractPerms {
   int shift1 = 0, shift2 = 0, shiftres = 0;
 };
 ContractPerms get_permutations(const std::vector<int>& a1, int rank1, const std::vector<int>& a2, int rank2, int rankres);
+
+// P1 = S^-1/2 U^dag T1, P2 = T2 V S^-1/2 from a tSVD of T1*T2 (PEPSContractions.cpp:30-40)
+std::pair<Tensor, Tensor> projectors_from_svd(const SVDResult& r, const Tensor& t1, const Tensor& t2);
+
+// Last projector decomposition of one CTM direction, per sector charge.
+struct SectorHistory {
+  int64_t rows = 0, cols = 0, keep = 0, width = 0;
+  double s_first = 0, s_last = 0, s_next = 0;  // first / last kept value, first dropped value (0 if none)
+  double s_max = 0;                            // largest value of the whole matrix
+};
+using History = std::map<int, SectorHistory>;
+
+// Sketch widths of the randomized projector SVD.
+struct WidthPolicy {
+  virtual ~WidthPolicy() = default;
+  // one width per sector of `m` (sector order); <= 0 asks for an exact sector
+  virtual std::vector<int64_t> widths(const TensorMeta& m, const History& last, int64_t chi) = 0;
+};
+// Without a model: last kept count + max(oversample, growth * kept); sectors
+// with no history are decomposed exactly.
+struct HistoryPolicy : WidthPolicy {
+  int64_t oversample = 16;
+  double growth = 0.5;
+  std::vector<int64_t> widths(const TensorMeta& m, const History& last, int64_t chi) override;
+};
+
+// Per-sector input features of the rank predictor (kFeatures floats per
+// sector, sector order), from the matrix shape and the direction's history.
+constexpr int kFeatures = 8;
+void sector_features(const TensorMeta& m, const History& last, int64_t chi, std::vector<float>& out);
+
+// One projector decomposition as seen by the learner: the features it was
+// predicted from and what the decomposition then kept.
+struct DecompRecord {
+  int dir = 0;
+  std::vector<int> sectors;
+  std::vector<float> features;            // sectors x kFeatures
+  std::vector<int64_t> keep, width, kmin;
+  std::vector<double> spectrum;           // all computed values, per sector
+  std::vector<int64_t> spec_begin;
+};
+
+struct CTMStats {
+  int64_t decompositions = 0, sketched_sectors = 0, exact_sectors = 0, redo = 0, sketch_cols = 0;
+};
 
 // CTMRG environment on a 1x1 unit cell (src/PEPS/CTM.cpp).
 class CTM {
@@ -105,13 +186,31 @@ class CTM {
   Tensor contract_corner(const char* corner);
   std::pair<Tensor, Tensor> get_projectors(char dir);
   std::tuple<Tensor, Tensor, Tensor> renormalize(char dir, const Tensor& P1, const Tensor& P2);
+  // computeRDM_h / computeRDM_v (src/PEPS/CTM.cpp:583-627, 756-790), normalised
+  Tensor rdm(bool vertical);
   Tensor& slot(int which);  // 0..3 = C1..C4, 4..7 = T1..T4, 8 = A, 9 = Adag
   int64_t chi = 0;
 
+  // projector SVD form: 0 exact FP64 tSVD, 1 randomized with `policy` widths
+  int svd_mode = 0;
+  int power_iters = 3;
+  uint64_t seed = 1;
+  std::shared_ptr<WidthPolicy> policy;
+  bool record = false;
+  std::vector<DecompRecord> records;
+  CTMStats stats;
+  History hist[4];
+
  private:
+  std::pair<Tensor, Tensor> decompose_dir(int d, const Tensor& t1, const Tensor& t2);
   Tensor A, Ad;
   Tensor C1, C2, C3, C4, T1, T2, T3, T4;
 };
+
+// avg of a two-site operator (src/PEPS/LinearAlgebra.cpp:58-64)
+double bond_expectation(const Tensor& rho, const Tensor& op);
+// the single entry of a rank-0 tensor (0 if it holds no sector)
+double scalar_value(const Tensor& t);
 
 // Host-side plan tables (what the permute / GEMM kernels consume), built
 // without touching the device; used by the CPU tests and by the plan caches.

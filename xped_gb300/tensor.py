@@ -222,6 +222,26 @@ class Tensor:
                                     C.byref(S), C.byref(V), C.byref(tw), C.byref(ent), keep), "tSVD")
         return Tensor(U.value), Tensor(S.value), Tensor(V.value), tw.value, ent.value, list(keep[:n])
 
+    def tSVD_randomized(self, max_keep: int, eps_svd: float, sketch: Sequence[int], power_iters: int = 1,
+                        seed: int = 0):
+        """Randomized blockwise tSVD: ``sketch[i]`` Gaussian columns for sector i
+        (<= 0: exact).  Returns (U, S, V, truncWeight, entropy, keep, width,
+        n_saturated)."""
+        U, S, V = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        tw, ent = C.c_double(), C.c_double()
+        n = len(self.sectors()[0])
+        if len(sketch) != n:
+            raise ValueError("one sketch width per sector required")
+        keep = (C.c_int32 * max(n, 1))()
+        width = (C.c_int64 * max(n, 1))()
+        nsat = C.c_int32()
+        sk = (C.c_int64 * max(n, 1))(*[int(x) for x in sketch])
+        check(lib().xgb_tensor_tsvd_randomized(self._h, int(max_keep), float(eps_svd), n, sk, int(power_iters),
+                                               int(seed), C.byref(U), C.byref(S), C.byref(V), C.byref(tw),
+                                               C.byref(ent), keep, width, C.byref(nsat)), "tSVD_randomized")
+        return (Tensor(U.value), Tensor(S.value), Tensor(V.value), tw.value, ent.value, list(keep[:n]),
+                list(width[:n]), nsat.value)
+
     def tQR(self):
         Q, R = C.c_void_p(), C.c_void_p()
         check(lib().xgb_tensor_tqr(self._h, C.byref(Q), C.byref(R)), "tQR")
@@ -306,3 +326,63 @@ class CTM:
 
     def env(self):
         return {k: self.get(k) for k in ("C1", "C2", "C3", "C4", "T1", "T2", "T3", "T4")}
+
+    # -- projector SVD form, statistics, decomposition log --------------------------------
+    def set_svd(self, mode: str = "exact", power_iters: int = 3, seed: int = 1, oversample: int = 16,
+                growth: float = 0.5):
+        """``mode`` "exact" (full FP64 tSVD) or "randomized" (sketch widths from the
+        direction's last kept counts + max(oversample, growth * kept))."""
+        m = {"exact": 0, "randomized": 1}[mode]
+        check(lib().xgb_ctm_set_svd(self._h, m, int(power_iters), int(seed), int(oversample), float(growth)),
+              "ctm_set_svd")
+        return self
+
+    def stats(self):
+        out = (C.c_int64 * 5)()
+        check(lib().xgb_ctm_stats(self._h, out), "ctm_stats")
+        return dict(zip(("decompositions", "sketched_sectors", "exact_sectors", "redo", "sketch_cols"), out))
+
+    def record(self, on: bool = True):
+        check(lib().xgb_ctm_record(self._h, int(on)), "ctm_record")
+        return self
+
+    def records(self):
+        """Logged projector decompositions: dicts with dir, sectors, features
+        (n x F float32), keep, width, kmin, spectrum (list of per-sector arrays)."""
+        out = []
+        L = lib()
+        for i in range(L.xgb_ctm_record_count(self._h)):
+            d, n, ns = C.c_int(), C.c_int(), C.c_int64()
+            check(L.xgb_ctm_record_get(self._h, i, C.byref(d), C.byref(n), C.byref(ns), None, None, None, None, None,
+                                       None, None), "ctm_record_get")
+            k = n.value
+            sec = np.zeros(k, np.int32)
+            feats = np.zeros(k * FEATURES, np.float32)
+            keep = np.zeros(k, np.int64)
+            width = np.zeros(k, np.int64)
+            kmin = np.zeros(k, np.int64)
+            spec = np.zeros(max(ns.value, 1))
+            sb = np.zeros(k + 1, np.int64)
+            f = lambda a, t: a.ctypes.data_as(C.POINTER(t))
+            check(L.xgb_ctm_record_get(self._h, i, None, None, None, f(sec, C.c_int32), f(feats, C.c_float),
+                                       f(keep, C.c_int64), f(width, C.c_int64), f(kmin, C.c_int64),
+                                       f(spec, C.c_double), f(sb, C.c_int64)), "ctm_record_get")
+            out.append(dict(dir=d.value, sectors=sec.tolist(), features=feats.reshape(k, FEATURES), keep=keep,
+                            width=width, kmin=kmin, spectrum=[spec[sb[a]:sb[a + 1]].copy() for a in range(k)]))
+        return out
+
+    # -- observables ------------------------------------------------------------------------
+    def rdm_h(self) -> Tensor:
+        return Tensor(lib().xgb_ctm_rdm(self._h, 0))
+
+    def rdm_v(self) -> Tensor:
+        return Tensor(lib().xgb_ctm_rdm(self._h, 1))
+
+
+FEATURES = 8  # per-sector inputs of the rank predictor
+
+
+def bond_expectation(rho: Tensor, op: Tensor) -> float:
+    out = C.c_double()
+    check(lib().xgb_tensor_bond_expectation(rho._h, op._h, C.byref(out)), "bond_expectation")
+    return out.value
