@@ -1,17 +1,28 @@
 #!/usr/bin/env python
-"""CTMRG-step benchmark of the GB300 backend.
+"""CTMRG-step benchmark of the GB300 backend: chosen form against plain FP64.
 
 Workload (U(1) iPEPS, 1x1 unit cell): physical q in {-1,+1} (dim 2), virtual
-D=4 with q in {-1,0,1} and degeneracies [1,2,1], chi=32, site tensor N(0,1)
+D=6 with q in {-1,0,1} and degeneracies [2,2,2], chi=128, site tensor N(0,1)
 from a fixed seed, environment initialised FROM_A and grown for `warmup`
-steps (so chi is saturated) before timing.  One step = grow_all (left, right,
-top, bottom moves), all tensor work on the GPU in FP64.
+steps before timing (chi saturates at 128 after the first step).  One step =
+grow_all (left, right, top, bottom moves), all tensor work on the GPU.
+
+Forms, same workload, same GPU:
+  chosen   randomized projector SVD (seeded Gaussian sketches, 8 subspace
+           iterations, widths = the direction's last kept counts + max(16, 50 %),
+           exact FP64 fallback), FP64 SVD core / projectors / normalisation;
+           block GEMMs in FP64 or 3xTF32 (--gemm)
+  plain    the exact FP64 tSVD in every move (the reference algorithm)
+The energy per site (Heisenberg bonds, horizontal + vertical RDM) of both
+forms after the same number of steps from the same start is reported with
+their difference.
 
 Arms:
   default            this backend on cuda:LOCAL_RANK
   --impl reference   the CPU restatement of the reference algorithm (oracle
-                     port; the reference itself cannot be built here), all
-                     host cores, same workload and metric.
+                     port; the reference itself cannot be built here) on all
+                     host cores, same workload and metric; each timed sample
+                     is one CTM move, a step counted as four moves.
 Replicas only across GPUs: each rank runs the same workload independently.
 """
 from __future__ import annotations
@@ -30,12 +41,16 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-AUX = [(-1, 1), (0, 2), (1, 1)]
+AUX = [(-1, 2), (0, 2), (1, 2)]
 PHYS = [(-1, 1), (1, 1)]
-CHI = 32
+CHI = 128
 SEED = 1234
-METRIC = "CTMRG step throughput, U(1) iPEPS D=4 chi=32, plain FP64"
-WORKLOAD = "u1_ipeps_D4_chi32_ctmrg_step"
+AUX_SMALL = [(-1, 1), (0, 2), (1, 1)]  # D=4, chi=32: the plain FP64 GPU configuration
+CHI_SMALL = 32
+COMPARE_STEPS = 3
+POWER_ITERS = 8  # subspace iterations of the chosen form: energy within ~1e-9 of plain FP64 at this workload
+METRIC = "CTMRG step throughput, U(1) iPEPS D=6 chi=128, chosen form vs plain FP64"
+WORKLOAD = "u1_ipeps_D6_chi128_ctmrg_step"
 
 
 def dist_info():
@@ -95,33 +110,55 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_site_tensor_data(sizes_by_sector):
-    rng = np.random.default_rng(SEED)
-    return [rng.standard_normal(n) for n in sizes_by_sector]
+def site_tensor(aux_pairs):
+    from xped_gb300 import Basis, Tensor
+    aux = Basis.from_pairs("U1", aux_pairs)
+    phys = Basis.from_pairs("U1", PHYS)
+    A = Tensor.zeros([aux, aux], [aux, aux, phys])
+    A.set_data(np.random.default_rng(SEED).standard_normal(A.size))
+    return A, phys
+
+
+def make_ctm(A, chi, form, gemm):
+    from xped_gb300 import CTM
+    c = CTM(A, chi).init()
+    if form == "chosen":
+        c.set_svd("randomized", power_iters=POWER_ITERS, seed=SEED, oversample=16, growth=0.5)
+    c.set_gemm(gemm)
+    return c
 
 
 # ----------------------------------------------------------------------------- GPU arm
 def run_gpu(args):
     import ctypes as C
 
-    from xped_gb300 import CTM, Basis, Tensor, ensure_device, lib
+    from xped_gb300 import ensure_device, lib
     from xped_gb300._lib import profile_read
+    from xped_gb300.observables import energy, heisenberg_bond
 
     rank, world, local = dist_info()
     ensure_device(local)
     L = lib()
-    aux = Basis.from_pairs("U1", AUX)
-    phys = Basis.from_pairs("U1", PHYS)
-    A = Tensor.zeros([aux, aux], [aux, aux, phys])
-    qs, rs, cs = A.sectors()
-    A.set_data(np.concatenate(make_site_tensor_data([r * c for r, c in zip(rs, cs)])))
-    ctm = CTM(A, CHI).init()
-    for _ in range(args.warmup):
-        ctm.grow_all()
-    L.xgb_synchronize()
+    A, phys = site_tensor(AUX)
+    H = heisenberg_bond(phys)
+    res = {}
 
-    # L2 flush buffer (> 129 MB L2), written between timed steps outside the events
-    flush_bytes = 512 << 20
+    # ---- chosen form: warm-up (the energy after COMPARE_STEPS steps is kept for the comparison);
+    # its projector decompositions are logged to train the width predictor
+    t0 = time.perf_counter()
+    ctm = make_ctm(A, CHI, "chosen", args.gemm)
+    ctm.record(True)
+    e_chosen = None
+    for i in range(max(args.warmup, COMPARE_STEPS)):
+        ctm.grow_all()
+        if i + 1 == COMPARE_STEPS:
+            e_chosen = energy(ctm, H)
+    L.xgb_synchronize()
+    records = ctm.records()
+    ctm.record(False)
+    res["chosen_setup_s"] = time.perf_counter() - t0
+
+    flush_bytes = 512 << 20  # > 129 MB L2, written between timed steps outside the events
     flush = C.c_void_p()
     L.xgb_malloc(C.byref(flush), flush_bytes)
 
@@ -134,6 +171,7 @@ def run_gpu(args):
     time.sleep(0.4)
     step_ms = []
     launches0 = L.xgb_launch_count()
+    st0 = ctm.stats()
     for _ in range(args.steps):
         flush_l2()
         L.xgb_synchronize()
@@ -141,10 +179,15 @@ def run_gpu(args):
         ctm.grow_all()
         L.xgb_event_record(1)
         step_ms.append(L.xgb_event_elapsed_ms(0, 1))
-    launches = (L.xgb_launch_count() - launches0) / max(args.steps, 1)
-    clocks = sampler.stop()
+    st1 = ctm.stats()
+    res["cols_per_step"] = (st1["sketch_cols"] - st0["sketch_cols"]) / args.steps
+    res["redo_per_step"] = (st1["redo"] - st0["redo"]) / args.steps
+    res["launches"] = (L.xgb_launch_count() - launches0) / max(args.steps, 1)
+    res["clocks"] = sampler.stop()
+    res["step_ms"] = float(np.mean(step_ms))
+    res["step_ms_all"] = step_ms
 
-    # ---- end to end: env + site tensor from pinned host buffers, result back to host
+    # ---- end to end: environment and site tensor from pinned host buffers, result back to host
     names = ["C1", "C2", "C3", "C4", "T1", "T2", "T3", "T4"]
     env = ctm.env()
     try:
@@ -157,7 +200,6 @@ def run_gpu(args):
         host_in[k][:] = env[k].data()
     host_A = pin(A.size)
     host_A[:] = A.data()
-    host_out = {k: None for k in names}
     e2e_ms = []
     h2d = d2h = 0
     for _ in range(args.steps):
@@ -170,28 +212,185 @@ def run_gpu(args):
             ctm.set(k, env[k])
         ctm.grow_all()
         out = ctm.env()
-        for k in names:
-            host_out[k] = out[k].data()
+        host_out = {k: out[k].data() for k in names}
         L.xgb_event_record(3)
         e2e_ms.append(L.xgb_event_elapsed_ms(2, 3))
         h2d = host_A.nbytes + sum(host_in[k].nbytes for k in names)
         d2h = sum(v.nbytes for v in host_out.values())
+    res["e2e_ms"] = float(np.mean(e2e_ms))
+    res["h2d"], res["d2h"] = h2d, d2h
 
-    # ---- kernel profile pass over the same steps (CUDA events around every launch)
+    # ---- kernel profile pass (CUDA events around every launch)
     L.xgb_profile_reset()
     L.xgb_profile_enable(1)
-    for _ in range(args.steps):
+    prof_steps = 2
+    for _ in range(prof_steps):
         flush_l2()
         ctm.grow_all()
     L.xgb_synchronize()
     L.xgb_profile_enable(0)
-    prof = profile_read()
-    L.xgb_free(flush)
+    res["prof"] = profile_read()
+    res["prof_steps"] = prof_steps
+    res["sketch"] = ctm.stats()
+    res["ctm"] = ctm
 
-    t_step = float(np.mean(step_ms))
-    t_e2e = float(np.mean(e2e_ms))
-    res = dict(step_ms=t_step, e2e_ms=t_e2e, launches=launches, clocks=clocks, prof=prof, h2d=h2d, d2h=d2h)
+    # ---- learned widths: the rank predictor trained (device kernels) on the chosen run's own
+    # logged spectra, then a fresh run with predicted widths
+    if not args.no_learned:
+        from xped_gb300.learn import RankModel, dataset
+        X, T = dataset(records)
+        model = RankModel(seed=SEED)
+        t0 = time.perf_counter()
+        loss0 = model.gradient(X, T)[0]
+        loss = model.train(X, T, steps=2000, lr=2e-3)
+        res["learned_train"] = {"samples": int(X.shape[0]), "adam_steps": 2000, "loss_first": loss0,
+                                "loss_last": loss, "seconds": time.perf_counter() - t0}
+        lc = make_ctm(A, CHI, "plain", args.gemm)  # exact first step, then predicted widths
+        lc.set_rank_model(model, margin=0.0, min_oversample=2, power_iters=POWER_ITERS, seed=SEED)
+        for _ in range(COMPARE_STEPS):
+            lc.grow_all()
+        res["e_learned"] = energy(lc, H)
+        s0 = lc.stats()
+        ms = []
+        for _ in range(args.steps):
+            flush_l2()
+            L.xgb_synchronize()
+            L.xgb_event_record(8)
+            lc.grow_all()
+            L.xgb_event_record(9)
+            ms.append(L.xgb_event_elapsed_ms(8, 9))
+        s1 = lc.stats()
+        res["learned_ms"] = float(np.mean(ms))
+        res["learned_cols_per_step"] = (s1["sketch_cols"] - s0["sketch_cols"]) / args.steps
+        res["learned_redo_per_step"] = (s1["redo"] - s0["redo"]) / args.steps
+        del lc
+
+    # ---- plain FP64 form, same workload: COMPARE_STEPS steps, the last one timed
+    if not args.no_plain:
+        t0 = time.perf_counter()
+        plain = make_ctm(A, CHI, "plain", "fp64")
+        for _ in range(COMPARE_STEPS - 1):
+            plain.grow_all()
+        flush_l2()
+        L.xgb_synchronize()
+        L.xgb_event_record(4)
+        plain.grow_all()
+        L.xgb_event_record(5)
+        res["plain_ms"] = L.xgb_event_elapsed_ms(4, 5)
+        res["e_plain"] = energy(plain, H)
+        res["plain_wall_s"] = time.perf_counter() - t0
+        del plain
+    res["e_chosen"] = e_chosen
+
+    # ---- plain FP64 at D=4 chi=32 (the reference's GPU configuration), for the record
+    A4, _ = site_tensor(AUX_SMALL)
+    small = make_ctm(A4, CHI_SMALL, "plain", "fp64")
+    for _ in range(3):
+        small.grow_all()
+    ms = []
+    for _ in range(3):
+        flush_l2()
+        L.xgb_synchronize()
+        L.xgb_event_record(6)
+        small.grow_all()
+        L.xgb_event_record(7)
+        ms.append(L.xgb_event_elapsed_ms(6, 7))
+    res["small_plain_ms"] = float(np.mean(ms))
+    L.xgb_free(flush)
+    res["gemm_sweep"] = gemm_sweep()
     return res
+
+
+# ----------------------------------------------------------------------------- block-GEMM sweep
+def gemm_sweep(reps=5):
+    """Grouped block GEMMs FP64 vs 3xTF32: (i) the sector GEMMs of an SU(2)
+    Tensor<2,2> product (irreps q = 2j+1, j = 0..3 integer, multiplicities 1-24);
+    (ii) synthetic lists of G blocks, m, n, k log-uniform in [8, 512].  Useful
+    TFLOP/s = sum 2mnk / time; error = max over blocks of ||C - C_fp64||_F / ||C_fp64||_F."""
+    import ctypes as C
+
+    from xped_gb300 import Basis, Tensor, lib
+    from xped_gb300._lib import GemmDesc, check
+    from xped_gb300.tensor import set_gemm_precision
+    L = lib()
+    rng = np.random.default_rng(SEED)
+    out = {}
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        L.xgb_synchronize()
+        L.xgb_event_record(10)
+        for _ in range(reps):
+            fn()
+        L.xgb_event_record(11)
+        return L.xgb_event_elapsed_ms(10, 11) / reps
+
+    # (i) SU(2) contraction blocks through the tensor API
+    pairs = [(q, int(rng.integers(1, 25))) for q in (1, 3, 5, 7)]
+    B = Basis.from_pairs("SU2", pairs)
+    T1 = Tensor.zeros([B, B], [B, B])
+    T2 = Tensor.zeros([B, B], [B, B])
+    T1.set_data(rng.standard_normal(T1.size))
+    T2.set_data(rng.standard_normal(T2.size))
+    descs = T1.gemm_plan(T2)[0]
+    flops = sum(2.0 * d.m * d.n * d.k for d in descs)
+    res = {}
+    ref = None
+    for form in ("fp64", "3xtf32"):
+        set_gemm_precision(form)
+        ms = timed(lambda: T1.matmul(T2))
+        Cm = T1.matmul(T2)
+        set_gemm_precision("fp64")
+        blocks = Cm.blocks()
+        if ref is None:
+            ref = blocks
+            err = 0.0
+        else:
+            err = max(np.linalg.norm(blocks[q] - ref[q]) / max(np.linalg.norm(ref[q]), 1e-300) for q in ref)
+        res[form] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "max_rel_err": err}
+    out["su2_tensor22"] = dict(res, blocks=len(descs), gflop=flops / 1e9,
+                               multiplicities=[d for _, d in pairs])
+
+    # (ii) synthetic grouped lists
+    for G in (40, 100, 200, 400):
+        dims = np.exp(rng.uniform(np.log(8), np.log(512), size=(G, 3))).astype(int)
+        ds, ao, bo, co = [], 0, 0, 0
+        for m, n, k in dims:
+            ds.append(GemmDesc(int(m), int(n), int(k), ao, int(m), bo, int(k), co, int(m), 0, 0))
+            ao += m * k
+            bo += k * n
+            co += m * n
+        arr = (GemmDesc * G)(*ds)
+        flops = float(sum(2.0 * m * n * k for m, n, k in dims))
+        bufs = []
+        for nel in (ao, bo, co):
+            p_ = C.c_void_p()
+            check(L.xgb_malloc(C.byref(p_), 8 * int(nel)), "malloc")
+            bufs.append(p_)
+        for p_, nel in zip(bufs[:2], (ao, bo)):
+            h = rng.standard_normal(int(nel))
+            L.xgb_memcpy_h2d(p_, h.ctypes.data, h.nbytes)
+        res = {}
+        ref = None
+        for prec, form in ((0, "fp64"), (1, "3xtf32")):
+            ms = timed(lambda: L.xgb_grouped_gemm(prec, G, arr, bufs[0], bufs[1], bufs[2], 1.0, 0.0, None))
+            check(L.xgb_gemm_tc_status(), "tensor-core gemm")
+            h = np.empty(int(co))
+            L.xgb_memcpy_d2h(h.ctypes.data, bufs[2], h.nbytes)
+            if ref is None:
+                ref, err = h, 0.0
+            else:
+                err, o = 0.0, 0
+                for m, n, k in dims:
+                    a, b = h[o:o + m * n], ref[o:o + m * n]
+                    err = max(err, float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)))
+                    o += m * n
+            res[form] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "max_rel_err": err}
+        for p_ in bufs:
+            L.xgb_free(p_)
+        out[f"synthetic_G{G}"] = dict(res, gflop=flops / 1e9)
+    return out
 
 
 def roofline(prof, steps):
@@ -215,6 +414,12 @@ def roofline(prof, steps):
         out = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
                "peak_source": "nominal GB300 FP64 rate (MEASURED_PEAKS.json has no FP64 figure)",
                "work": "LAPACK-equivalent flops" if dom == "svd_jacobi" else "useful flops"}
+    elif dom == "gemm_tc":
+        tf = peaks.get("bf16_tflops", 1900.0) / 2.0  # dense TF32 issues at half the BF16 rate
+        achieved = per_launch_work / (per_launch_ms * 1e-3) / 1e12
+        out = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": tf, "unit": "TFLOP/s",
+               "peak_source": "half of MEASURED_PEAKS.json bf16_tflops (dense TF32 rate)",
+               "work": "useful flops (each taken as three TF32 products)"}
     else:
         achieved = per_launch_work / (per_launch_ms * 1e-3) / 1e9
         out = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -224,36 +429,49 @@ def roofline(prof, steps):
     out["launches_per_step"] = n / max(steps, 1)
     out["ms_per_launch"] = per_launch_ms
     out["kernel_share"] = {k: round(v[1] / sum(x[1] for x in kinds.values()), 4) for k, v in kinds.items()}
+    out["kernel_ms_per_step"] = {k: round(v[1] / max(steps, 1), 3) for k, v in kinds.items()}
     return out
 
 
 # ----------------------------------------------------------------------------- CPU oracle
-def cpu_ctm_steps(n_steps, warmup, budget_s=None):
+def oracle_ctm(aux_pairs, chi):
     import oracle
     from oracle.basis import Qbasis
     from oracle.ctm import CTM as OCTM
     from oracle.ctm import IPEPS
 
     s = oracle.make_symmetry("u1")
-    aux = Qbasis.from_pairs(s, AUX)
+    aux = Qbasis.from_pairs(s, aux_pairs)
     phys = Qbasis.from_pairs(s, PHYS)
     peps = IPEPS(s, aux, phys)
-    data = make_site_tensor_data([b.size for b in peps.A.blocks])
+    data = np.random.default_rng(SEED).standard_normal(sum(b.size for b in peps.A.blocks))
+    o = 0
     for i, b in enumerate(peps.A.blocks):
-        peps.A.blocks[i] = data[i].reshape(b.shape, order="F")
+        peps.A.blocks[i] = data[o:o + b.size].reshape(b.shape, order="F")
+        o += b.size
     peps.update_adag()
-    c = OCTM(peps, CHI).init()
-    for _ in range(warmup):
-        c.grow_all()
+    return OCTM(peps, chi).init()
+
+
+def time_moves(c, n_moves):
     times = []
-    t_start = time.perf_counter()
-    for _ in range(n_steps):
+    for i in range(n_moves):
         t0 = time.perf_counter()
-        c.grow_all()
+        c.move("LRTB"[i % 4])
         times.append(time.perf_counter() - t0)
-        if budget_s is not None and time.perf_counter() - t_start > budget_s:
-            break
     return times
+
+
+def cpu_baseline_from_device(ctm):
+    """One move of the oracle port on a host copy of the device environment
+    (saturated chi), all host cores."""
+    import oracle
+    from oracle.convert import ctm_from_native
+    oc = ctm_from_native(oracle.make_symmetry("u1"), ctm, CHI)
+    t = time_moves(oc, 1)[0]
+    return {"value": 1.0 / (4.0 * t), "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"one left move ({t:.1f} s) of the numpy/OpenBLAS oracle on a host copy of the saturated "
+                      "device environment; step time counted as four moves"}
 
 
 def main():
@@ -262,23 +480,34 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--gemm", default="fp64", choices=["fp64", "3xtf32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-width run")
     args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
     rank, world, local = dist_info()
+    config = {"workload": WORKLOAD, "chi": CHI, "D": 6, "aux": "q -1,0,1 deg [2,2,2]", "phys": 2, "cell": "1x1",
+              "l2": "512 MB buffer written between timed steps (outside the timed events)"}
 
     if args.impl == "reference":
         if rank != 0:
             return
-        times = cpu_ctm_steps(args.steps, args.warmup)
-        t = float(np.mean(times))
+        c = oracle_ctm(AUX, CHI)
+        for _ in range(args.warmup):
+            c.grow_all()
+        times = time_moves(c, args.steps)
+        t = 4.0 * float(np.mean(times))
         v = 1.0 / t
         line = {"metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus, "steps": len(times),
                 "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded N(0,1) site tensor)",
-                "config": {"workload": WORKLOAD, "chi": CHI, "D": 4, "phys": 2, "cell": "1x1"},
+                "config": dict(config, form="reference algorithm (exact FP64 tSVD), numpy/OpenBLAS"),
                 "impl": "reference",
                 "cpu_baseline": {"value": v, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-                                 "sample": f"{len(times)} grow_all steps after {args.warmup} warm-up steps"},
+                                 "sample": f"{len(times)} single moves (L, R, T, B in turn) after {args.warmup} "
+                                           "warm-up steps; step time counted as four moves"},
                 "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -298,22 +527,41 @@ def main():
     if rank != 0:
         return
     value = world * 1e3 / t_step
+    prof = r["prof"]
+    gemm_kind = "gemm_tc" if args.gemm == "3xtf32" else "gemm_f64"
+    g = prof.get(gemm_kind, (0, 0.0, 0.0))
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded N(0,1) site tensor)",
-            "config": {"workload": WORKLOAD, "chi": CHI, "D": 4, "phys": 2, "cell": "1x1",
-                       "l2": "512 MB buffer written between timed steps (outside the timed events)",
-                       "parallelism": f"replicas x{world}"},
+            "vs_baseline": None, "dtype": "f64" if args.gemm == "fp64" else "f64 (3xtf32 block GEMMs)",
+            "data": "synthetic (seeded N(0,1) site tensor)",
+            "config": dict(config, form=f"chosen: randomized projector SVD ({POWER_ITERS} subspace iterations, widths last kept "
+                                        "+ max(16, 50%), exact FP64 fallback), FP64 SVD core",
+                           gemm=args.gemm, parallelism=f"replicas x{world}"),
             "e2e": {"value": world * 1e3 / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"]},
             "gpu_launches": r["launches"], "clocks": r["clocks"],
-            "roofline": roofline(r["prof"], args.steps)}
+            "roofline": roofline(prof, r["prof_steps"]),
+            "block_gemm": {"form": args.gemm, "tflops": (g[2] / (g[1] * 1e-3) / 1e12) if g[1] > 0 else None,
+                           "ms_per_step": g[1] / r["prof_steps"]},
+            "sketch": dict(r["sketch"], cols_per_step=r["cols_per_step"], redo_per_step=r["redo_per_step"]),
+            "step_ms_each": [round(x, 3) for x in r["step_ms_all"]]}
+    if "plain_ms" in r:
+        line["plain_fp64"] = {"ms_per_step": r["plain_ms"], "steps_per_s": 1e3 / r["plain_ms"],
+                              "timed": f"step {COMPARE_STEPS} of a fresh plain run (one step)"}
+        line["chosen_vs_plain"] = r["plain_ms"] / t_step
+        line["energy"] = {"after_steps": COMPARE_STEPS, "chosen": r["e_chosen"], "plain": r["e_plain"],
+                          "abs_diff": abs(r["e_chosen"] - r["e_plain"]),
+                          "observable": "Heisenberg energy per site (rho_h + rho_v bonds)"}
+    if "learned_ms" in r:
+        line["learned_widths"] = {"ms_per_step": r["learned_ms"], "steps_per_s": 1e3 / r["learned_ms"],
+                                  "sketch_cols_per_step": r["learned_cols_per_step"],
+                                  "redo_per_step": r["learned_redo_per_step"], "train": r["learned_train"]}
+        if "e_plain" in r:
+            line["learned_widths"]["energy_abs_diff_vs_plain"] = abs(r["e_learned"] - r["e_plain"])
+    line["plain_fp64_D4_chi32_ms_per_step"] = r["small_plain_ms"]
+    line["block_gemm_sweep"] = r["gemm_sweep"]
     if not args.no_cpu_baseline:
-        times = cpu_ctm_steps(30, 1, budget_s=12.0)
-        tc = float(np.mean(times))
-        line["cpu_baseline"] = {"value": 1.0 / tc, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"{len(times)} grow_all steps of the same workload after 1 warm-up step, "
-                                          "numpy/OpenBLAS on all host cores"}
+        line["cpu_baseline"] = cpu_baseline_from_device(r["ctm"])
     print(json.dumps(line))
 
 

@@ -104,6 +104,14 @@ void xgb_ctm_release(xgb_ctm c);
    widths are the direction's last kept counts + max(oversample, growth * kept)
    (exact for sectors not seen before); power_iters subspace iterations. */
 int xgb_ctm_set_svd(xgb_ctm c, int mode, int power_iters, uint64_t seed, int64_t oversample, double growth);
+/* Precision form of the block GEMMs behind xgb_tensor_matmul / xgb_tensor_contract
+   issued from the calling host thread: XGB_PREC_FP64 (default) or XGB_PREC_3XTF32
+   (xgb.h).  Selects what XPED_MATRIX_LIB selects for operator* in the reference. */
+int xgb_set_gemm_precision(int precision);
+/* Precision form of the block GEMMs in the corner contractions and the
+   renormalisation of the moves (XGB_PREC_FP64 or XGB_PREC_3XTF32 from xgb.h);
+   the projector SVD, the projector construction and the normalisation stay FP64. */
+int xgb_ctm_set_gemm_precision(xgb_ctm c, int precision);
 /* out5: decompositions, sketched sectors, exact sectors, sketch redos, sketch columns */
 int xgb_ctm_stats(xgb_ctm c, int64_t* out5);
 /* Decomposition log for learning sketch widths (features of the rank predictor,

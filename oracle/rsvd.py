@@ -8,7 +8,8 @@ the device algorithm step by step so both can be compared on the same
 seeded test matrices:
 
   Omega_i = N(0,1) from (seed, stream i)          n_i x l_i
-  Q = orth(A Omega)                               left singular vectors
+  Q = orth(A Omega)                               left singular vectors (noise
+                                                  directions zeroed)
   repeat p times: Q = orth(A orth(A^T Q))
   B = Q^T A = U_B S V^T ,  U = Q U_B ,  sign convention of fix_svd_signs
 
@@ -51,8 +52,16 @@ def gaussian(seed: int, stream: int, count: int) -> np.ndarray:
     return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
 
 
+NOISE = 64.0 * 2.0 ** -53
+
+
 def _orth(Y):
-    return np.linalg.svd(Y, full_matrices=False)[0]
+    """Left singular vectors of Y; directions with singular value at
+    round-off level of the largest (<= NOISE * s_0) become zero columns."""
+    u, s, _ = np.linalg.svd(Y, full_matrices=False)
+    if s.size:
+        u[:, s <= NOISE * s[0]] = 0.0
+    return u
 
 
 def sketch_svd(A, l, power_iters, seed, stream):

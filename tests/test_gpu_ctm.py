@@ -106,3 +106,35 @@ def test_randomized_projectors_keep_the_energy():
     for a, b in zip(ex.records(), rz.records()):
         assert a["sectors"] == b["sectors"]
         assert list(a["keep"]) == list(b["keep"])
+
+
+def test_oracle_copy_of_device_ctm_continues_identically():
+    """A device CTM copied into the oracle (same bases, sectors and data)
+    gives the same environment after one more step on both sides."""
+    from oracle.convert import ctm_from_native
+    _, nc = _setup("u1", [(-1, 1), (0, 2), (1, 1)], [(-1, 1), (1, 1)], 12, 2)
+    for _ in range(2):
+        nc.grow_all()
+    s = oracle.make_symmetry("u1")
+    oc = ctm_from_native(s, nc, 12)
+    _compare(oc, nc, 0)
+    oc.grow_all()
+    nc.grow_all()
+    _compare(oc, nc, 1e-8)
+
+
+def test_split_precision_contractions_stay_close():
+    """3xTF32 block GEMMs in the corner contractions / renormalisation (the
+    projector SVD and construction in FP64): energy per site within 1e-6 of
+    the all-FP64 run after four steps."""
+    from xped_gb300.observables import energy, heisenberg_bond
+    _, ex = _setup("u1", [(-1, 1), (0, 2), (1, 1)], [(-1, 1), (1, 1)], 32, 7)
+    _, tc = _setup("u1", [(-1, 1), (0, 2), (1, 1)], [(-1, 1), (1, 1)], 32, 7)
+    tc.set_gemm("3xtf32")
+    for _ in range(4):
+        ex.grow_all()
+        tc.grow_all()
+    H = heisenberg_bond(ex.get("A").leg(4))
+    e_ex, e_tc = energy(ex, H), energy(tc, H)
+    print("energy fp64", e_ex, "3xtf32", e_tc, "diff", abs(e_ex - e_tc))
+    assert abs(e_ex - e_tc) < 1e-6

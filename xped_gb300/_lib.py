@@ -115,6 +115,8 @@ PROTOS = [
     ("xgb_ctm_grow_all", C.c_int, [P]),
     ("xgb_ctm_set_svd", C.c_int, [P, C.c_int, C.c_int, C.c_uint64, C.c_int64, C.c_double]),
     ("xgb_ctm_stats", C.c_int, [P, i64p]),
+    ("xgb_ctm_set_gemm_precision", C.c_int, [P, C.c_int]),
+    ("xgb_set_gemm_precision", C.c_int, [C.c_int]),
     ("xgb_ctm_record", C.c_int, [P, C.c_int]),
     ("xgb_ctm_record_count", C.c_int, [P]),
     ("xgb_ctm_record_get", C.c_int, [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), i64p, i32p,

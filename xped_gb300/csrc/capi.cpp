@@ -283,6 +283,24 @@ int xgb_ctm_set_svd(xgb_ctm c, int mode, int power_iters, uint64_t seed, int64_t
   })
 }
 
+int xgb_set_gemm_precision(int precision) {
+  GUARD(XGB_E_BADPLAN, {
+    if (precision != XGB_PREC_FP64 && precision != XGB_PREC_3XTF32)
+      return set_error(XGB_E_UNSUPPORTED, "GEMM precision form not available");
+    set_gemm_precision(precision);
+    return XGB_OK;
+  })
+}
+
+int xgb_ctm_set_gemm_precision(xgb_ctm c, int precision) {
+  GUARD(XGB_E_BADPLAN, {
+    if (precision != XGB_PREC_FP64 && precision != XGB_PREC_3XTF32)
+      return set_error(XGB_E_UNSUPPORTED, "GEMM precision form not available");
+    c->c->gemm_prec = precision;
+    return XGB_OK;
+  })
+}
+
 int xgb_ctm_stats(xgb_ctm c, int64_t* out5) {
   GUARD(XGB_E_BADPLAN, {
     const CTMStats& s = c->c->stats;

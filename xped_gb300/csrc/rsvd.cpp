@@ -92,19 +92,32 @@ void batched_svd(const std::vector<xgb_svd_desc>& d, const double* A, double* U,
   dev_free(W);
 }
 
-// Orthonormal basis of each tall m x l block of Y (left singular vectors) into Q.
+// Orthonormal basis of each tall m x l block of Y (left singular vectors) into
+// Q; directions whose singular value is at round-off level of the largest
+// (<= kNoise * s_0) are set to zero columns instead.
+constexpr double kNoise = 64.0 * 1.1102230246251565e-16;
+
 void orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64_t>& cols, const std::vector<int64_t>& y_off,
                     const double* Y, double* Q, cudaStream_t s) {
   std::vector<xgb_svd_desc> d;
-  int64_t so = 0, vo = 0;
+  std::vector<SignFixDesc> z;
+  int64_t so = 0, vo = 0, mx = 0;
   for (size_t i = 0; i < rows.size(); ++i) {
     d.push_back({rows[i], cols[i], y_off[i], y_off[i], so, vo});
+    z.push_back({rows[i], 0, cols[i], y_off[i], so});
+    mx = std::max(mx, cols[i]);
     so += cols[i];
     vo += cols[i] * cols[i];
   }
   double* Ss = alloc_d(so);
   double* Vs = alloc_d(vo);
   batched_svd(d, Y, Q, Ss, Vs, s);
+  Staging st;
+  const size_t o = st.add(z);
+  st.upload(s);
+  prof_begin(K_SKETCH, s);
+  launch_zero_noise_columns(st.at<SignFixDesc>(o), int(z.size()), mx, Ss, kNoise, Q, s);
+  prof_end(K_SKETCH, s, 8.0 * double(so));
   dev_free(Ss);
   dev_free(Vs);
 }

@@ -75,7 +75,28 @@ __global__ void sign_fix_kernel(const SignFixDesc* __restrict__ descs, double* _
   for (int64_t c = lane; c < d.n; c += 32) v[c * d.k] = -v[c * d.k];
 }
 
+// Zero the basis columns whose singular value is at round-off level of the
+// largest (s_j <= rel * s_0): their directions are noise of the sketch, and a
+// zero column keeps the basis orthonormal on the rest.
+__global__ void zero_noise_columns_kernel(const SignFixDesc* __restrict__ descs, const double* __restrict__ S,
+                                          double rel, double* __restrict__ Q) {
+  const SignFixDesc d = descs[blockIdx.y];  // m x k block of Q at u_off, singular values at v_off
+  const double s0 = S[d.v_off];
+  for (int64_t j = blockIdx.x; j < d.k; j += gridDim.x) {
+    if (S[d.v_off + j] > rel * s0) continue;
+    for (int64_t i = threadIdx.x; i < d.m; i += blockDim.x) Q[d.u_off + i + j * d.m] = 0.0;
+  }
+}
+
 }  // namespace
+
+void launch_zero_noise_columns(const SignFixDesc* d_descs, int n, int64_t max_k, const double* S, double rel, double* Q,
+                               cudaStream_t s) {
+  if (n <= 0 || max_k <= 0) return;
+  dim3 grid(unsigned(max_k < 1024 ? max_k : 1024), unsigned(n));
+  zero_noise_columns_kernel<<<grid, 128, 0, s>>>(d_descs, S, rel, Q);
+  count_launch();
+}
 
 void launch_gauss_fill(const GaussBlock* d_blocks, int n_blocks, int64_t max_count, uint64_t seed, double* out,
                        cudaStream_t s) {

@@ -54,6 +54,19 @@ constexpr int kCluster = 8;
 constexpr int kBlocks = 2 * kCluster;
 constexpr int kMaxSweeps32 = 30;
 constexpr int kMaxSweeps64 = 20;
+// Squared column norms at or below these fractions of the largest one are
+// left out of the rotations of the FP32 preconditioning and the FP64
+// polish.  Both are 0 (only exactly zero columns are skipped): positive
+// floors shortened rank-deficient inputs but changed the singular vectors of
+// the kept near-null directions that CTM projectors use.
+#ifndef XGB_SVD_FLOOR32
+#define XGB_SVD_FLOOR32 0.0f
+#endif
+#ifndef XGB_SVD_FLOOR64
+#define XGB_SVD_FLOOR64 0.0
+#endif
+constexpr float kFloor32 = XGB_SVD_FLOOR32;
+constexpr double kFloor64 = XGB_SVD_FLOOR64;
 constexpr int kSmemLimit = 200 * 1024;
 constexpr int kCgemmCols = 16;
 
@@ -99,10 +112,12 @@ __device__ __forceinline__ float angle32(float al, float be, float ga) {
 
 // One plane rotation between columns p and q (warp-cooperative).  Returns
 // true if a rotation was applied.
+// Pairs with a column whose squared norm is at most `floor` are left alone:
+// such a column changes no singular value by more than its norm.
 template <class T, bool G>
-__device__ bool rotate(T* wp, T* wq, T* vp, T* vq, T* np, T* nq, int64_t mm, int nn, T tol, int lane) {
+__device__ bool rotate(T* wp, T* wq, T* vp, T* vq, T* np, T* nq, int64_t mm, int nn, T tol, T floor, int lane) {
   const T al = ld<T, G>(np), be = ld<T, G>(nq);
-  if (!(al > T(0)) || !(be > T(0))) return false;
+  if (!(al > floor) || !(be > floor)) return false;
   T ga = 0;
   for (int64_t i = lane; i < mm; i += 32) ga = fma(ld<T, G>(wp + i), ld<T, G>(wq + i), ga);
   ga = wsum(ga);
@@ -147,7 +162,7 @@ __device__ bool rotate(T* wp, T* wq, T* vp, T* vq, T* np, T* nq, int64_t mm, int
 // [0, la), block B is [b, b+lb).
 template <class T>
 __device__ bool round_rotations(const Ctx& c, T* W, T* V, T* N, int b, int la, int lb, bool inner, int64_t mm, int nn,
-                                T tol) {
+                                T tol, T floor) {
   bool any = false;
   if (inner) {
     // pairs inside block A and inside block B: circle method over each block
@@ -161,7 +176,7 @@ __device__ bool round_rotations(const Ctx& c, T* W, T* V, T* N, int b, int la, i
         else { rr_pair(r, k - na, pb, p, q); base = b; if (p >= lb || q >= lb) continue; }
         p += base;
         q += base;
-        any |= rotate<T, false>(W + p * mm, W + q * mm, V + p * nn, V + q * nn, N + p, N + q, mm, nn, tol, c.lane);
+        any |= rotate<T, false>(W + p * mm, W + q * mm, V + p * nn, V + q * nn, N + p, N + q, mm, nn, tol, floor, c.lane);
       }
       __syncthreads();
     }
@@ -172,7 +187,7 @@ __device__ bool round_rotations(const Ctx& c, T* W, T* V, T* N, int b, int la, i
       const int j = (i + r) % b;
       if (i >= la || j >= lb) continue;
       const int p = i, q = b + j;
-      any |= rotate<T, false>(W + p * mm, W + q * mm, V + p * nn, V + q * nn, N + p, N + q, mm, nn, tol, c.lane);
+      any |= rotate<T, false>(W + p * mm, W + q * mm, V + p * nn, V + q * nn, N + p, N + q, mm, nn, tol, floor, c.lane);
     }
     __syncthreads();
   }
@@ -181,7 +196,7 @@ __device__ bool round_rotations(const Ctx& c, T* W, T* V, T* N, int b, int la, i
 
 template <class T>
 __device__ int block_jacobi(cg::cluster_group& cl, const Ctx& c, T* W, T* V, T* norms, int* flag, int64_t mm, int nn,
-                            T tol, int max_sweeps, T* smem, bool staged) {
+                            T tol, T rel_floor, int max_sweeps, T* smem, bool staged) {
   const int b = (nn + kBlocks - 1) / kBlocks;
   int sweeps = 0;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
@@ -194,6 +209,12 @@ __device__ int block_jacobi(cg::cluster_group& cl, const Ctx& c, T* W, T* V, T* 
     }
     if (c.rank == 0 && c.tid == 0) atomicExch(flag, 0);
     cl.sync();
+    // columns below rel_floor * (largest squared column norm) are numerically zero at this precision
+    T gmax = 0;
+    for (int j = c.lane; j < nn; j += 32) gmax = fmax(gmax, ldg(norms + j));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gmax = fmax(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
+    const T floor = rel_floor * gmax;
     for (int round = 0; round < kBlocks - 1; ++round) {
       int ba, bb;
       rr_pair(round, c.rank, kBlocks, ba, bb);
@@ -212,7 +233,7 @@ __device__ int block_jacobi(cg::cluster_group& cl, const Ctx& c, T* W, T* V, T* 
           if (c.lane == 0) sN[col] = g >= 0 ? ldg(norms + g) : T(0);
         }
         __syncthreads();
-        any = round_rotations<T>(c, sW, sV, sN, b, la, lb, round == 0, mm, nn, tol);
+        any = round_rotations<T>(c, sW, sV, sN, b, la, lb, round == 0, mm, nn, tol, floor);
         for (int col = c.warp; col < 2 * b; col += kWarps) {
           const int g = gcol(col);
           if (g < 0) continue;
@@ -235,7 +256,7 @@ __device__ int block_jacobi(cg::cluster_group& cl, const Ctx& c, T* W, T* V, T* 
               p += base;
               q += base;
               any |= rotate<T, true>(W + int64_t(p) * mm, W + int64_t(q) * mm, V + int64_t(p) * nn, V + int64_t(q) * nn,
-                                     norms + p, norms + q, mm, nn, tol, c.lane);
+                                     norms + p, norms + q, mm, nn, tol, floor, c.lane);
             }
             __syncthreads();
           }
@@ -246,7 +267,7 @@ __device__ int block_jacobi(cg::cluster_group& cl, const Ctx& c, T* W, T* V, T* 
             if (i >= la || j >= lb) continue;
             const int p = ca + i, q = cb + j;
             any |= rotate<T, true>(W + int64_t(p) * mm, W + int64_t(q) * mm, V + int64_t(p) * nn, V + int64_t(q) * nn,
-                                   norms + p, norms + q, mm, nn, tol, c.lane);
+                                   norms + p, norms + q, mm, nn, tol, floor, c.lane);
           }
           __syncthreads();
         }
@@ -397,7 +418,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
   }
   cl.sync();
   const float tol32 = 8.0f * sqrtf(float(mm)) * 6.0e-8f;
-  const int sw32 = nn > 1 ? block_jacobi<float>(cl, c, W32, V32, n32, flag, mm, nn, tol32, kMaxSweeps32,
+  const int sw32 = nn > 1 ? block_jacobi<float>(cl, c, W32, V32, n32, flag, mm, nn, tol32, kFloor32, kMaxSweeps32,
                                                 reinterpret_cast<float*>(smem_raw), staged32)
                           : 0;
   const long long t1 = clock64();
@@ -454,7 +475,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
 
   // ---- phase 3: FP64 block Jacobi polish
   const double tol64 = 1.0e-13;
-  const int sw64 = nn > 1 ? block_jacobi<double>(cl, c, W64, V, n64, flag, mm, nn, tol64, kMaxSweeps64,
+  const int sw64 = nn > 1 ? block_jacobi<double>(cl, c, W64, V, n64, flag, mm, nn, tol64, kFloor64, kMaxSweeps64,
                                                  reinterpret_cast<double*>(smem_raw), staged64)
                           : 0;
   const long long t3 = clock64();

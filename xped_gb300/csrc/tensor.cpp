@@ -134,6 +134,9 @@ struct GemmPlan {
   int n_tiles = 0, tile = 16;
   xgb_gemm_desc* d_descs = nullptr;
   GemmTile* d_tiles = nullptr;
+  int n_tc_tiles = 0;          // 128 x 128 tiles of the tensor-core form (built on first use)
+  GemmTile* d_tc_tiles = nullptr;
+  std::vector<xgb_gemm_desc> host_descs;
 };
 std::shared_ptr<PermPlan> upload_tables(const PermTables& t) {
   auto plan = std::make_shared<PermPlan>();
@@ -451,6 +454,9 @@ GemmTables build_gemm_tables(const TensorMeta& A, bool adj_a, const TensorMeta& 
   return gt;
 }
 
+// precision form of the block GEMMs issued by matmul (per host thread)
+thread_local int g_gemm_precision = XGB_PREC_FP64;
+
 Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
   // TensorBase::operator* (TensorBase.cpp:237-288), with AdjointOp operands
   // handled as transposed GEMM operands (no materialised transpose).
@@ -479,6 +485,7 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
         for (int64_t x = 0; x < tm; ++x) tiles.push_back({int32_t(g), int32_t(x), int32_t(y), plan->tile});
     }
     plan->n_tiles = int(tiles.size());
+    plan->host_descs = descs;
     plan->d_descs = dev_table(descs);
     plan->d_tiles = dev_table(tiles);
     for (const auto& d : descs) plan->flops += 2.0 * double(d.m) * double(d.n) * double(d.k);
@@ -487,10 +494,37 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
     g_gemm_plans[key] = plan;
   }
   Tensor out = empty_like_meta(plan->out);
+  if (g_gemm_precision == XGB_PREC_3XTF32) {
+    if (!plan->d_tc_tiles) {
+      const int tile = gemm_tc_tile();
+      std::vector<GemmTile> tiles;
+      for (size_t g = 0; g < plan->host_descs.size(); ++g) {
+        const auto& d = plan->host_descs[g];
+        const int64_t tm = (d.m + tile - 1) / tile, tn = (d.n + tile - 1) / tile;
+        for (int64_t y = 0; y < tn; ++y)
+          for (int64_t x = 0; x < tm; ++x) tiles.push_back({int32_t(g), int32_t(x), int32_t(y), tile});
+      }
+      std::lock_guard<std::mutex> lk(g_plan_mu);
+      if (!plan->d_tc_tiles) {
+        plan->n_tc_tiles = int(tiles.size());
+        plan->d_tc_tiles = dev_table(tiles);
+      }
+    }
+    prof_begin(K_GEMM_TC, stream());
+    launch_gemm_tc(plan->d_descs, plan->d_tc_tiles, plan->n_tc_tiles, a.data(), b.data(), out.data(), 1.0, 0.0, stream());
+    prof_end(K_GEMM_TC, stream(), plan->flops);
+    return out;
+  }
   prof_begin(K_GEMM, stream());
   launch_gemm_f64(plan->d_descs, plan->d_tiles, plan->n_tiles, plan->tile, a.data(), b.data(), out.data(), 1.0, 0.0, stream());
   prof_end(K_GEMM, stream(), plan->flops);
   return out;
+}
+
+int gemm_precision() { return g_gemm_precision; }
+void set_gemm_precision(int prec) {
+  if (prec != XGB_PREC_FP64 && prec != XGB_PREC_3XTF32) throw std::runtime_error("unsupported GEMM precision form");
+  g_gemm_precision = prec;
 }
 
 // ======================================================================= contract
@@ -992,7 +1026,9 @@ Tensor CTM::contract_corner(const char* corner) {
 }
 
 std::pair<Tensor, Tensor> CTM::decompose_dir(int d, const Tensor& t1, const Tensor& t2) {
-  // decompose (src/PEPS/PEPSContractions.cpp:16-43) with the configured SVD form
+  // decompose (src/PEPS/PEPSContractions.cpp:16-43) with the configured SVD form;
+  // the product, the SVD and the projectors are FP64 whatever the GEMM form
+  GemmPrecisionScope fp64(XGB_PREC_FP64);
   Tensor prod = matmul(t1, t2);
   const TensorMeta& m = *prod.meta;
   const size_t n = m.sectors.size();
@@ -1175,6 +1211,7 @@ std::tuple<Tensor, Tensor, Tensor> CTM::renormalize(char dir, const Tensor& P1, 
 }
 
 void CTM::move(char dir) {
+  GemmPrecisionScope prec(gemm_prec);
   auto [P1, P2] = get_projectors(dir);
   auto [a, b, c] = renormalize(dir, P1, P2);
   switch (dir) {

@@ -191,6 +191,10 @@ class CTM {
   Tensor& slot(int which);  // 0..3 = C1..C4, 4..7 = T1..T4, 8 = A, 9 = Adag
   int64_t chi = 0;
 
+  // block GEMMs of the corner contractions and the renormalisation:
+  // XGB_PREC_FP64 or XGB_PREC_3XTF32 (the projector SVD, the projector
+  // construction and the normalisation stay FP64)
+  int gemm_prec = XGB_PREC_FP64;
   // projector SVD form: 0 exact FP64 tSVD, 1 randomized with `policy` widths
   int svd_mode = 0;
   int power_iters = 3;
@@ -205,6 +209,16 @@ class CTM {
   std::pair<Tensor, Tensor> decompose_dir(int d, const Tensor& t1, const Tensor& t2);
   Tensor A, Ad;
   Tensor C1, C2, C3, C4, T1, T2, T3, T4;
+};
+
+// Precision form of the block GEMMs behind matmul / contract on this host
+// thread: XGB_PREC_FP64 (default) or XGB_PREC_3XTF32 (tensor cores).
+int gemm_precision();
+void set_gemm_precision(int prec);
+struct GemmPrecisionScope {
+  int saved;
+  explicit GemmPrecisionScope(int prec) : saved(gemm_precision()) { set_gemm_precision(prec); }
+  ~GemmPrecisionScope() { set_gemm_precision(saved); }
 };
 
 // avg of a two-site operator (src/PEPS/LinearAlgebra.cpp:58-64)

@@ -337,6 +337,20 @@ class CTM:
               "ctm_set_svd")
         return self
 
+    def set_gemm(self, precision: str = "fp64"):
+        """Block GEMMs of the corner contractions / renormalisation: "fp64" or
+        "3xtf32" (tensor cores)."""
+        check(lib().xgb_ctm_set_gemm_precision(self._h, {"fp64": 0, "3xtf32": 1}[precision]), "ctm_set_gemm")
+        return self
+
+    def set_rank_model(self, model, margin: float = 0.0, min_oversample: int = 2, power_iters: int = 3,
+                       seed: int = 1):
+        """Randomized projector SVD with widths predicted by a trained RankModel."""
+        self._model = model  # keep the model alive as long as the CTM uses it
+        check(lib().xgb_ctm_set_rank_model(self._h, model._h, float(margin), int(min_oversample), int(power_iters),
+                                           int(seed)), "ctm_set_rank_model")
+        return self
+
     def stats(self):
         out = (C.c_int64 * 5)()
         check(lib().xgb_ctm_stats(self._h, out), "ctm_stats")
@@ -380,6 +394,11 @@ class CTM:
 
 
 FEATURES = 8  # per-sector inputs of the rank predictor
+
+
+def set_gemm_precision(precision: str = "fp64"):
+    """Precision form of matmul / contract block GEMMs on this thread: "fp64" or "3xtf32"."""
+    check(lib().xgb_set_gemm_precision({"fp64": 0, "3xtf32": 1}[precision]), "set_gemm_precision")
 
 
 def bond_expectation(rho: Tensor, op: Tensor) -> float:
