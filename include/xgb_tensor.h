@@ -76,13 +76,16 @@ int xgb_tensor_tsvd(xgb_tensor t, int64_t max_keep, double eps_svd, int preserve
 /* Randomized blockwise tSVD with per-sector sketch widths (no counterpart in the
    reference; its results follow Tensor::tSVD's cutoff_matrices semantics).
    sketch[i] <= 0 or 2*sketch[i] >= min(rows, cols) decomposes sector i exactly;
-   power_iters subspace iterations; Gaussian test matrices from `seed`.  A sketched
-   sector that keeps all of its sketch is redone exactly (n_saturated counts them).
+   power_iters subspace iterations; Gaussian test matrices from `seed`; `warm` (may
+   be NULL): a V^dag of an earlier decomposition with the same column bases whose
+   rows of charge q replace the first Gaussian columns of sector q.  A sketched
+   sector that keeps all of its sketch is redone with twice the columns, exactly
+   after the third doubling (n_saturated counts the redos).
    keep[] and width[] (may be NULL) get, per input sector, the kept count and the
    sketch width used (min(rows, cols) for exact sectors). */
 int xgb_tensor_tsvd_randomized(xgb_tensor t, int64_t max_keep, double eps_svd, int n_sectors, const int64_t* sketch,
-                               int power_iters, uint64_t seed, xgb_tensor* U, xgb_tensor* S, xgb_tensor* Vdag,
-                               double* trunc_weight, double* entropy, int32_t* keep, int64_t* width,
+                               int power_iters, uint64_t seed, xgb_tensor warm, xgb_tensor* U, xgb_tensor* S,
+                               xgb_tensor* Vdag, double* trunc_weight, double* entropy, int32_t* keep, int64_t* width,
                                int32_t* n_saturated);
 int xgb_tensor_tqr(xgb_tensor t, xgb_tensor* Q, xgb_tensor* R);                    /* Tensor::tQR (Tensor.cpp:757-780) */
 /* decompose (src/PEPS/PEPSContractions.cpp:16-43) */
@@ -112,6 +115,10 @@ int xgb_set_gemm_precision(int precision);
    renormalisation of the moves (XGB_PREC_FP64 or XGB_PREC_3XTF32 from xgb.h);
    the projector SVD, the projector construction and the normalisation stay FP64. */
 int xgb_ctm_set_gemm_precision(xgb_ctm c, int precision);
+/* Warm start of the randomized projector SVD: the direction's previous V^dag seeds
+   the sketch and warm_iters subspace iterations are run instead of power_iters
+   (warm_iters < 0: off, the default). */
+int xgb_ctm_set_warm_start(xgb_ctm c, int warm_iters);
 /* out5: decompositions, sketched sectors, exact sectors, sketch redos, sketch columns */
 int xgb_ctm_stats(xgb_ctm c, int64_t* out5);
 /* Decomposition log for learning sketch widths (features of the rank predictor,

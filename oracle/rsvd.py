@@ -64,10 +64,15 @@ def _orth(Y):
     return u
 
 
-def sketch_svd(A, l, power_iters, seed, stream):
-    """Rank-l randomized SVD of one block (U m x l, s l, Vt l x n), sign-fixed."""
+def sketch_svd(A, l, power_iters, seed, stream, warm_rows=None):
+    """Rank-l randomized SVD of one block (U m x l, s l, Vt l x n), sign-fixed.
+    ``warm_rows`` (k x n, optional): its first min(k, l) rows replace the first
+    Gaussian columns of Omega."""
     m, n = A.shape
     Om = gaussian(seed, stream, n * l).reshape((n, l), order="F")
+    if warm_rows is not None and warm_rows.shape[1] == n:
+        kw = min(warm_rows.shape[0], l)
+        Om[:, :kw] = warm_rows[:kw, :].T
     Q = _orth(A @ Om)
     for _ in range(power_iters):
         Q = _orth(A @ _orth(A.T @ Q))
@@ -76,8 +81,10 @@ def sketch_svd(A, l, power_iters, seed, stream):
     return u, s, vt
 
 
-def tsvd_randomized(T: Tensor, max_keep, eps_svd, sketch, power_iters=1, seed=0):
-    """Returns (U, S, Vdag, truncWeight, entropy, keep, width, n_saturated)."""
+def tsvd_randomized(T: Tensor, max_keep, eps_svd, sketch, power_iters=1, seed=0, warm=None):
+    """Returns (U, S, Vdag, truncWeight, entropy, keep, width, n_saturated).
+    ``warm``: optional V^dag tensor of an earlier decomposition (same column
+    bases) seeding the sketches."""
     n = len(T.sectors)
     assert len(sketch) == n
     exact = [False] * n
@@ -105,7 +112,8 @@ def tsvd_randomized(T: Tensor, max_keep, eps_svd, sketch, power_iters=1, seed=0)
                 u, s, vt = sla.svd(b, full_matrices=False, lapack_driver="gesvd")
                 u, vt = fix_svd_signs(u, vt)
             else:
-                u, s, vt = sketch_svd(b, width[i], power_iters, seed, i)
+                wr = warm.block(q) if warm is not None and warm.has(q) else None
+                u, s, vt = sketch_svd(b, width[i], power_iters, seed, i, wr)
             allsv.extend((q, float(v)) for v in s)
             U.push_back(q, u)
             S.push_back(q, np.diag(s))

@@ -124,3 +124,29 @@ def test_rsvd_rank_deficient_blocks():
     assert np.allclose(rS.data(), eS.data(), rtol=1e-11, atol=0)
     assert np.allclose(rU.data(), eU.data(), rtol=0, atol=1e-9)
     assert np.allclose(rV.data(), eV.data(), rtol=0, atol=1e-9)
+
+
+def test_rsvd_warm_start_matches_oracle():
+    """Sketch seeded with the V^dag of a nearby matrix: device and oracle agree
+    element by element, and one subspace iteration resolves the truncation
+    of the perturbed matrix."""
+    from oracle.convert import tensor_from_native
+    secs = power_law_sectors(9, size=(24, 160), alphas=(2.0, 3.0))
+    ot, nt = _pair(secs)
+    rng = np.random.default_rng(10)
+    # perturbed copy (same structure)
+    pert = [(q, n, a, c, b + 1e-4 * rng.standard_normal(b.shape)) for q, n, a, c, b in secs]
+    ot2, nt2 = _pair(pert)
+    chi = 48
+    _U, _S, nV, *_ = nt.tSVD(chi, 1e-10)
+    s = oracle.make_symmetry("u1")
+    oV = tensor_from_native(s, nV)
+    _U2, eS, _V2, _tw, _e, keep_ex = nt2.tSVD(chi, 1e-10)
+    sketch = [k + 8 for k in keep_ex]
+    rU, rS, rV, rtw, _r, keep, width, nsat = nt2.tSVD_randomized(chi, 1e-10, sketch, 1, seed=4, warm=nV)
+    oU, oS, oVd, otw, _o, okeep, owidth, osat = oracle_rsvd(ot2, chi, 1e-10, sketch, 1, seed=4, warm=oV)
+    assert keep == okeep == keep_ex and nsat == osat == 0
+    assert_same(rS, oS, 1e-10, 1e-12)
+    assert_same(rU, oU, 1e-8, 1e-8)
+    assert_same(rV, oVd, 1e-8, 1e-8)
+    assert np.abs(rS.data() - eS.data()).max() <= 1e-8 * np.abs(eS.data()).max()

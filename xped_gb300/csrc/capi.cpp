@@ -203,15 +203,15 @@ int xgb_tensor_tsvd(xgb_tensor t, int64_t max_keep, double eps_svd, int preserve
 }
 
 int xgb_tensor_tsvd_randomized(xgb_tensor t, int64_t max_keep, double eps_svd, int n_sectors, const int64_t* sketch,
-                               int power_iters, uint64_t seed, xgb_tensor* U, xgb_tensor* S, xgb_tensor* Vdag,
-                               double* trunc_weight, double* entropy, int32_t* keep, int64_t* width,
+                               int power_iters, uint64_t seed, xgb_tensor warm, xgb_tensor* U, xgb_tensor* S,
+                               xgb_tensor* Vdag, double* trunc_weight, double* entropy, int32_t* keep, int64_t* width,
                                int32_t* n_saturated) {
   GUARD(XGB_E_BADPLAN, {
     if (n_sectors != int(t->t.meta->sectors.size()) || (n_sectors > 0 && !sketch))
       return set_error(XGB_E_BADPLAN, "randomized tSVD: one sketch width per sector required");
     RsvdInfo info;
     SVDResult r = tsvd_randomized(t->t, max_keep, eps_svd, std::vector<int64_t>(sketch, sketch + n_sectors),
-                                  power_iters, seed, &info);
+                                  power_iters, seed, &info, warm ? &warm->t : nullptr);
     if (U) *U = wrap(r.U);
     if (S) *S = wrap(r.S);
     if (Vdag) *Vdag = wrap(r.Vdag);
@@ -297,6 +297,15 @@ int xgb_ctm_set_gemm_precision(xgb_ctm c, int precision) {
     if (precision != XGB_PREC_FP64 && precision != XGB_PREC_3XTF32)
       return set_error(XGB_E_UNSUPPORTED, "GEMM precision form not available");
     c->c->gemm_prec = precision;
+    return XGB_OK;
+  })
+}
+
+int xgb_ctm_set_warm_start(xgb_ctm c, int warm_iters) {
+  GUARD(XGB_E_BADPLAN, {
+    c->c->warm_iters = warm_iters < 0 ? -1 : warm_iters;
+    if (warm_iters < 0)
+      for (auto& w : c->c->warm_v) w = Tensor();
     return XGB_OK;
   })
 }

@@ -58,6 +58,9 @@ struct SignFixDesc { int64_t m, n, k, u_off, v_off; };      // U m x k (ld m), V
 void launch_gauss_fill(const GaussBlock* d_blocks, int n_blocks, int64_t max_count, uint64_t seed, double* out,
                        cudaStream_t s);
 void launch_sign_fix(const SignFixDesc* d_descs, int n, int64_t max_k, double* U, double* Vt, cudaStream_t s);
+// transposed block copies: src block rows x cols (ld src_ld) -> dst cols x rows (ld dst_ld)
+void launch_transpose_copy(const xgb_copy2d_desc* d_descs, int n, int64_t max_elems, const double* src, double* dst,
+                           cudaStream_t s);
 // Q columns j with S[v_off + j] <= rel * S[v_off] set to zero (descs: m, k, u_off of Q, v_off into S)
 void launch_zero_noise_columns(const SignFixDesc* d_descs, int n, int64_t max_k, const double* S, double rel, double* Q,
                                cudaStream_t s);

@@ -127,7 +127,7 @@ constexpr int kMaxRetries = 3;
 }  // namespace
 
 SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, const std::vector<int64_t>& sketch,
-                          int power_iters, uint64_t seed, RsvdInfo* info) {
+                          int power_iters, uint64_t seed, RsvdInfo* info, const Tensor* warm) {
   Tensor t = materialize(t0);
   const TensorMeta& m = *t.meta;
   const int n = int(m.sectors.size());
@@ -207,6 +207,29 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
         prof_begin(K_SKETCH, st);
         launch_gauss_fill(sg.at<GaussBlock>(o), nr, mx, seed, Om, st);
         prof_end(K_SKETCH, st, 8.0 * double(omt));
+      }
+      // ---- warm start: the first columns of Omega_i are the rows of the
+      // previous V^dag block of the same charge (its right singular vectors)
+      if (warm && warm->valid()) {
+        const TensorMeta& wm = *warm->meta;
+        std::vector<xgb_copy2d_desc> td;  // src k x n (ld k) -> dst n x k (ld n), transposed
+        int64_t mx = 0;
+        for (int a = 0; a < nr; ++a) {
+          const int wi = wm.index(m.sectors[R[a]]);
+          if (wi < 0 || wm.cols[wi] != rc[a]) continue;
+          const int64_t kw = std::min<int64_t>(wm.rows[wi], rl[a]);
+          if (kw <= 0) continue;
+          td.push_back({wm.offset[wi], wm.rows[wi], om[a], rc[a], kw, rc[a]});
+          mx = std::max(mx, kw * rc[a]);
+        }
+        if (!td.empty()) {
+          Staging sw;
+          const size_t o = sw.add(td);
+          sw.upload(st);
+          prof_begin(K_SKETCH, st);
+          launch_transpose_copy(sw.at<xgb_copy2d_desc>(o), int(td.size()), mx, materialize(*warm).data(), Om, st);
+          prof_end(K_SKETCH, st, 16.0 * double(mx) * double(td.size()));
+        }
       }
       // ---- Y = A Omega, Q = orth(Y)
       std::vector<xgb_gemm_desc> g;

@@ -88,7 +88,28 @@ __global__ void zero_noise_columns_kernel(const SignFixDesc* __restrict__ descs,
   }
 }
 
+// dst[d.dst_off + c + j * d.dst_ld] = src[d.src_off + j + c * d.src_ld] for j < rows, c < cols
+// (descriptor: rows = k rows of the source block, cols = n its columns)
+__global__ void transpose_copy_kernel(const xgb_copy2d_desc* __restrict__ descs, const double* __restrict__ src,
+                                      double* __restrict__ dst) {
+  const xgb_copy2d_desc d = descs[blockIdx.y];
+  const int64_t ne = d.rows * d.cols;
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < ne; e += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t c = e % d.cols, j = e / d.cols;  // consecutive threads write consecutive dst rows
+    dst[d.dst_off + c + j * d.dst_ld] = src[d.src_off + j + c * d.src_ld];
+  }
+}
+
 }  // namespace
+
+void launch_transpose_copy(const xgb_copy2d_desc* d_descs, int n, int64_t max_elems, const double* src, double* dst,
+                           cudaStream_t s) {
+  if (n <= 0 || max_elems <= 0) return;
+  const int64_t want = (max_elems + 255) / 256;
+  dim3 grid(unsigned(want < 1024 ? want : 1024), unsigned(n));
+  transpose_copy_kernel<<<grid, 256, 0, s>>>(d_descs, src, dst);
+  count_launch();
+}
 
 void launch_zero_noise_columns(const SignFixDesc* d_descs, int n, int64_t max_k, const double* S, double rel, double* Q,
                                cudaStream_t s) {

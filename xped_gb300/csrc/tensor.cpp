@@ -1048,7 +1048,9 @@ std::pair<Tensor, Tensor> CTM::decompose_dir(int d, const Tensor& t1, const Tens
     if (!policy) throw std::runtime_error("CTM: randomized projector SVD without a width policy");
     std::vector<int64_t> want = policy->widths(m, hist[d], chi);
     RsvdInfo info;
-    r = tsvd_randomized(prod, chi, 1.0e-10, want, power_iters, seed + uint64_t(stats.decompositions), &info);
+    const bool warm = warm_iters >= 0 && warm_v[d].valid() && warm_v[d].meta->cod == m.cod;
+    r = tsvd_randomized(prod, chi, 1.0e-10, want, warm ? warm_iters : power_iters,
+                        seed + uint64_t(stats.decompositions), &info, warm ? &warm_v[d] : nullptr);
     width = info.width;
     stats.exact_sectors += info.exact_sectors;
     stats.sketched_sectors += int64_t(n) - info.exact_sectors;
@@ -1074,6 +1076,7 @@ std::pair<Tensor, Tensor> CTM::decompose_dir(int d, const Tensor& t1, const Tens
     h[m.sectors[i]] = e;
   }
   hist[d] = std::move(h);
+  if (warm_iters >= 0) warm_v[d] = r.Vdag;
   if (record) {
     rec.keep.assign(r.keep.begin(), r.keep.end());
     rec.width = width;

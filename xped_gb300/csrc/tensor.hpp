@@ -119,8 +119,11 @@ struct RsvdInfo {
   int64_t sketch_cols = 0;     // sum of widths over sketched sectors
   int exact_sectors = 0;
 };
+// `warm` (optional): a V^dag from an earlier decomposition of a matrix with the
+// same column bases; its rows of charge q become the first sketch columns of
+// sector q (the remaining columns stay Gaussian).
 SVDResult tsvd_randomized(const Tensor& t, int64_t max_keep, double eps_svd, const std::vector<int64_t>& sketch,
-                          int power_iters, uint64_t seed, RsvdInfo* info = nullptr);
+                          int power_iters, uint64_t seed, RsvdInfo* info = nullptr, const Tensor* warm = nullptr);
 std::pair<Tensor, Tensor> tqr(const Tensor& t);
 std::pair<Tensor, Tensor> decompose(const Tensor& t1, const Tensor& t2, int64_t max_nsv);
 
@@ -198,12 +201,16 @@ class CTM {
   // projector SVD form: 0 exact FP64 tSVD, 1 randomized with `policy` widths
   int svd_mode = 0;
   int power_iters = 3;
+  // subspace iterations when the direction's previous V^dag (same matrix
+  // structure) seeds the sketch; < 0 disables the warm start
+  int warm_iters = -1;
   uint64_t seed = 1;
   std::shared_ptr<WidthPolicy> policy;
   bool record = false;
   std::vector<DecompRecord> records;
   CTMStats stats;
   History hist[4];
+  Tensor warm_v[4];  // last V^dag per direction (warm start of the randomized SVD)
 
  private:
   std::pair<Tensor, Tensor> decompose_dir(int d, const Tensor& t1, const Tensor& t2);

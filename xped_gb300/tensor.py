@@ -223,7 +223,7 @@ class Tensor:
         return Tensor(U.value), Tensor(S.value), Tensor(V.value), tw.value, ent.value, list(keep[:n])
 
     def tSVD_randomized(self, max_keep: int, eps_svd: float, sketch: Sequence[int], power_iters: int = 1,
-                        seed: int = 0):
+                        seed: int = 0, warm: "Tensor" = None):
         """Randomized blockwise tSVD: ``sketch[i]`` Gaussian columns for sector i
         (<= 0: exact).  Returns (U, S, V, truncWeight, entropy, keep, width,
         n_saturated)."""
@@ -237,7 +237,8 @@ class Tensor:
         nsat = C.c_int32()
         sk = (C.c_int64 * max(n, 1))(*[int(x) for x in sketch])
         check(lib().xgb_tensor_tsvd_randomized(self._h, int(max_keep), float(eps_svd), n, sk, int(power_iters),
-                                               int(seed), C.byref(U), C.byref(S), C.byref(V), C.byref(tw),
+                                               int(seed), warm._h if warm is not None else None, C.byref(U),
+                                               C.byref(S), C.byref(V), C.byref(tw),
                                                C.byref(ent), keep, width, C.byref(nsat)), "tSVD_randomized")
         return (Tensor(U.value), Tensor(S.value), Tensor(V.value), tw.value, ent.value, list(keep[:n]),
                 list(width[:n]), nsat.value)
@@ -335,6 +336,12 @@ class CTM:
         m = {"exact": 0, "randomized": 1}[mode]
         check(lib().xgb_ctm_set_svd(self._h, m, int(power_iters), int(seed), int(oversample), float(growth)),
               "ctm_set_svd")
+        return self
+
+    def set_warm_start(self, warm_iters: int = 2):
+        """Seed each randomized projector SVD with the direction's previous V^dag and
+        run warm_iters subspace iterations (negative: off)."""
+        check(lib().xgb_ctm_set_warm_start(self._h, int(warm_iters)), "ctm_set_warm_start")
         return self
 
     def set_gemm(self, precision: str = "fp64"):
