@@ -484,6 +484,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-width run")
+    ap.add_argument("--gemm-sweep-only", action="store_true",
+                    help="run only the block-GEMM sweep and print it (for kernel profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
@@ -510,6 +512,12 @@ def main():
                                            "warm-up steps; step time counted as four moves"},
                 "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
+        return
+
+    if args.gemm_sweep_only:
+        from xped_gb300 import ensure_device
+        ensure_device(local)
+        print(json.dumps({"block_gemm_sweep": gemm_sweep()}))
         return
 
     if world > 1:

@@ -1,19 +1,25 @@
 // Split-precision grouped GEMM on the 5th-generation tensor cores.
 //
 // C_g = alpha op(A_g) op(B_g) + beta C_g for FP64 column-major blocks, with
-// the products taken as three TF32 tensor-core products per K slice
-// (3xTF32): every FP64 operand x is split in the kernel into
-// hi = tf32(x) and lo = tf32(x - hi), and C ~ Ahi Bhi + Ahi Blo + Alo Bhi
-// is accumulated in FP32 in tensor memory (TMEM).  The dropped Alo Blo term
-// and the TF32 rounding of lo bound the product error near 2^-21 of |A||B|.
+// the products taken as three TF32 tensor-core products (3xTF32): every FP64
+// operand x is split into hi = tf32(x) and lo = tf32(x - hi), and
+// C ~ Ahi Bhi + Ahi Blo + Alo Bhi is accumulated in FP32 in tensor memory
+// (TMEM).  The dropped Alo Blo term and the TF32 rounding of lo bound the
+// product error near 2^-21 of |A||B|.
 //
-// One CTA computes one 128 x 128 output tile: threads load FP64 K slices of
-// 32, split them and store the four operand tiles (Ahi, Alo, Bhi, Blo) into
-// shared memory in the K-major, unswizzled canonical layout (8-row x 16-byte
-// core matrices); thread 0 issues the tcgen05.mma instructions and commits
-// them to an mbarrier; two slice buffers alternate so that loading the next
-// slice overlaps the tensor cores working on the current one.  The
-// epilogue reads the accumulator with tcgen05.ld and writes FP64.
+// Two kernels:
+//  * pack: every operand is split once into 16 KB chunks - one 128-row x
+//    32-K slice, hi or lo - already in the K-major, unswizzled canonical
+//    layout the MMA reads (8-row x 16-byte core matrices), zero padded past
+//    the block edges.  A chunk is read through shared memory so that the
+//    FP64 loads are coalesced whatever the operand's transpose.
+//  * gemm: one CTA per 128 x 128 output tile.  Thread 0 streams the chunks
+//    of the tile's A rows and B columns into a 3-stage shared-memory ring
+//    with bulk asynchronous copies (cp.async.bulk, completion counted in
+//    bytes on an mbarrier); thread 32 issues the tcgen05.mma instructions of
+//    each slice and commits them to the slice's "empty" mbarrier, which
+//    frees the stage for the next copy; the four warps then read the
+//    accumulator with tcgen05.ld and write FP64.
 //
 // Every mbarrier wait is bounded; on timeout the CTA records an error flag,
 // skips the epilogue and still frees its TMEM.
@@ -27,17 +33,18 @@ namespace xgb {
 namespace {
 
 constexpr int BM = 128, BN = 128, BK = 32;
-constexpr int kThreads = 256;
-constexpr int kTileBytes = BM * BK * 4;                 // one operand tile (A or B, hi or lo): 16 KB
-constexpr int kStageBytes = 4 * kTileBytes;             // Ahi, Alo, Bhi, Blo
-constexpr int kStages = 2;
+constexpr int kChunkFloats = BM * BK;               // 4096 floats = 16 KB
+constexpr int kChunkBytes = kChunkFloats * 4;
+constexpr int kStageBytes = 4 * kChunkBytes;        // Ahi, Alo, Bhi, Blo
+constexpr int kStages = 3;
 constexpr int kSmemBytes = kStages * kStageBytes + 1024;  // + alignment slack
-constexpr uint32_t kTmemCols = 128;                     // FP32 accumulator, N = 128 columns
+constexpr int kThreads = 128;
+constexpr uint32_t kTmemCols = 128;                 // FP32 accumulator, N = 128 columns
 constexpr long long kSpinLimit = 1ll << 26;
 
-// K-major canonical layout, no swizzle: element (r, k) of a 128-row tile at
+// K-major canonical layout, no swizzle: element (r, k) of a 128-row chunk at
 // byte (k / 4) * LBO + (r / 8) * SBO + (r % 8) * 16 + (k % 4) * 4
-constexpr uint32_t SBO = 128;           // next 8-row group
+constexpr uint32_t SBO = 128;             // next 8-row group
 constexpr uint32_t LBO = (BM / 8) * 128;  // next 4-column (16-byte) K group: 2048 bytes
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -88,6 +95,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy(void* dst_smem, const void* src_gmem, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst_smem)),
+      "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
 __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -100,38 +119,71 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                : "memory");
 }
 
-// op(X)[r][k] of a 128 x 32 slice into hi / lo tiles (rows >= rows_valid or k >= k_valid are zero)
-__device__ __forceinline__ void load_split(const double* __restrict__ X, int64_t off, int64_t ld, int trans,
-                                           int64_t r0, int64_t rows_valid, int64_t k0, int64_t k_valid,
-                                           unsigned char* hi, unsigned char* lo) {
-  for (int e = threadIdx.x; e < BM * BK; e += kThreads) {
-    // consecutive threads walk the contiguous direction of the stored block
+// ----------------------------------------------------------------------------- pack
+// One CTA per chunk pair (hi and lo of one 128-row x 32-K slice of op(A) or op(B)^T).
+__global__ void __launch_bounds__(256) tc_pack_kernel(const xgb_gemm_desc* __restrict__ descs,
+                                                       const TcGroup* __restrict__ groups,
+                                                       const TcPackTask* __restrict__ tasks,
+                                                       const double* __restrict__ A, const double* __restrict__ B,
+                                                       float* __restrict__ apack, float* __restrict__ bpack) {
+  __shared__ double X[BM][BK + 1];
+  const TcPackTask t = tasks[blockIdx.x];
+  const xgb_gemm_desc d = descs[t.g];
+  const TcGroup gr = groups[t.g];
+  const bool isB = t.which != 0;
+  const double* src = isB ? B : A;
+  const int64_t off = isB ? d.b_off : d.a_off, ld = isB ? d.ldb : d.lda;
+  const int64_t rows = isB ? d.n : d.m;
+  // element (r, k) of the chunk is op(X)[r0 + r][k0 + k]; "rowfast" when r is the contiguous direction
+  const bool rowfast = isB ? d.trans_b != 0 : d.trans_a == 0;
+  const int64_t r0 = int64_t(t.tile) * BM, k0 = int64_t(t.slice) * BK;
+  for (int e = threadIdx.x; e < BM * BK; e += 256) {
     int r, k;
-    if (!trans) { r = e % BM; k = e / BM; } else { k = e % BK; r = e / BK; }
-    const int64_t gr = r0 + r, gk = k0 + k;
+    if (rowfast) { r = e % BM; k = e / BM; } else { k = e % BK; r = e / BK; }
+    const int64_t gr_ = r0 + r, gk = k0 + k;
     double x = 0.0;
-    if (gr < rows_valid && gk < k_valid) x = trans ? X[off + gk + gr * ld] : X[off + gr + gk * ld];
-    const float h = to_tf32(float(x));
-    const float l = to_tf32(float(x - double(h)));
-    const uint32_t b = uint32_t(k >> 2) * LBO + uint32_t(r >> 3) * SBO + uint32_t(r & 7) * 16 + uint32_t(k & 3) * 4;
-    *reinterpret_cast<float*>(hi + b) = h;
-    *reinterpret_cast<float*>(lo + b) = l;
+    if (gr_ < rows && gk < d.k) x = rowfast ? src[off + gr_ + gk * ld] : src[off + gk + gr_ * ld];
+    X[r][k] = x;
+  }
+  __syncthreads();
+  const int64_t chunk = (int64_t(t.tile) * gr.slices + t.slice) * 2;
+  float* hi = (isB ? bpack + gr.b_pack : apack + gr.a_pack) + chunk * kChunkFloats;
+  float* lo = hi + kChunkFloats;
+  for (int e = threadIdx.x; e < BM * (BK / 4); e += 256) {
+    const int r = e % BM, kq = e / BM;  // one 16-byte core-matrix row: 4 consecutive K of row r
+    float4 h, l;
+    float* hp = &h.x;
+    float* lp = &l.x;
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      const double x = X[r][kq * 4 + kk];
+      hp[kk] = to_tf32(float(x));
+      lp[kk] = to_tf32(float(x - double(hp[kk])));
+    }
+    const uint32_t fo = (uint32_t(kq) * LBO + uint32_t(r >> 3) * SBO + uint32_t(r & 7) * 16) / 4;
+    *reinterpret_cast<float4*>(hi + fo) = h;
+    *reinterpret_cast<float4*>(lo + fo) = l;
   }
 }
 
+// ----------------------------------------------------------------------------- gemm
 __global__ void __launch_bounds__(kThreads, 1)
-    gemm_tc_kernel(const xgb_gemm_desc* __restrict__ descs, const GemmTile* __restrict__ tiles,
-                   const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C, double alpha,
-                   double beta, int* __restrict__ err) {
+    gemm_tc_kernel(const xgb_gemm_desc* __restrict__ descs, const TcGroup* __restrict__ groups,
+                   const GemmTile* __restrict__ tiles, const float* __restrict__ apack,
+                   const float* __restrict__ bpack, double* __restrict__ C, double alpha, double beta,
+                   int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
-  __shared__ uint64_t bars[kStages];
+  __shared__ uint64_t full[kStages], empty[kStages], done;
   __shared__ uint32_t tmem_slot;
+  __shared__ int fail, issued, consumed;
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
 
   const GemmTile t = tiles[blockIdx.x];
   const xgb_gemm_desc d = descs[t.g];
+  const TcGroup gr = groups[t.g];
   const int64_t m0 = int64_t(t.tm) * BM, n0 = int64_t(t.tn) * BN;
   const int warp = threadIdx.x >> 5;
+  const int nk = gr.slices;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -139,7 +191,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
+    fail = 0;
+    issued = 0;
+    consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -147,29 +206,34 @@ __global__ void __launch_bounds__(kThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
 
-  const int64_t K = d.k;
-  const int nk = int((K + BK - 1) / BK);
-  uint32_t parity[kStages] = {0, 0};
-  bool ok = true;
-  const uint32_t idesc = make_idesc();
-
-  for (int kc = 0; kc < nk && ok; ++kc) {
-    const int s = kc % kStages;
-    unsigned char* st = smem + s * kStageBytes;
-    if (kc >= kStages) {  // the MMAs of slice kc - 2 read this buffer
-      if (!mbar_wait(&bars[s], parity[s])) ok = false;
-      parity[s] ^= 1u;
+  if (nk > 0 && threadIdx.x == 0) {
+    // producer: bulk copies of the four chunks of every slice into the stage ring
+    const float* a_base = apack + gr.a_pack + int64_t(t.tm) * gr.slices * 2 * kChunkFloats;
+    const float* b_base = bpack + gr.b_pack + int64_t(t.tn) * gr.slices * 2 * kChunkFloats;
+    uint32_t ph[kStages] = {0, 0, 0};
+    for (int kc = 0; kc < nk; ++kc) {
+      const int s = kc % kStages;
+      if (kc >= kStages) {
+        if (!mbar_wait(&empty[s], ph[s])) { atomicExch(&fail, 1); break; }
+        ph[s] ^= 1u;
+      }
+      unsigned char* st = smem + s * kStageBytes;
+      mbar_expect_tx(&full[s], kStageBytes);
+      bulk_copy(st, a_base + int64_t(kc) * 2 * kChunkFloats, 2 * kChunkBytes, &full[s]);
+      bulk_copy(st + 2 * kChunkBytes, b_base + int64_t(kc) * 2 * kChunkFloats, 2 * kChunkBytes, &full[s]);
+      issued = kc + 1;
     }
-    if (!__syncthreads_and(ok)) { ok = false; break; }
-    const int64_t k0 = int64_t(kc) * BK;
-    load_split(A, d.a_off, d.lda, d.trans_a, m0, d.m, k0, K, st, st + kTileBytes);
-    load_split(B, d.b_off, d.ldb, !d.trans_b, n0, d.n, k0, K, st + 2 * kTileBytes, st + 3 * kTileBytes);
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (threadIdx.x == 0) {
+  } else if (nk > 0 && threadIdx.x == 32) {
+    // MMA issuer: three TF32 products per K step of 8, accumulated in TMEM
+    const uint32_t idesc = make_idesc();
+    uint32_t ph[kStages] = {0, 0, 0};
+    for (int kc = 0; kc < nk; ++kc) {
+      const int s = kc % kStages;
+      if (!mbar_wait(&full[s], ph[s])) { atomicExch(&fail, 1); break; }
+      ph[s] ^= 1u;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t base = smem_u32(st);
-      const uint32_t ahi = base, alo = base + kTileBytes, bhi = base + 2 * kTileBytes, blo = base + 3 * kTileBytes;
+      const uint32_t base = smem_u32(smem + s * kStageBytes);
+      const uint32_t ahi = base, alo = base + kChunkBytes, bhi = base + 2 * kChunkBytes, blo = base + 3 * kChunkBytes;
 #pragma unroll
       for (int kk = 0; kk < BK / 8; ++kk) {
         const uint32_t ko = uint32_t(kk) * 2 * LBO;  // 8 TF32 = two 16-byte K groups
@@ -178,34 +242,35 @@ __global__ void __launch_bounds__(kThreads, 1)
         mma_tf32(tmem, make_desc(ahi + ko), make_desc(blo + ko), idesc, 1u);
         mma_tf32(tmem, make_desc(alo + ko), make_desc(bhi + ko), idesc, 1u);
       }
-      mma_commit(&bars[s]);
+      mma_commit(&empty[s]);
+      consumed = kc + 1;
     }
+    mma_commit(&done);  // arrives when every MMA issued above has completed
   }
-  // drain: wait for every outstanding commit
-  for (int kc = (nk > kStages ? nk - kStages : 0); kc < nk; ++kc) {
-    const int s = kc % kStages;
-    if (ok && !mbar_wait(&bars[s], parity[s])) ok = false;
-    parity[s] ^= 1u;
-  }
+  // everyone waits for the accumulator
+  bool ok = true;
+  if (nk > 0) ok = mbar_wait(&done, 0);
+  __syncthreads();
+  ok = ok && (fail == 0);
   ok = __syncthreads_and(ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
   if (ok && nk > 0) {
-    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, columns (w / 4) * 64 .. +63
-    const int lane_grp = warp & 3, half = warp >> 2;
-    const int64_t row = m0 + lane_grp * 32 + (threadIdx.x & 31);
-    for (int c = 0; c < BN / 2; c += 8) {
-      const int col0 = half * (BN / 2) + c;
-      uint32_t v[8];
-      const uint32_t taddr = tmem + (uint32_t(lane_grp * 32) << 16) + uint32_t(col0);
-      asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                   : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
-                   : "r"(taddr));
+    // epilogue: warp w reads TMEM lanes 32 w .. 32 w + 31 (rows), all 128 columns
+    const int64_t row = m0 + warp * 32 + (threadIdx.x & 31);
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      uint32_t v[16];
+      const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       if (row < d.m) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int64_t col = n0 + col0 + j;
+        for (int j = 0; j < 16; ++j) {
+          const int64_t col = n0 + c0 + j;
           if (col < d.n) {
             double* cp = C + d.c_off + row + col * d.ldc;
             const double acc = double(__uint_as_float(v[j]));
@@ -223,7 +288,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   }
-  if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+  if (!ok && threadIdx.x == 0) {
+    atomicExch(err, 1);
+    // copies still in flight must land before the CTA leaves: wait (bounded) for
+    // every slice that was issued but not consumed
+    for (int kc = consumed; kc < issued; ++kc) mbar_wait(&full[kc % kStages], uint32_t((kc / kStages) & 1));
+  }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
@@ -236,8 +306,32 @@ int* g_tc_err = nullptr;
 
 int gemm_tc_tile() { return BM; }
 
-void launch_gemm_tc(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, const double* A,
-                    const double* B, double* C, double alpha, double beta, cudaStream_t s) {
+TcPlanHost build_tc_plan(const xgb_gemm_desc* descs, int n) {
+  TcPlanHost p;
+  for (int g = 0; g < n; ++g) {
+    const xgb_gemm_desc& d = descs[g];
+    TcGroup gr{};
+    gr.a_tiles = int32_t((d.m + BM - 1) / BM);
+    gr.b_tiles = int32_t((d.n + BN - 1) / BN);
+    gr.slices = int32_t((d.k + BK - 1) / BK);
+    gr.a_pack = p.a_floats;
+    gr.b_pack = p.b_floats;
+    p.a_floats += int64_t(gr.a_tiles) * gr.slices * 2 * kChunkFloats;
+    p.b_floats += int64_t(gr.b_tiles) * gr.slices * 2 * kChunkFloats;
+    for (int32_t s = 0; s < gr.slices; ++s) {
+      for (int32_t t = 0; t < gr.a_tiles; ++t) p.tasks.push_back({g, t, s, 0});
+      for (int32_t t = 0; t < gr.b_tiles; ++t) p.tasks.push_back({g, t, s, 1});
+    }
+    for (int32_t y = 0; y < gr.b_tiles; ++y)
+      for (int32_t x = 0; x < gr.a_tiles; ++x) p.tiles.push_back({g, x, y, BM});
+    p.groups.push_back(gr);
+  }
+  return p;
+}
+
+void launch_gemm_tc(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
+                    const GemmTile* d_tiles, int n_tiles, const double* A, const double* B, float* apack,
+                    float* bpack, double* C, double alpha, double beta, cudaStream_t s) {
   if (n_tiles <= 0) return;
   if (!g_tc_attr) {
     cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
@@ -245,7 +339,12 @@ void launch_gemm_tc(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n
     cudaMemset(g_tc_err, 0, sizeof(int));
     g_tc_attr = true;
   }
-  gemm_tc_kernel<<<n_tiles, kThreads, kSmemBytes, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, g_tc_err);
+  if (n_tasks > 0) {
+    tc_pack_kernel<<<n_tasks, 256, 0, s>>>(d_descs, d_groups, d_tasks, A, B, apack, bpack);
+    count_launch();
+  }
+  gemm_tc_kernel<<<n_tiles, kThreads, kSmemBytes, s>>>(d_descs, d_groups, d_tiles, apack, bpack, C, alpha, beta,
+                                                       g_tc_err);
   count_launch();
 }
 

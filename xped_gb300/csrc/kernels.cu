@@ -734,23 +734,22 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
   for (int g = 0; g < n_groups; ++g)
     if (descs[g].m < 0 || descs[g].n < 0 || descs[g].k < 0) return set_error(XGB_E_BADPLAN, "negative GEMM extent");
   if (precision == XGB_PREC_3XTF32) {
-    const int tile = gemm_tc_tile();
-    std::vector<GemmTile> tiles;
+    TcPlanHost tp = build_tc_plan(descs, n_groups);
+    if (tp.tiles.empty()) return XGB_OK;
     double flops = 0;
-    for (int g = 0; g < n_groups; ++g) {
-      int64_t tm = (descs[g].m + tile - 1) / tile, tn = (descs[g].n + tile - 1) / tile;
-      for (int64_t j = 0; j < tn; ++j)
-        for (int64_t i = 0; i < tm; ++i) tiles.push_back({g, int32_t(i), int32_t(j), tile});
-      flops += 2.0 * double(descs[g].m) * double(descs[g].n) * double(descs[g].k);
-    }
-    if (tiles.empty()) return XGB_OK;
+    for (int g = 0; g < n_groups; ++g) flops += 2.0 * double(descs[g].m) * double(descs[g].n) * double(descs[g].k);
     auto* dd = upload(descs, size_t(n_groups), s);
-    auto* dt = upload(tiles.data(), tiles.size(), s);
+    auto* dg = upload(tp.groups.data(), tp.groups.size(), s);
+    auto* dk = upload(tp.tasks.data(), std::max<size_t>(tp.tasks.size(), 1), s);
+    auto* dt = upload(tp.tiles.data(), tp.tiles.size(), s);
+    auto* ap = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.a_floats, 4))));
+    auto* bp = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.b_floats, 4))));
     prof_begin(K_GEMM_TC, s);
-    launch_gemm_tc(dd, dt, int(tiles.size()), A, B, C, alpha, beta, s);
+    launch_gemm_tc(dd, dg, dk, int(tp.tasks.size()), dt, int(tp.tiles.size()), A, B, ap, bp, C, alpha, beta, s);
     prof_end(K_GEMM_TC, s, flops);
-    dev_free(dd);
-    dev_free(dt);
+    for (void* p : {static_cast<void*>(dd), static_cast<void*>(dg), static_cast<void*>(dk), static_cast<void*>(dt),
+                    static_cast<void*>(ap), static_cast<void*>(bp)})
+      dev_free(p);
     return check_cuda(cudaGetLastError(), "tensor-core gemm launch");
   }
   const int tile = choose_gemm_tile(descs, n_groups);

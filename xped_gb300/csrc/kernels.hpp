@@ -8,6 +8,7 @@
 
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "../../include/xgb.h"
 
@@ -46,10 +47,24 @@ void launch_diag_from_vec(const xgb_copy2d_desc* d_descs, int n, int64_t max_k, 
                           cudaStream_t s);
 void launch_diag_apply(const xgb_copy2d_desc* d_descs, int n, int64_t max_k, int fn, double* x, cudaStream_t s);
 
-// split-precision (3xTF32) tensor-core grouped GEMM (gemm_tc.cu): 128 x 128 tiles
+// split-precision (3xTF32) tensor-core grouped GEMM (gemm_tc.cu): operands packed into
+// 16 KB hi/lo chunks (128 rows x 32 K, canonical MMA layout), 128 x 128 output tiles
+struct TcGroup {
+  int64_t a_pack, b_pack;           // float offsets of the group's packed op(A) / op(B)^T chunks
+  int32_t a_tiles, b_tiles, slices, pad;
+};
+struct TcPackTask { int32_t g, tile, slice, which; };  // which: 0 = A, 1 = B
+struct TcPlanHost {
+  std::vector<TcGroup> groups;
+  std::vector<TcPackTask> tasks;
+  std::vector<GemmTile> tiles;
+  int64_t a_floats = 0, b_floats = 0;
+};
+TcPlanHost build_tc_plan(const xgb_gemm_desc* descs, int n);
 int gemm_tc_tile();
-void launch_gemm_tc(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, const double* A,
-                    const double* B, double* C, double alpha, double beta, cudaStream_t s);
+void launch_gemm_tc(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
+                    const GemmTile* d_tiles, int n_tiles, const double* A, const double* B, float* apack,
+                    float* bpack, double* C, double alpha, double beta, cudaStream_t s);
 int gemm_tc_error(bool reset);  // 1 if a tensor-core GEMM CTA gave up waiting (synchronous read)
 
 // randomized tSVD helpers (rsvd.cu)

@@ -134,7 +134,12 @@ struct GemmPlan {
   int n_tiles = 0, tile = 16;
   xgb_gemm_desc* d_descs = nullptr;
   GemmTile* d_tiles = nullptr;
-  int n_tc_tiles = 0;          // 128 x 128 tiles of the tensor-core form (built on first use)
+  // tensor-core form (built on first use): packing tasks, groups, 128 x 128 tiles
+  bool tc_ready = false;
+  int n_tc_tiles = 0, n_tc_tasks = 0;
+  int64_t tc_a_floats = 0, tc_b_floats = 0;
+  TcGroup* d_tc_groups = nullptr;
+  TcPackTask* d_tc_tasks = nullptr;
   GemmTile* d_tc_tiles = nullptr;
   std::vector<xgb_gemm_desc> host_descs;
 };
@@ -495,24 +500,28 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
   }
   Tensor out = empty_like_meta(plan->out);
   if (g_gemm_precision == XGB_PREC_3XTF32) {
-    if (!plan->d_tc_tiles) {
-      const int tile = gemm_tc_tile();
-      std::vector<GemmTile> tiles;
-      for (size_t g = 0; g < plan->host_descs.size(); ++g) {
-        const auto& d = plan->host_descs[g];
-        const int64_t tm = (d.m + tile - 1) / tile, tn = (d.n + tile - 1) / tile;
-        for (int64_t y = 0; y < tn; ++y)
-          for (int64_t x = 0; x < tm; ++x) tiles.push_back({int32_t(g), int32_t(x), int32_t(y), tile});
-      }
+    {
       std::lock_guard<std::mutex> lk(g_plan_mu);
-      if (!plan->d_tc_tiles) {
-        plan->n_tc_tiles = int(tiles.size());
-        plan->d_tc_tiles = dev_table(tiles);
+      if (!plan->tc_ready) {
+        TcPlanHost tp = build_tc_plan(plan->host_descs.data(), int(plan->host_descs.size()));
+        plan->n_tc_tiles = int(tp.tiles.size());
+        plan->n_tc_tasks = int(tp.tasks.size());
+        plan->tc_a_floats = tp.a_floats;
+        plan->tc_b_floats = tp.b_floats;
+        plan->d_tc_groups = dev_table(tp.groups);
+        plan->d_tc_tasks = dev_table(tp.tasks);
+        plan->d_tc_tiles = dev_table(tp.tiles);
+        plan->tc_ready = true;
       }
     }
+    auto* ap = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(plan->tc_a_floats, 4))));
+    auto* bp = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(plan->tc_b_floats, 4))));
     prof_begin(K_GEMM_TC, stream());
-    launch_gemm_tc(plan->d_descs, plan->d_tc_tiles, plan->n_tc_tiles, a.data(), b.data(), out.data(), 1.0, 0.0, stream());
+    launch_gemm_tc(plan->d_descs, plan->d_tc_groups, plan->d_tc_tasks, plan->n_tc_tasks, plan->d_tc_tiles,
+                   plan->n_tc_tiles, a.data(), b.data(), ap, bp, out.data(), 1.0, 0.0, stream());
     prof_end(K_GEMM_TC, stream(), plan->flops);
+    dev_free(ap);
+    dev_free(bp);
     return out;
   }
   prof_begin(K_GEMM, stream());
