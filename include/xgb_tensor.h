@@ -61,6 +61,13 @@ int xgb_tensor_download(xgb_tensor t, double* host, int64_t n);
 double* xgb_tensor_device_data(xgb_tensor t);
 
 xgb_tensor xgb_tensor_permute(xgb_tensor t, int shift, const int32_t* p, int n);   /* Tensor::permute (Tensor.cpp:335-355) */
+/* Tensor::permute_adj<shift, p...> (Tensor.cpp:258-333): the transpose of permute<shift, p> on
+   a tensor shaped like its output - the reverse rule of permute (ADTensor.hpp:172-184) */
+xgb_tensor xgb_tensor_permute_adj(xgb_tensor t, int shift, const int32_t* p, int n);
+/* reverse rule of operator* (ADTensor.hpp:741-752): left_adj = res_adj * right^dag,
+   right_adj = left^dag * res_adj, each with exactly its operand's structure */
+int xgb_tensor_matmul_backward(xgb_tensor left, xgb_tensor right, xgb_tensor res_adj, xgb_tensor* left_adj,
+                               xgb_tensor* right_adj);
 xgb_tensor xgb_tensor_twist(xgb_tensor t, int leg);                                /* Tensor::twist (Tensor.cpp:357-377) */
 xgb_tensor xgb_tensor_adjoint(xgb_tensor t);                                       /* adjoint().eval() */
 xgb_tensor xgb_tensor_matmul(xgb_tensor a, xgb_tensor b, int adj_a, int adj_b);    /* operator* (TensorBase.cpp:237-288) */

@@ -3,6 +3,7 @@
 References:
   storage layout:   include/Xped/Core/storage/StorageType_contiguous.hpp:79-171
   permute:          src/Core/Tensor.cpp:83-214, 335-355
+  permute_adj:      src/Core/Tensor.cpp:258-333
   twist:            src/Core/Tensor.cpp:357-377
   subBlock:         src/Core/Tensor.cpp:951-981
   operator*:        src/Core/TensorBase.cpp:237-288
@@ -218,6 +219,43 @@ class Tensor:
                         r0 = out.cdom.left_offset(g1)
                         c0 = out.ccod.left_offset(g2)
                         ob[r0:r0 + g1.dim, c0:c0 + g2.dim] += coeff * T.reshape((g1.dim, g2.dim), order="F")
+        return out
+
+    def permute_adj(self, shift, p):
+        """Tensor::permute_adj<shift, p...> (Tensor.cpp:258-333): the transpose
+        (with respect to the stored entries) of the linear map permute<shift, p>,
+        applied to a tensor shaped like that map's output.  Returns a tensor shaped
+        like the map's input."""
+        p = list(p)
+        sym = self.sym
+        R, C = self.rank, self.corank
+        if shift == 0 and p == list(range(R + C)):
+            return self
+        pinv = inverse_permutation(p)
+        newR, newC = R + shift, C - shift
+        new_dom, new_cod = [], []
+        for i in range(newR):
+            if pinv[i] > R - 1 or R == 0:
+                new_dom.append(self.cod[pinv[i] - R].conj())
+            else:
+                new_dom.append(self.dom[pinv[i]])
+        for i in range(newC):
+            if pinv[i + newR] > R - 1 or R == 0:
+                new_cod.append(self.cod[pinv[i + newR] - R])
+            else:
+                new_cod.append(self.dom[pinv[i + newR]].conj())
+        out = Tensor(sym, new_dom, new_cod)
+        for q in out.sectors:
+            ob = out.block(q)
+            for f1 in out.cdom.trees[q]:
+                for f2 in out.ccod.trees[q]:
+                    r0 = out.cdom.left_offset(f1)
+                    c0 = out.ccod.left_offset(f2)
+                    for (g1, g2), coeff in treepair_permute(sym, shift, f1, f2, p).items():
+                        if abs(coeff) < COEFF_CUT:
+                            continue
+                        T = np.transpose(self.sub_block(g1, g2), pinv)
+                        ob[r0:r0 + f1.dim, c0:c0 + f2.dim] += coeff * T.reshape((f1.dim, f2.dim), order="F")
         return out
 
     # -- elementwise --------------------------------------------------------------

@@ -161,3 +161,51 @@ def test_decompose_projectors():
     nP1, nP2 = decompose(n1, n2, 12)
     assert_same(nP1, oP1, 1e-9, 1e-9)
     assert_same(nP2, oP2, 1e-9, 1e-9)
+
+
+@pytest.mark.parametrize("symname,pB,pC", CASES)
+def test_permute_adj_matches_oracle(symname, pB, pC):
+    """permute_adj (Tensor.cpp:258-333) on cotangents shaped like permute's
+    output, all permutations with shifts -1..1."""
+    from oracle.convert import tensor_from_native
+    from xped_gb300 import Tensor
+    s, ob, nb, ot, nt = _pair_tensors(symname, pB, pC, seed=3)
+    rng = np.random.default_rng(5)
+    tol = 0 if symname != "su2" else 1e-13
+    for shift in (-1, 0, 1):
+        for p in itertools.permutations(range(4)):
+            Y = nt.permute(shift, p)                      # forward output structure
+            oY = tensor_from_native(s, Y)
+            oYb = oracle.Tensor(s, oY.dom, oY.cod).set_random(rng)
+            r, c = Y.rank
+            nYb = Tensor.zeros([Y.leg(i) for i in range(r)], [Y.leg(i) for i in range(r, r + c)])
+            nYb.set_data(oYb.data())
+            assert_same(nYb.permute_adj(shift, p), oYb.permute_adj(shift, p), tol, tol)
+
+
+@pytest.mark.parametrize("symname", ["u1", "fz2", "su2"])
+def test_matmul_backward_matches_oracle(symname):
+    """Reverse rule of operator* (ADTensor.hpp:741-752) with the operands'
+    structures; includes sectors of `left` absent from the product."""
+    rng = np.random.default_rng(9)
+    pairs = {"u1": [(-1, 2), (0, 3), (1, 2)], "fz2": [(0, 2), (1, 3)], "su2": [(1, 2), (2, 1), (3, 1)]}[symname]
+    pairs2 = {"u1": [(0, 2), (1, 1), (2, 1)], "fz2": [(0, 1), (1, 2)], "su2": [(1, 1), (2, 2)]}[symname]
+    s, oB, nB = pair_basis(symname, pairs)
+    _, oD, nD = pair_basis(symname, pairs2)
+    oL = oracle.Tensor(s, [oB, oB], [oD]).set_random(rng)
+    oR = oracle.Tensor(s, [oD], [oB]).set_random(rng)
+    oC = oL * oR
+    oCb = oracle.Tensor(s, oC.dom, oC.cod).set_random(rng)
+    nL = to_native(oL, [nB, nB], [nD])
+    nR = to_native(oR, [nD], [nB])
+    nCb = to_native(oCb, [nB, nB], [nB])
+    la, ra = nL.matmul_backward(nR, nCb)
+    ola = oCb * oR.adjoint()
+    ora = oL.adjoint() * oCb
+    for nt, ref, like in ((la, ola, oL), (ra, ora, oR)):
+        qs, rows, cols = nt.sectors()
+        assert qs == like.sectors
+        got = nt.blocks()
+        for q in qs:
+            want = ref.block(q) if ref.has(q) else np.zeros((rows[qs.index(q)], cols[qs.index(q)]))
+            assert np.allclose(got[q], want, rtol=0, atol=1e-12 * max(1.0, np.abs(want).max()))

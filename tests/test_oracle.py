@@ -11,6 +11,7 @@ import oracle
 from oracle.basis import Qbasis, decompose_permutation, inverse_permutation, treepair_permute
 from oracle.sym import wigner6j_twice
 from oracle.tensor import get_permutations, decompose
+from helpers import random_pairs
 
 
 def _rand_basis(rng, sym, n, qrange):
@@ -184,3 +185,23 @@ def test_decompose_projector_identity():
     I = P1 * P2
     for q, b in zip(I.sectors, I.blocks):
         assert np.allclose(b, np.eye(b.shape[0]), atol=1e-9)
+
+
+def test_permute_adj_is_the_adjoint_of_permute():
+    """<permute(X), Y> == <X, permute_adj(Y)> on the stored entries
+    (Tensor.cpp:258-333 is the transpose of permute_impl), for every
+    permutation of a rank-4 tensor and shifts -1..1; U(1), fermionic U(1), SU(2)."""
+    import itertools
+    rng = np.random.default_rng(0)
+    for sym in ("u1", "fu1", "su2"):
+        s = oracle.make_symmetry(sym)
+        legs = [Qbasis.from_pairs(s, random_pairs(rng, sym, 6 if sym != "su2" else 8), sort=True) for _ in range(4)]
+        X = oracle.Tensor(s, legs[:2], legs[2:]).set_random(rng)
+        for shift in (-1, 0, 1):
+            for p in itertools.permutations(range(4)):
+                Y = X.permute(shift, p)
+                Yb = oracle.Tensor(s, Y.dom, Y.cod).set_random(rng)
+                Xb = Yb.permute_adj(shift, p)
+                assert Xb.sectors == X.sectors
+                lhs, rhs = float(Y.data() @ Yb.data()), float(X.data() @ Xb.data())
+                assert abs(lhs - rhs) <= 1e-12 * max(1.0, abs(lhs)), (sym, shift, p)

@@ -96,6 +96,8 @@ PROTOS = [
     ("xgb_tensor_download", C.c_int, [P, dblp, C.c_int64]),
     ("xgb_tensor_device_data", P, [P]),
     ("xgb_tensor_permute", P, [P, C.c_int, i32p, C.c_int]),
+    ("xgb_tensor_permute_adj", P, [P, C.c_int, i32p, C.c_int]),
+    ("xgb_tensor_matmul_backward", C.c_int, [P, P, P, C.POINTER(P), C.POINTER(P)]),
     ("xgb_tensor_twist", P, [P, C.c_int]),
     ("xgb_tensor_adjoint", P, [P]),
     ("xgb_tensor_matmul", P, [P, P, C.c_int, C.c_int]),

@@ -173,6 +173,18 @@ double* xgb_tensor_device_data(xgb_tensor t) {
 xgb_tensor xgb_tensor_permute(xgb_tensor t, int shift, const int32_t* p, int n) {
   GUARD(nullptr, { return wrap(permute(t->t, shift, std::vector<int>(p, p + n))); })
 }
+xgb_tensor xgb_tensor_permute_adj(xgb_tensor t, int shift, const int32_t* p, int n) {
+  GUARD(nullptr, { return wrap(permute_adj(t->t, shift, std::vector<int>(p, p + n))); })
+}
+int xgb_tensor_matmul_backward(xgb_tensor left, xgb_tensor right, xgb_tensor res_adj, xgb_tensor* left_adj,
+                               xgb_tensor* right_adj) {
+  GUARD(XGB_E_BADPLAN, {
+    auto [la, ra] = matmul_backward(left->t, right->t, res_adj->t);
+    if (left_adj) *left_adj = wrap(la);
+    if (right_adj) *right_adj = wrap(ra);
+    return XGB_OK;
+  })
+}
 xgb_tensor xgb_tensor_twist(xgb_tensor t, int leg) { GUARD(nullptr, { return wrap(twist(t->t, leg)); }) }
 xgb_tensor xgb_tensor_adjoint(xgb_tensor t) { GUARD(nullptr, { return wrap(adjoint(t->t)); }) }
 xgb_tensor xgb_tensor_matmul(xgb_tensor a, xgb_tensor b, int adj_a, int adj_b) {

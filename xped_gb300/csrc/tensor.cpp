@@ -313,6 +313,52 @@ PermTables build_perm_tables(const TensorMeta& in, uint32_t mask, int shift, con
   return tb.tables(out);
 }
 
+PermTables build_perm_adj_tables(const TensorMeta& in, int shift, const std::vector<int>& p) {
+  // Tensor::permute_adj<shift, p...> (Tensor.cpp:258-333): `in` is shaped like
+  // the output of permute<shift, p>; every sub-block (f1, f2) of the result
+  // (shaped like that permute's input) gathers coeff * shuffle^-1 of the
+  // sub-blocks that the forward treepair::permute maps (f1, f2) to.
+  const Sym& s = in.sym;
+  const int R = in.rank(), C = in.corank(), N = R + C;
+  const int newR = R + shift, newC = C - shift;
+  std::vector<int> pinv(N);
+  for (int i = 0; i < N; ++i) pinv[p[i]] = i;
+  std::vector<BasisPtr> nd, nc;
+  for (int i = 0; i < newR; ++i)
+    nd.push_back((pinv[i] > R - 1 || R == 0) ? basis_conj(in.cod[pinv[i] - R]) : in.dom[pinv[i]]);
+  for (int i = 0; i < newC; ++i) {
+    const int x = pinv[i + newR];
+    nc.push_back((x > R - 1 || R == 0) ? in.cod[x - R] : basis_conj(in.dom[x]));
+  }
+  MetaPtr out = make_meta(s, nd, nc);
+  TaskBuilder tb;
+  int64_t ist[kMaxRank], ost[kMaxRank], sst[kMaxRank];
+  int32_t odims[kMaxRank];
+  for (size_t so = 0; so < out->sectors.size(); ++so) {
+    const int q = out->sectors[so];
+    const int dq = out->cdom->index(q), cq = out->ccod->index(q);
+    for (const auto& f1 : out->cdom->trees[dq]) {
+      for (const auto& f2 : out->ccod->trees[cq]) {
+        const int64_t dst_base = out->offset[so] + out->cdom->left_offset(f1) + out->ccod->left_offset(f2) * out->rows[so];
+        sub_strides(f1, f2, out->rows[so], ost);
+        for (int k = 0; k < N; ++k) odims[k] = (k < f1.rank) ? f1.dims[k] : f2.dims[k - f1.rank];
+        for (const auto& [pr, c] : treepair_permute(s, shift, f1, f2, p)) {
+          if (std::abs(c) < kCoeffCut) continue;
+          const FusionTree& g1 = pr.first;
+          const FusionTree& g2 = pr.second;
+          const int si = in.index(g1.qc);
+          if (si < 0) throw std::runtime_error("permute_adj plan: input sector missing");
+          const int64_t src_base = in.offset[si] + in.cdom->left_offset(g1) + in.ccod->left_offset(g2) * in.rows[si];
+          sub_strides(g1, g2, in.rows[si], ist);
+          for (int k = 0; k < N; ++k) sst[k] = ist[pinv[k]];
+          tb.add(dst_base, N, odims, ost, src_base, sst, c);
+        }
+      }
+    }
+  }
+  return tb.tables(out);
+}
+
 namespace {
 std::string perm_key(const TensorMeta& m, uint32_t mask, int shift, const std::vector<int>& p) {
   std::ostringstream os;
@@ -373,6 +419,33 @@ Tensor permute(const Tensor& t, int shift, const std::vector<int>& p) {
   for (int i = 0; i < R + C && id; ++i) id = (p[i] == i);
   if (id) return materialize(t);
   auto plan = get_perm_plan(*t.meta, t.twist_mask, shift, p);
+  return run_perm_plan(*plan, t);
+}
+
+Tensor permute_adj(const Tensor& t0, int shift, const std::vector<int>& p) {
+  Tensor t = materialize(t0);
+  const int R = t.meta->rank(), C = t.meta->corank();
+  if (int(p.size()) != R + C) throw std::runtime_error("permute_adj: permutation length mismatch");
+  if (-shift > R || shift > C) throw std::runtime_error("permute_adj: invalid shift");
+  bool id = shift == 0;
+  for (int i = 0; i < R + C && id; ++i) id = (p[i] == i);
+  if (id) return t;
+  std::ostringstream os;
+  os << "padj|" << t.meta->id << '|' << shift << '|';
+  for (int x : p) os << x << ',';
+  const std::string key = os.str();
+  std::shared_ptr<PermPlan> plan;
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    auto it = g_perm_plans.find(key);
+    if (it != g_perm_plans.end()) { plan = it->second; ++g_stats.perm_hits; }
+  }
+  if (!plan) {
+    plan = upload_tables(build_perm_adj_tables(*t.meta, shift, p));
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    ++g_stats.perm_misses;
+    g_perm_plans[key] = plan;
+  }
   return run_perm_plan(*plan, t);
 }
 
@@ -528,6 +601,40 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
   launch_gemm_f64(plan->d_descs, plan->d_tiles, plan->n_tiles, plan->tile, a.data(), b.data(), out.data(), 1.0, 0.0, stream());
   prof_end(K_GEMM, stream(), plan->flops);
   return out;
+}
+
+Tensor embed(const Tensor& src0, const MetaPtr& target) {
+  // blocks of `src` copied into a zero tensor with `target`'s structure, sector
+  // by sector (charges absent from src stay zero; shapes must agree)
+  Tensor src = materialize(src0);
+  Tensor out = zeros(target);
+  std::vector<xgb_copy2d_desc> d;
+  int64_t mx = 0;
+  for (size_t i = 0; i < target->sectors.size(); ++i) {
+    const int si = src.meta->index(target->sectors[i]);
+    if (si < 0) continue;
+    if (src.meta->rows[si] != target->rows[i] || src.meta->cols[si] != target->cols[i])
+      throw std::runtime_error("embed: block shapes differ");
+    d.push_back({src.meta->offset[si], src.meta->rows[si], target->offset[i], target->rows[i], target->rows[i],
+                 target->cols[i]});
+    mx = std::max(mx, target->rows[i] * target->cols[i]);
+  }
+  if (d.empty()) return out;
+  auto* dd = static_cast<xgb_copy2d_desc*>(dev_alloc(sizeof(xgb_copy2d_desc) * d.size()));
+  cuda_ok(cudaMemcpyAsync(dd, d.data(), sizeof(xgb_copy2d_desc) * d.size(), cudaMemcpyHostToDevice, stream()), "h2d");
+  prof_begin(K_COPY2D, stream());
+  launch_copy2d(dd, int(d.size()), mx, src.data(), out.data(), stream());
+  prof_end(K_COPY2D, stream(), 16.0 * double(target->size));
+  dev_free(dd);
+  return out;
+}
+
+std::pair<Tensor, Tensor> matmul_backward(const Tensor& left, const Tensor& right, const Tensor& res_adj) {
+  // reverse rule of operator* (ADTensor.hpp:741-752):
+  //   left.adj += res.adj * right^dag,  right.adj += left^dag * res.adj
+  Tensor la = matmul(res_adj, right, false, true);
+  Tensor ra = matmul(left, res_adj, true, false);
+  return {embed(la, left.meta), embed(ra, right.meta)};
 }
 
 int gemm_precision() { return g_gemm_precision; }

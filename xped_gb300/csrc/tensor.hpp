@@ -70,6 +70,14 @@ Tensor empty_like_meta(const MetaPtr& m);
 // Operations (names follow the reference).
 Tensor materialize(const Tensor& t);  // apply pending twists
 Tensor permute(const Tensor& t, int shift, const std::vector<int>& p);
+// reverse rule of operator* (ADTensor.hpp:741-752): the cotangents of left and
+// right (with exactly their structures) from the cotangent of left * right
+std::pair<Tensor, Tensor> matmul_backward(const Tensor& left, const Tensor& right, const Tensor& res_adj);
+// blocks of src placed in a zero tensor of the target structure (matching charges)
+Tensor embed(const Tensor& src, const MetaPtr& target);
+// Tensor::permute_adj<shift, p...>: transpose of permute<shift, p> applied to a
+// tensor shaped like its output (the reverse rule of permute, ADTensor.hpp:172-184)
+Tensor permute_adj(const Tensor& t, int shift, const std::vector<int>& p);
 Tensor twist(const Tensor& t, int leg);
 Tensor adjoint(const Tensor& t);
 Tensor matmul(const Tensor& a, const Tensor& b, bool adj_a = false, bool adj_b = false);
@@ -243,6 +251,7 @@ struct PermTables {
   bool needs_zero = false;
 };
 PermTables build_perm_tables(const TensorMeta& in, uint32_t mask, int shift, const std::vector<int>& p);
+PermTables build_perm_adj_tables(const TensorMeta& in, int shift, const std::vector<int>& p);
 struct GemmTables {
   MetaPtr out;
   std::vector<xgb_gemm_desc> descs;

@@ -186,6 +186,17 @@ class Tensor:
     def permute(self, shift: int, p: Sequence[int]) -> "Tensor":
         return Tensor(lib().xgb_tensor_permute(self._h, int(shift), _i32(list(p)), len(p)))
 
+    def permute_adj(self, shift: int, p: Sequence[int]) -> "Tensor":
+        """Tensor::permute_adj<shift, p...>: transpose of permute on its output shape."""
+        return Tensor(lib().xgb_tensor_permute_adj(self._h, int(shift), _i32(list(p)), len(p)))
+
+    def matmul_backward(self, right: "Tensor", res_adj: "Tensor"):
+        """Reverse rule of self * right: (self_adj, right_adj)."""
+        la, ra = C.c_void_p(), C.c_void_p()
+        check(lib().xgb_tensor_matmul_backward(self._h, right._h, res_adj._h, C.byref(la), C.byref(ra)),
+              "matmul_backward")
+        return Tensor(la.value), Tensor(ra.value)
+
     def twist(self, leg: int) -> "Tensor":
         return Tensor(lib().xgb_tensor_twist(self._h, int(leg)))
 
