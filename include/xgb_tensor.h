@@ -85,15 +85,17 @@ int xgb_tensor_tsvd(xgb_tensor t, int64_t max_keep, double eps_svd, int preserve
    sketch[i] <= 0 or 2*sketch[i] >= min(rows, cols) decomposes sector i exactly;
    power_iters subspace iterations; Gaussian test matrices from `seed`; `warm` (may
    be NULL): a V^dag of an earlier decomposition with the same column bases whose
-   rows of charge q replace the first Gaussian columns of sector q.  A sketched
+   rows of charge q replace the first Gaussian columns of sector q; res_tol > 0: a
+   sector whose kept triplets have ||A v - s u|| > res_tol * s_max gets power_iters
+   more subspace iterations from its current basis (at most three times).  A sketched
    sector that keeps all of its sketch is redone with twice the columns, exactly
    after the third doubling (n_saturated counts the redos).
    keep[] and width[] (may be NULL) get, per input sector, the kept count and the
    sketch width used (min(rows, cols) for exact sectors). */
 int xgb_tensor_tsvd_randomized(xgb_tensor t, int64_t max_keep, double eps_svd, int n_sectors, const int64_t* sketch,
-                               int power_iters, uint64_t seed, xgb_tensor warm, xgb_tensor* U, xgb_tensor* S,
-                               xgb_tensor* Vdag, double* trunc_weight, double* entropy, int32_t* keep, int64_t* width,
-                               int32_t* n_saturated);
+                               int power_iters, uint64_t seed, xgb_tensor warm, double res_tol, xgb_tensor* U,
+                               xgb_tensor* S, xgb_tensor* Vdag, double* trunc_weight, double* entropy, int32_t* keep,
+                               int64_t* width, int32_t* n_saturated);
 int xgb_tensor_tqr(xgb_tensor t, xgb_tensor* Q, xgb_tensor* R);                    /* Tensor::tQR (Tensor.cpp:757-780) */
 /* decompose (src/PEPS/PEPSContractions.cpp:16-43) */
 int xgb_decompose(xgb_tensor t1, xgb_tensor t2, int64_t max_nsv, xgb_tensor* P1, xgb_tensor* P2);
@@ -126,6 +128,11 @@ int xgb_ctm_set_gemm_precision(xgb_ctm c, int precision);
    the sketch and warm_iters subspace iterations are run instead of power_iters
    (warm_iters < 0: off, the default). */
 int xgb_ctm_set_warm_start(xgb_ctm c, int warm_iters);
+/* Residual control of the randomized projector SVD: kept triplets must satisfy
+   ||A v - s u|| <= tol * s_max, else more subspace iterations (0: off) */
+int xgb_ctm_set_residual_tol(xgb_ctm c, double tol);
+/* refinement passes so far and the largest relative residual of the last decomposition */
+int xgb_ctm_residual_stats(xgb_ctm c, int64_t* refinements, double* max_residual);
 /* out5: decompositions, sketched sectors, exact sectors, sketch redos, sketch columns */
 int xgb_ctm_stats(xgb_ctm c, int64_t* out5);
 /* Decomposition log for learning sketch widths (features of the rank predictor,

@@ -108,7 +108,8 @@ PROTOS = [
     ("xgb_tensor_tsvd", C.c_int, [P, C.c_int64, C.c_double, C.c_int, C.POINTER(P), C.POINTER(P), C.POINTER(P),
                                   dblp, dblp, i32p]),
     ("xgb_tensor_tsvd_randomized", C.c_int, [P, C.c_int64, C.c_double, C.c_int, i64p, C.c_int, C.c_uint64, P,
-                                             C.POINTER(P), C.POINTER(P), C.POINTER(P), dblp, dblp, i32p, i64p, i32p]),
+                                             C.c_double, C.POINTER(P), C.POINTER(P), C.POINTER(P), dblp, dblp, i32p,
+                                             i64p, i32p]),
     ("xgb_tensor_tqr", C.c_int, [P, C.POINTER(P), C.POINTER(P)]),
     ("xgb_decompose", C.c_int, [P, P, C.c_int64, C.POINTER(P), C.POINTER(P)]),
     ("xgb_tensor_release", None, [P]),
@@ -118,6 +119,8 @@ PROTOS = [
     ("xgb_ctm_set_svd", C.c_int, [P, C.c_int, C.c_int, C.c_uint64, C.c_int64, C.c_double]),
     ("xgb_ctm_stats", C.c_int, [P, i64p]),
     ("xgb_ctm_set_warm_start", C.c_int, [P, C.c_int]),
+    ("xgb_ctm_set_residual_tol", C.c_int, [P, C.c_double]),
+    ("xgb_ctm_residual_stats", C.c_int, [P, i64p, dblp]),
     ("xgb_ctm_set_gemm_precision", C.c_int, [P, C.c_int]),
     ("xgb_set_gemm_precision", C.c_int, [C.c_int]),
     ("xgb_ctm_record", C.c_int, [P, C.c_int]),

@@ -215,15 +215,15 @@ int xgb_tensor_tsvd(xgb_tensor t, int64_t max_keep, double eps_svd, int preserve
 }
 
 int xgb_tensor_tsvd_randomized(xgb_tensor t, int64_t max_keep, double eps_svd, int n_sectors, const int64_t* sketch,
-                               int power_iters, uint64_t seed, xgb_tensor warm, xgb_tensor* U, xgb_tensor* S,
-                               xgb_tensor* Vdag, double* trunc_weight, double* entropy, int32_t* keep, int64_t* width,
-                               int32_t* n_saturated) {
+                               int power_iters, uint64_t seed, xgb_tensor warm, double res_tol, xgb_tensor* U,
+                               xgb_tensor* S, xgb_tensor* Vdag, double* trunc_weight, double* entropy, int32_t* keep,
+                               int64_t* width, int32_t* n_saturated) {
   GUARD(XGB_E_BADPLAN, {
     if (n_sectors != int(t->t.meta->sectors.size()) || (n_sectors > 0 && !sketch))
       return set_error(XGB_E_BADPLAN, "randomized tSVD: one sketch width per sector required");
     RsvdInfo info;
     SVDResult r = tsvd_randomized(t->t, max_keep, eps_svd, std::vector<int64_t>(sketch, sketch + n_sectors),
-                                  power_iters, seed, &info, warm ? &warm->t : nullptr);
+                                  power_iters, seed, &info, warm ? &warm->t : nullptr, res_tol);
     if (U) *U = wrap(r.U);
     if (S) *S = wrap(r.S);
     if (Vdag) *Vdag = wrap(r.Vdag);
@@ -318,6 +318,22 @@ int xgb_ctm_set_warm_start(xgb_ctm c, int warm_iters) {
     c->c->warm_iters = warm_iters < 0 ? -1 : warm_iters;
     if (warm_iters < 0)
       for (auto& w : c->c->warm_v) w = Tensor();
+    return XGB_OK;
+  })
+}
+
+int xgb_ctm_set_residual_tol(xgb_ctm c, double tol) {
+  GUARD(XGB_E_BADPLAN, {
+    if (!(tol >= 0)) throw std::runtime_error("residual tolerance must be >= 0");
+    c->c->res_tol = tol;
+    return XGB_OK;
+  })
+}
+
+int xgb_ctm_residual_stats(xgb_ctm c, int64_t* refinements, double* max_residual) {
+  GUARD(XGB_E_BADPLAN, {
+    if (refinements) *refinements = c->c->stats.refinements;
+    if (max_residual) *max_residual = c->c->stats.max_residual;
     return XGB_OK;
   })
 }

@@ -73,6 +73,10 @@ struct SignFixDesc { int64_t m, n, k, u_off, v_off; };      // U m x k (ld m), V
 void launch_gauss_fill(const GaussBlock* d_blocks, int n_blocks, int64_t max_count, uint64_t seed, double* out,
                        cudaStream_t s);
 void launch_sign_fix(const SignFixDesc* d_descs, int n, int64_t max_k, double* U, double* Vt, cudaStream_t s);
+// per-column residuals ||R[:, j] - S[j] U[:, j]|| (desc: m, n = output offset, k columns, u_off of R and U,
+// v_off = offset of S)
+void launch_residual_norms(const SignFixDesc* d_descs, int n, int64_t max_k, const double* R, const double* U,
+                           const double* S, double* res, cudaStream_t s);
 // transposed block copies: src block rows x cols (ld src_ld) -> dst cols x rows (ld dst_ld)
 void launch_transpose_copy(const xgb_copy2d_desc* d_descs, int n, int64_t max_elems, const double* src, double* dst,
                            cudaStream_t s);

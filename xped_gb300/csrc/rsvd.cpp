@@ -123,11 +123,12 @@ void orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64_t>
 }
 
 constexpr int kMaxRetries = 3;
+constexpr int kMaxRefine = 3;  // refinement passes of unconverged sectors per round
 
 }  // namespace
 
 SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, const std::vector<int64_t>& sketch,
-                          int power_iters, uint64_t seed, RsvdInfo* info, const Tensor* warm) {
+                          int power_iters, uint64_t seed, RsvdInfo* info, const Tensor* warm, double res_tol) {
   Tensor t = materialize(t0);
   const TensorMeta& m = *t.meta;
   const int n = int(m.sectors.size());
@@ -135,9 +136,25 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
   if (int(sketch.size()) != n) throw std::runtime_error("randomized tSVD: one sketch width per sector required");
   if (power_iters < 0) throw std::runtime_error("randomized tSVD: negative number of power iterations");
   cudaStream_t st = stream();
+  // warm-start rows per sector (a V^dag block of the same charge and column dimension)
+  Tensor warm_t;
+  std::vector<int64_t> w_off(n, -1), w_rows(n, 0);
+  if (warm && warm->valid()) {
+    warm_t = materialize(*warm);
+    const TensorMeta& wm = *warm_t.meta;
+    for (int i = 0; i < n; ++i) {
+      const int wi = wm.index(m.sectors[i]);
+      if (wi >= 0 && wm.cols[wi] == m.cols[i]) {
+        w_off[i] = wm.offset[wi];
+        w_rows[i] = wm.rows[wi];
+      }
+    }
+  }
   std::vector<char> exact(n, 0);
   std::vector<int64_t> want(sketch);
   std::vector<int> saturated;
+  int refinements = 0;
+  double max_res = 0;
   for (int round = 0;; ++round) {
     // ---- widths and layout
     std::vector<int64_t> width(n);
@@ -189,11 +206,63 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
     sp.V = alloc_d(vt);
     double* Bb = alloc_d(bt);
     double* Q = nr ? alloc_d(yt) : nullptr;
+    double* Om = nr ? alloc_d(std::max(omt, zt)) : nullptr;
+    double* Y = nr ? alloc_d(yt) : nullptr;
+    double* Z = nr ? alloc_d(zt) : nullptr;
+
+    // subspace iterations Q <- orth(A orth(A^T Q)) for the sketched sectors `sub` (indices into R)
+    auto iterate = [&](const std::vector<int>& sub, int iters) {
+      std::vector<int64_t> srr, src, srl, syo, szo;
+      for (int a : sub) {
+        srr.push_back(rr[a]);
+        src.push_back(rc[a]);
+        srl.push_back(rl[a]);
+        syo.push_back(yo[a]);
+        szo.push_back(zo[a]);
+      }
+      std::vector<xgb_gemm_desc> g;
+      for (int p = 0; p < iters; ++p) {
+        g.clear();
+        for (int a : sub) g.push_back({rc[a], rl[a], rr[a], m.offset[R[a]], rr[a], yo[a], rr[a], zo[a], rc[a], 1, 0});
+        grouped_gemm(g, t.data(), Q, Z, st);
+        orthonormalise(src, srl, szo, Z, Om, st);  // Omega's storage holds Qz (same layout as Z)
+        g.clear();
+        for (int a : sub) g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], zo[a], rc[a], yo[a], rr[a], 0, 0});
+        grouped_gemm(g, t.data(), Om, Y, st);
+        orthonormalise(srr, srl, syo, Y, Q, st);
+      }
+    };
+    // Rayleigh-Ritz on span(Q) for `sub`: B = Q^T A, then (with the exact sectors `ex`) one
+    // batched SVD, U = Q U_B, sign rule
+    auto project = [&](const std::vector<int>& sub, const std::vector<int>& ex) {
+      std::vector<xgb_gemm_desc> g;
+      for (int a : sub) g.push_back({rl[a], rc[a], rr[a], yo[a], rr[a], m.offset[R[a]], rr[a], bo[R[a]], rl[a], 1, 0});
+      grouped_gemm(g, Q, t.data(), Bb, st);
+      std::vector<xgb_svd_desc> d;
+      for (int i : ex) d.push_back({m.rows[i], m.cols[i], bo[i], sp.u_off[i], sp.s_begin[i], sp.v_off[i]});
+      for (int a : sub) d.push_back({rl[a], rc[a], bo[R[a]], ub[a], sp.s_begin[R[a]], sp.v_off[R[a]]});
+      batched_svd(d, Bb, sp.U, sp.S, sp.V, st);
+      if (sub.empty()) return;
+      g.clear();
+      std::vector<SignFixDesc> sf;
+      int64_t mx = 0;
+      for (int a : sub) {
+        const int i = R[a];
+        g.push_back({rr[a], rl[a], rl[a], yo[a], rr[a], ub[a], rl[a], sp.u_off[i], rr[a], 0, 0});
+        sf.push_back({rr[a], rc[a], rl[a], sp.u_off[i], sp.v_off[i]});
+        mx = std::max(mx, rl[a]);
+      }
+      grouped_gemm(g, Q, sp.U, sp.U, st);
+      Staging ss;
+      const size_t o = ss.add(sf);
+      ss.upload(st);
+      prof_begin(K_SKETCH, st);
+      launch_sign_fix(ss.at<SignFixDesc>(o), int(sf.size()), mx, sp.U, sp.V, st);
+      prof_end(K_SKETCH, st, 16.0 * double(yt + vt));
+    };
 
     if (nr) {
-      double* Om = alloc_d(std::max(omt, zt));
-      double* Y = alloc_d(yt);
-      // ---- Omega
+      // ---- Omega: seeded Gaussian columns, the first ones replaced by warm-start rows
       {
         std::vector<GaussBlock> gb;
         int64_t mx = 0;
@@ -208,18 +277,14 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
         launch_gauss_fill(sg.at<GaussBlock>(o), nr, mx, seed, Om, st);
         prof_end(K_SKETCH, st, 8.0 * double(omt));
       }
-      // ---- warm start: the first columns of Omega_i are the rows of the
-      // previous V^dag block of the same charge (its right singular vectors)
-      if (warm && warm->valid()) {
-        const TensorMeta& wm = *warm->meta;
+      if (warm_t.valid()) {
         std::vector<xgb_copy2d_desc> td;  // src k x n (ld k) -> dst n x k (ld n), transposed
         int64_t mx = 0;
         for (int a = 0; a < nr; ++a) {
-          const int wi = wm.index(m.sectors[R[a]]);
-          if (wi < 0 || wm.cols[wi] != rc[a]) continue;
-          const int64_t kw = std::min<int64_t>(wm.rows[wi], rl[a]);
-          if (kw <= 0) continue;
-          td.push_back({wm.offset[wi], wm.rows[wi], om[a], rc[a], kw, rc[a]});
+          const int i = R[a];
+          const int64_t kw = std::min<int64_t>(w_rows[i], rl[a]);
+          if (w_off[i] < 0 || kw <= 0) continue;
+          td.push_back({w_off[i], w_rows[i], om[a], rc[a], kw, rc[a]});
           mx = std::max(mx, kw * rc[a]);
         }
         if (!td.empty()) {
@@ -227,43 +292,21 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
           const size_t o = sw.add(td);
           sw.upload(st);
           prof_begin(K_SKETCH, st);
-          launch_transpose_copy(sw.at<xgb_copy2d_desc>(o), int(td.size()), mx, materialize(*warm).data(), Om, st);
+          launch_transpose_copy(sw.at<xgb_copy2d_desc>(o), int(td.size()), mx, warm_t.data(), Om, st);
           prof_end(K_SKETCH, st, 16.0 * double(mx) * double(td.size()));
         }
       }
-      // ---- Y = A Omega, Q = orth(Y)
+      // ---- Y = A Omega, Q = orth(Y), subspace iterations
       std::vector<xgb_gemm_desc> g;
       for (int a = 0; a < nr; ++a)
         g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], om[a], rc[a], yo[a], rr[a], 0, 0});
       grouped_gemm(g, t.data(), Om, Y, st);
       orthonormalise(rr, rl, yo, Y, Q, st);
-      // ---- subspace iterations: Z = A^T Q, Qz = orth(Z), Y = A Qz, Q = orth(Y)
-      if (power_iters > 0) {
-        double* Z = alloc_d(zt);
-        double* Qz = Om;  // Omega is no longer needed
-        for (int p = 0; p < power_iters; ++p) {
-          g.clear();
-          for (int a = 0; a < nr; ++a)
-            g.push_back({rc[a], rl[a], rr[a], m.offset[R[a]], rr[a], yo[a], rr[a], zo[a], rc[a], 1, 0});
-          grouped_gemm(g, t.data(), Q, Z, st);
-          orthonormalise(rc, rl, zo, Z, Qz, st);
-          g.clear();
-          for (int a = 0; a < nr; ++a)
-            g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], zo[a], rc[a], yo[a], rr[a], 0, 0});
-          grouped_gemm(g, t.data(), Qz, Y, st);
-          orthonormalise(rr, rl, yo, Y, Q, st);
-        }
-        dev_free(Z);
-      }
-      // ---- B = Q^T A (l x n)
-      g.clear();
-      for (int a = 0; a < nr; ++a)
-        g.push_back({rl[a], rc[a], rr[a], yo[a], rr[a], m.offset[R[a]], rr[a], bo[R[a]], rl[a], 1, 0});
-      grouped_gemm(g, Q, t.data(), Bb, st);
-      dev_free(Y);
-      dev_free(Om);
+      std::vector<int> all(nr);
+      for (int a = 0; a < nr; ++a) all[a] = a;
+      iterate(all, power_iters);
     }
-    // ---- exact sectors: their blocks join the final batched SVD
+    // ---- exact sectors: their blocks join the batched SVD of the projected blocks
     if (!E.empty()) {
       std::vector<xgb_copy2d_desc> cd;
       int64_t mx = 0;
@@ -278,42 +321,71 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       launch_copy2d(sc.at<xgb_copy2d_desc>(o), int(cd.size()), mx, t.data(), Bb, st);
       prof_end(K_COPY2D, st, 16.0 * double(bt));
     }
-    // ---- one batched SVD: exact sectors (largest first) and the sketched B blocks
-    {
-      std::vector<xgb_svd_desc> d;
-      std::vector<int> order(E.begin(), E.end());
-      std::sort(order.begin(), order.end(), [&](int x, int y) {
-        return m.rows[x] * m.cols[x] * std::min(m.rows[x], m.cols[x]) > m.rows[y] * m.cols[y] * std::min(m.rows[y], m.cols[y]);
-      });
-      for (int i : order) d.push_back({m.rows[i], m.cols[i], bo[i], sp.u_off[i], sp.s_begin[i], sp.v_off[i]});
-      for (int a = 0; a < nr; ++a) {
-        const int i = R[a];
-        d.push_back({rl[a], rc[a], bo[i], ub[a], sp.s_begin[i], sp.v_off[i]});
-      }
-      batched_svd(d, Bb, sp.U, sp.S, sp.V, st);
-    }
-    dev_free(Bb);
-    if (nr) {
-      // ---- U = Q U_B, then the sign convention on the lifted vectors
+    std::vector<int> order(E.begin(), E.end());  // largest exact blocks first
+    std::sort(order.begin(), order.end(), [&](int x, int y) {
+      return m.rows[x] * m.cols[x] * std::min(m.rows[x], m.cols[x]) > m.rows[y] * m.cols[y] * std::min(m.rows[y], m.cols[y]);
+    });
+    std::vector<int> all(nr);
+    for (int a = 0; a < nr; ++a) all[a] = a;
+    project(all, order);
+
+    // ---- residuals ||A v_j - s_j u_j|| of the sketched triplets; refinement of the sectors whose
+    // kept triplets miss the tolerance (more subspace iterations from the current basis)
+    SVDResult res = truncate_spectra(m, sp, max_keep, eps_svd, false);
+    double smax = 0;
+    for (double v : res.spectrum) smax = std::max(smax, v);
+    for (int pass = 0; nr > 0; ++pass) {
       std::vector<xgb_gemm_desc> g;
-      std::vector<SignFixDesc> sf;
-      int64_t mx = 0;
+      std::vector<SignFixDesc> rd;
+      int64_t rtot = 0, mx = 0;
+      std::vector<int64_t> r_off(nr);
       for (int a = 0; a < nr; ++a) {
         const int i = R[a];
-        g.push_back({rr[a], rl[a], rl[a], yo[a], rr[a], ub[a], rl[a], sp.u_off[i], rr[a], 0, 0});
-        sf.push_back({rr[a], rc[a], rl[a], sp.u_off[i], sp.v_off[i]});
+        // A V into the residual buffer at the U offsets (V = (V^dag)^T, ld of V^dag = l)
+        g.push_back({rr[a], rl[a], rc[a], m.offset[i], rr[a], sp.v_off[i], rl[a], sp.u_off[i], rr[a], 0, 1});
+        r_off[a] = rtot;
+        rd.push_back({rr[a], rtot, rl[a], sp.u_off[i], sp.s_begin[i]});
+        rtot += rl[a];
         mx = std::max(mx, rl[a]);
       }
-      grouped_gemm(g, Q, sp.U, sp.U, st);
-      Staging ss;
-      const size_t o = ss.add(sf);
-      ss.upload(st);
-      prof_begin(K_SKETCH, st);
-      launch_sign_fix(ss.at<SignFixDesc>(o), nr, mx, sp.U, sp.V, st);
-      prof_end(K_SKETCH, st, 16.0 * double(yt + vt));
+      double* Rb = alloc_d(ut);
+      grouped_gemm(g, t.data(), sp.V, Rb, st);
+      double* rv = alloc_d(rtot);
+      {
+        Staging sr;
+        const size_t o = sr.add(rd);
+        sr.upload(st);
+        prof_begin(K_SKETCH, st);
+        launch_residual_norms(sr.at<SignFixDesc>(o), nr, mx, Rb, sp.U, sp.S, rv, st);
+        prof_end(K_SKETCH, st, 16.0 * double(ut));
+      }
+      std::vector<double> rh(size_t(std::max<int64_t>(rtot, 1)));
+      ok(cudaMemcpyAsync(rh.data(), rv, sizeof(double) * size_t(rtot), cudaMemcpyDeviceToHost, st), "d2h residuals");
+      ok(cudaStreamSynchronize(st), "sync");
+      dev_free(rv);
+      dev_free(Rb);
+      std::vector<int> bad;
+      double worst = 0;
+      for (int a = 0; a < nr; ++a) {
+        double ra = 0;
+        for (int64_t j = 0; j < std::min<int64_t>(res.keep[R[a]], rl[a]); ++j) ra = std::max(ra, rh[size_t(r_off[a] + j)]);
+        worst = std::max(worst, smax > 0 ? ra / smax : 0.0);
+        if (res_tol > 0 && smax > 0 && ra > res_tol * smax) bad.push_back(a);
+      }
+      max_res = worst;
+      if (bad.empty() || pass >= kMaxRefine) break;
+      ++refinements;
+      iterate(bad, std::max(power_iters, 1));
+      project(bad, {});
+      res = truncate_spectra(m, sp, max_keep, eps_svd, false);
+    }
+    if (nr) {
+      dev_free(Om);
+      dev_free(Y);
+      dev_free(Z);
       dev_free(Q);
     }
-    SVDResult res = truncate_spectra(m, sp, max_keep, eps_svd, false);
+    dev_free(Bb);
     dev_free(sp.U);
     dev_free(sp.S);
     dev_free(sp.V);
@@ -327,6 +399,8 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
         info->sketch_cols = 0;
         for (int i : R) info->sketch_cols += width[i];
         info->exact_sectors = int(E.size());
+        info->refinements = refinements;
+        info->max_residual = max_res;
       }
       return res;
     }

@@ -100,7 +100,38 @@ __global__ void transpose_copy_kernel(const xgb_copy2d_desc* __restrict__ descs,
   }
 }
 
+// res[out_off + j] = || R[:, j] - s_j U[:, j] ||_2 for the k columns of one
+// sector (R = A V, one warp per column); descriptor fields reused from
+// SignFixDesc: m rows, k columns, u_off (U and R share offsets), v_off = s_off,
+// n = out_off.
+__global__ void residual_norms_kernel(const SignFixDesc* __restrict__ descs, const double* __restrict__ R,
+                                      const double* __restrict__ U, const double* __restrict__ S,
+                                      double* __restrict__ res) {
+  const SignFixDesc d = descs[blockIdx.y];
+  const int lane = threadIdx.x & 31;
+  const int64_t j = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (j >= d.k) return;
+  const double sj = S[d.v_off + j];
+  const double* r = R + d.u_off + j * d.m;
+  const double* u = U + d.u_off + j * d.m;
+  double acc = 0;
+  for (int64_t i = lane; i < d.m; i += 32) {
+    const double x = r[i] - sj * u[i];
+    acc = fma(x, x, acc);
+  }
+  acc = warp_sum_d(acc);
+  if (lane == 0) res[d.n + j] = sqrt(acc);
+}
+
 }  // namespace
+
+void launch_residual_norms(const SignFixDesc* d_descs, int n, int64_t max_k, const double* R, const double* U,
+                           const double* S, double* res, cudaStream_t s) {
+  if (n <= 0 || max_k <= 0) return;
+  dim3 grid(unsigned((max_k + 7) / 8), unsigned(n));
+  residual_norms_kernel<<<grid, 256, 0, s>>>(d_descs, R, U, S, res);
+  count_launch();
+}
 
 void launch_transpose_copy(const xgb_copy2d_desc* d_descs, int n, int64_t max_elems, const double* src, double* dst,
                            cudaStream_t s) {

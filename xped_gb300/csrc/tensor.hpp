@@ -126,12 +126,17 @@ struct RsvdInfo {
   std::vector<int> saturated;  // sector indices, once per redo
   int64_t sketch_cols = 0;     // sum of widths over sketched sectors
   int exact_sectors = 0;
+  int refinements = 0;         // refinement passes (more subspace iterations) taken
+  double max_residual = 0;     // max over kept sketched triplets of ||A v - s u|| / s_max
 };
 // `warm` (optional): a V^dag from an earlier decomposition of a matrix with the
 // same column bases; its rows of charge q become the first sketch columns of
 // sector q (the remaining columns stay Gaussian).
+// `res_tol` > 0: sectors whose kept triplets have ||A v_j - s_j u_j|| > res_tol * s_max
+// get power_iters more subspace iterations from their current basis (up to three times).
 SVDResult tsvd_randomized(const Tensor& t, int64_t max_keep, double eps_svd, const std::vector<int64_t>& sketch,
-                          int power_iters, uint64_t seed, RsvdInfo* info = nullptr, const Tensor* warm = nullptr);
+                          int power_iters, uint64_t seed, RsvdInfo* info = nullptr, const Tensor* warm = nullptr,
+                          double res_tol = 0.0);
 std::pair<Tensor, Tensor> tqr(const Tensor& t);
 std::pair<Tensor, Tensor> decompose(const Tensor& t1, const Tensor& t2, int64_t max_nsv);
 
@@ -185,6 +190,8 @@ struct DecompRecord {
 
 struct CTMStats {
   int64_t decompositions = 0, sketched_sectors = 0, exact_sectors = 0, redo = 0, sketch_cols = 0;
+  int64_t refinements = 0;  // residual-driven refinement passes
+  double max_residual = 0;  // largest ||A v - s u|| / s_max of a kept sketched triplet (last decomposition)
 };
 
 // CTMRG environment on a 1x1 unit cell (src/PEPS/CTM.cpp).
@@ -212,6 +219,9 @@ class CTM {
   // subspace iterations when the direction's previous V^dag (same matrix
   // structure) seeds the sketch; < 0 disables the warm start
   int warm_iters = -1;
+  // > 0: kept sketched triplets must satisfy ||A v - s u|| <= res_tol * s_max
+  // (unconverged sectors get more subspace iterations)
+  double res_tol = 0.0;
   uint64_t seed = 1;
   std::shared_ptr<WidthPolicy> policy;
   bool record = false;

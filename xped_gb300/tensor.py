@@ -234,7 +234,7 @@ class Tensor:
         return Tensor(U.value), Tensor(S.value), Tensor(V.value), tw.value, ent.value, list(keep[:n])
 
     def tSVD_randomized(self, max_keep: int, eps_svd: float, sketch: Sequence[int], power_iters: int = 1,
-                        seed: int = 0, warm: "Tensor" = None):
+                        seed: int = 0, warm: "Tensor" = None, res_tol: float = 0.0):
         """Randomized blockwise tSVD: ``sketch[i]`` Gaussian columns for sector i
         (<= 0: exact).  Returns (U, S, V, truncWeight, entropy, keep, width,
         n_saturated)."""
@@ -248,7 +248,8 @@ class Tensor:
         nsat = C.c_int32()
         sk = (C.c_int64 * max(n, 1))(*[int(x) for x in sketch])
         check(lib().xgb_tensor_tsvd_randomized(self._h, int(max_keep), float(eps_svd), n, sk, int(power_iters),
-                                               int(seed), warm._h if warm is not None else None, C.byref(U),
+                                               int(seed), warm._h if warm is not None else None, float(res_tol),
+                                               C.byref(U),
                                                C.byref(S), C.byref(V), C.byref(tw),
                                                C.byref(ent), keep, width, C.byref(nsat)), "tSVD_randomized")
         return (Tensor(U.value), Tensor(S.value), Tensor(V.value), tw.value, ent.value, list(keep[:n]),
@@ -354,6 +355,16 @@ class CTM:
         run warm_iters subspace iterations (negative: off)."""
         check(lib().xgb_ctm_set_warm_start(self._h, int(warm_iters)), "ctm_set_warm_start")
         return self
+
+    def set_residual_tol(self, tol: float):
+        """Kept randomized triplets must satisfy ||A v - s u|| <= tol * s_max (0: off)."""
+        check(lib().xgb_ctm_set_residual_tol(self._h, float(tol)), "ctm_set_residual_tol")
+        return self
+
+    def residual_stats(self):
+        n, r = C.c_int64(), C.c_double()
+        check(lib().xgb_ctm_residual_stats(self._h, C.byref(n), C.byref(r)), "ctm_residual_stats")
+        return {"refinements": n.value, "max_residual": r.value}
 
     def set_gemm(self, precision: str = "fp64"):
         """Block GEMMs of the corner contractions / renormalisation: "fp64" or
