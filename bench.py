@@ -301,6 +301,57 @@ def run_gpu(args):
     return res
 
 
+# ----------------------------------------------------------------------------- fermionic Z2 workload
+FZ2_AUX = [(0, 3), (1, 3)]   # D = 6
+FZ2_PHYS = [(0, 1), (1, 1)]  # spinless fermion: empty / occupied
+FZ2_CHI = 144
+FZ2_ITERS = 20
+
+
+def run_fz2(args):
+    """Fermionic Z2 iPEPS (ZN<FChargeU1,2>), D=6 with q in {0,1} and degeneracies [3,3], physical
+    parity 0/1, chi=144: FZ2_ITERS CTMRG iterations of the chosen form from FROM_A, every step
+    timed with CUDA events; the density-density bond expectation after the last step.  With
+    --fz2-plain the exact FP64 form runs the same iterations for the comparison."""
+    from xped_gb300 import CTM, Basis, Tensor, ensure_device, lib
+    from xped_gb300.observables import density_bond, energy
+
+    _, _, local = dist_info()
+    ensure_device(local)
+    L = lib()
+    aux = Basis.from_pairs("fZ2", FZ2_AUX)
+    phys = Basis.from_pairs("fZ2", FZ2_PHYS)
+    A = Tensor.zeros([aux, aux], [aux, aux, phys])
+    A.set_data(np.random.default_rng(SEED).standard_normal(A.size))
+    H = density_bond(phys)
+    out = {}
+    for form in (("chosen", "plain") if args.fz2_plain else ("chosen",)):
+        c = CTM(A, FZ2_CHI).init()
+        if form == "chosen":
+            c.set_svd("randomized", power_iters=POWER_ITERS, seed=SEED, oversample=16, growth=0.5)
+            c.set_gemm(args.gemm)
+        ms = []
+        for _ in range(FZ2_ITERS):
+            L.xgb_synchronize()
+            L.xgb_event_record(12)
+            c.grow_all()
+            L.xgb_event_record(13)
+            ms.append(L.xgb_event_elapsed_ms(12, 13))
+        out[form] = {"ms_per_step_each": [round(x, 2) for x in ms], "total_s": sum(ms) / 1e3,
+                     "ms_per_step_after_3": float(np.mean(ms[3:])), "nn_bond": energy(c, H), "stats": c.stats()}
+    line = {"metric": f"CTMRG iterations, fermionic Z2 iPEPS D=6 chi={FZ2_CHI}, chosen form",
+            "value": 1e3 / out["chosen"]["ms_per_step_after_3"], "unit": "steps/s", "n_gpus": 1,
+            "steps": FZ2_ITERS, "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded N(0,1))",
+            "config": {"workload": f"fz2_ipeps_D6_chi{FZ2_CHI}_{FZ2_ITERS}_iterations", "aux": "q 0,1 deg [3,3]",
+                       "phys": "q 0,1", "gemm": args.gemm, "graph_capture": "none (host-side truncation between "
+                       "launches; see the design notes)"},
+            "forms": out}
+    if "plain" in out:
+        line["chosen_vs_plain"] = out["plain"]["total_s"] / out["chosen"]["total_s"]
+        line["nn_bond_abs_diff"] = abs(out["plain"]["nn_bond"] - out["chosen"]["nn_bond"])
+    print(json.dumps(line))
+
+
 # ----------------------------------------------------------------------------- block-GEMM sweep
 def gemm_sweep(reps=5):
     """Grouped block GEMMs FP64 vs 3xTF32: (i) the sector GEMMs of an SU(2)
@@ -484,6 +535,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-width run")
+    ap.add_argument("--workload", default="u1", choices=["u1", "fz2"],
+                    help="u1: the headline U(1) D=6 chi=128 step; fz2: fermionic Z2 D=6 chi=144, 20 iterations")
+    ap.add_argument("--fz2-plain", action="store_true", help="also run the plain FP64 form on the fz2 workload")
     ap.add_argument("--gemm-sweep-only", action="store_true",
                     help="run only the block-GEMM sweep and print it (for kernel profiling)")
     args = ap.parse_args()
@@ -512,6 +566,11 @@ def main():
                                            "warm-up steps; step time counted as four moves"},
                 "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
+        return
+
+    if args.workload == "fz2" and args.impl == "ours":
+        if rank == 0:
+            run_fz2(args)
         return
 
     if args.gemm_sweep_only:

@@ -64,6 +64,11 @@ xgb_tensor xgb_tensor_permute(xgb_tensor t, int shift, const int32_t* p, int n);
 /* Tensor::permute_adj<shift, p...> (Tensor.cpp:258-333): the transpose of permute<shift, p> on
    a tensor shaped like its output - the reverse rule of permute (ADTensor.hpp:172-184) */
 xgb_tensor xgb_tensor_permute_adj(xgb_tensor t, int shift, const int32_t* p, int n);
+/* reverse rule of the per-sector SVD (full_svd_impl, ADTensor.hpp:257-301), real scalars:
+   dA from the untruncated factors U, S, Vdag of tSVD(A) and their cotangents dU, dS, dVdag
+   (same structures as the factors); sectors of A without singular values get zero */
+xgb_tensor xgb_tensor_svd_backward(xgb_tensor A, xgb_tensor U, xgb_tensor S, xgb_tensor Vdag, xgb_tensor dU,
+                                   xgb_tensor dS, xgb_tensor dVdag);
 /* reverse rule of operator* (ADTensor.hpp:741-752): left_adj = res_adj * right^dag,
    right_adj = left^dag * res_adj, each with exactly its operand's structure */
 int xgb_tensor_matmul_backward(xgb_tensor left, xgb_tensor right, xgb_tensor res_adj, xgb_tensor* left_adj,

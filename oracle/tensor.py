@@ -549,3 +549,23 @@ def decompose(T1: Tensor, T2: Tensor, max_nsv: int):
     P1 = (isqrtS * U.adjoint()) * T1
     P2 = (T2 * Vd.adjoint()) * isqrtS
     return P1, P2
+
+
+def svd_backward_block(U, s, Vd, dU, dS, dVd):
+    """Reverse rule of the per-sector SVD A = U diag(s) Vd, real case
+    (ADTensor.hpp:257-301): the cotangent of A from those of U, S (a k x k
+    matrix) and Vd.  F_ij = 1 / (s_j^2 - s_i^2), with d -> d / (d^2 + 1e-12)
+    for |d| < 1e-12 (vec_diff, PlainInterface_Eigen_impl.cpp:82-85)."""
+    s = np.asarray(s, dtype=float)
+    s2 = s * s
+    Finv = s2[None, :] - s2[:, None]
+    small = np.abs(Finv) < 1e-12
+    F = np.where(small, Finv / (Finv * Finv + 1e-12), 1.0 / np.where(small, 1.0, Finv))
+    S = np.diag(s)
+    sinv = np.diag(1.0 / s)
+    J = F * (U.T @ dU)
+    K = F * (Vd @ dVd.T)
+    dA = U @ (dS + (J + J.T) @ S + S @ (K + K.T)) @ Vd
+    dA += (np.eye(U.shape[0]) - U @ U.T) @ dU @ sinv @ Vd
+    dA += U @ sinv @ dVd @ (np.eye(Vd.shape[1]) - Vd.T @ Vd)
+    return dA

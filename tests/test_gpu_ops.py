@@ -209,3 +209,34 @@ def test_matmul_backward_matches_oracle(symname):
         for q in qs:
             want = ref.block(q) if ref.has(q) else np.zeros((rows[qs.index(q)], cols[qs.index(q)]))
             assert np.allclose(got[q], want, rtol=0, atol=1e-12 * max(1.0, np.abs(want).max()))
+
+
+@pytest.mark.parametrize("symname", ["u1", "fz2", "su2"])
+def test_svd_backward_matches_oracle(symname):
+    """Reverse rule of the per-sector SVD (ADTensor.hpp:257-301) on the
+    untruncated device tSVD factors, against the numpy restatement."""
+    from oracle.convert import tensor_from_native
+    from oracle.tensor import svd_backward_block
+    from xped_gb300 import Tensor
+    rng = np.random.default_rng(12)
+    pairs = {"u1": [(-1, 2), (0, 3), (1, 2)], "fz2": [(0, 2), (1, 3)], "su2": [(1, 2), (2, 1), (3, 1)]}[symname]
+    s, oB, nB = pair_basis(symname, pairs)
+    oA = oracle.Tensor(s, [oB, oB], [oB]).set_random(rng)
+    nA = to_native(oA, [nB, nB], [nB])
+    U, S, V, *_ = nA.tSVD(10 ** 6, 0.0)
+
+    def rand_like(t):
+        r, c = t.rank
+        z = Tensor.zeros([t.leg(i) for i in range(r)], [t.leg(i) for i in range(r, r + c)])
+        z.set_data(rng.standard_normal(z.size))
+        return z
+
+    dU, dS, dV = rand_like(U), rand_like(S), rand_like(V)
+    dA = nA.svd_backward(U, S, V, dU, dS, dV)
+    oU, oS, oV = (tensor_from_native(s, t) for t in (U, S, V))
+    odU, odS, odV = (tensor_from_native(s, t) for t in (dU, dS, dV))
+    got = dA.blocks()
+    for q in oA.sectors:
+        ref = svd_backward_block(oU.block(q), np.diag(oS.block(q)), oV.block(q), odU.block(q), odS.block(q),
+                                 odV.block(q))
+        assert np.allclose(got[q], ref, rtol=0, atol=1e-10 * max(1.0, np.abs(ref).max())), q

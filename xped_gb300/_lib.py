@@ -98,6 +98,7 @@ PROTOS = [
     ("xgb_tensor_permute", P, [P, C.c_int, i32p, C.c_int]),
     ("xgb_tensor_permute_adj", P, [P, C.c_int, i32p, C.c_int]),
     ("xgb_tensor_matmul_backward", C.c_int, [P, P, P, C.POINTER(P), C.POINTER(P)]),
+    ("xgb_tensor_svd_backward", P, [P, P, P, P, P, P, P]),
     ("xgb_tensor_twist", P, [P, C.c_int]),
     ("xgb_tensor_adjoint", P, [P]),
     ("xgb_tensor_matmul", P, [P, P, C.c_int, C.c_int]),

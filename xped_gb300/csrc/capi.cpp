@@ -176,6 +176,10 @@ xgb_tensor xgb_tensor_permute(xgb_tensor t, int shift, const int32_t* p, int n) 
 xgb_tensor xgb_tensor_permute_adj(xgb_tensor t, int shift, const int32_t* p, int n) {
   GUARD(nullptr, { return wrap(permute_adj(t->t, shift, std::vector<int>(p, p + n))); })
 }
+xgb_tensor xgb_tensor_svd_backward(xgb_tensor A, xgb_tensor U, xgb_tensor S, xgb_tensor Vdag, xgb_tensor dU,
+                                   xgb_tensor dS, xgb_tensor dVdag) {
+  GUARD(nullptr, { return wrap(tsvd_backward(A->t, U->t, S->t, Vdag->t, dU->t, dS->t, dVdag->t)); })
+}
 int xgb_tensor_matmul_backward(xgb_tensor left, xgb_tensor right, xgb_tensor res_adj, xgb_tensor* left_adj,
                                xgb_tensor* right_adj) {
   GUARD(XGB_E_BADPLAN, {

@@ -73,6 +73,14 @@ struct SignFixDesc { int64_t m, n, k, u_off, v_off; };      // U m x k (ld m), V
 void launch_gauss_fill(const GaussBlock* d_blocks, int n_blocks, int64_t max_count, uint64_t seed, double* out,
                        cudaStream_t s);
 void launch_sign_fix(const SignFixDesc* d_descs, int n, int64_t max_k, double* U, double* Vt, cudaStream_t s);
+// SVD reverse rule helpers (rsvd.cu): per sector m x n block with k singular values;
+// offsets of U / dU (m x k), the k x k diagonal S block, dS (k x k, ld ds_ld), V^dag / dV^dag (k x n),
+// k x k work, W (k x n), P (m x k)
+struct SvdBwdDesc { int64_t m, n, k, u_off, s_off, ds_off, ds_ld, v_off, kk_off, w_off, p_off; };
+void launch_svd_bwd_mid(const SvdBwdDesc* d_descs, int n, int64_t max_kk, const double* S, const double* X,
+                        const double* Y, const double* dS, double* N, double* XS, cudaStream_t s);
+void launch_svd_bwd_scale(const SvdBwdDesc* d_descs, int n, int64_t max_elems, const double* S, const double* dVd,
+                          const double* dU, double* W, double* P, cudaStream_t s);
 // per-column residuals ||R[:, j] - S[j] U[:, j]|| (desc: m, n = output offset, k columns, u_off of R and U,
 // v_off = offset of S)
 void launch_residual_norms(const SignFixDesc* d_descs, int n, int64_t max_k, const double* R, const double* U,

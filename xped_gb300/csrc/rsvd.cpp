@@ -50,7 +50,8 @@ class Staging {
 
 double* alloc_d(int64_t n) { return static_cast<double*>(dev_alloc(sizeof(double) * size_t(std::max<int64_t>(n, 1)))); }
 
-void grouped_gemm(const std::vector<xgb_gemm_desc>& d, const double* A, const double* B, double* C, cudaStream_t s) {
+void grouped_gemm(const std::vector<xgb_gemm_desc>& d, const double* A, const double* B, double* C, cudaStream_t s,
+                  double alpha = 1.0, double beta = 0.0) {
   if (d.empty()) return;
   const int tile = choose_gemm_tile(d.data(), int(d.size()));
   std::vector<GemmTile> tiles;
@@ -65,7 +66,7 @@ void grouped_gemm(const std::vector<xgb_gemm_desc>& d, const double* A, const do
   const size_t od = st.add(d), ot = st.add(tiles);
   st.upload(s);
   prof_begin(K_GEMM, s);
-  launch_gemm_f64(st.at<xgb_gemm_desc>(od), st.at<GemmTile>(ot), int(tiles.size()), tile, A, B, C, 1.0, 0.0, s);
+  launch_gemm_f64(st.at<xgb_gemm_desc>(od), st.at<GemmTile>(ot), int(tiles.size()), tile, A, B, C, alpha, beta, s);
   prof_end(K_GEMM, s, flops);
 }
 
@@ -412,6 +413,71 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       saturated.push_back(i);
     }
   }
+}
+
+Tensor tsvd_backward(const Tensor& A0, const Tensor& U0, const Tensor& S0, const Tensor& Vd0, const Tensor& dU0,
+                     const Tensor& dS0, const Tensor& dVd0) {
+  // reverse rule of full_svd_impl (ADTensor.hpp:257-301), real scalars, per sector:
+  //   dA = U [dS + (J + J^T) S + S (K + K^T)] V^dag + (1 - U U^T) dU S^-1 V^dag + U S^-1 dV^dag (1 - V V^dag)
+  //   J = F.(U^T dU), K = F.(V^dag dV^dag^T), F_ij = 1 / (s_j^2 - s_i^2)
+  // evaluated as dA = U [N V^dag + S^-1 dV^dag] + (dU S^-1 - U X S^-1) V^dag with X = U^T dU,
+  // Y = V^dag dV^dag^T and N = dS + (J + J^T) S + S (K + K^T) - S^-1 Y.
+  Tensor A = materialize(A0), U = materialize(U0), S = materialize(S0), Vd = materialize(Vd0);
+  Tensor dU = materialize(dU0), dS = materialize(dS0), dVd = materialize(dVd0);
+  const TensorMeta &ma = *A.meta, &mu = *U.meta, &ms = *S.meta, &mv = *Vd.meta;
+  if (dU.meta->id != mu.id || dS.meta->id != ms.id || dVd.meta->id != mv.id)
+    throw std::runtime_error("svd backward: cotangents must have the structures of U, S, V^dag");
+  cudaStream_t st = stream();
+  std::vector<SvdBwdDesc> bd;
+  std::vector<xgb_gemm_desc> gX, gY, gW, gP, gA1, gA2;
+  std::vector<int64_t> a_off;
+  int64_t kkt = 0, wt = 0, pt = 0, mxkk = 0, mxsc = 0;
+  for (size_t iu = 0; iu < mu.sectors.size(); ++iu) {
+    const int q = mu.sectors[iu];
+    const int ia = ma.index(q), is = ms.index(q), iv = mv.index(q);
+    if (ia < 0 || is < 0 || iv < 0) throw std::runtime_error("svd backward: sector missing in A, S or V^dag");
+    const int64_t m = ma.rows[ia], n = ma.cols[ia], k = mu.cols[iu];
+    if (mu.rows[iu] != m || mv.cols[iv] != n || mv.rows[iv] != k || ms.rows[is] != k || ms.cols[is] != k)
+      throw std::runtime_error("svd backward: block shapes of A, U, S, V^dag disagree");
+    SvdBwdDesc d{m, n, k, mu.offset[iu], ms.offset[is], ms.offset[is], k, mv.offset[iv], kkt, wt, pt};
+    bd.push_back(d);
+    gX.push_back({k, k, m, d.u_off, m, d.u_off, m, kkt, k, 1, 0});            // X = U^T dU
+    gY.push_back({k, k, n, d.v_off, k, d.v_off, k, kkt, k, 0, 1});            // Y = V^dag dV^dag^T
+    gW.push_back({k, n, k, kkt, k, d.v_off, k, wt, k, 0, 0});                 // W = N V^dag
+    gP.push_back({m, k, k, d.u_off, m, kkt, k, pt, m, 0, 0});                 // P -= U XS
+    gA1.push_back({m, n, k, d.u_off, m, wt, k, ma.offset[ia], m, 0, 0});      // dA = U W
+    gA2.push_back({m, n, k, pt, m, d.v_off, k, ma.offset[ia], m, 0, 0});      // dA += P V^dag
+    kkt += k * k;
+    wt += k * n;
+    pt += m * k;
+    mxkk = std::max(mxkk, k * k);
+    mxsc = std::max(mxsc, k * n + m * k);
+  }
+  Tensor dA = zeros(A.meta);
+  if (bd.empty()) return dA;
+  double* X = alloc_d(kkt);
+  double* Y = alloc_d(kkt);
+  double* N = alloc_d(kkt);
+  double* XS = alloc_d(kkt);
+  double* W = alloc_d(wt);
+  double* P = alloc_d(pt);
+  grouped_gemm(gX, U.data(), dU.data(), X, st);
+  grouped_gemm(gY, Vd.data(), dVd.data(), Y, st);
+  Staging sb;
+  const size_t o = sb.add(bd);
+  sb.upload(st);
+  prof_begin(K_DIAG, st);
+  launch_svd_bwd_mid(sb.at<SvdBwdDesc>(o), int(bd.size()), mxkk, S.data(), X, Y, dS.data(), N, XS, st);
+  prof_end(K_DIAG, st, 48.0 * double(kkt));
+  grouped_gemm(gW, N, Vd.data(), W, st);
+  prof_begin(K_DIAG, st);
+  launch_svd_bwd_scale(sb.at<SvdBwdDesc>(o), int(bd.size()), mxsc, S.data(), dVd.data(), dU.data(), W, P, st);
+  prof_end(K_DIAG, st, 24.0 * double(wt + pt));
+  grouped_gemm(gP, U.data(), XS, P, st, -1.0, 1.0);
+  grouped_gemm(gA1, U.data(), W, dA.data(), st);
+  grouped_gemm(gA2, P, Vd.data(), dA.data(), st, 1.0, 1.0);
+  for (double* p : {X, Y, N, XS, W, P}) dev_free(p);
+  return dA;
 }
 
 }  // namespace xgb

@@ -123,7 +123,70 @@ __global__ void residual_norms_kernel(const SignFixDesc* __restrict__ descs, con
   if (lane == 0) res[d.n + j] = sqrt(acc);
 }
 
+// Middle factor of the SVD reverse rule for one k x k sector (column-major;
+// S is the k x k diagonal block, s_i = S[i + i k]):
+//   N  = dS + (F.X + (F.X)^T) S + S (F.Y + (F.Y)^T) - S^-1 Y
+//   XS = X S^-1
+// with F_ij = 1 / (s_j^2 - s_i^2) (d -> d / (d^2 + 1e-12) for |d| < 1e-12).
+__global__ void svd_bwd_mid_kernel(const SvdBwdDesc* __restrict__ descs, const double* __restrict__ S,
+                                   const double* __restrict__ X, const double* __restrict__ Y,
+                                   const double* __restrict__ dS, double* __restrict__ N, double* __restrict__ XS) {
+  const SvdBwdDesc d = descs[blockIdx.y];
+  const int64_t k = d.k, kk = k * k;
+  auto F = [&](int64_t i, int64_t j) {
+    const double si = S[d.s_off + i * (k + 1)], sj = S[d.s_off + j * (k + 1)];
+    const double dd = sj * sj - si * si;
+    return fabs(dd) < 1e-12 ? dd / (dd * dd + 1e-12) : 1.0 / dd;
+  };
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < kk; e += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t i = e % k, j = e / k;
+    const double si = S[d.s_off + i * (k + 1)], sj = S[d.s_off + j * (k + 1)];
+    const double xij = X[d.kk_off + i + j * k], xji = X[d.kk_off + j + i * k];
+    const double yij = Y[d.kk_off + i + j * k], yji = Y[d.kk_off + j + i * k];
+    const double fij = F(i, j), fji = F(j, i);
+    const double jsym = fij * xij + fji * xji;  // (F.X + (F.X)^T)_ij
+    const double ksym = fij * yij + fji * yji;
+    N[d.kk_off + e] = dS[d.ds_off + i + j * d.ds_ld] + jsym * sj + si * ksym - yij / si;
+    XS[d.kk_off + e] = xij / sj;
+  }
+}
+
+// W (k x n) += S^-1 dVd  (rows scaled) and P (m x k) = dU S^-1 (columns scaled), one sector per grid row
+__global__ void svd_bwd_scale_kernel(const SvdBwdDesc* __restrict__ descs, const double* __restrict__ S,
+                                     const double* __restrict__ dVd, const double* __restrict__ dU,
+                                     double* __restrict__ W, double* __restrict__ P) {
+  const SvdBwdDesc d = descs[blockIdx.y];
+  const int64_t kn = d.k * d.n, mk = d.m * d.k;
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < kn + mk; e += int64_t(gridDim.x) * blockDim.x) {
+    if (e < kn) {
+      const int64_t i = e % d.k;
+      W[d.w_off + e] += dVd[d.v_off + e] / S[d.s_off + i * (d.k + 1)];
+    } else {
+      const int64_t f = e - kn, j = f / d.m;
+      P[d.p_off + f] = dU[d.u_off + f] / S[d.s_off + j * (d.k + 1)];
+    }
+  }
+}
+
 }  // namespace
+
+void launch_svd_bwd_mid(const SvdBwdDesc* d_descs, int n, int64_t max_kk, const double* S, const double* X,
+                        const double* Y, const double* dS, double* N, double* XS, cudaStream_t s) {
+  if (n <= 0 || max_kk <= 0) return;
+  const int64_t want = (max_kk + 255) / 256;
+  dim3 grid(unsigned(want < 1024 ? want : 1024), unsigned(n));
+  svd_bwd_mid_kernel<<<grid, 256, 0, s>>>(d_descs, S, X, Y, dS, N, XS);
+  count_launch();
+}
+
+void launch_svd_bwd_scale(const SvdBwdDesc* d_descs, int n, int64_t max_elems, const double* S, const double* dVd,
+                          const double* dU, double* W, double* P, cudaStream_t s) {
+  if (n <= 0 || max_elems <= 0) return;
+  const int64_t want = (max_elems + 255) / 256;
+  dim3 grid(unsigned(want < 1024 ? want : 1024), unsigned(n));
+  svd_bwd_scale_kernel<<<grid, 256, 0, s>>>(d_descs, S, dVd, dU, W, P);
+  count_launch();
+}
 
 void launch_residual_norms(const SignFixDesc* d_descs, int n, int64_t max_k, const double* R, const double* U,
                            const double* S, double* res, cudaStream_t s) {

@@ -73,6 +73,11 @@ Tensor permute(const Tensor& t, int shift, const std::vector<int>& p);
 // reverse rule of operator* (ADTensor.hpp:741-752): the cotangents of left and
 // right (with exactly their structures) from the cotangent of left * right
 std::pair<Tensor, Tensor> matmul_backward(const Tensor& left, const Tensor& right, const Tensor& res_adj);
+// reverse rule of the per-sector SVD (full_svd_impl, ADTensor.hpp:257-301), real
+// scalars: the cotangent of A from the factors U, S, V^dag of its (untruncated) tSVD
+// and their cotangents (same structures as the factors)
+Tensor tsvd_backward(const Tensor& A, const Tensor& U, const Tensor& S, const Tensor& Vdag, const Tensor& dU,
+                     const Tensor& dS, const Tensor& dVdag);
 // blocks of src placed in a zero tensor of the target structure (matching charges)
 Tensor embed(const Tensor& src, const MetaPtr& target);
 // Tensor::permute_adj<shift, p...>: transpose of permute<shift, p> applied to a

@@ -197,6 +197,11 @@ class Tensor:
               "matmul_backward")
         return Tensor(la.value), Tensor(ra.value)
 
+    def svd_backward(self, U: "Tensor", S: "Tensor", Vdag: "Tensor", dU: "Tensor", dS: "Tensor",
+                     dVdag: "Tensor") -> "Tensor":
+        """Reverse rule of the per-sector SVD of self (untruncated factors)."""
+        return Tensor(lib().xgb_tensor_svd_backward(self._h, U._h, S._h, Vdag._h, dU._h, dS._h, dVdag._h))
+
     def twist(self, leg: int) -> "Tensor":
         return Tensor(lib().xgb_tensor_twist(self._h, int(leg)))
 
