@@ -311,8 +311,9 @@ FZ2_ITERS = 20
 def run_fz2(args):
     """Fermionic Z2 iPEPS (ZN<FChargeU1,2>), D=6 with q in {0,1} and degeneracies [3,3], physical
     parity 0/1, chi=144: FZ2_ITERS CTMRG iterations of the chosen form from FROM_A, every step
-    timed with CUDA events; the density-density bond expectation after the last step.  With
-    --fz2-plain the exact FP64 form runs the same iterations for the comparison."""
+    timed with CUDA events; the density-density bond expectation after --fz2-plain-steps steps and
+    after the last one.  The plain FP64 form runs --fz2-plain-steps steps from the same start
+    (its exact SVDs of ~2600-wide sector blocks take minutes per step)."""
     from xped_gb300 import CTM, Basis, Tensor, ensure_device, lib
     from xped_gb300.observables import density_bond, energy
 
@@ -324,31 +325,39 @@ def run_fz2(args):
     A = Tensor.zeros([aux, aux], [aux, aux, phys])
     A.set_data(np.random.default_rng(SEED).standard_normal(A.size))
     H = density_bond(phys)
+    npl = args.fz2_plain_steps
     out = {}
-    for form in (("chosen", "plain") if args.fz2_plain else ("chosen",)):
+    for form, iters in (("chosen", FZ2_ITERS), ("plain", npl)):
+        if iters <= 0:
+            continue
         c = CTM(A, FZ2_CHI).init()
         if form == "chosen":
             c.set_svd("randomized", power_iters=POWER_ITERS, seed=SEED, oversample=16, growth=0.5)
             c.set_gemm(args.gemm)
-        ms = []
-        for _ in range(FZ2_ITERS):
+        ms, marks = [], {}
+        for i in range(iters):
             L.xgb_synchronize()
             L.xgb_event_record(12)
             c.grow_all()
             L.xgb_event_record(13)
             ms.append(L.xgb_event_elapsed_ms(12, 13))
-        out[form] = {"ms_per_step_each": [round(x, 2) for x in ms], "total_s": sum(ms) / 1e3,
-                     "ms_per_step_after_3": float(np.mean(ms[3:])), "nn_bond": energy(c, H), "stats": c.stats()}
+            if i + 1 == npl:
+                marks["nn_bond_at_plain_steps"] = energy(c, H)
+        out[form] = dict(marks, ms_per_step_each=[round(x, 2) for x in ms], total_s=sum(ms) / 1e3,
+                         ms_per_step_after_1=float(np.mean(ms[1:])) if len(ms) > 1 else None,
+                         nn_bond_last=energy(c, H), stats=c.stats())
+    ch = out["chosen"]
     line = {"metric": f"CTMRG iterations, fermionic Z2 iPEPS D=6 chi={FZ2_CHI}, chosen form",
-            "value": 1e3 / out["chosen"]["ms_per_step_after_3"], "unit": "steps/s", "n_gpus": 1,
+            "value": 1e3 / float(np.mean(ch["ms_per_step_each"][3:])), "unit": "steps/s", "n_gpus": 1,
             "steps": FZ2_ITERS, "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded N(0,1))",
             "config": {"workload": f"fz2_ipeps_D6_chi{FZ2_CHI}_{FZ2_ITERS}_iterations", "aux": "q 0,1 deg [3,3]",
-                       "phys": "q 0,1", "gemm": args.gemm, "graph_capture": "none (host-side truncation between "
-                       "launches; see the design notes)"},
+                       "phys": "q 0,1", "gemm": args.gemm,
+                       "graph_capture": "none: every move synchronises on the host for the truncation result"},
             "forms": out}
-    if "plain" in out:
-        line["chosen_vs_plain"] = out["plain"]["total_s"] / out["chosen"]["total_s"]
-        line["nn_bond_abs_diff"] = abs(out["plain"]["nn_bond"] - out["chosen"]["nn_bond"])
+    if "plain" in out and out["plain"]["ms_per_step_after_1"]:
+        line["chosen_vs_plain_per_step"] = out["plain"]["ms_per_step_after_1"] / ch["ms_per_step_after_1"]
+        line["nn_bond_abs_diff_after_plain_steps"] = abs(out["plain"]["nn_bond_at_plain_steps"] -
+                                                         ch["nn_bond_at_plain_steps"])
     print(json.dumps(line))
 
 
@@ -460,11 +469,11 @@ def roofline(prof, steps):
     per_launch_work = work / n
     if dom in ("gemm_f64", "svd_jacobi", "qr"):
         # FP64 runs on the DFMA pipe; GB300's nominal dense FP64 rate is 1.25 TFLOP/s.
-        # SVD work is counted as LAPACK dgesvd-equivalent flops (4m^2n + 8mn^2 + 9n^3, m >= n).
+        # SVD work is counted as the thin R-SVD flop count 6mn^2 + 20n^3 (m >= n, Golub & Van Loan).
         achieved = per_launch_work / (per_launch_ms * 1e-3) / 1e12
         out = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
                "peak_source": "nominal GB300 FP64 rate (MEASURED_PEAKS.json has no FP64 figure)",
-               "work": "LAPACK-equivalent flops" if dom == "svd_jacobi" else "useful flops"}
+               "work": "thin R-SVD flops 6mn^2+20n^3" if dom == "svd_jacobi" else "useful flops"}
     elif dom == "gemm_tc":
         tf = peaks.get("bf16_tflops", 1900.0) / 2.0  # dense TF32 issues at half the BF16 rate
         achieved = per_launch_work / (per_launch_ms * 1e-3) / 1e12
@@ -476,7 +485,14 @@ def roofline(prof, steps):
         out = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s"}
     out["frac"] = out["achieved"] / out["peak"]
-    out["traffic"] = None
+    # DRAM bytes per launch of the dominant kernel from one ncu capture (profiles/): the chosen
+    # step's orthonormalisation launches are L2-resident
+    traffic = {"svd_jacobi": (1.884e6, "ncu capture of one orthonormalisation launch, U(1) D=6 chi=128 "
+                                       "(dram__bytes_read.sum 1.864 MB + write 0.021 MB)"),
+               "gemm_tc": (7.025e9, "ncu capture, SU(2) Tensor<2,2> product (6.613 GB read + 0.412 GB written)")}
+    out["traffic"] = traffic[dom][0] if dom in traffic else None
+    if dom in traffic:
+        out["traffic_source"] = traffic[dom][1]
     out["launches_per_step"] = n / max(steps, 1)
     out["ms_per_launch"] = per_launch_ms
     out["kernel_share"] = {k: round(v[1] / sum(x[1] for x in kinds.values()), 4) for k, v in kinds.items()}
@@ -537,7 +553,8 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-width run")
     ap.add_argument("--workload", default="u1", choices=["u1", "fz2"],
                     help="u1: the headline U(1) D=6 chi=128 step; fz2: fermionic Z2 D=6 chi=144, 20 iterations")
-    ap.add_argument("--fz2-plain", action="store_true", help="also run the plain FP64 form on the fz2 workload")
+    ap.add_argument("--fz2-plain-steps", type=int, default=2,
+                    help="steps of the plain FP64 form on the fz2 workload (0: skip)")
     ap.add_argument("--gemm-sweep-only", action="store_true",
                     help="run only the block-GEMM sweep and print it (for kernel profiling)")
     args = ap.parse_args()

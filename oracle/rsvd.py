@@ -8,8 +8,7 @@ the device algorithm step by step so both can be compared on the same
 seeded test matrices:
 
   Omega_i = N(0,1) from (seed, stream i)          n_i x l_i
-  Q = orth(A Omega)                               left singular vectors (noise
-                                                  directions zeroed)
+  Q = orth(A Omega)                               shifted CholeskyQR3
   repeat p times: Q = orth(A orth(A^T Q))
   B = Q^T A = U_B S V^T ,  U = Q U_B ,  sign convention of fix_svd_signs
 
@@ -52,16 +51,28 @@ def gaussian(seed: int, stream: int, count: int) -> np.ndarray:
     return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
 
 
-NOISE = 64.0 * 2.0 ** -53
+def _chol_pass(Y, shift):
+    """One CholeskyQR pass: Y R^-1 with R^T R = Y^T Y + shift * (m l + l (l + 1)) tr(Y^T Y) I;
+    a non-positive pivot is replaced by the smallest normal double."""
+    m, l = Y.shape
+    G = Y.T @ Y
+    s = shift * (m * l + l * (l + 1)) * np.trace(G)
+    L = np.zeros((l, l))
+    for j in range(l):
+        d = G[j, j] + s - L[j, :j] @ L[j, :j]
+        L[j, j] = np.sqrt(d) if d > 0 else np.sqrt(np.finfo(float).tiny)
+        L[j + 1:, j] = (G[j + 1:, j] - L[j + 1:, :j] @ L[j, :j]) / L[j, j]
+    return sla.solve_triangular(L, Y.T, lower=True).T  # Y L^-T
 
 
 def _orth(Y):
-    """Left singular vectors of Y; directions with singular value at
-    round-off level of the largest (<= NOISE * s_0) become zero columns."""
-    u, s, _ = np.linalg.svd(Y, full_matrices=False)
-    if s.size:
-        u[:, s <= NOISE * s[0]] = 0.0
-    return u
+    """Shifted CholeskyQR3 (Fukaya et al., SIAM J. Sci. Comput. 2020), as on
+    the device: one pass with shift 11 u, then two plain passes."""
+    if Y.size == 0:
+        return Y.copy()
+    Q = _chol_pass(Y, 11.0 * 2.0 ** -53)
+    Q = _chol_pass(Q, 0.0)
+    return _chol_pass(Q, 0.0)
 
 
 def sketch_svd(A, l, power_iters, seed, stream, warm_rows=None):

@@ -73,6 +73,10 @@ struct SignFixDesc { int64_t m, n, k, u_off, v_off; };      // U m x k (ld m), V
 void launch_gauss_fill(const GaussBlock* d_blocks, int n_blocks, int64_t max_count, uint64_t seed, double* out,
                        cudaStream_t s);
 void launch_sign_fix(const SignFixDesc* d_descs, int n, int64_t max_k, double* U, double* Vt, cudaStream_t s);
+// CholeskyQR helper (rsvd.cu): per sketch block m x l, Gram matrix l x l at g_off
+struct CholDesc { int64_t m, l, g_off; };
+void launch_chol_inv(const CholDesc* d_descs, int n, double* G, double* Rinv, double rel_shift, int* bad,
+                     cudaStream_t s);
 // SVD reverse rule helpers (rsvd.cu): per sector m x n block with k singular values;
 // offsets of U / dU (m x k), the k x k diagonal S block, dS (k x k, ld ds_ld), V^dag / dV^dag (k x n),
 // k x k work, W (k x n), P (m x k)
@@ -88,9 +92,6 @@ void launch_residual_norms(const SignFixDesc* d_descs, int n, int64_t max_k, con
 // transposed block copies: src block rows x cols (ld src_ld) -> dst cols x rows (ld dst_ld)
 void launch_transpose_copy(const xgb_copy2d_desc* d_descs, int n, int64_t max_elems, const double* src, double* dst,
                            cudaStream_t s);
-// Q columns j with S[v_off + j] <= rel * S[v_off] set to zero (descs: m, k, u_off of Q, v_off into S)
-void launch_zero_noise_columns(const SignFixDesc* d_descs, int n, int64_t max_k, const double* S, double rel, double* Q,
-                               cudaStream_t s);
 
 // rank-predictor MLP (mlp.cu): kMlpIn -> kMlpHidden x 3 (ReLU) -> kMlpOut, FP32,
 // parameters packed as W1, b1, W2, b2, W3, b3, W4, b4 with row-major W[out][in]

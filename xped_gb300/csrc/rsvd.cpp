@@ -2,10 +2,10 @@
 //
 // Every stage is one grouped launch over all sketched sectors: the Gaussian
 // test matrices, the sketch GEMMs (A Omega, A^T Q, Q^T A, Q U_B), the
-// orthonormalisations (thin SVD of the tall sketch, whose left factor is
-// orthonormal to FP64 round-off even when the sketch is rank deficient), the
-// small exact SVD of B = Q^T A together with the exactly decomposed sectors,
-// and the sign convention.  Truncation is the shared cutoff_matrices step
+// orthonormalisations (shifted CholeskyQR3: grouped Gram / triangular-solve
+// GEMMs and one small Cholesky launch per pass), the small exact SVD of
+// B = Q^T A together with the exactly decomposed sectors, and the sign
+// convention.  Truncation is the shared cutoff_matrices step
 // (src/Core/Tensor.cpp:523-633) on the resulting per-sector spectra.
 #include <cuda_runtime.h>
 
@@ -70,7 +70,8 @@ void grouped_gemm(const std::vector<xgb_gemm_desc>& d, const double* A, const do
   prof_end(K_GEMM, s, flops);
 }
 
-// Batched thin SVD through the cluster Jacobi kernel (work counted as LAPACK dgesvd flops).
+// Batched thin SVD through the cluster Jacobi kernel (work counted as the thin R-SVD flop count
+// 6 m n^2 + 20 n^3, m >= n, Golub & Van Loan, Matrix Computations, Table 5.5.1).
 void batched_svd(const std::vector<xgb_svd_desc>& d, const double* A, double* U, double* S, double* Vt, cudaStream_t s) {
   if (d.empty()) return;
   std::vector<int64_t> woff(d.size());
@@ -81,7 +82,7 @@ void batched_svd(const std::vector<xgb_svd_desc>& d, const double* A, double* U,
     wt += int64_t(svd_work_elems(d[i].m, d[i].n));
     const double mm = double(std::max(d[i].m, d[i].n)), nn = double(std::min(d[i].m, d[i].n));
     maxk = std::max(maxk, std::min(d[i].m, d[i].n));
-    flops += 4 * mm * mm * nn + 8 * mm * nn * nn + 9 * nn * nn * nn;
+    flops += 6 * mm * nn * nn + 20 * nn * nn * nn;  // thin R-SVD count (U m x n, S, V)
   }
   Staging st;
   const size_t od = st.add(d), ow = st.add(woff);
@@ -93,34 +94,55 @@ void batched_svd(const std::vector<xgb_svd_desc>& d, const double* A, double* U,
   dev_free(W);
 }
 
-// Orthonormal basis of each tall m x l block of Y (left singular vectors) into
-// Q; directions whose singular value is at round-off level of the largest
-// (<= kNoise * s_0) are set to zero columns instead.
-constexpr double kNoise = 64.0 * 1.1102230246251565e-16;
-
+// Orthonormal basis of each tall m x l block of Y into Q by shifted CholeskyQR3
+// (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa, SIAM J. Sci. Comput. 2020):
+// one shifted pass Q1 = Y chol(Y^T Y + s I)^-1, s = 11 (m l + l (l + 1)) u ||Y||_F^2,
+// then two plain CholeskyQR passes.  Every pass is two grouped FP64 GEMMs (Gram
+// matrix, Q R^-1) spread over all SMs plus one small Cholesky / triangular-inverse
+// launch (one CTA per block).  Y is used as scratch and holds garbage afterwards.
 void orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64_t>& cols, const std::vector<int64_t>& y_off,
-                    const double* Y, double* Q, cudaStream_t s) {
-  std::vector<xgb_svd_desc> d;
-  std::vector<SignFixDesc> z;
-  int64_t so = 0, vo = 0, mx = 0;
-  for (size_t i = 0; i < rows.size(); ++i) {
-    d.push_back({rows[i], cols[i], y_off[i], y_off[i], so, vo});
-    z.push_back({rows[i], 0, cols[i], y_off[i], so});
-    mx = std::max(mx, cols[i]);
-    so += cols[i];
-    vo += cols[i] * cols[i];
+                    double* Y, double* Q, cudaStream_t s) {
+  const size_t n = rows.size();
+  if (n == 0) return;
+  std::vector<CholDesc> cd;
+  std::vector<xgb_gemm_desc> gram_y, gram_q, mul_yq, mul_qy;
+  int64_t gt = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const int64_t m = rows[i], l = cols[i];
+    cd.push_back({m, l, gt});
+    gram_y.push_back({l, l, m, y_off[i], m, y_off[i], m, gt, l, 1, 0});  // G = Y^T Y
+    gram_q.push_back({l, l, m, y_off[i], m, y_off[i], m, gt, l, 1, 0});  // same layout for Q
+    mul_yq.push_back({m, l, l, y_off[i], m, gt, l, y_off[i], m, 0, 0});  // dst = src R^-1
+    mul_qy.push_back(mul_yq.back());
+    gt += l * l;
   }
-  double* Ss = alloc_d(so);
-  double* Vs = alloc_d(vo);
-  batched_svd(d, Y, Q, Ss, Vs, s);
-  Staging st;
-  const size_t o = st.add(z);
-  st.upload(s);
-  prof_begin(K_SKETCH, s);
-  launch_zero_noise_columns(st.at<SignFixDesc>(o), int(z.size()), mx, Ss, kNoise, Q, s);
-  prof_end(K_SKETCH, s, 8.0 * double(so));
-  dev_free(Ss);
-  dev_free(Vs);
+  double* G = alloc_d(gt);
+  double* Ri = alloc_d(gt);
+  int* bad = static_cast<int*>(dev_alloc(sizeof(int)));
+  ok(cudaMemsetAsync(bad, 0, sizeof(int), s), "memset");
+  Staging sc;
+  const size_t o = sc.add(cd);
+  sc.upload(s);
+  constexpr double kShift = 11.0 * 1.1102230246251565e-16;
+  // pass 1 (shifted): Y -> Q;  pass 2: Q -> Y;  pass 3: Y -> Q
+  grouped_gemm(gram_y, Y, Y, G, s);
+  prof_begin(K_QR, s);
+  launch_chol_inv(sc.at<CholDesc>(o), int(n), G, Ri, kShift, bad, s);
+  prof_end(K_QR, s, 0.0);
+  grouped_gemm(mul_yq, Y, Ri, Q, s);
+  grouped_gemm(gram_q, Q, Q, G, s);
+  prof_begin(K_QR, s);
+  launch_chol_inv(sc.at<CholDesc>(o), int(n), G, Ri, 0.0, bad, s);
+  prof_end(K_QR, s, 0.0);
+  grouped_gemm(mul_qy, Q, Ri, Y, s);
+  grouped_gemm(gram_y, Y, Y, G, s);
+  prof_begin(K_QR, s);
+  launch_chol_inv(sc.at<CholDesc>(o), int(n), G, Ri, 0.0, bad, s);
+  prof_end(K_QR, s, 0.0);
+  grouped_gemm(mul_yq, Y, Ri, Q, s);
+  dev_free(G);
+  dev_free(Ri);
+  dev_free(bad);
 }
 
 constexpr int kMaxRetries = 3;
@@ -421,7 +443,8 @@ Tensor tsvd_backward(const Tensor& A0, const Tensor& U0, const Tensor& S0, const
   //   dA = U [dS + (J + J^T) S + S (K + K^T)] V^dag + (1 - U U^T) dU S^-1 V^dag + U S^-1 dV^dag (1 - V V^dag)
   //   J = F.(U^T dU), K = F.(V^dag dV^dag^T), F_ij = 1 / (s_j^2 - s_i^2)
   // evaluated as dA = U [N V^dag + S^-1 dV^dag] + (dU S^-1 - U X S^-1) V^dag with X = U^T dU,
-  // Y = V^dag dV^dag^T and N = dS + (J + J^T) S + S (K + K^T) - S^-1 Y.
+  // Y = V^dag dV^dag^T and N = dS + (J + J^T) S + S (K + K^T) - S^-1 Y^T
+  // (S^-1 dV^dag V^dag^T V^dag = S^-1 Y^T V^dag).
   Tensor A = materialize(A0), U = materialize(U0), S = materialize(S0), Vd = materialize(Vd0);
   Tensor dU = materialize(dU0), dS = materialize(dS0), dVd = materialize(dVd0);
   const TensorMeta &ma = *A.meta, &mu = *U.meta, &ms = *S.meta, &mv = *Vd.meta;

@@ -75,19 +75,6 @@ __global__ void sign_fix_kernel(const SignFixDesc* __restrict__ descs, double* _
   for (int64_t c = lane; c < d.n; c += 32) v[c * d.k] = -v[c * d.k];
 }
 
-// Zero the basis columns whose singular value is at round-off level of the
-// largest (s_j <= rel * s_0): their directions are noise of the sketch, and a
-// zero column keeps the basis orthonormal on the rest.
-__global__ void zero_noise_columns_kernel(const SignFixDesc* __restrict__ descs, const double* __restrict__ S,
-                                          double rel, double* __restrict__ Q) {
-  const SignFixDesc d = descs[blockIdx.y];  // m x k block of Q at u_off, singular values at v_off
-  const double s0 = S[d.v_off];
-  for (int64_t j = blockIdx.x; j < d.k; j += gridDim.x) {
-    if (S[d.v_off + j] > rel * s0) continue;
-    for (int64_t i = threadIdx.x; i < d.m; i += blockDim.x) Q[d.u_off + i + j * d.m] = 0.0;
-  }
-}
-
 // dst[d.dst_off + c + j * d.dst_ld] = src[d.src_off + j + c * d.src_ld] for j < rows, c < cols
 // (descriptor: rows = k rows of the source block, cols = n its columns)
 __global__ void transpose_copy_kernel(const xgb_copy2d_desc* __restrict__ descs, const double* __restrict__ src,
@@ -125,7 +112,7 @@ __global__ void residual_norms_kernel(const SignFixDesc* __restrict__ descs, con
 
 // Middle factor of the SVD reverse rule for one k x k sector (column-major;
 // S is the k x k diagonal block, s_i = S[i + i k]):
-//   N  = dS + (F.X + (F.X)^T) S + S (F.Y + (F.Y)^T) - S^-1 Y
+//   N  = dS + (F.X + (F.X)^T) S + S (F.Y + (F.Y)^T) - S^-1 Y^T
 //   XS = X S^-1
 // with F_ij = 1 / (s_j^2 - s_i^2) (d -> d / (d^2 + 1e-12) for |d| < 1e-12).
 __global__ void svd_bwd_mid_kernel(const SvdBwdDesc* __restrict__ descs, const double* __restrict__ S,
@@ -146,7 +133,7 @@ __global__ void svd_bwd_mid_kernel(const SvdBwdDesc* __restrict__ descs, const d
     const double fij = F(i, j), fji = F(j, i);
     const double jsym = fij * xij + fji * xji;  // (F.X + (F.X)^T)_ij
     const double ksym = fij * yij + fji * yji;
-    N[d.kk_off + e] = dS[d.ds_off + i + j * d.ds_ld] + jsym * sj + si * ksym - yij / si;
+    N[d.kk_off + e] = dS[d.ds_off + i + j * d.ds_ld] + jsym * sj + si * ksym - yji / si;
     XS[d.kk_off + e] = xij / sj;
   }
 }
@@ -168,7 +155,85 @@ __global__ void svd_bwd_scale_kernel(const SvdBwdDesc* __restrict__ descs, const
   }
 }
 
+// Upper-triangular inverse factor of the Gram matrix of one sketch block, for
+// CholeskyQR: G (l x l, column-major at d.g_off, overwritten) = L L^T with
+// L lower triangular after adding `shift` = rel_shift * (m l + l (l + 1)) *
+// trace(G) to the diagonal (shifted CholeskyQR, Fukaya et al. 2020; rel_shift
+// = 0 for the unshifted passes); Rinv (at the same offset) = L^-T, upper
+// triangular, zeros below the diagonal.  A pivot that is not positive is
+// replaced by the smallest positive normal double and counted in *bad.
+__global__ void __launch_bounds__(512) chol_inv_kernel(const CholDesc* __restrict__ descs, double* __restrict__ G,
+                                                      double* __restrict__ Rinv, double rel_shift,
+                                                      int* __restrict__ bad) {
+  const CholDesc d = descs[blockIdx.x];
+  const int l = int(d.l);
+  double* A = G + d.g_off;   // lower triangle becomes L
+  double* X = Rinv + d.g_off;
+  __shared__ double red[16];
+  __shared__ double bcast;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // shift from the trace
+  double tr = 0;
+  for (int i = tid; i < l; i += 512) tr += A[i + i * l];
+  tr = warp_sum_d(tr);
+  if (lane == 0) red[warp] = tr;
+  __syncthreads();
+  if (tid == 0) {
+    double t = 0;
+    for (int w = 0; w < 16; ++w) t += red[w];
+    bcast = rel_shift * (double(d.m) * l + double(l) * (l + 1)) * t;
+  }
+  __syncthreads();
+  const double shift = bcast;
+  __syncthreads();
+  // left-looking Cholesky, one column per step
+  for (int j = 0; j < l; ++j) {
+    double part = 0;
+    for (int k = tid; k < j; k += 512) part = fma(A[j + k * l], A[j + k * l], part);
+    part = warp_sum_d(part);
+    if (lane == 0) red[warp] = part;
+    __syncthreads();
+    if (tid == 0) {
+      double ssum = 0;
+      for (int w = 0; w < 16; ++w) ssum += red[w];
+      double dj = A[j + j * l] + shift - ssum;
+      if (!(dj > 0.0)) { dj = 2.2250738585072014e-308; atomicAdd(bad, 1); }
+      A[j + j * l] = sqrt(dj);
+    }
+    __syncthreads();
+    const double ljj = A[j + j * l];
+    for (int i = j + 1 + tid; i < l; i += 512) {
+      double acc = A[i + j * l];
+      for (int k = 0; k < j; ++k) acc = fma(-A[i + k * l], A[j + k * l], acc);
+      A[i + j * l] = acc / ljj;
+    }
+    __syncthreads();
+  }
+  // X = L^-1 column by column (one thread per column), written transposed: Rinv = X^T
+  for (int c = tid; c < l; c += 512) {
+    // forward substitution L x = e_c, x_i = 0 for i < c
+    for (int i = 0; i < l; ++i) {
+      double xi = 0.0;
+      if (i == c) {
+        xi = 1.0 / A[c + c * l];
+      } else if (i > c) {
+        double acc = 0.0;
+        for (int k = c; k < i; ++k) acc = fma(A[i + k * l], X[c + k * l], acc);  // x_k stored at X[c, k]
+        xi = -acc / A[i + i * l];
+      }
+      X[c + i * l] = xi;  // Rinv[c][i] = (L^-1)[i][c]
+    }
+  }
+}
+
 }  // namespace
+
+void launch_chol_inv(const CholDesc* d_descs, int n, double* G, double* Rinv, double rel_shift, int* bad,
+                     cudaStream_t s) {
+  if (n <= 0) return;
+  chol_inv_kernel<<<n, 512, 0, s>>>(d_descs, G, Rinv, rel_shift, bad);
+  count_launch();
+}
 
 void launch_svd_bwd_mid(const SvdBwdDesc* d_descs, int n, int64_t max_kk, const double* S, const double* X,
                         const double* Y, const double* dS, double* N, double* XS, cudaStream_t s) {
@@ -202,14 +267,6 @@ void launch_transpose_copy(const xgb_copy2d_desc* d_descs, int n, int64_t max_el
   const int64_t want = (max_elems + 255) / 256;
   dim3 grid(unsigned(want < 1024 ? want : 1024), unsigned(n));
   transpose_copy_kernel<<<grid, 256, 0, s>>>(d_descs, src, dst);
-  count_launch();
-}
-
-void launch_zero_noise_columns(const SignFixDesc* d_descs, int n, int64_t max_k, const double* S, double rel, double* Q,
-                               cudaStream_t s) {
-  if (n <= 0 || max_k <= 0) return;
-  dim3 grid(unsigned(max_k < 1024 ? max_k : 1024), unsigned(n));
-  zero_noise_columns_kernel<<<grid, 128, 0, s>>>(d_descs, S, rel, Q);
   count_launch();
 }
 

@@ -775,7 +775,7 @@ namespace {
 struct SvdPlan {
   int n = 0;
   int64_t u_total = 0, s_total = 0, v_total = 0, work_total = 0, maxk = 0;
-  double lapack_flops = 0;  // dgesvd-equivalent work: 4m^2n + 8mn^2 + 9n^3 (m >= n)
+  double lapack_flops = 0;  // thin R-SVD work 6 m n^2 + 20 n^3 (m >= n; Golub & Van Loan, Table 5.5.1)
   std::vector<int64_t> s_begin;  // per sector prefix (host), size n+1
   std::vector<int64_t> u_off, s_off, v_off, kfull;
   xgb_svd_desc* d_descs = nullptr;
@@ -812,7 +812,7 @@ std::shared_ptr<SvdPlan> get_svd_plan(const TensorMeta& m) {
     p->maxk = std::max(p->maxk, k);
     {
       const double M = double(std::max(r, c)), N = double(std::min(r, c));
-      p->lapack_flops += 4.0 * M * M * N + 8.0 * M * N * N + 9.0 * N * N * N;
+      p->lapack_flops += 6.0 * M * N * N + 20.0 * N * N * N;
     }
     descs.push_back(d);
     deg.push_back(m.sym.deg(m.sectors[i]));
