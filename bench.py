@@ -9,7 +9,8 @@ grow_all (left, right, top, bottom moves), all tensor work on the GPU.
 
 Forms, same workload, same GPU:
   chosen   randomized projector SVD (seeded Gaussian sketches, 8 subspace
-           iterations, widths = the direction's last kept counts + max(16, 50 %),
+           iterations, CholeskyQR3 orthonormalisation, widths = the direction's
+           last kept counts + max(16, 50 %), chi + 16 for sectors not seen yet,
            exact FP64 fallback), FP64 SVD core / projectors / normalisation;
            block GEMMs in FP64 or 3xTF32 (--gemm)
   plain    the exact FP64 tSVD in every move (the reference algorithm)
@@ -124,6 +125,7 @@ def make_ctm(A, chi, form, gemm):
     c = CTM(A, chi).init()
     if form == "chosen":
         c.set_svd("randomized", power_iters=POWER_ITERS, seed=SEED, oversample=16, growth=0.5)
+        c.set_sketch_unseen(True)
     c.set_gemm(gemm)
     return c
 
@@ -245,8 +247,9 @@ def run_gpu(args):
         loss = model.train(X, T, steps=2000, lr=2e-3)
         res["learned_train"] = {"samples": int(X.shape[0]), "adam_steps": 2000, "loss_first": loss0,
                                 "loss_last": loss, "seconds": time.perf_counter() - t0}
-        lc = make_ctm(A, CHI, "plain", args.gemm)  # exact first step, then predicted widths
+        lc = make_ctm(A, CHI, "plain", args.gemm)
         lc.set_rank_model(model, margin=0.0, min_oversample=2, power_iters=POWER_ITERS, seed=SEED)
+        lc.set_sketch_unseen(True)
         for _ in range(COMPARE_STEPS):
             lc.grow_all()
         res["e_learned"] = energy(lc, H)
@@ -333,6 +336,7 @@ def run_fz2(args):
         c = CTM(A, FZ2_CHI).init()
         if form == "chosen":
             c.set_svd("randomized", power_iters=POWER_ITERS, seed=SEED, oversample=16, growth=0.5)
+            c.set_sketch_unseen(True)
             c.set_gemm(args.gemm)
         ms, marks = [], {}
         for i in range(iters):
@@ -618,8 +622,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.gemm == "fp64" else "f64 (3xtf32 block GEMMs)",
             "data": "synthetic (seeded N(0,1) site tensor)",
-            "config": dict(config, form=f"chosen: randomized projector SVD ({POWER_ITERS} subspace iterations, widths last kept "
-                                        "+ max(16, 50%), exact FP64 fallback), FP64 SVD core",
+            "config": dict(config, form=f"chosen: randomized projector SVD ({POWER_ITERS} subspace iterations, "
+                                        "CholeskyQR3 bases, widths last kept + max(16, 50%), chi + 16 for unseen "
+                                        "sectors, exact FP64 fallback), FP64 SVD core",
                            gemm=args.gemm, parallelism=f"replicas x{world}"),
             "e2e": {"value": world * 1e3 / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"]},

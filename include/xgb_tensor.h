@@ -129,6 +129,10 @@ int xgb_set_gemm_precision(int precision);
    renormalisation of the moves (XGB_PREC_FP64 or XGB_PREC_3XTF32 from xgb.h);
    the projector SVD, the projector construction and the normalisation stay FP64. */
 int xgb_ctm_set_gemm_precision(xgb_ctm c, int precision);
+/* Sectors without history (the first decomposition of each direction) in the
+   randomized form: exact FP64 tSVD (on = 0, the default) or a sketch of
+   min(chi, min(rows, cols)) + 16 columns (on = 1), for either width rule. */
+int xgb_ctm_set_sketch_unseen(xgb_ctm c, int on);
 /* Warm start of the randomized projector SVD: the direction's previous V^dag seeds
    the sketch and warm_iters subspace iterations are run instead of power_iters
    (warm_iters < 0: off, the default). */

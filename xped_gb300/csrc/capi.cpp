@@ -317,6 +317,13 @@ int xgb_ctm_set_gemm_precision(xgb_ctm c, int precision) {
   })
 }
 
+int xgb_ctm_set_sketch_unseen(xgb_ctm c, int on) {
+  GUARD(XGB_E_BADPLAN, {
+    c->c->sketch_unseen = on != 0;
+    return XGB_OK;
+  })
+}
+
 int xgb_ctm_set_warm_start(xgb_ctm c, int warm_iters) {
   GUARD(XGB_E_BADPLAN, {
     c->c->warm_iters = warm_iters < 0 ? -1 : warm_iters;

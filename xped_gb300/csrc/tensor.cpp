@@ -1022,7 +1022,7 @@ std::vector<int64_t> HistoryPolicy::widths(const TensorMeta& m, const History& l
   std::vector<int64_t> w(m.sectors.size(), 0);
   for (size_t i = 0; i < m.sectors.size(); ++i) {
     auto it = last.find(m.sectors[i]);
-    if (it == last.end()) continue;  // never seen: exact
+    if (it == last.end()) continue;  // never seen
     const int64_t k = it->second.keep;
     w[i] = std::min<int64_t>(chi, k) + std::max<int64_t>(oversample, int64_t(std::ceil(growth * double(k))));
   }
@@ -1163,6 +1163,10 @@ std::pair<Tensor, Tensor> CTM::decompose_dir(int d, const Tensor& t1, const Tens
   } else {
     if (!policy) throw std::runtime_error("CTM: randomized projector SVD without a width policy");
     std::vector<int64_t> want = policy->widths(m, hist[d], chi);
+    if (sketch_unseen)
+      for (size_t i = 0; i < n; ++i)
+        if (want[i] <= 0 && hist[d].find(m.sectors[i]) == hist[d].end())
+          want[i] = std::min<int64_t>(chi, std::min(m.rows[i], m.cols[i])) + 16;
     RsvdInfo info;
     const bool warm = warm_iters >= 0 && warm_v[d].valid() && warm_v[d].meta->cod == m.cod;
     r = tsvd_randomized(prod, chi, 1.0e-10, want, warm ? warm_iters : power_iters,

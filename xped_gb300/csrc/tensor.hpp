@@ -170,7 +170,7 @@ struct WidthPolicy {
   virtual std::vector<int64_t> widths(const TensorMeta& m, const History& last, int64_t chi) = 0;
 };
 // Without a model: last kept count + max(oversample, growth * kept); sectors
-// with no history are decomposed exactly.
+// with no history get 0 (exact, or the CTM's unseen-sector sketch).
 struct HistoryPolicy : WidthPolicy {
   int64_t oversample = 16;
   double growth = 0.5;
@@ -224,6 +224,10 @@ class CTM {
   // subspace iterations when the direction's previous V^dag (same matrix
   // structure) seeds the sketch; < 0 disables the warm start
   int warm_iters = -1;
+  // sectors a direction has not seen yet: exact FP64 tSVD (false) or a sketch
+  // of min(chi, min(rows, cols)) + 16 columns (true; a sector keeps at most chi
+  // values, so this sketch cannot saturate)
+  bool sketch_unseen = false;
   // > 0: kept sketched triplets must satisfy ||A v - s u|| <= res_tol * s_max
   // (unconverged sectors get more subspace iterations)
   double res_tol = 0.0;

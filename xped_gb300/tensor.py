@@ -355,6 +355,11 @@ class CTM:
               "ctm_set_svd")
         return self
 
+    def set_sketch_unseen(self, on: bool = True):
+        """Sketch (instead of decomposing exactly) the sectors a direction has not seen yet."""
+        check(lib().xgb_ctm_set_sketch_unseen(self._h, int(on)), "ctm_set_sketch_unseen")
+        return self
+
     def set_warm_start(self, warm_iters: int = 2):
         """Seed each randomized projector SVD with the direction's previous V^dag and
         run warm_iters subspace iterations (negative: off)."""
