@@ -156,74 +156,105 @@ __global__ void svd_bwd_scale_kernel(const SvdBwdDesc* __restrict__ descs, const
 }
 
 // Upper-triangular inverse factor of the Gram matrix of one sketch block, for
-// CholeskyQR: G (l x l, column-major at d.g_off, overwritten) = L L^T with
-// L lower triangular after adding `shift` = rel_shift * (m l + l (l + 1)) *
-// trace(G) to the diagonal (shifted CholeskyQR, Fukaya et al. 2020; rel_shift
-// = 0 for the unshifted passes); Rinv (at the same offset) = L^-T, upper
-// triangular, zeros below the diagonal.  A pivot that is not positive is
-// replaced by the smallest positive normal double and counted in *bad.
-__global__ void __launch_bounds__(512) chol_inv_kernel(const CholDesc* __restrict__ descs, double* __restrict__ G,
-                                                      double* __restrict__ Rinv, double rel_shift,
-                                                      int* __restrict__ bad) {
-  const CholDesc d = descs[blockIdx.x];
-  const int l = int(d.l);
-  double* A = G + d.g_off;   // lower triangle becomes L
-  double* X = Rinv + d.g_off;
+// CholeskyQR: G (l x l, column-major at d.g_off) = L L^T with L lower
+// triangular after adding `shift` = rel_shift * (m l + l (l + 1)) * trace(G)
+// to the diagonal (shifted CholeskyQR, Fukaya et al. 2020; rel_shift = 0 for
+// the unshifted passes); Rinv (at the same offset) = L^-T, upper triangular,
+// zeros below the diagonal.  A pivot that is not positive is replaced by the
+// smallest positive normal double and counted in *bad.
+//
+// Both factorisations run with all threads in lockstep over the inner index
+// (the broadcast operand is one shared-memory word): Cholesky left-looking,
+// threads over the rows of the current column; the inverse row by row,
+// threads over the columns.  Matrices live in shared memory, row-major with
+// an odd leading dimension (conflict-free column access), when two of them
+// fit; larger blocks use the same loops on global memory (G is then
+// overwritten).
+template <bool kShared>
+__device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double* __restrict__ Xg, double rel_shift,
+                              int* __restrict__ bad, double* sm) {
+  const int l = int(d.l), tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ld = kShared ? (l | 1) : l;
+  // L[i][k] and X[i][k] accessors: shared row-major (ld odd) or global column-major (ld = l)
+  double* Ls = kShared ? sm : Gg;
+  double* Xs = kShared ? sm + int64_t(ld) * l : Xg;
+  auto LA = [&](int i, int k) -> double& { return kShared ? Ls[i * ld + k] : Ls[i + int64_t(k) * l]; };
+  auto XA = [&](int i, int k) -> double& { return kShared ? Xs[i * ld + k] : Xs[i + int64_t(k) * l]; };
   __shared__ double red[16];
   __shared__ double bcast;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // shift from the trace
+  if (kShared)
+    for (int e = tid; e < l * l; e += blockDim.x) LA(e % l, e / l) = Gg[e];  // G column-major -> L row-major
+  __syncthreads();
   double tr = 0;
-  for (int i = tid; i < l; i += 512) tr += A[i + i * l];
+  for (int i = tid; i < l; i += blockDim.x) tr += LA(i, i);
   tr = warp_sum_d(tr);
   if (lane == 0) red[warp] = tr;
   __syncthreads();
   if (tid == 0) {
     double t = 0;
-    for (int w = 0; w < 16; ++w) t += red[w];
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) t += red[w];
     bcast = rel_shift * (double(d.m) * l + double(l) * (l + 1)) * t;
   }
   __syncthreads();
   const double shift = bcast;
   __syncthreads();
-  // left-looking Cholesky, one column per step
+  // Cholesky, left-looking: column j from the finished columns k < j
   for (int j = 0; j < l; ++j) {
-    double part = 0;
-    for (int k = tid; k < j; k += 512) part = fma(A[j + k * l], A[j + k * l], part);
-    part = warp_sum_d(part);
-    if (lane == 0) red[warp] = part;
-    __syncthreads();
     if (tid == 0) {
-      double ssum = 0;
-      for (int w = 0; w < 16; ++w) ssum += red[w];
-      double dj = A[j + j * l] + shift - ssum;
+      double dj = LA(j, j) + shift;
+      for (int k = 0; k < j; ++k) dj = fma(-LA(j, k), LA(j, k), dj);
       if (!(dj > 0.0)) { dj = 2.2250738585072014e-308; atomicAdd(bad, 1); }
-      A[j + j * l] = sqrt(dj);
+      LA(j, j) = sqrt(dj);
     }
     __syncthreads();
-    const double ljj = A[j + j * l];
-    for (int i = j + 1 + tid; i < l; i += 512) {
-      double acc = A[i + j * l];
-      for (int k = 0; k < j; ++k) acc = fma(-A[i + k * l], A[j + k * l], acc);
-      A[i + j * l] = acc / ljj;
+    const double inv = 1.0 / LA(j, j);
+    for (int i = j + 1 + tid; i < l; i += blockDim.x) {
+      double acc = LA(i, j);
+      for (int k = 0; k < j; ++k) acc = fma(-LA(i, k), LA(j, k), acc);
+      LA(i, j) = acc * inv;
     }
     __syncthreads();
   }
-  // X = L^-1 column by column (one thread per column), written transposed: Rinv = X^T
-  for (int c = tid; c < l; c += 512) {
-    // forward substitution L x = e_c, x_i = 0 for i < c
-    for (int i = 0; i < l; ++i) {
-      double xi = 0.0;
-      if (i == c) {
-        xi = 1.0 / A[c + c * l];
-      } else if (i > c) {
-        double acc = 0.0;
-        for (int k = c; k < i; ++k) acc = fma(A[i + k * l], X[c + k * l], acc);  // x_k stored at X[c, k]
-        xi = -acc / A[i + i * l];
+  // X = L^-1 row by row: X[i][c] = -(sum_{k=c}^{i-1} L[i][k] X[k][c]) / L[i][i], X[i][i] = 1 / L[i][i]
+  for (int i = 0; i < l; ++i) {
+    const double inv = 1.0 / LA(i, i);
+    for (int c = tid; c < l; c += blockDim.x) {
+      double acc = 0.0;
+      if (c < i)
+        for (int k = c; k < i; ++k) acc = fma(LA(i, k), XA(k, c), acc);
+      XA(i, c) = c < i ? -acc * inv : (c == i ? inv : 0.0);
+    }
+    __syncthreads();
+  }
+  // Rinv = X^T (column-major l x l at g_off): Rinv[c + i l] = X[i][c]
+  if (kShared) {
+    for (int e = tid; e < l * l; e += blockDim.x) {
+      const int c = e % l, i = e / l;
+      Xg[e] = XA(i, c);
+    }
+  } else {
+    // X was written column-major into Xg: transpose in place through the pairs (i, c), i > c
+    __syncthreads();
+    for (int e = tid; e < l * l; e += blockDim.x) {
+      const int i = e % l, c = e / l;
+      if (i > c) {
+        const double a = Xg[i + int64_t(c) * l], b = Xg[c + int64_t(i) * l];
+        Xg[i + int64_t(c) * l] = b;
+        Xg[c + int64_t(i) * l] = a;
       }
-      X[c + i * l] = xi;  // Rinv[c][i] = (L^-1)[i][c]
     }
   }
+}
+
+__global__ void __launch_bounds__(256) chol_inv_kernel(const CholDesc* __restrict__ descs, double* __restrict__ G,
+                                                      double* __restrict__ Rinv, double rel_shift,
+                                                      int* __restrict__ bad, int smem_cap_l) {
+  extern __shared__ double sm[];
+  const CholDesc d = descs[blockIdx.x];
+  if (d.l <= smem_cap_l)
+    chol_inv_body<true>(d, G + d.g_off, Rinv + d.g_off, rel_shift, bad, sm);
+  else
+    chol_inv_body<false>(d, G + d.g_off, Rinv + d.g_off, rel_shift, bad, sm);
 }
 
 }  // namespace
@@ -231,7 +262,15 @@ __global__ void __launch_bounds__(512) chol_inv_kernel(const CholDesc* __restric
 void launch_chol_inv(const CholDesc* d_descs, int n, double* G, double* Rinv, double rel_shift, int* bad,
                      cudaStream_t s) {
   if (n <= 0) return;
-  chol_inv_kernel<<<n, 512, 0, s>>>(d_descs, G, Rinv, rel_shift, bad);
+  // two l x (l | 1) double matrices in shared memory up to l = 111 (< 200 KB)
+  constexpr int kCapL = 111;
+  static bool attr = false;
+  const int bytes = 2 * kCapL * (kCapL | 1) * int(sizeof(double));
+  if (!attr) {
+    cudaFuncSetAttribute(chol_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    attr = true;
+  }
+  chol_inv_kernel<<<n, 256, bytes, s>>>(d_descs, G, Rinv, rel_shift, bad, kCapL);
   count_launch();
 }
 
