@@ -306,11 +306,14 @@ __global__ void __launch_bounds__(1024) truncate_kernel(int n_sectors, const int
   int64_t* flag = ws + 3 * total;      // flag[i] = 1 kept, 0 dropped; fpos stored in gstart reuse below
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int g = tid; g < n_sectors; g += blockDim.x) keep[g] = 0;
+  // exact ranks under a total order (NaN ranks below every number, ties by
+  // index), so that `exact` is a permutation whatever the values are
+  auto key = [](double v) { return v == v ? v : -INFINITY; };
   for (int64_t i = tid; i < total; i += blockDim.x) {
-    const double si = s[i];
+    const double si = key(s[i]);
     int64_t r = 0;
     for (int64_t j = 0; j < total; ++j) {
-      const double sj = s[j];
+      const double sj = key(s[j]);
       r += (sj > si) || (sj == si && j < i);
     }
     exact[r] = i;

@@ -160,82 +160,92 @@ __global__ void svd_bwd_scale_kernel(const SvdBwdDesc* __restrict__ descs, const
 // triangular after adding `shift` = rel_shift * (m l + l (l + 1)) * trace(G)
 // to the diagonal (shifted CholeskyQR, Fukaya et al. 2020; rel_shift = 0 for
 // the unshifted passes); Rinv (at the same offset) = L^-T, upper triangular,
-// zeros below the diagonal.  A pivot that is not positive is replaced by the
-// smallest positive normal double and counted in *bad.
+// zeros below the diagonal.  A pivot at or below eps * trace / l (a direction
+// the block does not span) becomes sqrt(eps * trace / l) with a zero column
+// below it, so the factor stays finite and well scaled; such pivots are
+// counted in *bad.
 //
-// Both factorisations run with all threads in lockstep over the inner index
-// (the broadcast operand is one shared-memory word): Cholesky left-looking,
-// threads over the rows of the current column; the inverse row by row,
-// threads over the columns.  Matrices live in shared memory, row-major with
-// an odd leading dimension (conflict-free column access), when two of them
-// fit; larger blocks use the same loops on global memory (G is then
-// overwritten).
+// Both factorisations are right-looking, so every step is a parallel update
+// of a trailing block: Cholesky by columns (scale the column, rank-1 update of
+// the trailing lower triangle), the inverse by forward elimination of the
+// identity (X <- rows of L^-1 as they are finished).  Matrices live in shared
+// memory, row-major with an odd leading dimension, when two of them fit;
+// larger blocks use the same loops on global memory.
 template <bool kShared>
 __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double* __restrict__ Xg, double rel_shift,
                               int* __restrict__ bad, double* sm) {
-  const int l = int(d.l), tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int l = int(d.l), tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
   const int ld = kShared ? (l | 1) : l;
-  // L[i][k] and X[i][k] accessors: shared row-major (ld odd) or global column-major (ld = l)
   double* Ls = kShared ? sm : Gg;
   double* Xs = kShared ? sm + int64_t(ld) * l : Xg;
+  // element accessors: shared row-major (ld odd) or global column-major (ld = l); symmetric G
   auto LA = [&](int i, int k) -> double& { return kShared ? Ls[i * ld + k] : Ls[i + int64_t(k) * l]; };
   auto XA = [&](int i, int k) -> double& { return kShared ? Xs[i * ld + k] : Xs[i + int64_t(k) * l]; };
-  __shared__ double red[16];
+  __shared__ double red[32];
   __shared__ double bcast;
   if (kShared)
-    for (int e = tid; e < l * l; e += blockDim.x) LA(e % l, e / l) = Gg[e];  // G column-major -> L row-major
+    for (int e = tid; e < l * l; e += nt) LA(e % l, e / l) = Gg[e];
+  for (int e = tid; e < l * l; e += nt) XA(e % l, e / l) = (e % l == e / l) ? 1.0 : 0.0;
   __syncthreads();
   double tr = 0;
-  for (int i = tid; i < l; i += blockDim.x) tr += LA(i, i);
+  for (int i = tid; i < l; i += nt) tr += LA(i, i);
   tr = warp_sum_d(tr);
   if (lane == 0) red[warp] = tr;
   __syncthreads();
+  __shared__ double floor_s;
+  __shared__ int dead;
   if (tid == 0) {
     double t = 0;
-    for (int w = 0; w < int(blockDim.x >> 5); ++w) t += red[w];
+    for (int w = 0; w < (nt >> 5); ++w) t += red[w];
     bcast = rel_shift * (double(d.m) * l + double(l) * (l + 1)) * t;
+    const double avg = t > 0.0 ? t / l : 0.0;
+    floor_s = fmax(2.220446049250313e-16 * avg, 1e-300);
   }
   __syncthreads();
-  const double shift = bcast;
+  const double shift = bcast, dfloor = floor_s;
+  for (int i = tid; i < l; i += nt) LA(i, i) += shift;
   __syncthreads();
-  // Cholesky, left-looking: column j from the finished columns k < j
+  // Cholesky (right-looking), lower triangle in place
   for (int j = 0; j < l; ++j) {
     if (tid == 0) {
-      double dj = LA(j, j) + shift;
-      for (int k = 0; k < j; ++k) dj = fma(-LA(j, k), LA(j, k), dj);
-      if (!(dj > 0.0)) { dj = 2.2250738585072014e-308; atomicAdd(bad, 1); }
-      LA(j, j) = sqrt(dj);
+      const double dj = LA(j, j);
+      dead = !(dj > dfloor);  // also true for NaN
+      if (dead) atomicAdd(bad, 1);
+      LA(j, j) = sqrt(dead ? dfloor : dj);
     }
     __syncthreads();
     const double inv = 1.0 / LA(j, j);
-    for (int i = j + 1 + tid; i < l; i += blockDim.x) {
-      double acc = LA(i, j);
-      for (int k = 0; k < j; ++k) acc = fma(-LA(i, k), LA(j, k), acc);
-      LA(i, j) = acc * inv;
+    const bool zero_col = dead != 0;
+    for (int i = j + 1 + tid; i < l; i += nt) LA(i, j) = zero_col ? 0.0 : LA(i, j) * inv;
+    __syncthreads();
+    const int t = l - j - 1;  // trailing lower triangle: rows i >= k > j
+    for (int e = tid; e < t * t; e += nt) {
+      const int i = j + 1 + e % t, k = j + 1 + e / t;
+      if (i >= k) LA(i, k) = fma(-LA(i, j), LA(k, j), LA(i, k));
     }
     __syncthreads();
   }
-  // X = L^-1 row by row: X[i][c] = -(sum_{k=c}^{i-1} L[i][k] X[k][c]) / L[i][i], X[i][i] = 1 / L[i][i]
-  for (int i = 0; i < l; ++i) {
-    const double inv = 1.0 / LA(i, i);
-    for (int c = tid; c < l; c += blockDim.x) {
-      double acc = 0.0;
-      if (c < i)
-        for (int k = c; k < i; ++k) acc = fma(LA(i, k), XA(k, c), acc);
-      XA(i, c) = c < i ? -acc * inv : (c == i ? inv : 0.0);
+  // X = L^-1 by forward elimination of the identity: row j of X is final after
+  // dividing by L[j][j]; then rows i > j subtract L[i][j] * row j (columns c <= j)
+  for (int j = 0; j < l; ++j) {
+    const double inv = 1.0 / LA(j, j);
+    for (int c = tid; c <= j; c += nt) XA(j, c) *= inv;
+    __syncthreads();
+    const int t = l - j - 1;
+    for (int e = tid; e < t * (j + 1); e += nt) {
+      const int i = j + 1 + e % t, c = e / t;
+      XA(i, c) = fma(-LA(i, j), XA(j, c), XA(i, c));
     }
     __syncthreads();
   }
-  // Rinv = X^T (column-major l x l at g_off): Rinv[c + i l] = X[i][c]
+  // Rinv = X^T, column-major l x l: Rinv[c + i l] = X[i][c]
   if (kShared) {
-    for (int e = tid; e < l * l; e += blockDim.x) {
+    for (int e = tid; e < l * l; e += nt) {
       const int c = e % l, i = e / l;
       Xg[e] = XA(i, c);
     }
   } else {
-    // X was written column-major into Xg: transpose in place through the pairs (i, c), i > c
-    __syncthreads();
-    for (int e = tid; e < l * l; e += blockDim.x) {
+    for (int e = tid; e < l * l; e += nt) {
       const int i = e % l, c = e / l;
       if (i > c) {
         const double a = Xg[i + int64_t(c) * l], b = Xg[c + int64_t(i) * l];

@@ -868,6 +868,8 @@ SVDResult truncate_spectra(const TensorMeta& m, const Spectra& sp, int64_t max_k
   cuda_ok(cudaMemcpyAsync(res.spectrum.data(), sp.S, sizeof(double) * size_t(s_total), cudaMemcpyDeviceToHost, st), "d2h");
   cuda_ok(cudaStreamSynchronize(st), "sync");
   dev_free(keep_d);
+  for (double v : res.spectrum)
+    if (!std::isfinite(v)) throw std::runtime_error("tSVD: non-finite singular value (non-finite input block?)");
   if (own_tables) {
     dev_free(d_sb);
     dev_free(d_deg);
@@ -876,6 +878,8 @@ SVDResult truncate_spectra(const TensorMeta& m, const Spectra& sp, int64_t max_k
   res.trunc_weight = g_out2_host[0];
   res.entropy = g_out2_host[1];
   res.keep.assign(g_keep_host, g_keep_host + n);
+  for (int i = 0; i < n; ++i)
+    if (res.keep[i] < 0 || res.keep[i] > sp.k[i]) throw std::runtime_error("tSVD: truncation returned an invalid count");
   // truncated basis: charges with kept values in ascending order (std::map, Tensor.cpp:592-598)
   std::vector<std::pair<int, int>> kept;  // (q, sector index)
   for (int i = 0; i < n; ++i)
