@@ -218,10 +218,22 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
     const bool zero_col = dead != 0;
     for (int i = j + 1 + tid; i < l; i += nt) LA(i, j) = zero_col ? 0.0 : LA(i, j) * inv;
     __syncthreads();
-    const int t = l - j - 1;  // trailing lower triangle: rows i >= k > j
-    for (int e = tid; e < t * t; e += nt) {
-      const int i = j + 1 + e % t, k = j + 1 + e / t;
-      if (i >= k) LA(i, k) = fma(-LA(i, j), LA(k, j), LA(i, k));
+    // trailing lower triangle (rows i >= k > j) folded into whole columns: column c and column
+    // t-1-c together hold t+1 elements; an odd t leaves the middle column alone
+    const int t = l - j - 1, half = t >> 1;
+    const int total = (t + 1) * half + ((t & 1) ? (t + 1) >> 1 : 0);
+    for (int e = tid; e < total; e += nt) {
+      int i, k;
+      if (e < (t + 1) * half) {
+        const int r = e % (t + 1), c = e / (t + 1);
+        if (r < t - c) { i = c + r; k = c; } else { i = (t - 1 - c) + (r - (t - c)); k = t - 1 - c; }
+      } else {
+        k = (t - 1) >> 1;
+        i = k + (e - (t + 1) * half);
+      }
+      i += j + 1;
+      k += j + 1;
+      LA(i, k) = fma(-LA(i, j), LA(k, j), LA(i, k));
     }
     __syncthreads();
   }
@@ -256,7 +268,7 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   }
 }
 
-__global__ void __launch_bounds__(256) chol_inv_kernel(const CholDesc* __restrict__ descs, double* __restrict__ G,
+__global__ void __launch_bounds__(1024) chol_inv_kernel(const CholDesc* __restrict__ descs, double* __restrict__ G,
                                                       double* __restrict__ Rinv, double rel_shift,
                                                       int* __restrict__ bad, int smem_cap_l) {
   extern __shared__ double sm[];
@@ -272,15 +284,15 @@ __global__ void __launch_bounds__(256) chol_inv_kernel(const CholDesc* __restric
 void launch_chol_inv(const CholDesc* d_descs, int n, double* G, double* Rinv, double rel_shift, int* bad,
                      cudaStream_t s) {
   if (n <= 0) return;
-  // two l x (l | 1) double matrices in shared memory up to l = 111 (< 200 KB)
-  constexpr int kCapL = 111;
+  // two l x (l | 1) double matrices in shared memory up to l = 119 (< 227 KB)
+  constexpr int kCapL = 119;
   static bool attr = false;
   const int bytes = 2 * kCapL * (kCapL | 1) * int(sizeof(double));
   if (!attr) {
     cudaFuncSetAttribute(chol_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     attr = true;
   }
-  chol_inv_kernel<<<n, 256, bytes, s>>>(d_descs, G, Rinv, rel_shift, bad, kCapL);
+  chol_inv_kernel<<<n, 1024, bytes, s>>>(d_descs, G, Rinv, rel_shift, bad, kCapL);
   count_launch();
 }
 
