@@ -10,8 +10,9 @@ grow_all (left, right, top, bottom moves), all tensor work on the GPU.
 Forms, same workload, same GPU:
   chosen   randomized projector SVD (seeded Gaussian sketches, 8 subspace
            iterations, CholeskyQR3 orthonormalisation, widths = the direction's
-           last kept counts + max(16, 50 %), chi + 16 for sectors not seen yet,
-           exact FP64 fallback), FP64 SVD core / projectors / normalisation;
+           last kept counts + max(16, 50 %), exact FP64 tSVD for the first
+           decomposition of each direction and as fallback), FP64 SVD core /
+           projectors / normalisation;
            block GEMMs in FP64 or 3xTF32 (--gemm)
   plain    the exact FP64 tSVD in every move (the reference algorithm)
 The energy per site (Heisenberg bonds, horizontal + vertical RDM) of both
@@ -125,7 +126,6 @@ def make_ctm(A, chi, form, gemm):
     c = CTM(A, chi).init()
     if form == "chosen":
         c.set_svd("randomized", power_iters=POWER_ITERS, seed=SEED, oversample=16, growth=0.5)
-        c.set_sketch_unseen(True)
     c.set_gemm(gemm)
     return c
 
@@ -249,7 +249,6 @@ def run_gpu(args):
                                 "loss_last": loss, "seconds": time.perf_counter() - t0}
         lc = make_ctm(A, CHI, "plain", args.gemm)
         lc.set_rank_model(model, margin=0.0, min_oversample=2, power_iters=POWER_ITERS, seed=SEED)
-        lc.set_sketch_unseen(True)
         for _ in range(COMPARE_STEPS):
             lc.grow_all()
         res["e_learned"] = energy(lc, H)
@@ -314,8 +313,9 @@ FZ2_ITERS = 20
 def run_fz2(args):
     """Fermionic Z2 iPEPS (ZN<FChargeU1,2>), D=6 with q in {0,1} and degeneracies [3,3], physical
     parity 0/1, chi=144: FZ2_ITERS CTMRG iterations of the chosen form from FROM_A, every step
-    timed with CUDA events; the density-density bond expectation after --fz2-plain-steps steps and
-    after the last one.  The plain FP64 form runs --fz2-plain-steps steps from the same start
+    timed with CUDA events (the chosen form sketches the first decomposition of each direction too:
+    chi + 16 columns); the density-density bond expectation after --fz2-plain-steps steps and after
+    the last one.  The plain FP64 form runs --fz2-plain-steps steps from the same start
     (its exact SVDs of ~2600-wide sector blocks take minutes per step)."""
     from xped_gb300 import CTM, Basis, Tensor, ensure_device, lib
     from xped_gb300.observables import density_bond, energy
@@ -623,8 +623,8 @@ def main():
             "vs_baseline": None, "dtype": "f64" if args.gemm == "fp64" else "f64 (3xtf32 block GEMMs)",
             "data": "synthetic (seeded N(0,1) site tensor)",
             "config": dict(config, form=f"chosen: randomized projector SVD ({POWER_ITERS} subspace iterations, "
-                                        "CholeskyQR3 bases, widths last kept + max(16, 50%), chi + 16 for unseen "
-                                        "sectors, exact FP64 fallback), FP64 SVD core",
+                                        "CholeskyQR3 bases, widths last kept + max(16, 50%), exact first decomposition "
+                                        "per direction and exact FP64 fallback), FP64 SVD core",
                            gemm=args.gemm, parallelism=f"replicas x{world}"),
             "e2e": {"value": world * 1e3 / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"]},
