@@ -300,6 +300,7 @@ def run_gpu(args):
     res["small_plain_ms"] = float(np.mean(ms))
     L.xgb_free(flush)
     res["gemm_sweep"] = gemm_sweep()
+    res["config1"] = config1_ops()
     return res
 
 
@@ -367,7 +368,7 @@ def run_fz2(args):
 
 # ----------------------------------------------------------------------------- block-GEMM sweep
 def gemm_sweep(reps=5):
-    """Grouped block GEMMs FP64 vs 3xTF32: (i) the sector GEMMs of an SU(2)
+    """Grouped block GEMMs FP64 vs 3xTF32 vs FP32 (CUDA cores): (i) the sector GEMMs of an SU(2)
     Tensor<2,2> product (irreps q = 2j+1, j = 0..3 integer, multiplicities 1-24);
     (ii) synthetic lists of G blocks, m, n, k log-uniform in [8, 512].  Useful
     TFLOP/s = sum 2mnk / time; error = max over blocks of ||C - C_fp64||_F / ||C_fp64||_F."""
@@ -401,7 +402,7 @@ def gemm_sweep(reps=5):
     flops = sum(2.0 * d.m * d.n * d.k for d in descs)
     res = {}
     ref = None
-    for form in ("fp64", "3xtf32"):
+    for form in ("fp64", "3xtf32", "fp32"):
         set_gemm_precision(form)
         ms = timed(lambda: T1.matmul(T2))
         Cm = T1.matmul(T2)
@@ -437,7 +438,7 @@ def gemm_sweep(reps=5):
             L.xgb_memcpy_h2d(p_, h.ctypes.data, h.nbytes)
         res = {}
         ref = None
-        for prec, form in ((0, "fp64"), (1, "3xtf32")):
+        for prec, form in ((0, "fp64"), (1, "3xtf32"), (3, "fp32")):
             ms = timed(lambda: L.xgb_grouped_gemm(prec, G, arr, bufs[0], bufs[1], bufs[2], 1.0, 0.0, None))
             check(L.xgb_gemm_tc_status(), "tensor-core gemm")
             h = np.empty(int(co))
@@ -455,6 +456,176 @@ def gemm_sweep(reps=5):
             L.xgb_free(p_)
         out[f"synthetic_G{G}"] = dict(res, gflop=flops / 1e9)
     return out
+
+
+def config1_ops(seeds=(0, 1, 2, 3, 4), reps=20):
+    """The plain FP64 op chain on a U(1) Tensor<2,2> (every leg q = -2..2, deg [2, 4, 6, 4, 2]; 9 coupled
+    sectors, 17,712 doubles): T1*T2 -> permute<0>(0, 2, 1, 3) -> tSVD(16, 1e-10), N(0,1) entries per seed.
+    Device time per chain (CUDA events, `reps` chains after warm-up, plans cached) beside the numpy/OpenBLAS
+    oracle on the host cores; the largest |sigma| difference between the two."""
+    from xped_gb300 import Basis, Tensor, lib
+    import oracle
+    from oracle.convert import tensor_from_native
+    L = lib()
+    sym = oracle.make_symmetry("u1")
+    B = Basis.from_pairs("U1", [(-2, 2), (-1, 4), (0, 6), (1, 4), (2, 2)], sort=True)
+    gpu_ms, cpu_ms, err = [], [], 0.0
+    flops = None
+    for seed in seeds:
+        rng = np.random.default_rng(seed)
+        T1, T2 = Tensor.zeros([B, B], [B, B]), Tensor.zeros([B, B], [B, B])
+        T1.set_data(rng.standard_normal(T1.size))
+        T2.set_data(rng.standard_normal(T2.size))
+        if flops is None:
+            flops = sum(2.0 * d.m * d.n * d.k for d in T1.gemm_plan(T2)[0])
+
+        def chain():
+            return T1.matmul(T2).permute(0, [0, 2, 1, 3]).tSVD(16, 1e-10)
+        chain()
+        L.xgb_synchronize()
+        L.xgb_event_record(10)
+        for _ in range(reps):
+            out = chain()
+        L.xgb_event_record(11)
+        gpu_ms.append(L.xgb_event_elapsed_ms(10, 11) / reps)
+        o1, o2 = tensor_from_native(sym, T1), tensor_from_native(sym, T2)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            ref = (o1 * o2).permute(0, [0, 2, 1, 3]).tsvd(16, 1e-10)
+        cpu_ms.append((time.perf_counter() - t0) * 1e3 / reps)
+        got = np.sort(np.concatenate([np.diag(b) for b in out[1].blocks().values()]))
+        exp = np.sort(np.concatenate([np.diag(b) for b in ref[1].blocks]))
+        err = max(err, float(np.abs(got - exp).max() / exp.max()))
+    return {"gpu_ms_per_chain": float(np.median(gpu_ms)), "cpu_ms_per_chain": float(np.median(cpu_ms)),
+            "cpu": {"kind": "port", "cores": os.cpu_count(), "sample": f"{reps} chains per seed, median over seeds"},
+            "gemm_flop": flops, "sigma_max_rel_diff": err, "seeds": len(seeds)}
+
+
+def tsvd_sweep(eval_seeds=(0, 1, 2, 3, 4), train_seeds=tuple(range(100, 112)), steps=6, chi=128, p=3,
+               drift=0.02):
+    """Learned-width randomized tSVD on U(1) block matrices with power-law spectra (9-15 square sectors,
+    n log-uniform in [16, 1024], A_q = U_q diag(c_q (i+1)^-alpha_q s) V_q^T, Haar U_q / V_q, alpha in
+    {1, 2, 3}, c_q in [0.1, 1]); every sequence drifts its exponents by s = 1 + drift * t over `steps`
+    decompositions, like the projector matrices of consecutive CTM steps.  Step 0 is exact; steps >= 1
+    compare, with the previous step's exact result as history:
+      exact     the FP64 tSVD (one batched Jacobi launch),
+      history   randomized, widths last kept + max(16, 50 %),
+      learned   randomized, widths from the MLP trained (device Adam) on the train seeds' sequences
+    (p subspace iterations, chi = 128, eps 1e-10).  Reported per form: time (CUDA events), sketch columns,
+    sectors whose kept count differs from the exact one, largest kept-value error relative to the largest
+    value, saturated sectors; the CPU gesdd + cutoff_matrices time (oracle) of one matrix beside it."""
+    from xped_gb300 import Basis, Tensor, lib
+    from xped_gb300.learn import (RankModel, history_from_spectra, oversampling_label, sector_features,
+                                  widths_from_prediction)
+    from xped_gb300.workloads import power_law_sectors, power_law_spectra
+    L = lib()
+
+    def exact_keep(spectra):
+        vals = np.concatenate(spectra)
+        sec = np.concatenate([np.full(len(sp), a) for a, sp in enumerate(spectra)])
+        top = np.argsort(-vals, kind="stable")[:chi]
+        return np.bincount(sec[top], minlength=len(spectra))
+
+    def sequence(seed):
+        for t in range(steps):
+            sc = 1.0 + drift * t
+            secs = power_law_sectors(seed, exponent_scale=sc)
+            yield t, secs, power_law_spectra(secs, sc)
+
+    # training set: features from step t-1, labels from step t (known spectra, no decomposition needed)
+    X, T = [], []
+    for seed in train_seeds:
+        prev = None
+        for t, secs, spectra in sequence(seed):
+            keep = exact_keep(spectra)
+            if prev is not None:
+                ns = [n for _q, n, *_ in secs]
+                X.append(sector_features(ns, ns, chi, history_from_spectra(*prev)))
+                for sp, k, n in zip(spectra, keep, ns):
+                    T.append([np.log2(1.0 + k), np.log2(1.0 + oversampling_label(sp, int(k), n))])
+            prev = (spectra, keep)
+    X = np.concatenate(X).astype(np.float32)
+    T = np.asarray(T, np.float32)
+    model = RankModel(seed=SEED)
+    t0 = time.perf_counter()
+    loss0 = model.gradient(X, T)[0]
+    loss = model.train(X, T, steps=3000, lr=2e-3)
+    train = {"samples": int(X.shape[0]), "adam_steps": 3000, "loss_first": loss0, "loss_last": loss,
+             "seconds": time.perf_counter() - t0}
+
+    forms = ("exact", "history", "learned")
+    acc = {f: {"ms": 0.0, "sketch_cols": 0, "exact_cols": 0, "keep_mismatch": 0, "max_rel_err": 0.0,
+               "saturated": 0} for f in forms}
+    n_dec = n_sec = 0
+    cpu = None
+    for seed in eval_seeds:
+        prev = None
+        for t, secs, spectra in sequence(seed):
+            pairs = [(q, n) for q, n, *_ in secs]
+            B = Basis.from_pairs("U1", pairs, sort=True)
+            A = Tensor.zeros([B], [B])
+            A.set_data(np.concatenate([b.ravel(order="F") for *_r, b in secs]))
+            keep_true = exact_keep(spectra)
+            if prev is None:
+                prev = (spectra, keep_true)
+                continue
+            ns = [n for _q, n, *_ in secs]
+            hist = history_from_spectra(*prev)
+            widths = {"history": [h["keep"] + max(16, int(np.ceil(0.5 * h["keep"]))) for h in hist],
+                      "learned": widths_from_prediction(model.predict(sector_features(ns, ns, chi, hist)))}
+            ref_s = np.concatenate([sp[:k] for sp, k in zip(spectra, keep_true)])
+            for f in forms:
+                def run():
+                    if f == "exact":
+                        return A.tSVD(chi, 1e-10)
+                    return A.tSVD_randomized(chi, 1e-10, widths[f], p, seed=SEED)
+                if t == 1:
+                    run()  # build the plans (the structure is fixed along a sequence)
+                L.xgb_synchronize()
+                L.xgb_event_record(10)
+                out = run()
+                L.xgb_event_record(11)
+                acc[f]["ms"] += L.xgb_event_elapsed_ms(10, 11)
+                keep = out[5]
+                acc[f]["keep_mismatch"] += int(sum(int(a) != int(b) for a, b in zip(keep, keep_true)))
+                got = np.concatenate([np.diag(b) for b in out[1].blocks().values()])
+                if got.size == ref_s.size:
+                    acc[f]["max_rel_err"] = max(acc[f]["max_rel_err"],
+                                                float(np.abs(np.sort(got)[::-1] - np.sort(ref_s)[::-1]).max()
+                                                      / ref_s.max()))
+                else:
+                    acc[f]["max_rel_err"] = float("inf")
+                if f == "exact":
+                    acc[f]["exact_cols"] += sum(ns)
+                else:
+                    for w, n in zip(out[6], ns):
+                        if 0 < w and 2 * w < n:
+                            acc[f]["sketch_cols"] += int(w)
+                        else:
+                            acc[f]["exact_cols"] += n
+                    acc[f]["saturated"] += int(out[7])
+            n_dec += 1
+            n_sec += len(secs)
+            if cpu is None:
+                import oracle
+                from oracle.basis import Qbasis
+                sym = oracle.make_symmetry("u1")
+                oB = Qbasis.from_pairs(sym, pairs, sort=True)
+                ot = oracle.Tensor(sym, [oB], [oB], fill=False)
+                for q, _n, _a, _c, b in secs:
+                    ot.push_back(q, b)
+                t0 = time.perf_counter()
+                ot.tsvd(chi, 1e-10)
+                cpu = {"ms": (time.perf_counter() - t0) * 1e3, "cores": os.cpu_count(), "kind": "port",
+                       "sample": f"seed {seed} step {t}: numpy/OpenBLAS gesvd per sector + cutoff_matrices"}
+            prev = (spectra, keep_true)
+    res = {"decompositions": n_dec, "sectors": n_sec, "chi": chi, "power_iters": p, "drift": drift,
+           "train": train, "cpu_one_matrix": cpu}
+    for f in forms:
+        a = acc[f]
+        a["ms_per_decomposition"] = a.pop("ms") / n_dec
+        res[f] = a
+    return res
 
 
 def roofline(prof, steps):
@@ -561,6 +732,8 @@ def main():
                     help="steps of the plain FP64 form on the fz2 workload (0: skip)")
     ap.add_argument("--gemm-sweep-only", action="store_true",
                     help="run only the block-GEMM sweep and print it (for kernel profiling)")
+    ap.add_argument("--tsvd-sweep-only", action="store_true",
+                    help="run only the learned-width randomized tSVD sweep on power-law block matrices")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
@@ -592,6 +765,12 @@ def main():
     if args.workload == "fz2" and args.impl == "ours":
         if rank == 0:
             run_fz2(args)
+        return
+
+    if args.tsvd_sweep_only:
+        from xped_gb300 import ensure_device
+        ensure_device(local)
+        print(json.dumps({"tsvd_sweep": tsvd_sweep()}))
         return
 
     if args.gemm_sweep_only:
@@ -649,6 +828,7 @@ def main():
             line["learned_widths"]["energy_abs_diff_vs_plain"] = abs(r["e_learned"] - r["e_plain"])
     line["plain_fp64_D4_chi32_ms_per_step"] = r["small_plain_ms"]
     line["block_gemm_sweep"] = r["gemm_sweep"]
+    line["tensor22_chain"] = r["config1"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_from_device(r["ctm"])
     print(json.dumps(line))

@@ -53,7 +53,7 @@ enum {
 };
 
 /* precision forms of the block GEMM */
-enum { XGB_PREC_FP64 = 0, XGB_PREC_3XTF32 = 1, XGB_PREC_BF16X9 = 2 };
+enum { XGB_PREC_FP64 = 0, XGB_PREC_3XTF32 = 1, XGB_PREC_BF16X9 = 2, XGB_PREC_FP32 = 3 };
 
 /* ---------------------------------------------------------------- runtime */
 int xgb_init(int device);
@@ -93,7 +93,9 @@ typedef struct xgb_gemm_desc {
 /* C_g = alpha * op(A_g) op(B_g) + beta * C_g for every group g, one launch.
    precision XGB_PREC_FP64: FP64 FMA; XGB_PREC_3XTF32: FP64 in and out, products
    as three TF32 tensor-core products (hi*hi + hi*lo + lo*hi) accumulated in FP32
-   (about 1e-6 relative); XGB_PREC_BF16X9 is not available (XGB_E_UNSUPPORTED). */
+   (about 1e-6 relative); XGB_PREC_FP32: FP64 in and out, operands rounded to
+   FP32 and FP32 accumulation on the CUDA cores (about 1e-7 relative per product,
+   growing with k); XGB_PREC_BF16X9 is not available (XGB_E_UNSUPPORTED). */
 int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, const double* A, const double* B,
                      double* C, double alpha, double beta, void* stream);
 /* Synchronises and reports whether a tensor-core GEMM CTA gave up on a bounded

@@ -122,11 +122,11 @@ void xgb_ctm_release(xgb_ctm c);
    (exact for sectors not seen before); power_iters subspace iterations. */
 int xgb_ctm_set_svd(xgb_ctm c, int mode, int power_iters, uint64_t seed, int64_t oversample, double growth);
 /* Precision form of the block GEMMs behind xgb_tensor_matmul / xgb_tensor_contract
-   issued from the calling host thread: XGB_PREC_FP64 (default) or XGB_PREC_3XTF32
-   (xgb.h).  Selects what XPED_MATRIX_LIB selects for operator* in the reference. */
+   issued from the calling host thread: XGB_PREC_FP64 (default), XGB_PREC_3XTF32 or
+   XGB_PREC_FP32 (xgb.h).  Selects what XPED_MATRIX_LIB selects for operator* in the reference. */
 int xgb_set_gemm_precision(int precision);
 /* Precision form of the block GEMMs in the corner contractions and the
-   renormalisation of the moves (XGB_PREC_FP64 or XGB_PREC_3XTF32 from xgb.h);
+   renormalisation of the moves (XGB_PREC_FP64, XGB_PREC_3XTF32 or XGB_PREC_FP32);
    the projector SVD, the projector construction and the normalisation stay FP64. */
 int xgb_ctm_set_gemm_precision(xgb_ctm c, int precision);
 /* Sectors without history (the first decomposition of each direction) in the

@@ -218,7 +218,7 @@ PROTOS_EXTRA = [
 ]
 PROTOS.extend(PROTOS_EXTRA)
 
-KERNEL_KINDS = ["gemm_f64", "permute", "svd_jacobi", "truncate", "qr", "absmax", "scale", "copy2d", "diag", "gemm_tc", "sketch", "mlp"]
+KERNEL_KINDS = ["gemm_f64", "permute", "svd_jacobi", "truncate", "qr", "absmax", "scale", "copy2d", "diag", "gemm_tc", "sketch", "mlp", "gemm_f32"]
 
 
 def profile_read():

@@ -301,7 +301,7 @@ int xgb_ctm_set_svd(xgb_ctm c, int mode, int power_iters, uint64_t seed, int64_t
 
 int xgb_set_gemm_precision(int precision) {
   GUARD(XGB_E_BADPLAN, {
-    if (precision != XGB_PREC_FP64 && precision != XGB_PREC_3XTF32)
+    if (!gemm_precision_available(precision))
       return set_error(XGB_E_UNSUPPORTED, "GEMM precision form not available");
     set_gemm_precision(precision);
     return XGB_OK;
@@ -310,7 +310,7 @@ int xgb_set_gemm_precision(int precision) {
 
 int xgb_ctm_set_gemm_precision(xgb_ctm c, int precision) {
   GUARD(XGB_E_BADPLAN, {
-    if (precision != XGB_PREC_FP64 && precision != XGB_PREC_3XTF32)
+    if (!gemm_precision_available(precision))
       return set_error(XGB_E_UNSUPPORTED, "GEMM precision form not available");
     c->c->gemm_prec = precision;
     return XGB_OK;

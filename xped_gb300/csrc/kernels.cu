@@ -126,29 +126,31 @@ void prof_end(int kind, cudaStream_t s, double work) {
 }
 
 // ======================================================================= GEMM
-// FP64 grouped GEMM: C_g = alpha*op(A_g)op(B_g) + beta*C_g.  One CTA per
-// TILE x TILE output tile of one group; 256 threads, each owning a
-// (TILE/16)^2 micro-tile.  FP64 on GB300 runs on the narrow DFMA pipe, so the
-// host picks the tile edge that spreads the work over the most SMs.
-template <int TILE>
-__global__ void __launch_bounds__(256) gemm_f64_kernel(const xgb_gemm_desc* __restrict__ descs,
-                                                       const GemmTile* __restrict__ tiles, const double* __restrict__ A,
-                                                       const double* __restrict__ B, double* __restrict__ C, double alpha,
-                                                       double beta) {
+// Grouped GEMM on the CUDA cores: C_g = alpha*op(A_g)op(B_g) + beta*C_g.  One
+// CTA per TILE x TILE output tile of one group; 256 threads, each owning a
+// (TILE/16)^2 micro-tile.  T = double is the FP64 form (FP64 on GB300 runs on
+// the narrow DFMA pipe, so the host picks the tile edge that spreads the work
+// over the most SMs); T = float is the FP32 form (operands rounded to FP32 as
+// they are staged, FP32 accumulation, alpha/beta and the store in FP64).
+template <int TILE, typename T>
+__global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __restrict__ descs,
+                                                        const GemmTile* __restrict__ tiles, const double* __restrict__ A,
+                                                        const double* __restrict__ B, double* __restrict__ C,
+                                                        double alpha, double beta) {
   constexpr int BK = 16;
   constexpr int R = TILE / 16;
-  __shared__ double As[BK][TILE + 1];
-  __shared__ double Bs[BK][TILE + 1];
+  __shared__ T As[BK][TILE + 1];
+  __shared__ T Bs[BK][TILE + 1];
   const GemmTile t = tiles[blockIdx.x];
   const xgb_gemm_desc d = descs[t.g];
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int64_t row0 = int64_t(t.tm) * TILE, col0 = int64_t(t.tn) * TILE;
-  double acc[R][R];
+  T acc[R][R];
 #pragma unroll
   for (int i = 0; i < R; ++i)
 #pragma unroll
-    for (int j = 0; j < R; ++j) acc[i][j] = 0.0;
+    for (int j = 0; j < R; ++j) acc[i][j] = T(0);
 
   for (int64_t k0 = 0; k0 < d.k; k0 += BK) {
     // A tile: TILE rows x BK
@@ -158,7 +160,7 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const xgb_gemm_desc* __re
       int64_t gi = row0 + i, gk = k0 + kk;
       double v = 0.0;
       if (gi < d.m && gk < d.k) v = d.trans_a ? A[d.a_off + gk + gi * d.lda] : A[d.a_off + gi + gk * d.lda];
-      As[kk][i] = v;
+      As[kk][i] = T(v);
     }
     for (int e = tid; e < TILE * BK; e += 256) {
       int j, kk;
@@ -166,12 +168,12 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const xgb_gemm_desc* __re
       int64_t gj = col0 + j, gk = k0 + kk;
       double v = 0.0;
       if (gj < d.n && gk < d.k) v = d.trans_b ? B[d.b_off + gj + gk * d.ldb] : B[d.b_off + gk + gj * d.ldb];
-      Bs[kk][j] = v;
+      Bs[kk][j] = T(v);
     }
     __syncthreads();
     const int kmax = (d.k - k0) < BK ? int(d.k - k0) : BK;
     for (int kk = 0; kk < kmax; ++kk) {
-      double a[R], b[R];
+      T a[R], b[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) a[r] = As[kk][tx + 16 * r];
 #pragma unroll
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const xgb_gemm_desc* __re
       int64_t i = row0 + tx + 16 * r, j = col0 + ty + 16 * c;
       if (i < d.m && j < d.n) {
         double* p = C + d.c_off + i + j * d.ldc;
-        double v = alpha * acc[r][c];
+        double v = alpha * double(acc[r][c]);
         if (beta != 0.0) v += beta * (*p);
         *p = v;
       }
@@ -200,9 +202,18 @@ __global__ void __launch_bounds__(256) gemm_f64_kernel(const xgb_gemm_desc* __re
 void launch_gemm_f64(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
                      const double* B, double* C, double alpha, double beta, cudaStream_t s) {
   if (n_tiles <= 0) return;
-  if (tile == 64) gemm_f64_kernel<64><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
-  else if (tile == 32) gemm_f64_kernel<32><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
-  else gemm_f64_kernel<16><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
+  if (tile == 64) gemm_simt_kernel<64, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
+  else if (tile == 32) gemm_simt_kernel<32, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
+  else gemm_simt_kernel<16, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
+  count_launch();
+}
+
+void launch_gemm_f32(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
+                     const double* B, double* C, double alpha, double beta, cudaStream_t s) {
+  if (n_tiles <= 0) return;
+  if (tile == 64) gemm_simt_kernel<64, float><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
+  else if (tile == 32) gemm_simt_kernel<32, float><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
+  else gemm_simt_kernel<16, float><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
   count_launch();
 }
 
@@ -729,7 +740,7 @@ int xgb_memset_zero(void* dst, size_t bytes) {
 int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, const double* A, const double* B,
                      double* C, double alpha, double beta, void* stream_) {
   XGB_REQUIRE_INIT();
-  if (precision != XGB_PREC_FP64 && precision != XGB_PREC_3XTF32)
+  if (!gemm_precision_available(precision))
     return set_error(XGB_E_UNSUPPORTED, "precision form not available through this entry");
   if (n_groups < 0) return set_error(XGB_E_BADPLAN, "n_groups < 0");
   XGB_GUARD_BEGIN
@@ -765,7 +776,15 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
   if (tiles.empty()) return XGB_OK;
   auto* dd = upload(descs, size_t(n_groups), s);
   auto* dt = upload(tiles.data(), tiles.size(), s);
-  launch_gemm_f64(dd, dt, int(tiles.size()), tile, A, B, C, alpha, beta, s);
+  if (precision == XGB_PREC_FP32) {
+    double flops = 0;
+    for (int g = 0; g < n_groups; ++g) flops += 2.0 * double(descs[g].m) * double(descs[g].n) * double(descs[g].k);
+    prof_begin(K_GEMM_F32, s);
+    launch_gemm_f32(dd, dt, int(tiles.size()), tile, A, B, C, alpha, beta, s);
+    prof_end(K_GEMM_F32, s, flops);
+  } else {
+    launch_gemm_f64(dd, dt, int(tiles.size()), tile, A, B, C, alpha, beta, s);
+  }
   dev_free(dd);
   dev_free(dt);
   return check_cuda(cudaGetLastError(), "gemm launch");

@@ -31,6 +31,13 @@ double* scalar_scratch();
 // launchers (descriptor arrays are device pointers) -----------------------------------
 void launch_gemm_f64(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
                      const double* B, double* C, double alpha, double beta, cudaStream_t s);
+// FP32 form: same tiles, operands rounded to FP32, FP32 accumulation, FP64 store
+void launch_gemm_f32(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
+                     const double* B, double* C, double alpha, double beta, cudaStream_t s);
+// precision forms of the block GEMM this build implements (XGB_PREC_*)
+inline bool gemm_precision_available(int p) {
+  return p == XGB_PREC_FP64 || p == XGB_PREC_3XTF32 || p == XGB_PREC_FP32;
+}
 void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_task_start, int n_tasks, int64_t total,
                     const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s);
 void launch_svd(const xgb_svd_desc* d_descs, const int64_t* d_work_off, int n, int64_t max_k, const double* A, double* U,
@@ -107,7 +114,7 @@ void launch_mlp_reduce_adam(float* params, float* mom, float* vel, const float* 
 
 // per-kernel-kind instrumentation (CUDA events around each launch when enabled;
 // algorithmic work - flops for GEMMs, bytes for data movement - always counted)
-enum KernelKind { K_GEMM = 0, K_PERMUTE, K_SVD, K_TRUNC, K_QR, K_ABSMAX, K_SCALE, K_COPY2D, K_DIAG, K_GEMM_TC, K_SKETCH, K_MLP, K_COUNT };
+enum KernelKind { K_GEMM = 0, K_PERMUTE, K_SVD, K_TRUNC, K_QR, K_ABSMAX, K_SCALE, K_COPY2D, K_DIAG, K_GEMM_TC, K_SKETCH, K_MLP, K_GEMM_F32, K_COUNT };
 void prof_begin(int kind, cudaStream_t s);
 void prof_end(int kind, cudaStream_t s, double work);
 

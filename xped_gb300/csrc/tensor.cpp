@@ -597,6 +597,13 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
     dev_free(bp);
     return out;
   }
+  if (g_gemm_precision == XGB_PREC_FP32) {
+    prof_begin(K_GEMM_F32, stream());
+    launch_gemm_f32(plan->d_descs, plan->d_tiles, plan->n_tiles, plan->tile, a.data(), b.data(), out.data(), 1.0, 0.0,
+                    stream());
+    prof_end(K_GEMM_F32, stream(), plan->flops);
+    return out;
+  }
   prof_begin(K_GEMM, stream());
   launch_gemm_f64(plan->d_descs, plan->d_tiles, plan->n_tiles, plan->tile, a.data(), b.data(), out.data(), 1.0, 0.0, stream());
   prof_end(K_GEMM, stream(), plan->flops);
@@ -639,7 +646,7 @@ std::pair<Tensor, Tensor> matmul_backward(const Tensor& left, const Tensor& righ
 
 int gemm_precision() { return g_gemm_precision; }
 void set_gemm_precision(int prec) {
-  if (prec != XGB_PREC_FP64 && prec != XGB_PREC_3XTF32) throw std::runtime_error("unsupported GEMM precision form");
+  if (!gemm_precision_available(prec)) throw std::runtime_error("unsupported GEMM precision form");
   g_gemm_precision = prec;
 }
 

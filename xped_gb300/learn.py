@@ -162,3 +162,55 @@ def policy_outcome(records: List[Dict], widths, rho: float = RHO):
             elif wa < k + oversampling_label(r["spectrum"][a], k, kmin, rho):
                 under += 1
     return dict(columns=cols, saturated=sat, under_resolved=under, sketched=sketched, exact_columns=exact_cols)
+
+
+def sector_features(rows, cols, chi: int, hist=None) -> np.ndarray:
+    """The predictor's 8 features per sector, as the native ``sector_features``
+    (tensor.cpp) computes them in the CTM, for matrices decomposed outside it.
+    ``hist[i]`` is None (no history) or a dict with the sector's previous
+    ``keep``, ``s_first`` (largest value), ``s_last`` (last kept, 0 if none),
+    ``s_next`` (first dropped, 0 if none) and the matrix's ``s_max``."""
+    n = len(rows)
+    X = np.zeros((n, 8), np.float32)
+
+    def lg10(x, floor_):
+        return max(np.log10(x), floor_) if x > 0 else floor_
+
+    for i in range(n):
+        X[i, 0] = np.log2(1.0 + rows[i]) / 12.0
+        X[i, 1] = np.log2(1.0 + cols[i]) / 12.0
+        X[i, 7] = np.log2(1.0 + chi) / 8.0
+        h = None if hist is None else hist[i]
+        if h is None:
+            continue
+        smax = h["s_max"] if h["s_max"] > 0 else 1.0
+        X[i, 2] = 1.0
+        X[i, 3] = np.log2(1.0 + h["keep"]) / 8.0
+        X[i, 4] = lg10(h["s_first"] / smax, -16.0) / 16.0
+        X[i, 5] = lg10(h["s_last"] / smax, -16.0) / 16.0
+        X[i, 6] = (lg10(h["s_next"] / max(h["s_last"], 1e-300), -8.0) if h["keep"] > 0 and h["s_next"] > 0
+                   else -8.0) / 8.0
+    return X
+
+
+def history_from_spectra(spectra, keep):
+    """Per-sector history dicts (see ``sector_features``) from full descending
+    spectra and kept counts."""
+    smax = max((float(s[0]) for s in spectra if len(s)), default=0.0)
+    out = []
+    for s, k in zip(spectra, keep):
+        k = int(k)
+        out.append(dict(keep=k, s_first=float(s[0]) if len(s) else 0.0, s_last=float(s[k - 1]) if k > 0 else 0.0,
+                        s_next=float(s[k]) if k < len(s) else 0.0, s_max=smax))
+    return out
+
+
+def widths_from_prediction(Y: np.ndarray, margin: float = 0.0, min_oversample: int = 2):
+    """Sketch widths from predicted (log2(1+keep), log2(1+p)) rows, the rule
+    ``MlpPolicy`` applies in the CTM."""
+    w = []
+    for y0, y1 in np.asarray(Y, np.float64):
+        k = max(0.0, 2.0 ** y0 - 1.0)
+        p = max(0.0, 2.0 ** y1 - 1.0)
+        w.append(int(np.ceil(k * (1.0 + margin))) + max(min_oversample, int(np.ceil(p))))
+    return w

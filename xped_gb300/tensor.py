@@ -16,6 +16,7 @@ import numpy as np
 from ._lib import (PermContrib, PermTask, GemmDesc, check, check_handle, ensure_device, lib)
 
 SYM_IDS = {"U1": 0, "fU1": 1, "Z2": 2, "fZ2": 3, "SU2": 4}
+GEMM_FORMS = {"fp64": 0, "3xtf32": 1, "fp32": 3}  # XGB_PREC_* of xgb.h
 
 
 def _i32(seq):
@@ -377,9 +378,9 @@ class CTM:
         return {"refinements": n.value, "max_residual": r.value}
 
     def set_gemm(self, precision: str = "fp64"):
-        """Block GEMMs of the corner contractions / renormalisation: "fp64" or
-        "3xtf32" (tensor cores)."""
-        check(lib().xgb_ctm_set_gemm_precision(self._h, {"fp64": 0, "3xtf32": 1}[precision]), "ctm_set_gemm")
+        """Block GEMMs of the corner contractions / renormalisation: "fp64",
+        "3xtf32" (tensor cores) or "fp32"."""
+        check(lib().xgb_ctm_set_gemm_precision(self._h, GEMM_FORMS[precision]), "ctm_set_gemm")
         return self
 
     def set_rank_model(self, model, margin: float = 0.0, min_oversample: int = 2, power_iters: int = 3,
@@ -436,8 +437,8 @@ FEATURES = 8  # per-sector inputs of the rank predictor
 
 
 def set_gemm_precision(precision: str = "fp64"):
-    """Precision form of matmul / contract block GEMMs on this thread: "fp64" or "3xtf32"."""
-    check(lib().xgb_set_gemm_precision({"fp64": 0, "3xtf32": 1}[precision]), "set_gemm_precision")
+    """Precision form of matmul / contract block GEMMs on this thread: "fp64", "3xtf32" or "fp32"."""
+    check(lib().xgb_set_gemm_precision(GEMM_FORMS[precision]), "set_gemm_precision")
 
 
 def bond_expectation(rho: Tensor, op: Tensor) -> float:

@@ -16,8 +16,12 @@ def haar_orthogonal(rng: np.random.Generator, n: int) -> np.ndarray:
     return q * np.sign(np.where(np.diag(r) == 0, 1.0, np.diag(r)))
 
 
-def power_law_sectors(seed: int, n_sectors=(9, 15), size=(16, 1024), alphas=(1.0, 2.0, 3.0), scale=(0.1, 1.0)):
-    """Returns a list of (q, n, alpha, c, block) with charges q centred on 0."""
+def power_law_sectors(seed: int, n_sectors=(9, 15), size=(16, 1024), alphas=(1.0, 2.0, 3.0), scale=(0.1, 1.0),
+                      exponent_scale: float = 1.0):
+    """Returns a list of (q, n, alpha, c, block) with charges q centred on 0.
+    ``exponent_scale`` multiplies every exponent (same sizes, U_q, V_q and c_q
+    for a given seed): a sequence of seeds-fixed matrices whose spectra drift,
+    like the projector matrices of consecutive CTM steps."""
     rng = np.random.default_rng(seed)
     ns = int(rng.integers(n_sectors[0], n_sectors[1] + 1))
     lo, hi = np.log(size[0]), np.log(size[1])
@@ -27,8 +31,14 @@ def power_law_sectors(seed: int, n_sectors=(9, 15), size=(16, 1024), alphas=(1.0
         n = int(round(np.exp(rng.uniform(lo, hi))))
         alpha = float(rng.choice(alphas))
         c = float(rng.uniform(*scale))
-        s = c * np.arange(1, n + 1, dtype=np.float64) ** -alpha
+        s = c * np.arange(1, n + 1, dtype=np.float64) ** -(alpha * exponent_scale)
         U = haar_orthogonal(rng, n)
         V = haar_orthogonal(rng, n)
         out.append((q, n, alpha, c, (U * s) @ V.T))
     return out
+
+
+def power_law_spectra(secs, exponent_scale: float = 1.0):
+    """The exact singular values (descending) of each block of
+    ``power_law_sectors(..., exponent_scale)``."""
+    return [c * np.arange(1, n + 1, dtype=np.float64) ** -(alpha * exponent_scale) for _q, n, alpha, c, _b in secs]
