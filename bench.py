@@ -558,6 +558,28 @@ def tsvd_sweep(eval_seeds=(0, 1, 2, 3, 4), train_seeds=tuple(range(100, 112)), s
                "saturated": 0} for f in forms}
     n_dec = n_sec = 0
     cpu = None
+    vendor = []
+
+    def vendor_svd_ms(blocks):
+        """torch.linalg.svd (cuSOLVER, FP64) of every block, same GPU: a library reference point
+        for the exact per-sector SVD, not part of this library."""
+        import torch
+        dev = torch.device("cuda", torch.cuda.current_device())
+        tb = [torch.from_numpy(np.ascontiguousarray(b)).to(dev) for b in blocks]
+        out = {}
+        for drv in ("gesvd", "gesvdj"):
+            for b in tb[:2]:
+                torch.linalg.svd(b, full_matrices=False, driver=drv)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for b in tb:
+                torch.linalg.svd(b, full_matrices=False, driver=drv)
+            e1.record()
+            torch.cuda.synchronize()
+            out[drv] = e0.elapsed_time(e1)
+        return out
+
     for seed in eval_seeds:
         prev = None
         for t, secs, spectra in sequence(seed):
@@ -606,6 +628,8 @@ def tsvd_sweep(eval_seeds=(0, 1, 2, 3, 4), train_seeds=tuple(range(100, 112)), s
                     acc[f]["saturated"] += int(out[7])
             n_dec += 1
             n_sec += len(secs)
+            if seed == eval_seeds[0]:
+                vendor.append(vendor_svd_ms([b for *_r, b in secs]))
             if cpu is None:
                 import oracle
                 from oracle.basis import Qbasis
@@ -621,6 +645,11 @@ def tsvd_sweep(eval_seeds=(0, 1, 2, 3, 4), train_seeds=tuple(range(100, 112)), s
             prev = (spectra, keep_true)
     res = {"decompositions": n_dec, "sectors": n_sec, "chi": chi, "power_iters": p, "drift": drift,
            "train": train, "cpu_one_matrix": cpu}
+    if vendor:
+        res["torch_linalg_svd_ms_per_decomposition"] = {
+            k: float(np.mean([v[k] for v in vendor])) for k in vendor[0]}
+        res["torch_linalg_svd_sample"] = (f"seed {eval_seeds[0]}, {len(vendor)} matrices, full thin SVD of every "
+                                          "block (cuSOLVER through torch, FP64), no truncation")
     for f in forms:
         a = acc[f]
         a["ms_per_decomposition"] = a.pop("ms") / n_dec

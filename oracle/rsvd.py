@@ -52,27 +52,35 @@ def gaussian(seed: int, stream: int, count: int) -> np.ndarray:
 
 
 def _chol_pass(Y, shift):
-    """One CholeskyQR pass: Y R^-1 with R^T R = Y^T Y + shift * (m l + l (l + 1)) tr(Y^T Y) I;
-    a non-positive pivot is replaced by the smallest normal double."""
+    """One CholeskyQR pass: Y R^-1 with R^T R = Y^T Y + shift * (m l + l (l + 1)) tr(Y^T Y) I.
+    A pivot that is not above f = max(eps tr(Y^T Y) / l, 1e-300) (an exactly or
+    numerically rank-deficient Y) becomes sqrt(f) with the rest of its column
+    zeroed, so the factor stays finite and the direction is dropped."""
     m, l = Y.shape
     G = Y.T @ Y
-    s = shift * (m * l + l * (l + 1)) * np.trace(G)
+    tr = np.trace(G)
+    s = shift * (m * l + l * (l + 1)) * tr
+    floor = max(np.finfo(float).eps * (tr / l if tr > 0 else 0.0), 1e-300)
     L = np.zeros((l, l))
     for j in range(l):
         d = G[j, j] + s - L[j, :j] @ L[j, :j]
-        L[j, j] = np.sqrt(d) if d > 0 else np.sqrt(np.finfo(float).tiny)
-        L[j + 1:, j] = (G[j + 1:, j] - L[j + 1:, :j] @ L[j, :j]) / L[j, j]
+        if d > floor:
+            L[j, j] = np.sqrt(d)
+            L[j + 1:, j] = (G[j + 1:, j] - L[j + 1:, :j] @ L[j, :j]) / L[j, j]
+        else:
+            L[j, j] = np.sqrt(floor)
     return sla.solve_triangular(L, Y.T, lower=True).T  # Y L^-T
 
 
-def _orth(Y):
+def _orth(Y, passes=3):
     """Shifted CholeskyQR3 (Fukaya et al., SIAM J. Sci. Comput. 2020), as on
-    the device: one pass with shift 11 u, then two plain passes."""
+    the device: one pass with shift 11 u, then two plain passes (passes=3) or
+    one (passes=2, the bases between the products of a subspace iteration)."""
     if Y.size == 0:
         return Y.copy()
     Q = _chol_pass(Y, 11.0 * 2.0 ** -53)
     Q = _chol_pass(Q, 0.0)
-    return _chol_pass(Q, 0.0)
+    return _chol_pass(Q, 0.0) if passes == 3 else Q
 
 
 def sketch_svd(A, l, power_iters, seed, stream, warm_rows=None):
@@ -84,9 +92,9 @@ def sketch_svd(A, l, power_iters, seed, stream, warm_rows=None):
     if warm_rows is not None and warm_rows.shape[1] == n:
         kw = min(warm_rows.shape[0], l)
         Om[:, :kw] = warm_rows[:kw, :].T
-    Q = _orth(A @ Om)
-    for _ in range(power_iters):
-        Q = _orth(A @ _orth(A.T @ Q))
+    Q = _orth(A @ Om, 2 if power_iters > 0 else 3)
+    for it in range(power_iters):
+        Q = _orth(A @ _orth(A.T @ Q, 2), 3 if it + 1 == power_iters else 2)
     ub, s, vt = np.linalg.svd(Q.T @ A, full_matrices=False)
     u, vt = fix_svd_signs(Q @ ub, vt)
     return u, s, vt

@@ -136,13 +136,14 @@ template <int TILE, typename T>
 __global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __restrict__ descs,
                                                         const GemmTile* __restrict__ tiles, const double* __restrict__ A,
                                                         const double* __restrict__ B, double* __restrict__ C,
-                                                        double alpha, double beta) {
+                                                        double alpha, double beta, double* __restrict__ ws) {
   constexpr int BK = 16;
   constexpr int R = TILE / 16;
   __shared__ T As[BK][TILE + 1];
   __shared__ T Bs[BK][TILE + 1];
   const GemmTile t = tiles[blockIdx.x];
   const xgb_gemm_desc d = descs[t.g];
+  const int64_t kbeg = t.k0, kend = t.k1 < 0 ? d.k : t.k1;
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int64_t row0 = int64_t(t.tm) * TILE, col0 = int64_t(t.tn) * TILE;
@@ -152,14 +153,14 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __r
 #pragma unroll
     for (int j = 0; j < R; ++j) acc[i][j] = T(0);
 
-  for (int64_t k0 = 0; k0 < d.k; k0 += BK) {
+  for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
     // A tile: TILE rows x BK
     for (int e = tid; e < TILE * BK; e += 256) {
       int i, kk;
       if (d.trans_a) { kk = e % BK; i = e / BK; } else { i = e % TILE; kk = e / TILE; }
       int64_t gi = row0 + i, gk = k0 + kk;
       double v = 0.0;
-      if (gi < d.m && gk < d.k) v = d.trans_a ? A[d.a_off + gk + gi * d.lda] : A[d.a_off + gi + gk * d.lda];
+      if (gi < d.m && gk < kend) v = d.trans_a ? A[d.a_off + gk + gi * d.lda] : A[d.a_off + gi + gk * d.lda];
       As[kk][i] = T(v);
     }
     for (int e = tid; e < TILE * BK; e += 256) {
@@ -167,11 +168,11 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __r
       if (d.trans_b) { j = e % TILE; kk = e / TILE; } else { kk = e % BK; j = e / BK; }
       int64_t gj = col0 + j, gk = k0 + kk;
       double v = 0.0;
-      if (gj < d.n && gk < d.k) v = d.trans_b ? B[d.b_off + gj + gk * d.ldb] : B[d.b_off + gk + gj * d.ldb];
+      if (gj < d.n && gk < kend) v = d.trans_b ? B[d.b_off + gj + gk * d.ldb] : B[d.b_off + gk + gj * d.ldb];
       Bs[kk][j] = T(v);
     }
     __syncthreads();
-    const int kmax = (d.k - k0) < BK ? int(d.k - k0) : BK;
+    const int kmax = (kend - k0) < BK ? int(kend - k0) : BK;
     for (int kk = 0; kk < kmax; ++kk) {
       T a[R], b[R];
 #pragma unroll
@@ -184,6 +185,14 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __r
         for (int c = 0; c < R; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
     }
     __syncthreads();
+  }
+  if (t.slot >= 0) {  // split-K partial: the whole tile, raw sums, column-major TILE x TILE
+    double* w = ws + int64_t(t.slot) * TILE * TILE;
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+      for (int c = 0; c < R; ++c) w[(tx + 16 * r) + (ty + 16 * c) * TILE] = double(acc[r][c]);
+    return;
   }
 #pragma unroll
   for (int r = 0; r < R; ++r)
@@ -202,18 +211,52 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __r
 void launch_gemm_f64(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
                      const double* B, double* C, double alpha, double beta, cudaStream_t s) {
   if (n_tiles <= 0) return;
-  if (tile == 64) gemm_simt_kernel<64, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
-  else if (tile == 32) gemm_simt_kernel<32, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
-  else gemm_simt_kernel<16, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
+  if (tile == 64) gemm_simt_kernel<64, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, nullptr);
+  else if (tile == 32) gemm_simt_kernel<32, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, nullptr);
+  else gemm_simt_kernel<16, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, nullptr);
+  count_launch();
+}
+
+// C tile = alpha * (sum of its partial slots in slot order) + beta * C: the result does not
+// depend on which CTA finished first
+__global__ void __launch_bounds__(256) splitk_reduce_kernel(const xgb_gemm_desc* __restrict__ descs,
+                                                            const SplitReduce* __restrict__ red, int tile,
+                                                            const double* __restrict__ ws, double* __restrict__ C,
+                                                            double alpha, double beta) {
+  const SplitReduce r = red[blockIdx.x];
+  const xgb_gemm_desc d = descs[r.g];
+  const int64_t tt = int64_t(tile) * tile;
+  for (int64_t e = threadIdx.x; e < tt; e += blockDim.x) {
+    const int64_t i = int64_t(r.tm) * tile + e % tile, j = int64_t(r.tn) * tile + e / tile;
+    if (i >= d.m || j >= d.n) continue;
+    double acc = 0.0;
+    for (int p = 0; p < r.count; ++p) acc += ws[(int64_t(r.first) + p) * tt + e];
+    double* c = C + d.c_off + i + j * d.ldc;
+    double v = alpha * acc;
+    if (beta != 0.0) v += beta * (*c);
+    *c = v;
+  }
+}
+
+void launch_gemm_f64_splitk(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile,
+                            const SplitReduce* d_reduce, int n_reduce, const double* A, const double* B, double* C,
+                            double* ws, double alpha, double beta, cudaStream_t s) {
+  if (n_tiles <= 0) return;
+  if (tile == 64) gemm_simt_kernel<64, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, ws);
+  else if (tile == 32) gemm_simt_kernel<32, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, ws);
+  else gemm_simt_kernel<16, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, ws);
+  count_launch();
+  if (n_reduce <= 0) return;
+  splitk_reduce_kernel<<<n_reduce, 256, 0, s>>>(d_descs, d_reduce, tile, ws, C, alpha, beta);
   count_launch();
 }
 
 void launch_gemm_f32(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
                      const double* B, double* C, double alpha, double beta, cudaStream_t s) {
   if (n_tiles <= 0) return;
-  if (tile == 64) gemm_simt_kernel<64, float><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
-  else if (tile == 32) gemm_simt_kernel<32, float><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
-  else gemm_simt_kernel<16, float><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta);
+  if (tile == 64) gemm_simt_kernel<64, float><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, nullptr);
+  else if (tile == 32) gemm_simt_kernel<32, float><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, nullptr);
+  else gemm_simt_kernel<16, float><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, nullptr);
   count_launch();
 }
 

@@ -14,7 +14,15 @@
 
 namespace xgb {
 
-struct GemmTile { int32_t g, tm, tn, tile; };  // tile = edge length (16/32/64)
+// One output tile of a grouped GEMM: tile = edge length (16/32/64).  A split-K
+// tile covers k in [k0, k1) (k1 < 0: all of k) and stores its raw partial sum
+// into slot `slot` of a workspace (slot < 0: alpha/beta applied, stored in C).
+struct GemmTile {
+  int32_t g, tm, tn, tile;
+  int32_t k0 = 0, k1 = -1, slot = -1, pad = 0;
+};
+// Fixed-order sum of the partial slots [first, first + count) of one output tile.
+struct SplitReduce { int32_t g, tm, tn, first, count, pad; };
 
 // runtime ------------------------------------------------------------------------
 cudaStream_t stream();
@@ -31,6 +39,11 @@ double* scalar_scratch();
 // launchers (descriptor arrays are device pointers) -----------------------------------
 void launch_gemm_f64(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
                      const double* B, double* C, double alpha, double beta, cudaStream_t s);
+// split-K form: `tiles` may hold partial tiles (slot >= 0) writing TILE*TILE raw sums
+// into `ws`; `reduce` then adds the slots of each split output tile in slot order
+void launch_gemm_f64_splitk(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile,
+                            const SplitReduce* d_reduce, int n_reduce, const double* A, const double* B, double* C,
+                            double* ws, double alpha, double beta, cudaStream_t s);
 // FP32 form: same tiles, operands rounded to FP32, FP32 accumulation, FP64 store
 void launch_gemm_f32(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
                      const double* B, double* C, double alpha, double beta, cudaStream_t s);

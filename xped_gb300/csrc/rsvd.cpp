@@ -50,23 +50,55 @@ class Staging {
 
 double* alloc_d(int64_t n) { return static_cast<double*>(dev_alloc(sizeof(double) * size_t(std::max<int64_t>(n, 1)))); }
 
+// Grouped FP64 GEMM of the sketch pipeline.  When the output tiles cannot fill the SMs
+// (the l x l Gram matrices Y^T Y: few tiles, k = the block's row count) the k range of each
+// tile is split so that about two CTAs per SM run; the partial tiles land in a workspace and
+// one reduce launch adds them in a fixed order (deterministic result).
 void grouped_gemm(const std::vector<xgb_gemm_desc>& d, const double* A, const double* B, double* C, cudaStream_t s,
                   double alpha = 1.0, double beta = 0.0) {
   if (d.empty()) return;
   const int tile = choose_gemm_tile(d.data(), int(d.size()));
-  std::vector<GemmTile> tiles;
+  const int64_t target = 2 * int64_t(num_sms() > 0 ? num_sms() : 152);
+  int64_t n_out = 0;
   double flops = 0;
+  for (const auto& g : d) {
+    n_out += ((g.m + tile - 1) / tile) * ((g.n + tile - 1) / tile);
+    flops += 2.0 * double(g.m) * double(g.n) * double(g.k);
+  }
+  constexpr int64_t kMinChunk = 64;  // k per partial tile, multiple of the 16-deep k step
+  const int64_t want = n_out > 0 ? (target + n_out - 1) / n_out : 1;
+  std::vector<GemmTile> tiles;
+  std::vector<SplitReduce> red;
+  int32_t slots = 0;
   for (size_t g = 0; g < d.size(); ++g) {
     const int64_t tm = (d[g].m + tile - 1) / tile, tn = (d[g].n + tile - 1) / tile;
+    const int64_t splits = std::max<int64_t>(1, std::min<int64_t>(want, d[g].k / kMinChunk));
+    const int64_t chunk = splits > 1 ? (((d[g].k + splits - 1) / splits + 15) / 16) * 16 : d[g].k;
     for (int64_t y = 0; y < tn; ++y)
-      for (int64_t x = 0; x < tm; ++x) tiles.push_back({int32_t(g), int32_t(x), int32_t(y), tile});
-    flops += 2.0 * double(d[g].m) * double(d[g].n) * double(d[g].k);
+      for (int64_t x = 0; x < tm; ++x) {
+        if (splits == 1) {
+          tiles.push_back({int32_t(g), int32_t(x), int32_t(y), tile});
+          continue;
+        }
+        const int32_t first = slots;
+        for (int64_t k0 = 0; k0 < d[g].k; k0 += chunk)
+          tiles.push_back({int32_t(g), int32_t(x), int32_t(y), tile, int32_t(k0),
+                           int32_t(std::min<int64_t>(k0 + chunk, d[g].k)), slots++});
+        red.push_back({int32_t(g), int32_t(x), int32_t(y), first, slots - first, 0});
+      }
   }
   Staging st;
-  const size_t od = st.add(d), ot = st.add(tiles);
+  const size_t od = st.add(d), ot = st.add(tiles), orr = st.add(red);
   st.upload(s);
   prof_begin(K_GEMM, s);
-  launch_gemm_f64(st.at<xgb_gemm_desc>(od), st.at<GemmTile>(ot), int(tiles.size()), tile, A, B, C, alpha, beta, s);
+  if (red.empty()) {
+    launch_gemm_f64(st.at<xgb_gemm_desc>(od), st.at<GemmTile>(ot), int(tiles.size()), tile, A, B, C, alpha, beta, s);
+  } else {
+    double* ws = alloc_d(int64_t(slots) * tile * tile);
+    launch_gemm_f64_splitk(st.at<xgb_gemm_desc>(od), st.at<GemmTile>(ot), int(tiles.size()), tile,
+                           st.at<SplitReduce>(orr), int(red.size()), A, B, C, ws, alpha, beta, s);
+    dev_free(ws);
+  }
   prof_end(K_GEMM, s, flops);
 }
 
@@ -94,16 +126,20 @@ void batched_svd(const std::vector<xgb_svd_desc>& d, const double* A, double* U,
   dev_free(W);
 }
 
-// Orthonormal basis of each tall m x l block of Y into Q by shifted CholeskyQR3
-// (Fukaya, Kannan, Nakatsukasa, Yamamoto, Yanagisawa, SIAM J. Sci. Comput. 2020):
-// one shifted pass Q1 = Y chol(Y^T Y + s I)^-1, s = 11 (m l + l (l + 1)) u ||Y||_F^2,
-// then two plain CholeskyQR passes.  Every pass is two grouped FP64 GEMMs (Gram
-// matrix, Q R^-1) spread over all SMs plus one small Cholesky / triangular-inverse
-// launch (one CTA per block).  Y is used as scratch and holds garbage afterwards.
-void orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64_t>& cols, const std::vector<int64_t>& y_off,
-                    double* Y, double* Q, cudaStream_t s) {
+// Orthonormal basis of each tall m x l block of Y by shifted CholeskyQR3 (Fukaya,
+// Kannan, Nakatsukasa, Yamamoto, Yanagisawa, SIAM J. Sci. Comput. 2020): one
+// shifted pass Q1 = Y chol(Y^T Y + s I)^-1, s = 11 (m l + l (l + 1)) u ||Y||_F^2,
+// then two plain CholeskyQR passes (passes = 3), or one (passes = 2: the bases
+// between the products of a subspace iteration only have to stay well
+// conditioned; their span is what the iteration carries).  Every pass is two
+// grouped FP64 GEMMs (Gram matrix, Q R^-1) spread over all SMs plus one small
+// Cholesky / triangular-inverse launch (one CTA per block).  The passes alternate
+// between Y and Q; returns the buffer holding the basis (Q for 3 passes, Y for
+// 2); the other one holds garbage afterwards.
+double* orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64_t>& cols,
+                       const std::vector<int64_t>& y_off, double* Y, double* Q, cudaStream_t s, int passes = 3) {
   const size_t n = rows.size();
-  if (n == 0) return;
+  if (n == 0) return passes == 2 ? Y : Q;
   std::vector<CholDesc> cd;
   std::vector<xgb_gemm_desc> gram_y, gram_q, mul_yq, mul_qy;
   int64_t gt = 0;
@@ -135,14 +171,17 @@ void orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64_t>
   launch_chol_inv(sc.at<CholDesc>(o), int(n), G, Ri, 0.0, bad, s);
   prof_end(K_QR, s, 0.0);
   grouped_gemm(mul_qy, Q, Ri, Y, s);
-  grouped_gemm(gram_y, Y, Y, G, s);
-  prof_begin(K_QR, s);
-  launch_chol_inv(sc.at<CholDesc>(o), int(n), G, Ri, 0.0, bad, s);
-  prof_end(K_QR, s, 0.0);
-  grouped_gemm(mul_yq, Y, Ri, Q, s);
+  if (passes != 2) {
+    grouped_gemm(gram_y, Y, Y, G, s);
+    prof_begin(K_QR, s);
+    launch_chol_inv(sc.at<CholDesc>(o), int(n), G, Ri, 0.0, bad, s);
+    prof_end(K_QR, s, 0.0);
+    grouped_gemm(mul_yq, Y, Ri, Q, s);
+  }
   dev_free(G);
   dev_free(Ri);
   dev_free(bad);
+  return passes == 2 ? Y : Q;
 }
 
 constexpr int kMaxRetries = 3;
@@ -233,8 +272,9 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
     double* Y = nr ? alloc_d(yt) : nullptr;
     double* Z = nr ? alloc_d(zt) : nullptr;
 
-    // subspace iterations Q <- orth(A orth(A^T Q)) for the sketched sectors `sub` (indices into R)
-    auto iterate = [&](const std::vector<int>& sub, int iters) {
+    // subspace iterations Q <- orth(A orth(A^T Q)) for the sketched sectors `sub` (indices into R);
+    // the basis enters in `cur` (Q or Y) and leaves in Q (last orthonormalisation with 3 passes)
+    auto iterate = [&](const std::vector<int>& sub, int iters, double* cur) {
       std::vector<int64_t> srr, src, srl, syo, szo;
       for (int a : sub) {
         srr.push_back(rr[a]);
@@ -247,12 +287,13 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       for (int p = 0; p < iters; ++p) {
         g.clear();
         for (int a : sub) g.push_back({rc[a], rl[a], rr[a], m.offset[R[a]], rr[a], yo[a], rr[a], zo[a], rc[a], 1, 0});
-        grouped_gemm(g, t.data(), Q, Z, st);
-        orthonormalise(src, srl, szo, Z, Om, st);  // Omega's storage holds Qz (same layout as Z)
+        grouped_gemm(g, t.data(), cur, Z, st);
+        // Omega's storage holds Qz (same layout as Z)
+        double* qz = orthonormalise(src, srl, szo, Z, Om, st, 2);
         g.clear();
         for (int a : sub) g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], zo[a], rc[a], yo[a], rr[a], 0, 0});
-        grouped_gemm(g, t.data(), Om, Y, st);
-        orthonormalise(srr, srl, syo, Y, Q, st);
+        grouped_gemm(g, t.data(), qz, Y, st);
+        cur = orthonormalise(srr, srl, syo, Y, Q, st, p + 1 == iters ? 3 : 2);
       }
     };
     // Rayleigh-Ritz on span(Q) for `sub`: B = Q^T A, then (with the exact sectors `ex`) one
@@ -324,10 +365,10 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       for (int a = 0; a < nr; ++a)
         g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], om[a], rc[a], yo[a], rr[a], 0, 0});
       grouped_gemm(g, t.data(), Om, Y, st);
-      orthonormalise(rr, rl, yo, Y, Q, st);
+      double* q0 = orthonormalise(rr, rl, yo, Y, Q, st, power_iters > 0 ? 2 : 3);
       std::vector<int> all(nr);
       for (int a = 0; a < nr; ++a) all[a] = a;
-      iterate(all, power_iters);
+      iterate(all, power_iters, q0);
     }
     // ---- exact sectors: their blocks join the batched SVD of the projected blocks
     if (!E.empty()) {
@@ -398,7 +439,7 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       max_res = worst;
       if (bad.empty() || pass >= kMaxRefine) break;
       ++refinements;
-      iterate(bad, std::max(power_iters, 1));
+      iterate(bad, std::max(power_iters, 1), Q);
       project(bad, {});
       res = truncate_spectra(m, sp, max_keep, eps_svd, false);
     }
