@@ -458,6 +458,37 @@ def gemm_sweep(reps=5):
     return out
 
 
+def u1_product(degs, reps=10, form="fp64"):
+    """One grouped block GEMM T1*T2 of U(1) Tensor<2,2> operands whose legs carry charges centred on 0
+    with degeneracies `degs` (e.g. 6,12,16,12,6: coupled sectors up to 616 wide, as in the CTM
+    projector products); N(0,1) entries.  CUDA-event time per product after two warm-up products."""
+    from xped_gb300 import Basis, Tensor, lib
+    from xped_gb300.tensor import set_gemm_precision
+    L = lib()
+    qs = list(range(-(len(degs) // 2), len(degs) - len(degs) // 2))
+    B = Basis.from_pairs("U1", list(zip(qs, degs)), sort=True)
+    rng = np.random.default_rng(SEED)
+    T1, T2 = Tensor.zeros([B, B], [B, B]), Tensor.zeros([B, B], [B, B])
+    T1.set_data(rng.standard_normal(T1.size))
+    T2.set_data(rng.standard_normal(T2.size))
+    descs = T1.gemm_plan(T2)[0]
+    flops = sum(2.0 * d.m * d.n * d.k for d in descs)
+    set_gemm_precision(form)
+    try:
+        for _ in range(2):
+            T1.matmul(T2)
+        L.xgb_synchronize()
+        L.xgb_event_record(10)
+        for _ in range(reps):
+            T1.matmul(T2)
+        L.xgb_event_record(11)
+        ms = L.xgb_event_elapsed_ms(10, 11) / reps
+    finally:
+        set_gemm_precision("fp64")
+    return {"degs": list(degs), "form": form, "blocks": [d.m for d in descs], "gflop": flops / 1e9, "ms": ms,
+            "tflops": flops / (ms * 1e-3) / 1e12}
+
+
 def config1_ops(seeds=(0, 1, 2, 3, 4), reps=20):
     """The plain FP64 op chain on a U(1) Tensor<2,2> (every leg q = -2..2, deg [2, 4, 6, 4, 2]; 9 coupled
     sectors, 17,712 doubles): T1*T2 -> permute<0>(0, 2, 1, 3) -> tSVD(16, 1e-10), N(0,1) entries per seed.
@@ -751,7 +782,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--gemm", default="fp64", choices=["fp64", "3xtf32"])
+    ap.add_argument("--gemm", default="fp64", choices=["fp64", "3xtf32", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-width run")
@@ -761,6 +792,9 @@ def main():
                     help="steps of the plain FP64 form on the fz2 workload (0: skip)")
     ap.add_argument("--gemm-sweep-only", action="store_true",
                     help="run only the block-GEMM sweep and print it (for kernel profiling)")
+    ap.add_argument("--u1-product", default=None, metavar="DEGS",
+                    help="time only T1*T2 of U(1) Tensor<2,2> operands with these leg degeneracies (e.g. 6,12,16,12,6)")
+    ap.add_argument("--reps", type=int, default=10, help="products timed by --u1-product")
     ap.add_argument("--tsvd-sweep-only", action="store_true",
                     help="run only the learned-width randomized tSVD sweep on power-law block matrices")
     args = ap.parse_args()
@@ -796,6 +830,13 @@ def main():
             run_fz2(args)
         return
 
+    if args.u1_product:
+        from xped_gb300 import ensure_device
+        ensure_device(local)
+        print(json.dumps({"u1_product": u1_product([int(x) for x in args.u1_product.split(",")], args.reps,
+                                                     args.gemm)}))
+        return
+
     if args.tsvd_sweep_only:
         from xped_gb300 import ensure_device
         ensure_device(local)
@@ -824,11 +865,11 @@ def main():
         return
     value = world * 1e3 / t_step
     prof = r["prof"]
-    gemm_kind = "gemm_tc" if args.gemm == "3xtf32" else "gemm_f64"
+    gemm_kind = {"3xtf32": "gemm_tc", "fp32": "gemm_f32"}.get(args.gemm, "gemm_f64")
     g = prof.get(gemm_kind, (0, 0.0, 0.0))
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if args.gemm == "fp64" else "f64 (3xtf32 block GEMMs)",
+            "vs_baseline": None, "dtype": "f64" if args.gemm == "fp64" else f"f64 ({args.gemm} block GEMMs)",
             "data": "synthetic (seeded N(0,1) site tensor)",
             "config": dict(config, form=f"chosen: randomized projector SVD ({POWER_ITERS} subspace iterations, "
                                         "CholeskyQR3 bases, widths last kept + max(16, 50%), exact first decomposition "

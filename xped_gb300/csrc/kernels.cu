@@ -260,6 +260,12 @@ void launch_gemm_f32(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int 
   count_launch();
 }
 
+void order_tiles_by_work(std::vector<GemmTile>& tiles, const xgb_gemm_desc* descs) {
+  auto extent = [&](const GemmTile& t) { return int64_t(t.k1 < 0 ? descs[t.g].k : t.k1) - t.k0; };
+  std::stable_sort(tiles.begin(), tiles.end(),
+                   [&](const GemmTile& a, const GemmTile& b) { return extent(a) > extent(b); });
+}
+
 int choose_gemm_tile(const xgb_gemm_desc* descs, int n) {
   // Largest tile edge that still yields >= 2 CTAs per SM; FP64 throughput is
   // per SM, so spreading tiles over SMs beats bigger tiles' reuse here.
@@ -817,6 +823,7 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
       for (int64_t i = 0; i < tm; ++i) tiles.push_back({g, int32_t(i), int32_t(j), tile});
   }
   if (tiles.empty()) return XGB_OK;
+  order_tiles_by_work(tiles, descs);
   auto* dd = upload(descs, size_t(n_groups), s);
   auto* dt = upload(tiles.data(), tiles.size(), s);
   if (precision == XGB_PREC_FP32) {

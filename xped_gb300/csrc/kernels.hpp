@@ -23,6 +23,10 @@ struct GemmTile {
 };
 // Fixed-order sum of the partial slots [first, first + count) of one output tile.
 struct SplitReduce { int32_t g, tm, tn, first, count, pad; };
+// Tiles in descending k extent: the block scheduler hands out CTAs in index
+// order, so the longest tiles start first and the short ones fill the gaps
+// (longest-processing-time-first) instead of a long tile starting last.
+void order_tiles_by_work(std::vector<GemmTile>& tiles, const xgb_gemm_desc* descs);
 
 // runtime ------------------------------------------------------------------------
 cudaStream_t stream();
@@ -95,7 +99,7 @@ void launch_gauss_fill(const GaussBlock* d_blocks, int n_blocks, int64_t max_cou
 void launch_sign_fix(const SignFixDesc* d_descs, int n, int64_t max_k, double* U, double* Vt, cudaStream_t s);
 // CholeskyQR helper (rsvd.cu): per sketch block m x l, Gram matrix l x l at g_off
 struct CholDesc { int64_t m, l, g_off; };
-void launch_chol_inv(const CholDesc* d_descs, int n, double* G, double* Rinv, double rel_shift, int* bad,
+void launch_chol_inv(const CholDesc* d_descs, int n, int64_t max_l, double* G, double* Rinv, double rel_shift, int* bad,
                      cudaStream_t s);
 // SVD reverse rule helpers (rsvd.cu): per sector m x n block with k singular values;
 // offsets of U / dU (m x k), the k x k diagonal S block, dS (k x k, ld ds_ld), V^dag / dV^dag (k x n),

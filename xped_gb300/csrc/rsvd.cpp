@@ -87,6 +87,7 @@ void grouped_gemm(const std::vector<xgb_gemm_desc>& d, const double* A, const do
         red.push_back({int32_t(g), int32_t(x), int32_t(y), first, slots - first, 0});
       }
   }
+  order_tiles_by_work(tiles, d.data());
   Staging st;
   const size_t od = st.add(d), ot = st.add(tiles), orr = st.add(red);
   st.upload(s);
@@ -143,8 +144,10 @@ double* orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64
   std::vector<CholDesc> cd;
   std::vector<xgb_gemm_desc> gram_y, gram_q, mul_yq, mul_qy;
   int64_t gt = 0;
+  int64_t max_l = 0;
   for (size_t i = 0; i < n; ++i) {
     const int64_t m = rows[i], l = cols[i];
+    max_l = std::max(max_l, l);
     cd.push_back({m, l, gt});
     gram_y.push_back({l, l, m, y_off[i], m, y_off[i], m, gt, l, 1, 0});  // G = Y^T Y
     gram_q.push_back({l, l, m, y_off[i], m, y_off[i], m, gt, l, 1, 0});  // same layout for Q
@@ -163,18 +166,18 @@ double* orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64
   // pass 1 (shifted): Y -> Q;  pass 2: Q -> Y;  pass 3: Y -> Q
   grouped_gemm(gram_y, Y, Y, G, s);
   prof_begin(K_QR, s);
-  launch_chol_inv(sc.at<CholDesc>(o), int(n), G, Ri, kShift, bad, s);
+  launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, kShift, bad, s);
   prof_end(K_QR, s, 0.0);
   grouped_gemm(mul_yq, Y, Ri, Q, s);
   grouped_gemm(gram_q, Q, Q, G, s);
   prof_begin(K_QR, s);
-  launch_chol_inv(sc.at<CholDesc>(o), int(n), G, Ri, 0.0, bad, s);
+  launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, 0.0, bad, s);
   prof_end(K_QR, s, 0.0);
   grouped_gemm(mul_qy, Q, Ri, Y, s);
   if (passes != 2) {
     grouped_gemm(gram_y, Y, Y, G, s);
     prof_begin(K_QR, s);
-    launch_chol_inv(sc.at<CholDesc>(o), int(n), G, Ri, 0.0, bad, s);
+    launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, 0.0, bad, s);
     prof_end(K_QR, s, 0.0);
     grouped_gemm(mul_yq, Y, Ri, Q, s);
   }

@@ -171,7 +171,10 @@ __global__ void svd_bwd_scale_kernel(const SvdBwdDesc* __restrict__ descs, const
 // identity (X <- rows of L^-1 as they are finished).  Matrices live in shared
 // memory, row-major with an odd leading dimension, when two of them fit;
 // larger blocks use the same loops on global memory.
-template <bool kShared>
+//
+// kInverse = false: the Cholesky factor only; L (lower triangle and diagonal) is
+// left column-major in G for trinv_kernel, which forms L^-1 with many CTAs.
+template <bool kShared, bool kInverse>
 __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double* __restrict__ Xg, double rel_shift,
                               int* __restrict__ bad, double* sm) {
   const int l = int(d.l), tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
@@ -185,7 +188,8 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   __shared__ double bcast;
   if (kShared)
     for (int e = tid; e < l * l; e += nt) LA(e % l, e / l) = Gg[e];
-  for (int e = tid; e < l * l; e += nt) XA(e % l, e / l) = (e % l == e / l) ? 1.0 : 0.0;
+  if (kInverse)
+    for (int e = tid; e < l * l; e += nt) XA(e % l, e / l) = (e % l == e / l) ? 1.0 : 0.0;
   __syncthreads();
   double tr = 0;
   for (int i = tid; i < l; i += nt) tr += LA(i, i);
@@ -206,15 +210,21 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   for (int i = tid; i < l; i += nt) LA(i, i) += shift;
   __syncthreads();
   // Cholesky (right-looking), lower triangle in place
+  // The reciprocal of each pivot is formed once (thread 0) and broadcast through shared memory:
+  // an FP64 division is a multi-instruction DFMA sequence, and on GB300's narrow FP64 pipe 1024
+  // threads each dividing cost ~2 us per column.
+  __shared__ double inv_s;
   for (int j = 0; j < l; ++j) {
     if (tid == 0) {
       const double dj = LA(j, j);
       dead = !(dj > dfloor);  // also true for NaN
       if (dead) atomicAdd(bad, 1);
-      LA(j, j) = sqrt(dead ? dfloor : dj);
+      const double p = sqrt(dead ? dfloor : dj);
+      LA(j, j) = p;
+      inv_s = 1.0 / p;
     }
     __syncthreads();
-    const double inv = 1.0 / LA(j, j);
+    const double inv = inv_s;
     const bool zero_col = dead != 0;
     for (int i = j + 1 + tid; i < l; i += nt) LA(i, j) = zero_col ? 0.0 : LA(i, j) * inv;
     __syncthreads();
@@ -237,10 +247,20 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
     }
     __syncthreads();
   }
+  if (!kInverse) {
+    if (kShared)  // L back to G, column-major, lower triangle and diagonal
+      for (int e = tid; e < l * l; e += nt) {
+        const int i = e % l, k = e / l;
+        if (i >= k) Gg[e] = LA(i, k);
+      }
+    return;
+  }
   // X = L^-1 by forward elimination of the identity: row j of X is final after
   // dividing by L[j][j]; then rows i > j subtract L[i][j] * row j (columns c <= j)
   for (int j = 0; j < l; ++j) {
-    const double inv = 1.0 / LA(j, j);
+    if (tid == 0) inv_s = 1.0 / LA(j, j);
+    __syncthreads();
+    const double inv = inv_s;
     for (int c = tid; c <= j; c += nt) XA(j, c) *= inv;
     __syncthreads();
     const int t = l - j - 1;
@@ -268,31 +288,102 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   }
 }
 
+template <bool kInverse>
 __global__ void __launch_bounds__(1024) chol_inv_kernel(const CholDesc* __restrict__ descs, double* __restrict__ G,
                                                       double* __restrict__ Rinv, double rel_shift,
                                                       int* __restrict__ bad, int smem_cap_l) {
   extern __shared__ double sm[];
   const CholDesc d = descs[blockIdx.x];
   if (d.l <= smem_cap_l)
-    chol_inv_body<true>(d, G + d.g_off, Rinv + d.g_off, rel_shift, bad, sm);
+    chol_inv_body<true, kInverse>(d, G + d.g_off, Rinv + d.g_off, rel_shift, bad, sm);
   else
-    chol_inv_body<false>(d, G + d.g_off, Rinv + d.g_off, rel_shift, bad, sm);
+    chol_inv_body<false, kInverse>(d, G + d.g_off, Rinv + d.g_off, rel_shift, bad, sm);
+}
+
+// Rinv = L^-T from the Cholesky factor L (column-major, lower triangle, in G): one warp per
+// column c of X = L^-1, kTrinvCols columns per CTA, so the l^3/6 FMAs of a block spread over
+// ceil(l / kTrinvCols) SMs.  Column c by forward substitution in the same operation order as
+// the single-CTA elimination (x_k = r_k * (1 / L_kk), then r_i -= L_ik x_k for i > k), so
+// both give the same bits; lane t keeps r_i for i = t + 32 j in registers (j < T).
+constexpr int kTrinvCols = 8;
+template <int T>
+__global__ void __launch_bounds__(32 * kTrinvCols) trinv_kernel(const CholDesc* __restrict__ descs, int chunks,
+                                                                 const double* __restrict__ G,
+                                                                 double* __restrict__ Rinv) {
+  extern __shared__ double inv_diag[];
+  const int sector = blockIdx.x / chunks, c0 = (blockIdx.x % chunks) * kTrinvCols;
+  const CholDesc d = descs[sector];
+  const int l = int(d.l);
+  if (c0 >= l) return;  // uniform over the CTA
+  const double* L = G + d.g_off;
+  double* R = Rinv + d.g_off;
+  for (int k = c0 + int(threadIdx.x); k < l; k += blockDim.x) inv_diag[k - c0] = 1.0 / L[k + int64_t(k) * l];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, c = c0 + int(threadIdx.x >> 5);
+  if (c >= l) return;
+  double r[T];
+#pragma unroll
+  for (int j = 0; j < T; ++j) r[j] = (lane + 32 * j == c) ? 1.0 : 0.0;
+  for (int k = c; k < l; ++k) {
+    const int slot = k >> 5;
+    double v = 0.0;
+#pragma unroll
+    for (int j = 0; j < T; ++j)
+      if (j == slot) v = r[j];
+    const double xk = __shfl_sync(0xffffffffu, v, k & 31) * inv_diag[k - c0];
+    const double* Lk = L + int64_t(k) * l;
+#pragma unroll
+    for (int j = 0; j < T; ++j) {
+      const int i = lane + 32 * j;
+      if (i == k) r[j] = xk;
+      else if (i > k && i < l) r[j] = fma(-__ldg(Lk + i), xk, r[j]);
+    }
+  }
+  // row c of Rinv (= column c of X): Rinv[c + i l] = X[i][c], zero for i < c
+#pragma unroll
+  for (int j = 0; j < T; ++j) {
+    const int i = lane + 32 * j;
+    if (i < l) R[c + int64_t(i) * l] = i >= c ? r[j] : 0.0;
+  }
 }
 
 }  // namespace
 
-void launch_chol_inv(const CholDesc* d_descs, int n, double* G, double* Rinv, double rel_shift, int* bad,
-                     cudaStream_t s) {
-  if (n <= 0) return;
-  // two l x (l | 1) double matrices in shared memory up to l = 119 (< 227 KB)
-  constexpr int kCapL = 119;
+void launch_chol_inv(const CholDesc* d_descs, int n, int64_t max_l, double* G, double* Rinv, double rel_shift,
+                     int* bad, cudaStream_t s) {
+  if (n <= 0 || max_l <= 0) return;
   static bool attr = false;
-  const int bytes = 2 * kCapL * (kCapL | 1) * int(sizeof(double));
+  // Cholesky alone: one l x (l | 1) matrix in shared memory up to l = 167 (< 227 KB)
+  constexpr int kCapChol = 167;
+  // Cholesky and inverse in one CTA (blocks wider than the register-resident inverse allows):
+  // two matrices up to l = 119
+  constexpr int kCapBoth = 119;
+  constexpr int kBytesChol = kCapChol * (kCapChol | 1) * int(sizeof(double));
+  constexpr int kBytesBoth = 2 * kCapBoth * (kCapBoth | 1) * int(sizeof(double));
   if (!attr) {
-    cudaFuncSetAttribute(chol_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(chol_inv_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBytesChol);
+    cudaFuncSetAttribute(chol_inv_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBytesBoth);
     attr = true;
   }
-  chol_inv_kernel<<<n, 1024, bytes, s>>>(d_descs, G, Rinv, rel_shift, bad, kCapL);
+  if (max_l > 64 * 32) {
+    chol_inv_kernel<true><<<n, 1024, kBytesBoth, s>>>(d_descs, G, Rinv, rel_shift, bad, kCapBoth);
+    count_launch();
+    return;
+  }
+  const int lc = int(std::min<int64_t>(max_l, kCapChol));
+  chol_inv_kernel<false><<<n, 1024, lc * (lc | 1) * int(sizeof(double)), s>>>(d_descs, G, Rinv, rel_shift, bad,
+                                                                                kCapChol);
+  count_launch();
+  const int chunks = int((max_l + kTrinvCols - 1) / kTrinvCols);
+  const size_t sm = sizeof(double) * size_t(max_l);
+  if (max_l <= 256)
+    trinv_kernel<8><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
+  else if (max_l <= 512)
+    trinv_kernel<16><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
+  else if (max_l <= 1024)
+    trinv_kernel<32><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
+  else
+    trinv_kernel<64><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
   count_launch();
 }
 

@@ -562,6 +562,7 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
       for (int64_t y = 0; y < tn; ++y)
         for (int64_t x = 0; x < tm; ++x) tiles.push_back({int32_t(g), int32_t(x), int32_t(y), plan->tile});
     }
+    order_tiles_by_work(tiles, descs.data());
     plan->n_tiles = int(tiles.size());
     plan->host_descs = descs;
     plan->d_descs = dev_table(descs);
