@@ -301,6 +301,7 @@ def run_gpu(args):
     L.xgb_free(flush)
     res["gemm_sweep"] = gemm_sweep()
     res["config1"] = config1_ops()
+    res["su"] = su_step()
     return res
 
 
@@ -456,6 +457,57 @@ def gemm_sweep(reps=5):
             L.xgb_free(p_)
         out[f"synthetic_G{G}"] = dict(res, gflop=flops / 1e9)
     return out
+
+
+def su_step(steps=3, D=6, tau=0.05):
+    """Simple-update imaginary-time steps (TimePropagator::t_step: 8 bond updates, each two full
+    tSVDs and one truncated to D) of a U(1) spin-1/2 Heisenberg iPEPS on the checkerboard cell
+    [[0, 1], [1, 0]]: virtual q -1,0,1 with degeneracies [2,2,2] (D = 6), N(0,1) site tensors,
+    gates exp(-tau H).  Device time per step (CUDA events) beside the numpy oracle on the host
+    cores; the largest weight difference between the two after `steps` steps."""
+    import oracle
+    from oracle.basis import Qbasis
+    from oracle.ctm import IPEPS, heisenberg_u1
+    from oracle.simple_update import SimpleUpdate as OSU
+    from oracle.simple_update import gate
+    from xped_gb300 import Basis, SimpleUpdate, Tensor, lib
+    L = lib()
+    s = oracle.make_symmetry("u1")
+    aux_p, phys_p = [(-1, 2), (0, 2), (1, 2)], [(-1, 1), (1, 1)]
+    oaux, ophys = Qbasis.from_pairs(s, aux_p), Qbasis.from_pairs(s, phys_p)
+    naux, nphys = Basis.from_pairs("U1", aux_p), Basis.from_pairs("U1", phys_p)
+    rng = np.random.default_rng(SEED)
+    oG = [IPEPS(s, oaux, ophys).set_random(rng).A for _ in range(2)]
+    nG = []
+    for g in oG:
+        t = Tensor.zeros([naux, naux], [naux, naux, nphys])
+        t.set_data(g.data())
+        nG.append(t)
+    U = gate(heisenberg_u1(s, ophys), tau)
+    nU = Tensor.zeros([nphys, nphys], [nphys, nphys])
+    nU.set_data(U.data())
+    pat = [[0, 1], [1, 0]]
+    nsu = SimpleUpdate(pat, nG, D)
+    nsu.step(nU, nU)  # plans
+    ms = []
+    for _ in range(steps):
+        L.xgb_synchronize()
+        L.xgb_event_record(10)
+        nsu.step(nU, nU)
+        L.xgb_event_record(11)
+        ms.append(L.xgb_event_elapsed_ms(10, 11))
+    osu = OSU(pat, oG, D)
+    t0 = time.perf_counter()
+    for _ in range(steps + 1):
+        osu.step(U, U)
+    cpu_ms = (time.perf_counter() - t0) * 1e3 / (steps + 1)
+    err = 0.0
+    for i in range(2):
+        for name, ow in (("wh", osu.wh[i]), ("wv", osu.wv[i])):
+            err = max(err, float(np.abs(nsu.get(name, i).data() - ow.data()).max()))
+    return {"gpu_ms_per_step": float(np.median(ms)), "cpu_ms_per_step": cpu_ms, "cores": os.cpu_count(),
+            "D": D, "steps": steps + 1, "weights_max_abs_diff": err,
+            "workload": "checkerboard U(1) Heisenberg, q -1,0,1 deg [2,2,2], tau 0.05"}
 
 
 def u1_product(degs, reps=10, form="fp64"):
@@ -899,6 +951,7 @@ def main():
     line["plain_fp64_D4_chi32_ms_per_step"] = r["small_plain_ms"]
     line["block_gemm_sweep"] = r["gemm_sweep"]
     line["tensor22_chain"] = r["config1"]
+    line["simple_update_step"] = r["su"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_from_device(r["ctm"])
     print(json.dumps(line))

@@ -24,6 +24,7 @@ typedef struct xgb_basis_s* xgb_basis;
 typedef struct xgb_tensor_s* xgb_tensor;
 typedef struct xgb_ctm_s* xgb_ctm;
 typedef struct xgb_rank_model_s* xgb_rank_model;
+typedef struct xgb_su_s* xgb_su;
 
 /* symmetry kinds */
 enum { XGB_SYM_U1 = 0, XGB_SYM_U1_FERMIONIC = 1, XGB_SYM_Z2 = 2, XGB_SYM_Z2_FERMIONIC = 3, XGB_SYM_SU2 = 4 };
@@ -116,6 +117,27 @@ int xgb_ctm_move(xgb_ctm c, char dir);                      /* 'L','R','T','B' m
 xgb_tensor xgb_ctm_get(xgb_ctm c, int which);
 int xgb_ctm_set(xgb_ctm c, int which, xgb_tensor t);
 void xgb_ctm_release(xgb_ctm c);
+
+/* ----------------------------------------------------------- simple update */
+/* Simple-update imaginary-time evolution of an iPEPS with nearest-neighbour gates
+   (TimePropagator::t_step / t_step_h / t_step_v, src/PEPS/TimePropagator.cpp:7-215;
+   SimpleUpdate::renormalize, src/PEPS/SimpleUpdate.cpp:5-14).  Unit cell: Lx x Ly
+   labels, labels[x * Ly + y] = data[x][y] of the reference's Pattern (periodic;
+   site i sits at (i % Lx, i / Lx)); neighbouring sites must differ (the reference
+   asserts it, TimePropagator.cpp:86-87, 93-94).  G[label]: Tensor<2,3> (left, top |
+   right, bottom, phys); bond weights start as identities (iPEPS::initWeightTensors,
+   src/PEPS/iPEPS.cpp:575-592); D: bond dimension kept by the bond tSVD (eps 1e-14).
+   Gates Uh, Uv: Tensor<2,2> on (phys, phys), e.g. exp(-dt H) (TimePropagator::initU,
+   TimePropagator.cpp:453-487), the same on every bond of their direction. */
+xgb_su xgb_su_create(int Lx, int Ly, const int* labels, int n_sites, const xgb_tensor* G, int64_t D);
+int xgb_su_step(xgb_su s, xgb_tensor Uh, xgb_tensor Uv);    /* t_step (TimePropagator.cpp:83-109) */
+int xgb_su_step_h(xgb_su s, int x, int y, xgb_tensor Uh);   /* t_step_h: bond (x, y) - (x+1, y) */
+int xgb_su_step_v(xgb_su s, int x, int y, xgb_tensor Uv);   /* t_step_v: bond (x, y-1) - (x, y) */
+/* which: 0 = G, 1 = horizontal weight (right leg), 2 = vertical weight (top leg) of
+   label `site`; 3 = site tensor at coords(site) with sqrt weights on its four legs
+   (iPEPS::updateAtensors, iPEPS.cpp:594-603) */
+xgb_tensor xgb_su_get(xgb_su s, int which, int site);
+void xgb_su_release(xgb_su s);
 /* Projector SVD form of the moves (no counterpart in the reference, which always
    runs the full tSVD): mode 0 exact FP64 tSVD, mode 1 randomized tSVD whose sketch
    widths are the direction's last kept counts + max(oversample, growth * kept)

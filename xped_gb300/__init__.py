@@ -14,8 +14,8 @@ This package only binds that library; it has no CPU implementation of the
 hot path and raises if the library has not been built.
 """
 from ._lib import XgbError, ensure_device, lib  # noqa: F401
-from .tensor import CTM, Basis, Tensor, bond_expectation, contract_perms, decompose  # noqa: F401
+from .tensor import CTM, Basis, SimpleUpdate, Tensor, bond_expectation, contract_perms, decompose  # noqa: F401
 from .learn import RankModel  # noqa: F401
 
-__all__ = ["Basis", "Tensor", "CTM", "RankModel", "bond_expectation", "decompose", "contract_perms", "XgbError",
+__all__ = ["Basis", "Tensor", "CTM", "SimpleUpdate", "RankModel", "bond_expectation", "decompose", "contract_perms", "XgbError",
            "ensure_device", "lib"]

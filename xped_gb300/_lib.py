@@ -145,6 +145,12 @@ PROTOS = [
     ("xgb_ctm_get", P, [P, C.c_int]),
     ("xgb_ctm_set", C.c_int, [P, C.c_int, P]),
     ("xgb_ctm_release", None, [P]),
+    ("xgb_su_create", P, [C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(P), C.c_int64]),
+    ("xgb_su_step", C.c_int, [P, P, P]),
+    ("xgb_su_step_h", C.c_int, [P, C.c_int, C.c_int, P]),
+    ("xgb_su_step_v", C.c_int, [P, C.c_int, C.c_int, P]),
+    ("xgb_su_get", P, [P, C.c_int, C.c_int]),
+    ("xgb_su_release", None, [P]),
     ("xgb_permute_plan_host", C.c_int, [P, C.c_int, i32p, C.c_int, C.c_uint32, C.POINTER(C.c_int),
                                         C.POINTER(C.c_int), C.POINTER(PermTask), C.c_int, C.POINTER(PermContrib),
                                         C.c_int, C.POINTER(P)]),

@@ -13,6 +13,7 @@
 struct xgb_basis_s { xgb::BasisPtr b; };
 struct xgb_tensor_s { xgb::Tensor t; };
 struct xgb_ctm_s { std::unique_ptr<xgb::CTM> c; };
+struct xgb_su_s { std::unique_ptr<xgb::SimpleUpdate> s; };
 
 using namespace xgb;
 
@@ -282,6 +283,54 @@ int xgb_ctm_set(xgb_ctm c, int which, xgb_tensor t) {
   })
 }
 void xgb_ctm_release(xgb_ctm c) { delete c; }
+
+xgb_su xgb_su_create(int Lx, int Ly, const int* labels, int n_sites, const xgb_tensor* G, int64_t D) {
+  GUARD(nullptr, {
+    if (Lx <= 0 || Ly <= 0 || !labels || n_sites <= 0 || !G) throw std::runtime_error("simple update: bad arguments");
+    std::vector<Tensor> gs;
+    for (int i = 0; i < n_sites; ++i) {
+      if (!G[i]) throw std::runtime_error("simple update: null site tensor");
+      gs.push_back(G[i]->t);
+    }
+    std::vector<int> lab(labels, labels + size_t(Lx) * size_t(Ly));
+    return new xgb_su_s{std::make_unique<SimpleUpdate>(Lx, Ly, lab, gs, D)};
+  })
+}
+int xgb_su_step(xgb_su s, xgb_tensor Uh, xgb_tensor Uv) {
+  GUARD(XGB_E_BADPLAN, {
+    if (!s || !Uh || !Uv) throw std::runtime_error("simple update: null argument");
+    s->s->step(Uh->t, Uv->t);
+    return XGB_OK;
+  })
+}
+int xgb_su_step_h(xgb_su s, int x, int y, xgb_tensor Uh) {
+  GUARD(XGB_E_BADPLAN, {
+    if (!s || !Uh) throw std::runtime_error("simple update: null argument");
+    s->s->step_h(x, y, Uh->t);
+    return XGB_OK;
+  })
+}
+int xgb_su_step_v(xgb_su s, int x, int y, xgb_tensor Uv) {
+  GUARD(XGB_E_BADPLAN, {
+    if (!s || !Uv) throw std::runtime_error("simple update: null argument");
+    s->s->step_v(x, y, Uv->t);
+    return XGB_OK;
+  })
+}
+xgb_tensor xgb_su_get(xgb_su s, int which, int site) {
+  GUARD(nullptr, {
+    if (!s) throw std::runtime_error("simple update: null handle");
+    if (site < 0 || site >= int(s->s->G.size())) throw std::runtime_error("simple update: site out of range");
+    switch (which) {
+      case 0: return wrap(s->s->G[size_t(site)]);
+      case 1: return wrap(s->s->wh[size_t(site)]);
+      case 2: return wrap(s->s->wv[size_t(site)]);
+      case 3: return wrap(s->s->site_tensor(site));
+      default: throw std::runtime_error("simple update slot out of range");
+    }
+  })
+}
+void xgb_su_release(xgb_su s) { delete s; }
 
 int xgb_ctm_set_svd(xgb_ctm c, int mode, int power_iters, uint64_t seed, int64_t oversample, double growth) {
   GUARD(XGB_E_BADPLAN, {

@@ -197,7 +197,6 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   if (lane == 0) red[warp] = tr;
   __syncthreads();
   __shared__ double floor_s;
-  __shared__ int dead;
   if (tid == 0) {
     double t = 0;
     for (int w = 0; w < (nt >> 5); ++w) t += red[w];
@@ -210,26 +209,32 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   for (int i = tid; i < l; i += nt) LA(i, i) += shift;
   __syncthreads();
   // Cholesky (right-looking), lower triangle in place
-  // The reciprocal of each pivot is formed once (thread 0) and broadcast through shared memory:
-  // an FP64 division is a multi-instruction DFMA sequence, and on GB300's narrow FP64 pipe 1024
-  // threads each dividing cost ~2 us per column.
-  __shared__ double inv_s;
+  // Two barriers per column: (1) scale column j by the broadcast reciprocal of its pivot,
+  // (2) rank-1 update of the trailing lower triangle, during which thread 0 - the owner of
+  // element (j+1, j+1), the first of the folded order - finishes that element and forms the
+  // next pivot into the other slot of a two-entry buffer.  The reciprocal is formed once:
+  // an FP64 division is a multi-instruction DFMA sequence on GB300's narrow FP64 pipe.
+  __shared__ double inv_s[2];
+  __shared__ int dead_s[2];
+  auto pivot = [&](int j) {
+    const double dj = LA(j, j);
+    const int dd = !(dj > dfloor);  // also true for NaN
+    if (dd) atomicAdd(bad, 1);
+    const double p = sqrt(dd ? dfloor : dj);
+    LA(j, j) = p;
+    inv_s[j & 1] = 1.0 / p;
+    dead_s[j & 1] = dd;
+  };
+  if (tid == 0 && l > 0) pivot(0);
+  __syncthreads();
   for (int j = 0; j < l; ++j) {
-    if (tid == 0) {
-      const double dj = LA(j, j);
-      dead = !(dj > dfloor);  // also true for NaN
-      if (dead) atomicAdd(bad, 1);
-      const double p = sqrt(dead ? dfloor : dj);
-      LA(j, j) = p;
-      inv_s = 1.0 / p;
-    }
-    __syncthreads();
-    const double inv = inv_s;
-    const bool zero_col = dead != 0;
+    const double inv = inv_s[j & 1];
+    const bool zero_col = dead_s[j & 1] != 0;
     for (int i = j + 1 + tid; i < l; i += nt) LA(i, j) = zero_col ? 0.0 : LA(i, j) * inv;
     __syncthreads();
     // trailing lower triangle (rows i >= k > j) folded into whole columns: column c and column
-    // t-1-c together hold t+1 elements; an odd t leaves the middle column alone
+    // t-1-c together hold t+1 elements; an odd t leaves the middle column alone.  e = 0 is
+    // element (j+1, j+1) in both branches.
     const int t = l - j - 1, half = t >> 1;
     const int total = (t + 1) * half + ((t & 1) ? (t + 1) >> 1 : 0);
     for (int e = tid; e < total; e += nt) {
@@ -244,6 +249,7 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
       i += j + 1;
       k += j + 1;
       LA(i, k) = fma(-LA(i, j), LA(k, j), LA(i, k));
+      if (e == 0) pivot(j + 1);
     }
     __syncthreads();
   }
@@ -258,9 +264,9 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   // X = L^-1 by forward elimination of the identity: row j of X is final after
   // dividing by L[j][j]; then rows i > j subtract L[i][j] * row j (columns c <= j)
   for (int j = 0; j < l; ++j) {
-    if (tid == 0) inv_s = 1.0 / LA(j, j);
+    if (tid == 0) inv_s[0] = 1.0 / LA(j, j);
     __syncthreads();
-    const double inv = inv_s;
+    const double inv = inv_s[0];
     for (int c = tid; c <= j; c += nt) XA(j, c) *= inv;
     __syncthreads();
     const int t = l - j - 1;
@@ -306,18 +312,28 @@ __global__ void __launch_bounds__(1024) chol_inv_kernel(const CholDesc* __restri
 // the single-CTA elimination (x_k = r_k * (1 / L_kk), then r_i -= L_ik x_k for i > k), so
 // both give the same bits; lane t keeps r_i for i = t + 32 j in registers (j < T).
 constexpr int kTrinvCols = 8;
-template <int T>
+constexpr int kTrinvStageL = 150;  // trailing factor staged in shared memory up to this width (176 KB)
+template <int T, bool kStaged>
 __global__ void __launch_bounds__(32 * kTrinvCols) trinv_kernel(const CholDesc* __restrict__ descs, int chunks,
                                                                  const double* __restrict__ G,
                                                                  double* __restrict__ Rinv) {
-  extern __shared__ double inv_diag[];
+  extern __shared__ double tsm[];
   const int sector = blockIdx.x / chunks, c0 = (blockIdx.x % chunks) * kTrinvCols;
   const CholDesc d = descs[sector];
   const int l = int(d.l);
   if (c0 >= l) return;  // uniform over the CTA
+  const int lt = l - c0;  // trailing order: rows / columns c0 .. l-1 are all this CTA reads
+  double* inv_diag = tsm;
   const double* L = G + d.g_off;
   double* R = Rinv + d.g_off;
   for (int k = c0 + int(threadIdx.x); k < l; k += blockDim.x) inv_diag[k - c0] = 1.0 / L[k + int64_t(k) * l];
+  // staged: column k of the trailing factor at Ls + (k - c0) * lt, rows c0 .. l-1
+  double* Ls = tsm + lt;
+  if (kStaged)
+    for (int e = threadIdx.x; e < lt * lt; e += blockDim.x) {
+      const int i = e % lt, k = e / lt;
+      Ls[e] = i >= k ? L[(c0 + i) + int64_t(c0 + k) * l] : 0.0;
+    }
   __syncthreads();
   const int lane = threadIdx.x & 31, c = c0 + int(threadIdx.x >> 5);
   if (c >= l) return;
@@ -331,12 +347,15 @@ __global__ void __launch_bounds__(32 * kTrinvCols) trinv_kernel(const CholDesc* 
     for (int j = 0; j < T; ++j)
       if (j == slot) v = r[j];
     const double xk = __shfl_sync(0xffffffffu, v, k & 31) * inv_diag[k - c0];
-    const double* Lk = L + int64_t(k) * l;
+    // column k of L: staged rows start at c0, global rows at 0
+    const double* Lk = kStaged ? Ls + int64_t(k - c0) * lt : L + int64_t(k) * l;
+    const int base = kStaged ? c0 : 0;
 #pragma unroll
     for (int j = 0; j < T; ++j) {
+      if (32 * j + 31 < k) continue;  // warp-uniform: rows of this slot are all finished
       const int i = lane + 32 * j;
       if (i == k) r[j] = xk;
-      else if (i > k && i < l) r[j] = fma(-__ldg(Lk + i), xk, r[j]);
+      else if (i > k && i < l) r[j] = fma(-(kStaged ? Lk[i - base] : __ldg(Lk + i)), xk, r[j]);
     }
   }
   // row c of Rinv (= column c of X): Rinv[c + i l] = X[i][c], zero for i < c
@@ -375,15 +394,30 @@ void launch_chol_inv(const CholDesc* d_descs, int n, int64_t max_l, double* G, d
                                                                                 kCapChol);
   count_launch();
   const int chunks = int((max_l + kTrinvCols - 1) / kTrinvCols);
-  const size_t sm = sizeof(double) * size_t(max_l);
-  if (max_l <= 256)
-    trinv_kernel<8><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
-  else if (max_l <= 512)
-    trinv_kernel<16><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
-  else if (max_l <= 1024)
-    trinv_kernel<32><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
-  else
-    trinv_kernel<64><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
+  if (max_l <= kTrinvStageL) {
+    static bool tattr = false;
+    if (!tattr) {
+      for (auto f : {trinv_kernel<4, true>, trinv_kernel<8, true>})
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(sizeof(double)) * kTrinvStageL * (kTrinvStageL + 1));
+      tattr = true;
+    }
+    const size_t sm = sizeof(double) * size_t(max_l) * size_t(max_l + 1);
+    if (max_l <= 128)
+      trinv_kernel<4, true><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
+    else
+      trinv_kernel<8, true><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
+  } else {
+    const size_t sm = sizeof(double) * size_t(max_l);
+    if (max_l <= 256)
+      trinv_kernel<8, false><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
+    else if (max_l <= 512)
+      trinv_kernel<16, false><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
+    else if (max_l <= 1024)
+      trinv_kernel<32, false><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
+    else
+      trinv_kernel<64, false><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);
+  }
   count_launch();
 }
 

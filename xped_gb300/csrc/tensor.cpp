@@ -998,25 +998,42 @@ std::pair<Tensor, Tensor> tqr(const Tensor& t0) {
   return {Q, R};
 }
 
+// fn applied in place, in order, to the main diagonal of every block of `t`
+static void diag_apply_inplace(Tensor& t, std::initializer_list<int> fns) {
+  const TensorMeta& ms = *t.meta;
+  std::vector<xgb_copy2d_desc> descs;
+  int64_t mx = 0;
+  for (size_t i = 0; i < ms.sectors.size(); ++i) {
+    descs.push_back({ms.offset[i], ms.rows[i], ms.offset[i], ms.rows[i], ms.rows[i], ms.cols[i]});
+    mx = std::max(mx, std::max(ms.rows[i], ms.cols[i]));
+  }
+  if (descs.empty()) return;
+  auto* dd = static_cast<xgb_copy2d_desc*>(dev_alloc(sizeof(xgb_copy2d_desc) * descs.size()));
+  cuda_ok(cudaMemcpyAsync(dd, descs.data(), sizeof(xgb_copy2d_desc) * descs.size(), cudaMemcpyHostToDevice, stream()), "h2d");
+  for (int fn : fns) {
+    prof_begin(K_DIAG, stream());
+    launch_diag_apply(dd, int(descs.size()), mx, fn, t.data(), stream());
+    prof_end(K_DIAG, stream(), 16.0 * double(mx) * double(descs.size()));
+  }
+  cuda_ok(cudaStreamSynchronize(stream()), "sync");
+  dev_free(dd);
+}
+
+Tensor diag_apply(const Tensor& t0, int fn) {
+  Tensor t = materialize(t0);
+  Tensor out = empty_like_meta(t.meta);
+  cuda_ok(cudaMemcpyAsync(out.data(), t.data(), sizeof(double) * t.meta->size, cudaMemcpyDeviceToDevice, stream()),
+          "copy");
+  diag_apply_inplace(out, {fn});
+  return out;
+}
+
 std::pair<Tensor, Tensor> projectors_from_svd(const SVDResult& r, const Tensor& t1, const Tensor& t2) {
   // isqrtS = S.diag_sqrt().diag_inv(): 1/sqrt(s) on the diagonal
   Tensor isq = empty_like_meta(r.S.meta);
-  {
-    const TensorMeta& ms = *r.S.meta;
-    std::vector<xgb_copy2d_desc> descs;
-    int64_t mx = 0;
-    for (size_t i = 0; i < ms.sectors.size(); ++i) {
-      descs.push_back({ms.offset[i], ms.rows[i], ms.offset[i], ms.rows[i], ms.rows[i], ms.cols[i]});
-      mx = std::max(mx, std::max(ms.rows[i], ms.cols[i]));
-    }
-    cuda_ok(cudaMemcpyAsync(isq.data(), r.S.data(), sizeof(double) * ms.size, cudaMemcpyDeviceToDevice, stream()), "copy");
-    auto* dd = static_cast<xgb_copy2d_desc*>(dev_alloc(sizeof(xgb_copy2d_desc) * std::max<size_t>(descs.size(), 1)));
-    cuda_ok(cudaMemcpyAsync(dd, descs.data(), sizeof(xgb_copy2d_desc) * descs.size(), cudaMemcpyHostToDevice, stream()), "h2d");
-    launch_diag_apply(dd, int(descs.size()), mx, XGB_DIAG_SQRT, isq.data(), stream());
-    launch_diag_apply(dd, int(descs.size()), mx, XGB_DIAG_INV, isq.data(), stream());
-    cuda_ok(cudaStreamSynchronize(stream()), "sync");
-    dev_free(dd);
-  }
+  cuda_ok(cudaMemcpyAsync(isq.data(), r.S.data(), sizeof(double) * r.S.meta->size, cudaMemcpyDeviceToDevice, stream()),
+          "copy");
+  diag_apply_inplace(isq, {XGB_DIAG_SQRT, XGB_DIAG_INV});
   Tensor P1 = matmul(matmul(isq, r.U, false, true), t1);      // isqrtS * U.adjoint() * T1
   Tensor P2 = matmul(matmul(t2, r.Vdag, false, true), isq);   // T2 * Vdag.adjoint() * isqrtS
   return {P1, P2};
@@ -1060,6 +1077,119 @@ void sector_features(const TensorMeta& m, const History& last, int64_t chi, std:
     f[5] = float(lg10(h.s_last / smax, -16.0) / 16.0);
     f[6] = float((h.keep > 0 && h.s_next > 0 ? lg10(h.s_next / std::max(h.s_last, 1e-300), -8.0) : -8.0) / 8.0);
   }
+}
+
+// ======================================================================= simple update
+Tensor apply_weights(const Tensor& A, const Tensor& wL, const Tensor& wT, const Tensor& wR, const Tensor& wB) {
+  Tensor t = contract(A, twist(wL, 1), {1, -2, -3, -4, -5}, {-1, 1}, 2);
+  t = contract(t, twist(wT, 1), {-1, 1, -3, -4, -5}, {-2, 1}, 2);
+  t = contract(t, wR, {-1, -2, 1, -4, -5}, {1, -3}, 2);
+  return contract(t, wB, {-1, -2, -3, 1, -5}, {1, -4}, 2);
+}
+
+namespace {
+// tSVD(std::numeric_limits<std::size_t>::max(), 0.): every singular value kept
+constexpr int64_t kKeepAll = int64_t(1) << 62;
+Tensor id_like(const Tensor& w) { return identity(w.meta->sym, w.meta->dom, w.meta->cod); }
+}  // namespace
+
+SimpleUpdate::SimpleUpdate(int Lx_, int Ly_, const std::vector<int>& labels_, const std::vector<Tensor>& G_,
+                           int64_t D_)
+    : Lx(Lx_), Ly(Ly_), labels(labels_), D(D_) {
+  if (Lx <= 0 || Ly <= 0 || int64_t(labels.size()) != int64_t(Lx) * Ly)
+    throw std::runtime_error("simple update: pattern must have Lx * Ly labels");
+  if (D <= 0) throw std::runtime_error("simple update: bond dimension must be positive");
+  const int n = int(G_.size());
+  std::vector<int> seen(size_t(std::max(n, 1)), 0);
+  for (int v : labels) {
+    if (v < 0 || v >= n) throw std::runtime_error("simple update: labels must be 0 .. number of site tensors - 1");
+    seen[size_t(v)] = 1;
+  }
+  for (int v = 0; v < n; ++v)
+    if (!seen[size_t(v)]) throw std::runtime_error("simple update: a site tensor has no label in the pattern");
+  for (int i = 0; i < n; ++i) {
+    auto [x, y] = coords(i);
+    if (label(x, y) == label(x + 1, y) || label(x, y) == label(x, y + 1))
+      throw std::runtime_error("simple update: neighbouring sites must carry different labels");
+  }
+  for (const Tensor& g0 : G_) {
+    Tensor g = materialize(g0);
+    if (g.meta->rank() != 2 || g.meta->corank() != 3)
+      throw std::runtime_error("simple update: site tensors must be Tensor<2,3>");
+    const Sym& s = g.meta->sym;
+    wh.push_back(identity(s, {g.meta->cod[0]}, {g.meta->cod[0]}));  // right leg
+    wv.push_back(identity(s, {g.meta->dom[1]}, {g.meta->dom[1]}));  // top leg
+    G.push_back(g);
+  }
+}
+
+int SimpleUpdate::label(int x, int y) const {
+  x %= Lx;
+  if (x < 0) x += Lx;
+  y %= Ly;
+  if (y < 0) y += Ly;
+  return labels[size_t(x) * size_t(Ly) + size_t(y)];
+}
+
+void SimpleUpdate::step_h(int x, int y, const Tensor& Uh) {
+  // t_step_h (TimePropagator.cpp:112-186)
+  auto u = [&](int a, int b) { return size_t(label(a, b)); };
+  const Tensor sq = diag_apply(wh[u(x, y)], XGB_DIAG_SQRT);
+  Tensor left_full = apply_weights(G[u(x, y)], wh[u(x - 1, y)], wv[u(x, y)], sq, wv[u(x, y + 1)]);
+  Tensor right_full = apply_weights(G[u(x + 1, y)], sq, wv[u(x + 1, y)], wh[u(x + 1, y)], wv[u(x + 1, y + 1)]);
+  SVDResult l = tsvd(permute(left_full, -1, {0, 1, 3, 2, 4}), kKeepAll, 0.0, false);
+  Tensor bond_l = matmul(l.S, l.Vdag);
+  SVDResult r = tsvd(permute(right_full, 0, {0, 4, 1, 2, 3}), kKeepAll, 0.0, false);
+  Tensor bond_r = matmul(r.U, r.S);
+  Tensor bond = contract(bond_l, bond_r, {-1, 1, -2}, {1, -3, -4}, 2);
+  Tensor enlarged = contract(twist(twist(Uh, 0), 1), bond, {1, 2, -1, -3}, {-2, 1, 2, -4}, 2);
+  SVDResult b = tsvd(enlarged, D, 1.0e-14, false);  // SimpleUpdate::renormalize
+  wh[u(x, y)] = normalize_max(b.S);
+  const Tensor idh = id_like(wh[u(x, y)]);
+  Tensor g1 = contract(l.U, b.U, {-1, -2, -4, 1}, {-5, 1, -3}, 2);
+  G[u(x, y)] = apply_weights(g1, diag_apply(wh[u(x - 1, y)], XGB_DIAG_INV), diag_apply(wv[u(x, y)], XGB_DIAG_INV), idh,
+                             diag_apply(wv[u(x, y + 1)], XGB_DIAG_INV));
+  g1 = contract(b.Vdag, r.Vdag, {-1, -5, 1}, {1, -2, -3, -4}, 2);
+  G[u(x + 1, y)] = apply_weights(g1, idh, diag_apply(wv[u(x + 1, y)], XGB_DIAG_INV),
+                                 diag_apply(wh[u(x + 1, y)], XGB_DIAG_INV), diag_apply(wv[u(x + 1, y + 1)], XGB_DIAG_INV));
+}
+
+void SimpleUpdate::step_v(int x, int y, const Tensor& Uv) {
+  // t_step_v (TimePropagator.cpp:188-215)
+  auto u = [&](int a, int b) { return size_t(label(a, b)); };
+  const Tensor sq = diag_apply(wv[u(x, y)], XGB_DIAG_SQRT);
+  Tensor top_full = apply_weights(G[u(x, y - 1)], wh[u(x - 1, y - 1)], wv[u(x, y - 1)], wh[u(x, y - 1)], sq);
+  Tensor bottom_full = apply_weights(G[u(x, y)], wh[u(x - 1, y)], sq, wh[u(x, y)], wv[u(x, y + 1)]);
+  SVDResult t = tsvd(permute(top_full, -1, {0, 1, 2, 3, 4}), kKeepAll, 0.0, false);
+  Tensor bond_t = matmul(t.S, t.Vdag);
+  SVDResult v = tsvd(permute(bottom_full, 0, {1, 4, 0, 2, 3}), kKeepAll, 0.0, false);
+  Tensor bond_b = matmul(v.U, v.S);
+  Tensor bond = contract(bond_t, bond_b, {-1, 1, -2}, {1, -3, -4}, 2);
+  Tensor enlarged = contract(twist(twist(Uv, 0), 1), bond, {1, 2, -1, -3}, {-2, 1, 2, -4}, 2);
+  SVDResult b = tsvd(enlarged, D, 1.0e-14, false);
+  wv[u(x, y)] = normalize_max(b.S);
+  const Tensor idv = id_like(wv[u(x, y)]);
+  Tensor g1 = contract(t.U, b.U, {-1, -2, -3, 1}, {-5, 1, -4}, 2);
+  G[u(x, y - 1)] = apply_weights(g1, diag_apply(wh[u(x - 1, y - 1)], XGB_DIAG_INV),
+                                 diag_apply(wv[u(x, y - 1)], XGB_DIAG_INV), diag_apply(wh[u(x, y - 1)], XGB_DIAG_INV), idv);
+  g1 = contract(b.Vdag, v.Vdag, {-2, -5, 1}, {1, -1, -3, -4}, 2);
+  G[u(x, y)] = apply_weights(g1, diag_apply(wh[u(x - 1, y)], XGB_DIAG_INV), idv, diag_apply(wh[u(x, y)], XGB_DIAG_INV),
+                             diag_apply(wv[u(x, y + 1)], XGB_DIAG_INV));
+}
+
+void SimpleUpdate::step(const Tensor& Uh, const Tensor& Uv) {
+  const int n = int(G.size());
+  for (int i = 0; i < n; ++i) { auto [x, y] = coords(i); step_h(x, y, Uh); }
+  for (int i = 0; i < n; ++i) { auto [x, y] = coords(i); step_v(x, y, Uv); }
+  for (int i = n - 1; i >= 0; --i) { auto [x, y] = coords(i); step_v(x, y, Uv); }
+  for (int i = n - 1; i >= 0; --i) { auto [x, y] = coords(i); step_h(x, y, Uh); }
+}
+
+Tensor SimpleUpdate::site_tensor(int i) const {
+  auto [x, y] = coords(i);
+  auto u = [&](int a, int b) { return size_t(label(a, b)); };
+  return apply_weights(G[u(x, y)], diag_apply(wh[u(x - 1, y)], XGB_DIAG_SQRT), diag_apply(wv[u(x, y)], XGB_DIAG_SQRT),
+                       diag_apply(wh[u(x, y)], XGB_DIAG_SQRT), diag_apply(wv[u(x, y + 1)], XGB_DIAG_SQRT));
 }
 
 // ======================================================================= CTM

@@ -257,6 +257,38 @@ struct GemmPrecisionScope {
 
 // avg of a two-site operator (src/PEPS/LinearAlgebra.cpp:58-64)
 double bond_expectation(const Tensor& rho, const Tensor& op);
+
+// fn (XGB_DIAG_SQRT / XGB_DIAG_INV / XGB_DIAG_INV_SQRT) on the main diagonal of every block
+// (diag_sqrt / diag_inv of the reference, TensorBase.cpp:191-201); the rest of each block is copied
+Tensor diag_apply(const Tensor& t, int fn);
+
+// applyWeights (src/PEPS/PEPSContractions.cpp:93-104): weights on the left, top, right and
+// bottom legs of a Tensor<2,3> site tensor; left and top weights twisted on their second leg
+Tensor apply_weights(const Tensor& A, const Tensor& wL, const Tensor& wT, const Tensor& wR, const Tensor& wB);
+
+// Simple-update imaginary-time evolution of an iPEPS with nearest-neighbour gates
+// (TimePropagator::t_step / t_step_h / t_step_v, src/PEPS/TimePropagator.cpp:7-215;
+// SimpleUpdate::renormalize, src/PEPS/SimpleUpdate.cpp:5-14).  The unit cell is a pattern of
+// site labels data[x][y] (Pattern, src/PEPS/Pattern.cpp: periodic wrapping, coords(i) =
+// (i % Lx, i / Lx)); per label a site tensor G: Tensor<2,3> (left, top | right, bottom,
+// phys) and diagonal Tensor<1,1> weights wh (its right leg) and wv (its top leg), initially
+// identities (iPEPS::initWeightTensors, iPEPS.cpp:575-592).  Neighbouring sites must carry
+// different labels (TimePropagator.cpp:86-87, 93-94); one gate for every horizontal and one
+// for every vertical bond.
+class SimpleUpdate {
+ public:
+  SimpleUpdate(int Lx, int Ly, const std::vector<int>& labels, const std::vector<Tensor>& G, int64_t D);
+  void step_h(int x, int y, const Tensor& Uh);  // bond (x, y) - (x+1, y)
+  void step_v(int x, int y, const Tensor& Uv);  // bond (x, y-1) - (x, y)
+  void step(const Tensor& Uh, const Tensor& Uv);  // TimePropagator.cpp:83-109
+  Tensor site_tensor(int i) const;                // iPEPS::updateAtensors (iPEPS.cpp:594-603)
+  int label(int x, int y) const;
+  std::pair<int, int> coords(int i) const { return {i % Lx, i / Lx}; }
+  int Lx, Ly;
+  std::vector<int> labels;  // data[x][y] at x * Ly + y
+  std::vector<Tensor> G, wh, wv;
+  int64_t D;
+};
 // the single entry of a rank-0 tensor (0 if it holds no sector)
 double scalar_value(const Tensor& t);
 

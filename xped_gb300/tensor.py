@@ -311,6 +311,49 @@ def contract_perms(a1, rank1, a2, rank2, rankres):
     return p1, s1, p2, s2, pres, sres
 
 
+class SimpleUpdate:
+    """Simple-update imaginary-time evolution of an iPEPS with nearest-neighbour
+    gates (TimePropagator::t_step, src/PEPS/TimePropagator.cpp:7-215;
+    SimpleUpdate::renormalize, src/PEPS/SimpleUpdate.cpp:5-14), all tensor work on
+    the GPU.  ``pattern``: data[x][y] site labels of the unit cell (the reference's
+    Pattern; neighbours must differ, e.g. [[0, 1], [1, 0]]); ``Gs[label]``:
+    Tensor<2,3> (left, top | right, bottom, phys); D: kept bond dimension; gates:
+    Tensor<2,2> on (phys, phys)."""
+
+    SLOTS = {"G": 0, "wh": 1, "wv": 2, "A": 3}
+
+    def __init__(self, pattern: Sequence[Sequence[int]], Gs: Sequence[Tensor], D: int):
+        Lx, Ly = len(pattern), len(pattern[0])
+        labels = (C.c_int * (Lx * Ly))(*[int(pattern[x][y]) for x in range(Lx) for y in range(Ly)])
+        hs = (C.c_void_p * len(Gs))(*[g._h for g in Gs])
+        self._h = check_handle(lib().xgb_su_create(Lx, Ly, labels, len(Gs), hs, int(D)), "su_create")
+        self.Lx, self.n = Lx, len(Gs)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().xgb_su_release(h)
+            self._h = None
+
+    def step(self, Uh: Tensor, Uv: Tensor):
+        """t_step: horizontal bonds of every site, vertical, vertical reversed, horizontal reversed."""
+        check(lib().xgb_su_step(self._h, Uh._h, Uv._h), "su_step")
+        return self
+
+    def step_h(self, x: int, y: int, Uh: Tensor):
+        check(lib().xgb_su_step_h(self._h, int(x), int(y), Uh._h), "su_step_h")
+        return self
+
+    def step_v(self, x: int, y: int, Uv: Tensor):
+        check(lib().xgb_su_step_v(self._h, int(x), int(y), Uv._h), "su_step_v")
+        return self
+
+    def get(self, name: str, site: int = 0) -> Tensor:
+        """"G", "wh", "wv" of label ``site``, or "A": the site tensor at coords(site) with
+        sqrt weights on its four legs."""
+        return Tensor(check_handle(lib().xgb_su_get(self._h, self.SLOTS[name], int(site)), "su_get"))
+
+
 class CTM:
     """CTM<double, Sym, TRank=2, ALL_OUT_LEGS=false> on a 1x1 unit cell
     (src/PEPS/CTM.cpp), all tensor work on the GPU."""
