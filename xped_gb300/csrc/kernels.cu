@@ -14,10 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
-#include <functional>
-#include <queue>
 #include <new>
-#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -136,12 +133,15 @@ void prof_end(int kind, cudaStream_t s, double work) {
 // over the most SMs); T = float is the FP32 form (operands rounded to FP32 as
 // they are staged, FP32 accumulation, alpha/beta and the store in FP64).
 template <int TILE, typename T>
-__device__ __forceinline__ void gemm_tile(const xgb_gemm_desc* __restrict__ descs, const GemmTile t,
-                                          const double* __restrict__ A, const double* __restrict__ B,
-                                          double* __restrict__ C, double alpha, double beta, double* __restrict__ ws,
-                                          T (&As)[16][TILE + 1], T (&Bs)[16][TILE + 1]) {
+__global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __restrict__ descs,
+                                                        const GemmTile* __restrict__ tiles, const double* __restrict__ A,
+                                                        const double* __restrict__ B, double* __restrict__ C,
+                                                        double alpha, double beta, double* __restrict__ ws) {
   constexpr int BK = 16;
   constexpr int R = TILE / 16;
+  __shared__ T As[BK][TILE + 1];
+  __shared__ T Bs[BK][TILE + 1];
+  const GemmTile t = tiles[blockIdx.x];
   const xgb_gemm_desc d = descs[t.g];
   const int64_t kbeg = t.k0, kend = t.k1 < 0 ? d.k : t.k1;
   const int tid = threadIdx.x;
@@ -208,65 +208,13 @@ __device__ __forceinline__ void gemm_tile(const xgb_gemm_desc* __restrict__ desc
     }
 }
 
-// Persistent form: CTA b starts with tile b, then takes the next unclaimed tile from `next`
-// (zeroed before the launch) until all n_tiles are done.  The tiles arrive longest first, so
-// an SM whose tiles were short simply takes more of them: the busiest SM ends about one short
-// tile after the average instead of carrying whatever long tiles the launch order gave it.
-template <int TILE, typename T>
-__global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __restrict__ descs,
-                                                        const GemmTile* __restrict__ tiles, int n_tiles,
-                                                        const double* __restrict__ A, const double* __restrict__ B,
-                                                        double* __restrict__ C, double alpha, double beta,
-                                                        double* __restrict__ ws, int* __restrict__ next) {
-  __shared__ T As[16][TILE + 1];
-  __shared__ T Bs[16][TILE + 1];
-  __shared__ int s_tile;
-  int cur = blockIdx.x;
-  while (cur < n_tiles) {
-    gemm_tile<TILE, T>(descs, tiles[cur], A, B, C, alpha, beta, ws, As, Bs);
-    __syncthreads();  // shared tiles free again; s_tile read by every thread below
-    if (threadIdx.x == 0) s_tile = int(gridDim.x) + atomicAdd(next, 1);
-    __syncthreads();
-    cur = s_tile;
-  }
-}
-
-namespace {
-template <int TILE, typename T>
-int gemm_grid(int n_tiles) {
-  static int per_sm = 0;
-  if (per_sm == 0) {
-    int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gemm_simt_kernel<TILE, T>, 256, 0) != cudaSuccess || nb < 1)
-      nb = 1;
-    per_sm = nb;
-  }
-  return std::max(1, std::min(n_tiles, per_sm * (g_rt.sms > 0 ? g_rt.sms : 152)));
-}
-
-template <typename T>
-void launch_simt(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
-                 const double* B, double* C, double alpha, double beta, double* ws, cudaStream_t s) {
-  int* next = static_cast<int*>(dev_alloc(sizeof(int)));
-  if (cudaMemsetAsync(next, 0, sizeof(int), s) != cudaSuccess) throw std::runtime_error("gemm: tile counter reset");
-  if (tile == 64)
-    gemm_simt_kernel<64, T><<<gemm_grid<64, T>(n_tiles), 256, 0, s>>>(d_descs, d_tiles, n_tiles, A, B, C, alpha, beta,
-                                                                      ws, next);
-  else if (tile == 32)
-    gemm_simt_kernel<32, T><<<gemm_grid<32, T>(n_tiles), 256, 0, s>>>(d_descs, d_tiles, n_tiles, A, B, C, alpha, beta,
-                                                                      ws, next);
-  else
-    gemm_simt_kernel<16, T><<<gemm_grid<16, T>(n_tiles), 256, 0, s>>>(d_descs, d_tiles, n_tiles, A, B, C, alpha, beta,
-                                                                      ws, next);
-  count_launch();
-  dev_free(next);
-}
-}  // namespace
-
 void launch_gemm_f64(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
                      const double* B, double* C, double alpha, double beta, cudaStream_t s) {
   if (n_tiles <= 0) return;
-  launch_simt<double>(d_descs, d_tiles, n_tiles, tile, A, B, C, alpha, beta, nullptr, s);
+  if (tile == 64) gemm_simt_kernel<64, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, nullptr);
+  else if (tile == 32) gemm_simt_kernel<32, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, nullptr);
+  else gemm_simt_kernel<16, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, nullptr);
+  count_launch();
 }
 
 // C tile = alpha * (sum of its partial slots in slot order) + beta * C: the result does not
@@ -294,7 +242,10 @@ void launch_gemm_f64_splitk(const xgb_gemm_desc* d_descs, const GemmTile* d_tile
                             const SplitReduce* d_reduce, int n_reduce, const double* A, const double* B, double* C,
                             double* ws, double alpha, double beta, cudaStream_t s) {
   if (n_tiles <= 0) return;
-  launch_simt<double>(d_descs, d_tiles, n_tiles, tile, A, B, C, alpha, beta, ws, s);
+  if (tile == 64) gemm_simt_kernel<64, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, ws);
+  else if (tile == 32) gemm_simt_kernel<32, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, ws);
+  else gemm_simt_kernel<16, double><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, ws);
+  count_launch();
   if (n_reduce <= 0) return;
   splitk_reduce_kernel<<<n_reduce, 256, 0, s>>>(d_descs, d_reduce, tile, ws, C, alpha, beta);
   count_launch();
@@ -303,7 +254,10 @@ void launch_gemm_f64_splitk(const xgb_gemm_desc* d_descs, const GemmTile* d_tile
 void launch_gemm_f32(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int n_tiles, int tile, const double* A,
                      const double* B, double* C, double alpha, double beta, cudaStream_t s) {
   if (n_tiles <= 0) return;
-  launch_simt<float>(d_descs, d_tiles, n_tiles, tile, A, B, C, alpha, beta, nullptr, s);
+  if (tile == 64) gemm_simt_kernel<64, float><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, nullptr);
+  else if (tile == 32) gemm_simt_kernel<32, float><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, nullptr);
+  else gemm_simt_kernel<16, float><<<n_tiles, 256, 0, s>>>(d_descs, d_tiles, A, B, C, alpha, beta, nullptr);
+  count_launch();
 }
 
 void order_tiles_by_work(std::vector<GemmTile>& tiles, const xgb_gemm_desc* descs) {
@@ -313,40 +267,15 @@ void order_tiles_by_work(std::vector<GemmTile>& tiles, const xgb_gemm_desc* desc
 }
 
 int choose_gemm_tile(const xgb_gemm_desc* descs, int n) {
-  // Tile edge with the shortest estimated makespan.  FP64 throughput is per SM, so what counts
-  // is the busiest SM: every tile's FMA count (edge^2 * k) is placed longest-first on the
-  // least-loaded SM (the order order_tiles_by_work launches them in), and the largest load is
-  // divided by the edge's relative efficiency (register reuse per staged operand: 64 > 32 > 16).
-  const int sms = g_rt.sms > 0 ? g_rt.sms : 152;
-  static const struct { int tile; double eff; } kOpts[] = {{64, 1.0}, {32, 0.85}, {16, 0.6}};
-  int best = 16;
-  double best_t = 0.0;
-  std::vector<double> w;
-  for (const auto& o : kOpts) {
-    w.clear();
-    for (int g = 0; g < n; ++g) {
-      const int64_t tiles = ((descs[g].m + o.tile - 1) / o.tile) * ((descs[g].n + o.tile - 1) / o.tile);
-      const double work = double(o.tile) * o.tile * double(std::max<int64_t>(descs[g].k, 1));
-      w.insert(w.end(), size_t(tiles), work);
-    }
-    if (w.empty()) return 16;
-    std::sort(w.begin(), w.end(), std::greater<double>());
-    std::priority_queue<double, std::vector<double>, std::greater<double>> load;
-    for (int i = 0; i < sms; ++i) load.push(0.0);
-    double mx = 0.0;
-    for (double x : w) {
-      const double l = load.top() + x;
-      load.pop();
-      load.push(l);
-      mx = std::max(mx, l);
-    }
-    const double t = mx / o.eff;
-    if (best_t == 0.0 || t < best_t * 0.999) {
-      best = o.tile;
-      best_t = t;
-    }
+  // Largest tile edge that still yields >= 2 CTAs per SM; FP64 throughput is
+  // per SM, so spreading tiles over SMs beats bigger tiles' reuse here.
+  const int target = 2 * (g_rt.sms > 0 ? g_rt.sms : 152);
+  for (int tile : {64, 32}) {
+    int64_t cnt = 0;
+    for (int g = 0; g < n; ++g) cnt += ((descs[g].m + tile - 1) / tile) * ((descs[g].n + tile - 1) / tile);
+    if (cnt >= target) return tile;
   }
-  return best;
+  return 16;
 }
 
 // ======================================================================= permute
