@@ -299,15 +299,51 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
         cur = orthonormalise(srr, srl, syo, Y, Q, st, p + 1 == iters ? 3 : 2);
       }
     };
-    // Rayleigh-Ritz on span(Q) for `sub`: B = Q^T A, then (with the exact sectors `ex`) one
-    // batched SVD, U = Q U_B, sign rule
+    // Rayleigh-Ritz on span(Q) for `sub`: the SVD of B = Q^T A (l x n) through its transpose's QR,
+    // Z = A^T Q = Q_z R (shifted CholeskyQR3, R = Q_z^T Z), so that the Jacobi SVD runs on the l x l
+    // factor R = U_R S V_R^T instead of the n-long rows of B: U_B = V_R, V_B^T = U_R^T Q_z^T.  R joins
+    // the exact sectors `ex` in one batched SVD; then U = Q V_R, V^T = U_R^T Q_z^T and the sign rule.
     auto project = [&](const std::vector<int>& sub, const std::vector<int>& ex) {
       std::vector<xgb_gemm_desc> g;
-      for (int a : sub) g.push_back({rl[a], rc[a], rr[a], yo[a], rr[a], m.offset[R[a]], rr[a], bo[R[a]], rl[a], 1, 0});
-      grouped_gemm(g, Q, t.data(), Bb, st);
+      std::vector<int64_t> src, srl, szo, r_off;
+      std::vector<xgb_copy2d_desc> zc, rc2;
+      int64_t rt = 0, mxz = 0, mxr = 0;
+      for (int a : sub) {
+        const int i = R[a];
+        g.push_back({rc[a], rl[a], rr[a], m.offset[i], rr[a], yo[a], rr[a], zo[a], rc[a], 1, 0});  // Z = A^T Q
+        src.push_back(rc[a]);
+        srl.push_back(rl[a]);
+        szo.push_back(zo[a]);
+        zc.push_back({zo[a], rc[a], bo[i], rc[a], rc[a], rl[a]});  // keep Z (n x l) in B's slot
+        r_off.push_back(rt);
+        rc2.push_back({rt, rl[a], bo[i], rl[a], rl[a], rl[a]});    // R (l x l) into B's slot
+        rt += rl[a] * rl[a];
+        mxz = std::max(mxz, rc[a] * rl[a]);
+        mxr = std::max(mxr, rl[a] * rl[a]);
+      }
+      if (!sub.empty()) {
+        grouped_gemm(g, t.data(), Q, Z, st);
+        Staging sc;
+        const size_t oz = sc.add(zc), orr = sc.add(rc2);
+        sc.upload(st);
+        prof_begin(K_COPY2D, st);
+        launch_copy2d(sc.at<xgb_copy2d_desc>(oz), int(zc.size()), mxz, Z, Bb, st);
+        prof_end(K_COPY2D, st, 16.0 * double(zt));
+        orthonormalise(src, srl, szo, Z, Om, st, 3);  // Q_z in Om (Z's layout)
+        g.clear();
+        for (size_t s2 = 0; s2 < sub.size(); ++s2) {  // R = Q_z^T Z (l x l) into Y
+          const int a = sub[s2];
+          g.push_back({rl[a], rl[a], rc[a], zo[a], rc[a], bo[R[a]], rc[a], r_off[s2], rl[a], 1, 0});
+        }
+        grouped_gemm(g, Om, Bb, Y, st);
+        prof_begin(K_COPY2D, st);
+        launch_copy2d(sc.at<xgb_copy2d_desc>(orr), int(rc2.size()), mxr, Y, Bb, st);
+        prof_end(K_COPY2D, st, 16.0 * double(rt));
+      }
       std::vector<xgb_svd_desc> d;
       for (int i : ex) d.push_back({m.rows[i], m.cols[i], bo[i], sp.u_off[i], sp.s_begin[i], sp.v_off[i]});
-      for (int a : sub) d.push_back({rl[a], rc[a], bo[R[a]], ub[a], sp.s_begin[R[a]], sp.v_off[R[a]]});
+      // U_R (l x l) behind the U blocks, V_R^T (l x l, ld l) at the sector's V^dag offset for now
+      for (int a : sub) d.push_back({rl[a], rl[a], bo[R[a]], ub[a], sp.s_begin[R[a]], sp.v_off[R[a]]});
       batched_svd(d, Bb, sp.U, sp.S, sp.V, st);
       if (sub.empty()) return;
       g.clear();
@@ -315,11 +351,15 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       int64_t mx = 0;
       for (int a : sub) {
         const int i = R[a];
-        g.push_back({rr[a], rl[a], rl[a], yo[a], rr[a], ub[a], rl[a], sp.u_off[i], rr[a], 0, 0});
+        g.push_back({rr[a], rl[a], rl[a], yo[a], rr[a], sp.v_off[i], rl[a], sp.u_off[i], rr[a], 0, 1});  // U = Q V_R
         sf.push_back({rr[a], rc[a], rl[a], sp.u_off[i], sp.v_off[i]});
         mx = std::max(mx, rl[a]);
       }
-      grouped_gemm(g, Q, sp.U, sp.U, st);
+      grouped_gemm(g, Q, sp.V, sp.U, st);
+      g.clear();
+      for (int a : sub)  // V^dag = U_R^T Q_z^T (l x n)
+        g.push_back({rl[a], rc[a], rl[a], ub[a], rl[a], zo[a], rc[a], sp.v_off[R[a]], rl[a], 1, 1});
+      grouped_gemm(g, sp.U, Om, sp.V, st);
       Staging ss;
       const size_t o = ss.add(sf);
       ss.upload(st);
