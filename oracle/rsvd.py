@@ -72,15 +72,20 @@ def _chol_pass(Y, shift):
     return sla.solve_triangular(L, Y.T, lower=True).T  # Y L^-T
 
 
+# CholeskyQR passes of the bases between the products of a subspace iteration
+INTER_PASSES = 1
+
+
 def _orth(Y, passes=3):
     """Shifted CholeskyQR3 (Fukaya et al., SIAM J. Sci. Comput. 2020), as on
-    the device: one pass with shift 11 u, then two plain passes (passes=3) or
-    one (passes=2, the bases between the products of a subspace iteration)."""
+    the device: one pass with shift 11 u, then up to two plain passes
+    (``passes`` in 1..3)."""
     if Y.size == 0:
         return Y.copy()
     Q = _chol_pass(Y, 11.0 * 2.0 ** -53)
-    Q = _chol_pass(Q, 0.0)
-    return _chol_pass(Q, 0.0) if passes == 3 else Q
+    for _ in range(passes - 1):
+        Q = _chol_pass(Q, 0.0)
+    return Q
 
 
 def sketch_svd(A, l, power_iters, seed, stream, warm_rows=None):
@@ -92,9 +97,9 @@ def sketch_svd(A, l, power_iters, seed, stream, warm_rows=None):
     if warm_rows is not None and warm_rows.shape[1] == n:
         kw = min(warm_rows.shape[0], l)
         Om[:, :kw] = warm_rows[:kw, :].T
-    Q = _orth(A @ Om, 2 if power_iters > 0 else 3)
+    Q = _orth(A @ Om, INTER_PASSES if power_iters > 0 else 3)
     for it in range(power_iters):
-        Q = _orth(A @ _orth(A.T @ Q, 2), 3 if it + 1 == power_iters else 2)
+        Q = _orth(A @ _orth(A.T @ Q, INTER_PASSES), 3 if it + 1 == power_iters else INTER_PASSES)
     ub, s, vt = np.linalg.svd(Q.T @ A, full_matrices=False)
     u, vt = fix_svd_signs(Q @ ub, vt)
     return u, s, vt

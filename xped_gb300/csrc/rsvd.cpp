@@ -169,12 +169,14 @@ double* orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64
   launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, kShift, bad, s);
   prof_end(K_QR, s, 0.0);
   grouped_gemm(mul_yq, Y, Ri, Q, s);
-  grouped_gemm(gram_q, Q, Q, G, s);
-  prof_begin(K_QR, s);
-  launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, 0.0, bad, s);
-  prof_end(K_QR, s, 0.0);
-  grouped_gemm(mul_qy, Q, Ri, Y, s);
-  if (passes != 2) {
+  if (passes >= 2) {
+    grouped_gemm(gram_q, Q, Q, G, s);
+    prof_begin(K_QR, s);
+    launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, 0.0, bad, s);
+    prof_end(K_QR, s, 0.0);
+    grouped_gemm(mul_qy, Q, Ri, Y, s);
+  }
+  if (passes >= 3) {
     grouped_gemm(gram_y, Y, Y, G, s);
     prof_begin(K_QR, s);
     launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, 0.0, bad, s);
@@ -188,6 +190,7 @@ double* orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64
 }
 
 constexpr int kMaxRetries = 3;
+constexpr int kInterPasses = 1;  // CholeskyQR passes of the bases between subspace-iteration products
 constexpr int kMaxRefine = 3;  // refinement passes of unconverged sectors per round
 
 }  // namespace
@@ -292,11 +295,11 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
         for (int a : sub) g.push_back({rc[a], rl[a], rr[a], m.offset[R[a]], rr[a], yo[a], rr[a], zo[a], rc[a], 1, 0});
         grouped_gemm(g, t.data(), cur, Z, st);
         // Omega's storage holds Qz (same layout as Z)
-        double* qz = orthonormalise(src, srl, szo, Z, Om, st, 2);
+        double* qz = orthonormalise(src, srl, szo, Z, Om, st, kInterPasses);
         g.clear();
         for (int a : sub) g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], zo[a], rc[a], yo[a], rr[a], 0, 0});
         grouped_gemm(g, t.data(), qz, Y, st);
-        cur = orthonormalise(srr, srl, syo, Y, Q, st, p + 1 == iters ? 3 : 2);
+        cur = orthonormalise(srr, srl, syo, Y, Q, st, p + 1 == iters ? 3 : kInterPasses);
       }
     };
     // Rayleigh-Ritz on span(Q) for `sub`: the SVD of B = Q^T A (l x n) through its transpose's QR,
@@ -408,7 +411,7 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       for (int a = 0; a < nr; ++a)
         g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], om[a], rc[a], yo[a], rr[a], 0, 0});
       grouped_gemm(g, t.data(), Om, Y, st);
-      double* q0 = orthonormalise(rr, rl, yo, Y, Q, st, power_iters > 0 ? 2 : 3);
+      double* q0 = orthonormalise(rr, rl, yo, Y, Q, st, power_iters > 0 ? kInterPasses : 3);
       std::vector<int> all(nr);
       for (int a = 0; a < nr; ++a) all[a] = a;
       iterate(all, power_iters, q0);

@@ -216,23 +216,13 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   // an FP64 division is a multi-instruction DFMA sequence on GB300's narrow FP64 pipe.
   __shared__ double inv_s[2];
   __shared__ int dead_s[2];
-  // The pivot chain is the critical path of the factorisation (every column waits for it), so
-  // 1/sqrt(x) is formed without an FP64 square root or division: x = xs 4^k with xs in [1, 4)
-  // (exact power-of-two scaling; x >= the floor, a normal number), an FP32 estimate of
-  // 1/sqrt(xs) refined by two Newton steps y <- y (3 - xs y^2) / 2 (quadratic convergence from
-  // ~2^-23 to below FP64 rounding), L_jj = xs y 2^k and its reciprocal y 2^-k.
   auto pivot = [&](int j) {
     const double dj = LA(j, j);
     const int dd = !(dj > dfloor);  // also true for NaN
     if (dd) atomicAdd(bad, 1);
-    const double x = dd ? dfloor : dj;
-    const int k = (int((__double_as_longlong(x) >> 52) & 0x7ff) - 1023) >> 1;
-    const double xs = x * __longlong_as_double((long long)(1023 - 2 * k) << 52);
-    double y = double(rsqrtf(float(xs)));
-    y = y * fma(-0.5 * xs, y * y, 1.5);
-    y = y * fma(-0.5 * xs, y * y, 1.5);
-    LA(j, j) = xs * y * __longlong_as_double((long long)(1023 + k) << 52);
-    inv_s[j & 1] = y * __longlong_as_double((long long)(1023 - k) << 52);
+    const double p = sqrt(dd ? dfloor : dj);
+    LA(j, j) = p;
+    inv_s[j & 1] = 1.0 / p;
     dead_s[j & 1] = dd;
   };
   if (tid == 0 && l > 0) pivot(0);

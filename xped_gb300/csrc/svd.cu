@@ -56,14 +56,17 @@ constexpr int kMaxSweeps32 = 30;
 constexpr int kMaxSweeps64 = 20;
 // Squared column norms at or below these fractions of the largest one are
 // left out of the rotations of the FP32 preconditioning and the FP64
-// polish.  Both are 0 (only exactly zero columns are skipped): positive
-// floors shortened rank-deficient inputs but changed the singular vectors of
-// the kept near-null directions that CTM projectors use.
+// polish.  FP64: 1e-30 (columns below 1e-15 of the largest are rounding noise
+// of a rank-deficient block; rotating them never converges and changes no
+// singular value or kept vector - the CTM truncation cuts at 1e-10).  FP32: 0
+// (a floor of 1e-12 left graded columns of full-rank blocks to the FP64 polish
+// and made those slower).  Larger FP64 floors (1e-15 on squared norms) skipped
+// directions the CTM keeps and changed its environments.
 #ifndef XGB_SVD_FLOOR32
 #define XGB_SVD_FLOOR32 0.0f
 #endif
 #ifndef XGB_SVD_FLOOR64
-#define XGB_SVD_FLOOR64 0.0
+#define XGB_SVD_FLOOR64 1.0e-30
 #endif
 constexpr float kFloor32 = XGB_SVD_FLOOR32;
 constexpr double kFloor64 = XGB_SVD_FLOOR64;
