@@ -798,7 +798,10 @@ def roofline(prof, steps, fp64_peak=None):
     # step's orthonormalisation launches are L2-resident
     traffic = {"svd_jacobi": (1.884e6, "ncu capture of one orthonormalisation launch, U(1) D=6 chi=128 "
                                        "(dram__bytes_read.sum 1.864 MB + write 0.021 MB)"),
-               "gemm_tc": (7.025e9, "ncu capture, SU(2) Tensor<2,2> product (6.613 GB read + 0.412 GB written)")}
+               "gemm_tc": (7.025e9, "ncu capture, SU(2) Tensor<2,2> product (6.613 GB read + 0.412 GB written)"),
+               "gemm_f64": (14.10e6, "ncu one-pass capture of 348 consecutive gemm_simt_kernel launches of the "
+                                     "chosen U(1) D=6 chi=128 run (dram read + write per launch, average; the "
+                                     "operands are L2-resident after their first touch)")}
     out["traffic"] = traffic[dom][0] if dom in traffic else None
     if dom in traffic:
         out["traffic_source"] = traffic[dom][1]
