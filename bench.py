@@ -59,6 +59,24 @@ def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def ranks_barrier():
+    """Barrier over the replicas (gloo) when the bench runs under torchrun with N > 1."""
+    if dist_info()[1] > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(values):
+    """Element-wise maximum of per-rank timings (the slowest replica sets the whole-job time)."""
+    if dist_info()[1] <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
 
@@ -174,6 +192,8 @@ def run_gpu(args):
     step_ms = []
     launches0 = L.xgb_launch_count()
     st0 = ctm.stats()
+    L.xgb_synchronize()
+    ranks_barrier()
     for _ in range(args.steps):
         flush_l2()
         L.xgb_synchronize()
@@ -181,6 +201,8 @@ def run_gpu(args):
         ctm.grow_all()
         L.xgb_event_record(1)
         step_ms.append(L.xgb_event_elapsed_ms(0, 1))
+    L.xgb_synchronize()
+    ranks_barrier()
     st1 = ctm.stats()
     res["cols_per_step"] = (st1["sketch_cols"] - st0["sketch_cols"]) / args.steps
     res["redo_per_step"] = (st1["redo"] - st0["redo"]) / args.steps
@@ -204,6 +226,8 @@ def run_gpu(args):
     host_A[:] = A.data()
     e2e_ms = []
     h2d = d2h = 0
+    L.xgb_synchronize()
+    ranks_barrier()
     for _ in range(args.steps):
         flush_l2()
         L.xgb_synchronize()
@@ -219,6 +243,8 @@ def run_gpu(args):
         e2e_ms.append(L.xgb_event_elapsed_ms(2, 3))
         h2d = host_A.nbytes + sum(host_in[k].nbytes for k in names)
         d2h = sum(v.nbytes for v in host_out.values())
+    L.xgb_synchronize()
+    ranks_barrier()
     res["e2e_ms"] = float(np.mean(e2e_ms))
     res["h2d"], res["d2h"] = h2d, d2h
 
@@ -932,12 +958,8 @@ def main():
     r = run_gpu(args)
     t_step, t_e2e = r["step_ms"], r["e2e_ms"]
     if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([t_step, t_e2e], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step, t_e2e = float(t[0]), float(t[1])
-        dist.barrier()
+        t_step, t_e2e = max_over_ranks([t_step, t_e2e])
+        ranks_barrier()
     if rank != 0:
         return
     value = world * 1e3 / t_step
