@@ -240,3 +240,33 @@ def test_svd_backward_matches_oracle(symname):
         ref = svd_backward_block(oU.block(q), np.diag(oS.block(q)), oV.block(q), odU.block(q), odS.block(q),
                                  odV.block(q))
         assert np.allclose(got[q], ref, rtol=0, atol=1e-10 * max(1.0, np.abs(ref).max())), q
+
+
+@pytest.mark.parametrize("sizes", [[(520, 600), (40, 30)], [(700, 640), (1024, 1024)]])
+def test_tsvd_wide_blocks_match_lapack(sizes):
+    """Blocks at least 512 wide run on the grid-wide Jacobi kernel (the narrow ones of the same batch on
+    the cluster kernel): singular values against LAPACK, full reconstruction, on graded spectra
+    (sigma_i = 10^(-10 i / n)) that keep the Jacobi sweeps long."""
+    from xped_gb300 import Basis, Tensor
+    rng = np.random.default_rng(21)
+    pairs_r = [(q, m) for q, (m, _n) in zip((-1, 1), sizes)]
+    pairs_c = [(q, n) for q, (_m, n) in zip((-1, 1), sizes)]
+    R, Cb = Basis.from_pairs("U1", pairs_r, sort=True), Basis.from_pairs("U1", pairs_c, sort=True)
+    t = Tensor.zeros([R], [Cb])
+    blocks, ref = [], []
+    for m, n in sizes:
+        k = min(m, n)
+        u, _ = np.linalg.qr(rng.standard_normal((m, k)))
+        v, _ = np.linalg.qr(rng.standard_normal((n, k)))
+        s = 10.0 ** (-10.0 * np.arange(k) / k)
+        blocks.append((u * s) @ v.T)
+        ref.append(s)
+    t.set_data(np.concatenate([b.ravel(order="F") for b in blocks]))
+    U, S, V, _tw, _ent, keep = t.tSVD(1 << 30, 0.0)
+    got = S.blocks()
+    Ub, Vb = U.blocks(), V.blocks()
+    for (q, _), blk, s in zip(pairs_r, blocks, ref):
+        sv = np.diag(got[q])
+        assert np.abs(sv - s).max() <= 1e-13 * s[0]
+        rec = (Ub[q] * sv) @ Vb[q]
+        assert np.abs(rec - blk).max() <= 1e-12 * np.abs(blk).max()

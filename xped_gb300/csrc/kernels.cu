@@ -896,7 +896,7 @@ int xgb_batched_svd(int n, const xgb_svd_desc* descs, const double* A, double* U
   if (n == 0) return XGB_OK;
   auto* dd = upload(descs, size_t(n), s);
   auto* dof = upload(off.data(), off.size(), s);
-  launch_svd(dd, dof, n, maxk, A, U, S, Vt, static_cast<double*>(work), s);
+  launch_svd(dd, descs, dof, n, maxk, A, U, S, Vt, static_cast<double*>(work), s);
   dev_free(dd);
   dev_free(dof);
   return check_cuda(cudaGetLastError(), "svd launch");

@@ -57,8 +57,10 @@ inline bool gemm_precision_available(int p) {
 }
 void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_task_start, int n_tasks, int64_t total,
                     const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s);
-void launch_svd(const xgb_svd_desc* d_descs, const int64_t* d_work_off, int n, int64_t max_k, const double* A, double* U,
-                double* S, double* Vt, double* work, cudaStream_t s);
+// h_descs: host copy of the descriptors (blocks at least kSvdGridMin wide run one at a time on a
+// grid-wide Jacobi kernel over all SMs; nullptr keeps every block on the cluster kernel)
+void launch_svd(const xgb_svd_desc* d_descs, const xgb_svd_desc* h_descs, const int64_t* d_work_off, int n,
+                int64_t max_k, const double* A, double* U, double* S, double* Vt, double* work, cudaStream_t s);
 void launch_truncate(int n_sectors, const int64_t* d_s_begin, const int32_t* d_deg, const double* sv, int64_t total,
                      int64_t max_keep, double eps, int preserve, int32_t* keep, double* out2, cudaStream_t s);
 void launch_qr(const xgb_qr_desc* d_descs, const int64_t* d_work_off, int n, const double* A, double* Q, double* R,

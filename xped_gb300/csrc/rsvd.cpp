@@ -122,7 +122,7 @@ void batched_svd(const std::vector<xgb_svd_desc>& d, const double* A, double* U,
   st.upload(s);
   double* W = alloc_d(wt);
   prof_begin(K_SVD, s);
-  launch_svd(st.at<xgb_svd_desc>(od), st.at<int64_t>(ow), int(d.size()), maxk, A, U, S, Vt, W, s);
+  launch_svd(st.at<xgb_svd_desc>(od), d.data(), st.at<int64_t>(ow), int(d.size()), maxk, A, U, S, Vt, W, s);
   prof_end(K_SVD, s, flops);
   dev_free(W);
 }

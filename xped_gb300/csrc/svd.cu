@@ -37,6 +37,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
+#include <stdexcept>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -72,6 +74,8 @@ constexpr float kFloor32 = XGB_SVD_FLOOR32;
 constexpr double kFloor64 = XGB_SVD_FLOOR64;
 constexpr int kSmemLimit = 200 * 1024;
 constexpr int kCgemmCols = 16;
+// blocks at least this wide (min(m, n)) take the grid-wide kernel
+constexpr int64_t kSvdGridMin = 512;
 
 template <class T>
 __device__ __forceinline__ T wsum(T v) {
@@ -197,10 +201,11 @@ __device__ bool round_rotations(const Ctx& c, T* W, T* V, T* N, int b, int la, i
   return any;
 }
 
-template <class T>
-__device__ int block_jacobi(cg::cluster_group& cl, const Ctx& c, T* W, T* V, T* norms, int* flag, int64_t mm, int nn,
-                            T tol, T rel_floor, int max_sweeps, T* smem, bool staged) {
-  const int b = (nn + kBlocks - 1) / kBlocks;
+template <class T, class Group>
+__device__ int block_jacobi(Group& cl, const Ctx& c, T* W, T* V, T* norms, int* flag, int64_t mm, int nn,
+                            T tol, T rel_floor, int max_sweeps, T* smem, bool staged, int nblocks) {
+  // nblocks = 2 x (CTAs of the group): one block pair per CTA and round
+  const int b = (nn + nblocks - 1) / nblocks;
   int sweeps = 0;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     for (int j = c.gw; j < nn; j += c.gnw) {
@@ -218,9 +223,9 @@ __device__ int block_jacobi(cg::cluster_group& cl, const Ctx& c, T* W, T* V, T* 
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) gmax = fmax(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
     const T floor = rel_floor * gmax;
-    for (int round = 0; round < kBlocks - 1; ++round) {
+    for (int round = 0; round < nblocks - 1; ++round) {
       int ba, bb;
-      rr_pair(round, c.rank, kBlocks, ba, bb);
+      rr_pair(round, c.rank, nblocks, ba, bb);
       const int ca = ba * b, cb = bb * b;
       const int la = max(0, min(b, nn - ca)), lb = max(0, min(b, nn - cb));
       auto gcol = [&](int col) { return col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1); };
@@ -356,11 +361,48 @@ __device__ double sign_of(const double* u, int64_t len, double scale, int lane) 
   return bval < 0 ? -1.0 : 1.0;
 }
 
+// Phase 4 of both SVD kernels: sigma_j = |w_j| sorted descending (ties by column), u_j = w_j / sigma_j,
+// v_j = V[:, j] (roles swapped when op(A) = A^T), every pair sign-normalised; `sval` is scratch (nn).
+template <class Group>
+__device__ void finish_svd(Group& cl, const Ctx& c, const xgb_svd_desc& d, bool tr, int64_t mm, int nn,
+                           const double* W64, const double* V, double* sval, double* __restrict__ U,
+                           double* __restrict__ S, double* __restrict__ Vt) {
+  for (int j = c.gw; j < nn; j += c.gnw) {
+    const double* w = W64 + int64_t(j) * mm;
+    double a = 0;
+    for (int64_t i = c.lane; i < mm; i += 32) { const double x = ldg(w + i); a = fma(x, x, a); }
+    a = wsum(a);
+    if (c.lane == 0) stg(sval + j, sqrt(a));
+  }
+  cl.sync();
+  const int64_t k = nn;
+  for (int j = c.gw; j < nn; j += c.gnw) {
+    const double sj = ldg(sval + j);
+    int r = 0;
+    for (int i = c.lane; i < nn; i += 32) {
+      const double si = ldg(sval + i);
+      r += (si > sj) || (si == sj && i < j);
+    }
+    r = wsum(r);
+    const double inv = sj > 0 ? 1.0 / sj : 0.0;
+    const double* ucol = tr ? V + int64_t(j) * nn : W64 + int64_t(j) * mm;
+    const double uscale = tr ? 1.0 : inv;
+    const int64_t ulen = tr ? nn : mm;
+    const double sg = sign_of(ucol, ulen, uscale, c.lane);
+    for (int64_t i = c.lane; i < ulen; i += 32) U[d.u_off + i + int64_t(r) * d.m] = sg * uscale * ldg(ucol + i);
+    const double* vcol = tr ? W64 + int64_t(j) * mm : V + int64_t(j) * nn;
+    const double vscale = tr ? inv : 1.0;
+    const int64_t vlen = tr ? mm : nn;
+    for (int64_t cc = c.lane; cc < vlen; cc += 32) Vt[d.vt_off + r + cc * k] = sg * vscale * ldg(vcol + cc);
+    if (c.lane == 0) S[d.s_off + r] = sj;
+  }
+}
+
 __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
     svd_cluster_kernel(const xgb_svd_desc* __restrict__ descs, const int64_t* __restrict__ work_off,
                        const double* __restrict__ A, double* __restrict__ U, double* __restrict__ S,
                        double* __restrict__ Vt, double* __restrict__ work, int* __restrict__ sweep_stats,
-                       int smem_bytes) {
+                       int smem_bytes, int64_t grid_min) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cl = cg::this_cluster();
   const int sector = blockIdx.x / kCluster;
@@ -368,7 +410,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
   const bool tr = d.m < d.n;
   const int64_t mm = tr ? d.n : d.m;
   const int nn = int(tr ? d.m : d.n);
-  if (nn == 0) return;  // uniform across the cluster
+  if (nn == 0 || nn >= grid_min) return;  // uniform across the cluster (wide blocks: svd_grid_kernel)
 
   Ctx c;
   c.tid = threadIdx.x;
@@ -422,7 +464,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
   cl.sync();
   const float tol32 = 8.0f * sqrtf(float(mm)) * 6.0e-8f;
   const int sw32 = nn > 1 ? block_jacobi<float>(cl, c, W32, V32, n32, flag, mm, nn, tol32, kFloor32, kMaxSweeps32,
-                                                reinterpret_cast<float*>(smem_raw), staged32)
+                                                reinterpret_cast<float*>(smem_raw), staged32, kBlocks)
                           : 0;
   const long long t1 = clock64();
 
@@ -479,41 +521,12 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
   // ---- phase 3: FP64 block Jacobi polish
   const double tol64 = 1.0e-13;
   const int sw64 = nn > 1 ? block_jacobi<double>(cl, c, W64, V, n64, flag, mm, nn, tol64, kFloor64, kMaxSweeps64,
-                                                 reinterpret_cast<double*>(smem_raw), staged64)
+                                                 reinterpret_cast<double*>(smem_raw), staged64, kBlocks)
                           : 0;
   const long long t3 = clock64();
 
   // ---- phase 4: sort, sign, write
-  double* sval = n64;
-  for (int j = c.gw; j < nn; j += c.gnw) {
-    const double* w = W64 + int64_t(j) * mm;
-    double a = 0;
-    for (int64_t i = c.lane; i < mm; i += 32) { const double x = ldg(w + i); a = fma(x, x, a); }
-    a = wsum(a);
-    if (c.lane == 0) stg(sval + j, sqrt(a));
-  }
-  cl.sync();
-  const int64_t k = nn;
-  for (int j = c.gw; j < nn; j += c.gnw) {
-    const double sj = ldg(sval + j);
-    int r = 0;
-    for (int i = c.lane; i < nn; i += 32) {
-      const double si = ldg(sval + i);
-      r += (si > sj) || (si == sj && i < j);
-    }
-    r = wsum(r);
-    const double inv = sj > 0 ? 1.0 / sj : 0.0;
-    const double* ucol = tr ? V + int64_t(j) * nn : W64 + int64_t(j) * mm;
-    const double uscale = tr ? 1.0 : inv;
-    const int64_t ulen = tr ? nn : mm;
-    const double sg = sign_of(ucol, ulen, uscale, c.lane);
-    for (int64_t i = c.lane; i < ulen; i += 32) U[d.u_off + i + int64_t(r) * d.m] = sg * uscale * ldg(ucol + i);
-    const double* vcol = tr ? W64 + int64_t(j) * mm : V + int64_t(j) * nn;
-    const double vscale = tr ? inv : 1.0;
-    const int64_t vlen = tr ? mm : nn;
-    for (int64_t cc = c.lane; cc < vlen; cc += 32) Vt[d.vt_off + r + cc * k] = sg * vscale * ldg(vcol + cc);
-    if (c.lane == 0) S[d.s_off + r] = sj;
-  }
+  finish_svd(cl, c, d, tr, mm, nn, W64, V, n64, U, S, Vt);
   if (sweep_stats && c.rank == 0 && c.tid == 0) {
     int* st6 = sweep_stats + 6 * sector;
     st6[0] = sw32;
@@ -522,6 +535,67 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
     st6[3] = int((t2 - t1) >> 10);
     st6[4] = int((t3 - t2) >> 10);
     st6[5] = int((clock64() - t3) >> 10);
+  }
+}
+
+// Wide blocks: the same one-sided block Jacobi spread over every SM of the GPU (a cooperative launch of
+// one CTA per SM, grid-wide barriers between the rounds) instead of one 8-SM cluster, FP64 throughout
+// (no FP32 preconditioning: with 2 x SMs column blocks of a few columns each, a sweep is ~150x the
+// cluster's FP64 throughput per block).  One launch per block; the cluster kernel takes the narrower
+// blocks of the batch.
+constexpr int kMaxSweepsGrid = 30;
+__global__ void __launch_bounds__(kThreads)
+    svd_grid_kernel(const xgb_svd_desc* __restrict__ descs, const int64_t* __restrict__ work_off, int sector,
+                    const double* __restrict__ A, double* __restrict__ U, double* __restrict__ S,
+                    double* __restrict__ Vt, double* __restrict__ work, int* __restrict__ sweep_stats,
+                    int smem_bytes) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cg::grid_group gg = cg::this_grid();
+  const xgb_svd_desc d = descs[sector];
+  const bool tr = d.m < d.n;
+  const int64_t mm = tr ? d.n : d.m;
+  const int nn = int(tr ? d.m : d.n);
+  if (nn == 0) return;  // uniform across the grid
+
+  Ctx c;
+  c.tid = threadIdx.x;
+  c.lane = c.tid & 31;
+  c.warp = c.tid >> 5;
+  c.rank = int(blockIdx.x);
+  c.gw = c.rank * kWarps + c.warp;
+  c.gnw = int(gridDim.x) * kWarps;
+  c.gtid = c.rank * kThreads + c.tid;
+  c.gnt = int(gridDim.x) * kThreads;
+
+  // workspace as in the cluster kernel: W64 mm*nn | V64 nn*nn | (2 nn*nn unused) | n64 nn | misc
+  const int64_t nn2 = int64_t(nn) * nn;
+  double* W64 = work + work_off[sector];
+  double* V64 = W64 + mm * nn;
+  double* n64 = V64 + 3 * nn2;
+  int* flag = reinterpret_cast<int*>(n64 + nn);
+  auto opA = [&](int64_t i, int64_t j) { return tr ? A[d.a_off + j + i * d.m] : A[d.a_off + i + j * d.m]; };
+  const long long t0 = clock64();
+  for (int j = c.gw; j < nn; j += c.gnw) {
+    for (int64_t i = c.lane; i < mm; i += 32) stg(W64 + int64_t(j) * mm + i, opA(i, j));
+    for (int i = c.lane; i < nn; i += 32) stg(V64 + int64_t(j) * nn + i, i == j ? 1.0 : 0.0);
+  }
+  gg.sync();
+  const int nblocks = 2 * int(gridDim.x);
+  const int b = (nn + nblocks - 1) / nblocks;
+  const bool staged = int64_t(2 * b) * (mm + nn + 1) * 8 <= smem_bytes;
+  const int sw = nn > 1 ? block_jacobi<double>(gg, c, W64, V64, n64, flag, mm, nn, 1.0e-13, kFloor64, kMaxSweepsGrid,
+                                               reinterpret_cast<double*>(smem_raw), staged, nblocks)
+                        : 0;
+  const long long t1 = clock64();
+  finish_svd(gg, c, d, tr, mm, nn, W64, V64, n64, U, S, Vt);
+  if (sweep_stats && c.rank == 0 && c.tid == 0) {
+    int* st6 = sweep_stats + 6 * sector;
+    st6[0] = 0;
+    st6[1] = sw;
+    st6[2] = 0;
+    st6[3] = 0;
+    st6[4] = int((t1 - t0) >> 10);
+    st6[5] = int((clock64() - t1) >> 10);
   }
 }
 
@@ -538,8 +612,8 @@ size_t svd_work_elems(int64_t m, int64_t n) {
   return size_t(doubles + (floats + 1) / 2 + 2);
 }
 
-void launch_svd(const xgb_svd_desc* d_descs, const int64_t* d_work_off, int n, int64_t max_k, const double* A,
-                double* U, double* S, double* Vt, double* work, cudaStream_t s) {
+void launch_svd(const xgb_svd_desc* d_descs, const xgb_svd_desc* h_descs, const int64_t* d_work_off, int n,
+                int64_t max_k, const double* A, double* U, double* S, double* Vt, double* work, cudaStream_t s) {
   if (n <= 0) return;
   if (g_stats_cap < n) {
     if (g_stats_dev) cudaFree(g_stats_dev);
@@ -554,10 +628,28 @@ void launch_svd(const xgb_svd_desc* d_descs, const int64_t* d_work_off, int n, i
   static bool configured = false;
   if (!configured) {
     cudaFuncSetAttribute(svd_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+    cudaFuncSetAttribute(svd_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
     configured = true;
   }
-  svd_cluster_kernel<<<n * kCluster, kThreads, smem, s>>>(d_descs, d_work_off, A, U, S, Vt, work, g_stats_dev, smem);
+  std::vector<int> wide;
+  if (h_descs)
+    for (int i = 0; i < n; ++i)
+      if (std::min(h_descs[i].m, h_descs[i].n) >= kSvdGridMin) wide.push_back(i);
+  const int64_t grid_min = wide.empty() ? INT64_MAX : kSvdGridMin;
+  svd_cluster_kernel<<<n * kCluster, kThreads, smem, s>>>(d_descs, d_work_off, A, U, S, Vt, work, g_stats_dev, smem,
+                                                          grid_min);
   count_launch();
+  if (wide.empty()) return;
+  // widest blocks first is irrelevant here (one launch each, in stream order)
+  int sms = num_sms();
+  for (int sector : wide) {
+    void* args[] = {const_cast<xgb_svd_desc**>(&d_descs), const_cast<int64_t**>(&d_work_off), &sector,
+                    const_cast<double**>(&A), &U, &S, &Vt, &work, &g_stats_dev, const_cast<int*>(&smem)};
+    const cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(svd_grid_kernel), dim3(sms),
+                                                      dim3(kThreads), args, size_t(smem), s);
+    if (e != cudaSuccess) throw std::runtime_error(std::string("svd grid launch: ") + cudaGetErrorString(e));
+    count_launch();
+  }
 }
 
 }  // namespace xgb
@@ -628,7 +720,7 @@ extern "C" int xgb_batched_svd_noalloc(int n, const xgb_svd_desc* descs, const d
   if (e != cudaSuccess) return set_error(XGB_E_CUDA, std::string("descriptor copy: ") + cudaGetErrorString(e));
   cudaFuncSetAttribute(svd_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
   svd_cluster_kernel<<<n * kCluster, kThreads, kSmemLimit, s>>>(d_descs, d_off, A, U, S, Vt, d_work, nullptr,
-                                                                kSmemLimit);
+                                                                kSmemLimit, INT64_MAX);
   count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(XGB_E_CUDA, std::string("svd launch: ") + cudaGetErrorString(e));

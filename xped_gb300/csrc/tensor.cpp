@@ -787,6 +787,7 @@ struct SvdPlan {
   std::vector<int64_t> s_begin;  // per sector prefix (host), size n+1
   std::vector<int64_t> u_off, s_off, v_off, kfull;
   xgb_svd_desc* d_descs = nullptr;
+  std::vector<xgb_svd_desc> h_descs;
   int64_t* d_work_off = nullptr;
   int64_t* d_s_begin = nullptr;
   int32_t* d_deg = nullptr;
@@ -828,6 +829,7 @@ std::shared_ptr<SvdPlan> get_svd_plan(const TensorMeta& m) {
   }
   if (p->maxk > 8192) throw std::runtime_error("tSVD: sector block larger than 8192 columns");
   p->d_descs = dev_table(descs);
+  p->h_descs = descs;
   p->d_work_off = dev_table(woff);
   p->d_s_begin = dev_table(p->s_begin);
   p->d_deg = dev_table(deg);
@@ -945,7 +947,8 @@ SVDResult tsvd(const Tensor& t0, int64_t max_keep, double eps_svd, bool preserve
   sp.V = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->v_total, 1)));
   double* W = static_cast<double*>(dev_alloc(sizeof(double) * std::max<int64_t>(plan->work_total, 1)));
   prof_begin(K_SVD, st);
-  launch_svd(plan->d_descs, plan->d_work_off, plan->n, plan->maxk, t.data(), sp.U, sp.S, sp.V, W, st);
+  launch_svd(plan->d_descs, plan->h_descs.data(), plan->d_work_off, plan->n, plan->maxk, t.data(), sp.U, sp.S, sp.V, W,
+             st);
   prof_end(K_SVD, st, plan->lapack_flops);
   dev_free(W);
   sp.k = plan->kfull;
