@@ -203,9 +203,12 @@ __device__ bool round_rotations(const Ctx& c, T* W, T* V, T* N, int b, int la, i
 
 template <class T, class Group>
 __device__ int block_jacobi(Group& cl, const Ctx& c, T* W, T* V, T* norms, int* flag, int64_t mm, int nn,
-                            T tol, T rel_floor, int max_sweeps, T* smem, bool staged, int nblocks) {
-  // nblocks = 2 x (CTAs of the group): one block pair per CTA and round
+                            T tol, T rel_floor, int max_sweeps, T* smem, bool staged, int nblocks, int* perm) {
+  // nblocks = 2 x (CTAs of the group): one block pair per CTA and round.  perm (nn ints): at the start
+  // of every sweep the columns are ordered by decreasing norm (de Rijk's pivoting, as in LAPACK's
+  // dgesvj) and the blocks are cut from that order, which keeps graded columns converging.
   const int b = (nn + nblocks - 1) / nblocks;
+  auto col_of = [&](int idx) { return __ldcg(perm + idx); };
   int sweeps = 0;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     for (int j = c.gw; j < nn; j += c.gnw) {
@@ -223,12 +226,25 @@ __device__ int block_jacobi(Group& cl, const Ctx& c, T* W, T* V, T* norms, int* 
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) gmax = fmax(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
     const T floor = rel_floor * gmax;
+    for (int j = c.gw; j < nn; j += c.gnw) {
+      const T nj = ldg(norms + j);
+      int r = 0;
+      for (int i = c.lane; i < nn; i += 32) {
+        const T ni = ldg(norms + i);
+        r += (ni > nj) || (ni == nj && i < j);
+      }
+      r = wsum(r);
+      if (c.lane == 0) __stcg(perm + r, j);
+    }
+    cl.sync();
     for (int round = 0; round < nblocks - 1; ++round) {
       int ba, bb;
       rr_pair(round, c.rank, nblocks, ba, bb);
       const int ca = ba * b, cb = bb * b;
       const int la = max(0, min(b, nn - ca)), lb = max(0, min(b, nn - cb));
-      auto gcol = [&](int col) { return col < b ? (col < la ? ca + col : -1) : (col - b < lb ? cb + col - b : -1); };
+      auto gcol = [&](int col) {
+        return col < b ? (col < la ? col_of(ca + col) : -1) : (col - b < lb ? col_of(cb + col - b) : -1);
+      };
       bool any = false;
       if (staged) {
         T* sW = smem;                        // 2b columns of mm
@@ -261,8 +277,8 @@ __device__ int block_jacobi(Group& cl, const Ctx& c, T* W, T* V, T* norms, int* 
               int p, q, base;
               if (k < na) { rr_pair(r, k, pa, p, q); base = ca; if (p >= la || q >= la) continue; }
               else { rr_pair(r, k - na, pb, p, q); base = cb; if (p >= lb || q >= lb) continue; }
-              p += base;
-              q += base;
+              p = col_of(p + base);
+              q = col_of(q + base);
               any |= rotate<T, true>(W + int64_t(p) * mm, W + int64_t(q) * mm, V + int64_t(p) * nn, V + int64_t(q) * nn,
                                      norms + p, norms + q, mm, nn, tol, floor, c.lane);
             }
@@ -273,7 +289,7 @@ __device__ int block_jacobi(Group& cl, const Ctx& c, T* W, T* V, T* norms, int* 
           for (int i = c.warp; i < b; i += kWarps) {
             const int j = (i + r) % b;
             if (i >= la || j >= lb) continue;
-            const int p = ca + i, q = cb + j;
+            const int p = col_of(ca + i), q = col_of(cb + j);
             any |= rotate<T, true>(W + int64_t(p) * mm, W + int64_t(q) * mm, V + int64_t(p) * nn, V + int64_t(q) * nn,
                                    norms + p, norms + q, mm, nn, tol, floor, c.lane);
           }
@@ -464,7 +480,8 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
   cl.sync();
   const float tol32 = 8.0f * sqrtf(float(mm)) * 6.0e-8f;
   const int sw32 = nn > 1 ? block_jacobi<float>(cl, c, W32, V32, n32, flag, mm, nn, tol32, kFloor32, kMaxSweeps32,
-                                                reinterpret_cast<float*>(smem_raw), staged32, kBlocks)
+                                                reinterpret_cast<float*>(smem_raw), staged32, kBlocks,
+                                                reinterpret_cast<int*>(T2))
                           : 0;
   const long long t1 = clock64();
 
@@ -521,7 +538,8 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
   // ---- phase 3: FP64 block Jacobi polish
   const double tol64 = 1.0e-13;
   const int sw64 = nn > 1 ? block_jacobi<double>(cl, c, W64, V, n64, flag, mm, nn, tol64, kFloor64, kMaxSweeps64,
-                                                 reinterpret_cast<double*>(smem_raw), staged64, kBlocks)
+                                                 reinterpret_cast<double*>(smem_raw), staged64, kBlocks,
+                                                 reinterpret_cast<int*>(T2))
                           : 0;
   const long long t3 = clock64();
 
@@ -543,7 +561,7 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
 // (no FP32 preconditioning: with 2 x SMs column blocks of a few columns each, a sweep is ~150x the
 // cluster's FP64 throughput per block).  One launch per block; the cluster kernel takes the narrower
 // blocks of the batch.
-constexpr int kMaxSweepsGrid = 30;
+constexpr int kMaxSweepsGrid = 80;
 __global__ void __launch_bounds__(kThreads)
     svd_grid_kernel(const xgb_svd_desc* __restrict__ descs, const int64_t* __restrict__ work_off, int sector,
                     const double* __restrict__ A, double* __restrict__ U, double* __restrict__ S,
@@ -584,7 +602,8 @@ __global__ void __launch_bounds__(kThreads)
   const int b = (nn + nblocks - 1) / nblocks;
   const bool staged = int64_t(2 * b) * (mm + nn + 1) * 8 <= smem_bytes;
   const int sw = nn > 1 ? block_jacobi<double>(gg, c, W64, V64, n64, flag, mm, nn, 1.0e-13, kFloor64, kMaxSweepsGrid,
-                                               reinterpret_cast<double*>(smem_raw), staged, nblocks)
+                                               reinterpret_cast<double*>(smem_raw), staged, nblocks,
+                                               reinterpret_cast<int*>(V64 + nn2))
                         : 0;
   const long long t1 = clock64();
   finish_svd(gg, c, d, tr, mm, nn, W64, V64, n64, U, S, Vt);
