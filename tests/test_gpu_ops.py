@@ -270,3 +270,20 @@ def test_tsvd_wide_blocks_match_lapack(sizes):
         assert np.abs(sv - s).max() <= 1e-13 * s[0]
         rec = (Ub[q] * sv) @ Vb[q]
         assert np.abs(rec - blk).max() <= 1e-12 * np.abs(blk).max()
+
+
+def test_tsvd_wide_block_matches_oracle_vectors():
+    """A 560-wide U(1) sector (grid-wide Jacobi) next to narrower ones (cluster kernel): U, S, V^dag against
+    the oracle's LAPACK tSVD with the shared sign rule, truncated to 200 values."""
+    rng = np.random.default_rng(8)
+    s, oB, nB = pair_basis("u1", [(-1, 24), (0, 40), (1, 24)], sort=True)
+    _, oC, nC = pair_basis("u1", [(-1, 5), (0, 8), (1, 5)], sort=True)
+    ot = oracle.Tensor(s, [oB, oC], [oB, oC]).set_random(rng)  # sectors 120 .. 560 wide
+    nt = to_native(ot, [nB, nC], [nB, nC])
+    assert max(min(b.shape) for b in ot.blocks) >= 512
+    oU, oS, oV, otw, oent = ot.tsvd(200, 1e-10)
+    nU, nS, nV, ntw, nent, _keep = nt.tSVD(200, 1e-10)
+    assert_same(nS, oS, 1e-11, 1e-12)
+    assert_same(nU, oU, 1e-8, 1e-9)
+    assert_same(nV, oV, 1e-8, 1e-9)
+    assert abs(ntw - otw) <= 1e-10 * max(1.0, otw)
