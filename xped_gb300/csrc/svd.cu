@@ -76,6 +76,8 @@ constexpr int kSmemLimit = 200 * 1024;
 constexpr int kCgemmCols = 16;
 // blocks at least this wide (min(m, n)) take the grid-wide kernel
 constexpr int64_t kSvdGridMin = 512;
+// target columns per Jacobi block of the grid-wide kernel
+constexpr int64_t kGridCols = 4;
 
 template <class T>
 __device__ __forceinline__ T wsum(T v) {
@@ -659,12 +661,15 @@ void launch_svd(const xgb_svd_desc* d_descs, const xgb_svd_desc* h_descs, const 
                                                           grid_min);
   count_launch();
   if (wide.empty()) return;
-  // widest blocks first is irrelevant here (one launch each, in stream order)
-  int sms = num_sms();
+  const int sms = num_sms();
   for (int sector : wide) {
+    // one CTA per SM at most, and about kGridCols columns per Jacobi block: each round costs a grid
+    // barrier and a staging pass, so narrower blocks use fewer CTAs with more columns each
+    const int64_t nn = std::min(h_descs[sector].m, h_descs[sector].n);
+    const int ctas = int(std::max<int64_t>(1, std::min<int64_t>(sms, (nn + 2 * kGridCols - 1) / (2 * kGridCols))));
     void* args[] = {const_cast<xgb_svd_desc**>(&d_descs), const_cast<int64_t**>(&d_work_off), &sector,
                     const_cast<double**>(&A), &U, &S, &Vt, &work, &g_stats_dev, const_cast<int*>(&smem)};
-    const cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(svd_grid_kernel), dim3(sms),
+    const cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(svd_grid_kernel), dim3(ctas),
                                                       dim3(kThreads), args, size_t(smem), s);
     if (e != cudaSuccess) throw std::runtime_error(std::string("svd grid launch: ") + cudaGetErrorString(e));
     count_launch();
