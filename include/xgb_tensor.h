@@ -118,6 +118,19 @@ xgb_tensor xgb_ctm_get(xgb_ctm c, int which);
 int xgb_ctm_set(xgb_ctm c, int which, xgb_tensor t);
 void xgb_ctm_release(xgb_ctm c);
 
+/* ------------------------------------------------------------- checkpoints */
+/* The fields the reference serialises for a tensor (StorageType_contiguous::serialize,
+   include/Xped/Core/storage/StorageType_contiguous.hpp:191-204) and for a CTM environment
+   (CTM::serialize, include/Xped/PEPS/CTM.hpp:184-204: chi, C1..C4, T1..T4) in this library's own
+   byte layout (the reference's yas archive format is not claimed).  Plain leg bases only.
+   With buf == NULL the call stores the needed byte count in *size; otherwise cap must hold it. */
+int xgb_tensor_serialize(xgb_tensor t, uint8_t* buf, int64_t cap, int64_t* size);
+xgb_tensor xgb_tensor_deserialize(const uint8_t* buf, int64_t size);
+int xgb_ctm_serialize(xgb_ctm c, uint8_t* buf, int64_t cap, int64_t* size);
+/* a CTM for site tensor A with chi and the environment of the checkpoint (the projector-SVD
+   configuration and the sketch-width history are not part of it) */
+xgb_ctm xgb_ctm_deserialize(xgb_tensor A, const uint8_t* buf, int64_t size);
+
 /* ----------------------------------------------------------- simple update */
 /* Simple-update imaginary-time evolution of an iPEPS with nearest-neighbour gates
    (TimePropagator::t_step / t_step_h / t_step_v, src/PEPS/TimePropagator.cpp:7-215;

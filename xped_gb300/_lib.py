@@ -145,6 +145,10 @@ PROTOS = [
     ("xgb_ctm_get", P, [P, C.c_int]),
     ("xgb_ctm_set", C.c_int, [P, C.c_int, P]),
     ("xgb_ctm_release", None, [P]),
+    ("xgb_tensor_serialize", C.c_int, [P, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    ("xgb_tensor_deserialize", P, [C.c_void_p, C.c_int64]),
+    ("xgb_ctm_serialize", C.c_int, [P, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    ("xgb_ctm_deserialize", P, [P, C.c_void_p, C.c_int64]),
     ("xgb_su_create", P, [C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(P), C.c_int64]),
     ("xgb_su_step", C.c_int, [P, P, P]),
     ("xgb_su_step_h", C.c_int, [P, C.c_int, C.c_int, P]),

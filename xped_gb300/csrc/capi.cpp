@@ -284,6 +284,39 @@ int xgb_ctm_set(xgb_ctm c, int which, xgb_tensor t) {
 }
 void xgb_ctm_release(xgb_ctm c) { delete c; }
 
+static int copy_out(const std::vector<uint8_t>& bytes, uint8_t* buf, int64_t cap, int64_t* size) {
+  if (size) *size = int64_t(bytes.size());
+  if (!buf) return XGB_OK;
+  if (cap < int64_t(bytes.size())) return set_error(XGB_E_BADPLAN, "checkpoint: buffer too small");
+  std::memcpy(buf, bytes.data(), bytes.size());
+  return XGB_OK;
+}
+
+int xgb_tensor_serialize(xgb_tensor t, uint8_t* buf, int64_t cap, int64_t* size) {
+  GUARD(XGB_E_BADPLAN, {
+    if (!t) throw std::runtime_error("checkpoint: null tensor");
+    return copy_out(serialize_tensor(t->t), buf, cap, size);
+  })
+}
+xgb_tensor xgb_tensor_deserialize(const uint8_t* buf, int64_t size) {
+  GUARD(nullptr, {
+    if (!buf || size < 0) throw std::runtime_error("checkpoint: null buffer");
+    return wrap(deserialize_tensor(buf, size_t(size)));
+  })
+}
+int xgb_ctm_serialize(xgb_ctm c, uint8_t* buf, int64_t cap, int64_t* size) {
+  GUARD(XGB_E_BADPLAN, {
+    if (!c) throw std::runtime_error("checkpoint: null CTM");
+    return copy_out(serialize_ctm(*c->c), buf, cap, size);
+  })
+}
+xgb_ctm xgb_ctm_deserialize(xgb_tensor A, const uint8_t* buf, int64_t size) {
+  GUARD(nullptr, {
+    if (!A || !buf || size < 0) throw std::runtime_error("checkpoint: null argument");
+    return new xgb_ctm_s{deserialize_ctm(A->t, buf, size_t(size))};
+  })
+}
+
 xgb_su xgb_su_create(int Lx, int Ly, const int* labels, int n_sites, const xgb_tensor* G, int64_t D) {
   GUARD(nullptr, {
     if (Lx <= 0 || Ly <= 0 || !labels || n_sites <= 0 || !G) throw std::runtime_error("simple update: bad arguments");

@@ -258,6 +258,14 @@ struct GemmPrecisionScope {
 // avg of a two-site operator (src/PEPS/LinearAlgebra.cpp:58-64)
 double bond_expectation(const Tensor& rho, const Tensor& op);
 
+// Checkpoints (checkpoint.cpp): the reference's serialised fields of a tensor / CTM environment in
+// this library's byte layout; plain (depth-1) leg bases only.
+std::vector<uint8_t> serialize_tensor(const Tensor& t);
+Tensor deserialize_tensor(const uint8_t* p, size_t n);
+class CTM;
+std::vector<uint8_t> serialize_ctm(CTM& c);
+std::unique_ptr<CTM> deserialize_ctm(const Tensor& A, const uint8_t* p, size_t n);
+
 // fn (XGB_DIAG_SQRT / XGB_DIAG_INV / XGB_DIAG_INV_SQRT) on the main diagonal of every block
 // (diag_sqrt / diag_inv of the reference, TensorBase.cpp:191-201); the rest of each block is copied
 Tensor diag_apply(const Tensor& t, int fn);

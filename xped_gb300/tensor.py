@@ -173,6 +173,20 @@ class Tensor:
             off += r * c
         return out
 
+    def to_bytes(self) -> bytes:
+        """Checkpoint of this tensor (bases, sectors, data; the fields of the reference's
+        StorageType_contiguous::serialize) in the library's byte layout."""
+        n = C.c_int64()
+        check(lib().xgb_tensor_serialize(self._h, None, 0, C.byref(n)), "tensor_serialize")
+        buf = (C.c_uint8 * n.value)()
+        check(lib().xgb_tensor_serialize(self._h, buf, n.value, C.byref(n)), "tensor_serialize")
+        return bytes(buf)
+
+    @staticmethod
+    def from_bytes(data: bytes) -> "Tensor":
+        buf = (C.c_uint8 * len(data)).from_buffer_copy(data)
+        return Tensor(lib().xgb_tensor_deserialize(buf, len(data)))
+
     def set_blocks(self, blocks: Dict[int, np.ndarray]):
         qs, rs, cs = self.sectors()
         parts = []
@@ -382,6 +396,22 @@ class CTM:
 
     def get(self, name: str) -> Tensor:
         return Tensor(lib().xgb_ctm_get(self._h, self.SLOTS[name]))
+
+    def to_bytes(self) -> bytes:
+        """Checkpoint of chi and the environment C1..C4, T1..T4 (the reference's CTM::serialize fields)."""
+        n = C.c_int64()
+        check(lib().xgb_ctm_serialize(self._h, None, 0, C.byref(n)), "ctm_serialize")
+        buf = (C.c_uint8 * n.value)()
+        check(lib().xgb_ctm_serialize(self._h, buf, n.value, C.byref(n)), "ctm_serialize")
+        return bytes(buf)
+
+    @classmethod
+    def from_bytes(cls, A: Tensor, data: bytes) -> "CTM":
+        """A CTM for site tensor A resumed from a checkpoint (projector-SVD settings are not part of it)."""
+        buf = (C.c_uint8 * len(data)).from_buffer_copy(data)
+        obj = cls.__new__(cls)
+        obj._h = check_handle(lib().xgb_ctm_deserialize(A._h, buf, len(data)), "ctm_deserialize")
+        return obj
 
     def set(self, name: str, t: Tensor):
         check(lib().xgb_ctm_set(self._h, self.SLOTS[name], t._h), "ctm_set")
