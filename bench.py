@@ -396,7 +396,7 @@ def run_fz2(args):
 
 # ----------------------------------------------------------------------------- block-GEMM sweep
 def gemm_sweep(reps=5):
-    """Grouped block GEMMs FP64 vs 3xTF32 vs FP32 (CUDA cores): (i) the sector GEMMs of an SU(2)
+    """Grouped block GEMMs FP64 vs 3xTF32 vs BF16x9 vs FP32 (CUDA cores): (i) the sector GEMMs of an SU(2)
     Tensor<2,2> product (irreps q = 2j+1, j = 0..3 integer, multiplicities 1-24);
     (ii) synthetic lists of G blocks, m, n, k log-uniform in [8, 512].  Useful
     TFLOP/s = sum 2mnk / time; error = max over blocks of ||C - C_fp64||_F / ||C_fp64||_F."""
@@ -430,7 +430,7 @@ def gemm_sweep(reps=5):
     flops = sum(2.0 * d.m * d.n * d.k for d in descs)
     res = {}
     ref = None
-    for form in ("fp64", "3xtf32", "fp32"):
+    for form in ("fp64", "3xtf32", "bf16x9", "fp32"):
         set_gemm_precision(form)
         ms = timed(lambda: T1.matmul(T2))
         Cm = T1.matmul(T2)
@@ -466,7 +466,7 @@ def gemm_sweep(reps=5):
             L.xgb_memcpy_h2d(p_, h.ctypes.data, h.nbytes)
         res = {}
         ref = None
-        for prec, form in ((0, "fp64"), (1, "3xtf32"), (3, "fp32")):
+        for prec, form in ((0, "fp64"), (1, "3xtf32"), (2, "bf16x9"), (3, "fp32")):
             ms = timed(lambda: L.xgb_grouped_gemm(prec, G, arr, bufs[0], bufs[1], bufs[2], 1.0, 0.0, None))
             check(L.xgb_gemm_tc_status(), "tensor-core gemm")
             h = np.empty(int(co))

@@ -95,7 +95,9 @@ typedef struct xgb_gemm_desc {
    as three TF32 tensor-core products (hi*hi + hi*lo + lo*hi) accumulated in FP32
    (about 1e-6 relative); XGB_PREC_FP32: FP64 in and out, operands rounded to
    FP32 and FP32 accumulation on the CUDA cores (about 1e-7 relative per product,
-   growing with k); XGB_PREC_BF16X9 is not available (XGB_E_UNSUPPORTED). */
+   growing with k); XGB_PREC_BF16X9: FP64 in and out, every operand split into three BF16 pieces
+   (24 significant bits) and all nine piece products accumulated in FP32 on the tensor cores
+   (tcgen05.mma kind::f16; about 1e-6 relative, like 3xTF32). */
 int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, const double* A, const double* B,
                      double* C, double alpha, double beta, void* stream);
 /* Synchronises and reports whether a tensor-core GEMM CTA gave up on a bounded

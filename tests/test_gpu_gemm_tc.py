@@ -92,12 +92,48 @@ def test_fp32_form_ragged_blocks(seed):
     assert 0.0 < err < 2e-5  # rounded (not FP64) and within the FP32 budget
 
 
-def test_unavailable_form_is_rejected():
+def test_unknown_form_is_rejected():
     from xped_gb300 import ensure_device, lib
     from xped_gb300._lib import GemmDesc
     ensure_device(0)
     arr = (GemmDesc * 1)(GemmDesc(8, 8, 8, 0, 8, 0, 8, 0, 8, 0, 0))
-    assert lib().xgb_grouped_gemm(2, 1, arr, None, None, None, 1.0, 0.0, None) == -7  # XGB_PREC_BF16X9
+    assert lib().xgb_grouped_gemm(7, 1, arr, None, None, None, 1.0, 0.0, None) == -7  # XGB_E_UNSUPPORTED
+
+
+PREC_BF16X9 = 2
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_bf16x9_form_ragged_blocks(seed):
+    """BF16x9 (three BF16 pieces per operand, nine tensor-core products, FP32 accumulation):
+    relative error ~1e-6 like 3xTF32; bound 2e-5 for k up to 512, and not FP64-exact."""
+    rng = np.random.default_rng(seed)
+    blocks = []
+    for _ in range(30):
+        m, n, k = (int(np.exp(rng.uniform(np.log(8), np.log(512)))) for _ in range(3))
+        blocks.append((m, n, k, int(rng.integers(0, 2)), int(rng.integers(0, 2))))
+    blocks += [(128, 128, 32, 0, 0), (33, 17, 0, 0, 0)]
+    err = _run(blocks, alpha=-0.75, beta=1.5, seed=seed, prec=PREC_BF16X9)
+    assert 0.0 < err < 2e-5
+
+
+def test_bf16x9_form_through_the_tensor_api():
+    from xped_gb300 import Basis, Tensor, ensure_device
+    from xped_gb300.tensor import set_gemm_precision
+    ensure_device(0)
+    rng = np.random.default_rng(13)
+    B = Basis.from_pairs("U1", [(-1, 20), (0, 30), (1, 20)])
+    T1, T2 = Tensor.zeros([B, B], [B, B]), Tensor.zeros([B, B], [B, B])
+    T1.set_data(rng.standard_normal(T1.size))
+    T2.set_data(rng.standard_normal(T2.size))
+    ref = T1.matmul(T2).blocks()
+    set_gemm_precision("bf16x9")
+    try:
+        got = T1.matmul(T2).blocks()
+    finally:
+        set_gemm_precision("fp64")
+    err = max(np.linalg.norm(got[q] - ref[q]) / np.linalg.norm(ref[q]) for q in ref)
+    assert 0.0 < err < 2e-5
 
 
 def test_fp32_form_through_the_tensor_api():

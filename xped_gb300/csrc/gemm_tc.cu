@@ -21,8 +21,14 @@
 //    frees the stage for the next copy; the four warps then read the
 //    accumulator with tcgen05.ld and write FP64.
 //
+// BF16x9 form (same kernels, templated): every FP64 operand is split into three
+// BF16 pieces hi + mid + lo (8-bit significands, 24 bits together) and all nine
+// products of the pieces are accumulated in FP32 with tcgen05.mma kind::f16
+// (BF16 A and B), K = 16 per instruction; chunks are 8 KB (128 x 32 BF16).
+//
 // Every mbarrier wait is bounded; on timeout the CTA records an error flag,
 // skips the epilogue and still frees its TMEM.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -33,12 +39,25 @@ namespace xgb {
 namespace {
 
 constexpr int BM = 128, BN = 128, BK = 32;
-constexpr int kChunkFloats = BM * BK;               // 4096 floats = 16 KB
+constexpr int kChunkFloats = BM * BK;               // 4096 floats = 16 KB (3xTF32 chunk)
 constexpr int kChunkBytes = kChunkFloats * 4;
 constexpr int kStageBytes = 4 * kChunkBytes;        // Ahi, Alo, Bhi, Blo
 constexpr int kStages = 3;
-constexpr int kSmemBytes = kStages * kStageBytes + 1024;  // + alignment slack
+constexpr int kSmemBytes = kStages * kStageBytes + 1024;  // + alignment slack (the larger of the two forms)
 constexpr int kThreads = 128;
+
+// per split form (0 = 3xTF32, 1 = BF16x9): pieces per operand, bytes per element and per chunk,
+// chunk size in float units (the pack buffers are float arrays), stage bytes
+template <int F> struct Form;
+template <> struct Form<0> {
+  static constexpr int pieces = 2, elem = 4, chunk_bytes = BM * BK * 4, chunk_units = chunk_bytes / 4;
+  static constexpr int stage_bytes = 2 * pieces * chunk_bytes, kstep = 8;
+};
+template <> struct Form<1> {
+  static constexpr int pieces = 3, elem = 2, chunk_bytes = BM * BK * 2, chunk_units = chunk_bytes / 4;
+  static constexpr int stage_bytes = 2 * pieces * chunk_bytes, kstep = 16;
+};
+static_assert(kStages * Form<1>::stage_bytes + 1024 <= kSmemBytes, "BF16x9 stages fit the TF32 budget");
 constexpr uint32_t kTmemCols = 128;                 // FP32 accumulator, N = 128 columns
 constexpr long long kSpinLimit = 1ll << 26;
 
@@ -61,11 +80,14 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
   return d;
 }
 
-// kind::tf32 instruction descriptor: FP32 accumulate, TF32 A and B, both K-major, N = BN, M = BM
+// instruction descriptor: FP32 accumulate, both operands K-major, N = BN, M = BM; A and B formats
+// TF32 (code 2, kind::tf32) or BF16 (code 1, kind::f16) - always the same type for A and B
+template <int F>
 __host__ __device__ constexpr uint32_t make_idesc() {
+  constexpr uint32_t fmt = F == 0 ? 2u : 1u;
   return (1u << 4)                       // D format F32
-         | (2u << 7)                     // A format TF32
-         | (2u << 10)                    // B format TF32
+         | (fmt << 7)                    // A format
+         | (fmt << 10)                   // B format
          | (uint32_t(BN >> 3) << 17)     // N >> 3
          | (uint32_t(BM >> 4) << 24);    // M >> 4
 }
@@ -114,13 +136,27 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
 }
 
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+
+template <int F>
+__device__ __forceinline__ void mma_form(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+  if constexpr (F == 0) mma_tf32(tmem_d, adesc, bdesc, idesc, acc);
+  else mma_bf16(tmem_d, adesc, bdesc, idesc, acc);
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
 }
 
 // ----------------------------------------------------------------------------- pack
-// One CTA per chunk pair (hi and lo of one 128-row x 32-K slice of op(A) or op(B)^T).
+// One CTA per 128-row x 32-K slice of op(A) or op(B)^T: its pieces (hi, lo or hi, mid, lo) as chunks.
+template <int F>
 __global__ void __launch_bounds__(256) tc_pack_kernel(const xgb_gemm_desc* __restrict__ descs,
                                                        const TcGroup* __restrict__ groups,
                                                        const TcPackTask* __restrict__ tasks,
@@ -146,8 +182,30 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const xgb_gemm_desc* __res
     X[r][k] = x;
   }
   __syncthreads();
-  const int64_t chunk = (int64_t(t.tile) * gr.slices + t.slice) * 2;
-  float* hi = (isB ? bpack + gr.b_pack : apack + gr.a_pack) + chunk * kChunkFloats;
+  const int64_t chunk = (int64_t(t.tile) * gr.slices + t.slice) * Form<F>::pieces;
+  float* hi = (isB ? bpack + gr.b_pack : apack + gr.a_pack) + chunk * Form<F>::chunk_units;
+  if constexpr (F == 1) {
+    // element (r, k) at byte (k / 8) * LBO + (r / 8) * SBO + (r % 8) * 16 + (k % 8) * 2 of each piece
+    unsigned char* base = reinterpret_cast<unsigned char*>(hi);
+    for (int e = threadIdx.x; e < BM * (BK / 8); e += 256) {
+      const int r = e % BM, kq = e / BM;  // one 16-byte core-matrix row: 8 consecutive K of row r
+      __nv_bfloat16 ph[8], pm[8], pl[8];
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) {
+        const double x = X[r][kq * 8 + kk];
+        ph[kk] = __float2bfloat16_rn(float(x));
+        const double r1 = x - double(__bfloat162float(ph[kk]));
+        pm[kk] = __float2bfloat16_rn(float(r1));
+        const double r2 = r1 - double(__bfloat162float(pm[kk]));
+        pl[kk] = __float2bfloat16_rn(float(r2));
+      }
+      const uint32_t bo = uint32_t(kq) * LBO + uint32_t(r >> 3) * SBO + uint32_t(r & 7) * 16;
+      *reinterpret_cast<uint4*>(base + bo) = *reinterpret_cast<const uint4*>(ph);
+      *reinterpret_cast<uint4*>(base + Form<1>::chunk_bytes + bo) = *reinterpret_cast<const uint4*>(pm);
+      *reinterpret_cast<uint4*>(base + 2 * Form<1>::chunk_bytes + bo) = *reinterpret_cast<const uint4*>(pl);
+    }
+    return;
+  }
   float* lo = hi + kChunkFloats;
   for (int e = threadIdx.x; e < BM * (BK / 4); e += 256) {
     const int r = e % BM, kq = e / BM;  // one 16-byte core-matrix row: 4 consecutive K of row r
@@ -167,6 +225,7 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const xgb_gemm_desc* __res
 }
 
 // ----------------------------------------------------------------------------- gemm
+template <int F>
 __global__ void __launch_bounds__(kThreads, 1)
     gemm_tc_kernel(const xgb_gemm_desc* __restrict__ descs, const TcGroup* __restrict__ groups,
                    const GemmTile* __restrict__ tiles, const float* __restrict__ apack,
@@ -207,9 +266,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem = tmem_slot;
 
   if (nk > 0 && threadIdx.x == 0) {
-    // producer: bulk copies of the four chunks of every slice into the stage ring
-    const float* a_base = apack + gr.a_pack + int64_t(t.tm) * gr.slices * 2 * kChunkFloats;
-    const float* b_base = bpack + gr.b_pack + int64_t(t.tn) * gr.slices * 2 * kChunkFloats;
+    // producer: bulk copies of the A and B pieces of every slice into the stage ring
+    constexpr int P = Form<F>::pieces, CU = Form<F>::chunk_units, CB = Form<F>::chunk_bytes;
+    const float* a_base = apack + gr.a_pack + int64_t(t.tm) * gr.slices * P * CU;
+    const float* b_base = bpack + gr.b_pack + int64_t(t.tn) * gr.slices * P * CU;
     uint32_t ph[kStages] = {0, 0, 0};
     for (int kc = 0; kc < nk; ++kc) {
       const int s = kc % kStages;
@@ -217,30 +277,37 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (!mbar_wait(&empty[s], ph[s])) { atomicExch(&fail, 1); break; }
         ph[s] ^= 1u;
       }
-      unsigned char* st = smem + s * kStageBytes;
-      mbar_expect_tx(&full[s], kStageBytes);
-      bulk_copy(st, a_base + int64_t(kc) * 2 * kChunkFloats, 2 * kChunkBytes, &full[s]);
-      bulk_copy(st + 2 * kChunkBytes, b_base + int64_t(kc) * 2 * kChunkFloats, 2 * kChunkBytes, &full[s]);
+      unsigned char* st = smem + s * Form<F>::stage_bytes;
+      mbar_expect_tx(&full[s], Form<F>::stage_bytes);
+      bulk_copy(st, a_base + int64_t(kc) * P * CU, P * CB, &full[s]);
+      bulk_copy(st + P * CB, b_base + int64_t(kc) * P * CU, P * CB, &full[s]);
       issued = kc + 1;
     }
   } else if (nk > 0 && threadIdx.x == 32) {
-    // MMA issuer: three TF32 products per K step of 8, accumulated in TMEM
-    const uint32_t idesc = make_idesc();
+    // MMA issuer, per K step (8 TF32 or 16 BF16 = two 16-byte K groups): 3xTF32 takes hi*hi + hi*lo +
+    // lo*hi, BF16x9 all nine products of (hi, mid, lo) x (hi, mid, lo); all accumulated in TMEM
+    constexpr int P = Form<F>::pieces, CB = Form<F>::chunk_bytes;
+    const uint32_t idesc = make_idesc<F>();
     uint32_t ph[kStages] = {0, 0, 0};
     for (int kc = 0; kc < nk; ++kc) {
       const int s = kc % kStages;
       if (!mbar_wait(&full[s], ph[s])) { atomicExch(&fail, 1); break; }
       ph[s] ^= 1u;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t base = smem_u32(smem + s * kStageBytes);
-      const uint32_t ahi = base, alo = base + kChunkBytes, bhi = base + 2 * kChunkBytes, blo = base + 3 * kChunkBytes;
+      const uint32_t base = smem_u32(smem + s * Form<F>::stage_bytes);
 #pragma unroll
-      for (int kk = 0; kk < BK / 8; ++kk) {
-        const uint32_t ko = uint32_t(kk) * 2 * LBO;  // 8 TF32 = two 16-byte K groups
-        const uint32_t first = (kc == 0 && kk == 0) ? 0u : 1u;
-        mma_tf32(tmem, make_desc(ahi + ko), make_desc(bhi + ko), idesc, first);
-        mma_tf32(tmem, make_desc(ahi + ko), make_desc(blo + ko), idesc, 1u);
-        mma_tf32(tmem, make_desc(alo + ko), make_desc(bhi + ko), idesc, 1u);
+      for (int kk = 0; kk < BK / Form<F>::kstep; ++kk) {
+        const uint32_t ko = uint32_t(kk) * 2 * LBO;
+        bool first = kc == 0 && kk == 0;
+#pragma unroll
+        for (int i = 0; i < P; ++i)
+#pragma unroll
+          for (int j = 0; j < P; ++j) {
+            if (F == 0 && i + j > 1) continue;  // 3xTF32 drops lo*lo
+            mma_form<F>(tmem, make_desc(base + i * CB + ko), make_desc(base + (P + j) * CB + ko), idesc,
+                        first ? 0u : 1u);
+            first = false;
+          }
       }
       mma_commit(&empty[s]);
       consumed = kc + 1;
@@ -306,8 +373,9 @@ int* g_tc_err = nullptr;
 
 int gemm_tc_tile() { return BM; }
 
-TcPlanHost build_tc_plan(const xgb_gemm_desc* descs, int n) {
+TcPlanHost build_tc_plan(const xgb_gemm_desc* descs, int n, int form) {
   TcPlanHost p;
+  const int64_t per_slice = form == 1 ? Form<1>::pieces * Form<1>::chunk_units : Form<0>::pieces * Form<0>::chunk_units;
   for (int g = 0; g < n; ++g) {
     const xgb_gemm_desc& d = descs[g];
     TcGroup gr{};
@@ -316,8 +384,8 @@ TcPlanHost build_tc_plan(const xgb_gemm_desc* descs, int n) {
     gr.slices = int32_t((d.k + BK - 1) / BK);
     gr.a_pack = p.a_floats;
     gr.b_pack = p.b_floats;
-    p.a_floats += int64_t(gr.a_tiles) * gr.slices * 2 * kChunkFloats;
-    p.b_floats += int64_t(gr.b_tiles) * gr.slices * 2 * kChunkFloats;
+    p.a_floats += int64_t(gr.a_tiles) * gr.slices * per_slice;
+    p.b_floats += int64_t(gr.b_tiles) * gr.slices * per_slice;
     for (int32_t s = 0; s < gr.slices; ++s) {
       for (int32_t t = 0; t < gr.a_tiles; ++t) p.tasks.push_back({g, t, s, 0});
       for (int32_t t = 0; t < gr.b_tiles; ++t) p.tasks.push_back({g, t, s, 1});
@@ -331,20 +399,30 @@ TcPlanHost build_tc_plan(const xgb_gemm_desc* descs, int n) {
 
 void launch_gemm_tc(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
                     const GemmTile* d_tiles, int n_tiles, const double* A, const double* B, float* apack,
-                    float* bpack, double* C, double alpha, double beta, cudaStream_t s) {
+                    float* bpack, double* C, double alpha, double beta, cudaStream_t s, int form) {
   if (n_tiles <= 0) return;
   if (!g_tc_attr) {
-    cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    cudaFuncSetAttribute(gemm_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    cudaFuncSetAttribute(gemm_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
     cudaMalloc(&g_tc_err, sizeof(int));
     cudaMemset(g_tc_err, 0, sizeof(int));
     g_tc_attr = true;
   }
-  if (n_tasks > 0) {
-    tc_pack_kernel<<<n_tasks, 256, 0, s>>>(d_descs, d_groups, d_tasks, A, B, apack, bpack);
-    count_launch();
+  if (form == 1) {
+    if (n_tasks > 0) {
+      tc_pack_kernel<1><<<n_tasks, 256, 0, s>>>(d_descs, d_groups, d_tasks, A, B, apack, bpack);
+      count_launch();
+    }
+    gemm_tc_kernel<1><<<n_tiles, kThreads, kSmemBytes, s>>>(d_descs, d_groups, d_tiles, apack, bpack, C, alpha, beta,
+                                                            g_tc_err);
+  } else {
+    if (n_tasks > 0) {
+      tc_pack_kernel<0><<<n_tasks, 256, 0, s>>>(d_descs, d_groups, d_tasks, A, B, apack, bpack);
+      count_launch();
+    }
+    gemm_tc_kernel<0><<<n_tiles, kThreads, kSmemBytes, s>>>(d_descs, d_groups, d_tiles, apack, bpack, C, alpha, beta,
+                                                            g_tc_err);
   }
-  gemm_tc_kernel<<<n_tiles, kThreads, kSmemBytes, s>>>(d_descs, d_groups, d_tiles, apack, bpack, C, alpha, beta,
-                                                       g_tc_err);
   count_launch();
 }
 

@@ -796,8 +796,9 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
   cudaStream_t s = pick(stream_);
   for (int g = 0; g < n_groups; ++g)
     if (descs[g].m < 0 || descs[g].n < 0 || descs[g].k < 0) return set_error(XGB_E_BADPLAN, "negative GEMM extent");
-  if (precision == XGB_PREC_3XTF32) {
-    TcPlanHost tp = build_tc_plan(descs, n_groups);
+  if (precision == XGB_PREC_3XTF32 || precision == XGB_PREC_BF16X9) {
+    const int form = precision == XGB_PREC_BF16X9 ? 1 : 0;
+    TcPlanHost tp = build_tc_plan(descs, n_groups, form);
     if (tp.tiles.empty()) return XGB_OK;
     double flops = 0;
     for (int g = 0; g < n_groups; ++g) flops += 2.0 * double(descs[g].m) * double(descs[g].n) * double(descs[g].k);
@@ -808,7 +809,7 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
     auto* ap = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.a_floats, 4))));
     auto* bp = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.b_floats, 4))));
     prof_begin(K_GEMM_TC, s);
-    launch_gemm_tc(dd, dg, dk, int(tp.tasks.size()), dt, int(tp.tiles.size()), A, B, ap, bp, C, alpha, beta, s);
+    launch_gemm_tc(dd, dg, dk, int(tp.tasks.size()), dt, int(tp.tiles.size()), A, B, ap, bp, C, alpha, beta, s, form);
     prof_end(K_GEMM_TC, s, flops);
     for (void* p : {static_cast<void*>(dd), static_cast<void*>(dg), static_cast<void*>(dk), static_cast<void*>(dt),
                     static_cast<void*>(ap), static_cast<void*>(bp)})

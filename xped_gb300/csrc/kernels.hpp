@@ -53,7 +53,7 @@ void launch_gemm_f32(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int 
                      const double* B, double* C, double alpha, double beta, cudaStream_t s);
 // precision forms of the block GEMM this build implements (XGB_PREC_*)
 inline bool gemm_precision_available(int p) {
-  return p == XGB_PREC_FP64 || p == XGB_PREC_3XTF32 || p == XGB_PREC_FP32;
+  return p == XGB_PREC_FP64 || p == XGB_PREC_3XTF32 || p == XGB_PREC_FP32 || p == XGB_PREC_BF16X9;
 }
 void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_task_start, int n_tasks, int64_t total,
                     const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s);
@@ -86,11 +86,12 @@ struct TcPlanHost {
   std::vector<GemmTile> tiles;
   int64_t a_floats = 0, b_floats = 0;
 };
-TcPlanHost build_tc_plan(const xgb_gemm_desc* descs, int n);
+// form 0 = 3xTF32, 1 = BF16x9 (pack sizes differ)
+TcPlanHost build_tc_plan(const xgb_gemm_desc* descs, int n, int form = 0);
 int gemm_tc_tile();
 void launch_gemm_tc(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
                     const GemmTile* d_tiles, int n_tiles, const double* A, const double* B, float* apack,
-                    float* bpack, double* C, double alpha, double beta, cudaStream_t s);
+                    float* bpack, double* C, double alpha, double beta, cudaStream_t s, int form = 0);
 int gemm_tc_error(bool reset);  // 1 if a tensor-core GEMM CTA gave up waiting (synchronous read)
 
 // randomized tSVD helpers (rsvd.cu)

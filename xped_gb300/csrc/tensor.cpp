@@ -598,6 +598,29 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
     dev_free(bp);
     return out;
   }
+  if (g_gemm_precision == XGB_PREC_BF16X9) {  // tables built per call (the cached ones are the 3xTF32 layout)
+    TcPlanHost tp = build_tc_plan(plan->host_descs.data(), int(plan->host_descs.size()), 1);
+    cudaStream_t st = stream();
+    auto* dg = static_cast<TcGroup*>(dev_alloc(sizeof(TcGroup) * std::max<size_t>(tp.groups.size(), 1)));
+    auto* dk = static_cast<TcPackTask*>(dev_alloc(sizeof(TcPackTask) * std::max<size_t>(tp.tasks.size(), 1)));
+    auto* dt = static_cast<GemmTile*>(dev_alloc(sizeof(GemmTile) * std::max<size_t>(tp.tiles.size(), 1)));
+    cuda_ok(cudaMemcpyAsync(dg, tp.groups.data(), sizeof(TcGroup) * tp.groups.size(), cudaMemcpyHostToDevice, st), "h2d");
+    if (!tp.tasks.empty())
+      cuda_ok(cudaMemcpyAsync(dk, tp.tasks.data(), sizeof(TcPackTask) * tp.tasks.size(), cudaMemcpyHostToDevice, st),
+              "h2d");
+    cuda_ok(cudaMemcpyAsync(dt, tp.tiles.data(), sizeof(GemmTile) * tp.tiles.size(), cudaMemcpyHostToDevice, st), "h2d");
+    auto* ap = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.a_floats, 4))));
+    auto* bp = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.b_floats, 4))));
+    prof_begin(K_GEMM_TC, st);
+    launch_gemm_tc(plan->d_descs, dg, dk, int(tp.tasks.size()), dt, int(tp.tiles.size()), a.data(), b.data(), ap, bp,
+                   out.data(), 1.0, 0.0, st, 1);
+    prof_end(K_GEMM_TC, st, plan->flops);
+    cuda_ok(cudaStreamSynchronize(st), "sync");  // the host tables above are pageable
+    for (void* p : {static_cast<void*>(dg), static_cast<void*>(dk), static_cast<void*>(dt), static_cast<void*>(ap),
+                    static_cast<void*>(bp)})
+      dev_free(p);
+    return out;
+  }
   if (g_gemm_precision == XGB_PREC_FP32) {
     prof_begin(K_GEMM_F32, stream());
     launch_gemm_f32(plan->d_descs, plan->d_tiles, plan->n_tiles, plan->tile, a.data(), b.data(), out.data(), 1.0, 0.0,

@@ -16,7 +16,7 @@ import numpy as np
 from ._lib import (PermContrib, PermTask, GemmDesc, check, check_handle, ensure_device, lib)
 
 SYM_IDS = {"U1": 0, "fU1": 1, "Z2": 2, "fZ2": 3, "SU2": 4}
-GEMM_FORMS = {"fp64": 0, "3xtf32": 1, "fp32": 3}  # XGB_PREC_* of xgb.h
+GEMM_FORMS = {"fp64": 0, "3xtf32": 1, "bf16x9": 2, "fp32": 3}  # XGB_PREC_* of xgb.h
 
 
 def _i32(seq):
