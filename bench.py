@@ -51,6 +51,7 @@ AUX_SMALL = [(-1, 1), (0, 2), (1, 1)]  # D=4, chi=32: the plain FP64 GPU configu
 CHI_SMALL = 32
 COMPARE_STEPS = 3
 POWER_ITERS = 8  # subspace iterations of the chosen form: energy within ~1e-9 of plain FP64 at this workload
+SKETCH_TAIL = 2  # trailing subspace iterations in FP64; the first product and the earlier ones in 3xTF32
 METRIC = "CTMRG step throughput, U(1) iPEPS D=6 chi=128, chosen form vs plain FP64"
 WORKLOAD = "u1_ipeps_D6_chi128_ctmrg_step"
 
@@ -139,11 +140,12 @@ def site_tensor(aux_pairs):
     return A, phys
 
 
-def make_ctm(A, chi, form, gemm):
+def make_ctm(A, chi, form, gemm, tail=-1):
     from xped_gb300 import CTM
     c = CTM(A, chi).init()
     if form == "chosen":
         c.set_svd("randomized", power_iters=POWER_ITERS, seed=SEED, oversample=16, growth=0.5)
+        c.set_sketch_precision(tail)
     c.set_gemm(gemm)
     return c
 
@@ -166,7 +168,7 @@ def run_gpu(args):
     # ---- chosen form: warm-up (the energy after COMPARE_STEPS steps is kept for the comparison);
     # its projector decompositions are logged to train the width predictor
     t0 = time.perf_counter()
-    ctm = make_ctm(A, CHI, "chosen", args.gemm)
+    ctm = make_ctm(A, CHI, "chosen", args.gemm, args.sketch_tail)
     ctm.record(True)
     e_chosen = None
     for i in range(max(args.warmup, COMPARE_STEPS)):
@@ -275,6 +277,7 @@ def run_gpu(args):
                                 "loss_last": loss, "seconds": time.perf_counter() - t0}
         lc = make_ctm(A, CHI, "plain", args.gemm)
         lc.set_rank_model(model, margin=0.0, min_oversample=2, power_iters=POWER_ITERS, seed=SEED)
+        lc.set_sketch_precision(args.sketch_tail)
         for _ in range(COMPARE_STEPS):
             lc.grow_all()
         res["e_learned"] = energy(lc, H)
@@ -366,6 +369,7 @@ def run_fz2(args):
         if form == "chosen":
             c.set_svd("randomized", power_iters=POWER_ITERS, seed=SEED, oversample=16, growth=0.5)
             c.set_sketch_unseen(True)
+            c.set_sketch_precision(args.sketch_tail)
             c.set_gemm(args.gemm)
         ms, marks = [], {}
         for i in range(iters):
@@ -887,6 +891,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--gemm", default="fp64", choices=["fp64", "3xtf32", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sketch-tail", type=int, default=SKETCH_TAIL,
+                    help="subspace iterations of the chosen form kept in FP64 at the end; the earlier ones "
+                         "(and the first sketch product) multiply as 3xTF32 tensor-core GEMMs (< 0: all FP64)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-width run")
     ap.add_argument("--workload", default="u1", choices=["u1", "fz2"],
@@ -968,11 +975,14 @@ def main():
     g = prof.get(gemm_kind, (0, 0.0, 0.0))
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if args.gemm == "fp64" else f"f64 ({args.gemm} block GEMMs)",
+            "vs_baseline": None, "dtype": ("f64" if args.gemm == "fp64" else f"f64 ({args.gemm} block GEMMs)")
+            + (" + 3xTF32 early sketch products" if args.sketch_tail >= 0 else ""),
             "data": "synthetic (seeded N(0,1) site tensor)",
             "config": dict(config, form=f"chosen: randomized projector SVD ({POWER_ITERS} subspace iterations, "
                                         "CholeskyQR3 bases, widths last kept + max(16, 50%), exact first decomposition "
-                                        "per direction and exact FP64 fallback), FP64 SVD core",
+                                        "per direction and exact FP64 fallback), FP64 SVD core"
+                                        + (f"; sketch products of the first {POWER_ITERS - args.sketch_tail} "
+                                           "iterations 3xTF32" if args.sketch_tail >= 0 else ""),
                            gemm=args.gemm, parallelism=f"replicas x{world}"),
             "e2e": {"value": world * 1e3 / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"]},
@@ -989,6 +999,8 @@ def main():
         line["energy"] = {"after_steps": COMPARE_STEPS, "chosen": r["e_chosen"], "plain": r["e_plain"],
                           "abs_diff": abs(r["e_chosen"] - r["e_plain"]),
                           "observable": "Heisenberg energy per site (rho_h + rho_v bonds)"}
+    else:
+        line["energy"] = {"after_steps": COMPARE_STEPS, "chosen": r["e_chosen"]}
     if "learned_ms" in r:
         line["learned_widths"] = {"ms_per_step": r["learned_ms"], "steps_per_s": 1e3 / r["learned_ms"],
                                   "sketch_cols_per_step": r["learned_cols_per_step"],

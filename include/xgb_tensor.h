@@ -168,6 +168,12 @@ int xgb_ctm_set_gemm_precision(xgb_ctm c, int precision);
    randomized form: exact FP64 tSVD (on = 0, the default) or a sketch of
    min(chi, min(rows, cols)) + 16 columns (on = 1), for either width rule. */
 int xgb_ctm_set_sketch_unseen(xgb_ctm c, int on);
+/* Products of the randomized projector SVD's subspace iterations: fp64_tail >= 0
+   runs the first product A Omega and all but the last fp64_tail iterations as
+   3xTF32 tensor-core GEMMs (FP32 accumulation), the last fp64_tail iterations, the
+   projection and the small SVDs in FP64; fp64_tail < 0 (the default) keeps every
+   product FP64. */
+int xgb_ctm_set_sketch_precision(xgb_ctm c, int fp64_tail);
 /* Warm start of the randomized projector SVD: the direction's previous V^dag seeds
    the sketch and warm_iters subspace iterations are run instead of power_iters
    (warm_iters < 0: off, the default). */

@@ -155,3 +155,28 @@ def test_warm_started_projectors_keep_the_energy():
     e_ex, e_rz = energy(ex, H), energy(rz, H)
     print("energy exact", e_ex, "warm", e_rz, "diff", abs(e_ex - e_rz))
     assert abs(e_ex - e_rz) < 1e-8
+
+
+def test_tensor_core_sketch_iterations_keep_the_energy():
+    """Randomized projector SVD with 8 subspace iterations whose first product and
+    first six iterations multiply as 3xTF32 tensor-core GEMMs (the last two
+    iterations, the projection and the small SVDs in FP64): energy per site within
+    1e-8 of the all-FP64 randomized run and of the exact tSVD after four steps."""
+    from xped_gb300.observables import energy, heisenberg_bond
+    aux = [(-1, 2), (0, 2), (1, 2)]
+    _, ex = _setup("u1", aux, [(-1, 1), (1, 1)], 48, 3)
+    _, rz = _setup("u1", aux, [(-1, 1), (1, 1)], 48, 3)
+    _, tc = _setup("u1", aux, [(-1, 1), (1, 1)], 48, 3)
+    for c in (rz, tc):
+        c.set_svd("randomized", power_iters=8, oversample=16, growth=0.5)
+    tc.set_sketch_precision(2)
+    for _ in range(4):
+        ex.grow_all()
+        rz.grow_all()
+        tc.grow_all()
+    assert tc.stats()["sketched_sectors"] > 0
+    H = heisenberg_bond(ex.get("A").leg(4))
+    e_ex, e_rz, e_tc = energy(ex, H), energy(rz, H), energy(tc, H)
+    print("energy exact", e_ex, "fp64 sketch", e_rz, "tc sketch", e_tc, "diff", abs(e_rz - e_tc), abs(e_ex - e_tc))
+    assert abs(e_rz - e_tc) < 1e-8
+    assert abs(e_ex - e_tc) < 1e-8

@@ -406,6 +406,13 @@ int xgb_ctm_set_sketch_unseen(xgb_ctm c, int on) {
   })
 }
 
+int xgb_ctm_set_sketch_precision(xgb_ctm c, int fp64_tail) {
+  GUARD(XGB_E_BADPLAN, {
+    c->c->sketch_fp64_tail = fp64_tail < 0 ? -1 : fp64_tail;
+    return XGB_OK;
+  })
+}
+
 int xgb_ctm_set_warm_start(xgb_ctm c, int warm_iters) {
   GUARD(XGB_E_BADPLAN, {
     c->c->warm_iters = warm_iters < 0 ? -1 : warm_iters;

@@ -103,6 +103,35 @@ void grouped_gemm(const std::vector<xgb_gemm_desc>& d, const double* A, const do
   prof_end(K_GEMM, s, flops);
 }
 
+void gemm_fp64(const std::vector<xgb_gemm_desc>& d, const double* A, const double* B, double* C, cudaStream_t s) {
+  grouped_gemm(d, A, B, C, s);
+}
+
+// Grouped 3xTF32 tensor-core GEMM (gemm_tc.cu) for the early products of a subspace
+// iteration: their bases only have to approach the dominant subspace, which the
+// trailing FP64 iterations then resolve to FP64 accuracy.  Operands are packed
+// per call; a CTA that gives up waiting sets the tensor-core error flag, read
+// after the decomposition's residual synchronisation.
+void grouped_gemm_tc(const std::vector<xgb_gemm_desc>& d, const double* A, const double* B, double* C,
+                     cudaStream_t s) {
+  if (d.empty()) return;
+  TcPlanHost tp = build_tc_plan(d.data(), int(d.size()), 0);
+  if (tp.tiles.empty()) return;
+  double flops = 0;
+  for (const auto& g : d) flops += 2.0 * double(g.m) * double(g.n) * double(g.k);
+  Staging st;
+  const size_t od = st.add(d), og = st.add(tp.groups), ok_ = st.add(tp.tasks), ot = st.add(tp.tiles);
+  st.upload(s);
+  auto* ap = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.a_floats, 4))));
+  auto* bp = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.b_floats, 4))));
+  prof_begin(K_GEMM_TC, s);
+  launch_gemm_tc(st.at<xgb_gemm_desc>(od), st.at<TcGroup>(og), st.at<TcPackTask>(ok_), int(tp.tasks.size()),
+                 st.at<GemmTile>(ot), int(tp.tiles.size()), A, B, ap, bp, C, 1.0, 0.0, s, 0);
+  prof_end(K_GEMM_TC, s, flops);
+  dev_free(ap);
+  dev_free(bp);
+}
+
 // Batched thin SVD through the cluster Jacobi kernel (work counted as the thin R-SVD flop count
 // 6 m n^2 + 20 n^3, m >= n, Golub & Van Loan, Matrix Computations, Table 5.5.1).
 void batched_svd(const std::vector<xgb_svd_desc>& d, const double* A, double* U, double* S, double* Vt, cudaStream_t s) {
@@ -196,13 +225,16 @@ constexpr int kMaxRefine = 3;  // refinement passes of unconverged sectors per r
 }  // namespace
 
 SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, const std::vector<int64_t>& sketch,
-                          int power_iters, uint64_t seed, RsvdInfo* info, const Tensor* warm, double res_tol) {
+                          int power_iters, uint64_t seed, RsvdInfo* info, const Tensor* warm, double res_tol,
+                          int fp64_tail) {
   Tensor t = materialize(t0);
   const TensorMeta& m = *t.meta;
   const int n = int(m.sectors.size());
   if (n == 0) throw std::runtime_error("tSVD of a tensor without sectors");
   if (int(sketch.size()) != n) throw std::runtime_error("randomized tSVD: one sketch width per sector required");
   if (power_iters < 0) throw std::runtime_error("randomized tSVD: negative number of power iterations");
+  // leading iterations (and the first product A Omega) on the tensor cores; the last fp64_tail in FP64
+  const int tc_iters = fp64_tail >= 0 ? std::max(0, power_iters - fp64_tail) : 0;
   cudaStream_t st = stream();
   // warm-start rows per sector (a V^dag block of the same charge and column dimension)
   Tensor warm_t;
@@ -279,8 +311,9 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
     double* Z = nr ? alloc_d(zt) : nullptr;
 
     // subspace iterations Q <- orth(A orth(A^T Q)) for the sketched sectors `sub` (indices into R);
-    // the basis enters in `cur` (Q or Y) and leaves in Q (last orthonormalisation with 3 passes)
-    auto iterate = [&](const std::vector<int>& sub, int iters, double* cur) {
+    // the basis enters in `cur` (Q or Y) and leaves in Q (last orthonormalisation with 3 passes);
+    // the products of the first `tc_iters` iterations run as 3xTF32 tensor-core GEMMs
+    auto iterate = [&](const std::vector<int>& sub, int iters, double* cur, int tc_iters) {
       std::vector<int64_t> srr, src, srl, syo, szo;
       for (int a : sub) {
         srr.push_back(rr[a]);
@@ -293,12 +326,12 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       for (int p = 0; p < iters; ++p) {
         g.clear();
         for (int a : sub) g.push_back({rc[a], rl[a], rr[a], m.offset[R[a]], rr[a], yo[a], rr[a], zo[a], rc[a], 1, 0});
-        grouped_gemm(g, t.data(), cur, Z, st);
+        (p < tc_iters ? grouped_gemm_tc : gemm_fp64)(g, t.data(), cur, Z, st);
         // Omega's storage holds Qz (same layout as Z)
         double* qz = orthonormalise(src, srl, szo, Z, Om, st, kInterPasses);
         g.clear();
         for (int a : sub) g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], zo[a], rc[a], yo[a], rr[a], 0, 0});
-        grouped_gemm(g, t.data(), qz, Y, st);
+        (p < tc_iters ? grouped_gemm_tc : gemm_fp64)(g, t.data(), qz, Y, st);
         cur = orthonormalise(srr, srl, syo, Y, Q, st, p + 1 == iters ? 3 : kInterPasses);
       }
     };
@@ -410,11 +443,11 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       std::vector<xgb_gemm_desc> g;
       for (int a = 0; a < nr; ++a)
         g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], om[a], rc[a], yo[a], rr[a], 0, 0});
-      grouped_gemm(g, t.data(), Om, Y, st);
+      (tc_iters > 0 ? grouped_gemm_tc : gemm_fp64)(g, t.data(), Om, Y, st);
       double* q0 = orthonormalise(rr, rl, yo, Y, Q, st, power_iters > 0 ? kInterPasses : 3);
       std::vector<int> all(nr);
       for (int a = 0; a < nr; ++a) all[a] = a;
-      iterate(all, power_iters, q0);
+      iterate(all, power_iters, q0, tc_iters);
     }
     // ---- exact sectors: their blocks join the batched SVD of the projected blocks
     if (!E.empty()) {
@@ -472,6 +505,8 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       std::vector<double> rh(size_t(std::max<int64_t>(rtot, 1)));
       ok(cudaMemcpyAsync(rh.data(), rv, sizeof(double) * size_t(rtot), cudaMemcpyDeviceToHost, st), "d2h residuals");
       ok(cudaStreamSynchronize(st), "sync");
+      if (tc_iters > 0 && pass == 0 && gemm_tc_error(true))
+        throw std::runtime_error("randomized tSVD: a tensor-core GEMM CTA gave up waiting for its MMAs");
       dev_free(rv);
       dev_free(Rb);
       std::vector<int> bad;
@@ -485,7 +520,7 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       max_res = worst;
       if (bad.empty() || pass >= kMaxRefine) break;
       ++refinements;
-      iterate(bad, std::max(power_iters, 1), Q);
+      iterate(bad, std::max(power_iters, 1), Q, 0);
       project(bad, {});
       res = truncate_spectra(m, sp, max_keep, eps_svd, false);
     }

@@ -1338,7 +1338,8 @@ std::pair<Tensor, Tensor> CTM::decompose_dir(int d, const Tensor& t1, const Tens
     RsvdInfo info;
     const bool warm = warm_iters >= 0 && warm_v[d].valid() && warm_v[d].meta->cod == m.cod;
     r = tsvd_randomized(prod, chi, 1.0e-10, want, warm ? warm_iters : power_iters,
-                        seed + uint64_t(stats.decompositions), &info, warm ? &warm_v[d] : nullptr, res_tol);
+                        seed + uint64_t(stats.decompositions), &info, warm ? &warm_v[d] : nullptr, res_tol,
+                        sketch_fp64_tail);
     stats.refinements += info.refinements;
     stats.max_residual = info.max_residual;
     width = info.width;

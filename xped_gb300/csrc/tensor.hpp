@@ -139,9 +139,13 @@ struct RsvdInfo {
 // sector q (the remaining columns stay Gaussian).
 // `res_tol` > 0: sectors whose kept triplets have ||A v_j - s_j u_j|| > res_tol * s_max
 // get power_iters more subspace iterations from their current basis (up to three times).
+// `fp64_tail` >= 0: the first product A Omega and the products of all but the last
+// fp64_tail subspace iterations run as 3xTF32 tensor-core GEMMs (FP32 accumulation);
+// the trailing iterations, the projection and everything after it stay FP64.
+// < 0 (the default): every product in FP64.
 SVDResult tsvd_randomized(const Tensor& t, int64_t max_keep, double eps_svd, const std::vector<int64_t>& sketch,
                           int power_iters, uint64_t seed, RsvdInfo* info = nullptr, const Tensor* warm = nullptr,
-                          double res_tol = 0.0);
+                          double res_tol = 0.0, int fp64_tail = -1);
 std::pair<Tensor, Tensor> tqr(const Tensor& t);
 std::pair<Tensor, Tensor> decompose(const Tensor& t1, const Tensor& t2, int64_t max_nsv);
 
@@ -231,6 +235,9 @@ class CTM {
   // > 0: kept sketched triplets must satisfy ||A v - s u|| <= res_tol * s_max
   // (unconverged sectors get more subspace iterations)
   double res_tol = 0.0;
+  // >= 0: all but the last sketch_fp64_tail subspace iterations of the randomized
+  // projector SVD multiply in 3xTF32 on the tensor cores; < 0: all FP64
+  int sketch_fp64_tail = -1;
   uint64_t seed = 1;
   std::shared_ptr<WidthPolicy> policy;
   bool record = false;

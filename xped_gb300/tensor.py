@@ -434,6 +434,13 @@ class CTM:
         check(lib().xgb_ctm_set_sketch_unseen(self._h, int(on)), "ctm_set_sketch_unseen")
         return self
 
+    def set_sketch_precision(self, fp64_tail: int = 2):
+        """Run the first sketch product and all but the last fp64_tail subspace
+        iterations of the randomized projector SVD as 3xTF32 tensor-core GEMMs
+        (negative: every product FP64, the default)."""
+        check(lib().xgb_ctm_set_sketch_precision(self._h, int(fp64_tail)), "ctm_set_sketch_precision")
+        return self
+
     def set_warm_start(self, warm_iters: int = 2):
         """Seed each randomized projector SVD with the direction's previous V^dag and
         run warm_iters subspace iterations (negative: off)."""
