@@ -340,16 +340,19 @@ FZ2_AUX = [(0, 3), (1, 3)]   # D = 6
 FZ2_PHYS = [(0, 1), (1, 1)]  # spinless fermion: empty / occupied
 FZ2_CHI = 144
 FZ2_ITERS = 20
+FZ2_MARK = 2  # step after which the bond observable is compared with the plain form
 
 
 def run_fz2(args):
     """Fermionic Z2 iPEPS (ZN<FChargeU1,2>), D=6 with q in {0,1} and degeneracies [3,3], physical
     parity 0/1, chi=144: FZ2_ITERS CTMRG iterations of the chosen form from FROM_A, every step
     timed with CUDA events (the chosen form sketches the first decomposition of each direction too:
-    chi + 16 columns); the density-density bond expectation after --fz2-plain-steps steps and after
-    the last one.  The plain FP64 form runs --fz2-plain-steps steps from the same start
-    (its exact SVDs of ~2600-wide sector blocks take minutes per step)."""
+    chi + 16 columns); then the same iterations with learned widths (the rank predictor trained on
+    the chosen run's own logged decompositions, device Adam); the density-density bond expectation
+    after FZ2_MARK steps and after the last one.  The plain FP64 form runs --fz2-plain-steps steps
+    from the same start (its exact SVDs of ~2600-wide sector blocks take minutes per step)."""
     from xped_gb300 import CTM, Basis, Tensor, ensure_device, lib
+    from xped_gb300.learn import RankModel, dataset
     from xped_gb300.observables import density_bond, energy
 
     _, _, local = dist_info()
@@ -362,12 +365,17 @@ def run_fz2(args):
     H = density_bond(phys)
     npl = args.fz2_plain_steps
     out = {}
-    for form, iters in (("chosen", FZ2_ITERS), ("plain", npl)):
+    model = None
+    for form, iters in (("chosen", FZ2_ITERS), ("learned", FZ2_ITERS), ("plain", npl)):
         if iters <= 0:
             continue
         c = CTM(A, FZ2_CHI).init()
         if form == "chosen":
             c.set_svd("randomized", power_iters=POWER_ITERS, seed=SEED, oversample=16, growth=0.5)
+            c.record(True)
+        elif form == "learned":
+            c.set_rank_model(model, margin=0.0, min_oversample=2, power_iters=POWER_ITERS, seed=SEED)
+        if form != "plain":
             c.set_sketch_unseen(True)
             c.set_sketch_precision(args.sketch_tail)
             c.set_gemm(args.gemm)
@@ -378,23 +386,34 @@ def run_fz2(args):
             c.grow_all()
             L.xgb_event_record(13)
             ms.append(L.xgb_event_elapsed_ms(12, 13))
-            if i + 1 == npl:
-                marks["nn_bond_at_plain_steps"] = energy(c, H)
+            if i + 1 == FZ2_MARK:
+                marks["nn_bond_at_mark"] = energy(c, H)
         out[form] = dict(marks, ms_per_step_each=[round(x, 2) for x in ms], total_s=sum(ms) / 1e3,
                          ms_per_step_after_1=float(np.mean(ms[1:])) if len(ms) > 1 else None,
                          nn_bond_last=energy(c, H), stats=c.stats())
+        if form == "chosen":
+            X, T = dataset(c.records())
+            c.record(False)
+            model = RankModel(seed=SEED)
+            t0 = time.perf_counter()
+            loss = model.train(X, T, steps=2000, lr=2e-3)
+            out["learned_train"] = {"samples": int(X.shape[0]), "adam_steps": 2000, "loss_last": loss,
+                                    "seconds": time.perf_counter() - t0}
+        del c
     ch = out["chosen"]
     line = {"metric": f"CTMRG iterations, fermionic Z2 iPEPS D=6 chi={FZ2_CHI}, chosen form",
             "value": 1e3 / float(np.mean(ch["ms_per_step_each"][3:])), "unit": "steps/s", "n_gpus": 1,
             "steps": FZ2_ITERS, "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded N(0,1))",
             "config": {"workload": f"fz2_ipeps_D6_chi{FZ2_CHI}_{FZ2_ITERS}_iterations", "aux": "q 0,1 deg [3,3]",
-                       "phys": "q 0,1", "gemm": args.gemm,
+                       "phys": "q 0,1", "gemm": args.gemm, "sketch_fp64_tail": args.sketch_tail,
                        "graph_capture": "none: every move synchronises on the host for the truncation result"},
             "forms": out}
     if "plain" in out and out["plain"]["ms_per_step_after_1"]:
         line["chosen_vs_plain_per_step"] = out["plain"]["ms_per_step_after_1"] / ch["ms_per_step_after_1"]
-        line["nn_bond_abs_diff_after_plain_steps"] = abs(out["plain"]["nn_bond_at_plain_steps"] -
-                                                         ch["nn_bond_at_plain_steps"])
+        if "nn_bond_at_mark" in out["plain"]:
+            for f in ("chosen", "learned"):
+                line[f"nn_bond_abs_diff_{f}_vs_plain_at_step_{FZ2_MARK}"] = abs(out["plain"]["nn_bond_at_mark"] -
+                                                                              out[f]["nn_bond_at_mark"])
     print(json.dumps(line))
 
 
