@@ -426,6 +426,16 @@ void launch_gemm_tc(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const
   count_launch();
 }
 
+void launch_tc_pack(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
+                    const double* A, const double* B, float* apack, float* bpack, cudaStream_t s, int form) {
+  if (n_tasks <= 0) return;
+  if (form == 1)
+    tc_pack_kernel<1><<<n_tasks, 256, 0, s>>>(d_descs, d_groups, d_tasks, A, B, apack, bpack);
+  else
+    tc_pack_kernel<0><<<n_tasks, 256, 0, s>>>(d_descs, d_groups, d_tasks, A, B, apack, bpack);
+  count_launch();
+}
+
 int gemm_tc_error(bool reset) {
   if (!g_tc_err) return 0;
   int h = 0;

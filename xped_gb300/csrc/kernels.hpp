@@ -92,6 +92,10 @@ int gemm_tc_tile();
 void launch_gemm_tc(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
                     const GemmTile* d_tiles, int n_tiles, const double* A, const double* B, float* apack,
                     float* bpack, double* C, double alpha, double beta, cudaStream_t s, int form = 0);
+// the pack step of launch_gemm_tc alone (operands packed once and reused by later launches
+// whose task lists leave them out)
+void launch_tc_pack(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
+                    const double* A, const double* B, float* apack, float* bpack, cudaStream_t s, int form = 0);
 int gemm_tc_error(bool reset);  // 1 if a tensor-core GEMM CTA gave up waiting (synchronous read)
 
 // randomized tSVD helpers (rsvd.cu)

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -103,34 +104,57 @@ void grouped_gemm(const std::vector<xgb_gemm_desc>& d, const double* A, const do
   prof_end(K_GEMM, s, flops);
 }
 
-void gemm_fp64(const std::vector<xgb_gemm_desc>& d, const double* A, const double* B, double* C, cudaStream_t s) {
-  grouped_gemm(d, A, B, C, s);
-}
+// 3xTF32 tensor-core products op(A_q) X_q (gemm_tc.cu) over a fixed list of sector GEMMs, for the
+// early products of a subspace iteration: their bases only have to approach the dominant
+// subspace, which the trailing FP64 iterations then resolve to FP64 accuracy.  op(A_q) is split
+// into TF32 hi / lo chunks once, at construction; every apply() packs only X and runs the MMA
+// kernel.  A CTA that gives up waiting sets the tensor-core error flag, read after the
+// decomposition's residual synchronisation.
+class TcProducts {
+ public:
+  TcProducts(const std::vector<xgb_gemm_desc>& d, const double* A, cudaStream_t s) {
+    TcPlanHost tp = build_tc_plan(d.data(), int(d.size()), 0);
+    std::vector<TcPackTask> ta, tb;
+    for (const auto& t : tp.tasks) (t.which == 0 ? ta : tb).push_back(t);
+    n_tiles_ = int(tp.tiles.size());
+    n_b_ = int(tb.size());
+    for (const auto& g : d) flops_ += 2.0 * double(g.m) * double(g.n) * double(g.k);
+    od_ = st_.add(d);
+    og_ = st_.add(tp.groups);
+    oa_ = st_.add(ta);
+    ob_ = st_.add(tb);
+    ot_ = st_.add(tp.tiles);
+    st_.upload(s);
+    ap_ = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.a_floats, 4))));
+    bp_ = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.b_floats, 4))));
+    prof_begin(K_GEMM_TC, s);
+    launch_tc_pack(st_.at<xgb_gemm_desc>(od_), st_.at<TcGroup>(og_), st_.at<TcPackTask>(oa_), int(ta.size()), A,
+                   nullptr, ap_, bp_, s, 0);
+    prof_end(K_GEMM_TC, s, 0.0);
+  }
+  TcProducts(const TcProducts&) = delete;
+  TcProducts& operator=(const TcProducts&) = delete;
+  ~TcProducts() {
+    dev_free(ap_);
+    dev_free(bp_);
+  }
+  // C = op(A) X with the A packed at construction
+  void apply(const double* A, const double* X, double* C, cudaStream_t s) {
+    if (n_tiles_ == 0) return;
+    prof_begin(K_GEMM_TC, s);
+    launch_gemm_tc(st_.at<xgb_gemm_desc>(od_), st_.at<TcGroup>(og_), st_.at<TcPackTask>(ob_), n_b_,
+                   st_.at<GemmTile>(ot_), n_tiles_, A, X, ap_, bp_, C, 1.0, 0.0, s, 0);
+    prof_end(K_GEMM_TC, s, flops_);
+  }
 
-// Grouped 3xTF32 tensor-core GEMM (gemm_tc.cu) for the early products of a subspace
-// iteration: their bases only have to approach the dominant subspace, which the
-// trailing FP64 iterations then resolve to FP64 accuracy.  Operands are packed
-// per call; a CTA that gives up waiting sets the tensor-core error flag, read
-// after the decomposition's residual synchronisation.
-void grouped_gemm_tc(const std::vector<xgb_gemm_desc>& d, const double* A, const double* B, double* C,
-                     cudaStream_t s) {
-  if (d.empty()) return;
-  TcPlanHost tp = build_tc_plan(d.data(), int(d.size()), 0);
-  if (tp.tiles.empty()) return;
-  double flops = 0;
-  for (const auto& g : d) flops += 2.0 * double(g.m) * double(g.n) * double(g.k);
-  Staging st;
-  const size_t od = st.add(d), og = st.add(tp.groups), ok_ = st.add(tp.tasks), ot = st.add(tp.tiles);
-  st.upload(s);
-  auto* ap = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.a_floats, 4))));
-  auto* bp = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.b_floats, 4))));
-  prof_begin(K_GEMM_TC, s);
-  launch_gemm_tc(st.at<xgb_gemm_desc>(od), st.at<TcGroup>(og), st.at<TcPackTask>(ok_), int(tp.tasks.size()),
-                 st.at<GemmTile>(ot), int(tp.tiles.size()), A, B, ap, bp, C, 1.0, 0.0, s, 0);
-  prof_end(K_GEMM_TC, s, flops);
-  dev_free(ap);
-  dev_free(bp);
-}
+ private:
+  Staging st_;
+  size_t od_ = 0, og_ = 0, oa_ = 0, ob_ = 0, ot_ = 0;
+  int n_tiles_ = 0, n_b_ = 0;
+  double flops_ = 0;
+  float* ap_ = nullptr;
+  float* bp_ = nullptr;
+};
 
 // Batched thin SVD through the cluster Jacobi kernel (work counted as the thin R-SVD flop count
 // 6 m n^2 + 20 n^3, m >= n, Golub & Van Loan, Matrix Computations, Table 5.5.1).
@@ -312,8 +336,12 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
 
     // subspace iterations Q <- orth(A orth(A^T Q)) for the sketched sectors `sub` (indices into R);
     // the basis enters in `cur` (Q or Y) and leaves in Q (last orthonormalisation with 3 passes);
-    // the products of the first `tc_iters` iterations run as 3xTF32 tensor-core GEMMs
-    auto iterate = [&](const std::vector<int>& sub, int iters, double* cur, int tc_iters) {
+    // the products of the first `tc_iters` iterations run as 3xTF32 tensor-core GEMMs through
+    // tc_t (A^T X) and tc_n (A X), which cover all sketched sectors (sub = all)
+    auto iterate = [&](const std::vector<int>& sub, int iters, double* cur, int tc_iters, TcProducts* tc_t,
+                       TcProducts* tc_n) {
+      if (tc_iters > 0 && (!tc_t || !tc_n || int(sub.size()) != nr))
+        throw std::logic_error("randomized tSVD: tensor-core products need every sketched sector");
       std::vector<int64_t> srr, src, srl, syo, szo;
       for (int a : sub) {
         srr.push_back(rr[a]);
@@ -324,14 +352,22 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       }
       std::vector<xgb_gemm_desc> g;
       for (int p = 0; p < iters; ++p) {
-        g.clear();
-        for (int a : sub) g.push_back({rc[a], rl[a], rr[a], m.offset[R[a]], rr[a], yo[a], rr[a], zo[a], rc[a], 1, 0});
-        (p < tc_iters ? grouped_gemm_tc : gemm_fp64)(g, t.data(), cur, Z, st);
+        if (p < tc_iters) {
+          tc_t->apply(t.data(), cur, Z, st);
+        } else {
+          g.clear();
+          for (int a : sub) g.push_back({rc[a], rl[a], rr[a], m.offset[R[a]], rr[a], yo[a], rr[a], zo[a], rc[a], 1, 0});
+          grouped_gemm(g, t.data(), cur, Z, st);
+        }
         // Omega's storage holds Qz (same layout as Z)
         double* qz = orthonormalise(src, srl, szo, Z, Om, st, kInterPasses);
-        g.clear();
-        for (int a : sub) g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], zo[a], rc[a], yo[a], rr[a], 0, 0});
-        (p < tc_iters ? grouped_gemm_tc : gemm_fp64)(g, t.data(), qz, Y, st);
+        if (p < tc_iters) {
+          tc_n->apply(t.data(), qz, Y, st);
+        } else {
+          g.clear();
+          for (int a : sub) g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], zo[a], rc[a], yo[a], rr[a], 0, 0});
+          grouped_gemm(g, t.data(), qz, Y, st);
+        }
         cur = orthonormalise(srr, srl, syo, Y, Q, st, p + 1 == iters ? 3 : kInterPasses);
       }
     };
@@ -440,14 +476,24 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
         }
       }
       // ---- Y = A Omega, Q = orth(Y), subspace iterations
-      std::vector<xgb_gemm_desc> g;
-      for (int a = 0; a < nr; ++a)
+      std::vector<xgb_gemm_desc> g, gt;
+      for (int a = 0; a < nr; ++a) {
+        // Omega (n x l, ld n) has Z's layout: om[a] == zo[a], so A Omega and A Q_z share descriptors
         g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], om[a], rc[a], yo[a], rr[a], 0, 0});
-      (tc_iters > 0 ? grouped_gemm_tc : gemm_fp64)(g, t.data(), Om, Y, st);
+        gt.push_back({rc[a], rl[a], rr[a], m.offset[R[a]], rr[a], yo[a], rr[a], zo[a], rc[a], 1, 0});
+      }
+      std::unique_ptr<TcProducts> tc_n, tc_t;
+      if (tc_iters > 0) {
+        tc_n = std::make_unique<TcProducts>(g, t.data(), st);
+        tc_t = std::make_unique<TcProducts>(gt, t.data(), st);
+        tc_n->apply(t.data(), Om, Y, st);
+      } else {
+        grouped_gemm(g, t.data(), Om, Y, st);
+      }
       double* q0 = orthonormalise(rr, rl, yo, Y, Q, st, power_iters > 0 ? kInterPasses : 3);
       std::vector<int> all(nr);
       for (int a = 0; a < nr; ++a) all[a] = a;
-      iterate(all, power_iters, q0, tc_iters);
+      iterate(all, power_iters, q0, tc_iters, tc_t.get(), tc_n.get());
     }
     // ---- exact sectors: their blocks join the batched SVD of the projected blocks
     if (!E.empty()) {
@@ -520,7 +566,7 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       max_res = worst;
       if (bad.empty() || pass >= kMaxRefine) break;
       ++refinements;
-      iterate(bad, std::max(power_iters, 1), Q, 0);
+      iterate(bad, std::max(power_iters, 1), Q, 0, nullptr, nullptr);
       project(bad, {});
       res = truncate_spectra(m, sp, max_keep, eps_svd, false);
     }
