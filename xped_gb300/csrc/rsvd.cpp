@@ -336,11 +336,11 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
 
     // subspace iterations Q <- orth(A orth(A^T Q)) for the sketched sectors `sub` (indices into R);
     // the basis enters in `cur` (Q or Y) and leaves in Q (last orthonormalisation with 3 passes);
-    // the products of the first `tc_iters` iterations run as 3xTF32 tensor-core GEMMs through
+    // the products of the first `lead` iterations run as 3xTF32 tensor-core GEMMs through
     // tc_t (A^T X) and tc_n (A X), which cover all sketched sectors (sub = all)
-    auto iterate = [&](const std::vector<int>& sub, int iters, double* cur, int tc_iters, TcProducts* tc_t,
+    auto iterate = [&](const std::vector<int>& sub, int iters, double* cur, int lead, TcProducts* tc_t,
                        TcProducts* tc_n) {
-      if (tc_iters > 0 && (!tc_t || !tc_n || int(sub.size()) != nr))
+      if (lead > 0 && (!tc_t || !tc_n || int(sub.size()) != nr))
         throw std::logic_error("randomized tSVD: tensor-core products need every sketched sector");
       std::vector<int64_t> srr, src, srl, syo, szo;
       for (int a : sub) {
@@ -352,7 +352,7 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       }
       std::vector<xgb_gemm_desc> g;
       for (int p = 0; p < iters; ++p) {
-        if (p < tc_iters) {
+        if (p < lead) {
           tc_t->apply(t.data(), cur, Z, st);
         } else {
           g.clear();
@@ -361,7 +361,7 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
         }
         // Omega's storage holds Qz (same layout as Z)
         double* qz = orthonormalise(src, srl, szo, Z, Om, st, kInterPasses);
-        if (p < tc_iters) {
+        if (p < lead) {
           tc_n->apply(t.data(), qz, Y, st);
         } else {
           g.clear();
