@@ -329,7 +329,7 @@ def run_gpu(args):
     res["small_plain_ms"] = float(np.mean(ms))
     L.xgb_free(flush)
     res["gemm_sweep"] = gemm_sweep()
-    res["config1"] = config1_ops()
+    res["tensor22_chain"] = tensor22_chain()
     res["fp64_peak"] = fp64_library_peak()
     res["su"] = su_step()
     return res
@@ -591,7 +591,7 @@ def u1_product(degs, reps=10, form="fp64"):
             "tflops": flops / (ms * 1e-3) / 1e12}
 
 
-def config1_ops(seeds=(0, 1, 2, 3, 4), reps=20):
+def tensor22_chain(seeds=(0, 1, 2, 3, 4), reps=20):
     """The plain FP64 op chain on a U(1) Tensor<2,2> (every leg q = -2..2, deg [2, 4, 6, 4, 2]; 9 coupled
     sectors, 17,712 doubles): T1*T2 -> permute<0>(0, 2, 1, 3) -> tSVD(16, 1e-10), N(0,1) entries per seed.
     Device time per chain (CUDA events, `reps` chains after warm-up, plans cached) beside the numpy/OpenBLAS
@@ -1028,7 +1028,7 @@ def main():
             line["learned_widths"]["energy_abs_diff_vs_plain"] = abs(r["e_learned"] - r["e_plain"])
     line["plain_fp64_D4_chi32_ms_per_step"] = r["small_plain_ms"]
     line["block_gemm_sweep"] = r["gemm_sweep"]
-    line["tensor22_chain"] = r["config1"]
+    line["tensor22_chain"] = r["tensor22_chain"]
     line["simple_update_step"] = r["su"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_from_device(r["ctm"])

@@ -47,8 +47,8 @@ def test_ctm_steps_u1_small(seed):
     _compare(oc, nc, 1e-8)
 
 
-def test_ctm_config2_step():
-    """BASELINE config 2: U(1), phys dim 2, D=4 (q -1..1 deg [1,2,1]), chi=32."""
+def test_ctm_u1_d4_chi32_step():
+    """U(1) iPEPS CTMRG steps: phys dim 2, D=4 (q -1..1 deg [1,2,1]), chi=32."""
     oc, nc = _setup("u1", [(-1, 1), (0, 2), (1, 1)], [(-1, 1), (1, 1)], 32, 7)
     for _ in range(2):
         oc.grow_all()

@@ -77,8 +77,8 @@ def test_matmul_and_adjoint_operands():
     assert_same(nT2.matmul(nT2, adj_a=True), oT2.adjoint() * oT2, 1e-12, 1e-12)
 
 
-def test_config1_contract_permute_tsvd():
-    """BASELINE config 1: U(1) Tensor<2,2>, legs q=-2..2 deg [2,4,6,4,2];
+def test_tensor22_contract_permute_tsvd():
+    """U(1) Tensor<2,2> op chain, legs q=-2..2 deg [2,4,6,4,2];
     T1*T2 -> permute<0>(0,2,1,3) -> tSVD(chi=16, eps=1e-10)."""
     pairs = [(-2, 2), (-1, 4), (0, 6), (1, 4), (2, 2)]
     for seed in range(3):

@@ -153,7 +153,7 @@ def test_contract_permutations_match_oracle():
 
 
 def test_ctm_shapes_metadata_only():
-    """Sector structure of the configs[1] CTM after init (no GPU): corner
+    """Sector structure of the U(1) D=4 chi=32 CTM after init (no GPU): corner
     and edge tensors built by the oracle have the ranks the reference gives."""
     from oracle.basis import Qbasis
     from oracle.ctm import CTM, IPEPS
