@@ -137,6 +137,24 @@ def test_tsvd_truncation_edge_cases():
         assert_same(nV, oV, 1e-9, 1e-9)
 
 
+def test_tsvd_preserve_multiplets_matches_oracle():
+    """PRESERVE_MULTIPLETS (Tensor.cpp:568-582) on designed spectra: the kept
+    list of 6 is cut back to 4 at the last relative gap above 0.1; truncWeight
+    and entropy as the oracle gives them."""
+    spectra = [(-1, [1.0, 0.5]), (0, [0.9, 0.2, 0.19]), (1, [0.6, 0.195])]
+    s, oB, nB = pair_basis("u1", [(q, len(v)) for q, v in spectra], sort=True)
+    ot = oracle.Tensor(s, [oB], [oB])
+    for q, v in spectra:
+        ot.block(q)[:] = np.diag(v)
+    nt = to_native(ot, [nB], [nB])
+    for keep, preserve in [(6, True), (6, False), (3, True), (100, True)]:
+        oU, oS, oV, otw, oent = ot.tsvd(keep, 0.0, preserve_multiplets=preserve)
+        nU, nS, nV, ntw, nent, _ = nt.tSVD(keep, 0.0, preserve)
+        assert nS.sectors() == (oS.sectors, [b.shape[0] for b in oS.blocks], [b.shape[1] for b in oS.blocks])
+        assert_same(nS, oS, 1e-14, 1e-15)
+        assert abs(ntw - otw) <= 1e-14 and abs(nent - oent) <= 1e-14
+
+
 def test_tqr():
     rng = np.random.default_rng(2)
     s, oB, nB = pair_basis("u1", [(-1, 3), (0, 5), (1, 2)], sort=True)

@@ -234,3 +234,40 @@ def test_svd_backward_matches_finite_differences():
                 E[i, j] = 1e-6
                 fd[i, j] = (f(A + E) - f(A - E)) / 2e-6
         assert np.abs(fd - dA).max() <= 1e-7 * np.abs(fd).max()
+
+
+def _diag_tensor(spectra):
+    """Rank-(1,1) U(1) tensor whose sector q block is diag(spectra[q])."""
+    s = oracle.U1()
+    B = Qbasis.from_pairs(s, [(q, len(v)) for q, v in spectra])
+    t = oracle.Tensor(s, [B], [B])
+    for q, v in spectra:
+        t.block(q)[:] = np.diag(v)
+    return t
+
+
+def test_cutoff_keeps_the_first_unsorted_value_when_eps_removes_all():
+    """cutoff_matrices (Tensor.cpp:541-590): when eps removes every value the
+    first entry of the unsorted list (the largest value of the first sector)
+    is kept, not the global maximum; truncWeight sums the values beyond maxKeep."""
+    t = _diag_tensor([(-1, [0.3, 0.1]), (0, [0.9, 0.2, 0.05]), (1, [0.4, 0.01])])
+    U, S, V, tw, ent = t.tsvd(3, 10.0)
+    assert S.sectors == [-1] and len(S.blocks) == 1
+    assert S.blocks[0].shape == (1, 1) and abs(S.blocks[0][0, 0] - 0.3) < 1e-15
+    assert abs(tw - (0.2 ** 2 + 0.1 ** 2 + 0.05 ** 2 + 0.01 ** 2)) < 1e-15
+    assert abs(ent - (-0.09 * np.log(0.09))) < 1e-15
+
+
+def test_cutoff_preserve_multiplets_cuts_at_the_last_relative_gap():
+    """PRESERVE_MULTIPLETS (Tensor.cpp:568-582): scanning the kept values from
+    the end, the cut moves to the last position whose relative gap
+    2 (s_{i-1} - s_i) / (s_{i-1} + s_i) exceeds 0.1."""
+    t = _diag_tensor([(-1, [1.0, 0.5]), (0, [0.9, 0.2, 0.19]), (1, [0.6, 0.195])])
+    _, S, _, tw, ent = t.tsvd(6, 0.0, preserve_multiplets=True)
+    kept = {q: sorted(np.diag(b).tolist(), reverse=True) for q, b in zip(S.sectors, S.blocks)}
+    assert kept == {-1: [1.0, 0.5], 0: [0.9], 1: [0.6]}
+    assert abs(tw - 0.19 ** 2) < 1e-15  # the weight counts only the values beyond maxKeep
+    vals = [1.0, 0.9, 0.6, 0.5]
+    assert abs(ent - sum(-v * v * np.log(v * v) for v in vals)) < 1e-14
+    _, S2, _, _, _ = t.tsvd(6, 0.0, preserve_multiplets=False)
+    assert sum(b.shape[0] for b in S2.blocks) == 6
