@@ -50,11 +50,11 @@ constexpr int kThreads = 128;
 // chunk size in float units (the pack buffers are float arrays), stage bytes
 template <int F> struct Form;
 template <> struct Form<0> {
-  static constexpr int pieces = 2, elem = 4, chunk_bytes = BM * BK * 4, chunk_units = chunk_bytes / 4;
+  static constexpr int pieces = 2, elem = 4, chunk_bytes = BM * BK * elem, chunk_units = chunk_bytes / 4;
   static constexpr int stage_bytes = 2 * pieces * chunk_bytes, kstep = 8;
 };
 template <> struct Form<1> {
-  static constexpr int pieces = 3, elem = 2, chunk_bytes = BM * BK * 2, chunk_units = chunk_bytes / 4;
+  static constexpr int pieces = 3, elem = 2, chunk_bytes = BM * BK * elem, chunk_units = chunk_bytes / 4;
   static constexpr int stage_bytes = 2 * pieces * chunk_bytes, kstep = 16;
 };
 static_assert(kStages * Form<1>::stage_bytes + 1024 <= kSmemBytes, "BF16x9 stages fit the TF32 budget");
