@@ -253,42 +253,43 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
     }
     __syncthreads();
   }
-  if (!kInverse) {
+  if constexpr (!kInverse) {
     if (kShared)  // L back to G, column-major, lower triangle and diagonal
       for (int e = tid; e < l * l; e += nt) {
         const int i = e % l, k = e / l;
         if (i >= k) Gg[e] = LA(i, k);
       }
     return;
-  }
-  // X = L^-1 by forward elimination of the identity: row j of X is final after
-  // dividing by L[j][j]; then rows i > j subtract L[i][j] * row j (columns c <= j)
-  for (int j = 0; j < l; ++j) {
-    if (tid == 0) inv_s[0] = 1.0 / LA(j, j);
-    __syncthreads();
-    const double inv = inv_s[0];
-    for (int c = tid; c <= j; c += nt) XA(j, c) *= inv;
-    __syncthreads();
-    const int t = l - j - 1;
-    for (int e = tid; e < t * (j + 1); e += nt) {
-      const int i = j + 1 + e % t, c = e / t;
-      XA(i, c) = fma(-LA(i, j), XA(j, c), XA(i, c));
-    }
-    __syncthreads();
-  }
-  // Rinv = X^T, column-major l x l: Rinv[c + i l] = X[i][c]
-  if (kShared) {
-    for (int e = tid; e < l * l; e += nt) {
-      const int c = e % l, i = e / l;
-      Xg[e] = XA(i, c);
-    }
   } else {
-    for (int e = tid; e < l * l; e += nt) {
-      const int i = e % l, c = e / l;
-      if (i > c) {
-        const double a = Xg[i + int64_t(c) * l], b = Xg[c + int64_t(i) * l];
-        Xg[i + int64_t(c) * l] = b;
-        Xg[c + int64_t(i) * l] = a;
+    // X = L^-1 by forward elimination of the identity: row j of X is final after
+    // dividing by L[j][j]; then rows i > j subtract L[i][j] * row j (columns c <= j)
+    for (int j = 0; j < l; ++j) {
+      if (tid == 0) inv_s[0] = 1.0 / LA(j, j);
+      __syncthreads();
+      const double inv = inv_s[0];
+      for (int c = tid; c <= j; c += nt) XA(j, c) *= inv;
+      __syncthreads();
+      const int t = l - j - 1;
+      for (int e = tid; e < t * (j + 1); e += nt) {
+        const int i = j + 1 + e % t, c = e / t;
+        XA(i, c) = fma(-LA(i, j), XA(j, c), XA(i, c));
+      }
+      __syncthreads();
+    }
+    // Rinv = X^T, column-major l x l: Rinv[c + i l] = X[i][c]
+    if (kShared) {
+      for (int e = tid; e < l * l; e += nt) {
+        const int c = e % l, i = e / l;
+        Xg[e] = XA(i, c);
+      }
+    } else {
+      for (int e = tid; e < l * l; e += nt) {
+        const int i = e % l, c = e / l;
+        if (i > c) {
+          const double a = Xg[i + int64_t(c) * l], b = Xg[c + int64_t(i) * l];
+          Xg[i + int64_t(c) * l] = b;
+          Xg[c + int64_t(i) * l] = a;
+        }
       }
     }
   }
