@@ -1,6 +1,6 @@
 """Writes tests/golden/oracle_golden.npz: oracle outputs on the seeded cases of
-tests/golden_cases.py (Tensor<2,2> op chains, permutes of U(1), fermionic U(1),
-fermionic Z2 and SU(2) tensors).
+tests/golden_cases.py (U(1) Tensor<2,2> op chains, fermionic Z2 and SU(2) op
+chains, permutes of U(1), fermionic U(1), fermionic Z2 and SU(2) tensors).
 
 Run from the repository root:  python tests/golden/make_golden.py
 """
@@ -22,6 +22,9 @@ def main():
     for seed in gc.CHAIN_SEEDS:
         for k, v in gc.oracle_chain(seed).items():
             out[f"chain_{seed}_{k}"] = v
+    for symname, pB, pD in gc.SYM_CHAINS:
+        for k, v in gc.oracle_sym_chain(symname, pB, pD).items():
+            out[f"symchain_{symname}_{k}"] = v
     out.update(gc.oracle_permutes())
     path = os.path.join(HERE, "oracle_golden.npz")
     np.savez_compressed(path, **out)

@@ -87,6 +87,31 @@ def oracle_chain(seed):
     return chain_record(prod.data(), perm.data(), S.sectors, [b.shape[0] for b in S.blocks], S.data(), tw, ent)
 
 
+# fermionic Z2 and SU(2) op chains: L [B, B | D] * R [D | B, B] -> permute<0>(0,2,1,3) -> tSVD(12, 1e-10)
+SYM_CHAINS = [
+    ("fz2", [(0, 2), (1, 3)], [(0, 3), (1, 2)]),
+    ("su2", [(1, 2), (2, 1), (3, 1)], [(1, 2), (2, 2), (3, 1)]),
+]
+SYM_CHAIN_SEED = 3
+
+
+def sym_chain_inputs(symname, pB, pD):
+    rng = np.random.default_rng(SYM_CHAIN_SEED)
+    s = oracle.make_symmetry(symname)
+    B, D = Qbasis.from_pairs(s, pB), Qbasis.from_pairs(s, pD)
+    oL = oracle.Tensor(s, [B, B], [D]).set_random(rng)
+    oR = oracle.Tensor(s, [D], [B, B]).set_random(rng)
+    return oL, oR
+
+
+def oracle_sym_chain(symname, pB, pD):
+    oL, oR = sym_chain_inputs(symname, pB, pD)
+    prod = oL * oR
+    perm = prod.permute(0, [0, 2, 1, 3])
+    _, S, _, tw, ent = perm.tsvd(12, 1e-10)
+    return chain_record(prod.data(), perm.data(), S.sectors, [b.shape[0] for b in S.blocks], S.data(), tw, ent)
+
+
 def permute_key(symname, i):
     return f"permute_{symname}_{i}"
 
@@ -125,8 +150,8 @@ def compare_digest(gold, prefix, x, rtol, atol=0.0):
     return err
 
 
-def compare_chain(gold, seed, rec, rtol_data, rtol_sigma):
-    p = f"chain_{seed}"
+def compare_chain(gold, p, rec, rtol_data, rtol_sigma):
+    """Compare a chain record with the fixture arrays stored under prefix `p`."""
     assert np.array_equal(rec["s_sectors"], gold[f"{p}_s_sectors"])
     assert np.array_equal(rec["s_rows"], gold[f"{p}_s_rows"])
     for name in ("prod", "perm"):

@@ -19,7 +19,12 @@ def gold():
 
 @pytest.mark.parametrize("seed", gc.CHAIN_SEEDS)
 def test_oracle_chain_matches_golden(gold, seed):
-    gc.compare_chain(gold, seed, gc.oracle_chain(seed), 1e-13, 1e-13)
+    gc.compare_chain(gold, f"chain_{seed}", gc.oracle_chain(seed), 1e-13, 1e-13)
+
+
+@pytest.mark.parametrize("symname,pB,pD", gc.SYM_CHAINS)
+def test_oracle_sym_chain_matches_golden(gold, symname, pB, pD):
+    gc.compare_chain(gold, f"symchain_{symname}", gc.oracle_sym_chain(symname, pB, pD), 1e-13, 1e-13)
 
 
 def test_oracle_permutes_match_golden(gold):

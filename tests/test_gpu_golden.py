@@ -32,7 +32,22 @@ def test_chain_matches_golden(gold, seed):
     _, S, _, tw, ent, _ = perm.tSVD(16, 1e-10)
     qs, rs, _ = S.sectors()
     rec = gc.chain_record(prod.data(), perm.data(), list(qs), list(rs), S.data(), tw, ent)
-    gc.compare_chain(gold, seed, rec, 1e-12, 1e-10)
+    gc.compare_chain(gold, f"chain_{seed}", rec, 1e-12, 1e-10)
+
+
+@pytest.mark.parametrize("symname,pB,pD", gc.SYM_CHAINS)
+def test_sym_chain_matches_golden(gold, symname, pB, pD):
+    oL, oR = gc.sym_chain_inputs(symname, pB, pD)
+    _, _, nB = pair_basis(symname, pB)
+    _, _, nD = pair_basis(symname, pD)
+    nL = to_native(oL, [nB, nB], [nD])
+    nR = to_native(oR, [nD], [nB, nB])
+    prod = nL * nR
+    perm = prod.permute(0, [0, 2, 1, 3])
+    _, S, _, tw, ent, _ = perm.tSVD(12, 1e-10)
+    qs, rs, _ = S.sectors()
+    rec = gc.chain_record(prod.data(), perm.data(), list(qs), list(rs), S.data(), tw, ent)
+    gc.compare_chain(gold, f"symchain_{symname}", rec, 1e-12, 1e-10)
 
 
 @pytest.mark.parametrize("symname,pB,pC", gc.PERMUTE_CASES)
