@@ -844,9 +844,9 @@ def roofline(prof, steps, fp64_peak=None):
                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s"}
     out["frac"] = out["achieved"] / out["peak"]
     # DRAM bytes per launch of the dominant kernel from one ncu capture (profiles/): the chosen
-    # step's orthonormalisation launches are L2-resident
-    traffic = {"svd_jacobi": (1.884e6, "ncu capture of one orthonormalisation launch, U(1) D=6 chi=128 "
-                                       "(dram__bytes_read.sum 1.864 MB + write 0.021 MB)"),
+    # step's working sets are L2-resident
+    traffic = {"svd_jacobi": (0.355e6, "ncu capture of one svd_cluster_kernel launch of the projected l x l "
+                                       "factors, U(1) D=6 chi=128 (dram__bytes_read.sum 322 KB + write 33 KB)"),
                "gemm_tc": (7.025e9, "ncu capture, SU(2) Tensor<2,2> product (6.613 GB read + 0.412 GB written)"),
                "gemm_f64": (14.10e6, "ncu one-pass capture of 348 consecutive gemm_simt_kernel launches of the "
                                      "chosen U(1) D=6 chi=128 run (dram read + write per launch, average; the "
