@@ -9,6 +9,8 @@ References:
 """
 from __future__ import annotations
 
+import numpy as np
+
 from functools import lru_cache
 from math import prod
 
@@ -59,6 +61,29 @@ class FusionTree:
         if self.rank + 1 >= 3:
             qi.append(self.qc)
         return FusionTree(self.qu + other.qu[:1], qi, self.qc, self.dims + other.dims[:1], self.dual + other.dual[:1])
+
+    def as_tensor(self, sym):
+        """FusionTree::asTensor (src/Core/FusionTree.cpp:155-285): the tree's
+        Clebsch-Gordan tensor, indices (uncoupled legs..., coupled), built by
+        chaining the vertices left to right through the intermediate irreps;
+        every dual leg is then bent with the symmetry's 1j tensor."""
+        deg = sym.degeneracy
+        r = self.rank
+        if r == 0:
+            return np.ones(1)
+        if r == 1:
+            out = np.eye(deg(self.qu[0]), deg(self.qc))
+        else:
+            chain = [self.qu[0]] + list(self.qi) + [self.qc]
+            out = sym.cgc(self.qu[0], self.qu[1], chain[1])
+            for v in range(1, r - 1):
+                vert = sym.cgc(chain[v], self.qu[v + 1], chain[v + 1])
+                out = np.tensordot(out, vert, axes=([out.ndim - 1], [0]))
+        for k in range(r):
+            if self.dual[k]:
+                oj = sym.one_j(self.qu[k])
+                out = np.moveaxis(np.tensordot(oj, out, axes=([1], [k])), 0, k)
+        return out
 
     def compute_intermediates(self, sym):
         """FusionTree::computeIntermediates (FusionTree.cpp:136-152), abelian only."""

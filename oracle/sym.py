@@ -8,12 +8,15 @@ References:
   SU(2): include/Xped/Symmetry/SU2.hpp:108-180, src/Symmetry/SU2.cpp:17-119
   defaults (coeff_FS, coeff_turn): include/Xped/Symmetry/SymBase.hpp:69-77
   phase(): include/Xped/Symmetry/functions.hpp:79-84
+  CGC:   src/Symmetry/SU2.cpp:71-89 (3j symbol from GSL, SU2Wrappers.hpp:78-81)
 """
 from __future__ import annotations
 
 import math
 from fractions import Fraction
 from functools import lru_cache
+
+import numpy as np
 
 
 def phase(q: int) -> float:
@@ -51,6 +54,15 @@ class _Sym:
 
     def coeff_FS(self, q):
         return 1.0
+
+    def cgc(self, q1, q2, q3):
+        """Symmetry::CGC for abelian symmetries: the single coefficient 1 of a
+        one-dimensional vertex (U1.hpp / ZN.hpp CGC)."""
+        return np.ones((1, 1, 1)) if self.triangle(q1, q2, q3) else np.zeros((1, 1, 1))
+
+    def one_j(self, q):
+        """Symmetry::one_j_tensor for abelian symmetries (U1.hpp:139-143, ZN.hpp:150-154): [[1]]."""
+        return np.ones((1, 1))
 
     def __eq__(self, other):
         return type(self) is type(other) and self.__dict__ == other.__dict__
@@ -187,6 +199,42 @@ def wigner6j_twice(a2, b2, c2, d2, e2, f2) -> float:
     return val
 
 
+@lru_cache(maxsize=None)
+def wigner3j_twice(a2, b2, c2, ma2, mb2, mc2) -> float:
+    """Wigner 3j (a b c; ma mb mc) from doubled spins and projections by Racah's
+    closed form, in exact rational arithmetic (a published formula; replaces
+    GSL's gsl_sf_coupling_3j called at include/Xped/Symmetry/SU2Wrappers.hpp:78-81).
+    Zero unless ma + mb + mc = 0, |m| <= j with j - m integral and the triangle rule holds."""
+    if ma2 + mb2 + mc2 != 0:
+        return 0.0
+    for j2, m2 in ((a2, ma2), (b2, mb2), (c2, mc2)):
+        if j2 < 0 or abs(m2) > j2 or (j2 - m2) % 2:
+            return 0.0
+    if (a2 + b2 + c2) % 2 or not abs(a2 - b2) <= c2 <= a2 + b2:
+        return 0.0
+    f = _fact
+    # integer arguments (all sums below are even before halving)
+    jab_c, jac_b, jbc_a, jabc = (a2 + b2 - c2) // 2, (a2 - b2 + c2) // 2, (-a2 + b2 + c2) // 2, (a2 + b2 + c2) // 2
+    num_sq = Fraction(f(jab_c) * f(jac_b) * f(jbc_a), f(jabc + 1))
+    num_sq *= (f((a2 + ma2) // 2) * f((a2 - ma2) // 2) * f((b2 + mb2) // 2) * f((b2 - mb2) // 2)
+               * f((c2 + mc2) // 2) * f((c2 - mc2) // 2))
+    # summation bounds: every factorial argument non-negative
+    t1 = (c2 - b2 + ma2) // 2      # j3 - j2 + m1
+    t2 = (c2 - a2 - mb2) // 2      # j3 - j1 - m2
+    t3 = jab_c                     # j1 + j2 - j3
+    t4 = (a2 - ma2) // 2           # j1 - m1
+    t5 = (b2 + mb2) // 2           # j2 + m2
+    kmin = max(0, -t1, -t2)
+    kmax = min(t3, t4, t5)
+    total = Fraction(0)
+    for k in range(kmin, kmax + 1):
+        total += Fraction((-1) ** k, f(k) * f(t1 + k) * f(t2 + k) * f(t3 - k) * f(t4 - k) * f(t5 - k))
+    if total == 0:
+        return 0.0
+    sign = -1.0 if ((a2 - b2 - mc2) // 2) % 2 else 1.0   # (-1)^(j1 - j2 - m3)
+    return sign * math.sqrt(num_sq.numerator) / math.sqrt(num_sq.denominator) * float(total)
+
+
 class SU2(_Sym):
     """SU(2) with q = 2j+1 (SU2.hpp:108-180, SU2.cpp:17-119).  Non-fermionic
     (SpinSU2 kind)."""
@@ -228,6 +276,30 @@ class SU2(_Sym):
 
     def coeff_6j(self, q1, q2, q3, q4, q5, q6):
         return wigner6j_twice(q1 - 1, q2 - 1, q3 - 1, q4 - 1, q5 - 1, q6 - 1)
+
+    def one_j(self, q):
+        """SU2::one_j_tensor (src/Symmetry/SU2.cpp:42-61): entry (i, j) = (-1)^i where the
+        projections of i and j are opposite, 0 elsewhere."""
+        out = np.zeros((q, q))
+        for i in range(q):
+            out[i, q - 1 - i] = phase(i)
+        return out
+
+    def cgc(self, q1, q2, q3):
+        """SU2::CGC (src/Symmetry/SU2.cpp:71-89): the Clebsch-Gordan tensor of one
+        vertex, index i of an irrep q standing for the projection 2m = (q - 1) - 2i
+        (largest m first); value 3j(q1 q2 q3; m1 m2 -m3) (-1)^((q1 - q2 + 2 m3) / 2) sqrt(q3)."""
+        out = np.zeros((q1, q2, q3))
+        for i1 in range(q1):
+            m1 = (q1 - 1) - 2 * i1
+            for i2 in range(q2):
+                m2 = (q2 - 1) - 2 * i2
+                for i3 in range(q3):
+                    m3 = (q3 - 1) - 2 * i3
+                    w = wigner3j_twice(q1 - 1, q2 - 1, q3 - 1, m1, m2, -m3)
+                    if w != 0.0:
+                        out[i1, i2, i3] = w * phase(_cdiv(q1 - q2 + m3, 2)) * math.sqrt(q3)
+        return out
 
     def coeff_recouple(self, q1, q2, q3, Q, Q12, Q23):
         # sqrt(Q12*Q23) * phase((q1+q2+q3+Q)/2.) * 6j(q1,q2,Q12,q3,Q,Q23)   (SU2.hpp:164-167)

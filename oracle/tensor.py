@@ -403,29 +403,56 @@ class Tensor:
             Rt.push_back(q, Rm)
         return Q, Rt
 
-    # -- dense expansion (abelian, bosonic only) --------------------------------------------
-    def plain_tensor(self):
-        """Tensor::plainTensor (Tensor.cpp:1133+) for abelian bosonic
-        symmetries, where every Clebsch-Gordan coefficient is 1: each
-        (domain tree, codomain tree) sub-block is placed at the outer offsets
-        of its uncoupled charges in the sorted leg bases."""
+    # -- dense expansion ------------------------------------------------------------------
+    def _unitary(self, coupled, legs):
+        """Tensor::unitaryDomain / unitaryCodomain (src/Core/Tensor.cpp:1000-1132): the
+        dense map from the coupled basis (sorted, fused index = inner * deg(q) + m) to the
+        uncoupled legs (sorted bases, index per leg = inner * deg(q_i) + m_i), one identity
+        on the multiplicities times the tree's Clebsch-Gordan tensor per fusion tree."""
         sym = self.sym
-        assert sym.ABELIAN and not sym.FERMIONIC
+        deg = sym.degeneracy
+        out = np.zeros(tuple(b.fullDim() for b in legs) + (coupled.fullDim(),))
+        for q in coupled.qs:
+            col0 = coupled.full_outer_num(q)
+            for tree in coupled.trees[q]:
+                dims = [legs[i].inner_dim(tree.qu[i]) for i in range(len(legs))]
+                ud = int(np.prod(dims)) if dims else 1
+                tid = np.eye(ud).reshape(tuple(dims) + (ud,), order="F")
+                cg = tree.as_tensor(sym)
+                # tensorProd (src/Interfaces/TensorInterface_Eigen_impl.cpp:156-183): per index
+                # the CGC index runs fastest, the multiplicity index slowest
+                full = np.einsum(tid, list(range(0, 2 * tid.ndim, 2)), cg, list(range(1, 2 * tid.ndim, 2)))
+                full = full.reshape(tuple(a * b for a, b in zip(tid.shape, cg.shape)))
+                offs = [legs[i].full_outer_num(tree.qu[i]) for i in range(len(legs))]
+                offs.append(col0 + coupled.left_offset(tree) * deg(q))
+                out[tuple(slice(o, o + n) for o, n in zip(offs, full.shape))] = full
+        return out
+
+    def plain_tensor(self):
+        """Tensor::plainTensor (src/Core/Tensor.cpp:1133-1310): the dense tensor over the
+        sorted uncoupled legs (domain legs, then codomain legs).  Every block is expanded
+        as block (x) identity(deg(q)) into the coupled domain x coupled codomain matrix,
+        which is then contracted with the domain and codomain unitaries (fusion-tree
+        Clebsch-Gordan tensors; for abelian symmetries every coefficient is 1)."""
+        sym = self.sym
+        deg = sym.degeneracy
         sdom = [b.copy() for b in self.dom]
         scod = [b.copy() for b in self.cod]
         for b in sdom + scod:
             b.sort()
-        shape = tuple(b.fullDim() for b in sdom + scod)
-        out = np.zeros(shape)
-        for q in self.sectors:
-            for f1 in self.cdom.trees[q]:
-                for f2 in self.ccod.trees[q]:
-                    sub = self.sub_block(f1, f2)
-                    offs = [sdom[i].full_outer_num(f1.qu[i]) for i in range(self.rank)]
-                    offs += [scod[i].full_outer_num(f2.qu[i]) for i in range(self.corank)]
-                    sl = tuple(slice(o, o + d) for o, d in zip(offs, f1.dims + f2.dims))
-                    out[sl] += sub
-        return out
+        cdom = self.cdom.copy()
+        ccod = self.ccod.copy()
+        cdom.sort()
+        ccod.sort()
+        inner = np.zeros((cdom.fullDim(), ccod.fullDim()))
+        for q, b in zip(self.sectors, self.blocks):
+            d = deg(q)
+            r0, c0 = cdom.full_outer_num(q), ccod.full_outer_num(q)
+            inner[r0:r0 + d * b.shape[0], c0:c0 + d * b.shape[1]] += np.kron(b, np.eye(d))
+        ud = self._unitary(cdom, sdom)
+        uc = self._unitary(ccod, scod)
+        mid = np.tensordot(ud, inner, axes=([ud.ndim - 1], [0]))
+        return np.tensordot(mid, uc, axes=([mid.ndim - 1], [uc.ndim - 1]))
 
 
 def fix_svd_signs(u, vt):
