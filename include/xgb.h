@@ -100,6 +100,32 @@ typedef struct xgb_gemm_desc {
    (tcgen05.mma kind::f16; about 1e-6 relative, like 3xTF32). */
 int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, const double* A, const double* B,
                      double* C, double alpha, double beta, void* stream);
+/* Tile-shape autotuner of the FP64 grouped GEMM (no counterpart in the reference, whose
+   per-sector loop hands every block to BLAS separately, src/Core/TensorBase.cpp:262-279).
+   Candidates: output tile edge 16 / 32 / 64 x split-K target of 0 / 1 / 2 / 4 waves of CTAs
+   (xgb_autotune_candidates lists them).  mode 1: the first GEMM list of a size bucket (group
+   count, total flops, largest block area, longest k on a log2 scale) times every candidate on its
+   own operands (CUDA events on the launching stream, output into scratch memory) and the fastest
+   is cached for the bucket; mode 0 (default): the built-in rule of each call site.
+   xgb_autotune_save / _load write / read the cache as text lines keyed by the GPU's name (entries
+   of other GPU models are skipped; load returns the number of entries taken).  xgb_autotune_stats
+   returns the number of cached buckets (and, if non-NULL, buckets measured, cache hits and the
+   milliseconds spent measuring); xgb_autotune_choices the cached (tile, split) pairs.
+   xgb_autotune_gemm measures every candidate on one list now (times_ms: one entry per candidate,
+   best: the index of the fastest), leaving the cache alone; xgb_grouped_gemm_f64_config runs one
+   FP64 grouped GEMM with a given shape. */
+int xgb_autotune_set(int mode);
+int xgb_autotune_reset(void);
+int xgb_autotune_stats(int64_t* buckets_measured, int64_t* hits, double* tune_ms);
+int xgb_autotune_candidates(int32_t* tile, int32_t* split_waves, int cap);
+int xgb_autotune_choices(int32_t* tile, int32_t* split_waves, int cap);
+int xgb_autotune_gemm(int n_groups, const xgb_gemm_desc* descs, const double* A, const double* B, double* times_ms,
+                      int32_t* best);
+int xgb_grouped_gemm_f64_config(int tile, int split_waves, int n_groups, const xgb_gemm_desc* descs, const double* A,
+                                const double* B, double* C, double alpha, double beta, void* stream);
+int xgb_autotune_save(const char* path);
+int xgb_autotune_load(const char* path);
+
 /* Synchronises and reports whether a tensor-core GEMM CTA gave up on a bounded
    wait since the last call (XGB_E_TIMEOUT) - no counterpart in the reference. */
 int xgb_gemm_tc_status(void);
@@ -147,14 +173,19 @@ int xgb_batched_svd(int n, const xgb_svd_desc* descs, const double* A, double* U
 /* xgb_batched_svd for callers that cannot allocate device memory (a plugin
    whose host framework owns all device allocations, or a service with a
    fixed device-memory budget).  No counterpart in the reference: it exists
-   only for embedders of this library.  Same descriptors and outputs as
-   xgb_batched_svd, but the workspace comes from one fixed 16 MiB device
-   array per GPU (xgb_batched_svd_noalloc_capacity_bytes()) that the library
-   holds until exit; batches needing more return XGB_E_UNSUPPORTED.  The
-   array's address is looked up on the first call on each device, so make
-   that first call before any stream capture.  All calls share the array:
-   calls that overlap on the GPU race and must be serialised by the caller.
-   Calls no cudaMalloc/cudaFree and returns after the stream has finished. */
+   only for embedders of this library.  Same descriptors, outputs and kernels
+   as xgb_batched_svd (blocks at least 512 wide on the grid-wide Jacobi
+   kernel, the others on the cluster kernel), but the workspace comes from
+   one fixed 16 MiB device array per GPU
+   (xgb_batched_svd_noalloc_capacity_bytes()) that the library holds until
+   exit; batches needing more return XGB_E_UNSUPPORTED (one square block of
+   up to about 580 columns fits).  The array's address is looked up on the
+   first call on each device, so make that first call before any stream
+   capture.  All calls share the array: calls that overlap on the GPU
+   (different streams or host threads) race and must be serialised by the
+   caller.  Calls no cudaMalloc/cudaFree, records no sweep statistics
+   (xgb_svd_last_sweeps reports none afterwards) and returns after the
+   stream has finished.  Needs xgb_init (XGB_E_NOINIT otherwise). */
 int xgb_batched_svd_noalloc(int n, const xgb_svd_desc* descs, const double* A, double* U, double* S, double* Vt,
                             void* stream);
 size_t xgb_batched_svd_noalloc_capacity_bytes(void);

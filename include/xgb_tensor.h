@@ -195,6 +195,13 @@ int xgb_ctm_record_get(xgb_ctm c, int i, int* dir, int* n_sectors, int64_t* n_sp
 /* computeRDM_h (vertical = 0) / computeRDM_v (vertical = 1), normalised
    (src/PEPS/CTM.cpp:583-627, 756-790) */
 xgb_tensor xgb_ctm_rdm(xgb_ctm c, int vertical);
+/* CTMSolver::solve without AD (src/PEPS/CTMSolver.cpp:50-80) on the 1x1 cell: grow_all steps until
+   the bond energy per site E = <H>_h + <H>_v changes by less than tol_E, or comes back to within
+   tol_E of the value two steps earlier (oscillation), at most max_steps steps.  Writes the last E,
+   the steps run, flags (1 converged, 2 stopped on oscillation) and, if energies is non-NULL, the
+   energy after each step (up to cap values). */
+int xgb_ctm_solve(xgb_ctm c, xgb_tensor H, double tol_E, int max_steps, double* E, int* steps, int* flags,
+                  double* energies, int cap);
 /* Learned sketch widths (no counterpart in the reference).  A small MLP
    (xgb_rank_model_num_features() inputs per sector -> 3 x 64 ReLU -> 2 outputs,
    FP32) predicts log2(1 + kept count) and log2(1 + oversampling) of each sector of

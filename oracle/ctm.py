@@ -207,6 +207,25 @@ class CTM:
             self.move(d)
         return self
 
+    def solve(self, H, tol_E=1e-10, max_steps=100):
+        """CTMSolver::solve without AD (src/PEPS/CTMSolver.cpp:50-80), 1x1 cell: grow_all, then
+        E = <H>_h + <H>_v; stop when |E - E_prev| < tol_E or |E - E_prevprev| < tol_E."""
+        prev = prevprev = 1000.0
+        out = {"E": float("nan"), "steps": 0, "converged": False, "oscillation": False, "energies": []}
+        for step in range(max_steps):
+            self.grow_all()
+            E = bond_expectation(self.rdm_h(), H) + bond_expectation(self.rdm_v(), H)
+            out["energies"].append(E)
+            out["E"], out["steps"] = E, step + 1
+            if abs(E - prev) < tol_E:
+                out["converged"] = True
+                break
+            if abs(E - prevprev) < tol_E:
+                out["converged"] = out["oscillation"] = True
+                break
+            prevprev, prev = prev, E
+        return out
+
     # -- reduced density matrices and bond energies ---------------------------------
     def rdm_h(self):
         """computeRDM_h, TRank == 2 (CTM.cpp:583-619): rho_h Tensor<2,2>

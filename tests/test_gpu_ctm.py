@@ -1,9 +1,10 @@
 """CTMRG moves on the GPU against the oracle (1x1 cell, U(1) and fermionic Z2).
 
 The SVD gauge is fixed identically on both sides (largest |u_i| positive), so
-environments are compared entry by entry; tolerance 1e-8 relative after
-several full steps (FP64 round-off accumulates through ~100 contractions and
-four truncated SVDs per step)."""
+environments are compared entry by entry; tolerance 1e-10 relative to the
+largest entry after several full steps (the FP64 contract tolerance: FP64
+round-off accumulates through ~100 contractions and four truncated SVDs per
+step)."""
 import numpy as np
 import pytest
 
@@ -44,7 +45,7 @@ def test_ctm_steps_u1_small(seed):
     for _ in range(3):
         oc.grow_all()
         nc.grow_all()
-    _compare(oc, nc, 1e-8)
+    _compare(oc, nc, 1e-10)
 
 
 def test_ctm_u1_d4_chi32_step():
@@ -53,7 +54,7 @@ def test_ctm_u1_d4_chi32_step():
     for _ in range(2):
         oc.grow_all()
         nc.grow_all()
-    _compare(oc, nc, 1e-8)
+    _compare(oc, nc, 1e-10)
 
 
 def test_ctm_fermionic_z2():
@@ -62,7 +63,7 @@ def test_ctm_fermionic_z2():
     for _ in range(2):
         oc.grow_all()
         nc.grow_all()
-    _compare(oc, nc, 1e-8)
+    _compare(oc, nc, 1e-10)
 
 
 def test_rdm_and_energy_match_oracle():
@@ -80,7 +81,7 @@ def test_rdm_and_energy_match_oracle():
     nH = heisenberg_bond(nc.get("A").leg(4))
     assert_same(nH, oH, 0, 0)
     for orho, nrho in ((oc.rdm_h(), nc.rdm_h()), (oc.rdm_v(), nc.rdm_v())):
-        assert_same(nrho, orho, 1e-8, 1e-10)
+        assert_same(nrho, orho, 1e-10, 1e-10)
         assert abs(bond_expectation(nrho, nH) - obond(orho, oH)) < 1e-10
 
 
@@ -120,7 +121,7 @@ def test_oracle_copy_of_device_ctm_continues_identically():
     _compare(oc, nc, 0)
     oc.grow_all()
     nc.grow_all()
-    _compare(oc, nc, 1e-8)
+    _compare(oc, nc, 1e-10)
 
 
 def test_split_precision_contractions_stay_close():
@@ -180,3 +181,20 @@ def test_tensor_core_sketch_iterations_keep_the_energy():
     print("energy exact", e_ex, "fp64 sketch", e_rz, "tc sketch", e_tc, "diff", abs(e_rz - e_tc), abs(e_ex - e_tc))
     assert abs(e_rz - e_tc) < 1e-8
     assert abs(e_ex - e_tc) < 1e-8
+
+
+def test_solver_converges_like_the_oracle():
+    """CTMSolver::solve (src/PEPS/CTMSolver.cpp:50-80) on the device and in the oracle from the same
+    FROM_A start: the same number of grow_all steps, energies within 1e-10 after every step."""
+    from oracle.ctm import heisenberg_u1
+    from xped_gb300.observables import heisenberg_bond
+    oc, nc = _setup("u1", [(-1, 1), (0, 2), (1, 1)], [(-1, 1), (1, 1)], 16, 4)
+    s = oracle.make_symmetry("u1")
+    H = heisenberg_bond(nc.get("A").leg(4))
+    oH = heisenberg_u1(s, oc.peps.A.cod[2])
+    r = nc.solve(H, tol_E=1e-9, max_steps=40)
+    o = oc.solve(oH, tol_E=1e-9, max_steps=40)
+    print("device", r["steps"], r["E"], "oracle", o["steps"], o["E"])
+    assert r["converged"] and o["converged"]
+    assert r["steps"] == o["steps"]
+    assert np.abs(np.array(r["energies"]) - np.array(o["energies"])).max() < 1e-10

@@ -61,20 +61,59 @@ def test_bases_and_trees(symname, pB, pC):
     _cmp_basis(oB.combine(oC).forget_history(), nB.combine(nC).forget_history())
 
 
-def emulate_permute(tasks, contribs, src, n_out):
-    dst = np.zeros(n_out)
+def emulate_permute(tasks, contribs, src, n_out, sms=152):
+    """The index arithmetic of permute_rows_kernel: rows along output leg 0 (row_start prefix
+    sums, group size G from the element-weighted row length as perm_rows computes it), the
+    launch grid of launch_permute, group g taking rows g, g + ngroups, ... and lane l the row
+    elements l, l + G, ...; every source and destination index is checked against its buffer."""
+    n = len(tasks)
+    row_start = [0]
+    elems = weighted = 0.0
     for t in tasks:
-        dims = list(t.dims[:t.rank])
-        for e in range(t.nelem):
-            rem, idx = e, []
-            for d in dims:
-                idx.append(rem % d)
-                rem //= d
-            do = t.dst_base + sum(i * s for i, s in zip(idx, t.dst_stride[:t.rank]))
-            v = 0.0
-            for c in contribs[t.contrib0:t.contrib0 + t.n_contrib]:
-                v += c.coeff * src[c.src_base + sum(i * s for i, s in zip(idx, c.src_stride[:t.rank]))]
-            dst[do] = v
+        d0 = max(t.dims[0], 1) if t.rank > 0 else 1
+        row_start.append(row_start[-1] + t.nelem // d0)
+        elems += t.nelem
+        weighted += t.nelem * d0
+    total_rows = row_start[-1]
+    avg = weighted / elems if elems > 0 else 1.0
+    G = 1
+    while G < 32 and 2.0 * G <= avg * 1.25:
+        G *= 2
+    dst = np.zeros(n_out)
+    if total_rows == 0:
+        return dst
+    per_block = 256 // G
+    blocks = max(1, min(sms * 16, ((total_rows + 3) // 4 + per_block - 1) // per_block))
+    ngroups = blocks * 256 // G
+    seen = np.zeros(n_out, dtype=np.int64)
+    for r in range(total_rows):
+        g = r % ngroups  # the group that owns row r
+        assert 0 <= g < ngroups
+        ti = int(np.searchsorted(row_start, r, side="right") - 1)
+        assert 0 <= ti < n and row_start[ti] <= r < row_start[ti + 1]
+        t = tasks[ti]
+        d0 = t.dims[0] if t.rank > 0 else 1
+        rem = r - row_start[ti]
+        idx = [0]
+        for k in range(1, t.rank):
+            idx.append(rem % t.dims[k])
+            rem //= t.dims[k]
+        assert rem == 0
+        dofs = t.dst_base + sum(i * t.dst_stride[k] for k, i in enumerate(idx) if k > 0)
+        ds0 = t.dst_stride[0] if t.rank > 0 else 0
+        for lane in range(G):
+            for i in range(lane, d0, G):
+                v = 0.0
+                for c in contribs[t.contrib0:t.contrib0 + t.n_contrib]:
+                    so = c.src_base + i * (c.src_stride[0] if t.rank > 0 else 0)
+                    so += sum(x * c.src_stride[k] for k, x in enumerate(idx) if k > 0)
+                    assert 0 <= so < len(src)
+                    v += c.coeff * src[so]
+                do = dofs + i * ds0
+                assert 0 <= do < n_out
+                dst[do] = v
+                seen[do] += 1
+    assert seen.max() <= 1  # tasks tile disjoint regions of the output
     return dst
 
 

@@ -4,16 +4,27 @@ regular entry point (xgb_batched_svd with caller-provided workspace).
 The no-alloc variant serves embedders that cannot call cudaMalloc (their
 host framework owns every device allocation, or their device-memory budget
 is fixed up front); it takes its workspace from a fixed device array held
-by the library.  Both entry points run the same kernel, so their outputs
-must agree to round-off; the variant is called twice in a row because the
-shared array keeps the previous call's contents.  This file is named to be
-collected last."""
+by the library.  Both entry points run the same kernels (a 520 x 540 block
+takes the grid-wide Jacobi kernel, the others the cluster kernel), so their
+outputs must agree to round-off; the variant is called twice in a row
+because the shared array keeps the previous call's contents, once on the
+library stream and once on a stream the caller created.  This file is named
+to be collected last."""
 import ctypes as C
 
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+
+def _cudart():
+    """The CUDA runtime the native library itself loaded (for a caller-owned stream)."""
+    with open("/proc/self/maps") as f:
+        for line in f:
+            if "libcudart.so" in line:
+                return C.CDLL(line.split()[-1])
+    raise RuntimeError("libcudart is not loaded")
 
 
 def _alloc(L, nbytes):
@@ -29,7 +40,7 @@ def test_noalloc_svd_matches_allocating_entry_point():
     ensure_device(0)
     L = lib()
     rng = np.random.default_rng(17)
-    shapes = [(40, 40), (57, 23), (18, 61), (96, 96), (5, 5), (1, 7), (130, 130)]
+    shapes = [(40, 40), (57, 23), (18, 61), (96, 96), (5, 5), (1, 7), (130, 130), (520, 540)]
     descs, mats = [], []
     a_off = u_off = s_off = v_off = 0
     for m, n in shapes:
@@ -51,10 +62,16 @@ def test_noalloc_svd_matches_allocating_entry_point():
     dW = _alloc(L, wbytes)
     U, S, V = outs["ref"]
     assert L.xgb_batched_svd(len(descs), arr, dA, U, S, V, dW, None) == 0, last_error()
-    for tag in ("call1", "call2"):
+    assert L.xgb_synchronize() == 0
+    rt = _cudart()
+    own = C.c_void_p()
+    assert rt.cudaStreamCreate(C.byref(own)) == 0
+    for tag, st in (("call1", None), ("call2", own)):
         U, S, V = outs[tag]
-        rc = L.xgb_batched_svd_noalloc(len(descs), arr, dA, U, S, V, None)
+        rc = L.xgb_batched_svd_noalloc(len(descs), arr, dA, U, S, V, st)
         assert rc == 0, last_error()
+    assert rt.cudaStreamSynchronize(own) == 0
+    assert rt.cudaStreamDestroy(own) == 0
     assert L.xgb_synchronize() == 0
 
     def host(p, n):

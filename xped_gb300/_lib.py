@@ -131,6 +131,8 @@ PROTOS = [
     ("xgb_ctm_record_get", C.c_int, [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), i64p, i32p,
                                      C.POINTER(C.c_float), i64p, i64p, i64p, dblp, i64p]),
     ("xgb_ctm_rdm", P, [P, C.c_int]),
+    ("xgb_ctm_solve", C.c_int, [P, P, C.c_double, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_int]),
     ("xgb_rank_model_num_params", C.c_int, []),
     ("xgb_rank_model_num_features", C.c_int, []),
     ("xgb_rank_model_create", P, [C.c_uint64]),
@@ -226,6 +228,16 @@ PROTOS_EXTRA = [
     ("xgb_svd_last_sweeps", C.c_int, [i32p, C.c_int]),
     ("xgb_batched_svd_noalloc", C.c_int, [C.c_int, C.POINTER(SvdDesc), P, P, P, P, P]),
     ("xgb_batched_svd_noalloc_capacity_bytes", C.c_size_t, []),
+    ("xgb_autotune_set", C.c_int, [C.c_int]),
+    ("xgb_autotune_reset", C.c_int, []),
+    ("xgb_autotune_stats", C.c_int, [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    ("xgb_autotune_candidates", C.c_int, [i32p, i32p, C.c_int]),
+    ("xgb_autotune_choices", C.c_int, [i32p, i32p, C.c_int]),
+    ("xgb_autotune_gemm", C.c_int, [C.c_int, C.POINTER(GemmDesc), P, P, C.POINTER(C.c_double), i32p]),
+    ("xgb_grouped_gemm_f64_config", C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(GemmDesc), P, P, P, C.c_double,
+                                              C.c_double, P]),
+    ("xgb_autotune_save", C.c_int, [C.c_char_p]),
+    ("xgb_autotune_load", C.c_int, [C.c_char_p]),
 ]
 PROTOS.extend(PROTOS_EXTRA)
 

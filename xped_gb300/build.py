@@ -23,7 +23,7 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["kernels.cu", "svd.cu", "gemm_tc.cu", "rsvd.cu", "mlp.cu"]
-CPP_SOURCES = ["meta.cpp", "tensor.cpp", "capi.cpp", "rsvd.cpp", "mlp.cpp", "checkpoint.cpp"]
+CPP_SOURCES = ["meta.cpp", "tensor.cpp", "capi.cpp", "rsvd.cpp", "mlp.cpp", "checkpoint.cpp", "autotune.cpp"]
 
 
 def _run(cmd):

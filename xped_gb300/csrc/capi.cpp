@@ -550,6 +550,21 @@ int xgb_ctm_set_rank_model(xgb_ctm c, xgb_rank_model m, double margin, int64_t m
 
 xgb_tensor xgb_ctm_rdm(xgb_ctm c, int vertical) { GUARD(nullptr, { return wrap(c->c->rdm(vertical != 0)); }) }
 
+int xgb_ctm_solve(xgb_ctm c, xgb_tensor H, double tol_E, int max_steps, double* E, int* steps, int* flags,
+                  double* energies, int cap) {
+  GUARD(XGB_E_BADPLAN, {
+    if (!c || !H) return set_error(XGB_E_BADPLAN, "xgb_ctm_solve: null handle");
+    if (max_steps < 0) return set_error(XGB_E_BADPLAN, "xgb_ctm_solve: max_steps < 0");
+    const CTM::SolveResult r = c->c->solve(H->t, tol_E, max_steps);
+    if (E) *E = r.E;
+    if (steps) *steps = r.steps;
+    if (flags) *flags = (r.converged ? 1 : 0) | (r.oscillation ? 2 : 0);
+    if (energies)
+      for (int i = 0; i < cap && i < int(r.energies.size()); ++i) energies[i] = r.energies[i];
+    return XGB_OK;
+  })
+}
+
 int xgb_tensor_bond_expectation(xgb_tensor rho, xgb_tensor op, double* out) {
   GUARD(XGB_E_BADPLAN, {
     *out = bond_expectation(rho->t, op->t);

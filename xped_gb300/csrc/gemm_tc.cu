@@ -225,14 +225,34 @@ __global__ void __launch_bounds__(256) tc_pack_kernel(const xgb_gemm_desc* __res
 }
 
 // ----------------------------------------------------------------------------- gemm
+// One CTA (10 warps) per 128 x 128 output tile, warp-specialised:
+//  * warp 8 (lane 0) streams the A and B piece chunks of every 32-K slice into the 3-stage
+//    shared-memory ring with bulk copies;
+//  * warp 9 (lane 0) issues the slice's tcgen05.mma instructions into one of two 128-column TMEM
+//    accumulators (slice kc into buffer kc % 2), starting that buffer from zero, and commits the slice
+//    to the stage's "empty" barrier (frees the smem stage) and to the buffer's "full" barrier;
+//  * warps 0-7 drain every slice: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and columns
+//    64 (w / 4) .. + 63, adds the slice's partial products into FP32 register sums (round to nearest),
+//    then releases the buffer ("acc empty", one arrival per drain warp).
+// A TMEM partial therefore holds one slice's products only (12 accumulator additions for 3xTF32, 18
+// for BF16x9) instead of the whole K range.  The tensor core's own accumulation loses about 2^-26 of
+// the running sum per addition with a consistent sign, so an accumulator kept over k ~ 3000 drifts by
+// ~3e-5; restarted every slice and summed in round-to-nearest FP32 the error stays near 5e-7 of |C|
+// (with the 2^-22 operand split of 3xTF32) whatever k is.  The MMAs of slice kc + 1 run while the
+// drain warps read slice kc.
+constexpr int kDrainWarps = 8, kDrainCols = BN / (kDrainWarps / 4);  // 64 columns per drain warp
+constexpr int kTcWarps = kDrainWarps + 2, kTcThreads = kTcWarps * 32;
+constexpr int kProducerWarp = kDrainWarps, kMmaWarp = kDrainWarps + 1;
+constexpr uint32_t kTmemAlloc = 2 * kTmemCols;  // two accumulator buffers
+
 template <int F>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kTcThreads, 1)
     gemm_tc_kernel(const xgb_gemm_desc* __restrict__ descs, const TcGroup* __restrict__ groups,
                    const GemmTile* __restrict__ tiles, const float* __restrict__ apack,
                    const float* __restrict__ bpack, double* __restrict__ C, double alpha, double beta,
                    int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
-  __shared__ uint64_t full[kStages], empty[kStages], done;
+  __shared__ uint64_t full[kStages], empty[kStages], accf[2], acce[2], done;
   __shared__ uint32_t tmem_slot;
   __shared__ int fail, issued, consumed;
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -241,18 +261,22 @@ __global__ void __launch_bounds__(kThreads, 1)
   const xgb_gemm_desc d = descs[t.g];
   const TcGroup gr = groups[t.g];
   const int64_t m0 = int64_t(t.tm) * BM, n0 = int64_t(t.tn) * BN;
-  const int warp = threadIdx.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nk = gr.slices;
 
-  if (warp == 0) {
+  if (warp == kMmaWarp) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                 "r"(kTmemCols));
+                 "r"(kTmemAlloc));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], kDrainWarps);
     }
     mbar_init(&done, 1);
     fail = 0;
@@ -265,56 +289,96 @@ __global__ void __launch_bounds__(kThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
 
-  if (nk > 0 && threadIdx.x == 0) {
-    // producer: bulk copies of the A and B pieces of every slice into the stage ring
-    constexpr int P = Form<F>::pieces, CU = Form<F>::chunk_units, CB = Form<F>::chunk_bytes;
-    const float* a_base = apack + gr.a_pack + int64_t(t.tm) * gr.slices * P * CU;
-    const float* b_base = bpack + gr.b_pack + int64_t(t.tn) * gr.slices * P * CU;
-    uint32_t ph[kStages] = {0, 0, 0};
-    for (int kc = 0; kc < nk; ++kc) {
-      const int s = kc % kStages;
-      if (kc >= kStages) {
-        if (!mbar_wait(&empty[s], ph[s])) { atomicExch(&fail, 1); break; }
+  // drain-warp state: TMEM lane quarter (rows), column group and the FP32 sums of its 64 columns
+  const int quarter = warp & 3, colq = warp >> 2;
+  float sum[kDrainCols];
+#pragma unroll
+  for (int j = 0; j < kDrainCols; ++j) sum[j] = 0.f;
+
+  if (nk > 0 && warp == kProducerWarp) {
+    if (lane == 0) {
+      // producer: bulk copies of the A and B pieces of every slice into the stage ring
+      constexpr int P = Form<F>::pieces, CU = Form<F>::chunk_units, CB = Form<F>::chunk_bytes;
+      const float* a_base = apack + gr.a_pack + int64_t(t.tm) * gr.slices * P * CU;
+      const float* b_base = bpack + gr.b_pack + int64_t(t.tn) * gr.slices * P * CU;
+      uint32_t ph[kStages] = {0, 0, 0};
+      for (int kc = 0; kc < nk; ++kc) {
+        const int s = kc % kStages;
+        if (kc >= kStages) {
+          if (!mbar_wait(&empty[s], ph[s])) { atomicExch(&fail, 1); break; }
+          ph[s] ^= 1u;
+        }
+        unsigned char* st = smem + s * Form<F>::stage_bytes;
+        mbar_expect_tx(&full[s], Form<F>::stage_bytes);
+        bulk_copy(st, a_base + int64_t(kc) * P * CU, P * CB, &full[s]);
+        bulk_copy(st + P * CB, b_base + int64_t(kc) * P * CU, P * CB, &full[s]);
+        issued = kc + 1;
+      }
+    }
+  } else if (nk > 0 && warp == kMmaWarp) {
+    if (lane == 0) {
+      // MMA issuer, per K step (8 TF32 or 16 BF16 = two 16-byte K groups): 3xTF32 takes hi*hi + hi*lo +
+      // lo*hi, BF16x9 all nine products of (hi, mid, lo) x (hi, mid, lo)
+      constexpr int P = Form<F>::pieces, CB = Form<F>::chunk_bytes;
+      const uint32_t idesc = make_idesc<F>();
+      uint32_t ph[kStages] = {0, 0, 0};
+      for (int kc = 0; kc < nk; ++kc) {
+        const int s = kc % kStages, b = kc & 1;
+        if (kc >= 2 && !mbar_wait(&acce[b], uint32_t(((kc >> 1) - 1) & 1))) { atomicExch(&fail, 1); break; }
+        if (!mbar_wait(&full[s], ph[s])) { atomicExch(&fail, 1); break; }
         ph[s] ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t base = smem_u32(smem + s * Form<F>::stage_bytes);
+        const uint32_t acc = tmem + uint32_t(b) * kTmemCols;
+        bool first = true;
+#pragma unroll
+        for (int kk = 0; kk < BK / Form<F>::kstep; ++kk) {
+          const uint32_t ko = uint32_t(kk) * 2 * LBO;
+#pragma unroll
+          for (int i = 0; i < P; ++i)
+#pragma unroll
+            for (int j = 0; j < P; ++j) {
+              if (F == 0 && i + j > 1) continue;  // 3xTF32 drops lo*lo
+              mma_form<F>(acc, make_desc(base + i * CB + ko), make_desc(base + (P + j) * CB + ko), idesc,
+                          first ? 0u : 1u);
+              first = false;
+            }
+        }
+        mma_commit(&empty[s]);
+        mma_commit(&accf[b]);
+        consumed = kc + 1;
       }
-      unsigned char* st = smem + s * Form<F>::stage_bytes;
-      mbar_expect_tx(&full[s], Form<F>::stage_bytes);
-      bulk_copy(st, a_base + int64_t(kc) * P * CU, P * CB, &full[s]);
-      bulk_copy(st + P * CB, b_base + int64_t(kc) * P * CU, P * CB, &full[s]);
-      issued = kc + 1;
+      mma_commit(&done);  // arrives when every MMA issued above has completed
     }
-  } else if (nk > 0 && threadIdx.x == 32) {
-    // MMA issuer, per K step (8 TF32 or 16 BF16 = two 16-byte K groups): 3xTF32 takes hi*hi + hi*lo +
-    // lo*hi, BF16x9 all nine products of (hi, mid, lo) x (hi, mid, lo); all accumulated in TMEM
-    constexpr int P = Form<F>::pieces, CB = Form<F>::chunk_bytes;
-    const uint32_t idesc = make_idesc<F>();
-    uint32_t ph[kStages] = {0, 0, 0};
+  } else if (nk > 0 && warp < kDrainWarps) {
     for (int kc = 0; kc < nk; ++kc) {
-      const int s = kc % kStages;
-      if (!mbar_wait(&full[s], ph[s])) { atomicExch(&fail, 1); break; }
-      ph[s] ^= 1u;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t base = smem_u32(smem + s * Form<F>::stage_bytes);
-#pragma unroll
-      for (int kk = 0; kk < BK / Form<F>::kstep; ++kk) {
-        const uint32_t ko = uint32_t(kk) * 2 * LBO;
-        bool first = kc == 0 && kk == 0;
-#pragma unroll
-        for (int i = 0; i < P; ++i)
-#pragma unroll
-          for (int j = 0; j < P; ++j) {
-            if (F == 0 && i + j > 1) continue;  // 3xTF32 drops lo*lo
-            mma_form<F>(tmem, make_desc(base + i * CB + ko), make_desc(base + (P + j) * CB + ko), idesc,
-                        first ? 0u : 1u);
-            first = false;
-          }
+      const int b = kc & 1;
+      // warp-uniform decision: the TMEM loads below are warp-collective
+      const bool got = __all_sync(0xffffffffu, mbar_wait(&accf[b], uint32_t((kc >> 1) & 1)));
+      if (!got) {
+        if (lane == 0) atomicExch(&fail, 1);
+        break;
       }
-      mma_commit(&empty[s]);
-      consumed = kc + 1;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int c = 0; c < kDrainCols / 8; ++c) {
+        uint32_t v[8];
+        const uint32_t taddr = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(b) * kTmemCols +
+                               uint32_t(colq * kDrainCols + c * 8);
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                       "=r"(v[7])
+                     : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 8; ++j) sum[c * 8 + j] = __fadd_rn(sum[c * 8 + j], __uint_as_float(v[j]));
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acce[b])) : "memory");
     }
-    mma_commit(&done);  // arrives when every MMA issued above has completed
   }
-  // everyone waits for the accumulator
+  // the drain warps have read every slice; make sure every MMA has retired before TMEM is freed
   bool ok = true;
   if (nk > 0) ok = mbar_wait(&done, 0);
   __syncthreads();
@@ -322,32 +386,21 @@ __global__ void __launch_bounds__(kThreads, 1)
   ok = __syncthreads_and(ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
-  if (ok && nk > 0) {
-    // epilogue: warp w reads TMEM lanes 32 w .. 32 w + 31 (rows), all 128 columns
-    const int64_t row = m0 + warp * 32 + (threadIdx.x & 31);
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-      uint32_t v[16];
-      const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0);
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-          : "r"(taddr));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < d.m) {
+  if (ok && nk > 0 && warp < kDrainWarps) {
+    const int64_t row = m0 + quarter * 32 + lane;
+    if (row < d.m) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int64_t col = n0 + c0 + j;
-          if (col < d.n) {
-            double* cp = C + d.c_off + row + col * d.ldc;
-            const double acc = double(__uint_as_float(v[j]));
-            *cp = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *cp);
-          }
+      for (int j = 0; j < kDrainCols; ++j) {
+        const int64_t col = n0 + colq * kDrainCols + j;
+        if (col < d.n) {
+          double* cp = C + d.c_off + row + col * d.ldc;
+          const double acc = double(sum[j]);
+          *cp = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *cp);
         }
       }
     }
   } else if (ok && nk == 0) {
-    for (int e = threadIdx.x; e < BM * BN; e += kThreads) {
+    for (int e = threadIdx.x; e < BM * BN; e += kTcThreads) {
       const int64_t row = m0 + e % BM, col = n0 + e / BM;
       if (row < d.m && col < d.n) {
         double* cp = C + d.c_off + row + col * d.ldc;
@@ -363,7 +416,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  if (warp == kMmaWarp)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemAlloc));
 }
 
 bool g_tc_attr = false;
@@ -413,14 +467,14 @@ void launch_gemm_tc(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const
       tc_pack_kernel<1><<<n_tasks, 256, 0, s>>>(d_descs, d_groups, d_tasks, A, B, apack, bpack);
       count_launch();
     }
-    gemm_tc_kernel<1><<<n_tiles, kThreads, kSmemBytes, s>>>(d_descs, d_groups, d_tiles, apack, bpack, C, alpha, beta,
+    gemm_tc_kernel<1><<<n_tiles, kTcThreads, kSmemBytes, s>>>(d_descs, d_groups, d_tiles, apack, bpack, C, alpha, beta,
                                                             g_tc_err);
   } else {
     if (n_tasks > 0) {
       tc_pack_kernel<0><<<n_tasks, 256, 0, s>>>(d_descs, d_groups, d_tasks, A, B, apack, bpack);
       count_launch();
     }
-    gemm_tc_kernel<0><<<n_tiles, kThreads, kSmemBytes, s>>>(d_descs, d_groups, d_tiles, apack, bpack, C, alpha, beta,
+    gemm_tc_kernel<0><<<n_tiles, kTcThreads, kSmemBytes, s>>>(d_descs, d_groups, d_tiles, apack, bpack, C, alpha, beta,
                                                             g_tc_err);
   }
   count_launch();

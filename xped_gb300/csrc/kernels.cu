@@ -37,6 +37,7 @@ thread_local std::string g_err;
 }  // namespace
 
 cudaStream_t stream() { return g_rt.stream; }
+bool runtime_ready() { return g_rt.ready; }
 int num_sms() { return g_rt.sms; }
 double* scalar_scratch() { return g_rt.scratch; }
 void count_launch(int n) { g_launches += n; }
@@ -279,59 +280,132 @@ int choose_gemm_tile(const xgb_gemm_desc* descs, int n) {
 }
 
 // ======================================================================= permute
-// Gather-permute with recoupling coefficients.  The flat element space of all
-// output sub-blocks is walked in output memory order (leg 0 fastest), so the
-// stores of a warp are contiguous within a sub-block row; the loads gather
-// through the permuted strides.
-__global__ void __launch_bounds__(256) permute_kernel(const xgb_perm_task* __restrict__ tasks,
-                                                      const int64_t* __restrict__ start, int n_tasks, int64_t total,
-                                                      const xgb_perm_contrib* __restrict__ contribs,
-                                                      const double* __restrict__ src, double* __restrict__ dst) {
-  constexpr int EPT = 4;
-  int64_t g = int64_t(blockIdx.x) * blockDim.x * EPT + threadIdx.x;
-  int cached = -1;
-  for (int e = 0; e < EPT; ++e, g += blockDim.x) {
-    if (g >= total) return;
-    int ti;
-    if (cached >= 0 && g >= start[cached] && g < start[cached + 1]) {
-      ti = cached;
-    } else {
-      int lo = 0, hi = n_tasks - 1;
-      while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (start[mid] <= g) lo = mid; else hi = mid - 1;
+// Gather-permute with recoupling coefficients, one ROW at a time: a row is the run of a task's
+// output sub-block along output leg 0 (all other leg indices fixed), which is contiguous in the
+// output (leg 0 fastest) and, for the permutations that keep the block's leading leg in front,
+// contiguous in the source too.  A group of G threads (G a power of two up to a warp, chosen on
+// the host from the rows' typical length) takes a row: its multi-index is decoded once per row
+// (not per element), and the lanes walk the row with unit stride, so a warp's loads and stores
+// cover whole 32-byte sectors.  Each group decodes U = 4 rows before loading, so every thread has
+// up to four independent loads in flight.  Tasks with several contributions (SU(2) recoupling)
+// accumulate them in a fixed order.
+template <int G>
+__global__ void __launch_bounds__(256) permute_rows_kernel(const xgb_perm_task* __restrict__ tasks,
+                                                           const int64_t* __restrict__ row_start, int n_tasks,
+                                                           int64_t total_rows, const xgb_perm_contrib* __restrict__ contribs,
+                                                           const double* __restrict__ src, double* __restrict__ dst) {
+  constexpr int U = 4;
+  const int lane = int(threadIdx.x) % G;
+  const int64_t group = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) / G;
+  const int64_t ngroups = int64_t(gridDim.x) * blockDim.x / G;
+  int cached = 0;
+  for (int64_t base = group; base < total_rows; base += ngroups * U) {
+    int64_t doff[U], soff[U], ds0[U], ss0[U];
+    double coeff[U];
+    int len[U];
+    int maxlen = 0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      len[u] = 0;
+      doff[u] = soff[u] = ds0[u] = ss0[u] = 0;
+      coeff[u] = 0.0;
+      const int64_t r = base + int64_t(u) * ngroups;
+      if (r >= total_rows) continue;
+      int ti = cached;
+      if (!(r >= row_start[ti] && r < row_start[ti + 1])) {
+        int lo = 0, hi = n_tasks - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (row_start[mid] <= r) lo = mid; else hi = mid - 1;
+        }
+        ti = lo;
+        cached = ti;
       }
-      ti = lo;
-      cached = ti;
+      const xgb_perm_task& t = tasks[ti];
+      const int d0 = t.rank > 0 ? t.dims[0] : 1;
+      int64_t rem = r - row_start[ti];
+      int idx[XGB_MAX_LEGS];
+      idx[0] = 0;
+      int64_t dofs = t.dst_base;
+      for (int k = 1; k < t.rank; ++k) {
+        const int dk = t.dims[k];
+        const int64_t q = rem / dk;
+        idx[k] = int(rem - q * dk);
+        rem = q;
+        dofs += idx[k] * t.dst_stride[k];
+      }
+      const int64_t dstr0 = t.rank > 0 ? t.dst_stride[0] : 0;
+      if (t.n_contrib == 1) {
+        const xgb_perm_contrib& cc = contribs[t.contrib0];
+        int64_t so = cc.src_base;
+        for (int k = 1; k < t.rank; ++k) so += idx[k] * cc.src_stride[k];
+        doff[u] = dofs;
+        soff[u] = so;
+        ds0[u] = dstr0;
+        ss0[u] = t.rank > 0 ? cc.src_stride[0] : 0;
+        coeff[u] = cc.coeff;
+        len[u] = d0;
+        maxlen = max(maxlen, d0);
+        continue;
+      }
+      // several source sub-blocks add into this row (SU(2)): fixed contribution order
+      for (int i = lane; i < d0; i += G) {
+        double v = 0.0;
+        for (int c = 0; c < t.n_contrib; ++c) {
+          const xgb_perm_contrib& cc = contribs[t.contrib0 + c];
+          int64_t so = cc.src_base + int64_t(i) * (t.rank > 0 ? cc.src_stride[0] : 0);
+          for (int k = 1; k < t.rank; ++k) so += idx[k] * cc.src_stride[k];
+          v = fma(cc.coeff, __ldg(src + so), v);
+        }
+        dst[dofs + int64_t(i) * dstr0] = v;
+      }
     }
-    const xgb_perm_task& t = tasks[ti];
-    int64_t rem = g - start[ti];
-    int idx[XGB_MAX_LEGS];
-    int64_t dofs = t.dst_base;
-    for (int k = 0; k < t.rank; ++k) {
-      int dk = t.dims[k];
-      int64_t q = rem / dk;
-      idx[k] = int(rem - q * dk);
-      rem = q;
-      dofs += idx[k] * t.dst_stride[k];
+    for (int i = lane; i < maxlen; i += G) {
+      double v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (i < len[u]) v[u] = coeff[u] * __ldg(src + soff[u] + int64_t(i) * ss0[u]);
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (i < len[u]) dst[doff[u] + int64_t(i) * ds0[u]] = v[u];
     }
-    double v = 0.0;
-    for (int c = 0; c < t.n_contrib; ++c) {
-      const xgb_perm_contrib& cc = contribs[t.contrib0 + c];
-      int64_t so = cc.src_base;
-      for (int k = 0; k < t.rank; ++k) so += idx[k] * cc.src_stride[k];
-      v = fma(cc.coeff, src[so], v);
-    }
-    dst[dofs] = v;
   }
 }
 
-void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_task_start, int n_tasks, int64_t total,
-                    const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s) {
-  if (total <= 0 || n_tasks <= 0) return;
-  int64_t per_block = 256 * 4;
-  int64_t blocks = (total + per_block - 1) / per_block;
-  permute_kernel<<<unsigned(blocks), 256, 0, s>>>(d_tasks, d_task_start, n_tasks, total, d_contribs, src, dst);
+PermRows perm_rows(const xgb_perm_task* tasks, int n_tasks) {
+  PermRows r;
+  r.row_start.assign(size_t(n_tasks) + 1, 0);
+  double elems = 0, weighted = 0;
+  for (int t = 0; t < n_tasks; ++t) {
+    const int64_t d0 = tasks[t].rank > 0 ? std::max<int64_t>(tasks[t].dims[0], 1) : 1;
+    const int64_t rows = d0 > 0 ? tasks[t].nelem / d0 : 0;
+    r.row_start[t + 1] = r.row_start[t] + rows;
+    elems += double(tasks[t].nelem);
+    weighted += double(tasks[t].nelem) * double(d0);
+  }
+  r.total_rows = r.row_start.back();
+  const double avg = elems > 0 ? weighted / elems : 1.0;  // element-weighted row length
+  r.group = 1;
+  while (r.group < 32 && 2.0 * r.group <= avg * 1.25) r.group *= 2;
+  return r;
+}
+
+void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_row_start, int n_tasks, int64_t total_rows,
+                    int group, const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s) {
+  if (total_rows <= 0 || n_tasks <= 0) return;
+  // one group per row, four rows per group and pass; enough CTAs to fill the GPU a few times over
+  const int64_t groups_needed = (total_rows + 3) / 4;
+  const int64_t per_block = 256 / group;
+  const int64_t cap = int64_t(num_sms() > 0 ? num_sms() : 152) * 16;
+  const unsigned blocks = unsigned(std::max<int64_t>(1, std::min<int64_t>(cap, (groups_needed + per_block - 1) / per_block)));
+  switch (group) {
+    case 32: permute_rows_kernel<32><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case 16: permute_rows_kernel<16><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case 8: permute_rows_kernel<8><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case 4: permute_rows_kernel<4><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case 2: permute_rows_kernel<2><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    default: permute_rows_kernel<1><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+  }
   count_launch();
 }
 
@@ -817,6 +891,12 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
     return check_cuda(cudaGetLastError(), "tensor-core gemm launch");
   }
   const int tile = choose_gemm_tile(descs, n_groups);
+  if (precision == XGB_PREC_FP64) {
+    // FP64: the built-in shape (no split-K) or, with autotuning on, the tuned one of the list's bucket
+    const F64Config cfg = gemm_f64_config(descs, n_groups, A, B, {tile, 0}, s);
+    run_gemm_f64_config(descs, n_groups, cfg, A, B, C, alpha, beta, s);
+    return check_cuda(cudaGetLastError(), "gemm launch");
+  }
   std::vector<GemmTile> tiles;
   for (int g = 0; g < n_groups; ++g) {
     int64_t tm = (descs[g].m + tile - 1) / tile, tn = (descs[g].n + tile - 1) / tile;
@@ -827,15 +907,11 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
   order_tiles_by_work(tiles, descs);
   auto* dd = upload(descs, size_t(n_groups), s);
   auto* dt = upload(tiles.data(), tiles.size(), s);
-  if (precision == XGB_PREC_FP32) {
-    double flops = 0;
-    for (int g = 0; g < n_groups; ++g) flops += 2.0 * double(descs[g].m) * double(descs[g].n) * double(descs[g].k);
-    prof_begin(K_GEMM_F32, s);
-    launch_gemm_f32(dd, dt, int(tiles.size()), tile, A, B, C, alpha, beta, s);
-    prof_end(K_GEMM_F32, s, flops);
-  } else {
-    launch_gemm_f64(dd, dt, int(tiles.size()), tile, A, B, C, alpha, beta, s);
-  }
+  double flops = 0;  // XGB_PREC_FP32 (the other forms returned above)
+  for (int g = 0; g < n_groups; ++g) flops += 2.0 * double(descs[g].m) * double(descs[g].n) * double(descs[g].k);
+  prof_begin(K_GEMM_F32, s);
+  launch_gemm_f32(dd, dt, int(tiles.size()), tile, A, B, C, alpha, beta, s);
+  prof_end(K_GEMM_F32, s, flops);
   dev_free(dd);
   dev_free(dt);
   return check_cuda(cudaGetLastError(), "gemm launch");
@@ -855,18 +931,24 @@ int xgb_permute(int n_tasks, const xgb_perm_task* tasks, int n_contrib, const xg
   XGB_REQUIRE_INIT();
   XGB_GUARD_BEGIN
   cudaStream_t s = pick(stream_);
-  std::vector<int64_t> start(size_t(n_tasks) + 1, 0);
   for (int t = 0; t < n_tasks; ++t) {
     if (tasks[t].rank < 0 || tasks[t].rank > XGB_MAX_LEGS) return set_error(XGB_E_BADPLAN, "task rank out of range");
     if (tasks[t].contrib0 < 0 || tasks[t].contrib0 + tasks[t].n_contrib > n_contrib)
       return set_error(XGB_E_BADPLAN, "contribution index out of range");
-    start[t + 1] = start[t] + tasks[t].nelem;
+    int64_t prod = 1;
+    for (int k = 0; k < tasks[t].rank; ++k) {
+      if (tasks[t].dims[k] <= 0) return set_error(XGB_E_BADPLAN, "task extent must be positive");
+      prod *= tasks[t].dims[k];
+    }
+    if (prod != tasks[t].nelem) return set_error(XGB_E_BADPLAN, "task nelem differs from the product of its extents");
   }
-  if (n_tasks == 0 || start.back() == 0) return XGB_OK;
+  if (n_tasks == 0) return XGB_OK;
+  const PermRows rows = perm_rows(tasks, n_tasks);
+  if (rows.total_rows == 0) return XGB_OK;
   auto* dt = upload(tasks, size_t(n_tasks), s);
-  auto* ds = upload(start.data(), start.size(), s);
+  auto* ds = upload(rows.row_start.data(), rows.row_start.size(), s);
   auto* dc = upload(contribs, size_t(n_contrib), s);
-  launch_permute(dt, ds, n_tasks, start.back(), dc, src, dst, s);
+  launch_permute(dt, ds, n_tasks, rows.total_rows, rows.group, dc, src, dst, s);
   dev_free(dt);
   dev_free(ds);
   dev_free(dc);

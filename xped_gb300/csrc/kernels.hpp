@@ -30,6 +30,7 @@ void order_tiles_by_work(std::vector<GemmTile>& tiles, const xgb_gemm_desc* desc
 
 // runtime ------------------------------------------------------------------------
 cudaStream_t stream();
+bool runtime_ready();  // xgb_init has run
 int set_error(int code, const std::string& msg);
 int check_cuda(cudaError_t e, const char* what);
 void* dev_alloc(size_t bytes);          // stream-ordered; throws std::bad_alloc on failure
@@ -55,8 +56,16 @@ void launch_gemm_f32(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int 
 inline bool gemm_precision_available(int p) {
   return p == XGB_PREC_FP64 || p == XGB_PREC_3XTF32 || p == XGB_PREC_FP32 || p == XGB_PREC_BF16X9;
 }
-void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_task_start, int n_tasks, int64_t total,
-                    const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s);
+// permute launch shape: rows (runs along output leg 0) per task as prefix sums, and the number of
+// threads that share one row (a power of two up to 32, from the element-weighted row length)
+struct PermRows {
+  std::vector<int64_t> row_start;
+  int64_t total_rows = 0;
+  int group = 1;
+};
+PermRows perm_rows(const xgb_perm_task* tasks, int n_tasks);
+void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_row_start, int n_tasks, int64_t total_rows,
+                    int group, const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s);
 // h_descs: host copy of the descriptors (blocks at least kSvdGridMin wide run one at a time on a
 // grid-wide Jacobi kernel over all SMs; nullptr keeps every block on the cluster kernel)
 void launch_svd(const xgb_svd_desc* d_descs, const xgb_svd_desc* h_descs, const int64_t* d_work_off, int n,
@@ -141,6 +150,28 @@ void launch_mlp_reduce_adam(float* params, float* mom, float* vel, const float* 
 enum KernelKind { K_GEMM = 0, K_PERMUTE, K_SVD, K_TRUNC, K_QR, K_ABSMAX, K_SCALE, K_COPY2D, K_DIAG, K_GEMM_TC, K_SKETCH, K_MLP, K_GEMM_F32, K_COUNT };
 void prof_begin(int kind, cudaStream_t s);
 void prof_end(int kind, cudaStream_t s, double work);
+
+// FP64 grouped-GEMM launch shapes and their autotuner (autotune.cpp): tile edge 16/32/64 and a
+// split-K target of split_waves x SMs CTAs (0: no split)
+struct F64Config { int tile = 16; int split_waves = 0; };
+struct F64Plan {
+  int tile = 16;
+  std::vector<GemmTile> tiles;
+  std::vector<SplitReduce> red;
+  int32_t slots = 0;  // split-K partial tiles (workspace of slots x tile x tile doubles)
+};
+F64Plan plan_gemm_f64(const xgb_gemm_desc* d, int n, F64Config c);
+// executes a plan whose tables are on the device (workspace allocated stream-ordered for split-K)
+void run_f64_plan(const F64Plan& p, const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, const SplitReduce* d_red,
+                  const double* A, const double* B, double* C, double alpha, double beta, cudaStream_t s);
+// plans, stages the tables and runs one configuration (host descriptors)
+void run_gemm_f64_config(const xgb_gemm_desc* h_descs, int n, F64Config c, const double* A, const double* B, double* C,
+                         double alpha, double beta, cudaStream_t s);
+// the configuration to use for this list: tuned (measured on A, B the first time its size bucket is
+// met) when autotuning is on, `fallback` otherwise
+F64Config gemm_f64_config(const xgb_gemm_desc* d, int n, const double* A, const double* B, F64Config fallback,
+                          cudaStream_t s);
+int autotune_mode();
 
 // helpers
 size_t svd_work_elems(int64_t m, int64_t n);

@@ -54,53 +54,21 @@ double* alloc_d(int64_t n) { return static_cast<double*>(dev_alloc(sizeof(double
 // Grouped FP64 GEMM of the sketch pipeline.  When the output tiles cannot fill the SMs
 // (the l x l Gram matrices Y^T Y: few tiles, k = the block's row count) the k range of each
 // tile is split so that about two CTAs per SM run; the partial tiles land in a workspace and
-// one reduce launch adds them in a fixed order (deterministic result).
+// one reduce launch adds them in a fixed order (deterministic result).  With autotuning on, the
+// tile edge and the split target are the tuned ones of the list's size bucket.
 void grouped_gemm(const std::vector<xgb_gemm_desc>& d, const double* A, const double* B, double* C, cudaStream_t s,
                   double alpha = 1.0, double beta = 0.0) {
   if (d.empty()) return;
-  const int tile = choose_gemm_tile(d.data(), int(d.size()));
-  const int64_t target = 2 * int64_t(num_sms() > 0 ? num_sms() : 152);
-  int64_t n_out = 0;
+  const F64Config fallback{choose_gemm_tile(d.data(), int(d.size())), 2};
+  const F64Config cfg = gemm_f64_config(d.data(), int(d.size()), A, B, fallback, s);
+  const F64Plan p = plan_gemm_f64(d.data(), int(d.size()), cfg);
   double flops = 0;
-  for (const auto& g : d) {
-    n_out += ((g.m + tile - 1) / tile) * ((g.n + tile - 1) / tile);
-    flops += 2.0 * double(g.m) * double(g.n) * double(g.k);
-  }
-  constexpr int64_t kMinChunk = 64;  // k per partial tile, multiple of the 16-deep k step
-  const int64_t want = n_out > 0 ? (target + n_out - 1) / n_out : 1;
-  std::vector<GemmTile> tiles;
-  std::vector<SplitReduce> red;
-  int32_t slots = 0;
-  for (size_t g = 0; g < d.size(); ++g) {
-    const int64_t tm = (d[g].m + tile - 1) / tile, tn = (d[g].n + tile - 1) / tile;
-    const int64_t splits = std::max<int64_t>(1, std::min<int64_t>(want, d[g].k / kMinChunk));
-    const int64_t chunk = splits > 1 ? (((d[g].k + splits - 1) / splits + 15) / 16) * 16 : d[g].k;
-    for (int64_t y = 0; y < tn; ++y)
-      for (int64_t x = 0; x < tm; ++x) {
-        if (splits == 1) {
-          tiles.push_back({int32_t(g), int32_t(x), int32_t(y), tile});
-          continue;
-        }
-        const int32_t first = slots;
-        for (int64_t k0 = 0; k0 < d[g].k; k0 += chunk)
-          tiles.push_back({int32_t(g), int32_t(x), int32_t(y), tile, int32_t(k0),
-                           int32_t(std::min<int64_t>(k0 + chunk, d[g].k)), slots++});
-        red.push_back({int32_t(g), int32_t(x), int32_t(y), first, slots - first, 0});
-      }
-  }
-  order_tiles_by_work(tiles, d.data());
+  for (const auto& g : d) flops += 2.0 * double(g.m) * double(g.n) * double(g.k);
   Staging st;
-  const size_t od = st.add(d), ot = st.add(tiles), orr = st.add(red);
+  const size_t od = st.add(d), ot = st.add(p.tiles), orr = st.add(p.red);
   st.upload(s);
   prof_begin(K_GEMM, s);
-  if (red.empty()) {
-    launch_gemm_f64(st.at<xgb_gemm_desc>(od), st.at<GemmTile>(ot), int(tiles.size()), tile, A, B, C, alpha, beta, s);
-  } else {
-    double* ws = alloc_d(int64_t(slots) * tile * tile);
-    launch_gemm_f64_splitk(st.at<xgb_gemm_desc>(od), st.at<GemmTile>(ot), int(tiles.size()), tile,
-                           st.at<SplitReduce>(orr), int(red.size()), A, B, C, ws, alpha, beta, s);
-    dev_free(ws);
-  }
+  run_f64_plan(p, st.at<xgb_gemm_desc>(od), st.at<GemmTile>(ot), st.at<SplitReduce>(orr), A, B, C, alpha, beta, s);
   prof_end(K_GEMM, s, flops);
 }
 

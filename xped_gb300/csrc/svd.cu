@@ -38,6 +38,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <new>
 #include <stdexcept>
 #include <cmath>
 #include <string>
@@ -704,9 +705,11 @@ double* g_noalloc_ptr[64] = {nullptr};
 
 extern "C" size_t xgb_batched_svd_noalloc_capacity_bytes(void) { return xgb::kNoAllocDoubles * sizeof(double); }
 
-extern "C" int xgb_batched_svd_noalloc(int n, const xgb_svd_desc* descs, const double* A, double* U, double* S,
-                                       double* Vt, void* stream_) {
-  using namespace xgb;
+namespace xgb {
+namespace {
+int batched_svd_noalloc(int n, const xgb_svd_desc* descs, const double* A, double* U, double* S, double* Vt,
+                        void* stream_) {
+  if (!runtime_ready()) return set_error(XGB_E_NOINIT, "xgb_init was not called");
   if (n <= 0) return XGB_OK;
   if (!descs) return set_error(XGB_E_BADPLAN, "xgb_batched_svd_noalloc: descriptor array is NULL");
   int dev = 0;
@@ -716,11 +719,15 @@ extern "C" int xgb_batched_svd_noalloc(int n, const xgb_svd_desc* descs, const d
   const size_t desc_doubles = (sizeof(xgb_svd_desc) * size_t(n) + 255) / 256 * 32;
   const size_t off_doubles = (sizeof(int64_t) * size_t(n) + 255) / 256 * 32;
   std::vector<int64_t> off(static_cast<size_t>(n));
+  std::vector<int> wide;
   size_t work = 0;
   for (int i = 0; i < n; ++i) {
     if (descs[i].m < 0 || descs[i].n < 0) return set_error(XGB_E_BADPLAN, "xgb_batched_svd_noalloc: negative extent");
+    if (std::min(descs[i].m, descs[i].n) > 8192)
+      return set_error(XGB_E_UNSUPPORTED, "xgb_batched_svd_noalloc: SVD block larger than 8192 columns");
     off[i] = int64_t(work);
     work += svd_work_elems(descs[i].m, descs[i].n);
+    if (std::min(descs[i].m, descs[i].n) >= kSvdGridMin) wide.push_back(i);
   }
   const size_t need = desc_doubles + off_doubles + work;
   if (need > kNoAllocDoubles)
@@ -743,16 +750,47 @@ extern "C" int xgb_batched_svd_noalloc(int n, const xgb_svd_desc* descs, const d
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, off.data(), sizeof(int64_t) * size_t(n), cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return set_error(XGB_E_CUDA, std::string("descriptor copy: ") + cudaGetErrorString(e));
   cudaFuncSetAttribute(svd_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+  cudaFuncSetAttribute(svd_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+  // the same split as xgb_batched_svd: blocks at least kSvdGridMin wide run on the grid-wide kernel
+  // (a cooperative launch, which allocates nothing), the narrower ones on the cluster kernel
+  const int64_t grid_min = wide.empty() ? INT64_MAX : kSvdGridMin;
   svd_cluster_kernel<<<n * kCluster, kThreads, kSmemLimit, s>>>(d_descs, d_off, A, U, S, Vt, d_work, nullptr,
-                                                                kSmemLimit, INT64_MAX);
+                                                                kSmemLimit, grid_min);
   count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(XGB_E_CUDA, std::string("svd launch: ") + cudaGetErrorString(e));
+  int smem = kSmemLimit;
+  int* no_stats = nullptr;
+  for (int sector : wide) {
+    const int64_t nn = std::min(descs[sector].m, descs[sector].n);
+    const int ctas =
+        int(std::max<int64_t>(1, std::min<int64_t>(num_sms(), (nn + 2 * kGridCols - 1) / (2 * kGridCols))));
+    void* args[] = {&d_descs, &d_off, &sector, const_cast<double**>(&A), &U, &S, &Vt, &d_work, &no_stats, &smem};
+    e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(svd_grid_kernel), dim3(ctas), dim3(kThreads), args,
+                                    size_t(smem), s);
+    if (e != cudaSuccess) return set_error(XGB_E_CUDA, std::string("svd grid launch: ") + cudaGetErrorString(e));
+    count_launch();
+  }
+  // no sweep statistics are recorded here: xgb_svd_last_sweeps reports none after this call
+  g_stats_n = 0;
   // the descriptor copies read pageable host memory that the caller may free
-  // on return, so wait for them (and the kernel) before returning
+  // on return, so wait for them (and the kernels) before returning
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return set_error(XGB_E_CUDA, std::string("svd: ") + cudaGetErrorString(e));
   return XGB_OK;
+}
+}  // namespace
+}  // namespace xgb
+
+extern "C" int xgb_batched_svd_noalloc(int n, const xgb_svd_desc* descs, const double* A, double* U, double* S,
+                                       double* Vt, void* stream_) {
+  try {
+    return xgb::batched_svd_noalloc(n, descs, A, U, S, Vt, stream_);
+  } catch (const std::bad_alloc&) {
+    return xgb::set_error(XGB_E_OOM, "xgb_batched_svd_noalloc: host allocation failed");
+  } catch (const std::exception& ex) {
+    return xgb::set_error(XGB_E_BADPLAN, ex.what());
+  }
 }
 
 extern "C" int xgb_svd_last_sweeps(int32_t* out, int cap) {

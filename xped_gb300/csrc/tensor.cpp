@@ -122,9 +122,10 @@ struct PermPlan {
   MetaPtr out;
   bool needs_zero = false;
   int n_tasks = 0;
-  int64_t total = 0;
+  int64_t total_rows = 0;
+  int group = 1;
   xgb_perm_task* d_tasks = nullptr;
-  int64_t* d_start = nullptr;
+  int64_t* d_row_start = nullptr;
   xgb_perm_contrib* d_contribs = nullptr;
   double bytes = 0;  // algorithmic: every output written once, every contribution read once
 };
@@ -142,15 +143,21 @@ struct GemmPlan {
   TcPackTask* d_tc_tasks = nullptr;
   GemmTile* d_tc_tiles = nullptr;
   std::vector<xgb_gemm_desc> host_descs;
+  // FP64 launch shape (tile edge, split-K): the built-in rule, or the autotuner's choice
+  F64Plan f64;
+  GemmTile* d_f64_tiles = nullptr;
+  SplitReduce* d_f64_red = nullptr;
 };
 std::shared_ptr<PermPlan> upload_tables(const PermTables& t) {
   auto plan = std::make_shared<PermPlan>();
   plan->out = t.out;
   plan->n_tasks = int(t.tasks.size());
-  plan->total = t.start.back();
   plan->needs_zero = t.needs_zero;
   plan->d_tasks = dev_table(t.tasks);
-  plan->d_start = dev_table(t.start);
+  const PermRows rows = perm_rows(t.tasks.data(), int(t.tasks.size()));
+  plan->total_rows = rows.total_rows;
+  plan->group = rows.group;
+  plan->d_row_start = dev_table(rows.row_start);
   plan->d_contribs = dev_table(t.contribs);
   for (const auto& task : t.tasks) plan->bytes += 8.0 * double(task.nelem) * (1 + task.n_contrib);
   return plan;
@@ -384,7 +391,8 @@ std::shared_ptr<PermPlan> get_perm_plan(const TensorMeta& m, uint32_t mask, int 
 Tensor run_perm_plan(const PermPlan& plan, const Tensor& src) {
   Tensor out = plan.needs_zero ? zeros(plan.out) : empty_like_meta(plan.out);
   prof_begin(K_PERMUTE, stream());
-  launch_permute(plan.d_tasks, plan.d_start, plan.n_tasks, plan.total, plan.d_contribs, src.data(), out.data(), stream());
+  launch_permute(plan.d_tasks, plan.d_row_start, plan.n_tasks, plan.total_rows, plan.group, plan.d_contribs, src.data(),
+                 out.data(), stream());
   prof_end(K_PERMUTE, stream(), plan.bytes);
   return out;
 }
@@ -395,8 +403,13 @@ CacheStats cache_stats() { return g_stats; }
 void clear_plan_caches() {
   std::lock_guard<std::mutex> lk(g_plan_mu);
   cudaStreamSynchronize(stream());
-  for (auto& [k, p] : g_perm_plans) { cudaFree(p->d_tasks); cudaFree(p->d_start); cudaFree(p->d_contribs); }
-  for (auto& [k, p] : g_gemm_plans) { cudaFree(p->d_descs); cudaFree(p->d_tiles); }
+  for (auto& [k, p] : g_perm_plans) { cudaFree(p->d_tasks); cudaFree(p->d_row_start); cudaFree(p->d_contribs); }
+  for (auto& [k, p] : g_gemm_plans) {
+    cudaFree(p->d_descs);
+    cudaFree(p->d_tiles);
+    cudaFree(p->d_f64_tiles);
+    cudaFree(p->d_f64_red);
+  }
   g_perm_plans.clear();
   g_gemm_plans.clear();
 }
@@ -567,6 +580,11 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
     plan->host_descs = descs;
     plan->d_descs = dev_table(descs);
     plan->d_tiles = dev_table(tiles);
+    const F64Config cfg =
+        gemm_f64_config(descs.data(), int(descs.size()), a.data(), b.data(), {plan->tile, 0}, stream());
+    plan->f64 = plan_gemm_f64(descs.data(), int(descs.size()), cfg);
+    plan->d_f64_tiles = dev_table(plan->f64.tiles);
+    plan->d_f64_red = dev_table(plan->f64.red);
     for (const auto& d : descs) plan->flops += 2.0 * double(d.m) * double(d.n) * double(d.k);
     std::lock_guard<std::mutex> lk(g_plan_mu);
     ++g_stats.gemm_misses;
@@ -629,7 +647,8 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
     return out;
   }
   prof_begin(K_GEMM, stream());
-  launch_gemm_f64(plan->d_descs, plan->d_tiles, plan->n_tiles, plan->tile, a.data(), b.data(), out.data(), 1.0, 0.0, stream());
+  run_f64_plan(plan->f64, plan->d_descs, plan->d_f64_tiles, plan->d_f64_red, a.data(), b.data(), out.data(), 1.0, 0.0,
+               stream());
   prof_end(K_GEMM, stream(), plan->flops);
   return out;
 }
@@ -1522,6 +1541,33 @@ void CTM::grow_all() {
   move('R');
   move('T');
   move('B');
+}
+
+CTM::SolveResult CTM::solve(const Tensor& H, double tol_E, int max_steps) {
+  // CTMSolver::solve without AD (src/PEPS/CTMSolver.cpp:50-80) on a 1x1 cell: grow_all, the bond
+  // energy per site E = <H>_h + <H>_v from computeRDM, stop when |E - E_prev| < tol_E or, as an
+  // oscillation, |E - E_prevprev| < tol_E; `steps` counts the grow_all steps run
+  SolveResult r;
+  double prev = 1000.0, prevprev = 1000.0;
+  for (int step = 0; step < max_steps; ++step) {
+    grow_all();
+    const double E = bond_expectation(rdm(false), H) + bond_expectation(rdm(true), H);
+    r.energies.push_back(E);
+    r.E = E;
+    r.steps = step + 1;
+    if (std::abs(E - prev) < tol_E) {
+      r.converged = true;
+      break;
+    }
+    if (std::abs(E - prevprev) < tol_E) {
+      r.converged = true;
+      r.oscillation = true;
+      break;
+    }
+    prevprev = prev;
+    prev = E;
+  }
+  return r;
 }
 
 }  // namespace xgb

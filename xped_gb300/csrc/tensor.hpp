@@ -215,6 +215,15 @@ class CTM {
   std::tuple<Tensor, Tensor, Tensor> renormalize(char dir, const Tensor& P1, const Tensor& P2);
   // computeRDM_h / computeRDM_v (src/PEPS/CTM.cpp:583-627, 756-790), normalised
   Tensor rdm(bool vertical);
+  // CTMSolver::solve without AD (src/PEPS/CTMSolver.cpp:50-80): grow_all until the bond energy per
+  // site changes by less than tol_E (or returns to within tol_E of the value two steps back)
+  struct SolveResult {
+    double E = 0.0;
+    int steps = 0;
+    bool converged = false, oscillation = false;
+    std::vector<double> energies;
+  };
+  SolveResult solve(const Tensor& H, double tol_E, int max_steps);
   Tensor& slot(int which);  // 0..3 = C1..C4, 4..7 = T1..T4, 8 = A, 9 = Adag
   int64_t chi = 0;
 

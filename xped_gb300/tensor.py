@@ -512,6 +512,17 @@ class CTM:
     def rdm_v(self) -> Tensor:
         return Tensor(lib().xgb_ctm_rdm(self._h, 1))
 
+    def solve(self, H: Tensor, tol_E: float = 1e-10, max_steps: int = 100):
+        """CTMSolver::solve (src/PEPS/CTMSolver.cpp:50-80): grow_all until the bond energy per site
+        changes by less than tol_E (or oscillates within it).  Returns a dict with the final
+        energy, the steps run, whether it converged / stopped on oscillation and every step's energy."""
+        E, steps, flags = C.c_double(), C.c_int(), C.c_int()
+        buf = (C.c_double * max(max_steps, 1))()
+        check(lib().xgb_ctm_solve(self._h, H._h, float(tol_E), int(max_steps), C.byref(E), C.byref(steps),
+                                  C.byref(flags), buf, max_steps), "ctm_solve")
+        return {"E": E.value, "steps": steps.value, "converged": bool(flags.value & 1),
+                "oscillation": bool(flags.value & 2), "energies": list(buf[:steps.value])}
+
 
 FEATURES = 8  # per-sector inputs of the rank predictor
 
