@@ -165,6 +165,8 @@ def run_gpu(args):
     H = heisenberg_bond(phys)
     res = {}
 
+    if args.autotune:
+        L.xgb_autotune_set(1)  # FP64 GEMM tile / split-K shapes tuned per size bucket during the warm-up
     # ---- chosen form: warm-up (the energy after COMPARE_STEPS steps is kept for the comparison);
     # its projector decompositions are logged to train the width predictor
     t0 = time.perf_counter()
@@ -179,6 +181,7 @@ def run_gpu(args):
     records = ctm.records()
     ctm.record(False)
     res["chosen_setup_s"] = time.perf_counter() - t0
+    res["autotune"] = autotune_report(L)
 
     flush_bytes = 512 << 20  # > 129 MB L2, written between timed steps outside the events
     flush = C.c_void_p()
@@ -281,6 +284,12 @@ def run_gpu(args):
         for _ in range(COMPARE_STEPS):
             lc.grow_all()
         res["e_learned"] = energy(lc, H)
+        if not args.no_converge:
+            lc2 = make_ctm(A, CHI, "plain", args.gemm)
+            lc2.set_rank_model(model, margin=0.0, min_oversample=2, power_iters=POWER_ITERS, seed=SEED)
+            lc2.set_sketch_precision(args.sketch_tail)
+            res["solve_learned"] = timed_solve(L, lc2, H, args)
+            del lc2
         s0 = lc.stats()
         ms = []
         for _ in range(args.steps):
@@ -296,19 +305,28 @@ def run_gpu(args):
         res["learned_redo_per_step"] = (s1["redo"] - s0["redo"]) / args.steps
         del lc
 
-    # ---- plain FP64 form, same workload: COMPARE_STEPS steps, the last one timed
+    # ---- the chosen form run to convergence (CTMSolver::solve) from a fresh FROM_A start
+    if not args.no_converge:
+        cc = make_ctm(A, CHI, "chosen", args.gemm, args.sketch_tail)
+        res["solve_chosen"] = timed_solve(L, cc, H, args)
+        del cc
+
+    # ---- plain FP64 form, same workload: COMPARE_STEPS steps (energy compared with the chosen form's),
+    # then on to convergence; one more step at saturated chi is timed
     if not args.no_plain:
         t0 = time.perf_counter()
         plain = make_ctm(A, CHI, "plain", "fp64")
-        for _ in range(COMPARE_STEPS - 1):
+        for _ in range(COMPARE_STEPS):
             plain.grow_all()
+        res["e_plain"] = energy(plain, H)
+        if not args.no_converge:
+            res["solve_plain"] = timed_solve(L, plain, H, args, done=COMPARE_STEPS)
         flush_l2()
         L.xgb_synchronize()
         L.xgb_event_record(4)
         plain.grow_all()
         L.xgb_event_record(5)
         res["plain_ms"] = L.xgb_event_elapsed_ms(4, 5)
-        res["e_plain"] = energy(plain, H)
         res["plain_wall_s"] = time.perf_counter() - t0
         del plain
     res["e_chosen"] = e_chosen
@@ -332,7 +350,145 @@ def run_gpu(args):
     res["tensor22_chain"] = tensor22_chain()
     res["fp64_peak"] = fp64_library_peak()
     res["su"] = su_step()
+    res["permute_roofline"] = permute_roofline()
+    if not args.no_configs:
+        res["tsvd_sweep"] = tsvd_sweep(eval_seeds=(0, 1), train_seeds=tuple(range(100, 106)), steps=4)
+        res["fz2"] = fz2_compact(args)
     return res
+
+
+def autotune_report(L):
+    """The FP64 GEMM shapes the autotuner chose (per size bucket) and the time it spent measuring."""
+    import ctypes as C
+    measured, hits, ms = C.c_int64(), C.c_int64(), C.c_double()
+    n = L.xgb_autotune_stats(C.byref(measured), C.byref(hits), C.byref(ms))
+    tiles, waves = (C.c_int32 * max(n, 1))(), (C.c_int32 * max(n, 1))()
+    L.xgb_autotune_choices(tiles, waves, n)
+    hist = {}
+    for i in range(n):
+        k = f"tile{tiles[i]}_split{waves[i]}"
+        hist[k] = hist.get(k, 0) + 1
+    return {"enabled": True, "buckets": n, "cache_hits": hits.value, "measure_ms": ms.value, "choices": hist,
+            "candidates": "tile 16/32/64 x split-K target 0/1/2/4 waves"}
+
+
+def timed_solve(L, c, H, args, done=0):
+    """CTMSolver::solve on `c` (tol_E, at most --solve-max-steps grow_all steps); `done` steps were already
+    run on it.  Device time of the whole solve (CUDA events) and the energy trajectory."""
+    L.xgb_synchronize()
+    L.xgb_event_record(12)
+    r = c.solve(H, tol_E=args.tol_e, max_steps=args.solve_max_steps)
+    L.xgb_event_record(13)
+    r["seconds"] = L.xgb_event_elapsed_ms(12, 13) / 1e3
+    r["steps_total"] = r["steps"] + done
+    r["tol_E"] = args.tol_e
+    r["energies"] = [float(e) for e in r["energies"][-4:]]  # the last few are enough to show convergence
+    return r
+
+
+def permute_roofline(degs=(20, 40, 60, 40, 20), reps=5):
+    """Tensor::permute<0>(0, 2, 1, 3) of one U(1) Tensor<2,2> with every leg q = -2..2 at degeneracies
+    `degs` (1.42 GB of FP64 blocks, far above the 129 MB L2): kernel time per launch from the library's
+    per-launch CUDA events, achieved HBM GB/s = algorithmic bytes (every element read once and written
+    once, 16 B) / time, against the measured copy rate."""
+    from xped_gb300 import Basis, Tensor, lib
+    from xped_gb300._lib import profile_read
+    L = lib()
+    B = Basis.from_pairs("U1", list(zip(range(-2, 3), degs)), sort=True)
+    T = Tensor.zeros([B, B], [B, B])
+    T.set_data(np.random.default_rng(SEED).standard_normal(T.size))
+    out = T.permute(0, [0, 2, 1, 3])  # plan built and cached
+    del out
+    L.xgb_synchronize()
+    L.xgb_profile_reset()
+    L.xgb_profile_enable(1)
+    for _ in range(reps):
+        out = T.permute(0, [0, 2, 1, 3])
+        del out
+    L.xgb_synchronize()
+    L.xgb_profile_enable(0)
+    n, ms, work = profile_read()["permute"]
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    per_launch = ms / max(n, 1)
+    algorithmic = 16.0 * T.size
+    gbs = algorithmic / (per_launch * 1e-3) / 1e9
+    del T
+    return {"kernel": "permute_rows_kernel", "elements": int(algorithmic // 16), "gbytes_moved": algorithmic / 1e9,
+            "launches": int(n), "ms_per_launch": per_launch, "achieved": gbs, "peak": hbm, "unit": "GB/s",
+            "frac": gbs / hbm, "bound": "hbm",
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
+            "workload": "U(1) Tensor<2,2>, legs q -2..2 deg " + str(list(degs)) + ", permute<0>(0,2,1,3)"}
+
+
+FZ2_CHI_SMALL = 48  # the plain form's 20 iterations at chi = 144 take ~17 min; the equal-energy check runs here
+
+
+def fz2_compact(args):
+    """The full chosen form on the fermionic Z2 iPEPS (D=6, q 0,1 with degeneracies [3,3]): FZ2_ITERS CTMRG
+    iterations at chi = 144 of the chosen and the learned-width forms (per-step CUDA-event times), and the
+    density-density bond after FZ2_ITERS iterations of the chosen and the plain FP64 form at chi = 48
+    (the plain form's exact SVDs of ~2600-wide blocks take ~52 s per step at chi = 144)."""
+    from xped_gb300 import CTM, Basis, Tensor, lib
+    from xped_gb300.learn import RankModel, dataset
+    from xped_gb300.observables import density_bond, energy
+    L = lib()
+    aux = Basis.from_pairs("fZ2", FZ2_AUX)
+    phys = Basis.from_pairs("fZ2", FZ2_PHYS)
+    A = Tensor.zeros([aux, aux], [aux, aux, phys])
+    A.set_data(np.random.default_rng(SEED).standard_normal(A.size))
+    H = density_bond(phys)
+    out = {"aux": "q 0,1 deg [3,3]", "chi": FZ2_CHI, "iterations": FZ2_ITERS}
+    model = None
+
+    def chosen_ctm(chi, form):
+        c = CTM(A, chi).init()
+        if form == "chosen":
+            c.set_svd("randomized", power_iters=POWER_ITERS, seed=SEED, oversample=16, growth=0.5)
+        elif form == "learned":
+            c.set_rank_model(model, margin=0.0, min_oversample=2, power_iters=POWER_ITERS, seed=SEED)
+        if form != "plain":
+            c.set_sketch_unseen(True)
+            c.set_sketch_precision(args.sketch_tail)
+            c.set_gemm(args.gemm)
+        return c
+
+    for form in ("chosen", "learned"):
+        c = chosen_ctm(FZ2_CHI, form)
+        if form == "chosen":
+            c.record(True)
+        ms = []
+        for _ in range(FZ2_ITERS):
+            L.xgb_synchronize()
+            L.xgb_event_record(12)
+            c.grow_all()
+            L.xgb_event_record(13)
+            ms.append(L.xgb_event_elapsed_ms(12, 13))
+        out[form] = {"total_s": sum(ms) / 1e3, "ms_per_step_after_1": float(np.mean(ms[1:])),
+                     "nn_bond_last": energy(c, H)}
+        if form == "chosen":
+            X, T = dataset(c.records())
+            model = RankModel(seed=SEED)
+            model.train(X, T, steps=2000, lr=2e-3)
+            out["learned_train_samples"] = int(X.shape[0])
+        del c
+    nn = {}
+    for form in ("chosen", "plain"):
+        c = chosen_ctm(FZ2_CHI_SMALL, form)
+        t0 = time.perf_counter()
+        for _ in range(FZ2_ITERS):
+            c.grow_all()
+        L.xgb_synchronize()
+        nn[form] = (energy(c, H), time.perf_counter() - t0)
+        del c
+    out["equal_energy_check"] = {"chi": FZ2_CHI_SMALL, "iterations": FZ2_ITERS, "nn_bond_chosen": nn["chosen"][0],
+                                 "nn_bond_plain": nn["plain"][0], "abs_diff": abs(nn["chosen"][0] - nn["plain"][0]),
+                                 "wall_s_chosen": nn["chosen"][1], "wall_s_plain": nn["plain"][1]}
+    return out
 
 
 # ----------------------------------------------------------------------------- fermionic Z2 workload
@@ -419,7 +575,8 @@ def run_fz2(args):
 
 # ----------------------------------------------------------------------------- block-GEMM sweep
 def gemm_sweep(reps=5):
-    """Grouped block GEMMs FP64 vs 3xTF32 vs BF16x9 vs FP32 (CUDA cores): (i) the sector GEMMs of an SU(2)
+    """Grouped block GEMMs FP64 vs 3xTF32 vs BF16x9 vs FP32 (CUDA cores) vs F64TC (FP64-accurate, exact BF16
+    slices on the tensor cores): (i) the sector GEMMs of an SU(2)
     Tensor<2,2> product (irreps q = 2j+1, j = 0..3 integer, multiplicities 1-24);
     (ii) synthetic lists of G blocks, m, n, k log-uniform in [8, 512].  Useful
     TFLOP/s = sum 2mnk / time; error = max over blocks of ||C - C_fp64||_F / ||C_fp64||_F."""
@@ -453,7 +610,7 @@ def gemm_sweep(reps=5):
     flops = sum(2.0 * d.m * d.n * d.k for d in descs)
     res = {}
     ref = None
-    for form in ("fp64", "3xtf32", "bf16x9", "fp32"):
+    for form in ("fp64", "3xtf32", "bf16x9", "fp32", "f64tc"):
         set_gemm_precision(form)
         ms = timed(lambda: T1.matmul(T2))
         Cm = T1.matmul(T2)
@@ -489,7 +646,7 @@ def gemm_sweep(reps=5):
             L.xgb_memcpy_h2d(p_, h.ctypes.data, h.nbytes)
         res = {}
         ref = None
-        for prec, form in ((0, "fp64"), (1, "3xtf32"), (2, "bf16x9"), (3, "fp32")):
+        for prec, form in ((0, "fp64"), (1, "3xtf32"), (2, "bf16x9"), (3, "fp32"), (4, "f64tc")):
             ms = timed(lambda: L.xgb_grouped_gemm(prec, G, arr, bufs[0], bufs[1], bufs[2], 1.0, 0.0, None))
             check(L.xgb_gemm_tc_status(), "tensor-core gemm")
             h = np.empty(int(co))
@@ -832,6 +989,14 @@ def roofline(prof, steps, fp64_peak=None):
                "peak_source": ("cuBLAS DGEMM 4096^3 (torch.matmul FP64) measured on this GPU in this run; nominal "
                                "1.25" if fp64_peak else "nominal GB300 FP64 rate (no FP64 figure measured)"),
                "work": "thin R-SVD flops 6mn^2+20n^3" if dom == "svd_jacobi" else "useful flops"}
+    elif dom == "gemm_f64tc":
+        # FP64-accurate form: each useful FP64 multiply-add is 28 BF16 slice products on the tensor pipe
+        bf = peaks.get("bf16_tflops", 1900.0)
+        useful = per_launch_work / (per_launch_ms * 1e-3) / 1e12
+        out = {"bound": "tensor", "kernel": dom, "achieved": 28.0 * useful, "peak": bf, "unit": "TFLOP/s",
+               "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if "bf16_tflops" in peaks else "fallback 1900",
+               "work": "BF16 products issued: 28 slice products per useful FP64 flop (slicing launches included)",
+               "useful_fp64_equivalent_tflops": useful}
     elif dom == "gemm_tc":
         tf = peaks.get("bf16_tflops", 1900.0) / 2.0  # dense TF32 issues at half the BF16 rate
         achieved = per_launch_work / (per_launch_ms * 1e-3) / 1e12
@@ -891,15 +1056,15 @@ def time_moves(c, n_moves):
 
 
 def cpu_baseline_from_device(ctm):
-    """One move of the oracle port on a host copy of the device environment
+    """One whole grow_all step (four moves) of the oracle port on a host copy of the device environment
     (saturated chi), all host cores."""
     import oracle
     from oracle.convert import ctm_from_native
     oc = ctm_from_native(oracle.make_symmetry("u1"), ctm, CHI)
-    t = time_moves(oc, 1)[0]
-    return {"value": 1.0 / (4.0 * t), "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"one left move ({t:.1f} s) of the numpy/OpenBLAS oracle on a host copy of the saturated "
-                      "device environment; step time counted as four moves"}
+    t = float(sum(time_moves(oc, 4)))
+    return {"value": 1.0 / t, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"one grow_all step (L, R, T, B moves, {t:.1f} s) of the numpy/OpenBLAS oracle on a host copy "
+                      "of the saturated device environment"}
 
 
 def main():
@@ -908,13 +1073,22 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--gemm", default="fp64", choices=["fp64", "3xtf32", "fp32"])
+    ap.add_argument("--gemm", default="fp64", choices=["fp64", "3xtf32", "fp32", "f64tc"],
+                    help="block GEMM form of the chosen CTM step; f64tc (FP64-accurate tensor-core products from "
+                         "exact BF16 slices) also covers the projector and sketch products")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sketch-tail", type=int, default=SKETCH_TAIL,
                     help="subspace iterations of the chosen form kept in FP64 at the end; the earlier ones "
                          "(and the first sketch product) multiply as 3xTF32 tensor-core GEMMs (< 0: all FP64)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-width run")
+    ap.add_argument("--no-converge", action="store_true", help="skip the runs to convergence (CTMSolver::solve)")
+    ap.add_argument("--autotune", type=int, default=1, choices=[0, 1],
+                    help="1: FP64 GEMM shapes from the library's autotuner (tuned during the warm-up); 0: built-in rule")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the compact learned-tSVD sweep and fermionic Z2 runs folded into the default run")
+    ap.add_argument("--tol-e", type=float, default=1e-10, help="energy tolerance of the solver (reference default)")
+    ap.add_argument("--solve-max-steps", type=int, default=60, help="grow_all steps the solver may take")
     ap.add_argument("--workload", default="u1", choices=["u1", "fz2"],
                     help="u1: the headline U(1) D=6 chi=128 step; fz2: fermionic Z2 D=6 chi=144, 20 iterations")
     ap.add_argument("--fz2-plain-steps", type=int, default=2,
@@ -924,6 +1098,10 @@ def main():
     ap.add_argument("--u1-product", default=None, metavar="DEGS",
                     help="time only T1*T2 of U(1) Tensor<2,2> operands with these leg degeneracies (e.g. 6,12,16,12,6)")
     ap.add_argument("--reps", type=int, default=10, help="products timed by --u1-product")
+    ap.add_argument("--permute-only", action="store_true",
+                    help="run only the permute HBM roofline case (1.42 GB U(1) Tensor<2,2>) and print it")
+    ap.add_argument("--permute-degs", default="20,40,60,40,20",
+                    help="leg degeneracies of the permute case (charges -2..2), e.g. 10,20,30,20,10 for profiling")
     ap.add_argument("--tsvd-sweep-only", action="store_true",
                     help="run only the learned-width randomized tSVD sweep on power-law block matrices")
     args = ap.parse_args()
@@ -936,20 +1114,29 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
+        # one CPU step of this workload takes ~20 s on the GPU host's cores, so the K requested steps are
+        # sampled as ceil(K / 4) whole grow_all steps after min(W, 2) warm-up steps (chi saturates
+        # after the first step): ms_per_step x steps is the timed CPU work
         c = oracle_ctm(AUX, CHI)
-        for _ in range(args.warmup):
+        warm = min(args.warmup, 2)
+        for _ in range(warm):
             c.grow_all()
-        times = time_moves(c, args.steps)
-        t = 4.0 * float(np.mean(times))
+        n_steps = max(1, (args.steps + 3) // 4)
+        times = []
+        for _ in range(n_steps):
+            t0 = time.perf_counter()
+            c.grow_all()
+            times.append(time.perf_counter() - t0)
+        t = float(np.mean(times))
         v = 1.0 / t
-        line = {"metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus, "steps": len(times),
-                "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        line = {"metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus, "steps": n_steps,
+                "warmup": warm, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded N(0,1) site tensor)",
                 "config": dict(config, form="reference algorithm (exact FP64 tSVD), numpy/OpenBLAS"),
                 "impl": "reference",
                 "cpu_baseline": {"value": v, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-                                 "sample": f"{len(times)} single moves (L, R, T, B in turn) after {args.warmup} "
-                                           "warm-up steps; step time counted as four moves"},
+                                 "sample": f"{n_steps} whole grow_all steps (ceil(K/4) of the K = {args.steps} "
+                                           f"requested) after {warm} warm-up steps"},
                 "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -964,6 +1151,12 @@ def main():
         ensure_device(local)
         print(json.dumps({"u1_product": u1_product([int(x) for x in args.u1_product.split(",")], args.reps,
                                                      args.gemm)}))
+        return
+
+    if args.permute_only:
+        from xped_gb300 import ensure_device
+        ensure_device(local)
+        print(json.dumps({"permute_roofline": permute_roofline(tuple(int(x) for x in args.permute_degs.split(",")))}))
         return
 
     if args.tsvd_sweep_only:
@@ -990,7 +1183,7 @@ def main():
         return
     value = world * 1e3 / t_step
     prof = r["prof"]
-    gemm_kind = {"3xtf32": "gemm_tc", "fp32": "gemm_f32"}.get(args.gemm, "gemm_f64")
+    gemm_kind = {"3xtf32": "gemm_tc", "fp32": "gemm_f32", "f64tc": "gemm_f64tc"}.get(args.gemm, "gemm_f64")
     g = prof.get(gemm_kind, (0, 0.0, 0.0))
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
@@ -1010,6 +1203,7 @@ def main():
             "block_gemm": {"form": args.gemm, "tflops": (g[2] / (g[1] * 1e-3) / 1e12) if g[1] > 0 else None,
                            "ms_per_step": g[1] / r["prof_steps"]},
             "sketch": dict(r["sketch"], cols_per_step=r["cols_per_step"], redo_per_step=r["redo_per_step"]),
+            "autotune": r["autotune"] if args.autotune else {"enabled": False},
             "step_ms_each": [round(x, 3) for x in r["step_ms_all"]]}
     if "plain_ms" in r:
         line["plain_fp64"] = {"ms_per_step": r["plain_ms"], "steps_per_s": 1e3 / r["plain_ms"],
@@ -1020,6 +1214,24 @@ def main():
                           "observable": "Heisenberg energy per site (rho_h + rho_v bonds)"}
     else:
         line["energy"] = {"after_steps": COMPARE_STEPS, "chosen": r["e_chosen"]}
+    conv = {}
+    for form in ("chosen", "plain", "learned"):
+        if f"solve_{form}" in r:
+            conv[form] = r[f"solve_{form}"]
+    if conv:
+        # this workload's converged CTM energy alternates between two values from step to step (a
+        # period-2 environment): each form's last two energies are its two branches, compared branch
+        # by branch (the solver may stop on either branch)
+        for form, c in conv.items():
+            c["branches"] = sorted(c["energies"][-2:])
+        line["energy_converged"] = dict(conv, observable="Heisenberg energy per site (rho_h + rho_v bonds)",
+                                        rule="CTMSolver::solve: stop when |E - E_prev| < tol_E or |E - E_prevprev| < tol_E",
+                                        comparison="largest difference between the sorted last-two-step energies")
+        if "plain" in conv:
+            for form in ("chosen", "learned"):
+                if form in conv:
+                    line["energy_converged"][f"abs_diff_{form}_vs_plain"] = max(
+                        abs(a - b) for a, b in zip(conv[form]["branches"], conv["plain"]["branches"]))
     if "learned_ms" in r:
         line["learned_widths"] = {"ms_per_step": r["learned_ms"], "steps_per_s": 1e3 / r["learned_ms"],
                                   "sketch_cols_per_step": r["learned_cols_per_step"],
@@ -1030,6 +1242,11 @@ def main():
     line["block_gemm_sweep"] = r["gemm_sweep"]
     line["tensor22_chain"] = r["tensor22_chain"]
     line["simple_update_step"] = r["su"]
+    line["permute_roofline"] = r["permute_roofline"]
+    if "tsvd_sweep" in r:
+        line["learned_tsvd_sweep"] = r["tsvd_sweep"]
+    if "fz2" in r:
+        line["fermionic_z2_chosen_form"] = r["fz2"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_from_device(r["ctm"])
     print(json.dumps(line))

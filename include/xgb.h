@@ -53,7 +53,7 @@ enum {
 };
 
 /* precision forms of the block GEMM */
-enum { XGB_PREC_FP64 = 0, XGB_PREC_3XTF32 = 1, XGB_PREC_BF16X9 = 2, XGB_PREC_FP32 = 3 };
+enum { XGB_PREC_FP64 = 0, XGB_PREC_3XTF32 = 1, XGB_PREC_BF16X9 = 2, XGB_PREC_FP32 = 3, XGB_PREC_F64TC = 4 };
 
 /* ---------------------------------------------------------------- runtime */
 int xgb_init(int device);
@@ -72,7 +72,8 @@ void* xgb_stream_handle(void);
 /* Instrumentation: with profiling enabled every launch is bracketed by CUDA
    events on the library stream.  kind: 0 gemm, 1 permute, 2 svd, 3 truncate,
    4 qr, 5 absmax, 6 scale, 7 copy2d, 8 diag, 9 tensor-core gemm, 10 sketch
-   (Gaussian test matrices, sign fixing), 11 rank-predictor MLP.  work is the
+   (Gaussian test matrices, sign fixing), 11 rank-predictor MLP, 12 FP32 gemm,
+   13 FP64-accurate tensor-core gemm (slicing and product launches).  work is the
    algorithmic flop count (GEMMs) or bytes moved (everything else). */
 int xgb_profile_enable(int on);
 int xgb_profile_reset(void);
@@ -97,7 +98,12 @@ typedef struct xgb_gemm_desc {
    FP32 and FP32 accumulation on the CUDA cores (about 1e-7 relative per product,
    growing with k); XGB_PREC_BF16X9: FP64 in and out, every operand split into three BF16 pieces
    (24 significant bits) and all nine piece products accumulated in FP32 on the tensor cores
-   (tcgen05.mma kind::f16; about 1e-6 relative, like 3xTF32). */
+   (tcgen05.mma kind::f16; about 1e-6 relative, like 3xTF32); XGB_PREC_F64TC: FP64 in and out,
+   every op(A) row / op(B) column scaled by a power of two above its largest entry and cut into
+   seven exact 7-bit BF16 slices; the 28 slice products of significance s + t <= 8 are summed
+   exactly in FP32 tensor memory over 128-deep k chunks (Ozaki, Ogita, Oishi, Rump 2012) and the
+   chunks in double-FP32 registers: the error is of the order of FP64 rounding (about 1e-15 of
+   max|a| max|b| k per element). */
 int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, const double* A, const double* B,
                      double* C, double alpha, double beta, void* stream);
 /* Tile-shape autotuner of the FP64 grouped GEMM (no counterpart in the reference, whose

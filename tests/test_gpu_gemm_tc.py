@@ -164,3 +164,76 @@ def test_fp32_form_through_the_tensor_api():
         set_gemm_precision("fp64")
     err = max(np.linalg.norm(got[q] - ref[q]) / np.linalg.norm(ref[q]) for q in ref)
     assert 0.0 < err < 2e-5
+
+
+PREC_F64TC = 4
+
+
+def test_f64tc_ragged_blocks_and_transposes():
+    """FP64-accurate form from exact BF16 slices on ragged blocks of every transpose: relative error within
+    3e-13 (measured ~5e-14; FP64 GEMM ~1e-15, 3xTF32 ~3e-7)."""
+    rng = np.random.default_rng(21)
+    blocks = [(int(m), int(n), int(k), int(ta), int(tb)) for (m, n, k), ta, tb in
+              zip(rng.integers(1, 300, size=(10, 3)), rng.integers(0, 2, 10), rng.integers(0, 2, 10))]
+    err = _run(blocks, seed=21, prec=PREC_F64TC)
+    print("f64tc ragged relative error", err)
+    assert err < 3e-13
+
+
+def test_f64tc_long_k_and_alpha_beta():
+    err = _run([(256, 192, 3072, 0, 0), (130, 70, 2000, 1, 0), (33, 17, 0, 0, 0)], alpha=-0.5, beta=2.0, seed=22,
+               prec=PREC_F64TC)
+    print("f64tc long-k relative error", err)
+    assert err < 3e-13
+
+
+def test_f64tc_graded_rows_against_the_slice_error_bound():
+    """Entries spanning twelve decades within each row and column: every element within the scheme's
+    bound 4 k 2^-49 max_k|a_ik| max_k|b_kj| (the slices are taken relative to each row's and column's
+    largest entry, so small entries of a graded row carry the row's absolute precision)."""
+    from xped_gb300 import ensure_device, lib
+    from xped_gb300._lib import GemmDesc, last_error
+    ensure_device(0)
+    L = lib()
+    rng = np.random.default_rng(23)
+    m, n, k = 150, 90, 700
+    A = rng.standard_normal((m, k)) * 10.0 ** rng.uniform(-12, 0, size=(m, k))
+    B = rng.standard_normal((k, n)) * 10.0 ** rng.uniform(-12, 0, size=(k, n))
+    ptrs = []
+    for h in (A.ravel(order="F"), B.ravel(order="F"), np.zeros(m * n)):
+        p = C.c_void_p()
+        assert L.xgb_malloc(C.byref(p), h.nbytes) == 0
+        assert L.xgb_memcpy_h2d(p, h.ctypes.data, h.nbytes) == 0
+        ptrs.append(p)
+    arr = (GemmDesc * 1)(GemmDesc(m, n, k, 0, m, 0, k, 0, m, 0, 0))
+    assert L.xgb_grouped_gemm(PREC_F64TC, 1, arr, ptrs[0], ptrs[1], ptrs[2], 1.0, 0.0, None) == 0, last_error()
+    assert L.xgb_gemm_tc_status() == 0, last_error()
+    got = np.empty(m * n)
+    assert L.xgb_memcpy_d2h(got.ctypes.data, ptrs[2], got.nbytes) == 0
+    for p in ptrs:
+        L.xgb_free(p)
+    got = got.reshape((m, n), order="F")
+    bound = 4.0 * k * 2.0 ** -49 * np.outer(np.abs(A).max(axis=1), np.abs(B).max(axis=0))
+    ratio = float((np.abs(got - A @ B) / bound).max())
+    print("f64tc graded: largest error / (4 k 2^-49 max|a_i| max|b_j|)", ratio)
+    assert ratio < 1.0
+
+
+def test_f64tc_through_the_tensor_api():
+    from xped_gb300 import Basis, Tensor, ensure_device
+    from xped_gb300.tensor import set_gemm_precision
+    ensure_device(0)
+    rng = np.random.default_rng(24)
+    B = Basis.from_pairs("U1", [(-2, 3), (-1, 9), (0, 14), (1, 9), (2, 3)])
+    T1, T2 = Tensor.zeros([B, B], [B, B]), Tensor.zeros([B, B], [B, B])
+    T1.set_data(rng.standard_normal(T1.size))
+    T2.set_data(rng.standard_normal(T2.size))
+    ref = T1.matmul(T2).data()
+    set_gemm_precision("f64tc")
+    try:
+        got = T1.matmul(T2).data()
+    finally:
+        set_gemm_precision("fp64")
+    err = float(np.abs(got - ref).max() / np.abs(ref).max())
+    print("f64tc tensor api max relative error", err)
+    assert err < 3e-13

@@ -64,8 +64,10 @@ def test_bases_and_trees(symname, pB, pC):
 def emulate_permute(tasks, contribs, src, n_out, sms=152):
     """The index arithmetic of permute_rows_kernel: rows along output leg 0 (row_start prefix
     sums, group size G from the element-weighted row length as perm_rows computes it), the
-    launch grid of launch_permute, group g taking rows g, g + ngroups, ... and lane l the row
-    elements l, l + G, ...; every source and destination index is checked against its buffer."""
+    launch grid of launch_permute, chunks of 8 consecutive rows per group (the first row decoded,
+    the next ones stepped like an odometer, leg 1 fastest) and lane l taking row elements l, l + G,
+    ...; every source and destination index is checked against its buffer and every output
+    element is written at most once."""
     n = len(tasks)
     row_start = [0]
     elems = weighted = 0.0
@@ -82,37 +84,73 @@ def emulate_permute(tasks, contribs, src, n_out, sms=152):
     dst = np.zeros(n_out)
     if total_rows == 0:
         return dst
+    RPC = 8
     per_block = 256 // G
-    blocks = max(1, min(sms * 16, ((total_rows + 3) // 4 + per_block - 1) // per_block))
+    blocks = max(1, min(sms * 16, ((total_rows + RPC - 1) // RPC + per_block - 1) // per_block))
     ngroups = blocks * 256 // G
+    nchunks = (total_rows + RPC - 1) // RPC
     seen = np.zeros(n_out, dtype=np.int64)
-    for r in range(total_rows):
-        g = r % ngroups  # the group that owns row r
-        assert 0 <= g < ngroups
+
+    def seek(r):
         ti = int(np.searchsorted(row_start, r, side="right") - 1)
         assert 0 <= ti < n and row_start[ti] <= r < row_start[ti + 1]
         t = tasks[ti]
-        d0 = t.dims[0] if t.rank > 0 else 1
         rem = r - row_start[ti]
-        idx = [0]
+        idx = [0] * 8
+        dofs = t.dst_base
+        single = t.n_contrib == 1
+        sofs = contribs[t.contrib0].src_base if single else 0
         for k in range(1, t.rank):
-            idx.append(rem % t.dims[k])
+            idx[k] = rem % t.dims[k]
             rem //= t.dims[k]
-        assert rem == 0
-        dofs = t.dst_base + sum(i * t.dst_stride[k] for k, i in enumerate(idx) if k > 0)
-        ds0 = t.dst_stride[0] if t.rank > 0 else 0
-        for lane in range(G):
-            for i in range(lane, d0, G):
-                v = 0.0
-                for c in contribs[t.contrib0:t.contrib0 + t.n_contrib]:
-                    so = c.src_base + i * (c.src_stride[0] if t.rank > 0 else 0)
-                    so += sum(x * c.src_stride[k] for k, x in enumerate(idx) if k > 0)
-                    assert 0 <= so < len(src)
-                    v += c.coeff * src[so]
-                do = dofs + i * ds0
-                assert 0 <= do < n_out
-                dst[do] = v
-                seen[do] += 1
+            dofs += idx[k] * t.dst_stride[k]
+            if single:
+                sofs += idx[k] * contribs[t.contrib0].src_stride[k]
+        return {"ti": ti, "end": row_start[ti + 1], "idx": idx, "dofs": dofs, "sofs": sofs}
+
+    def step(c, t, cc):
+        for k in range(1, t.rank):
+            c["dofs"] += t.dst_stride[k]
+            if cc is not None:
+                c["sofs"] += cc.src_stride[k]
+            c["idx"][k] += 1
+            if c["idx"][k] < t.dims[k]:
+                return
+            c["idx"][k] = 0
+            c["dofs"] -= t.dims[k] * t.dst_stride[k]
+            if cc is not None:
+                c["sofs"] -= t.dims[k] * cc.src_stride[k]
+
+    for chunk in range(nchunks):
+        assert chunk % ngroups < ngroups  # owned by group chunk mod ngroups
+        r0, r1 = chunk * RPC, min(chunk * RPC + RPC, total_rows)
+        cur = seek(r0)
+        for r in range(r0, r1):
+            if r >= cur["end"]:
+                cur = seek(r)
+            t = tasks[cur["ti"]]
+            d0 = t.dims[0] if t.rank > 0 else 1
+            ds0 = t.dst_stride[0] if t.rank > 0 else 0
+            single = t.n_contrib == 1
+            for lane in range(G):
+                for i in range(lane, d0, G):
+                    if single:
+                        cc = contribs[t.contrib0]
+                        so = cur["sofs"] + i * (cc.src_stride[0] if t.rank > 0 else 0)
+                        assert 0 <= so < len(src)
+                        v = cc.coeff * src[so]
+                    else:
+                        v = 0.0
+                        for cc in contribs[t.contrib0:t.contrib0 + t.n_contrib]:
+                            so = cc.src_base + i * (cc.src_stride[0] if t.rank > 0 else 0)
+                            so += sum(cur["idx"][k] * cc.src_stride[k] for k in range(1, t.rank))
+                            assert 0 <= so < len(src)
+                            v += cc.coeff * src[so]
+                    do = cur["dofs"] + i * ds0
+                    assert 0 <= do < n_out
+                    dst[do] = v
+                    seen[do] += 1
+            step(cur, t, contribs[t.contrib0] if single else None)
     assert seen.max() <= 1  # tasks tile disjoint regions of the output
     return dst
 

@@ -241,7 +241,7 @@ PROTOS_EXTRA = [
 ]
 PROTOS.extend(PROTOS_EXTRA)
 
-KERNEL_KINDS = ["gemm_f64", "permute", "svd_jacobi", "truncate", "qr", "absmax", "scale", "copy2d", "diag", "gemm_tc", "sketch", "mlp", "gemm_f32"]
+KERNEL_KINDS = ["gemm_f64", "permute", "svd_jacobi", "truncate", "qr", "absmax", "scale", "copy2d", "diag", "gemm_tc", "sketch", "mlp", "gemm_f32", "gemm_f64tc"]
 
 
 def profile_read():

@@ -22,7 +22,7 @@ CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["kernels.cu", "svd.cu", "gemm_tc.cu", "rsvd.cu", "mlp.cu"]
+CU_SOURCES = ["kernels.cu", "svd.cu", "gemm_tc.cu", "gemm_oz.cu", "rsvd.cu", "mlp.cu"]
 CPP_SOURCES = ["meta.cpp", "tensor.cpp", "capi.cpp", "rsvd.cpp", "mlp.cpp", "checkpoint.cpp", "autotune.cpp"]
 
 

@@ -1,0 +1,491 @@
+// FP64-accurate grouped GEMM on the 5th-generation tensor cores from exact BF16 slices.
+//
+// C_g = alpha op(A_g) op(B_g) + beta C_g for FP64 column-major blocks.  Every row i of op(A) is
+// written relative to a power of two 2^e_i above its largest entry (taken over the whole k range)
+// and cut into seven 7-bit slices, a_ik = 2^e_i (sum_s m_s 2^(-7 s) + O(2^-50)) with integers
+// |m_s| <= 128; every column of op(B) likewise (2^f_j).  A slice m_s 2^(-7 s) is exact in BF16, the
+// product of two slices is exact in FP32, and all products of a "level" L = s + t share the unit
+// 2^(-7 L): a sum of at most 7 pairs x 128 k values x 2^14 stays below 2^24 and is exact in the
+// FP32 tensor-memory accumulator whatever order the tensor core adds in.  The row and column
+// scales 2^(e_i + f_j) are applied in FP64 when the tile is stored.  This is the slicing scheme of Ozaki,
+// Ogita, Oishi and Rump ("Error-free transformations of matrix multiplication by using fast
+// routines of matrix multiplication and its applications", Numer. Algorithms 59 (2012)), with BF16
+// tcgen05.mma as the fast routine.
+//
+// Kernels (one launch each, all groups of the list):
+//  * oz_rowmax_kernel: per 128-row (A) / 64-row (B) x 32-K chunk, the largest |entry| of every row
+//    into a max over the whole k range (atomicMax on the IEEE bits of a non-negative double);
+//  * oz_pack_kernel: the seven slices of every chunk as BF16 in the K-major, unswizzled canonical
+//    layout the MMA reads (8-row x 16-byte core matrices), zero padded past the block edges; the
+//    slices come from integer arithmetic on the FP64 significand (|x| rounded to 49 bits below the
+//    row's scale, every slice with the sign of its entry);
+//  * oz_gemm_kernel: one CTA (10 warps) per 128 x 64 output tile.  Warp 8 streams the slices of each
+//    32-wide K slice of the tile's rows and columns into a 2-stage shared-memory ring (84 KB per
+//    stage, bulk copies counted on mbarriers); warp 9 issues, per 16-deep k step, the 28 BF16 MMAs of
+//    the slice pairs with s + t <= 8 into seven 64-column TMEM accumulators (one per level, 448 of
+//    512 columns); after every four K slices (the exactness bound) warps 0-7 read the seven levels
+//    and add them into double-FP32 (hi + lo) register sums, then the next four slices start from
+//    zero.  The slice rounding (2^-50 of the row / column scale), the dropped pairs (s + t > 8) and
+//    the double-FP32 sums bound the error of an element by a small multiple of
+//    2^-49 k max_k |a_ik| max_k |b_kj|: about 5e-14 of ||C|| for Gaussian blocks, against ~1e-15 for an
+//    FP64 dot product and ~3e-7 for 3xTF32.
+//
+// Every mbarrier wait is bounded; on timeout the CTA records an error flag (shared with the 3xTF32
+// kernel, xgb_gemm_tc_status), skips the epilogue and still frees its TMEM.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.hpp"
+
+namespace xgb {
+namespace {
+
+constexpr int OM = 128, ON = 64, OK = 32;          // output tile rows / columns, K per slice
+constexpr int kPieces = 7, kBits = 7;               // seven 7-bit slices per entry
+constexpr int kLevels = kPieces;                    // levels s + t = 2 .. 8 (1-based slices)
+constexpr int kChunk = 4;                           // K slices per exact TMEM accumulation (7 x 128 x 2^14 < 2^24)
+constexpr int kAPieceBytes = OM * OK * 2;           // 8 KB
+constexpr int kBPieceBytes = ON * OK * 2;           // 4 KB
+constexpr int kOzStageBytes = kPieces * (kAPieceBytes + kBPieceBytes);  // 84 KB
+constexpr int kOzStages = 2;
+constexpr int kOzSmem = kOzStages * kOzStageBytes + 1024;
+constexpr uint32_t kOzTmemCols = 512;               // 7 levels x 64 columns used
+constexpr int kOzWarps = 10, kOzThreads = kOzWarps * 32;
+constexpr int kOzProducer = 8, kOzMma = 9, kOzDrainWarps = 8;
+constexpr long long kOzSpin = 1ll << 26;
+constexpr uint32_t kSboBytes = 128;                 // next 8-row group
+constexpr uint32_t kLboA = (OM / 8) * 128;          // next 16-byte K group, 128-row pieces
+constexpr uint32_t kLboB = (ON / 8) * 128;          // 64-row pieces
+static_assert(kLevels * ON <= int(kOzTmemCols), "level accumulators fit TMEM");
+static_assert(kOzSmem <= 227 * 1024, "stages fit shared memory");
+
+__device__ __forceinline__ uint32_t s_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ uint64_t oz_desc(uint32_t saddr, uint32_t lbo) {
+  uint64_t d = 0;
+  d |= uint64_t((saddr >> 4) & 0x3FFF);
+  d |= uint64_t((lbo >> 4) & 0x3FFF) << 16;
+  d |= uint64_t((kSboBytes >> 4) & 0x3FFF) << 32;
+  d |= uint64_t(1) << 46;  // tcgen05 descriptor version; base offset 0, no swizzle
+  return d;
+}
+
+// FP32 accumulate, BF16 A and B (kind::f16), both K-major, N = 64, M = 128
+constexpr uint32_t kOzIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(ON >> 3) << 17) | (uint32_t(OM >> 4) << 24);
+
+__device__ __forceinline__ void bar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = s_u32(bar);
+  for (long long it = 0; it < kOzSpin; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void bar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(s_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(s_u32(dst_smem)),
+      "l"(src_gmem), "r"(bytes), "r"(s_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16_oz(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(kOzIdesc), "r"(acc));
+}
+
+__device__ __forceinline__ void commit_to(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(s_u32(bar))
+               : "memory");
+}
+
+// ----------------------------------------------------------------------------- row scales
+// task: (group, tile of OM rows of op(A) or ON rows of op(B)^T, K slice, which)
+__global__ void __launch_bounds__(256) oz_rowmax_kernel(const xgb_gemm_desc* __restrict__ descs,
+                                                         const OzGroup* __restrict__ groups,
+                                                         const TcPackTask* __restrict__ tasks,
+                                                         const double* __restrict__ A, const double* __restrict__ B,
+                                                         unsigned long long* __restrict__ rowmax) {
+  __shared__ double X[OM][OK + 1];
+  const TcPackTask t = tasks[blockIdx.x];
+  const xgb_gemm_desc d = descs[t.g];
+  const OzGroup gr = groups[t.g];
+  const bool isB = t.which != 0;
+  const double* src = isB ? B : A;
+  const int64_t off = isB ? d.b_off : d.a_off, ld = isB ? d.ldb : d.lda;
+  const int64_t rows = isB ? d.n : d.m;
+  const int tr = isB ? ON : OM;
+  const bool rowfast = isB ? d.trans_b != 0 : d.trans_a == 0;
+  const int64_t r0 = int64_t(t.tile) * tr, k0 = int64_t(t.slice) * OK;
+  for (int e = threadIdx.x; e < tr * OK; e += 256) {
+    int r, k;
+    if (rowfast) { r = e % tr; k = e / tr; } else { k = e % OK; r = e / OK; }
+    const int64_t gr_ = r0 + r, gk = k0 + k;
+    double x = 0.0;
+    if (gr_ < rows && gk < d.k) x = rowfast ? src[off + gr_ + gk * ld] : src[off + gk + gr_ * ld];
+    X[r][k] = fabs(x);
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < tr; r += 256) {
+    if (r0 + r >= rows) continue;
+    double m = 0.0;
+    for (int k = 0; k < OK; ++k) m = fmax(m, X[r][k]);
+    unsigned long long* slot = rowmax + (isB ? gr.b_rowmax : gr.a_rowmax) + r0 + r;
+    atomicMax(slot, static_cast<unsigned long long>(__double_as_longlong(m)));
+  }
+}
+
+// exponent e with |x| < 2^e for every entry of the row (0 for an all-zero row)
+__device__ __forceinline__ int row_scale(unsigned long long bits) {
+  const double m = __longlong_as_double(static_cast<long long>(bits));
+  if (!(m > 0.0)) return 0;
+  int e;
+  frexp(m, &e);  // m = f 2^e, f in [0.5, 1)
+  return e;
+}
+
+// seven 7-bit slices of x relative to 2^e (|x| < 2^e): x = 2^e sum_s sign * m_s * 2^(-7 s) + O(2^(e - 50)),
+// 0 <= m_s <= 127 (the leading digit <= 128)
+__device__ __forceinline__ void slice7(double x, int e, float* out) {
+  const long long bits = __double_as_longlong(x);
+  const int ex = int((bits >> 52) & 0x7FF);
+  const bool neg = bits < 0;
+  unsigned long long q = 0;
+  if (ex != 0) {  // normal numbers (subnormals are below every slice of any realistic row)
+    const unsigned long long mant = (static_cast<unsigned long long>(bits) & ((1ull << 52) - 1)) | (1ull << 52);
+    // x = mant 2^(ex - 1075); |x| rounded to the nearest multiple of 2^(e - 49) (ties up): shift right
+    // by sh = e - 49 - (ex - 1075) >= 4 (|x| < 2^e) with one guard bit; q <= 2^49
+    const int sh = e - 49 - (ex - 1075);
+    q = sh >= 64 ? 0ull : (((mant >> (sh - 1)) + 1ull) >> 1);
+  }
+#pragma unroll
+  for (int s = 1; s <= kPieces; ++s) {
+    // 7-bit digits of q; the leading one may reach 128 (q = 2^49), still exact in BF16
+    const int m = s == 1 ? int(q >> (49 - kBits)) : int((q >> (49 - kBits * s)) & ((1u << kBits) - 1));
+    const float v = ldexpf(float(m), -kBits * s);
+    out[s - 1] = neg ? -v : v;
+  }
+}
+
+__global__ void __launch_bounds__(256) oz_pack_kernel(const xgb_gemm_desc* __restrict__ descs,
+                                                       const OzGroup* __restrict__ groups,
+                                                       const TcPackTask* __restrict__ tasks,
+                                                       const double* __restrict__ A, const double* __restrict__ B,
+                                                       const unsigned long long* __restrict__ rowmax,
+                                                       unsigned char* __restrict__ apack,
+                                                       unsigned char* __restrict__ bpack) {
+  __shared__ double X[OM][OK + 1];
+  __shared__ int E[OM];
+  const TcPackTask t = tasks[blockIdx.x];
+  const xgb_gemm_desc d = descs[t.g];
+  const OzGroup gr = groups[t.g];
+  const bool isB = t.which != 0;
+  const double* src = isB ? B : A;
+  const int64_t off = isB ? d.b_off : d.a_off, ld = isB ? d.ldb : d.lda;
+  const int64_t rows = isB ? d.n : d.m;
+  const int tr = isB ? ON : OM;
+  const bool rowfast = isB ? d.trans_b != 0 : d.trans_a == 0;
+  const int64_t r0 = int64_t(t.tile) * tr, k0 = int64_t(t.slice) * OK;
+  for (int e = threadIdx.x; e < tr * OK; e += 256) {
+    int r, k;
+    if (rowfast) { r = e % tr; k = e / tr; } else { k = e % OK; r = e / OK; }
+    const int64_t gr_ = r0 + r, gk = k0 + k;
+    double x = 0.0;
+    if (gr_ < rows && gk < d.k) x = rowfast ? src[off + gr_ + gk * ld] : src[off + gk + gr_ * ld];
+    X[r][k] = x;
+  }
+  for (int r = threadIdx.x; r < tr; r += 256)
+    E[r] = (r0 + r < rows) ? row_scale(rowmax[(isB ? gr.b_rowmax : gr.a_rowmax) + r0 + r]) : 0;
+  __syncthreads();
+  // slice block of this (tile, K slice): kPieces pieces of tr x OK BF16, each in canonical layout
+  const int piece_bytes = isB ? kBPieceBytes : kAPieceBytes;
+  const uint32_t lbo = isB ? kLboB : kLboA;
+  unsigned char* base = (isB ? bpack + gr.b_pack : apack + gr.a_pack) +
+                        (int64_t(t.tile) * gr.slices + t.slice) * int64_t(kPieces) * piece_bytes;
+  for (int e = threadIdx.x; e < tr * (OK / 8); e += 256) {
+    const int r = e % tr, kq = e / tr;  // one 16-byte core-matrix row: 8 consecutive K of row r
+    __nv_bfloat16 pc[kPieces][8];
+#pragma unroll
+    for (int kk = 0; kk < 8; ++kk) {
+      float v[kPieces];
+      slice7(X[r][kq * 8 + kk], E[r], v);
+#pragma unroll
+      for (int s = 0; s < kPieces; ++s) pc[s][kk] = __float2bfloat16_rn(v[s]);  // exact: <= 7 significant bits
+    }
+    const uint32_t bo = uint32_t(kq) * lbo + uint32_t(r >> 3) * kSboBytes + uint32_t(r & 7) * 16;
+#pragma unroll
+    for (int s = 0; s < kPieces; ++s)
+      *reinterpret_cast<uint4*>(base + int64_t(s) * piece_bytes + bo) = *reinterpret_cast<const uint4*>(pc[s]);
+  }
+}
+
+// ----------------------------------------------------------------------------- gemm
+__global__ void __launch_bounds__(kOzThreads, 1)
+    oz_gemm_kernel(const xgb_gemm_desc* __restrict__ descs, const OzGroup* __restrict__ groups,
+                   const GemmTile* __restrict__ tiles, const unsigned char* __restrict__ apack,
+                   const unsigned char* __restrict__ bpack, const unsigned long long* __restrict__ rowmax,
+                   double* __restrict__ C, double alpha, double beta, int* __restrict__ err) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ uint64_t full[kOzStages], empty[kOzStages], accf, acce, done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int fail, issued, consumed;
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+
+  const GemmTile t = tiles[blockIdx.x];
+  const xgb_gemm_desc d = descs[t.g];
+  const OzGroup gr = groups[t.g];
+  const int64_t m0 = int64_t(t.tm) * OM, n0 = int64_t(t.tn) * ON;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nk = gr.slices;
+  const int nchunks = (nk + kChunk - 1) / kChunk;
+
+  if (warp == kOzMma) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s_u32(&tmem_slot)),
+                 "r"(kOzTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kOzStages; ++s) {
+      bar_init(&full[s], 1);
+      bar_init(&empty[s], 1);
+    }
+    bar_init(&accf, 1);
+    bar_init(&acce, kOzDrainWarps);
+    bar_init(&done, 1);
+    fail = 0;
+    issued = 0;
+    consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  // drain-warp state: TMEM lane quarter (rows) and 32-column group; double-FP32 sums of 32 columns
+  const int quarter = warp & 3, colg = warp >> 2;
+  float hi[32], lo[32];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) { hi[j] = 0.f; lo[j] = 0.f; }
+
+  if (nk > 0 && warp == kOzProducer) {
+    if (lane == 0) {
+      const unsigned char* a_base = apack + gr.a_pack + int64_t(t.tm) * gr.slices * kPieces * kAPieceBytes;
+      const unsigned char* b_base = bpack + gr.b_pack + int64_t(t.tn) * gr.slices * kPieces * kBPieceBytes;
+      uint32_t ph[kOzStages] = {0, 0};
+      for (int kc = 0; kc < nk; ++kc) {
+        const int s = kc % kOzStages;
+        if (kc >= kOzStages) {
+          if (!bar_wait(&empty[s], ph[s])) { atomicExch(&fail, 1); break; }
+          ph[s] ^= 1u;
+        }
+        unsigned char* st = smem + s * kOzStageBytes;
+        bar_expect_tx(&full[s], kOzStageBytes);
+        bulk_g2s(st, a_base + int64_t(kc) * kPieces * kAPieceBytes, kPieces * kAPieceBytes, &full[s]);
+        bulk_g2s(st + kPieces * kAPieceBytes, b_base + int64_t(kc) * kPieces * kBPieceBytes, kPieces * kBPieceBytes,
+                 &full[s]);
+        issued = kc + 1;
+      }
+    }
+  } else if (nk > 0 && warp == kOzMma) {
+    if (lane == 0) {
+      uint32_t ph[kOzStages] = {0, 0};
+      for (int kc = 0; kc < nk; ++kc) {
+        const int s = kc % kOzStages, cs = kc % kChunk, ch = kc / kChunk;
+        // a new chunk overwrites the level accumulators: the previous chunk must be drained
+        if (cs == 0 && ch > 0 && !bar_wait(&acce, uint32_t((ch - 1) & 1))) { atomicExch(&fail, 1); break; }
+        if (!bar_wait(&full[s], ph[s])) { atomicExch(&fail, 1); break; }
+        ph[s] ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t abase = s_u32(smem + s * kOzStageBytes);
+        const uint32_t bbase = abase + kPieces * kAPieceBytes;
+#pragma unroll
+        for (int kk = 0; kk < OK / 16; ++kk) {
+#pragma unroll
+          for (int i = 0; i < kPieces; ++i)
+#pragma unroll
+            for (int j = 0; j + i < kPieces; ++j) {
+              const int level = i + j;  // 0-based: slices i + 1 and j + 1
+              const uint32_t acc = (cs == 0 && kk == 0 && i == 0) ? 0u : 1u;  // first pair of each level
+              mma_bf16_oz(tmem + uint32_t(level * ON), oz_desc(abase + i * kAPieceBytes + kk * 2 * kLboA, kLboA),
+                          oz_desc(bbase + j * kBPieceBytes + kk * 2 * kLboB, kLboB), acc);
+            }
+        }
+        commit_to(&empty[s]);
+        if (cs == kChunk - 1 || kc == nk - 1) commit_to(&accf);
+        consumed = kc + 1;
+      }
+      commit_to(&done);
+    }
+  } else if (nk > 0 && warp < kOzDrainWarps) {
+    for (int ch = 0; ch < nchunks; ++ch) {
+      const bool got = __all_sync(0xffffffffu, bar_wait(&accf, uint32_t(ch & 1)));
+      if (!got) {
+        if (lane == 0) atomicExch(&fail, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+      for (int level = kLevels - 1; level >= 0; --level) {  // smallest contributions first
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          uint32_t v[8];
+          const uint32_t taddr =
+              tmem + (uint32_t(quarter * 32) << 16) + uint32_t(level * ON + colg * 32 + c * 8);
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                       : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                         "=r"(v[7])
+                       : "r"(taddr));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            // two-sum of hi and the exact level partial; the rounding error goes to lo
+            const float x = __uint_as_float(v[j]);
+            const float s = __fadd_rn(hi[c * 8 + j], x);
+            const float bb = __fsub_rn(s, hi[c * 8 + j]);
+            const float e = __fadd_rn(__fsub_rn(hi[c * 8 + j], __fsub_rn(s, bb)), __fsub_rn(x, bb));
+            hi[c * 8 + j] = s;
+            lo[c * 8 + j] = __fadd_rn(lo[c * 8 + j], e);
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {  // renormalise: |lo| stays below one unit of hi
+        const float s = __fadd_rn(hi[j], lo[j]);
+        lo[j] = __fsub_rn(lo[j], __fsub_rn(s, hi[j]));
+        hi[j] = s;
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(s_u32(&acce)) : "memory");
+    }
+  }
+  bool ok = true;
+  if (nk > 0) ok = bar_wait(&done, 0);
+  __syncthreads();
+  ok = ok && (fail == 0);
+  ok = __syncthreads_and(ok);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+  if (ok && nk > 0 && warp < kOzDrainWarps) {
+    const int64_t row = m0 + quarter * 32 + lane;
+    if (row < d.m) {
+      const int ei = row_scale(rowmax[gr.a_rowmax + row]);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int64_t col = n0 + colg * 32 + j;
+        if (col < d.n) {
+          double* cp = C + d.c_off + row + col * d.ldc;
+          const double acc = ldexp(double(hi[j]) + double(lo[j]), ei + row_scale(rowmax[gr.b_rowmax + col]));
+          *cp = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *cp);
+        }
+      }
+    }
+  } else if (ok && nk == 0) {
+    for (int e = threadIdx.x; e < OM * ON; e += kOzThreads) {
+      const int64_t row = m0 + e % OM, col = n0 + e / OM;
+      if (row < d.m && col < d.n) {
+        double* cp = C + d.c_off + row + col * d.ldc;
+        *cp = beta == 0.0 ? 0.0 : beta * *cp;
+      }
+    }
+  }
+  if (!ok && threadIdx.x == 0) {
+    atomicExch(err, 1);
+    for (int kc = consumed; kc < issued; ++kc) bar_wait(&full[kc % kOzStages], uint32_t((kc / kOzStages) & 1));
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == kOzMma)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kOzTmemCols));
+}
+
+bool g_oz_attr = false;
+
+}  // namespace
+
+OzPlanHost build_oz_plan(const xgb_gemm_desc* descs, int n) {
+  // rowmax layout: every group's op(A) rows first, then every group's op(B) columns, so that the
+  // B part can be cleared and recomputed alone when only B changes between products
+  OzPlanHost p;
+  for (int g = 0; g < n; ++g) p.rowmax_a += descs[g].m;
+  int64_t ra = 0, rb = p.rowmax_a;
+  for (int g = 0; g < n; ++g) {
+    const xgb_gemm_desc& d = descs[g];
+    OzGroup gr{};
+    gr.a_tiles = int32_t((d.m + OM - 1) / OM);
+    gr.b_tiles = int32_t((d.n + ON - 1) / ON);
+    gr.slices = int32_t((d.k + OK - 1) / OK);
+    gr.a_pack = p.a_bytes;
+    gr.b_pack = p.b_bytes;
+    gr.a_rowmax = ra;
+    gr.b_rowmax = rb;
+    ra += d.m;
+    rb += d.n;
+    p.a_bytes += int64_t(gr.a_tiles) * gr.slices * kPieces * kAPieceBytes;
+    p.b_bytes += int64_t(gr.b_tiles) * gr.slices * kPieces * kBPieceBytes;
+    for (int32_t s = 0; s < gr.slices; ++s) {
+      for (int32_t t = 0; t < gr.a_tiles; ++t) p.tasks_a.push_back({g, t, s, 0});
+      for (int32_t t = 0; t < gr.b_tiles; ++t) p.tasks_b.push_back({g, t, s, 1});
+    }
+    for (int32_t y = 0; y < gr.b_tiles; ++y)
+      for (int32_t x = 0; x < gr.a_tiles; ++x) p.tiles.push_back({g, x, y, OM});
+    p.groups.push_back(gr);
+  }
+  p.rowmax = rb;
+  p.tasks = p.tasks_a;
+  p.tasks.insert(p.tasks.end(), p.tasks_b.begin(), p.tasks_b.end());
+  return p;
+}
+
+void launch_oz_pack(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
+                    const double* A, const double* B, unsigned long long* rowmax, int64_t clear_from,
+                    int64_t clear_count, unsigned char* apack, unsigned char* bpack, cudaStream_t s) {
+  if (n_tasks <= 0) return;
+  if (clear_count > 0) cudaMemsetAsync(rowmax + clear_from, 0, sizeof(unsigned long long) * size_t(clear_count), s);
+  oz_rowmax_kernel<<<n_tasks, 256, 0, s>>>(d_descs, d_groups, d_tasks, A, B, rowmax);
+  count_launch();
+  oz_pack_kernel<<<n_tasks, 256, 0, s>>>(d_descs, d_groups, d_tasks, A, B, rowmax, apack, bpack);
+  count_launch();
+}
+
+void launch_oz_gemm(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const GemmTile* d_tiles, int n_tiles,
+                    const unsigned char* apack, const unsigned char* bpack, const unsigned long long* rowmax, double* C,
+                    double alpha, double beta, cudaStream_t s) {
+  if (n_tiles <= 0) return;
+  if (!g_oz_attr) {
+    cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kOzSmem);
+    g_oz_attr = true;
+  }
+  oz_gemm_kernel<<<n_tiles, kOzThreads, kOzSmem, s>>>(d_descs, d_groups, d_tiles, apack, bpack, rowmax, C, alpha,
+                                                     beta, gemm_tc_error_flag());
+  count_launch();
+}
+
+void launch_gemm_oz(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
+                    const GemmTile* d_tiles, int n_tiles, const double* A, const double* B,
+                    unsigned long long* rowmax, int64_t n_rowmax, unsigned char* apack, unsigned char* bpack,
+                    double* C, double alpha, double beta, cudaStream_t s) {
+  if (n_tiles <= 0) return;
+  launch_oz_pack(d_descs, d_groups, d_tasks, n_tasks, A, B, rowmax, 0, n_rowmax, apack, bpack, s);
+  launch_oz_gemm(d_descs, d_groups, d_tiles, n_tiles, apack, bpack, rowmax, C, alpha, beta, s);
+}
+
+}  // namespace xgb

@@ -458,8 +458,7 @@ void launch_gemm_tc(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const
   if (!g_tc_attr) {
     cudaFuncSetAttribute(gemm_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
     cudaFuncSetAttribute(gemm_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-    cudaMalloc(&g_tc_err, sizeof(int));
-    cudaMemset(g_tc_err, 0, sizeof(int));
+    gemm_tc_error_flag();
     g_tc_attr = true;
   }
   if (form == 1) {
@@ -488,6 +487,14 @@ void launch_tc_pack(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const
   else
     tc_pack_kernel<0><<<n_tasks, 256, 0, s>>>(d_descs, d_groups, d_tasks, A, B, apack, bpack);
   count_launch();
+}
+
+int* gemm_tc_error_flag() {
+  if (!g_tc_err) {
+    cudaMalloc(&g_tc_err, sizeof(int));
+    cudaMemset(g_tc_err, 0, sizeof(int));
+  }
+  return g_tc_err;
 }
 
 int gemm_tc_error(bool reset) {

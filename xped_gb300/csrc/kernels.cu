@@ -284,11 +284,70 @@ int choose_gemm_tile(const xgb_gemm_desc* descs, int n) {
 // output sub-block along output leg 0 (all other leg indices fixed), which is contiguous in the
 // output (leg 0 fastest) and, for the permutations that keep the block's leading leg in front,
 // contiguous in the source too.  A group of G threads (G a power of two up to a warp, chosen on
-// the host from the rows' typical length) takes a row: its multi-index is decoded once per row
-// (not per element), and the lanes walk the row with unit stride, so a warp's loads and stores
-// cover whole 32-byte sectors.  Each group decodes U = 4 rows before loading, so every thread has
-// up to four independent loads in flight.  Tasks with several contributions (SU(2) recoupling)
-// accumulate them in a fixed order.
+// the host from the rows' typical length) takes a chunk of kRowsPerChunk consecutive rows: the
+// first row's multi-index is decoded once (32-bit division), the following rows step it like an
+// odometer (leg 1 fastest, adding the legs' strides), and the lanes walk each row with unit stride,
+// so a warp's loads and stores cover whole 32-byte sectors.  Four rows' loads are issued before
+// their stores.  Tasks with several contributions (SU(2) recoupling) accumulate them in a fixed
+// order.
+constexpr int kRowsPerChunk = 8;
+
+struct RowCursor {
+  int ti = -1;            // task
+  int64_t row_end = 0;    // first row past the task
+  int idx[XGB_MAX_LEGS];  // multi-index of legs 1..rank-1
+  int64_t dofs = 0, sofs = 0;
+};
+
+__device__ __forceinline__ void cursor_seek(RowCursor& c, const xgb_perm_task* __restrict__ tasks,
+                                            const int64_t* __restrict__ row_start, int n_tasks,
+                                            const xgb_perm_contrib* __restrict__ contribs, int64_t r) {
+  int ti = c.ti >= 0 ? c.ti : 0;
+  if (!(r >= row_start[ti] && r < row_start[ti + 1])) {
+    int lo = 0, hi = n_tasks - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (row_start[mid] <= r) lo = mid; else hi = mid - 1;
+    }
+    ti = lo;
+  }
+  const xgb_perm_task& t = tasks[ti];
+  c.ti = ti;
+  c.row_end = row_start[ti + 1];
+  int64_t rem = r - row_start[ti];
+  c.dofs = t.dst_base;
+  const bool single = t.n_contrib == 1;
+  c.sofs = single ? contribs[t.contrib0].src_base : 0;
+  for (int k = 1; k < t.rank; ++k) {
+    const int dk = t.dims[k];
+    int ik;
+    if (rem < (int64_t(1) << 31)) {  // 32-bit division for the common case
+      const uint32_t r32 = uint32_t(rem), q = r32 / uint32_t(dk);
+      ik = int(r32 - q * uint32_t(dk));
+      rem = q;
+    } else {
+      const int64_t q = rem / dk;
+      ik = int(rem - q * dk);
+      rem = q;
+    }
+    c.idx[k] = ik;
+    c.dofs += ik * t.dst_stride[k];
+    if (single) c.sofs += ik * contribs[t.contrib0].src_stride[k];
+  }
+}
+
+// next row of the same task: leg 1 fastest, carrying into the higher legs
+__device__ __forceinline__ void cursor_step(RowCursor& c, const xgb_perm_task& t, const xgb_perm_contrib* cc) {
+  for (int k = 1; k < t.rank; ++k) {
+    c.dofs += t.dst_stride[k];
+    if (cc) c.sofs += cc->src_stride[k];
+    if (++c.idx[k] < t.dims[k]) return;
+    c.idx[k] = 0;
+    c.dofs -= int64_t(t.dims[k]) * t.dst_stride[k];
+    if (cc) c.sofs -= int64_t(t.dims[k]) * cc->src_stride[k];
+  }
+}
+
 template <int G>
 __global__ void __launch_bounds__(256) permute_rows_kernel(const xgb_perm_task* __restrict__ tasks,
                                                            const int64_t* __restrict__ row_start, int n_tasks,
@@ -298,76 +357,62 @@ __global__ void __launch_bounds__(256) permute_rows_kernel(const xgb_perm_task* 
   const int lane = int(threadIdx.x) % G;
   const int64_t group = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) / G;
   const int64_t ngroups = int64_t(gridDim.x) * blockDim.x / G;
-  int cached = 0;
-  for (int64_t base = group; base < total_rows; base += ngroups * U) {
-    int64_t doff[U], soff[U], ds0[U], ss0[U];
-    double coeff[U];
-    int len[U];
-    int maxlen = 0;
+  const int64_t nchunks = (total_rows + kRowsPerChunk - 1) / kRowsPerChunk;
+  RowCursor cur;
+  for (int64_t chunk = group; chunk < nchunks; chunk += ngroups) {
+    const int64_t r0 = chunk * kRowsPerChunk;
+    const int64_t r1 = r0 + kRowsPerChunk < total_rows ? r0 + kRowsPerChunk : total_rows;
+    cursor_seek(cur, tasks, row_start, n_tasks, contribs, r0);
+    for (int64_t rb = r0; rb < r1; rb += U) {
+      int64_t doff[U], soff[U], ds0[U], ss0[U];
+      double coeff[U];
+      int len[U];
+      int maxlen = 0;
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      len[u] = 0;
-      doff[u] = soff[u] = ds0[u] = ss0[u] = 0;
-      coeff[u] = 0.0;
-      const int64_t r = base + int64_t(u) * ngroups;
-      if (r >= total_rows) continue;
-      int ti = cached;
-      if (!(r >= row_start[ti] && r < row_start[ti + 1])) {
-        int lo = 0, hi = n_tasks - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (row_start[mid] <= r) lo = mid; else hi = mid - 1;
+      for (int u = 0; u < U; ++u) {
+        len[u] = 0;
+        doff[u] = soff[u] = ds0[u] = ss0[u] = 0;
+        coeff[u] = 0.0;
+        const int64_t r = rb + u;
+        if (r >= r1) continue;
+        if (r >= cur.row_end) cursor_seek(cur, tasks, row_start, n_tasks, contribs, r);
+        const xgb_perm_task& t = tasks[cur.ti];
+        const int d0 = t.rank > 0 ? t.dims[0] : 1;
+        const int64_t dstr0 = t.rank > 0 ? t.dst_stride[0] : 0;
+        if (t.n_contrib == 1) {
+          const xgb_perm_contrib& cc = contribs[t.contrib0];
+          doff[u] = cur.dofs;
+          soff[u] = cur.sofs;
+          ds0[u] = dstr0;
+          ss0[u] = t.rank > 0 ? cc.src_stride[0] : 0;
+          coeff[u] = cc.coeff;
+          len[u] = d0;
+          maxlen = max(maxlen, d0);
+          cursor_step(cur, t, &cc);
+          continue;
         }
-        ti = lo;
-        cached = ti;
-      }
-      const xgb_perm_task& t = tasks[ti];
-      const int d0 = t.rank > 0 ? t.dims[0] : 1;
-      int64_t rem = r - row_start[ti];
-      int idx[XGB_MAX_LEGS];
-      idx[0] = 0;
-      int64_t dofs = t.dst_base;
-      for (int k = 1; k < t.rank; ++k) {
-        const int dk = t.dims[k];
-        const int64_t q = rem / dk;
-        idx[k] = int(rem - q * dk);
-        rem = q;
-        dofs += idx[k] * t.dst_stride[k];
-      }
-      const int64_t dstr0 = t.rank > 0 ? t.dst_stride[0] : 0;
-      if (t.n_contrib == 1) {
-        const xgb_perm_contrib& cc = contribs[t.contrib0];
-        int64_t so = cc.src_base;
-        for (int k = 1; k < t.rank; ++k) so += idx[k] * cc.src_stride[k];
-        doff[u] = dofs;
-        soff[u] = so;
-        ds0[u] = dstr0;
-        ss0[u] = t.rank > 0 ? cc.src_stride[0] : 0;
-        coeff[u] = cc.coeff;
-        len[u] = d0;
-        maxlen = max(maxlen, d0);
-        continue;
-      }
-      // several source sub-blocks add into this row (SU(2)): fixed contribution order
-      for (int i = lane; i < d0; i += G) {
-        double v = 0.0;
-        for (int c = 0; c < t.n_contrib; ++c) {
-          const xgb_perm_contrib& cc = contribs[t.contrib0 + c];
-          int64_t so = cc.src_base + int64_t(i) * (t.rank > 0 ? cc.src_stride[0] : 0);
-          for (int k = 1; k < t.rank; ++k) so += idx[k] * cc.src_stride[k];
-          v = fma(cc.coeff, __ldg(src + so), v);
+        // several source sub-blocks add into this row (SU(2)): fixed contribution order
+        for (int i = lane; i < d0; i += G) {
+          double v = 0.0;
+          for (int c = 0; c < t.n_contrib; ++c) {
+            const xgb_perm_contrib& cc = contribs[t.contrib0 + c];
+            int64_t so = cc.src_base + int64_t(i) * (t.rank > 0 ? cc.src_stride[0] : 0);
+            for (int k = 1; k < t.rank; ++k) so += cur.idx[k] * cc.src_stride[k];
+            v = fma(cc.coeff, __ldg(src + so), v);
+          }
+          dst[cur.dofs + int64_t(i) * dstr0] = v;
         }
-        dst[dofs + int64_t(i) * dstr0] = v;
+        cursor_step(cur, t, nullptr);
       }
-    }
-    for (int i = lane; i < maxlen; i += G) {
-      double v[U];
+      for (int i = lane; i < maxlen; i += G) {
+        double v[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u)
-        if (i < len[u]) v[u] = coeff[u] * __ldg(src + soff[u] + int64_t(i) * ss0[u]);
+        for (int u = 0; u < U; ++u)
+          if (i < len[u]) v[u] = coeff[u] * __ldg(src + soff[u] + int64_t(i) * ss0[u]);
 #pragma unroll
-      for (int u = 0; u < U; ++u)
-        if (i < len[u]) dst[doff[u] + int64_t(i) * ds0[u]] = v[u];
+        for (int u = 0; u < U; ++u)
+          if (i < len[u]) dst[doff[u] + int64_t(i) * ds0[u]] = v[u];
+      }
     }
   }
 }
@@ -393,8 +438,8 @@ PermRows perm_rows(const xgb_perm_task* tasks, int n_tasks) {
 void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_row_start, int n_tasks, int64_t total_rows,
                     int group, const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s) {
   if (total_rows <= 0 || n_tasks <= 0) return;
-  // one group per row, four rows per group and pass; enough CTAs to fill the GPU a few times over
-  const int64_t groups_needed = (total_rows + 3) / 4;
+  // one group per chunk of kRowsPerChunk rows; enough CTAs to fill the GPU a few times over
+  const int64_t groups_needed = (total_rows + kRowsPerChunk - 1) / kRowsPerChunk;
   const int64_t per_block = 256 / group;
   const int64_t cap = int64_t(num_sms() > 0 ? num_sms() : 152) * 16;
   const unsigned blocks = unsigned(std::max<int64_t>(1, std::min<int64_t>(cap, (groups_needed + per_block - 1) / per_block)));
@@ -870,6 +915,27 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
   cudaStream_t s = pick(stream_);
   for (int g = 0; g < n_groups; ++g)
     if (descs[g].m < 0 || descs[g].n < 0 || descs[g].k < 0) return set_error(XGB_E_BADPLAN, "negative GEMM extent");
+  if (precision == XGB_PREC_F64TC) {
+    OzPlanHost op = build_oz_plan(descs, n_groups);
+    if (op.tiles.empty()) return XGB_OK;
+    double flops = 0;
+    for (int g = 0; g < n_groups; ++g) flops += 2.0 * double(descs[g].m) * double(descs[g].n) * double(descs[g].k);
+    auto* dd = upload(descs, size_t(n_groups), s);
+    auto* dg = upload(op.groups.data(), op.groups.size(), s);
+    auto* dk = upload(op.tasks.data(), std::max<size_t>(op.tasks.size(), 1), s);
+    auto* dt = upload(op.tiles.data(), op.tiles.size(), s);
+    auto* rm = static_cast<unsigned long long*>(dev_alloc(sizeof(unsigned long long) * size_t(std::max<int64_t>(op.rowmax, 1))));
+    auto* ap = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(op.a_bytes, 16))));
+    auto* bp = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(op.b_bytes, 16))));
+    prof_begin(K_GEMM_OZ, s);
+    launch_gemm_oz(dd, dg, dk, int(op.tasks.size()), dt, int(op.tiles.size()), A, B, rm, op.rowmax, ap, bp, C, alpha,
+                   beta, s);
+    prof_end(K_GEMM_OZ, s, flops);
+    for (void* p : {static_cast<void*>(dd), static_cast<void*>(dg), static_cast<void*>(dk), static_cast<void*>(dt),
+                    static_cast<void*>(rm), static_cast<void*>(ap), static_cast<void*>(bp)})
+      dev_free(p);
+    return check_cuda(cudaGetLastError(), "f64tc gemm launch");
+  }
   if (precision == XGB_PREC_3XTF32 || precision == XGB_PREC_BF16X9) {
     const int form = precision == XGB_PREC_BF16X9 ? 1 : 0;
     TcPlanHost tp = build_tc_plan(descs, n_groups, form);

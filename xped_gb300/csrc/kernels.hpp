@@ -54,7 +54,8 @@ void launch_gemm_f32(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int 
                      const double* B, double* C, double alpha, double beta, cudaStream_t s);
 // precision forms of the block GEMM this build implements (XGB_PREC_*)
 inline bool gemm_precision_available(int p) {
-  return p == XGB_PREC_FP64 || p == XGB_PREC_3XTF32 || p == XGB_PREC_FP32 || p == XGB_PREC_BF16X9;
+  return p == XGB_PREC_FP64 || p == XGB_PREC_3XTF32 || p == XGB_PREC_FP32 || p == XGB_PREC_BF16X9 ||
+         p == XGB_PREC_F64TC;
 }
 // permute launch shape: rows (runs along output leg 0) per task as prefix sums, and the number of
 // threads that share one row (a power of two up to 32, from the element-weighted row length)
@@ -106,6 +107,35 @@ void launch_gemm_tc(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const
 void launch_tc_pack(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
                     const double* A, const double* B, float* apack, float* bpack, cudaStream_t s, int form = 0);
 int gemm_tc_error(bool reset);  // 1 if a tensor-core GEMM CTA gave up waiting (synchronous read)
+int* gemm_tc_error_flag();      // the device flag itself (allocated on first use)
+
+// FP64-accurate tensor-core grouped GEMM from exact BF16 slices (gemm_oz.cu): 128 x 64 output tiles,
+// 32-K slices, seven BF16 pieces per operand entry; per group the packed A / B slice blocks (bytes)
+// and the offsets of its op(A) rows' / op(B) columns' largest magnitudes in the rowmax array
+struct OzGroup {
+  int64_t a_pack, b_pack, a_rowmax, b_rowmax;
+  int32_t a_tiles, b_tiles, slices, pad;
+};
+struct OzPlanHost {
+  std::vector<OzGroup> groups;
+  std::vector<TcPackTask> tasks;            // tasks_a then tasks_b
+  std::vector<TcPackTask> tasks_a, tasks_b;  // the op(A) and op(B) chunks alone
+  std::vector<GemmTile> tiles;
+  int64_t a_bytes = 0, b_bytes = 0;
+  int64_t rowmax = 0, rowmax_a = 0;  // entries in all; the op(A) rows come first
+};
+OzPlanHost build_oz_plan(const xgb_gemm_desc* descs, int n);
+// the row scales and slices of the given chunks (rowmax[clear_from .. + clear_count) zeroed first)
+void launch_oz_pack(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
+                    const double* A, const double* B, unsigned long long* rowmax, int64_t clear_from,
+                    int64_t clear_count, unsigned char* apack, unsigned char* bpack, cudaStream_t s);
+void launch_oz_gemm(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const GemmTile* d_tiles, int n_tiles,
+                    const unsigned char* apack, const unsigned char* bpack, const unsigned long long* rowmax, double* C,
+                    double alpha, double beta, cudaStream_t s);
+void launch_gemm_oz(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
+                    const GemmTile* d_tiles, int n_tiles, const double* A, const double* B,
+                    unsigned long long* rowmax, int64_t n_rowmax, unsigned char* apack, unsigned char* bpack,
+                    double* C, double alpha, double beta, cudaStream_t s);
 
 // randomized tSVD helpers (rsvd.cu)
 struct GaussBlock { int64_t offset, count, stream; };       // fill out[offset .. offset+count) from stream
@@ -147,7 +177,7 @@ void launch_mlp_reduce_adam(float* params, float* mom, float* vel, const float* 
 
 // per-kernel-kind instrumentation (CUDA events around each launch when enabled;
 // algorithmic work - flops for GEMMs, bytes for data movement - always counted)
-enum KernelKind { K_GEMM = 0, K_PERMUTE, K_SVD, K_TRUNC, K_QR, K_ABSMAX, K_SCALE, K_COPY2D, K_DIAG, K_GEMM_TC, K_SKETCH, K_MLP, K_GEMM_F32, K_COUNT };
+enum KernelKind { K_GEMM = 0, K_PERMUTE, K_SVD, K_TRUNC, K_QR, K_ABSMAX, K_SCALE, K_COPY2D, K_DIAG, K_GEMM_TC, K_SKETCH, K_MLP, K_GEMM_F32, K_GEMM_OZ, K_COUNT };
 void prof_begin(int kind, cudaStream_t s);
 void prof_end(int kind, cudaStream_t s, double work);
 

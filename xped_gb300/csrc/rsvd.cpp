@@ -124,6 +124,60 @@ class TcProducts {
   float* bp_ = nullptr;
 };
 
+// FP64-accurate tensor-core products op(A_q) X_q (gemm_oz.cu, exact BF16 slices) over a fixed list of
+// sector GEMMs: op(A) is scaled and sliced once at construction, each apply() slices only X.
+class OzProducts {
+ public:
+  OzProducts(const std::vector<xgb_gemm_desc>& d, const double* A, cudaStream_t s) {
+    const OzPlanHost op = build_oz_plan(d.data(), int(d.size()));
+    n_tiles_ = int(op.tiles.size());
+    n_b_ = int(op.tasks_b.size());
+    rowmax_a_ = op.rowmax_a;
+    rowmax_ = op.rowmax;
+    for (const auto& g : d) flops_ += 2.0 * double(g.m) * double(g.n) * double(g.k);
+    od_ = st_.add(d);
+    og_ = st_.add(op.groups);
+    oa_ = st_.add(op.tasks_a);
+    ob_ = st_.add(op.tasks_b);
+    ot_ = st_.add(op.tiles);
+    st_.upload(s);
+    rm_ = static_cast<unsigned long long*>(dev_alloc(sizeof(unsigned long long) * size_t(std::max<int64_t>(rowmax_, 1))));
+    ap_ = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(op.a_bytes, 16))));
+    bp_ = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(op.b_bytes, 16))));
+    prof_begin(K_GEMM_OZ, s);
+    launch_oz_pack(st_.at<xgb_gemm_desc>(od_), st_.at<OzGroup>(og_), st_.at<TcPackTask>(oa_), int(op.tasks_a.size()), A,
+                   nullptr, rm_, 0, rowmax_a_, ap_, bp_, s);
+    prof_end(K_GEMM_OZ, s, 0.0);
+  }
+  OzProducts(const OzProducts&) = delete;
+  OzProducts& operator=(const OzProducts&) = delete;
+  ~OzProducts() {
+    dev_free(rm_);
+    dev_free(ap_);
+    dev_free(bp_);
+  }
+  // C = op(A) X with the A sliced at construction
+  void apply(const double* A, const double* X, double* C, cudaStream_t s) {
+    if (n_tiles_ == 0) return;
+    prof_begin(K_GEMM_OZ, s);
+    launch_oz_pack(st_.at<xgb_gemm_desc>(od_), st_.at<OzGroup>(og_), st_.at<TcPackTask>(ob_), n_b_, A, X, rm_,
+                   rowmax_a_, rowmax_ - rowmax_a_, ap_, bp_, s);
+    launch_oz_gemm(st_.at<xgb_gemm_desc>(od_), st_.at<OzGroup>(og_), st_.at<GemmTile>(ot_), n_tiles_, ap_, bp_, rm_, C,
+                   1.0, 0.0, s);
+    prof_end(K_GEMM_OZ, s, flops_);
+  }
+
+ private:
+  Staging st_;
+  size_t od_ = 0, og_ = 0, oa_ = 0, ob_ = 0, ot_ = 0;
+  int n_tiles_ = 0, n_b_ = 0;
+  int64_t rowmax_a_ = 0, rowmax_ = 0;
+  double flops_ = 0;
+  unsigned long long* rm_ = nullptr;
+  unsigned char* ap_ = nullptr;
+  unsigned char* bp_ = nullptr;
+};
+
 // Batched thin SVD through the cluster Jacobi kernel (work counted as the thin R-SVD flop count
 // 6 m n^2 + 20 n^3, m >= n, Golub & Van Loan, Matrix Computations, Table 5.5.1).
 void batched_svd(const std::vector<xgb_svd_desc>& d, const double* A, double* U, double* S, double* Vt, cudaStream_t s) {
@@ -218,7 +272,7 @@ constexpr int kMaxRefine = 3;  // refinement passes of unconverged sectors per r
 
 SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, const std::vector<int64_t>& sketch,
                           int power_iters, uint64_t seed, RsvdInfo* info, const Tensor* warm, double res_tol,
-                          int fp64_tail) {
+                          int fp64_tail, bool exact_tc) {
   Tensor t = materialize(t0);
   const TensorMeta& m = *t.meta;
   const int n = int(m.sectors.size());
@@ -226,7 +280,8 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
   if (int(sketch.size()) != n) throw std::runtime_error("randomized tSVD: one sketch width per sector required");
   if (power_iters < 0) throw std::runtime_error("randomized tSVD: negative number of power iterations");
   // leading iterations (and the first product A Omega) on the tensor cores; the last fp64_tail in FP64
-  const int tc_iters = fp64_tail >= 0 ? std::max(0, power_iters - fp64_tail) : 0;
+  // (exact_tc: every product A X / A^T X on the FP64-accurate tensor-core form instead)
+  const int tc_iters = (!exact_tc && fp64_tail >= 0) ? std::max(0, power_iters - fp64_tail) : 0;
   cudaStream_t st = stream();
   // warm-start rows per sector (a V^dag block of the same charge and column dimension)
   Tensor warm_t;
@@ -306,10 +361,13 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
     // the basis enters in `cur` (Q or Y) and leaves in Q (last orthonormalisation with 3 passes);
     // the products of the first `lead` iterations run as 3xTF32 tensor-core GEMMs through
     // tc_t (A^T X) and tc_n (A X), which cover all sketched sectors (sub = all)
+    // FP64-accurate tensor-core products over every sketched sector (exact_tc), built once per round
+    std::unique_ptr<OzProducts> oz_n, oz_t;
     auto iterate = [&](const std::vector<int>& sub, int iters, double* cur, int lead, TcProducts* tc_t,
                        TcProducts* tc_n) {
       if (lead > 0 && (!tc_t || !tc_n || int(sub.size()) != nr))
         throw std::logic_error("randomized tSVD: tensor-core products need every sketched sector");
+      const bool use_oz = oz_t && oz_n && int(sub.size()) == nr;
       std::vector<int64_t> srr, src, srl, syo, szo;
       for (int a : sub) {
         srr.push_back(rr[a]);
@@ -320,7 +378,9 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       }
       std::vector<xgb_gemm_desc> g;
       for (int p = 0; p < iters; ++p) {
-        if (p < lead) {
+        if (use_oz) {
+          oz_t->apply(t.data(), cur, Z, st);
+        } else if (p < lead) {
           tc_t->apply(t.data(), cur, Z, st);
         } else {
           g.clear();
@@ -329,7 +389,9 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
         }
         // Omega's storage holds Qz (same layout as Z)
         double* qz = orthonormalise(src, srl, szo, Z, Om, st, kInterPasses);
-        if (p < lead) {
+        if (use_oz) {
+          oz_n->apply(t.data(), qz, Y, st);
+        } else if (p < lead) {
           tc_n->apply(t.data(), qz, Y, st);
         } else {
           g.clear();
@@ -362,7 +424,8 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
         mxr = std::max(mxr, rl[a] * rl[a]);
       }
       if (!sub.empty()) {
-        grouped_gemm(g, t.data(), Q, Z, st);
+        if (oz_t && int(sub.size()) == nr) oz_t->apply(t.data(), Q, Z, st);  // same descriptors as A^T X
+        else grouped_gemm(g, t.data(), Q, Z, st);
         Staging sc;
         const size_t oz = sc.add(zc), orr = sc.add(rc2);
         sc.upload(st);
@@ -451,7 +514,11 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
         gt.push_back({rc[a], rl[a], rr[a], m.offset[R[a]], rr[a], yo[a], rr[a], zo[a], rc[a], 1, 0});
       }
       std::unique_ptr<TcProducts> tc_n, tc_t;
-      if (tc_iters > 0) {
+      if (exact_tc) {
+        oz_n = std::make_unique<OzProducts>(g, t.data(), st);
+        oz_t = std::make_unique<OzProducts>(gt, t.data(), st);
+        oz_n->apply(t.data(), Om, Y, st);
+      } else if (tc_iters > 0) {
         tc_n = std::make_unique<TcProducts>(g, t.data(), st);
         tc_t = std::make_unique<TcProducts>(gt, t.data(), st);
         tc_n->apply(t.data(), Om, Y, st);

@@ -143,6 +143,13 @@ struct GemmPlan {
   TcPackTask* d_tc_tasks = nullptr;
   GemmTile* d_tc_tiles = nullptr;
   std::vector<xgb_gemm_desc> host_descs;
+  // FP64-accurate tensor-core form from exact BF16 slices (built on first use)
+  bool oz_ready = false;
+  int n_oz_tiles = 0, n_oz_tasks = 0;
+  int64_t oz_a_bytes = 0, oz_b_bytes = 0, oz_rowmax = 0;
+  OzGroup* d_oz_groups = nullptr;
+  TcPackTask* d_oz_tasks = nullptr;
+  GemmTile* d_oz_tiles = nullptr;
   // FP64 launch shape (tile edge, split-K): the built-in rule, or the autotuner's choice
   F64Plan f64;
   GemmTile* d_f64_tiles = nullptr;
@@ -409,6 +416,9 @@ void clear_plan_caches() {
     cudaFree(p->d_tiles);
     cudaFree(p->d_f64_tiles);
     cudaFree(p->d_f64_red);
+    cudaFree(p->d_oz_groups);
+    cudaFree(p->d_oz_tasks);
+    cudaFree(p->d_oz_tiles);
   }
   g_perm_plans.clear();
   g_gemm_plans.clear();
@@ -612,6 +622,36 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
     launch_gemm_tc(plan->d_descs, plan->d_tc_groups, plan->d_tc_tasks, plan->n_tc_tasks, plan->d_tc_tiles,
                    plan->n_tc_tiles, a.data(), b.data(), ap, bp, out.data(), 1.0, 0.0, stream());
     prof_end(K_GEMM_TC, stream(), plan->flops);
+    dev_free(ap);
+    dev_free(bp);
+    return out;
+  }
+  if (g_gemm_precision == XGB_PREC_F64TC) {
+    {
+      std::lock_guard<std::mutex> lk(g_plan_mu);
+      if (!plan->oz_ready) {
+        OzPlanHost op = build_oz_plan(plan->host_descs.data(), int(plan->host_descs.size()));
+        plan->n_oz_tiles = int(op.tiles.size());
+        plan->n_oz_tasks = int(op.tasks.size());
+        plan->oz_a_bytes = op.a_bytes;
+        plan->oz_b_bytes = op.b_bytes;
+        plan->oz_rowmax = op.rowmax;
+        plan->d_oz_groups = dev_table(op.groups);
+        plan->d_oz_tasks = dev_table(op.tasks);
+        plan->d_oz_tiles = dev_table(op.tiles);
+        plan->oz_ready = true;
+      }
+    }
+    cudaStream_t st = stream();
+    auto* rm = static_cast<unsigned long long*>(
+        dev_alloc(sizeof(unsigned long long) * size_t(std::max<int64_t>(plan->oz_rowmax, 1))));
+    auto* ap = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(plan->oz_a_bytes, 16))));
+    auto* bp = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(plan->oz_b_bytes, 16))));
+    prof_begin(K_GEMM_OZ, st);
+    launch_gemm_oz(plan->d_descs, plan->d_oz_groups, plan->d_oz_tasks, plan->n_oz_tasks, plan->d_oz_tiles,
+                   plan->n_oz_tiles, a.data(), b.data(), rm, plan->oz_rowmax, ap, bp, out.data(), 1.0, 0.0, st);
+    prof_end(K_GEMM_OZ, st, plan->flops);
+    dev_free(rm);
     dev_free(ap);
     dev_free(bp);
     return out;
@@ -1329,9 +1369,10 @@ Tensor CTM::contract_corner(const char* corner) {
 }
 
 std::pair<Tensor, Tensor> CTM::decompose_dir(int d, const Tensor& t1, const Tensor& t2) {
-  // decompose (src/PEPS/PEPSContractions.cpp:16-43) with the configured SVD form;
-  // the product, the SVD and the projectors are FP64 whatever the GEMM form
-  GemmPrecisionScope fp64(XGB_PREC_FP64);
+  // decompose (src/PEPS/PEPSContractions.cpp:16-43) with the configured SVD form; the product, the
+  // SVD and the projectors are FP64 (or the FP64-accurate tensor-core form) whatever the GEMM form
+  const bool exact_tc = gemm_prec == XGB_PREC_F64TC;
+  GemmPrecisionScope fp64(exact_tc ? XGB_PREC_F64TC : XGB_PREC_FP64);
   Tensor prod = matmul(t1, t2);
   const TensorMeta& m = *prod.meta;
   const size_t n = m.sectors.size();
@@ -1358,7 +1399,7 @@ std::pair<Tensor, Tensor> CTM::decompose_dir(int d, const Tensor& t1, const Tens
     const bool warm = warm_iters >= 0 && warm_v[d].valid() && warm_v[d].meta->cod == m.cod;
     r = tsvd_randomized(prod, chi, 1.0e-10, want, warm ? warm_iters : power_iters,
                         seed + uint64_t(stats.decompositions), &info, warm ? &warm_v[d] : nullptr, res_tol,
-                        sketch_fp64_tail);
+                        sketch_fp64_tail, exact_tc);
     stats.refinements += info.refinements;
     stats.max_residual = info.max_residual;
     width = info.width;

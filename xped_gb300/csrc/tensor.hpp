@@ -142,10 +142,12 @@ struct RsvdInfo {
 // `fp64_tail` >= 0: the first product A Omega and the products of all but the last
 // fp64_tail subspace iterations run as 3xTF32 tensor-core GEMMs (FP32 accumulation);
 // the trailing iterations, the projection and everything after it stay FP64.
-// < 0 (the default): every product in FP64.
+// < 0 (the default): every product in FP64.  `exact_tc`: every product A X / A^T X of the sketch
+// (first product, subspace iterations, projection) on the FP64-accurate tensor-core form
+// (exact BF16 slices, XGB_PREC_F64TC) instead; fp64_tail is then ignored.
 SVDResult tsvd_randomized(const Tensor& t, int64_t max_keep, double eps_svd, const std::vector<int64_t>& sketch,
                           int power_iters, uint64_t seed, RsvdInfo* info = nullptr, const Tensor* warm = nullptr,
-                          double res_tol = 0.0, int fp64_tail = -1);
+                          double res_tol = 0.0, int fp64_tail = -1, bool exact_tc = false);
 std::pair<Tensor, Tensor> tqr(const Tensor& t);
 std::pair<Tensor, Tensor> decompose(const Tensor& t1, const Tensor& t2, int64_t max_nsv);
 
@@ -229,7 +231,9 @@ class CTM {
 
   // block GEMMs of the corner contractions and the renormalisation:
   // XGB_PREC_FP64 or XGB_PREC_3XTF32 (the projector SVD, the projector
-  // construction and the normalisation stay FP64)
+  // construction and the normalisation stay FP64); XGB_PREC_F64TC, being
+  // FP64-accurate, also takes the projector products T1 T2, the projectors
+  // and the randomized SVD's sketch products to the tensor cores
   int gemm_prec = XGB_PREC_FP64;
   // projector SVD form: 0 exact FP64 tSVD, 1 randomized with `policy` widths
   int svd_mode = 0;

@@ -16,7 +16,7 @@ import numpy as np
 from ._lib import (PermContrib, PermTask, GemmDesc, check, check_handle, ensure_device, lib)
 
 SYM_IDS = {"U1": 0, "fU1": 1, "Z2": 2, "fZ2": 3, "SU2": 4}
-GEMM_FORMS = {"fp64": 0, "3xtf32": 1, "bf16x9": 2, "fp32": 3}  # XGB_PREC_* of xgb.h
+GEMM_FORMS = {"fp64": 0, "3xtf32": 1, "bf16x9": 2, "fp32": 3, "f64tc": 4}  # XGB_PREC_* of xgb.h
 
 
 def _i32(seq):
@@ -458,8 +458,9 @@ class CTM:
         return {"refinements": n.value, "max_residual": r.value}
 
     def set_gemm(self, precision: str = "fp64"):
-        """Block GEMMs of the corner contractions / renormalisation: "fp64",
-        "3xtf32" (tensor cores) or "fp32"."""
+        """Block GEMMs of the corner contractions / renormalisation: "fp64", "3xtf32" (tensor cores)
+        or "fp32"; "f64tc" (FP64-accurate tensor-core form from exact BF16 slices) also takes the
+        projector products and the randomized SVD's sketch products to the tensor cores."""
         check(lib().xgb_ctm_set_gemm_precision(self._h, GEMM_FORMS[precision]), "ctm_set_gemm")
         return self
 
@@ -528,7 +529,8 @@ FEATURES = 8  # per-sector inputs of the rank predictor
 
 
 def set_gemm_precision(precision: str = "fp64"):
-    """Precision form of matmul / contract block GEMMs on this thread: "fp64", "3xtf32" or "fp32"."""
+    """Precision form of matmul / contract block GEMMs on this thread: "fp64", "3xtf32", "bf16x9", "fp32"
+    or "f64tc" (FP64-accurate, exact BF16 slices on the tensor cores)."""
     check(lib().xgb_set_gemm_precision(GEMM_FORMS[precision]), "set_gemm_precision")
 
 
