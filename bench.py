@@ -13,7 +13,9 @@ Forms, same workload, same GPU:
            last kept counts + max(16, 50 %), exact FP64 tSVD for the first
            decomposition of each direction and as fallback), FP64 SVD core /
            projectors / normalisation;
-           block GEMMs in FP64 or 3xTF32 (--gemm)
+           block GEMMs (--gemm): f64tc (default: FP64-accurate, exact BF16 slices on
+           the tensor cores or the FP64 CUDA cores, per size bucket from the
+           autotuner), fp64, 3xtf32 or fp32
   plain    the exact FP64 tSVD in every move (the reference algorithm)
 The energy per site (Heisenberg bonds, horizontal + vertical RDM) of both
 forms after the same number of steps from the same start is reported with
@@ -357,6 +359,22 @@ def run_gpu(args):
     return res
 
 
+def dtype_label(args):
+    if args.gemm == "f64tc":
+        return "f64 (FP64-accurate block GEMMs: exact BF16 slices on the tensor cores or FP64 CUDA cores)"
+    return (("f64" if args.gemm == "fp64" else f"f64 ({args.gemm} block GEMMs)")
+            + (" + 3xTF32 early sketch products" if args.sketch_tail >= 0 else ""))
+
+
+def gemm_form_label(args):
+    if args.gemm == "f64tc":
+        return ("; every block GEMM (corner contractions, renormalisation, T1 T2, projectors, sketch products) "
+                "FP64-accurate: exact BF16 slices on the tensor cores, or the FP64 CUDA cores where the autotuner "
+                "measures them faster")
+    return (f"; sketch products of the first {POWER_ITERS - args.sketch_tail} iterations 3xTF32"
+            if args.sketch_tail >= 0 else "")
+
+
 def autotune_report(L):
     """The FP64 GEMM shapes the autotuner chose (per size bucket) and the time it spent measuring."""
     import ctypes as C
@@ -366,10 +384,11 @@ def autotune_report(L):
     L.xgb_autotune_choices(tiles, waves, n)
     hist = {}
     for i in range(n):
-        k = f"tile{tiles[i]}_split{waves[i]}"
+        k = "f64tc" if tiles[i] == 0 else f"tile{tiles[i]}_split{waves[i]}"
         hist[k] = hist.get(k, 0) + 1
     return {"enabled": True, "buckets": n, "cache_hits": hits.value, "measure_ms": ms.value, "choices": hist,
-            "candidates": "tile 16/32/64 x split-K target 0/1/2/4 waves"}
+            "candidates": "CUDA-core FP64 tile 16/32/64 x split-K target 0/1/2/4 waves; with --gemm f64tc also the "
+                          "FP64-accurate tensor-core form"}
 
 
 def timed_solve(L, c, H, args, done=0):
@@ -1073,7 +1092,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--gemm", default="fp64", choices=["fp64", "3xtf32", "fp32", "f64tc"],
+    ap.add_argument("--gemm", default="f64tc", choices=["fp64", "3xtf32", "fp32", "f64tc"],
                     help="block GEMM form of the chosen CTM step; f64tc (FP64-accurate tensor-core products from "
                          "exact BF16 slices) also covers the projector and sketch products")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -1187,14 +1206,11 @@ def main():
     g = prof.get(gemm_kind, (0, 0.0, 0.0))
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": ("f64" if args.gemm == "fp64" else f"f64 ({args.gemm} block GEMMs)")
-            + (" + 3xTF32 early sketch products" if args.sketch_tail >= 0 else ""),
+            "vs_baseline": None, "dtype": dtype_label(args),
             "data": "synthetic (seeded N(0,1) site tensor)",
             "config": dict(config, form=f"chosen: randomized projector SVD ({POWER_ITERS} subspace iterations, "
                                         "CholeskyQR3 bases, widths last kept + max(16, 50%), exact first decomposition "
-                                        "per direction and exact FP64 fallback), FP64 SVD core"
-                                        + (f"; sketch products of the first {POWER_ITERS - args.sketch_tail} "
-                                           "iterations 3xTF32" if args.sketch_tail >= 0 else ""),
+                                        "per direction and exact FP64 fallback), FP64 SVD core" + gemm_form_label(args),
                            gemm=args.gemm, parallelism=f"replicas x{world}"),
             "e2e": {"value": world * 1e3 / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"]},

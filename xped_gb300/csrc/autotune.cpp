@@ -38,11 +38,13 @@ constexpr int64_t kMinChunk = 64;  // k per partial tile: a multiple of the kern
 
 struct Key {
   int groups, flops, area, k;
+  int tc;  // 1: the FP64-accurate tensor-core form is among the candidates
   bool operator<(const Key& o) const {
     if (groups != o.groups) return groups < o.groups;
     if (flops != o.flops) return flops < o.flops;
     if (area != o.area) return area < o.area;
-    return k < o.k;
+    if (k != o.k) return k < o.k;
+    return tc < o.tc;
   }
 };
 
@@ -61,7 +63,7 @@ Key key_of(const xgb_gemm_desc* d, int n) {
     area = std::max(area, double(d[g].m) * double(d[g].n));
     k = std::max(k, double(d[g].k));
   }
-  return {ilog2_ceil(n), ilog2_ceil(flops), ilog2_ceil(area) / 2, ilog2_ceil(k)};
+  return {ilog2_ceil(n), ilog2_ceil(flops), ilog2_ceil(area) / 2, ilog2_ceil(k), 0};
 }
 
 std::string gpu_name() {
@@ -141,7 +143,10 @@ void run_gemm_f64_config(const xgb_gemm_desc* h_descs, int n, F64Config c, const
   dev_free(dr);
 }
 
-int tune_gemm_f64(const xgb_gemm_desc* d, int n, const double* A, const double* B, cudaStream_t s, double* times_ms) {
+// times every CUDA-core candidate (and, with allow_tc, the tensor-core form as index kNumCandidates);
+// returns the index of the fastest
+int tune_gemm_f64(const xgb_gemm_desc* d, int n, const double* A, const double* B, cudaStream_t s, double* times_ms,
+                  bool allow_tc = false) {
   // scratch output covering every block's C range; the candidates write there with beta = 0
   int64_t extent = 1;
   for (int g = 0; g < n; ++g)
@@ -175,6 +180,21 @@ int tune_gemm_f64(const xgb_gemm_desc* d, int n, const double* A, const double* 
     times_ms[c] = best_ms;
     if (times_ms[c] < times_ms[best]) best = c;
   }
+  if (allow_tc) {
+    run_gemm_oz_host(d, n, A, B, scratch, 1.0, 0.0, s);  // warm-up
+    float best_ms = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
+      cudaEventRecord(e0, s);
+      run_gemm_oz_host(d, n, A, B, scratch, 1.0, 0.0, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best_ms = std::min(best_ms, ms);
+    }
+    times_ms[kNumCandidates] = best_ms;
+    if (times_ms[kNumCandidates] < times_ms[best]) best = kNumCandidates;
+  }
   dev_free(dd);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -183,24 +203,25 @@ int tune_gemm_f64(const xgb_gemm_desc* d, int n, const double* A, const double* 
 }
 
 F64Config gemm_f64_config(const xgb_gemm_desc* d, int n, const double* A, const double* B, F64Config fallback,
-                          cudaStream_t s) {
+                          cudaStream_t s, bool allow_tc) {
   Key k;
   {
     std::lock_guard<std::mutex> lk(g_mu);
     if (g_mode == 0 || n <= 0) return fallback;
     k = key_of(d, n);
+    k.tc = allow_tc ? 1 : 0;
     auto it = g_cache.find(k);
     if (it != g_cache.end()) {
       ++g_hits;
       return it->second;
     }
   }
-  double times[kNumCandidates];
+  double times[kNumCandidates + 1];
   cudaEvent_t t0, t1;
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
   cudaEventRecord(t0, s);
-  const int best = tune_gemm_f64(d, n, A, B, s, times);
+  const int best = tune_gemm_f64(d, n, A, B, s, times, allow_tc);
   cudaEventRecord(t1, s);
   cudaEventSynchronize(t1);
   float ms = 0.f;
@@ -208,7 +229,13 @@ F64Config gemm_f64_config(const xgb_gemm_desc* d, int n, const double* A, const 
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
   std::lock_guard<std::mutex> lk(g_mu);
-  g_cache[k] = f64_candidate(best);
+  if (best == kNumCandidates) {
+    F64Config c = fallback;
+    c.tc = true;
+    g_cache[k] = c;
+  } else {
+    g_cache[k] = f64_candidate(best);
+  }
   ++g_tuned;
   g_tune_ms += ms;
   return g_cache[k];
@@ -267,7 +294,7 @@ int xgb_autotune_choices(int32_t* tile, int32_t* split_waves, int cap) {
   int i = 0;
   for (const auto& kv : g_cache) {
     if (i >= cap) break;
-    if (tile) tile[i] = kv.second.tile;
+    if (tile) tile[i] = kv.second.tc ? 0 : kv.second.tile;  // 0: the FP64-accurate tensor-core form
     if (split_waves) split_waves[i] = kv.second.split_waves;
     ++i;
   }
@@ -317,7 +344,7 @@ int xgb_autotune_save(const char* path) {
   const std::string gpu = gpu_name();
   for (const auto& kv : g_cache)
     f << gpu << ' ' << kv.first.groups << ' ' << kv.first.flops << ' ' << kv.first.area << ' ' << kv.first.k << ' '
-      << kv.second.tile << ' ' << kv.second.split_waves << '\n';
+      << kv.first.tc << ' ' << kv.second.tile << ' ' << kv.second.split_waves << ' ' << (kv.second.tc ? 1 : 0) << '\n';
   return f.good() ? XGB_OK : set_error(XGB_E_BADPLAN, std::string("write failed: ") + path);
 }
 
@@ -334,7 +361,9 @@ int xgb_autotune_load(const char* path) {
     std::string name;
     Key k{};
     F64Config c{};
-    if (!(is >> name >> k.groups >> k.flops >> k.area >> k.k >> c.tile >> c.split_waves)) continue;
+    int ctc = 0;
+    if (!(is >> name >> k.groups >> k.flops >> k.area >> k.k >> k.tc >> c.tile >> c.split_waves >> ctc)) continue;
+    c.tc = ctc != 0;
     if (name != gpu) continue;  // entries measured on another GPU model do not apply
     if (c.tile != 16 && c.tile != 32 && c.tile != 64) continue;
     g_cache[k] = c;

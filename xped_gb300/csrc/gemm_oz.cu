@@ -35,6 +35,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "kernels.hpp"
@@ -241,7 +242,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     oz_gemm_kernel(const xgb_gemm_desc* __restrict__ descs, const OzGroup* __restrict__ groups,
                    const GemmTile* __restrict__ tiles, const unsigned char* __restrict__ apack,
                    const unsigned char* __restrict__ bpack, const unsigned long long* __restrict__ rowmax,
-                   double* __restrict__ C, double alpha, double beta, int* __restrict__ err) {
+                   double* __restrict__ C, double alpha, double beta, double* __restrict__ ws,
+                   int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ uint64_t full[kOzStages], empty[kOzStages], accf, acce, done;
   __shared__ uint32_t tmem_slot;
@@ -253,7 +255,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   const OzGroup gr = groups[t.g];
   const int64_t m0 = int64_t(t.tm) * OM, n0 = int64_t(t.tn) * ON;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nk = gr.slices;
+  // split-K: this CTA takes K slices [ks, ks + nk) and, with a slot, stores its raw partial tile
+  const int ks = t.k0, nk = (t.k1 < 0 ? gr.slices : t.k1) - t.k0;
   const int nchunks = (nk + kChunk - 1) / kChunk;
 
   if (warp == kOzMma) {
@@ -287,8 +290,10 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 
   if (nk > 0 && warp == kOzProducer) {
     if (lane == 0) {
-      const unsigned char* a_base = apack + gr.a_pack + int64_t(t.tm) * gr.slices * kPieces * kAPieceBytes;
-      const unsigned char* b_base = bpack + gr.b_pack + int64_t(t.tn) * gr.slices * kPieces * kBPieceBytes;
+      const unsigned char* a_base =
+          apack + gr.a_pack + (int64_t(t.tm) * gr.slices + ks) * kPieces * kAPieceBytes;
+      const unsigned char* b_base =
+          bpack + gr.b_pack + (int64_t(t.tn) * gr.slices + ks) * kPieces * kBPieceBytes;
       uint32_t ph[kOzStages] = {0, 0};
       for (int kc = 0; kc < nk; ++kc) {
         const int s = kc % kOzStages;
@@ -392,9 +397,13 @@ __global__ void __launch_bounds__(kOzThreads, 1)
       for (int j = 0; j < 32; ++j) {
         const int64_t col = n0 + colg * 32 + j;
         if (col < d.n) {
-          double* cp = C + d.c_off + row + col * d.ldc;
           const double acc = ldexp(double(hi[j]) + double(lo[j]), ei + row_scale(rowmax[gr.b_rowmax + col]));
-          *cp = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *cp);
+          if (t.slot >= 0) {  // split-K partial: raw sum, tile-local column-major OM x ON
+            ws[int64_t(t.slot) * OM * ON + (quarter * 32 + lane) + int64_t(colg * 32 + j) * OM] = acc;
+          } else {
+            double* cp = C + d.c_off + row + col * d.ldc;
+            *cp = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *cp);
+          }
         }
       }
     }
@@ -415,6 +424,23 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   __syncthreads();
   if (warp == kOzMma)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kOzTmemCols));
+}
+
+// C tile = alpha * (the split-K partials of the tile, added in slot order) + beta * C
+__global__ void __launch_bounds__(256) oz_splitk_reduce_kernel(const xgb_gemm_desc* __restrict__ descs,
+                                                                const SplitReduce* __restrict__ red,
+                                                                const double* __restrict__ ws, double* __restrict__ C,
+                                                                double alpha, double beta) {
+  const SplitReduce r = red[blockIdx.x];
+  const xgb_gemm_desc d = descs[r.g];
+  for (int e = threadIdx.x; e < OM * ON; e += blockDim.x) {
+    const int64_t i = int64_t(r.tm) * OM + e % OM, j = int64_t(r.tn) * ON + e / OM;
+    if (i >= d.m || j >= d.n) continue;
+    double acc = 0.0;
+    for (int p = 0; p < r.count; ++p) acc += ws[(int64_t(r.first) + p) * OM * ON + e];
+    double* c = C + d.c_off + i + j * d.ldc;
+    *c = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *c);
+  }
 }
 
 bool g_oz_attr = false;
@@ -445,9 +471,30 @@ OzPlanHost build_oz_plan(const xgb_gemm_desc* descs, int n) {
       for (int32_t t = 0; t < gr.a_tiles; ++t) p.tasks_a.push_back({g, t, s, 0});
       for (int32_t t = 0; t < gr.b_tiles; ++t) p.tasks_b.push_back({g, t, s, 1});
     }
-    for (int32_t y = 0; y < gr.b_tiles; ++y)
-      for (int32_t x = 0; x < gr.a_tiles; ++x) p.tiles.push_back({g, x, y, OM});
     p.groups.push_back(gr);
+  }
+  // output tiles; when they cannot fill the GPU twice over, the K slices of every tile are split into
+  // ranges of at least one exact-accumulation chunk (kChunk slices) whose partial tiles a fixed-order
+  // reduce adds
+  int64_t n_out = 0;
+  for (const auto& gr : p.groups) n_out += int64_t(gr.a_tiles) * gr.b_tiles;
+  const int64_t target = 2 * int64_t(num_sms() > 0 ? num_sms() : 152);
+  const int64_t want = n_out > 0 ? (target + n_out - 1) / n_out : 1;
+  for (int g = 0; g < n; ++g) {
+    const OzGroup& gr = p.groups[g];
+    const int64_t splits = std::max<int64_t>(1, std::min<int64_t>(want, gr.slices / kChunk));
+    const int64_t per = splits > 1 ? ((gr.slices + splits - 1) / splits + kChunk - 1) / kChunk * kChunk : gr.slices;
+    for (int32_t y = 0; y < gr.b_tiles; ++y)
+      for (int32_t x = 0; x < gr.a_tiles; ++x) {
+        if (splits == 1) {
+          p.tiles.push_back({g, x, y, OM});
+          continue;
+        }
+        const int32_t first = p.slots;
+        for (int64_t k0 = 0; k0 < gr.slices; k0 += per)
+          p.tiles.push_back({g, x, y, OM, int32_t(k0), int32_t(std::min<int64_t>(k0 + per, gr.slices)), p.slots++});
+        p.red.push_back({g, x, y, first, p.slots - first, 0});
+      }
   }
   p.rowmax = rb;
   p.tasks = p.tasks_a;
@@ -467,25 +514,66 @@ void launch_oz_pack(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const
 }
 
 void launch_oz_gemm(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const GemmTile* d_tiles, int n_tiles,
-                    const unsigned char* apack, const unsigned char* bpack, const unsigned long long* rowmax, double* C,
-                    double alpha, double beta, cudaStream_t s) {
+                    const SplitReduce* d_red, int n_red, int slots, const unsigned char* apack,
+                    const unsigned char* bpack, const unsigned long long* rowmax, double* C, double alpha, double beta,
+                    cudaStream_t s) {
   if (n_tiles <= 0) return;
   if (!g_oz_attr) {
     cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kOzSmem);
     g_oz_attr = true;
   }
+  double* ws = slots > 0 ? static_cast<double*>(dev_alloc(sizeof(double) * size_t(slots) * OM * ON)) : nullptr;
   oz_gemm_kernel<<<n_tiles, kOzThreads, kOzSmem, s>>>(d_descs, d_groups, d_tiles, apack, bpack, rowmax, C, alpha,
-                                                     beta, gemm_tc_error_flag());
+                                                     beta, ws, gemm_tc_error_flag());
   count_launch();
+  if (n_red > 0) {
+    oz_splitk_reduce_kernel<<<n_red, 256, 0, s>>>(d_descs, d_red, ws, C, alpha, beta);
+    count_launch();
+  }
+  if (ws) dev_free(ws);
+}
+
+bool f64tc_heuristic(const xgb_gemm_desc* d, int n) {
+  double flops = 0, out = 0;
+  for (int g = 0; g < n; ++g) {
+    flops += 2.0 * double(d[g].m) * double(d[g].n) * double(d[g].k);
+    out += double(d[g].m) * double(d[g].n);
+  }
+  return out > 0 && flops / out >= 128.0;  // average k >= 64
+}
+
+void run_gemm_oz_host(const xgb_gemm_desc* h_descs, int n, const double* A, const double* B, double* C, double alpha,
+                      double beta, cudaStream_t s) {
+  if (n <= 0) return;
+  OzPlanHost op = build_oz_plan(h_descs, n);
+  if (op.tiles.empty()) return;
+  auto up = [&](const void* h, size_t bytes) {
+    void* d = dev_alloc(std::max<size_t>(bytes, 16));
+    if (bytes) cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s);
+    return d;
+  };
+  auto* dd = static_cast<xgb_gemm_desc*>(up(h_descs, sizeof(xgb_gemm_desc) * size_t(n)));
+  auto* dg = static_cast<OzGroup*>(up(op.groups.data(), sizeof(OzGroup) * op.groups.size()));
+  auto* dk = static_cast<TcPackTask*>(up(op.tasks.data(), sizeof(TcPackTask) * op.tasks.size()));
+  auto* dt = static_cast<GemmTile*>(up(op.tiles.data(), sizeof(GemmTile) * op.tiles.size()));
+  auto* dr = static_cast<SplitReduce*>(up(op.red.data(), sizeof(SplitReduce) * op.red.size()));
+  auto* rm = static_cast<unsigned long long*>(dev_alloc(sizeof(unsigned long long) * size_t(std::max<int64_t>(op.rowmax, 1))));
+  auto* ap = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(op.a_bytes, 16))));
+  auto* bp = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(op.b_bytes, 16))));
+  launch_gemm_oz(dd, dg, dk, int(op.tasks.size()), dt, int(op.tiles.size()), dr, int(op.red.size()), op.slots, A, B,
+                 rm, op.rowmax, ap, bp, C, alpha, beta, s);
+  for (void* p : {static_cast<void*>(dd), static_cast<void*>(dg), static_cast<void*>(dk), static_cast<void*>(dt),
+                  static_cast<void*>(dr), static_cast<void*>(rm), static_cast<void*>(ap), static_cast<void*>(bp)})
+    dev_free(p);
 }
 
 void launch_gemm_oz(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
-                    const GemmTile* d_tiles, int n_tiles, const double* A, const double* B,
-                    unsigned long long* rowmax, int64_t n_rowmax, unsigned char* apack, unsigned char* bpack,
-                    double* C, double alpha, double beta, cudaStream_t s) {
+                    const GemmTile* d_tiles, int n_tiles, const SplitReduce* d_red, int n_red, int slots,
+                    const double* A, const double* B, unsigned long long* rowmax, int64_t n_rowmax,
+                    unsigned char* apack, unsigned char* bpack, double* C, double alpha, double beta, cudaStream_t s) {
   if (n_tiles <= 0) return;
   launch_oz_pack(d_descs, d_groups, d_tasks, n_tasks, A, B, rowmax, 0, n_rowmax, apack, bpack, s);
-  launch_oz_gemm(d_descs, d_groups, d_tiles, n_tiles, apack, bpack, rowmax, C, alpha, beta, s);
+  launch_oz_gemm(d_descs, d_groups, d_tiles, n_tiles, d_red, n_red, slots, apack, bpack, rowmax, C, alpha, beta, s);
 }
 
 }  // namespace xgb

@@ -924,15 +924,16 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
     auto* dg = upload(op.groups.data(), op.groups.size(), s);
     auto* dk = upload(op.tasks.data(), std::max<size_t>(op.tasks.size(), 1), s);
     auto* dt = upload(op.tiles.data(), op.tiles.size(), s);
+    auto* dr = upload(op.red.data(), std::max<size_t>(op.red.size(), 1), s);
     auto* rm = static_cast<unsigned long long*>(dev_alloc(sizeof(unsigned long long) * size_t(std::max<int64_t>(op.rowmax, 1))));
     auto* ap = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(op.a_bytes, 16))));
     auto* bp = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(op.b_bytes, 16))));
     prof_begin(K_GEMM_OZ, s);
-    launch_gemm_oz(dd, dg, dk, int(op.tasks.size()), dt, int(op.tiles.size()), A, B, rm, op.rowmax, ap, bp, C, alpha,
-                   beta, s);
+    launch_gemm_oz(dd, dg, dk, int(op.tasks.size()), dt, int(op.tiles.size()), dr, int(op.red.size()), op.slots, A, B,
+                   rm, op.rowmax, ap, bp, C, alpha, beta, s);
     prof_end(K_GEMM_OZ, s, flops);
     for (void* p : {static_cast<void*>(dd), static_cast<void*>(dg), static_cast<void*>(dk), static_cast<void*>(dt),
-                    static_cast<void*>(rm), static_cast<void*>(ap), static_cast<void*>(bp)})
+                    static_cast<void*>(dr), static_cast<void*>(rm), static_cast<void*>(ap), static_cast<void*>(bp)})
       dev_free(p);
     return check_cuda(cudaGetLastError(), "f64tc gemm launch");
   }

@@ -120,7 +120,9 @@ struct OzPlanHost {
   std::vector<OzGroup> groups;
   std::vector<TcPackTask> tasks;            // tasks_a then tasks_b
   std::vector<TcPackTask> tasks_a, tasks_b;  // the op(A) and op(B) chunks alone
-  std::vector<GemmTile> tiles;
+  std::vector<GemmTile> tiles;               // k0 / k1 in K slices; slot >= 0: split-K partial
+  std::vector<SplitReduce> red;              // fixed-order sums of the split tiles
+  int32_t slots = 0;                         // partial tiles (workspace slots x 128 x 64 doubles)
   int64_t a_bytes = 0, b_bytes = 0;
   int64_t rowmax = 0, rowmax_a = 0;  // entries in all; the op(A) rows come first
 };
@@ -129,13 +131,15 @@ OzPlanHost build_oz_plan(const xgb_gemm_desc* descs, int n);
 void launch_oz_pack(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
                     const double* A, const double* B, unsigned long long* rowmax, int64_t clear_from,
                     int64_t clear_count, unsigned char* apack, unsigned char* bpack, cudaStream_t s);
+// the product kernel (and, for split tiles, the fixed-order reduce; workspace allocated stream-ordered)
 void launch_oz_gemm(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const GemmTile* d_tiles, int n_tiles,
-                    const unsigned char* apack, const unsigned char* bpack, const unsigned long long* rowmax, double* C,
-                    double alpha, double beta, cudaStream_t s);
+                    const SplitReduce* d_red, int n_red, int slots, const unsigned char* apack,
+                    const unsigned char* bpack, const unsigned long long* rowmax, double* C, double alpha, double beta,
+                    cudaStream_t s);
 void launch_gemm_oz(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
-                    const GemmTile* d_tiles, int n_tiles, const double* A, const double* B,
-                    unsigned long long* rowmax, int64_t n_rowmax, unsigned char* apack, unsigned char* bpack,
-                    double* C, double alpha, double beta, cudaStream_t s);
+                    const GemmTile* d_tiles, int n_tiles, const SplitReduce* d_red, int n_red, int slots,
+                    const double* A, const double* B, unsigned long long* rowmax, int64_t n_rowmax,
+                    unsigned char* apack, unsigned char* bpack, double* C, double alpha, double beta, cudaStream_t s);
 
 // randomized tSVD helpers (rsvd.cu)
 struct GaussBlock { int64_t offset, count, stream; };       // fill out[offset .. offset+count) from stream
@@ -183,7 +187,11 @@ void prof_end(int kind, cudaStream_t s, double work);
 
 // FP64 grouped-GEMM launch shapes and their autotuner (autotune.cpp): tile edge 16/32/64 and a
 // split-K target of split_waves x SMs CTAs (0: no split)
-struct F64Config { int tile = 16; int split_waves = 0; };
+struct F64Config {
+  int tile = 16;
+  int split_waves = 0;
+  bool tc = false;  // the FP64-accurate tensor-core form (XGB_PREC_F64TC) instead of the CUDA-core kernel
+};
 struct F64Plan {
   int tile = 16;
   std::vector<GemmTile> tiles;
@@ -198,9 +206,17 @@ void run_f64_plan(const F64Plan& p, const xgb_gemm_desc* d_descs, const GemmTile
 void run_gemm_f64_config(const xgb_gemm_desc* h_descs, int n, F64Config c, const double* A, const double* B, double* C,
                          double alpha, double beta, cudaStream_t s);
 // the configuration to use for this list: tuned (measured on A, B the first time its size bucket is
-// met) when autotuning is on, `fallback` otherwise
+// met) when autotuning is on, `fallback` otherwise; allow_tc adds the FP64-accurate tensor-core form
+// to the candidates (callers that asked for FP64-class results on the tensor cores)
 F64Config gemm_f64_config(const xgb_gemm_desc* d, int n, const double* A, const double* B, F64Config fallback,
-                          cudaStream_t s);
+                          cudaStream_t s, bool allow_tc = false);
+// the FP64-accurate tensor-core GEMM of a host descriptor list (tables staged, pack buffers allocated
+// stream-ordered and freed)
+void run_gemm_oz_host(const xgb_gemm_desc* h_descs, int n, const double* A, const double* B, double* C, double alpha,
+                      double beta, cudaStream_t s);
+// built-in choice between the tensor-core form and the CUDA cores for a list whose caller allows both:
+// the tensor-core form pays a fixed cost per 128 x 64 tile that only k >= 64 amortises
+bool f64tc_heuristic(const xgb_gemm_desc* d, int n);
 int autotune_mode();
 
 // helpers

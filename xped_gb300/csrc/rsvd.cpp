@@ -131,6 +131,8 @@ class OzProducts {
   OzProducts(const std::vector<xgb_gemm_desc>& d, const double* A, cudaStream_t s) {
     const OzPlanHost op = build_oz_plan(d.data(), int(d.size()));
     n_tiles_ = int(op.tiles.size());
+    n_red_ = int(op.red.size());
+    slots_ = op.slots;
     n_b_ = int(op.tasks_b.size());
     rowmax_a_ = op.rowmax_a;
     rowmax_ = op.rowmax;
@@ -140,6 +142,7 @@ class OzProducts {
     oa_ = st_.add(op.tasks_a);
     ob_ = st_.add(op.tasks_b);
     ot_ = st_.add(op.tiles);
+    or_ = st_.add(op.red);
     st_.upload(s);
     rm_ = static_cast<unsigned long long*>(dev_alloc(sizeof(unsigned long long) * size_t(std::max<int64_t>(rowmax_, 1))));
     ap_ = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(op.a_bytes, 16))));
@@ -162,15 +165,15 @@ class OzProducts {
     prof_begin(K_GEMM_OZ, s);
     launch_oz_pack(st_.at<xgb_gemm_desc>(od_), st_.at<OzGroup>(og_), st_.at<TcPackTask>(ob_), n_b_, A, X, rm_,
                    rowmax_a_, rowmax_ - rowmax_a_, ap_, bp_, s);
-    launch_oz_gemm(st_.at<xgb_gemm_desc>(od_), st_.at<OzGroup>(og_), st_.at<GemmTile>(ot_), n_tiles_, ap_, bp_, rm_, C,
-                   1.0, 0.0, s);
+    launch_oz_gemm(st_.at<xgb_gemm_desc>(od_), st_.at<OzGroup>(og_), st_.at<GemmTile>(ot_), n_tiles_,
+                   st_.at<SplitReduce>(or_), n_red_, slots_, ap_, bp_, rm_, C, 1.0, 0.0, s);
     prof_end(K_GEMM_OZ, s, flops_);
   }
 
  private:
   Staging st_;
-  size_t od_ = 0, og_ = 0, oa_ = 0, ob_ = 0, ot_ = 0;
-  int n_tiles_ = 0, n_b_ = 0;
+  size_t od_ = 0, og_ = 0, oa_ = 0, ob_ = 0, ot_ = 0, or_ = 0;
+  int n_tiles_ = 0, n_b_ = 0, n_red_ = 0, slots_ = 0;
   int64_t rowmax_a_ = 0, rowmax_ = 0;
   double flops_ = 0;
   unsigned long long* rm_ = nullptr;

@@ -307,6 +307,52 @@ __global__ void __launch_bounds__(1024) chol_inv_kernel(const CholDesc* __restri
     chol_inv_body<false, kInverse>(d, G + d.g_off, Rinv + d.g_off, rel_shift, bad, sm);
 }
 
+// The same shifted Cholesky as chol_inv_body<true, false> for blocks up to kCholWarpL wide, run by one
+// warp per block with no block-wide barriers: the lanes own rows (i = lane + 32 j), every lane forms
+// the pivot itself, and each element sees the same FMAs in the same order as in the 1024-thread
+// kernel (the trace, which sets the shift, is summed in that kernel's order too), so both give the
+// same bits.  For narrow blocks the 1024-thread kernel spends two block barriers per column on a few
+// hundred FMAs; a lane's share grows like l^3 / 192 dependent shared-memory FMAs, so above 48 columns
+// (measured: ~390 us per launch at widths up to 128, against ~110 us) the block kernel is used.
+constexpr int kCholWarpL = 48;
+__global__ void __launch_bounds__(32) chol_warp_kernel(const CholDesc* __restrict__ descs, double* __restrict__ G,
+                                                       double rel_shift, int* __restrict__ bad) {
+  extern __shared__ double wsm[];
+  const CholDesc d = descs[blockIdx.x];
+  const int l = int(d.l), lane = threadIdx.x, ld = l | 1;
+  double* Gg = G + d.g_off;
+  auto LA = [&](int i, int k) -> double& { return wsm[i * ld + k]; };
+  for (int e = lane; e < l * l; e += 32) LA(e % l, e / l) = Gg[e];
+  __syncwarp();
+  double t = 0;
+  for (int g0 = 0; g0 < l; g0 += 32) t += warp_sum_d(g0 + lane < l ? LA(g0 + lane, g0 + lane) : 0.0);
+  const double shift = rel_shift * (double(d.m) * l + double(l) * (l + 1)) * t;
+  const double avg = t > 0.0 ? t / l : 0.0;
+  const double dfloor = fmax(2.220446049250313e-16 * avg, 1e-300);
+  for (int i = lane; i < l; i += 32) LA(i, i) += shift;
+  __syncwarp();
+  for (int j = 0; j < l; ++j) {
+    const double dj = LA(j, j);
+    const int dd = !(dj > dfloor);  // also true for NaN
+    const double p = sqrt(dd ? dfloor : dj);
+    const double inv = 1.0 / p;
+    __syncwarp();
+    if (lane == 0) {
+      LA(j, j) = p;
+      if (dd) atomicAdd(bad, 1);
+    }
+    for (int i = j + 1 + lane; i < l; i += 32) LA(i, j) = dd ? 0.0 : LA(i, j) * inv;
+    __syncwarp();
+    for (int i = j + 1 + lane; i < l; i += 32)
+      for (int k = j + 1; k <= i; ++k) LA(i, k) = fma(-LA(i, j), LA(k, j), LA(i, k));
+    __syncwarp();
+  }
+  for (int e = lane; e < l * l; e += 32) {
+    const int i = e % l, k = e / l;
+    if (i >= k) Gg[e] = LA(i, k);
+  }
+}
+
 // Rinv = L^-T from the Cholesky factor L (column-major, lower triangle, in G): one warp per
 // column c of X = L^-1, kTrinvCols columns per CTA, so the l^3/6 FMAs of a block spread over
 // ceil(l / kTrinvCols) SMs.  Column c by forward substitution in the same operation order as
@@ -390,9 +436,20 @@ void launch_chol_inv(const CholDesc* d_descs, int n, int64_t max_l, double* G, d
     count_launch();
     return;
   }
-  const int lc = int(std::min<int64_t>(max_l, kCapChol));
-  chol_inv_kernel<false><<<n, 1024, lc * (lc | 1) * int(sizeof(double)), s>>>(d_descs, G, Rinv, rel_shift, bad,
-                                                                                kCapChol);
+  if (max_l <= kCholWarpL) {
+    static bool wattr = false;
+    if (!wattr) {
+      cudaFuncSetAttribute(chol_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kCholWarpL * (kCholWarpL | 1) * int(sizeof(double)));
+      wattr = true;
+    }
+    const int lw = int(max_l);
+    chol_warp_kernel<<<n, 32, lw * (lw | 1) * int(sizeof(double)), s>>>(d_descs, G, rel_shift, bad);
+  } else {
+    const int lc = int(std::min<int64_t>(max_l, kCapChol));
+    chol_inv_kernel<false><<<n, 1024, lc * (lc | 1) * int(sizeof(double)), s>>>(d_descs, G, Rinv, rel_shift, bad,
+                                                                                  kCapChol);
+  }
   count_launch();
   const int chunks = int((max_l + kTrinvCols - 1) / kTrinvCols);
   if (max_l <= kTrinvStageL) {

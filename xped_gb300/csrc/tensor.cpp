@@ -143,9 +143,11 @@ struct GemmPlan {
   TcPackTask* d_tc_tasks = nullptr;
   GemmTile* d_tc_tiles = nullptr;
   std::vector<xgb_gemm_desc> host_descs;
-  // FP64-accurate tensor-core form from exact BF16 slices (built on first use)
-  bool oz_ready = false;
-  int n_oz_tiles = 0, n_oz_tasks = 0;
+  // FP64-accurate tensor-core form from exact BF16 slices (built on first use); oz_route: whether
+  // this product takes it (k too short to amortise the per-tile cost: the FP64 CUDA-core kernel)
+  bool oz_ready = false, oz_route = true, oz_routed = false;
+  int n_oz_tiles = 0, n_oz_tasks = 0, n_oz_red = 0, oz_slots = 0;
+  SplitReduce* d_oz_red = nullptr;
   int64_t oz_a_bytes = 0, oz_b_bytes = 0, oz_rowmax = 0;
   OzGroup* d_oz_groups = nullptr;
   TcPackTask* d_oz_tasks = nullptr;
@@ -419,6 +421,7 @@ void clear_plan_caches() {
     cudaFree(p->d_oz_groups);
     cudaFree(p->d_oz_tasks);
     cudaFree(p->d_oz_tiles);
+    cudaFree(p->d_oz_red);
   }
   g_perm_plans.clear();
   g_gemm_plans.clear();
@@ -626,7 +629,18 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
     dev_free(bp);
     return out;
   }
-  if (g_gemm_precision == XGB_PREC_F64TC) {
+  if (g_gemm_precision == XGB_PREC_F64TC && !plan->oz_routed) {
+    // both routes are FP64-class: the tensor-core form or the FP64 CUDA-core kernel, whichever the
+    // autotuner measures faster for this size bucket (built-in rule: average k >= 64)
+    const auto& hd = plan->host_descs;
+    const F64Config rc = gemm_f64_config(hd.data(), int(hd.size()), a.data(), b.data(),
+                                         F64Config{plan->f64.tile, 0, f64tc_heuristic(hd.data(), int(hd.size()))},
+                                         stream(), true);
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    plan->oz_route = rc.tc;
+    plan->oz_routed = true;
+  }
+  if (g_gemm_precision == XGB_PREC_F64TC && plan->oz_route) {
     {
       std::lock_guard<std::mutex> lk(g_plan_mu);
       if (!plan->oz_ready) {
@@ -639,6 +653,9 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
         plan->d_oz_groups = dev_table(op.groups);
         plan->d_oz_tasks = dev_table(op.tasks);
         plan->d_oz_tiles = dev_table(op.tiles);
+        plan->d_oz_red = dev_table(op.red);
+        plan->n_oz_red = int(op.red.size());
+        plan->oz_slots = op.slots;
         plan->oz_ready = true;
       }
     }
@@ -649,7 +666,8 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
     auto* bp = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(plan->oz_b_bytes, 16))));
     prof_begin(K_GEMM_OZ, st);
     launch_gemm_oz(plan->d_descs, plan->d_oz_groups, plan->d_oz_tasks, plan->n_oz_tasks, plan->d_oz_tiles,
-                   plan->n_oz_tiles, a.data(), b.data(), rm, plan->oz_rowmax, ap, bp, out.data(), 1.0, 0.0, st);
+                   plan->n_oz_tiles, plan->d_oz_red, plan->n_oz_red, plan->oz_slots, a.data(), b.data(), rm,
+                   plan->oz_rowmax, ap, bp, out.data(), 1.0, 0.0, st);
     prof_end(K_GEMM_OZ, st, plan->flops);
     dev_free(rm);
     dev_free(ap);
