@@ -182,6 +182,8 @@ def run_gpu(args):
     L.xgb_synchronize()
     records = ctm.records()
     ctm.record(False)
+    if args.autotune:
+        L.xgb_autotune_set(2)  # frozen: no measurement inside the timed steps
     res["chosen_setup_s"] = time.perf_counter() - t0
     res["autotune"] = autotune_report(L)
 
@@ -357,6 +359,39 @@ def run_gpu(args):
         res["tsvd_sweep"] = tsvd_sweep(eval_seeds=(0, 1), train_seeds=tuple(range(100, 106)), steps=4)
         res["fz2"] = fz2_compact(args)
     return res
+
+
+def profile_step(args):
+    """One chosen-form step of the headline workload after `warmup` steps, bracketed by the CUDA runtime's
+    profiler start / stop so that a profiler started with profiling off captures exactly its launches."""
+    import ctypes as C
+    from xped_gb300 import ensure_device, lib
+    ensure_device(dist_info()[2])
+    L = lib()
+    if args.autotune:
+        L.xgb_autotune_set(1)
+    A, _ = site_tensor(AUX)
+    c = make_ctm(A, CHI, "chosen", args.gemm, args.sketch_tail)
+    for _ in range(args.warmup):
+        c.grow_all()
+    L.xgb_synchronize()
+    if args.autotune:
+        L.xgb_autotune_set(2)
+    rt = None
+    with open("/proc/self/maps") as f:  # the CUDA runtime the library itself loaded
+        for line in f:
+            if "libcudart.so" in line:
+                rt = C.CDLL(line.split()[-1])
+                break
+    n0 = L.xgb_launch_count()
+    rt.cudaProfilerStart()
+    L.xgb_event_record(0)
+    c.grow_all()
+    L.xgb_event_record(1)
+    L.xgb_synchronize()
+    rt.cudaProfilerStop()
+    return {"ms": L.xgb_event_elapsed_ms(0, 1), "launches": L.xgb_launch_count() - n0, "gemm": args.gemm,
+            "workload": WORKLOAD}
 
 
 def dtype_label(args):
@@ -1015,7 +1050,8 @@ def roofline(prof, steps, fp64_peak=None):
         out = {"bound": "tensor", "kernel": dom, "achieved": 28.0 * useful, "peak": bf, "unit": "TFLOP/s",
                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if "bf16_tflops" in peaks else "fallback 1900",
                "work": "BF16 products issued: 28 slice products per useful FP64 flop (slicing launches included)",
-               "useful_fp64_equivalent_tflops": useful}
+               "useful_fp64_equivalent_tflops": useful,
+               "useful_vs_fp64_peak": useful / fp64_peak if fp64_peak else None}
     elif dom == "gemm_tc":
         tf = peaks.get("bf16_tflops", 1900.0) / 2.0  # dense TF32 issues at half the BF16 rate
         achieved = per_launch_work / (per_launch_ms * 1e-3) / 1e12
@@ -1032,6 +1068,9 @@ def roofline(prof, steps, fp64_peak=None):
     traffic = {"svd_jacobi": (0.355e6, "ncu capture of one svd_cluster_kernel launch of the projected l x l "
                                        "factors, U(1) D=6 chi=128 (dram__bytes_read.sum 322 KB + write 33 KB)"),
                "gemm_tc": (7.025e9, "ncu capture, SU(2) Tensor<2,2> product (6.613 GB read + 0.412 GB written)"),
+               "gemm_f64tc": (68.27e6, "ncu one-pass capture of the 76 oz_gemm_kernel launches of one chosen U(1) D=6 "
+                                       "chi=128 step (bench.py --profile-step): 67.44 MB read + 0.83 MB written per "
+                                       "launch, average (the packed slices of the sector blocks)"),
                "gemm_f64": (14.10e6, "ncu one-pass capture of 348 consecutive gemm_simt_kernel launches of the "
                                      "chosen U(1) D=6 chi=128 run (dram read + write per launch, average; the "
                                      "operands are L2-resident after their first touch)")}
@@ -1117,6 +1156,9 @@ def main():
     ap.add_argument("--u1-product", default=None, metavar="DEGS",
                     help="time only T1*T2 of U(1) Tensor<2,2> operands with these leg degeneracies (e.g. 6,12,16,12,6)")
     ap.add_argument("--reps", type=int, default=10, help="products timed by --u1-product")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="warm up the chosen form, then run one step between cudaProfilerStart / Stop (for ncu "
+                         "--profile-from-start off) and print its CUDA-event time")
     ap.add_argument("--permute-only", action="store_true",
                     help="run only the permute HBM roofline case (1.42 GB U(1) Tensor<2,2>) and print it")
     ap.add_argument("--permute-degs", default="20,40,60,40,20",
@@ -1170,6 +1212,10 @@ def main():
         ensure_device(local)
         print(json.dumps({"u1_product": u1_product([int(x) for x in args.u1_product.split(",")], args.reps,
                                                      args.gemm)}))
+        return
+
+    if args.profile_step:
+        print(json.dumps({"profiled_step": profile_step(args)}))
         return
 
     if args.permute_only:

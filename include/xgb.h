@@ -112,7 +112,9 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
    (xgb_autotune_candidates lists them).  mode 1: the first GEMM list of a size bucket (group
    count, total flops, largest block area, longest k on a log2 scale) times every candidate on its
    own operands (CUDA events on the launching stream, output into scratch memory) and the fastest
-   is cached for the bucket; mode 0 (default): the built-in rule of each call site.
+   is cached for the bucket; mode 2 (frozen): cached choices, the built-in rule for unseen buckets and
+   no measurement (for timed regions after a tuning warm-up); mode 0 (default): the built-in rule of
+   each call site.
    xgb_autotune_save / _load write / read the cache as text lines keyed by the GPU's name (entries
    of other GPU models are skipped; load returns the number of entries taken).  xgb_autotune_stats
    returns the number of cached buckets (and, if non-NULL, buckets measured, cache hits and the

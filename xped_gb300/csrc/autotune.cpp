@@ -49,7 +49,7 @@ struct Key {
 };
 
 std::mutex g_mu;
-int g_mode = 0;  // 0 off, 1 on
+int g_mode = 0;  // 0 off, 1 on (measure unseen buckets), 2 frozen (cached choices only)
 std::map<Key, F64Config> g_cache;
 int64_t g_tuned = 0, g_hits = 0;
 double g_tune_ms = 0.0;
@@ -215,6 +215,7 @@ F64Config gemm_f64_config(const xgb_gemm_desc* d, int n, const double* A, const 
       ++g_hits;
       return it->second;
     }
+    if (g_mode == 2) return fallback;  // frozen: no measurement, the built-in rule for unseen buckets
   }
   double times[kNumCandidates + 1];
   cudaEvent_t t0, t1;
@@ -258,7 +259,7 @@ using namespace xgb;
 extern "C" {
 
 int xgb_autotune_set(int mode) {
-  if (mode != 0 && mode != 1) return set_error(XGB_E_BADPLAN, "autotune mode must be 0 (off) or 1 (on)");
+  if (mode < 0 || mode > 2) return set_error(XGB_E_BADPLAN, "autotune mode must be 0 (off), 1 (on) or 2 (frozen)");
   autotune_set_mode(mode);
   return XGB_OK;
 }
