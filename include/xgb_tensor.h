@@ -86,6 +86,11 @@ xgb_tensor xgb_tensor_normalize_max(xgb_tensor t);                              
 /* Tensor::tSVD (Tensor.cpp:478-633); keep[] (may be NULL, one per input sector) gets kept counts */
 int xgb_tensor_tsvd(xgb_tensor t, int64_t max_keep, double eps_svd, int preserve_multiplets, xgb_tensor* U,
                     xgb_tensor* S, xgb_tensor* Vdag, double* trunc_weight, double* entropy, int32_t* keep);
+/* The SVspec map of Tensor::tSVD with RETURN_SPEC (src/Core/Tensor.cpp:486-491,618-624) from the truncated
+   singular-value tensor S of xgb_tensor_tsvd: per sector its charge (qs[i]), and its kept values
+   (descending) at values[begin[i] .. begin[i+1]); begin has n + 1 entries, values up to cap.  Returns the
+   number of sectors n (any output pointer may be NULL to query the sizes). */
+int xgb_tensor_svspec(xgb_tensor S, int32_t* qs, int64_t* begin, double* values, int64_t cap);
 /* Randomized blockwise tSVD with per-sector sketch widths (no counterpart in the
    reference; its results follow Tensor::tSVD's cutoff_matrices semantics).
    sketch[i] <= 0 or 2*sketch[i] >= min(rows, cols) decomposes sector i exactly;

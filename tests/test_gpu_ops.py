@@ -137,6 +137,22 @@ def test_tsvd_truncation_edge_cases():
         assert_same(nV, oV, 1e-9, 1e-9)
 
 
+def test_tsvd_return_spec_matches_oracle():
+    """RETURN_SPEC (Tensor.cpp:618-624): the per-sector kept singular values (SVspec) of the device tSVD
+    against the oracle's cutoff_matrices with return_spec."""
+    rng = np.random.default_rng(12)
+    s, oB, nB = pair_basis("u1", [(-1, 3), (0, 5), (1, 2)], sort=True)
+    ot = oracle.Tensor(s, [oB, oB], [oB, oB]).set_random(rng)
+    nt = to_native(ot, [nB, nB], [nB, nB])
+    for keep in (5, 17, 1000):
+        *_, ospec = ot.tsvd(keep, 1e-10, return_spec=True)
+        nspec = nt.tSVD(keep, 1e-10)[1].svspec()
+        assert sorted(nspec) == sorted(ospec)
+        for q, v in ospec.items():
+            assert nspec[q].shape == v.shape
+            assert np.abs(nspec[q] - v).max() <= 1e-10 * max(1.0, float(np.abs(v).max()))
+
+
 def test_tsvd_preserve_multiplets_matches_oracle():
     """PRESERVE_MULTIPLETS (Tensor.cpp:568-582) on designed spectra: the kept
     list of 6 is cut back to 4 at the last relative gap above 0.1; truncWeight

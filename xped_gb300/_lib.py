@@ -131,6 +131,7 @@ PROTOS = [
     ("xgb_ctm_record_get", C.c_int, [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), i64p, i32p,
                                      C.POINTER(C.c_float), i64p, i64p, i64p, dblp, i64p]),
     ("xgb_ctm_rdm", P, [P, C.c_int]),
+    ("xgb_tensor_svspec", C.c_int, [P, i32p, i64p, dblp, C.c_int64]),
     ("xgb_ctm_solve", C.c_int, [P, P, C.c_double, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int),
                                 C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_int]),
     ("xgb_rank_model_num_params", C.c_int, []),

@@ -164,6 +164,32 @@ int xgb_tensor_download(xgb_tensor t, double* host, int64_t n) {
   })
 }
 
+int xgb_tensor_svspec(xgb_tensor S, int32_t* qs, int64_t* begin, double* values, int64_t cap) {
+  // the SVspec map of Tensor::tSVD with RETURN_SPEC (src/Core/Tensor.cpp:618-624): per sector of the
+  // truncated singular-value tensor, the diagonal of its block (the kept values, descending)
+  GUARD(XGB_E_CUDA, {
+    const TensorMeta& m = *S->t.meta;
+    const int n = int(m.sectors.size());
+    std::vector<double> h(size_t(S->t.size()));
+    Tensor mt = materialize(S->t);
+    if (!h.empty()) {
+      cudaError_t e = cudaMemcpyAsync(h.data(), mt.data(), sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream());
+      if (e == cudaSuccess) e = cudaStreamSynchronize(stream());
+      if (e != cudaSuccess) return set_error(XGB_E_CUDA, cudaGetErrorString(e));
+    }
+    int64_t pos = 0;
+    for (int i = 0; i < n; ++i) {
+      const int64_t k = std::min(m.rows[i], m.cols[i]);
+      if (qs) qs[i] = m.sectors[i];
+      if (begin) begin[i] = pos;
+      for (int64_t j = 0; j < k; ++j, ++pos)
+        if (values && pos < cap) values[pos] = h[size_t(m.offset[i] + j + j * m.rows[i])];
+    }
+    if (begin) begin[n] = pos;
+    return n;
+  })
+}
+
 double* xgb_tensor_device_data(xgb_tensor t) {
   GUARD(nullptr, {
     t->t = materialize(t->t);

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -292,14 +293,23 @@ int choose_gemm_tile(const xgb_gemm_desc* descs, int n) {
 // order.
 constexpr int kRowsPerChunk = 8;
 
+// Row cursor with the current task's extents, strides and coefficient held in registers (loaded
+// once per task, not per row): SI is int32_t when every stride of the plan fits (the host checks),
+// int64_t otherwise.  All per-leg arrays are indexed only inside fully unrolled loops.
+template <typename SI>
 struct RowCursor {
-  int ti = -1;            // task
-  int64_t row_end = 0;    // first row past the task
-  int idx[XGB_MAX_LEGS];  // multi-index of legs 1..rank-1
+  int ti = -1;          // task
+  int64_t row_end = 0;  // first row past the task
+  int rank = 0, d0 = 1, n_contrib = 1, contrib0 = 0;
+  double coeff = 0.0;
+  int dims[XGB_MAX_LEGS];
+  SI dstr[XGB_MAX_LEGS], sstr[XGB_MAX_LEGS];  // sstr: strides of the single contribution
+  int idx[XGB_MAX_LEGS];                      // multi-index of legs 1..rank-1
   int64_t dofs = 0, sofs = 0;
 };
 
-__device__ __forceinline__ void cursor_seek(RowCursor& c, const xgb_perm_task* __restrict__ tasks,
+template <typename SI>
+__device__ __forceinline__ void cursor_seek(RowCursor<SI>& c, const xgb_perm_task* __restrict__ tasks,
                                             const int64_t* __restrict__ row_start, int n_tasks,
                                             const xgb_perm_contrib* __restrict__ contribs, int64_t r) {
   int ti = c.ti >= 0 ? c.ti : 0;
@@ -312,43 +322,64 @@ __device__ __forceinline__ void cursor_seek(RowCursor& c, const xgb_perm_task* _
     ti = lo;
   }
   const xgb_perm_task& t = tasks[ti];
-  c.ti = ti;
-  c.row_end = row_start[ti + 1];
+  if (ti != c.ti) {  // task fields into registers
+    c.ti = ti;
+    c.row_end = row_start[ti + 1];
+    c.rank = t.rank;
+    c.d0 = t.rank > 0 ? t.dims[0] : 1;
+    c.n_contrib = t.n_contrib;
+    c.contrib0 = t.contrib0;
+    const bool single = t.n_contrib == 1;
+    c.coeff = single ? contribs[t.contrib0].coeff : 0.0;
+#pragma unroll
+    for (int k = 0; k < XGB_MAX_LEGS; ++k) {
+      const bool on = k < t.rank;
+      c.dims[k] = on ? t.dims[k] : 1;
+      c.dstr[k] = on ? SI(t.dst_stride[k]) : SI(0);
+      c.sstr[k] = (on && single) ? SI(contribs[t.contrib0].src_stride[k]) : SI(0);
+    }
+  }
   int64_t rem = r - row_start[ti];
   c.dofs = t.dst_base;
-  const bool single = t.n_contrib == 1;
-  c.sofs = single ? contribs[t.contrib0].src_base : 0;
-  for (int k = 1; k < t.rank; ++k) {
-    const int dk = t.dims[k];
-    int ik;
-    if (rem < (int64_t(1) << 31)) {  // 32-bit division for the common case
-      const uint32_t r32 = uint32_t(rem), q = r32 / uint32_t(dk);
-      ik = int(r32 - q * uint32_t(dk));
-      rem = q;
-    } else {
-      const int64_t q = rem / dk;
-      ik = int(rem - q * dk);
-      rem = q;
+  c.sofs = c.n_contrib == 1 ? contribs[c.contrib0].src_base : 0;
+#pragma unroll
+  for (int k = 1; k < XGB_MAX_LEGS; ++k) {
+    c.idx[k] = 0;
+    if (k < c.rank) {
+      const int dk = c.dims[k];
+      int ik;
+      if (rem < (int64_t(1) << 31)) {  // 32-bit division for the common case
+        const uint32_t r32 = uint32_t(rem), q = r32 / uint32_t(dk);
+        ik = int(r32 - q * uint32_t(dk));
+        rem = q;
+      } else {
+        const int64_t q = rem / dk;
+        ik = int(rem - q * dk);
+        rem = q;
+      }
+      c.idx[k] = ik;
+      c.dofs += int64_t(ik) * c.dstr[k];
+      c.sofs += int64_t(ik) * c.sstr[k];
     }
-    c.idx[k] = ik;
-    c.dofs += ik * t.dst_stride[k];
-    if (single) c.sofs += ik * contribs[t.contrib0].src_stride[k];
   }
 }
 
 // next row of the same task: leg 1 fastest, carrying into the higher legs
-__device__ __forceinline__ void cursor_step(RowCursor& c, const xgb_perm_task& t, const xgb_perm_contrib* cc) {
-  for (int k = 1; k < t.rank; ++k) {
-    c.dofs += t.dst_stride[k];
-    if (cc) c.sofs += cc->src_stride[k];
-    if (++c.idx[k] < t.dims[k]) return;
+template <typename SI>
+__device__ __forceinline__ void cursor_step(RowCursor<SI>& c) {
+#pragma unroll
+  for (int k = 1; k < XGB_MAX_LEGS; ++k) {
+    if (k >= c.rank) return;
+    c.dofs += c.dstr[k];
+    c.sofs += c.sstr[k];
+    if (++c.idx[k] < c.dims[k]) return;
     c.idx[k] = 0;
-    c.dofs -= int64_t(t.dims[k]) * t.dst_stride[k];
-    if (cc) c.sofs -= int64_t(t.dims[k]) * cc->src_stride[k];
+    c.dofs -= int64_t(c.dims[k]) * c.dstr[k];
+    c.sofs -= int64_t(c.dims[k]) * c.sstr[k];
   }
 }
 
-template <int G>
+template <int G, typename SI>
 __global__ void __launch_bounds__(256) permute_rows_kernel(const xgb_perm_task* __restrict__ tasks,
                                                            const int64_t* __restrict__ row_start, int n_tasks,
                                                            int64_t total_rows, const xgb_perm_contrib* __restrict__ contribs,
@@ -358,51 +389,51 @@ __global__ void __launch_bounds__(256) permute_rows_kernel(const xgb_perm_task* 
   const int64_t group = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) / G;
   const int64_t ngroups = int64_t(gridDim.x) * blockDim.x / G;
   const int64_t nchunks = (total_rows + kRowsPerChunk - 1) / kRowsPerChunk;
-  RowCursor cur;
+  RowCursor<SI> cur;
   for (int64_t chunk = group; chunk < nchunks; chunk += ngroups) {
     const int64_t r0 = chunk * kRowsPerChunk;
     const int64_t r1 = r0 + kRowsPerChunk < total_rows ? r0 + kRowsPerChunk : total_rows;
     cursor_seek(cur, tasks, row_start, n_tasks, contribs, r0);
     for (int64_t rb = r0; rb < r1; rb += U) {
-      int64_t doff[U], soff[U], ds0[U], ss0[U];
+      int64_t doff[U], soff[U];
+      SI ds0[U], ss0[U];
       double coeff[U];
       int len[U];
       int maxlen = 0;
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         len[u] = 0;
-        doff[u] = soff[u] = ds0[u] = ss0[u] = 0;
+        doff[u] = soff[u] = 0;
+        ds0[u] = ss0[u] = 0;
         coeff[u] = 0.0;
         const int64_t r = rb + u;
         if (r >= r1) continue;
         if (r >= cur.row_end) cursor_seek(cur, tasks, row_start, n_tasks, contribs, r);
-        const xgb_perm_task& t = tasks[cur.ti];
-        const int d0 = t.rank > 0 ? t.dims[0] : 1;
-        const int64_t dstr0 = t.rank > 0 ? t.dst_stride[0] : 0;
-        if (t.n_contrib == 1) {
-          const xgb_perm_contrib& cc = contribs[t.contrib0];
+        if (cur.n_contrib == 1) {
           doff[u] = cur.dofs;
           soff[u] = cur.sofs;
-          ds0[u] = dstr0;
-          ss0[u] = t.rank > 0 ? cc.src_stride[0] : 0;
-          coeff[u] = cc.coeff;
-          len[u] = d0;
-          maxlen = max(maxlen, d0);
-          cursor_step(cur, t, &cc);
+          ds0[u] = cur.dstr[0];
+          ss0[u] = cur.sstr[0];
+          coeff[u] = cur.coeff;
+          len[u] = cur.d0;
+          maxlen = max(maxlen, cur.d0);
+          cursor_step(cur);
           continue;
         }
         // several source sub-blocks add into this row (SU(2)): fixed contribution order
-        for (int i = lane; i < d0; i += G) {
+        for (int i = lane; i < cur.d0; i += G) {
           double v = 0.0;
-          for (int c = 0; c < t.n_contrib; ++c) {
-            const xgb_perm_contrib& cc = contribs[t.contrib0 + c];
-            int64_t so = cc.src_base + int64_t(i) * (t.rank > 0 ? cc.src_stride[0] : 0);
-            for (int k = 1; k < t.rank; ++k) so += cur.idx[k] * cc.src_stride[k];
+          for (int c = 0; c < cur.n_contrib; ++c) {
+            const xgb_perm_contrib& cc = contribs[cur.contrib0 + c];
+            int64_t so = cc.src_base + int64_t(i) * (cur.rank > 0 ? cc.src_stride[0] : 0);
+#pragma unroll
+            for (int k = 1; k < XGB_MAX_LEGS; ++k)
+              if (k < cur.rank) so += cur.idx[k] * cc.src_stride[k];
             v = fma(cc.coeff, __ldg(src + so), v);
           }
-          dst[cur.dofs + int64_t(i) * dstr0] = v;
+          dst[cur.dofs + int64_t(i) * cur.dstr[0]] = v;
         }
-        cursor_step(cur, t, nullptr);
+        cursor_step(cur);
       }
       for (int i = lane; i < maxlen; i += G) {
         double v[U];
@@ -417,7 +448,7 @@ __global__ void __launch_bounds__(256) permute_rows_kernel(const xgb_perm_task* 
   }
 }
 
-PermRows perm_rows(const xgb_perm_task* tasks, int n_tasks) {
+PermRows perm_rows(const xgb_perm_task* tasks, int n_tasks, const xgb_perm_contrib* contribs, int n_contrib) {
   PermRows r;
   r.row_start.assign(size_t(n_tasks) + 1, 0);
   double elems = 0, weighted = 0;
@@ -429,14 +460,22 @@ PermRows perm_rows(const xgb_perm_task* tasks, int n_tasks) {
     weighted += double(tasks[t].nelem) * double(d0);
   }
   r.total_rows = r.row_start.back();
+  auto wide = [](int64_t v) { return v > INT32_MAX || v < INT32_MIN; };
+  for (int t = 0; t < n_tasks && r.narrow; ++t)
+    for (int k = 0; k < tasks[t].rank; ++k)
+      if (wide(tasks[t].dst_stride[k])) r.narrow = false;
+  for (int c = 0; c < n_contrib && r.narrow; ++c)
+    for (int k = 0; k < XGB_MAX_LEGS; ++k)
+      if (wide(contribs[c].src_stride[k])) r.narrow = false;
   const double avg = elems > 0 ? weighted / elems : 1.0;  // element-weighted row length
   r.group = 1;
   while (r.group < 32 && 2.0 * r.group <= avg * 1.25) r.group *= 2;
   return r;
 }
 
-void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_row_start, int n_tasks, int64_t total_rows,
-                    int group, const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s) {
+template <typename SI>
+void launch_permute_t(const xgb_perm_task* d_tasks, const int64_t* d_row_start, int n_tasks, int64_t total_rows,
+                      int group, const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s) {
   if (total_rows <= 0 || n_tasks <= 0) return;
   // one group per chunk of kRowsPerChunk rows; enough CTAs to fill the GPU a few times over
   const int64_t groups_needed = (total_rows + kRowsPerChunk - 1) / kRowsPerChunk;
@@ -444,14 +483,21 @@ void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_row_start, in
   const int64_t cap = int64_t(num_sms() > 0 ? num_sms() : 152) * 16;
   const unsigned blocks = unsigned(std::max<int64_t>(1, std::min<int64_t>(cap, (groups_needed + per_block - 1) / per_block)));
   switch (group) {
-    case 32: permute_rows_kernel<32><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
-    case 16: permute_rows_kernel<16><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
-    case 8: permute_rows_kernel<8><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
-    case 4: permute_rows_kernel<4><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
-    case 2: permute_rows_kernel<2><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
-    default: permute_rows_kernel<1><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case 32: permute_rows_kernel<32, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case 16: permute_rows_kernel<16, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case 8: permute_rows_kernel<8, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case 4: permute_rows_kernel<4, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case 2: permute_rows_kernel<2, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    default: permute_rows_kernel<1, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
   }
   count_launch();
+}
+
+void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_row_start, int n_tasks, int64_t total_rows,
+                    int group, bool narrow, const xgb_perm_contrib* d_contribs, const double* src, double* dst,
+                    cudaStream_t s) {
+  if (narrow) launch_permute_t<int32_t>(d_tasks, d_row_start, n_tasks, total_rows, group, d_contribs, src, dst, s);
+  else launch_permute_t<int64_t>(d_tasks, d_row_start, n_tasks, total_rows, group, d_contribs, src, dst, s);
 }
 
 // ======================================================================= shared helpers
@@ -1010,12 +1056,12 @@ int xgb_permute(int n_tasks, const xgb_perm_task* tasks, int n_contrib, const xg
     if (prod != tasks[t].nelem) return set_error(XGB_E_BADPLAN, "task nelem differs from the product of its extents");
   }
   if (n_tasks == 0) return XGB_OK;
-  const PermRows rows = perm_rows(tasks, n_tasks);
+  const PermRows rows = perm_rows(tasks, n_tasks, contribs, n_contrib);
   if (rows.total_rows == 0) return XGB_OK;
   auto* dt = upload(tasks, size_t(n_tasks), s);
   auto* ds = upload(rows.row_start.data(), rows.row_start.size(), s);
   auto* dc = upload(contribs, size_t(n_contrib), s);
-  launch_permute(dt, ds, n_tasks, rows.total_rows, rows.group, dc, src, dst, s);
+  launch_permute(dt, ds, n_tasks, rows.total_rows, rows.group, rows.narrow, dc, src, dst, s);
   dev_free(dt);
   dev_free(ds);
   dev_free(dc);

@@ -191,15 +191,28 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   if (kInverse)
     for (int e = tid; e < l * l; e += nt) XA(e % l, e / l) = (e % l == e / l) ? 1.0 : 0.0;
   __syncthreads();
-  double tr = 0;
-  for (int i = tid; i < l; i += nt) tr += LA(i, i);
-  tr = warp_sum_d(tr);
-  if (lane == 0) red[warp] = tr;
+  // the trace in the order of a 1024-thread block whatever blockDim is (one element per thread, butterfly
+  // sums per 32 elements, added in order), so that blocks of any size give the same shift and the same bits
+  __shared__ double trace_s;
+  if (l <= 1024) {
+    if (warp == 0) {
+      double t = 0;
+      for (int g0 = 0; g0 < l; g0 += 32) t += warp_sum_d(g0 + lane < l ? LA(g0 + lane, g0 + lane) : 0.0);
+      if (lane == 0) trace_s = t;
+    }
+  } else {
+    double tr = 0;
+    for (int i = tid; i < l; i += nt) tr += LA(i, i);
+    tr = warp_sum_d(tr);
+    if (lane == 0) red[warp] = tr;
+  }
   __syncthreads();
   __shared__ double floor_s;
   if (tid == 0) {
     double t = 0;
-    for (int w = 0; w < (nt >> 5); ++w) t += red[w];
+    if (l <= 1024) t = trace_s;
+    else
+      for (int w = 0; w < (nt >> 5); ++w) t += red[w];
     bcast = rel_shift * (double(d.m) * l + double(l) * (l + 1)) * t;
     const double avg = t > 0.0 ? t / l : 0.0;
     floor_s = fmax(2.220446049250313e-16 * avg, 1e-300);
@@ -446,6 +459,8 @@ void launch_chol_inv(const CholDesc* d_descs, int n, int64_t max_l, double* G, d
     const int lw = int(max_l);
     chol_warp_kernel<<<n, 32, lw * (lw | 1) * int(sizeof(double)), s>>>(d_descs, G, rel_shift, bad);
   } else {
+    // 1024 threads: the rank-1 update of a column is spread thinnest (measured: 128 / 256 threads per block
+    // made the CTM step's factorisations 55 % slower at widths 48-130)
     const int lc = int(std::min<int64_t>(max_l, kCapChol));
     chol_inv_kernel<false><<<n, 1024, lc * (lc | 1) * int(sizeof(double)), s>>>(d_descs, G, Rinv, rel_shift, bad,
                                                                                   kCapChol);

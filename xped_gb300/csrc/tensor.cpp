@@ -124,6 +124,7 @@ struct PermPlan {
   int n_tasks = 0;
   int64_t total_rows = 0;
   int group = 1;
+  bool narrow = true;
   xgb_perm_task* d_tasks = nullptr;
   int64_t* d_row_start = nullptr;
   xgb_perm_contrib* d_contribs = nullptr;
@@ -163,9 +164,10 @@ std::shared_ptr<PermPlan> upload_tables(const PermTables& t) {
   plan->n_tasks = int(t.tasks.size());
   plan->needs_zero = t.needs_zero;
   plan->d_tasks = dev_table(t.tasks);
-  const PermRows rows = perm_rows(t.tasks.data(), int(t.tasks.size()));
+  const PermRows rows = perm_rows(t.tasks.data(), int(t.tasks.size()), t.contribs.data(), int(t.contribs.size()));
   plan->total_rows = rows.total_rows;
   plan->group = rows.group;
+  plan->narrow = rows.narrow;
   plan->d_row_start = dev_table(rows.row_start);
   plan->d_contribs = dev_table(t.contribs);
   for (const auto& task : t.tasks) plan->bytes += 8.0 * double(task.nelem) * (1 + task.n_contrib);
@@ -400,8 +402,8 @@ std::shared_ptr<PermPlan> get_perm_plan(const TensorMeta& m, uint32_t mask, int 
 Tensor run_perm_plan(const PermPlan& plan, const Tensor& src) {
   Tensor out = plan.needs_zero ? zeros(plan.out) : empty_like_meta(plan.out);
   prof_begin(K_PERMUTE, stream());
-  launch_permute(plan.d_tasks, plan.d_row_start, plan.n_tasks, plan.total_rows, plan.group, plan.d_contribs, src.data(),
-                 out.data(), stream());
+  launch_permute(plan.d_tasks, plan.d_row_start, plan.n_tasks, plan.total_rows, plan.group, plan.narrow,
+                 plan.d_contribs, src.data(), out.data(), stream());
   prof_end(K_PERMUTE, stream(), plan.bytes);
   return out;
 }

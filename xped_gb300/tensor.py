@@ -253,6 +253,18 @@ class Tensor:
                                     C.byref(S), C.byref(V), C.byref(tw), C.byref(ent), keep), "tSVD")
         return Tensor(U.value), Tensor(S.value), Tensor(V.value), tw.value, ent.value, list(keep[:n])
 
+    def svspec(self):
+        """SVspec of Tensor::tSVD with RETURN_SPEC (src/Core/Tensor.cpp:618-624) for a singular-value tensor
+        returned by tSVD: {charge: kept values, descending}."""
+        n = check(lib().xgb_tensor_svspec(self._h, None, None, None, 0), "svspec")
+        qs = (C.c_int32 * max(n, 1))()
+        begin = (C.c_int64 * (n + 1))()
+        lib().xgb_tensor_svspec(self._h, qs, begin, None, 0)
+        vals = np.zeros(max(begin[n], 1))
+        check(lib().xgb_tensor_svspec(self._h, qs, begin, vals.ctypes.data_as(C.POINTER(C.c_double)), begin[n]),
+              "svspec")
+        return {int(qs[i]): vals[begin[i]:begin[i + 1]].copy() for i in range(n)}
+
     def tSVD_randomized(self, max_keep: int, eps_svd: float, sketch: Sequence[int], power_iters: int = 1,
                         seed: int = 0, warm: "Tensor" = None, res_tol: float = 0.0):
         """Randomized blockwise tSVD: ``sketch[i]`` Gaussian columns for sector i
