@@ -433,7 +433,9 @@ __global__ void __launch_bounds__(256) oz_splitk_reduce_kernel(const xgb_gemm_de
                                                                 double alpha, double beta) {
   const SplitReduce r = red[blockIdx.x];
   const xgb_gemm_desc d = descs[r.g];
-  for (int e = threadIdx.x; e < OM * ON; e += blockDim.x) {
+  // blockIdx.y: a 1024-element part of the tile (eight CTAs per tile keep the sums spread over the SMs)
+  const int e0 = int(blockIdx.y) * 1024, e1 = e0 + 1024 < OM * ON ? e0 + 1024 : OM * ON;
+  for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const int64_t i = int64_t(r.tm) * OM + e % OM, j = int64_t(r.tn) * ON + e / OM;
     if (i >= d.m || j >= d.n) continue;
     double acc = 0.0;
@@ -527,7 +529,8 @@ void launch_oz_gemm(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const
                                                      beta, ws, gemm_tc_error_flag());
   count_launch();
   if (n_red > 0) {
-    oz_splitk_reduce_kernel<<<n_red, 256, 0, s>>>(d_descs, d_red, ws, C, alpha, beta);
+    oz_splitk_reduce_kernel<<<dim3(unsigned(n_red), (OM * ON + 1023) / 1024), 256, 0, s>>>(d_descs, d_red, ws, C,
+                                                                                            alpha, beta);
     count_launch();
   }
   if (ws) dev_free(ws);
