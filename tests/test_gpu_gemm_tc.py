@@ -219,6 +219,39 @@ def test_f64tc_graded_rows_against_the_slice_error_bound():
     assert ratio < 1.0
 
 
+def test_f64tc_extreme_digits_over_several_exact_chunks():
+    """Every entry carries balanced digits at their largest magnitude of one sign (127, 63, ..., 63), so each
+    level adds close to its bound per k value; k spans three full 448-deep exact TMEM chunks and a ragged
+    one.  A level sum that lost a bit in the FP32 accumulator would show as a ~6e-8 relative error."""
+    from xped_gb300 import ensure_device, lib
+    from xped_gb300._lib import GemmDesc, last_error
+    ensure_device(0)
+    L = lib()
+    x = sum(d * 2.0 ** (-7 * (s + 1)) for s, d in enumerate([127, 63, 63, 63, 63, 63, 63]))
+    m, n, k = 130, 70, 3 * 448 + 100
+    A = np.full((m, k), x)
+    B = np.full((k, n), x)
+    A[::3] *= -1.0
+    ptrs = []
+    for h in (A.ravel(order="F"), B.ravel(order="F"), np.zeros(m * n)):
+        p = C.c_void_p()
+        assert L.xgb_malloc(C.byref(p), h.nbytes) == 0
+        assert L.xgb_memcpy_h2d(p, h.ctypes.data, h.nbytes) == 0
+        ptrs.append(p)
+    arr = (GemmDesc * 1)(GemmDesc(m, n, k, 0, m, 0, k, 0, m, 0, 0))
+    assert L.xgb_grouped_gemm(PREC_F64TC, 1, arr, ptrs[0], ptrs[1], ptrs[2], 1.0, 0.0, None) == 0, last_error()
+    assert L.xgb_gemm_tc_status() == 0, last_error()
+    got = np.empty(m * n)
+    assert L.xgb_memcpy_d2h(got.ctypes.data, ptrs[2], got.nbytes) == 0
+    for p in ptrs:
+        L.xgb_free(p)
+    got = got.reshape((m, n), order="F")
+    ref = A @ B
+    err = float(np.abs(got - ref).max() / np.abs(ref).max())
+    print("f64tc extreme digits relative error", err)
+    assert err < 4.0 * k * 2.0 ** -49
+
+
 def test_f64tc_through_the_tensor_api():
     from xped_gb300 import Basis, Tensor, ensure_device
     from xped_gb300.tensor import set_gemm_precision

@@ -2,15 +2,20 @@
 //
 // C_g = alpha op(A_g) op(B_g) + beta C_g for FP64 column-major blocks.  Every row i of op(A) is
 // written relative to a power of two 2^e_i above its largest entry (taken over the whole k range)
-// and cut into seven 7-bit slices, a_ik = 2^e_i (sum_s m_s 2^(-7 s) + O(2^-50)) with integers
-// |m_s| <= 128; every column of op(B) likewise (2^f_j).  A slice m_s 2^(-7 s) is exact in BF16, the
-// product of two slices is exact in FP32, and all products of a "level" L = s + t share the unit
-// 2^(-7 L): a sum of at most 7 pairs x 128 k values x 2^14 stays below 2^24 and is exact in the
-// FP32 tensor-memory accumulator whatever order the tensor core adds in.  The row and column
-// scales 2^(e_i + f_j) are applied in FP64 when the tile is stored.  This is the slicing scheme of Ozaki,
-// Ogita, Oishi and Rump ("Error-free transformations of matrix multiplication by using fast
+// and cut into seven balanced base-128 digits, a_ik = 2^e_i (sum_s m_s 2^(-7 s) + O(2^-50)) with
+// integers |m_1| <= 128 and |m_s| <= 64 for s >= 2; every column of op(B) likewise (2^f_j).  A slice
+// m_s 2^(-7 s) is exact in BF16, the product of two slices is exact in FP32, and all products of a
+// "level" L = s + t share the unit 2^(-7 L).  Per k value a level adds at most 2 x 128 x 64 + 5 x 64 x 64
+// = 36864 units, so a sum over 448 k values (14 K slices) stays below 2^24 and is exact in the FP32
+// tensor-memory accumulator whatever order the tensor core adds in.  The row and column scales
+// 2^(e_i + f_j) go into the exponent field when the tile is stored.  This is the slicing scheme of
+// Ozaki, Ogita, Oishi and Rump ("Error-free transformations of matrix multiplication by using fast
 // routines of matrix multiplication and its applications", Numer. Algorithms 59 (2012)), with BF16
 // tcgen05.mma as the fast routine.
+//
+// GB300 runs FP64 arithmetic at a small fraction of its FP32 and tensor rates, so nothing here
+// computes in FP64 but the one addition that joins the two FP32 halves of a result: the row
+// maxima, scales and slices are integer operations on the IEEE bits.
 //
 // Kernels (one launch each, all groups of the list):
 //  * oz_rowmax_kernel: per 128-row (A) / 64-row (B) x 32-K chunk, the largest |entry| of every row
@@ -18,17 +23,17 @@
 //  * oz_pack_kernel: the seven slices of every chunk as BF16 in the K-major, unswizzled canonical
 //    layout the MMA reads (8-row x 16-byte core matrices), zero padded past the block edges; the
 //    slices come from integer arithmetic on the FP64 significand (|x| rounded to 49 bits below the
-//    row's scale, every slice with the sign of its entry);
-//  * oz_gemm_kernel: one CTA (10 warps) per 128 x 64 output tile.  Warp 8 streams the slices of each
-//    32-wide K slice of the tile's rows and columns into a 2-stage shared-memory ring (84 KB per
-//    stage, bulk copies counted on mbarriers); warp 9 issues, per 16-deep k step, the 28 BF16 MMAs of
-//    the slice pairs with s + t <= 8 into seven 64-column TMEM accumulators (one per level, 448 of
-//    512 columns); after every four K slices (the exactness bound) warps 0-7 read the seven levels
-//    and add them into double-FP32 (hi + lo) register sums, then the next four slices start from
-//    zero.  The slice rounding (2^-50 of the row / column scale), the dropped pairs (s + t > 8) and
-//    the double-FP32 sums bound the error of an element by a small multiple of
-//    2^-49 k max_k |a_ik| max_k |b_kj|: about 5e-14 of ||C|| for Gaussian blocks, against ~1e-15 for an
-//    FP64 dot product and ~3e-7 for 3xTF32.
+//    row's scale, balanced digits, every slice with the sign of its entry);
+//  * oz_gemm_kernel: one CTA (10 warps) per 128 x 64 output tile and K range.  Warp 8 streams the
+//    slices of each 32-wide K slice of the tile's rows and columns into a 2-stage shared-memory ring
+//    (84 KB per stage, bulk copies counted on mbarriers); warp 9 issues, per 16-deep k step, the 28
+//    BF16 MMAs of the slice pairs with s + t <= 8 into seven 64-column TMEM accumulators (one per
+//    level, 448 of 512 columns); after every fourteen K slices (the exactness bound) and at the end
+//    of the range warps 0-7 read the seven levels and add them into double-FP32 (hi + lo) register
+//    sums, then the next chunk starts from zero.  The slice rounding (2^-50 of the row / column
+//    scale), the dropped pairs (s + t > 8) and the double-FP32 sums bound the error of an element by
+//    a small multiple of 2^-49 k max_k |a_ik| max_k |b_kj|: about 5e-14 of ||C|| for Gaussian blocks,
+//    against ~1e-15 for an FP64 dot product and ~3e-7 for 3xTF32.
 //
 // Every mbarrier wait is bounded; on timeout the CTA records an error flag (shared with the 3xTF32
 // kernel, xgb_gemm_tc_status), skips the epilogue and still frees its TMEM.
@@ -46,7 +51,8 @@ namespace {
 constexpr int OM = 128, ON = 64, OK = 32;          // output tile rows / columns, K per slice
 constexpr int kPieces = 7, kBits = 7;               // seven 7-bit slices per entry
 constexpr int kLevels = kPieces;                    // levels s + t = 2 .. 8 (1-based slices)
-constexpr int kChunk = 4;                           // K slices per exact TMEM accumulation (7 x 128 x 2^14 < 2^24)
+constexpr int kChunk = 14;                          // K slices per exact TMEM accumulation (448 x 36864 < 2^24)
+constexpr int kMinSplit = 4;                        // smallest K range of a split-K CTA, in K slices
 constexpr int kAPieceBytes = OM * OK * 2;           // 8 KB
 constexpr int kBPieceBytes = ON * OK * 2;           // 4 KB
 constexpr int kOzStageBytes = kPieces * (kAPieceBytes + kBPieceBytes);  // 84 KB
@@ -124,7 +130,8 @@ __global__ void __launch_bounds__(256) oz_rowmax_kernel(const xgb_gemm_desc* __r
                                                          const TcPackTask* __restrict__ tasks,
                                                          const double* __restrict__ A, const double* __restrict__ B,
                                                          unsigned long long* __restrict__ rowmax) {
-  __shared__ double X[OM][OK + 1];
+  // |x| as IEEE bits: for non-negative doubles the integer order is the numeric order
+  __shared__ unsigned long long X[OM][OK + 1];
   const TcPackTask t = tasks[blockIdx.x];
   const xgb_gemm_desc d = descs[t.g];
   const OzGroup gr = groups[t.g];
@@ -141,47 +148,54 @@ __global__ void __launch_bounds__(256) oz_rowmax_kernel(const xgb_gemm_desc* __r
     const int64_t gr_ = r0 + r, gk = k0 + k;
     double x = 0.0;
     if (gr_ < rows && gk < d.k) x = rowfast ? src[off + gr_ + gk * ld] : src[off + gk + gr_ * ld];
-    X[r][k] = fabs(x);
+    X[r][k] = static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7FFFFFFFFFFFFFFFull;
   }
   __syncthreads();
   for (int r = threadIdx.x; r < tr; r += 256) {
     if (r0 + r >= rows) continue;
-    double m = 0.0;
-    for (int k = 0; k < OK; ++k) m = fmax(m, X[r][k]);
-    unsigned long long* slot = rowmax + (isB ? gr.b_rowmax : gr.a_rowmax) + r0 + r;
-    atomicMax(slot, static_cast<unsigned long long>(__double_as_longlong(m)));
+    unsigned long long m = 0;
+    for (int k = 0; k < OK; ++k) m = m > X[r][k] ? m : X[r][k];
+    if (m) atomicMax(rowmax + (isB ? gr.b_rowmax : gr.a_rowmax) + r0 + r, m);
   }
 }
 
-// exponent e with |x| < 2^e for every entry of the row (0 for an all-zero row)
+// exponent e with |x| < 2^e for every entry of the row, from the bits of its largest |entry|
+// m = f 2^e, f in [0.5, 1): the biased exponent less 1022.  A zero row, or one whose largest entry
+// is subnormal (its slices are all zero), gets 0.
 __device__ __forceinline__ int row_scale(unsigned long long bits) {
-  const double m = __longlong_as_double(static_cast<long long>(bits));
-  if (!(m > 0.0)) return 0;
-  int e;
-  frexp(m, &e);  // m = f 2^e, f in [0.5, 1)
-  return e;
+  const int be = int((bits >> 52) & 0x7FF);
+  return be == 0 ? 0 : be - 1022;
 }
 
-// seven 7-bit slices of x relative to 2^e (|x| < 2^e): x = 2^e sum_s sign * m_s * 2^(-7 s) + O(2^(e - 50)),
-// 0 <= m_s <= 127 (the leading digit <= 128)
+// seven balanced base-128 digits of x relative to 2^e (|x| < 2^e):
+// x = 2^e sum_s m_s 2^(-7 s) + O(2^(e - 50)), |m_1| <= 128, |m_s| <= 64 for s >= 2
 __device__ __forceinline__ void slice7(double x, int e, float* out) {
   const long long bits = __double_as_longlong(x);
   const int ex = int((bits >> 52) & 0x7FF);
   const bool neg = bits < 0;
-  unsigned long long q = 0;
+  long long q = 0;
   if (ex != 0) {  // normal numbers (subnormals are below every slice of any realistic row)
     const unsigned long long mant = (static_cast<unsigned long long>(bits) & ((1ull << 52) - 1)) | (1ull << 52);
     // x = mant 2^(ex - 1075); |x| rounded to the nearest multiple of 2^(e - 49) (ties up): shift right
     // by sh = e - 49 - (ex - 1075) >= 4 (|x| < 2^e) with one guard bit; q <= 2^49
     const int sh = e - 49 - (ex - 1075);
-    q = sh >= 64 ? 0ull : (((mant >> (sh - 1)) + 1ull) >> 1);
+    q = sh >= 64 ? 0ll : static_cast<long long>(((mant >> (sh - 1)) + 1ull) >> 1);
   }
+  // lowest digit first: m in [-64, 63] and the carry moves into q; what is left after six digits is
+  // the leading digit, round(q / 2^42) <= 128
+  int m[kPieces];
+#pragma unroll
+  for (int s = kPieces; s >= 2; --s) {
+    int dg = int(q & ((1ll << kBits) - 1));
+    if (dg >= 64) dg -= 128;
+    m[s - 1] = dg;
+    q = (q - dg) >> kBits;
+  }
+  m[0] = int(q);
 #pragma unroll
   for (int s = 1; s <= kPieces; ++s) {
-    // 7-bit digits of q; the leading one may reach 128 (q = 2^49), still exact in BF16
-    const int m = s == 1 ? int(q >> (49 - kBits)) : int((q >> (49 - kBits * s)) & ((1u << kBits) - 1));
-    const float v = ldexpf(float(m), -kBits * s);
-    out[s - 1] = neg ? -v : v;
+    const float v = __fmul_rn(float(neg ? -m[s - 1] : m[s - 1]), __int_as_float((127 - kBits * s) << 23));  // x 2^(-7 s)
+    out[s - 1] = v;
   }
 }
 
@@ -238,6 +252,18 @@ __global__ void __launch_bounds__(256) oz_pack_kernel(const xgb_gemm_desc* __res
 }
 
 // ----------------------------------------------------------------------------- gemm
+// v 2^sc as a double, assembled from the FP32 bits (exact; no FP64 arithmetic) while the result is a
+// normal double, else through ldexp
+__device__ __forceinline__ double scaled_double(float v, int sc) {
+  const uint32_t b = __float_as_uint(v);
+  const int e8 = int((b >> 23) & 0xFF);
+  if ((b & 0x7FFFFFFFu) == 0u) return __longlong_as_double(static_cast<long long>(uint64_t(b >> 31) << 63));
+  const int e = e8 - 127 + 1023 + sc;
+  if (e8 == 0 || e8 == 255 || e <= 0 || e >= 2047) return ldexp(double(v), sc);
+  return __longlong_as_double(static_cast<long long>((uint64_t(b >> 31) << 63) | (uint64_t(e) << 52) |
+                                                     (uint64_t(b & 0x7FFFFFu) << 29)));
+}
+
 __global__ void __launch_bounds__(kOzThreads, 1)
     oz_gemm_kernel(const xgb_gemm_desc* __restrict__ descs, const OzGroup* __restrict__ groups,
                    const GemmTile* __restrict__ tiles, const unsigned char* __restrict__ apack,
@@ -248,6 +274,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   __shared__ uint64_t full[kOzStages], empty[kOzStages], accf, acce, done;
   __shared__ uint32_t tmem_slot;
   __shared__ int fail, issued, consumed;
+  __shared__ int rsc[OM], csc[ON];  // row and column scale exponents of the tile
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
 
   const GemmTile t = tiles[blockIdx.x];
@@ -259,6 +286,10 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   const int ks = t.k0, nk = (t.k1 < 0 ? gr.slices : t.k1) - t.k0;
   const int nchunks = (nk + kChunk - 1) / kChunk;
 
+  for (int i = threadIdx.x; i < OM + ON; i += kOzThreads) {
+    if (i < OM) rsc[i] = m0 + i < d.m ? row_scale(rowmax[gr.a_rowmax + m0 + i]) : 0;
+    else csc[i - OM] = n0 + (i - OM) < d.n ? row_scale(rowmax[gr.b_rowmax + n0 + (i - OM)]) : 0;
+  }
   if (warp == kOzMma) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s_u32(&tmem_slot)),
                  "r"(kOzTmemCols));
@@ -349,26 +380,26 @@ __global__ void __launch_bounds__(kOzThreads, 1)
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll 1
       for (int level = kLevels - 1; level >= 0; --level) {  // smallest contributions first
+        uint32_t v[32];
+        const uint32_t taddr = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(level * ON + colg * 32);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+              "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+              "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          uint32_t v[8];
-          const uint32_t taddr =
-              tmem + (uint32_t(quarter * 32) << 16) + uint32_t(level * ON + colg * 32 + c * 8);
-          asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                       : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-                         "=r"(v[7])
-                       : "r"(taddr));
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            // two-sum of hi and the exact level partial; the rounding error goes to lo
-            const float x = __uint_as_float(v[j]);
-            const float s = __fadd_rn(hi[c * 8 + j], x);
-            const float bb = __fsub_rn(s, hi[c * 8 + j]);
-            const float e = __fadd_rn(__fsub_rn(hi[c * 8 + j], __fsub_rn(s, bb)), __fsub_rn(x, bb));
-            hi[c * 8 + j] = s;
-            lo[c * 8 + j] = __fadd_rn(lo[c * 8 + j], e);
-          }
+        for (int j = 0; j < 32; ++j) {
+          // two-sum of hi and the exact level partial; the rounding error goes to lo
+          const float x = __uint_as_float(v[j]);
+          const float s = __fadd_rn(hi[j], x);
+          const float bb = __fsub_rn(s, hi[j]);
+          const float e = __fadd_rn(__fsub_rn(hi[j], __fsub_rn(s, bb)), __fsub_rn(x, bb));
+          hi[j] = s;
+          lo[j] = __fadd_rn(lo[j], e);
         }
       }
 #pragma unroll
@@ -392,17 +423,19 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   if (ok && nk > 0 && warp < kOzDrainWarps) {
     const int64_t row = m0 + quarter * 32 + lane;
     if (row < d.m) {
-      const int ei = row_scale(rowmax[gr.a_rowmax + row]);
+      const int ei = rsc[quarter * 32 + lane];
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const int64_t col = n0 + colg * 32 + j;
         if (col < d.n) {
-          const double acc = ldexp(double(hi[j]) + double(lo[j]), ei + row_scale(rowmax[gr.b_rowmax + col]));
+          const int sc = ei + csc[colg * 32 + j];
+          const double acc = scaled_double(hi[j], sc) + scaled_double(lo[j], sc);
           if (t.slot >= 0) {  // split-K partial: raw sum, tile-local column-major OM x ON
             ws[int64_t(t.slot) * OM * ON + (quarter * 32 + lane) + int64_t(colg * 32 + j) * OM] = acc;
           } else {
             double* cp = C + d.c_off + row + col * d.ldc;
-            *cp = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *cp);
+            if (beta == 0.0) *cp = alpha == 1.0 ? acc : alpha * acc;
+            else *cp = fma(alpha, acc, beta * *cp);
           }
         }
       }
@@ -475,17 +508,18 @@ OzPlanHost build_oz_plan(const xgb_gemm_desc* descs, int n) {
     }
     p.groups.push_back(gr);
   }
-  // output tiles; when they cannot fill the GPU twice over, the K slices of every tile are split into
-  // ranges of at least one exact-accumulation chunk (kChunk slices) whose partial tiles a fixed-order
-  // reduce adds
-  int64_t n_out = 0;
-  for (const auto& gr : p.groups) n_out += int64_t(gr.a_tiles) * gr.b_tiles;
-  const int64_t target = 2 * int64_t(num_sms() > 0 ? num_sms() : 152);
-  const int64_t want = n_out > 0 ? (target + n_out - 1) / n_out : 1;
+  // output tiles and their K ranges.  One CTA runs per SM (its stages and TMEM fill one), so the K
+  // slices of all tiles are cut into ranges of at most about total / SMs slices (and at least
+  // kMinSplit): the launch then is about one wave of CTAs with equal work, the largest tiles split the
+  // most.  The partial tiles of a split tile are added by a fixed-order reduce.
+  int64_t work = 0;
+  for (const auto& gr : p.groups) work += int64_t(gr.a_tiles) * gr.b_tiles * gr.slices;
+  const int64_t sms = num_sms() > 0 ? num_sms() : 152;
+  const int64_t cap = std::max<int64_t>(kMinSplit, (work + sms - 1) / sms);
   for (int g = 0; g < n; ++g) {
     const OzGroup& gr = p.groups[g];
-    const int64_t splits = std::max<int64_t>(1, std::min<int64_t>(want, gr.slices / kChunk));
-    const int64_t per = splits > 1 ? ((gr.slices + splits - 1) / splits + kChunk - 1) / kChunk * kChunk : gr.slices;
+    const int64_t splits = std::max<int64_t>(1, (gr.slices + cap - 1) / cap);
+    const int64_t per = (gr.slices + splits - 1) / splits;
     for (int32_t y = 0; y < gr.b_tiles; ++y)
       for (int32_t x = 0; x < gr.a_tiles; ++x) {
         if (splits == 1) {
@@ -498,6 +532,10 @@ OzPlanHost build_oz_plan(const xgb_gemm_desc* descs, int n) {
         p.red.push_back({g, x, y, first, p.slots - first, 0});
       }
   }
+  // longest K ranges first: CTAs start in index order, so the short ones fill the tail of the wave
+  auto range = [&](const GemmTile& t) { return (t.k1 < 0 ? p.groups[t.g].slices : t.k1) - t.k0; };
+  std::stable_sort(p.tiles.begin(), p.tiles.end(),
+                   [&](const GemmTile& a, const GemmTile& b) { return range(a) > range(b); });
   p.rowmax = rb;
   p.tasks = p.tasks_a;
   p.tasks.insert(p.tasks.end(), p.tasks_b.begin(), p.tasks_b.end());
