@@ -225,17 +225,19 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   // Two barriers per column: (1) scale column j by the broadcast reciprocal of its pivot,
   // (2) rank-1 update of the trailing lower triangle, during which thread 0 - the owner of
   // element (j+1, j+1), the first of the folded order - finishes that element and forms the
-  // next pivot into the other slot of a two-entry buffer.  The reciprocal is formed once:
-  // an FP64 division is a multi-instruction DFMA sequence on GB300's narrow FP64 pipe.
+  // next pivot into the other slot of a two-entry buffer.  The pivot chain is the critical
+  // path of the factorisation: on GB300 a dependent FP64 operation takes ~64 cycles, sqrt ~675
+  // and a division ~430, so the pivot is r = rsqrt(d) (~430) with L_jj = d r and 1 / L_jj = r.
   __shared__ double inv_s[2];
   __shared__ int dead_s[2];
   auto pivot = [&](int j) {
     const double dj = LA(j, j);
     const int dd = !(dj > dfloor);  // also true for NaN
     if (dd) atomicAdd(bad, 1);
-    const double p = sqrt(dd ? dfloor : dj);
-    LA(j, j) = p;
-    inv_s[j & 1] = 1.0 / p;
+    const double v = dd ? dfloor : dj;
+    const double r = rsqrt(v);
+    LA(j, j) = v * r;
+    inv_s[j & 1] = r;
     dead_s[j & 1] = dd;
   };
   if (tid == 0 && l > 0) pivot(0);
@@ -347,8 +349,9 @@ __global__ void __launch_bounds__(32) chol_warp_kernel(const CholDesc* __restric
   for (int j = 0; j < l; ++j) {
     const double dj = LA(j, j);
     const int dd = !(dj > dfloor);  // also true for NaN
-    const double p = sqrt(dd ? dfloor : dj);
-    const double inv = 1.0 / p;
+    const double v = dd ? dfloor : dj;
+    const double inv = rsqrt(v);
+    const double p = v * inv;
     __syncwarp();
     if (lane == 0) {
       LA(j, j) = p;
