@@ -63,8 +63,11 @@ constexpr int kOzWarps = 10, kOzThreads = kOzWarps * 32;
 constexpr int kOzProducer = 8, kOzMma = 9, kOzDrainWarps = 8;
 constexpr long long kOzSpin = 1ll << 26;
 constexpr uint32_t kSboBytes = 128;                 // next 8-row group
+// A: seven separate 128-row pieces.  B: the seven 64-row pieces stacked into one 448-row operand (row
+// group g of piece s is row group 8 s + g), so that pieces t .. t + c - 1 form one N = 64 c operand
 constexpr uint32_t kLboA = (OM / 8) * 128;          // next 16-byte K group, 128-row pieces
-constexpr uint32_t kLboB = (ON / 8) * 128;          // 64-row pieces
+constexpr uint32_t kBPieceStride = (ON / 8) * 128;  // 1 KB: next B piece within a K group
+constexpr uint32_t kLboB = kPieces * kBPieceStride; // 7 KB: next 16-byte K group of the stacked B
 static_assert(kLevels * ON <= int(kOzTmemCols), "level accumulators fit TMEM");
 static_assert(kOzSmem <= 227 * 1024, "stages fit shared memory");
 
@@ -79,8 +82,11 @@ __device__ __forceinline__ uint64_t oz_desc(uint32_t saddr, uint32_t lbo) {
   return d;
 }
 
-// FP32 accumulate, BF16 A and B (kind::f16), both K-major, N = 64, M = 128
-constexpr uint32_t kOzIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(ON >> 3) << 17) | (uint32_t(OM >> 4) << 24);
+// FP32 accumulate, BF16 A and B (kind::f16), both K-major, M = 128, N = 64 NC (NC stacked B pieces)
+template <int NC>
+__host__ __device__ constexpr uint32_t oz_idesc() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t((ON * NC) >> 3) << 17) | (uint32_t(OM >> 4) << 24);
+}
 
 __device__ __forceinline__ void bar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(s_u32(bar)), "r"(count));
@@ -111,11 +117,12 @@ __device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, u
       : "memory");
 }
 
+template <int NC>
 __device__ __forceinline__ void mma_bf16_oz(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(kOzIdesc), "r"(acc));
+      "l"(adesc), "l"(bdesc), "r"(oz_idesc<NC>()), "r"(acc));
 }
 
 __device__ __forceinline__ void commit_to(uint64_t* bar) {
@@ -231,6 +238,7 @@ __global__ void __launch_bounds__(256) oz_pack_kernel(const xgb_gemm_desc* __res
   __syncthreads();
   // slice block of this (tile, K slice): kPieces pieces of tr x OK BF16, each in canonical layout
   const int piece_bytes = isB ? kBPieceBytes : kAPieceBytes;
+  const int piece_stride = isB ? int(kBPieceStride) : kAPieceBytes;
   const uint32_t lbo = isB ? kLboB : kLboA;
   unsigned char* base = (isB ? bpack + gr.b_pack : apack + gr.a_pack) +
                         (int64_t(t.tile) * gr.slices + t.slice) * int64_t(kPieces) * piece_bytes;
@@ -247,7 +255,7 @@ __global__ void __launch_bounds__(256) oz_pack_kernel(const xgb_gemm_desc* __res
     const uint32_t bo = uint32_t(kq) * lbo + uint32_t(r >> 3) * kSboBytes + uint32_t(r & 7) * 16;
 #pragma unroll
     for (int s = 0; s < kPieces; ++s)
-      *reinterpret_cast<uint4*>(base + int64_t(s) * piece_bytes + bo) = *reinterpret_cast<const uint4*>(pc[s]);
+      *reinterpret_cast<uint4*>(base + int64_t(s) * piece_stride + bo) = *reinterpret_cast<const uint4*>(pc[s]);
   }
 }
 
@@ -354,15 +362,27 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         const uint32_t bbase = abase + kPieces * kAPieceBytes;
 #pragma unroll
         for (int kk = 0; kk < OK / 16; ++kk) {
-#pragma unroll
-          for (int i = 0; i < kPieces; ++i)
-#pragma unroll
-            for (int j = 0; j + i < kPieces; ++j) {
-              const int level = i + j;  // 0-based: slices i + 1 and j + 1
-              const uint32_t acc = (cs == 0 && kk == 0 && i == 0) ? 0u : 1u;  // first pair of each level
-              mma_bf16_oz(tmem + uint32_t(level * ON), oz_desc(abase + i * kAPieceBytes + kk * 2 * kLboA, kLboA),
-                          oz_desc(bbase + j * kBPieceBytes + kk * 2 * kLboB, kLboB), acc);
-            }
+          // slice pairs (i, j), j <= 6 - i, in MMAs of up to four stacked B pieces: the product of A piece
+          // i with B pieces j0 .. j0 + c - 1 lands in levels i + j0 .. i + j0 + c - 1, the adjacent
+          // 64-column accumulators from column 64 (i + j0); ten MMAs cover the 28 pairs
+          const uint64_t ad[kPieces] = {
+              oz_desc(abase + 0 * kAPieceBytes + kk * 2 * kLboA, kLboA), oz_desc(abase + 1 * kAPieceBytes + kk * 2 * kLboA, kLboA),
+              oz_desc(abase + 2 * kAPieceBytes + kk * 2 * kLboA, kLboA), oz_desc(abase + 3 * kAPieceBytes + kk * 2 * kLboA, kLboA),
+              oz_desc(abase + 4 * kAPieceBytes + kk * 2 * kLboA, kLboA), oz_desc(abase + 5 * kAPieceBytes + kk * 2 * kLboA, kLboA),
+              oz_desc(abase + 6 * kAPieceBytes + kk * 2 * kLboA, kLboA)};
+          auto bd = [&](int j0) { return oz_desc(bbase + j0 * kBPieceStride + kk * 2 * kLboB, kLboB); };
+          const uint32_t a0 = (cs == 0 && kk == 0) ? 0u : 1u;  // the i = 0 MMAs open every level of a chunk
+          auto col = [&](int lvl) { return tmem + uint32_t(lvl * ON); };
+          mma_bf16_oz<4>(col(0), ad[0], bd(0), a0);
+          mma_bf16_oz<3>(col(4), ad[0], bd(4), a0);
+          mma_bf16_oz<4>(col(1), ad[1], bd(0), 1u);
+          mma_bf16_oz<2>(col(5), ad[1], bd(4), 1u);
+          mma_bf16_oz<4>(col(2), ad[2], bd(0), 1u);
+          mma_bf16_oz<1>(col(6), ad[2], bd(4), 1u);
+          mma_bf16_oz<4>(col(3), ad[3], bd(0), 1u);
+          mma_bf16_oz<3>(col(4), ad[4], bd(0), 1u);
+          mma_bf16_oz<2>(col(5), ad[5], bd(0), 1u);
+          mma_bf16_oz<1>(col(6), ad[6], bd(0), 1u);
         }
         commit_to(&empty[s]);
         if (cs == kChunk - 1 || kc == nk - 1) commit_to(&accf);
