@@ -87,30 +87,42 @@ T* stage(const std::vector<T>& v, cudaStream_t s) {
 F64Config f64_candidate(int idx) { return {kTiles[idx / 4], kWaves[idx % 4]}; }
 int f64_candidate_count() { return kNumCandidates; }
 
-F64Plan plan_gemm_f64(const xgb_gemm_desc* d, int n, F64Config c) {
+F64Plan plan_gemm_f64(const xgb_gemm_desc* d, int n, F64Config c, int shape) {
   F64Plan p;
   p.tile = c.tile;
   const int tile = c.tile;
+  auto keep = [&](int64_t x, int64_t y) { return shape != kGemmSymUpper || x <= y; };
+  auto kmax = [&](int g, int64_t y) {
+    return shape == kGemmTriB ? std::min<int64_t>(d[g].k, (y + 1) * tile) : d[g].k;
+  };
   int64_t n_out = 0;
-  for (int g = 0; g < n; ++g) n_out += ((d[g].m + tile - 1) / tile) * ((d[g].n + tile - 1) / tile);
+  for (int g = 0; g < n; ++g) {
+    const int64_t tm = (d[g].m + tile - 1) / tile, tn = (d[g].n + tile - 1) / tile;
+    for (int64_t y = 0; y < tn; ++y)
+      for (int64_t x = 0; x < tm; ++x) n_out += keep(x, y);
+  }
   const int64_t target = int64_t(c.split_waves) * int64_t(num_sms() > 0 ? num_sms() : 152);
   const int64_t want = (c.split_waves > 0 && n_out > 0) ? (target + n_out - 1) / n_out : 1;
   for (int g = 0; g < n; ++g) {
     const int64_t tm = (d[g].m + tile - 1) / tile, tn = (d[g].n + tile - 1) / tile;
-    const int64_t splits = std::max<int64_t>(1, std::min<int64_t>(want, d[g].k / kMinChunk));
-    const int64_t chunk = splits > 1 ? (((d[g].k + splits - 1) / splits + 15) / 16) * 16 : d[g].k;
-    for (int64_t y = 0; y < tn; ++y)
+    for (int64_t y = 0; y < tn; ++y) {
+      const int64_t kk = kmax(g, y);
+      const int64_t splits = std::max<int64_t>(1, std::min<int64_t>(want, kk / kMinChunk));
+      const int64_t chunk = splits > 1 ? (((kk + splits - 1) / splits + 15) / 16) * 16 : kk;
       for (int64_t x = 0; x < tm; ++x) {
+        if (!keep(x, y)) continue;
         if (splits == 1) {
-          p.tiles.push_back({int32_t(g), int32_t(x), int32_t(y), tile});
+          if (kk == d[g].k) p.tiles.push_back({int32_t(g), int32_t(x), int32_t(y), tile});
+          else p.tiles.push_back({int32_t(g), int32_t(x), int32_t(y), tile, 0, int32_t(kk)});
           continue;
         }
         const int32_t first = p.slots;
-        for (int64_t k0 = 0; k0 < d[g].k; k0 += chunk)
+        for (int64_t k0 = 0; k0 < kk; k0 += chunk)
           p.tiles.push_back({int32_t(g), int32_t(x), int32_t(y), tile, int32_t(k0),
-                             int32_t(std::min<int64_t>(k0 + chunk, d[g].k)), p.slots++});
+                             int32_t(std::min<int64_t>(k0 + chunk, kk)), p.slots++});
         p.red.push_back({int32_t(g), int32_t(x), int32_t(y), first, p.slots - first, 0});
       }
+    }
   }
   order_tiles_by_work(p.tiles, d);
   return p;

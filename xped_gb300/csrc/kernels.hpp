@@ -149,7 +149,8 @@ struct SignFixDesc { int64_t m, n, k, u_off, v_off; };      // U m x k (ld m), V
 void launch_gauss_fill(const GaussBlock* d_blocks, int n_blocks, int64_t max_count, uint64_t seed, double* out,
                        cudaStream_t s);
 void launch_sign_fix(const SignFixDesc* d_descs, int n, int64_t max_k, double* U, double* Vt, cudaStream_t s);
-// CholeskyQR helper (rsvd.cu): per sketch block m x l, Gram matrix l x l at g_off
+// CholeskyQR helper (rsvd.cu): per sketch block m x l, Gram matrix l x l at g_off, of which only
+// the upper triangle (i <= j) is read
 struct CholDesc { int64_t m, l, g_off; };
 void launch_chol_inv(const CholDesc* d_descs, int n, int64_t max_l, double* G, double* Rinv, double rel_shift, int* bad,
                      cudaStream_t s);
@@ -200,7 +201,15 @@ struct F64Plan {
   std::vector<SplitReduce> red;
   int32_t slots = 0;  // split-K partial tiles (workspace of slots x tile x tile doubles)
 };
-F64Plan plan_gemm_f64(const xgb_gemm_desc* d, int n, F64Config c);
+// Output structure the plan may exploit (every group of the list alike):
+//  kGemmDense:    all tiles, full k;
+//  kGemmSymUpper: C is symmetric (a Gram matrix op(A) = B^T): only tiles on or above the diagonal
+//                 (tm <= tn) are computed; the strictly lower part of C is left unwritten;
+//  kGemmTriB:     op(B) is upper triangular (rows below the diagonal are zero): output column tile tn
+//                 sums k < min(k, (tn + 1) tile) only (the skipped terms are exact zeros).
+// Split-K ranges follow the reduced work, so results are deterministic but not the bits of the dense plan.
+enum GemmShape { kGemmDense = 0, kGemmSymUpper = 1, kGemmTriB = 2 };
+F64Plan plan_gemm_f64(const xgb_gemm_desc* d, int n, F64Config c, int shape = kGemmDense);
 // executes a plan whose tables are on the device (workspace allocated stream-ordered for split-K)
 void run_f64_plan(const F64Plan& p, const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, const SplitReduce* d_red,
                   const double* A, const double* B, double* C, double alpha, double beta, cudaStream_t s);

@@ -57,13 +57,13 @@ double* alloc_d(int64_t n) { return static_cast<double*>(dev_alloc(sizeof(double
 // one reduce launch adds them in a fixed order (deterministic result).  With autotuning on, the
 // tile edge and the split target are the tuned ones of the list's size bucket.
 void grouped_gemm(const std::vector<xgb_gemm_desc>& d, const double* A, const double* B, double* C, cudaStream_t s,
-                  double alpha = 1.0, double beta = 0.0) {
+                  double alpha = 1.0, double beta = 0.0, int shape = kGemmDense) {
   if (d.empty()) return;
   const F64Config fallback{choose_gemm_tile(d.data(), int(d.size())), 2};
   const F64Config cfg = gemm_f64_config(d.data(), int(d.size()), A, B, fallback, s);
-  const F64Plan p = plan_gemm_f64(d.data(), int(d.size()), cfg);
+  const F64Plan p = plan_gemm_f64(d.data(), int(d.size()), cfg, shape);
   double flops = 0;
-  for (const auto& g : d) flops += 2.0 * double(g.m) * double(g.n) * double(g.k);
+  for (const auto& g : d) flops += 2.0 * double(g.m) * double(g.n) * double(g.k) * (shape == kGemmDense ? 1.0 : 0.5);
   Staging st;
   const size_t od = st.add(d), ot = st.add(p.tiles), orr = st.add(p.red);
   st.upload(s);
@@ -241,25 +241,27 @@ double* orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64
   const size_t o = sc.add(cd);
   sc.upload(s);
   constexpr double kShift = 11.0 * 1.1102230246251565e-16;
-  // pass 1 (shifted): Y -> Q;  pass 2: Q -> Y;  pass 3: Y -> Q
-  grouped_gemm(gram_y, Y, Y, G, s);
+  // pass 1 (shifted): Y -> Q;  pass 2: Q -> Y;  pass 3: Y -> Q.  The Gram matrices are computed on and
+  // above the diagonal only (the Cholesky reads that triangle), and Q R^-1 skips the zero rows of the
+  // upper-triangular R^-1: about half the FP64 work of the full products.
+  grouped_gemm(gram_y, Y, Y, G, s, 1.0, 0.0, kGemmSymUpper);
   prof_begin(K_QR, s);
   launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, kShift, bad, s);
   prof_end(K_QR, s, 0.0);
-  grouped_gemm(mul_yq, Y, Ri, Q, s);
+  grouped_gemm(mul_yq, Y, Ri, Q, s, 1.0, 0.0, kGemmTriB);
   if (passes >= 2) {
-    grouped_gemm(gram_q, Q, Q, G, s);
+    grouped_gemm(gram_q, Q, Q, G, s, 1.0, 0.0, kGemmSymUpper);
     prof_begin(K_QR, s);
     launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, 0.0, bad, s);
     prof_end(K_QR, s, 0.0);
-    grouped_gemm(mul_qy, Q, Ri, Y, s);
+    grouped_gemm(mul_qy, Q, Ri, Y, s, 1.0, 0.0, kGemmTriB);
   }
   if (passes >= 3) {
-    grouped_gemm(gram_y, Y, Y, G, s);
+    grouped_gemm(gram_y, Y, Y, G, s, 1.0, 0.0, kGemmSymUpper);
     prof_begin(K_QR, s);
     launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, 0.0, bad, s);
     prof_end(K_QR, s, 0.0);
-    grouped_gemm(mul_yq, Y, Ri, Q, s);
+    grouped_gemm(mul_yq, Y, Ri, Q, s, 1.0, 0.0, kGemmTriB);
   }
   dev_free(G);
   dev_free(Ri);

@@ -186,8 +186,18 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   auto XA = [&](int i, int k) -> double& { return kShared ? Xs[i * ld + k] : Xs[i + int64_t(k) * l]; };
   __shared__ double red[32];
   __shared__ double bcast;
-  if (kShared)
-    for (int e = tid; e < l * l; e += nt) LA(e % l, e / l) = Gg[e];
+  // G is read from its upper triangle (the Gram products compute only that one): LA(i, k) = G(min, max)
+  if (kShared) {
+    for (int e = tid; e < l * l; e += nt) {
+      const int i = e % l, k = e / l;
+      LA(i, k) = Gg[i <= k ? e : k + int64_t(i) * l];
+    }
+  } else {
+    for (int e = tid; e < l * l; e += nt) {
+      const int i = e % l, k = e / l;
+      if (i > k) Gg[e] = Gg[k + int64_t(i) * l];
+    }
+  }
   if (kInverse)
     for (int e = tid; e < l * l; e += nt) XA(e % l, e / l) = (e % l == e / l) ? 1.0 : 0.0;
   __syncthreads();
@@ -221,50 +231,58 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   const double shift = bcast, dfloor = floor_s;
   for (int i = tid; i < l; i += nt) LA(i, i) += shift;
   __syncthreads();
-  // Cholesky (right-looking), lower triangle in place
-  // Two barriers per column: (1) scale column j by the broadcast reciprocal of its pivot,
-  // (2) rank-1 update of the trailing lower triangle, during which thread 0 - the owner of
-  // element (j+1, j+1), the first of the folded order - finishes that element and forms the
-  // next pivot into the other slot of a two-entry buffer.  The pivot chain is the critical
-  // path of the factorisation: on GB300 a dependent FP64 operation takes ~64 cycles, sqrt ~675
-  // and a division ~430, so the pivot is r = rsqrt(d) (~430) with L_jj = d r and 1 / L_jj = r.
-  __shared__ double inv_s[2];
-  __shared__ int dead_s[2];
-  auto pivot = [&](int j) {
-    const double dj = LA(j, j);
-    const int dd = !(dj > dfloor);  // also true for NaN
-    if (dd) atomicAdd(bad, 1);
-    const double v = dd ? dfloor : dj;
-    const double r = rsqrt(v);
-    LA(j, j) = v * r;
-    inv_s[j & 1] = r;
-    dead_s[j & 1] = dd;
+  // Cholesky (right-looking, one column of look-ahead), lower triangle in place.  Iteration j, with
+  // column j final (updated by every earlier column and scaled by its pivot's reciprocal):
+  //   warp 0 ("panel") applies column j to column j + 1 only, forms pivot j + 1 and scales column j + 1,
+  //   warps 1.. apply column j to the trailing columns j + 2 .. l - 1,
+  // and one barrier ends the iteration.  The pivot chain - on GB300 a dependent FP64 operation takes
+  // ~64 cycles, sqrt ~675 and a division ~430, so the pivot is r = rsqrt(d) (~430) with L_jj = d r and
+  // 1 / L_jj = r - runs beside the trailing update instead of between two barriers.  Every element sees
+  // the same FMAs in the same order as in the unblocked column algorithm.
+  const unsigned full_warp = 0xffffffffu;
+  auto panel = [&](int c) {  // warp 0: pivot of column c and its scaling; lane ln owns rows c + ln + 32 r
+    double r = 0.0;
+    int dd = 0;
+    if (lane == 0) {
+      const double dj = LA(c, c);
+      dd = !(dj > dfloor);  // also true for NaN
+      if (dd) atomicAdd(bad, 1);
+      const double v = dd ? dfloor : dj;
+      r = rsqrt(v);
+      LA(c, c) = v * r;
+    }
+    r = __shfl_sync(full_warp, r, 0);
+    dd = __shfl_sync(full_warp, dd, 0);
+    for (int i = c + lane; i < l; i += 32)
+      if (i > c) LA(i, c) = dd ? 0.0 : LA(i, c) * r;
+    __syncwarp();
   };
-  if (tid == 0 && l > 0) pivot(0);
+  if (warp == 0 && l > 0) panel(0);
   __syncthreads();
-  for (int j = 0; j < l; ++j) {
-    const double inv = inv_s[j & 1];
-    const bool zero_col = dead_s[j & 1] != 0;
-    for (int i = j + 1 + tid; i < l; i += nt) LA(i, j) = zero_col ? 0.0 : LA(i, j) * inv;
-    __syncthreads();
-    // trailing lower triangle (rows i >= k > j) folded into whole columns: column c and column
-    // t-1-c together hold t+1 elements; an odd t leaves the middle column alone.  e = 0 is
-    // element (j+1, j+1) in both branches.
-    const int t = l - j - 1, half = t >> 1;
-    const int total = (t + 1) * half + ((t & 1) ? (t + 1) >> 1 : 0);
-    for (int e = tid; e < total; e += nt) {
-      int i, k;
-      if (e < (t + 1) * half) {
-        const int r = e % (t + 1), c = e / (t + 1);
-        if (r < t - c) { i = c + r; k = c; } else { i = (t - 1 - c) + (r - (t - c)); k = t - 1 - c; }
-      } else {
-        k = (t - 1) >> 1;
-        i = k + (e - (t + 1) * half);
+  for (int j = 0; j + 1 < l; ++j) {
+    if (warp == 0) {
+      const double ljj = LA(j + 1, j);
+      for (int i = j + 1 + lane; i < l; i += 32) LA(i, j + 1) = fma(-LA(i, j), ljj, LA(i, j + 1));
+      __syncwarp();
+      panel(j + 1);
+    } else {
+      // trailing lower triangle (rows i >= k >= j + 2) folded into whole columns: column c and column
+      // t-1-c together hold t+1 elements; an odd t leaves the middle column alone
+      const int t = l - j - 2, half = t >> 1;
+      const int total = (t + 1) * half + ((t & 1) ? (t + 1) >> 1 : 0);
+      for (int e = tid - 32; e < total; e += nt - 32) {
+        int i, k;
+        if (e < (t + 1) * half) {
+          const int r = e % (t + 1), c = e / (t + 1);
+          if (r < t - c) { i = c + r; k = c; } else { i = (t - 1 - c) + (r - (t - c)); k = t - 1 - c; }
+        } else {
+          k = (t - 1) >> 1;
+          i = k + (e - (t + 1) * half);
+        }
+        i += j + 2;
+        k += j + 2;
+        LA(i, k) = fma(-LA(i, j), LA(k, j), LA(i, k));
       }
-      i += j + 1;
-      k += j + 1;
-      LA(i, k) = fma(-LA(i, j), LA(k, j), LA(i, k));
-      if (e == 0) pivot(j + 1);
     }
     __syncthreads();
   }
@@ -278,6 +296,7 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   } else {
     // X = L^-1 by forward elimination of the identity: row j of X is final after
     // dividing by L[j][j]; then rows i > j subtract L[i][j] * row j (columns c <= j)
+    __shared__ double inv_s[1];
     for (int j = 0; j < l; ++j) {
       if (tid == 0) inv_s[0] = 1.0 / LA(j, j);
       __syncthreads();
@@ -337,7 +356,10 @@ __global__ void __launch_bounds__(32) chol_warp_kernel(const CholDesc* __restric
   const int l = int(d.l), lane = threadIdx.x, ld = l | 1;
   double* Gg = G + d.g_off;
   auto LA = [&](int i, int k) -> double& { return wsm[i * ld + k]; };
-  for (int e = lane; e < l * l; e += 32) LA(e % l, e / l) = Gg[e];
+  for (int e = lane; e < l * l; e += 32) {  // upper triangle of G, as in chol_inv_body
+    const int i = e % l, k = e / l;
+    LA(i, k) = Gg[i <= k ? e : k + i * l];
+  }
   __syncwarp();
   double t = 0;
   for (int g0 = 0; g0 < l; g0 += 32) t += warp_sum_d(g0 + lane < l ? LA(g0 + lane, g0 + lane) : 0.0);
