@@ -24,15 +24,35 @@ static void cuda_ok(cudaError_t e, const char* what) {
   }
 }
 
-// persistent device copy of a host table (plans live as long as the cache)
-template <class T>
-static T* dev_table(const std::vector<T>& v) {
-  T* d = nullptr;
-  size_t bytes = sizeof(T) * std::max<size_t>(v.size(), 1);
-  cuda_ok(cudaMalloc(&d, bytes), "cudaMalloc(plan)");
-  if (!v.empty()) cuda_ok(cudaMemcpy(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice), "plan upload");
-  return d;
-}
+// Device copies of a plan's host tables.  Each table is a stream-ordered pool allocation filled by an
+// asynchronous copy, so building a plan neither allocates with cudaMalloc nor waits for the device
+// (both stall a queue that a synchronisation has just drained).  The host tables live as long as the
+// plan, so no copy can read freed host memory; the device memory is released in stream order when
+// the last user drops the plan.
+struct PlanMem {
+  std::vector<void*> dev;
+  std::vector<std::shared_ptr<const void>> host;
+  PlanMem() = default;
+  PlanMem(const PlanMem&) = delete;
+  PlanMem& operator=(const PlanMem&) = delete;
+  ~PlanMem() {
+    for (void* d : dev) dev_free(d);
+  }
+  template <class T>
+  T* table(std::vector<T> v) {
+    auto h = std::make_shared<const std::vector<T>>(std::move(v));
+    T* d = static_cast<T*>(dev_alloc(sizeof(T) * std::max<size_t>(h->size(), 1)));
+    dev.push_back(d);
+    if (!h->empty())
+      cuda_ok(cudaMemcpyAsync(d, h->data(), sizeof(T) * h->size(), cudaMemcpyHostToDevice, stream()), "plan upload");
+    host.push_back(h);
+    return d;
+  }
+};
+
+// plan caches hold at most this many plans each; a full cache is emptied (plans still in use stay
+// alive through their shared pointers), which bounds the memory of runs whose shapes keep changing
+constexpr size_t kPlanCacheCap = 4096;
 
 // ======================================================================= meta
 namespace {
@@ -119,6 +139,7 @@ Tensor zeros(const MetaPtr& m) {
 // ======================================================================= permute plans
 namespace {
 struct PermPlan {
+  PlanMem mem;
   MetaPtr out;
   bool needs_zero = false;
   int n_tasks = 0;
@@ -131,6 +152,7 @@ struct PermPlan {
   double bytes = 0;  // algorithmic: every output written once, every contribution read once
 };
 struct GemmPlan {
+  PlanMem mem;
   MetaPtr out;
   double flops = 0;  // useful 2*m*n*k summed over groups
   int n_tiles = 0, tile = 16;
@@ -153,7 +175,9 @@ struct GemmPlan {
   OzGroup* d_oz_groups = nullptr;
   TcPackTask* d_oz_tasks = nullptr;
   GemmTile* d_oz_tiles = nullptr;
-  // FP64 launch shape (tile edge, split-K): the built-in rule, or the autotuner's choice
+  // FP64 launch shape (tile edge, split-K): the built-in rule, or the autotuner's choice (built on
+  // first use); the FP32 form's one-CTA-per-tile list likewise
+  bool f64_ready = false, tiles_ready = false;
   F64Plan f64;
   GemmTile* d_f64_tiles = nullptr;
   SplitReduce* d_f64_red = nullptr;
@@ -163,13 +187,13 @@ std::shared_ptr<PermPlan> upload_tables(const PermTables& t) {
   plan->out = t.out;
   plan->n_tasks = int(t.tasks.size());
   plan->needs_zero = t.needs_zero;
-  plan->d_tasks = dev_table(t.tasks);
+  plan->d_tasks = plan->mem.table(t.tasks);
   const PermRows rows = perm_rows(t.tasks.data(), int(t.tasks.size()), t.contribs.data(), int(t.contribs.size()));
   plan->total_rows = rows.total_rows;
   plan->group = rows.group;
   plan->narrow = rows.narrow;
-  plan->d_row_start = dev_table(rows.row_start);
-  plan->d_contribs = dev_table(t.contribs);
+  plan->d_row_start = plan->mem.table(rows.row_start);
+  plan->d_contribs = plan->mem.table(t.contribs);
   for (const auto& task : t.tasks) plan->bytes += 8.0 * double(task.nelem) * (1 + task.n_contrib);
   return plan;
 }
@@ -395,6 +419,7 @@ std::shared_ptr<PermPlan> get_perm_plan(const TensorMeta& m, uint32_t mask, int 
   auto plan = upload_tables(build_perm_tables(m, mask, shift, p));
   std::lock_guard<std::mutex> lk(g_plan_mu);
   ++g_stats.perm_misses;
+  if (g_perm_plans.size() >= kPlanCacheCap) g_perm_plans.clear();
   g_perm_plans[key] = plan;
   return plan;
 }
@@ -412,19 +437,8 @@ Tensor run_perm_plan(const PermPlan& plan, const Tensor& src) {
 CacheStats cache_stats() { return g_stats; }
 
 void clear_plan_caches() {
+  // the plans' device tables are released in stream order by their last owners
   std::lock_guard<std::mutex> lk(g_plan_mu);
-  cudaStreamSynchronize(stream());
-  for (auto& [k, p] : g_perm_plans) { cudaFree(p->d_tasks); cudaFree(p->d_row_start); cudaFree(p->d_contribs); }
-  for (auto& [k, p] : g_gemm_plans) {
-    cudaFree(p->d_descs);
-    cudaFree(p->d_tiles);
-    cudaFree(p->d_f64_tiles);
-    cudaFree(p->d_f64_red);
-    cudaFree(p->d_oz_groups);
-    cudaFree(p->d_oz_tasks);
-    cudaFree(p->d_oz_tiles);
-    cudaFree(p->d_oz_red);
-  }
   g_perm_plans.clear();
   g_gemm_plans.clear();
 }
@@ -472,7 +486,8 @@ Tensor permute_adj(const Tensor& t0, int shift, const std::vector<int>& p) {
     plan = upload_tables(build_perm_adj_tables(*t.meta, shift, p));
     std::lock_guard<std::mutex> lk(g_plan_mu);
     ++g_stats.perm_misses;
-    g_perm_plans[key] = plan;
+    if (g_perm_plans.size() >= kPlanCacheCap) g_perm_plans.clear();
+  g_perm_plans[key] = plan;
   }
   return run_perm_plan(*plan, t);
 }
@@ -512,7 +527,8 @@ Tensor adjoint(const Tensor& t0) {
     }
     plan = tb.finish(out);
     std::lock_guard<std::mutex> lk(g_plan_mu);
-    g_perm_plans[key] = plan;
+    if (g_perm_plans.size() >= kPlanCacheCap) g_perm_plans.clear();
+  g_perm_plans[key] = plan;
   }
   return run_perm_plan(*plan, t);
 }
@@ -584,25 +600,12 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
     plan->out = gt.out;
     const std::vector<xgb_gemm_desc>& descs = gt.descs;
     plan->tile = choose_gemm_tile(descs.data(), int(descs.size()));
-    std::vector<GemmTile> tiles;
-    for (size_t g = 0; g < descs.size(); ++g) {
-      int64_t tm = (descs[g].m + plan->tile - 1) / plan->tile, tn = (descs[g].n + plan->tile - 1) / plan->tile;
-      for (int64_t y = 0; y < tn; ++y)
-        for (int64_t x = 0; x < tm; ++x) tiles.push_back({int32_t(g), int32_t(x), int32_t(y), plan->tile});
-    }
-    order_tiles_by_work(tiles, descs.data());
-    plan->n_tiles = int(tiles.size());
     plan->host_descs = descs;
-    plan->d_descs = dev_table(descs);
-    plan->d_tiles = dev_table(tiles);
-    const F64Config cfg =
-        gemm_f64_config(descs.data(), int(descs.size()), a.data(), b.data(), {plan->tile, 0}, stream());
-    plan->f64 = plan_gemm_f64(descs.data(), int(descs.size()), cfg);
-    plan->d_f64_tiles = dev_table(plan->f64.tiles);
-    plan->d_f64_red = dev_table(plan->f64.red);
+    plan->d_descs = plan->mem.table(descs);
     for (const auto& d : descs) plan->flops += 2.0 * double(d.m) * double(d.n) * double(d.k);
     std::lock_guard<std::mutex> lk(g_plan_mu);
     ++g_stats.gemm_misses;
+    if (g_gemm_plans.size() >= kPlanCacheCap) g_gemm_plans.clear();
     g_gemm_plans[key] = plan;
   }
   Tensor out = empty_like_meta(plan->out);
@@ -615,9 +618,9 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
         plan->n_tc_tasks = int(tp.tasks.size());
         plan->tc_a_floats = tp.a_floats;
         plan->tc_b_floats = tp.b_floats;
-        plan->d_tc_groups = dev_table(tp.groups);
-        plan->d_tc_tasks = dev_table(tp.tasks);
-        plan->d_tc_tiles = dev_table(tp.tiles);
+        plan->d_tc_groups = plan->mem.table(tp.groups);
+        plan->d_tc_tasks = plan->mem.table(tp.tasks);
+        plan->d_tc_tiles = plan->mem.table(tp.tiles);
         plan->tc_ready = true;
       }
     }
@@ -636,7 +639,7 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
     // autotuner measures faster for this size bucket (built-in rule: average k >= 64)
     const auto& hd = plan->host_descs;
     const F64Config rc = gemm_f64_config(hd.data(), int(hd.size()), a.data(), b.data(),
-                                         F64Config{plan->f64.tile, 0, f64tc_heuristic(hd.data(), int(hd.size()))},
+                                         F64Config{plan->tile, 0, f64tc_heuristic(hd.data(), int(hd.size()))},
                                          stream(), true);
     std::lock_guard<std::mutex> lk(g_plan_mu);
     plan->oz_route = rc.tc;
@@ -652,10 +655,10 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
         plan->oz_a_bytes = op.a_bytes;
         plan->oz_b_bytes = op.b_bytes;
         plan->oz_rowmax = op.rowmax;
-        plan->d_oz_groups = dev_table(op.groups);
-        plan->d_oz_tasks = dev_table(op.tasks);
-        plan->d_oz_tiles = dev_table(op.tiles);
-        plan->d_oz_red = dev_table(op.red);
+        plan->d_oz_groups = plan->mem.table(op.groups);
+        plan->d_oz_tasks = plan->mem.table(op.tasks);
+        plan->d_oz_tiles = plan->mem.table(op.tiles);
+        plan->d_oz_red = plan->mem.table(op.red);
         plan->n_oz_red = int(op.red.size());
         plan->oz_slots = op.slots;
         plan->oz_ready = true;
@@ -700,11 +703,39 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
     return out;
   }
   if (g_gemm_precision == XGB_PREC_FP32) {
+    {
+      std::lock_guard<std::mutex> lk(g_plan_mu);
+      if (!plan->tiles_ready) {  // one tile x tile CTA per output tile, longest k first
+        const auto& descs = plan->host_descs;
+        std::vector<GemmTile> tiles;
+        for (size_t g = 0; g < descs.size(); ++g) {
+          int64_t tm = (descs[g].m + plan->tile - 1) / plan->tile, tn = (descs[g].n + plan->tile - 1) / plan->tile;
+          for (int64_t y = 0; y < tn; ++y)
+            for (int64_t x = 0; x < tm; ++x) tiles.push_back({int32_t(g), int32_t(x), int32_t(y), plan->tile});
+        }
+        order_tiles_by_work(tiles, descs.data());
+        plan->n_tiles = int(tiles.size());
+        plan->d_tiles = plan->mem.table(std::move(tiles));
+        plan->tiles_ready = true;
+      }
+    }
     prof_begin(K_GEMM_F32, stream());
     launch_gemm_f32(plan->d_descs, plan->d_tiles, plan->n_tiles, plan->tile, a.data(), b.data(), out.data(), 1.0, 0.0,
                     stream());
     prof_end(K_GEMM_F32, stream(), plan->flops);
     return out;
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    if (!plan->f64_ready) {  // FP64 CUDA-core launch shape: the autotuner's choice or the built-in rule
+      const auto& descs = plan->host_descs;
+      const F64Config cfg =
+          gemm_f64_config(descs.data(), int(descs.size()), a.data(), b.data(), {plan->tile, 0}, stream());
+      plan->f64 = plan_gemm_f64(descs.data(), int(descs.size()), cfg);
+      plan->d_f64_tiles = plan->mem.table(plan->f64.tiles);
+      plan->d_f64_red = plan->mem.table(plan->f64.red);
+      plan->f64_ready = true;
+    }
   }
   prof_begin(K_GEMM, stream());
   run_f64_plan(plan->f64, plan->d_descs, plan->d_f64_tiles, plan->d_f64_red, a.data(), b.data(), out.data(), 1.0, 0.0,
@@ -883,6 +914,7 @@ Tensor identity(const Sym& s, const std::vector<BasisPtr>& dom, const std::vecto
 // ======================================================================= SVD / truncation
 namespace {
 struct SvdPlan {
+  PlanMem mem;
   int n = 0;
   int64_t u_total = 0, s_total = 0, v_total = 0, work_total = 0, maxk = 0;
   double lapack_flops = 0;  // thin R-SVD work 6 m n^2 + 20 n^3 (m >= n; Golub & Van Loan, Table 5.5.1)
@@ -930,12 +962,13 @@ std::shared_ptr<SvdPlan> get_svd_plan(const TensorMeta& m) {
     p->s_begin.push_back(p->s_total);
   }
   if (p->maxk > 8192) throw std::runtime_error("tSVD: sector block larger than 8192 columns");
-  p->d_descs = dev_table(descs);
+  p->d_descs = p->mem.table(descs);
   p->h_descs = descs;
-  p->d_work_off = dev_table(woff);
-  p->d_s_begin = dev_table(p->s_begin);
-  p->d_deg = dev_table(deg);
+  p->d_work_off = p->mem.table(woff);
+  p->d_s_begin = p->mem.table(p->s_begin);
+  p->d_deg = p->mem.table(deg);
   std::lock_guard<std::mutex> lk(g_plan_mu);
+  if (g_svd_plans.size() >= kPlanCacheCap) g_svd_plans.clear();
   g_svd_plans[m.id] = p;
   return p;
 }
