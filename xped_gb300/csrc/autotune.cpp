@@ -190,8 +190,19 @@ int tune_gemm_f64(const xgb_gemm_desc* d, int n, const double* A, const double* 
     dev_free(dt);
     dev_free(dr);
     times_ms[c] = best_ms;
-    if (times_ms[c] < times_ms[best]) best = c;
   }
+  // the fastest, except that a candidate within 3 % of it with a larger tile (then fewer split waves)
+  // wins: FP64-bound lists time alike on every tile edge, and larger tiles mean shorter launch tables
+  // to build whenever a step brings new shapes
+  for (int c = 1; c < kNumCandidates; ++c)
+    if (times_ms[c] < times_ms[best]) best = c;
+  const double near = 1.03 * times_ms[best];
+  for (int c = kNumCandidates - 1; c >= 0; --c)
+    if (times_ms[c] <= near) {
+      const bool larger = kTiles[c / 4] > kTiles[best / 4];
+      const bool fewer = kTiles[c / 4] == kTiles[best / 4] && kWaves[c % 4] < kWaves[best % 4];
+      if (larger || fewer) best = c;
+    }
   if (allow_tc) {
     run_gemm_oz_host(d, n, A, B, scratch, 1.0, 0.0, s);  // warm-up
     float best_ms = 1e30f;

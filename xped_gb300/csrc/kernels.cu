@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
@@ -263,9 +264,30 @@ void launch_gemm_f32(const xgb_gemm_desc* d_descs, const GemmTile* d_tiles, int 
 }
 
 void order_tiles_by_work(std::vector<GemmTile>& tiles, const xgb_gemm_desc* descs) {
+  // stable counting sort on the k extent, longest first: a list holds few distinct extents but up to
+  // ~10^5 tiles, and the plans of a step whose shapes changed are built while the GPU waits
   auto extent = [&](const GemmTile& t) { return int64_t(t.k1 < 0 ? descs[t.g].k : t.k1) - t.k0; };
-  std::stable_sort(tiles.begin(), tiles.end(),
-                   [&](const GemmTile& a, const GemmTile& b) { return extent(a) > extent(b); });
+  std::map<int64_t, size_t, std::greater<int64_t>> slot;  // extent -> first position, descending
+  for (const auto& t : tiles) ++slot[extent(t)];
+  if (slot.size() <= 1) return;
+  size_t off = 0;
+  for (auto& [e, c] : slot) {
+    const size_t n = c;
+    c = off;
+    off += n;
+  }
+  std::vector<GemmTile> out(tiles.size());
+  int64_t last_e = -1;
+  size_t* last_slot = nullptr;
+  for (const auto& t : tiles) {
+    const int64_t e = extent(t);
+    if (e != last_e) {  // runs of equal extents are common: one map lookup per run
+      last_slot = &slot.find(e)->second;
+      last_e = e;
+    }
+    out[(*last_slot)++] = t;
+  }
+  tiles.swap(out);
 }
 
 int choose_gemm_tile(const xgb_gemm_desc* descs, int n) {

@@ -9,6 +9,7 @@
 #include <numeric>
 #include <sstream>
 #include <stdexcept>
+#include <unordered_set>
 
 namespace xgb {
 
@@ -398,19 +399,26 @@ int64_t Qbasis::left_offset(const FusionTree& t) const {
 }
 
 std::string Qbasis::key() const {
-  std::ostringstream os;
-  os << sym.kind << ':' << sym.N << '|' << depth << '|' << conj_flag << '|';
+  // binary, not text: combined bases hold thousands of trees and are keyed every time one is built
+  size_t n = 16;
+  for (const auto& ts : trees) n += 16 + ts.size() * (12 + 12 * kMaxRank);
+  std::string k;
+  k.reserve(n);
+  auto put = [&](int64_t v) { k.append(reinterpret_cast<const char*>(&v), sizeof(v)); };
+  put(int64_t(sym.kind));
+  put(int64_t(sym.N));
+  put(int64_t(depth) * 2 + (conj_flag ? 1 : 0));
   for (size_t i = 0; i < qs.size(); ++i) {
-    os << qs[i] << ',' << dims[i] << '[';
+    put(qs[i]);
+    put(dims[i]);
+    put(int64_t(trees[i].size()));
     for (const auto& t : trees[i]) {
-      os << int(t.rank) << ';' << t.qc << ';' << t.dual << ';';
-      for (int k = 0; k < t.rank; ++k) os << t.qu[k] << ',' << t.dims[k] << ',';
-      for (int k = 0; k < t.nqi(); ++k) os << t.qi[k] << ',';
-      os << '/';
+      put((int64_t(t.rank) << 48) ^ (int64_t(t.dual) << 32) ^ int64_t(uint32_t(t.qc)));
+      for (int m = 0; m < t.rank; ++m) put((int64_t(t.qu[m]) << 32) ^ int64_t(uint32_t(t.dims[m])));
+      for (int m = 0; m < t.nqi(); ++m) put(t.qi[m]);
     }
-    os << ']';
   }
-  return os.str();
+  return k;
 }
 
 namespace {
@@ -542,6 +550,7 @@ BasisPtr basis_combine(const BasisPtr& a, const BasisPtr& bb) {
   const Sym& s = a->sym;
   std::vector<int> order;
   std::unordered_map<int, std::vector<FusionTree>> trees;
+  std::unordered_map<int, std::unordered_set<FusionTree, TreeHash>> seen;  // membership, O(1) per tree
   int buf[64];
   for (size_t i1 = 0; i1 < a->qs.size(); ++i1) {
     for (size_t i2 = 0; i2 < bb->qs.size(); ++i2) {
@@ -554,7 +563,7 @@ BasisPtr basis_combine(const BasisPtr& a, const BasisPtr& bb) {
             tt.qc = q;
             auto& lst = trees[q];
             if (lst.empty()) order.push_back(q);
-            if (std::find(lst.begin(), lst.end(), tt) == lst.end()) lst.push_back(tt);
+            if (seen[q].insert(tt).second) lst.push_back(tt);
           }
       }
     }

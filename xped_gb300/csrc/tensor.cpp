@@ -696,7 +696,6 @@ Tensor matmul(const Tensor& a0, const Tensor& b0, bool adj_a, bool adj_b) {
     launch_gemm_tc(plan->d_descs, dg, dk, int(tp.tasks.size()), dt, int(tp.tiles.size()), a.data(), b.data(), ap, bp,
                    out.data(), 1.0, 0.0, st, 1);
     prof_end(K_GEMM_TC, st, plan->flops);
-    cuda_ok(cudaStreamSynchronize(st), "sync");  // the host tables above are pageable
     for (void* p : {static_cast<void*>(dg), static_cast<void*>(dk), static_cast<void*>(dt), static_cast<void*>(ap),
                     static_cast<void*>(bp)})
       dev_free(p);
@@ -904,7 +903,6 @@ Tensor identity(const Sym& s, const std::vector<BasisPtr>& dom, const std::vecto
     cuda_ok(cudaMemcpyAsync(dones, ones.data(), sizeof(double) * ones.size(), cudaMemcpyHostToDevice, stream()), "h2d");
     cuda_ok(cudaMemcpyAsync(dd, descs.data(), sizeof(xgb_copy2d_desc) * descs.size(), cudaMemcpyHostToDevice, stream()), "h2d");
     launch_copy2d(dd, int(descs.size()), mx, dones, t.data(), stream());
-    cuda_ok(cudaStreamSynchronize(stream()), "sync");
     dev_free(dones);
     dev_free(dd);
   }
@@ -1064,8 +1062,7 @@ SVDResult truncate_spectra(const TensorMeta& m, const Spectra& sp, int64_t max_k
   launch_copy2d(dd + nb, int(nb), mxv, sp.V, res.Vdag.data(), st);
   launch_diag_from_vec(dd + 2 * nb, int(nb), mxs, -1, sp.S, res.S.data(), st);
   prof_end(K_COPY2D, st, 16.0 * double(res.U.size() + res.Vdag.size() + res.S.size()));
-  cuda_ok(cudaStreamSynchronize(st), "sync");  // descriptors are pageable host memory
-  dev_free(dd);
+  dev_free(dd);  // stream-ordered: released after the copies (the pageable descriptors were staged on return)
   return res;
 }
 
@@ -1128,7 +1125,6 @@ std::pair<Tensor, Tensor> tqr(const Tensor& t0) {
     cuda_ok(cudaMemcpyAsync(dd, descs.data(), sizeof(xgb_qr_desc) * descs.size(), cudaMemcpyHostToDevice, st), "h2d");
     cuda_ok(cudaMemcpyAsync(dw, woff.data(), sizeof(int64_t) * woff.size(), cudaMemcpyHostToDevice, st), "h2d");
     launch_qr(dd, dw, int(descs.size()), t.data(), Q.data(), R.data(), W, st);
-    cuda_ok(cudaStreamSynchronize(st), "sync");
     dev_free(dd);
     dev_free(dw);
     dev_free(W);
@@ -1153,7 +1149,6 @@ static void diag_apply_inplace(Tensor& t, std::initializer_list<int> fns) {
     launch_diag_apply(dd, int(descs.size()), mx, fn, t.data(), stream());
     prof_end(K_DIAG, stream(), 16.0 * double(mx) * double(descs.size()));
   }
-  cuda_ok(cudaStreamSynchronize(stream()), "sync");
   dev_free(dd);
 }
 
