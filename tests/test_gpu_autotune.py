@@ -66,7 +66,11 @@ def test_tuner_picks_the_measured_best(which):
     best = C.c_int32()
     assert L.xgb_autotune_gemm(len(blocks), arr, bufs[0], bufs[1], times, C.byref(best)) == 0, last_error()
     t = np.array(times[:])
-    assert best.value == int(np.argmin(t))
+    # the measured fastest, or - within 3 % of it - the candidate with the largest tile, then the fewest
+    # split waves (FP64-bound lists time alike on every tile edge; larger tiles mean shorter tables)
+    near = [c for c in range(ncand) if t[c] <= 1.03 * t.min()]
+    expect = max(near, key=lambda c: (tiles[c], -waves[c]))
+    assert best.value == expect, (best.value, expect, t)
     # independent re-timing of every candidate through the public entry point (min of 3 runs, CUDA events
     # on the library stream; these times include the per-call table upload the tuner leaves out)
     re = []

@@ -529,13 +529,23 @@ OzPlanHost build_oz_plan(const xgb_gemm_desc* descs, int n) {
     p.groups.push_back(gr);
   }
   // output tiles and their K ranges.  One CTA runs per SM (its stages and TMEM fill one), so the K
-  // slices of all tiles are cut into ranges of at most about total / SMs slices (and at least
-  // kMinSplit): the launch then is about one wave of CTAs with equal work, the largest tiles split the
-  // most.  The partial tiles of a split tile are added by a fixed-order reduce.
-  int64_t work = 0;
-  for (const auto& gr : p.groups) work += int64_t(gr.a_tiles) * gr.b_tiles * gr.slices;
+  // slices of all tiles are cut into ranges of at most `cap` slices (at least kMinSplit), the largest
+  // tiles split the most: cap starts at total / SMs and grows until the CTAs fit one wave (a second,
+  // partial wave costs a whole CTA's fixed part - first load, drain, epilogue - on the SMs it uses).
+  // The partial tiles of a split tile are added by a fixed-order reduce.
+  int64_t work = 0, smax = 0;
+  for (const auto& gr : p.groups) {
+    work += int64_t(gr.a_tiles) * gr.b_tiles * gr.slices;
+    smax = std::max<int64_t>(smax, gr.slices);
+  }
   const int64_t sms = num_sms() > 0 ? num_sms() : 152;
-  const int64_t cap = std::max<int64_t>(kMinSplit, (work + sms - 1) / sms);
+  auto ctas = [&](int64_t cp) {
+    int64_t c = 0;
+    for (const auto& gr : p.groups) c += int64_t(gr.a_tiles) * gr.b_tiles * std::max<int64_t>(1, (gr.slices + cp - 1) / cp);
+    return c;
+  };
+  int64_t cap = std::max<int64_t>(kMinSplit, (work + sms - 1) / sms);
+  while (cap < smax && ctas(cap) > sms) ++cap;
   for (int g = 0; g < n; ++g) {
     const OzGroup& gr = p.groups[g];
     const int64_t splits = std::max<int64_t>(1, (gr.slices + cap - 1) / cap);

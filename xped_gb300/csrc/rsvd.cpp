@@ -56,9 +56,22 @@ double* alloc_d(int64_t n) { return static_cast<double*>(dev_alloc(sizeof(double
 // tile is split so that about two CTAs per SM run; the partial tiles land in a workspace and
 // one reduce launch adds them in a fixed order (deterministic result).  With autotuning on, the
 // tile edge and the split target are the tuned ones of the list's size bucket.
+// allow_tc (callers running the FP64-accurate tensor-core form): the autotuner may also route the list
+// to that form when it measures it faster (built-in rule: average k >= 64), computing C in full.
 void grouped_gemm(const std::vector<xgb_gemm_desc>& d, const double* A, const double* B, double* C, cudaStream_t s,
-                  double alpha = 1.0, double beta = 0.0, int shape = kGemmDense) {
+                  double alpha = 1.0, double beta = 0.0, int shape = kGemmDense, bool allow_tc = false) {
   if (d.empty()) return;
+  if (allow_tc) {
+    const F64Config tfb{choose_gemm_tile(d.data(), int(d.size())), 2, f64tc_heuristic(d.data(), int(d.size()))};
+    if (gemm_f64_config(d.data(), int(d.size()), A, B, tfb, s, true).tc) {
+      double flops = 0;
+      for (const auto& g : d) flops += 2.0 * double(g.m) * double(g.n) * double(g.k);
+      prof_begin(K_GEMM_OZ, s);
+      run_gemm_oz_host(d.data(), int(d.size()), A, B, C, alpha, beta, s);
+      prof_end(K_GEMM_OZ, s, flops);
+      return;
+    }
+  }
   const F64Config fallback{choose_gemm_tile(d.data(), int(d.size())), 2};
   const F64Config cfg = gemm_f64_config(d.data(), int(d.size()), A, B, fallback, s);
   const F64Plan p = plan_gemm_f64(d.data(), int(d.size()), cfg, shape);
@@ -216,7 +229,8 @@ void batched_svd(const std::vector<xgb_svd_desc>& d, const double* A, double* U,
 // between Y and Q; returns the buffer holding the basis (Q for 3 passes, Y for
 // 2); the other one holds garbage afterwards.
 double* orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64_t>& cols,
-                       const std::vector<int64_t>& y_off, double* Y, double* Q, cudaStream_t s, int passes = 3) {
+                       const std::vector<int64_t>& y_off, double* Y, double* Q, cudaStream_t s, int passes = 3,
+                       bool exact_tc = false) {
   const size_t n = rows.size();
   if (n == 0) return passes == 2 ? Y : Q;
   std::vector<CholDesc> cd;
@@ -244,20 +258,20 @@ double* orthonormalise(const std::vector<int64_t>& rows, const std::vector<int64
   // pass 1 (shifted): Y -> Q;  pass 2: Q -> Y;  pass 3: Y -> Q.  The Gram matrices are computed on and
   // above the diagonal only (the Cholesky reads that triangle), and Q R^-1 skips the zero rows of the
   // upper-triangular R^-1: about half the FP64 work of the full products.
-  grouped_gemm(gram_y, Y, Y, G, s, 1.0, 0.0, kGemmSymUpper);
+  grouped_gemm(gram_y, Y, Y, G, s, 1.0, 0.0, kGemmSymUpper, exact_tc);
   prof_begin(K_QR, s);
   launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, kShift, bad, s);
   prof_end(K_QR, s, 0.0);
   grouped_gemm(mul_yq, Y, Ri, Q, s, 1.0, 0.0, kGemmTriB);
   if (passes >= 2) {
-    grouped_gemm(gram_q, Q, Q, G, s, 1.0, 0.0, kGemmSymUpper);
+    grouped_gemm(gram_q, Q, Q, G, s, 1.0, 0.0, kGemmSymUpper, exact_tc);
     prof_begin(K_QR, s);
     launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, 0.0, bad, s);
     prof_end(K_QR, s, 0.0);
     grouped_gemm(mul_qy, Q, Ri, Y, s, 1.0, 0.0, kGemmTriB);
   }
   if (passes >= 3) {
-    grouped_gemm(gram_y, Y, Y, G, s, 1.0, 0.0, kGemmSymUpper);
+    grouped_gemm(gram_y, Y, Y, G, s, 1.0, 0.0, kGemmSymUpper, exact_tc);
     prof_begin(K_QR, s);
     launch_chol_inv(sc.at<CholDesc>(o), int(n), max_l, G, Ri, 0.0, bad, s);
     prof_end(K_QR, s, 0.0);
@@ -393,7 +407,7 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
           grouped_gemm(g, t.data(), cur, Z, st);
         }
         // Omega's storage holds Qz (same layout as Z)
-        double* qz = orthonormalise(src, srl, szo, Z, Om, st, kInterPasses);
+        double* qz = orthonormalise(src, srl, szo, Z, Om, st, kInterPasses, exact_tc);
         if (use_oz) {
           oz_n->apply(t.data(), qz, Y, st);
         } else if (p < lead) {
@@ -403,7 +417,7 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
           for (int a : sub) g.push_back({rr[a], rl[a], rc[a], m.offset[R[a]], rr[a], zo[a], rc[a], yo[a], rr[a], 0, 0});
           grouped_gemm(g, t.data(), qz, Y, st);
         }
-        cur = orthonormalise(srr, srl, syo, Y, Q, st, p + 1 == iters ? 3 : kInterPasses);
+        cur = orthonormalise(srr, srl, syo, Y, Q, st, p + 1 == iters ? 3 : kInterPasses, exact_tc);
       }
     };
     // Rayleigh-Ritz on span(Q) for `sub`: the SVD of B = Q^T A (l x n) through its transpose's QR,
@@ -437,13 +451,13 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
         prof_begin(K_COPY2D, st);
         launch_copy2d(sc.at<xgb_copy2d_desc>(oz), int(zc.size()), mxz, Z, Bb, st);
         prof_end(K_COPY2D, st, 16.0 * double(zt));
-        orthonormalise(src, srl, szo, Z, Om, st, 3);  // Q_z in Om (Z's layout)
+        orthonormalise(src, srl, szo, Z, Om, st, 3, exact_tc);  // Q_z in Om (Z's layout)
         g.clear();
         for (size_t s2 = 0; s2 < sub.size(); ++s2) {  // R = Q_z^T Z (l x l) into Y
           const int a = sub[s2];
           g.push_back({rl[a], rl[a], rc[a], zo[a], rc[a], bo[R[a]], rc[a], r_off[s2], rl[a], 1, 0});
         }
-        grouped_gemm(g, Om, Bb, Y, st);
+        grouped_gemm(g, Om, Bb, Y, st, 1.0, 0.0, kGemmDense, exact_tc);
         prof_begin(K_COPY2D, st);
         launch_copy2d(sc.at<xgb_copy2d_desc>(orr), int(rc2.size()), mxr, Y, Bb, st);
         prof_end(K_COPY2D, st, 16.0 * double(rt));
@@ -530,7 +544,7 @@ SVDResult tsvd_randomized(const Tensor& t0, int64_t max_keep, double eps_svd, co
       } else {
         grouped_gemm(g, t.data(), Om, Y, st);
       }
-      double* q0 = orthonormalise(rr, rl, yo, Y, Q, st, power_iters > 0 ? kInterPasses : 3);
+      double* q0 = orthonormalise(rr, rl, yo, Y, Q, st, power_iters > 0 ? kInterPasses : 3, exact_tc);
       std::vector<int> all(nr);
       for (int a = 0; a < nr; ++a) all[a] = a;
       iterate(all, power_iters, q0, tc_iters, tc_t.get(), tc_n.get());
