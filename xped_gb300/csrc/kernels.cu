@@ -142,8 +142,11 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __r
                                                         double alpha, double beta, double* __restrict__ ws) {
   constexpr int BK = 16;
   constexpr int R = TILE / 16;
-  __shared__ T As[BK][TILE + 1];
-  __shared__ T Bs[BK][TILE + 1];
+  constexpr int PER = TILE * BK / 256;  // staged elements of A (and of B) per thread and k step
+  // two stages: the global loads of k step s + 1 are in flight (in registers) while step s is
+  // multiplied out of shared memory, and one barrier per step separates the stages
+  __shared__ T As[2][BK][TILE + 1];
+  __shared__ T Bs[2][BK][TILE + 1];
   const GemmTile t = tiles[blockIdx.x];
   const xgb_gemm_desc d = descs[t.g];
   const int64_t kbeg = t.k0, kend = t.k1 < 0 ? d.k : t.k1;
@@ -156,38 +159,61 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __r
 #pragma unroll
     for (int j = 0; j < R; ++j) acc[i][j] = T(0);
 
-  for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
-    // A tile: TILE rows x BK
-    for (int e = tid; e < TILE * BK; e += 256) {
+  T ra[PER], rb[PER];
+  auto fetch = [&](int64_t k0) {
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int e = tid + 256 * u;
       int i, kk;
       if (d.trans_a) { kk = e % BK; i = e / BK; } else { i = e % TILE; kk = e / TILE; }
-      int64_t gi = row0 + i, gk = k0 + kk;
+      const int64_t gi = row0 + i, gk = k0 + kk;
       double v = 0.0;
       if (gi < d.m && gk < kend) v = d.trans_a ? A[d.a_off + gk + gi * d.lda] : A[d.a_off + gi + gk * d.lda];
-      As[kk][i] = T(v);
+      ra[u] = T(v);
+      int j, kb;
+      if (d.trans_b) { j = e % TILE; kb = e / TILE; } else { kb = e % BK; j = e / BK; }
+      const int64_t gj = col0 + j, gkb = k0 + kb;
+      double w = 0.0;
+      if (gj < d.n && gkb < kend) w = d.trans_b ? B[d.b_off + gj + gkb * d.ldb] : B[d.b_off + gkb + gj * d.ldb];
+      rb[u] = T(w);
     }
-    for (int e = tid; e < TILE * BK; e += 256) {
-      int j, kk;
-      if (d.trans_b) { j = e % TILE; kk = e / TILE; } else { kk = e % BK; j = e / BK; }
-      int64_t gj = col0 + j, gk = k0 + kk;
-      double v = 0.0;
-      if (gj < d.n && gk < kend) v = d.trans_b ? B[d.b_off + gj + gk * d.ldb] : B[d.b_off + gk + gj * d.ldb];
-      Bs[kk][j] = T(v);
+  };
+  auto stash = [&](int st) {
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int e = tid + 256 * u;
+      int i, kk;
+      if (d.trans_a) { kk = e % BK; i = e / BK; } else { i = e % TILE; kk = e / TILE; }
+      As[st][kk][i] = ra[u];
+      int j, kb;
+      if (d.trans_b) { j = e % TILE; kb = e / TILE; } else { kb = e % BK; j = e / BK; }
+      Bs[st][kb][j] = rb[u];
     }
-    __syncthreads();
+  };
+  if (kbeg < kend) {
+    fetch(kbeg);
+    stash(0);
+  }
+  __syncthreads();
+  int st = 0;
+  for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
+    const bool more = k0 + BK < kend;
+    if (more) fetch(k0 + BK);
     const int kmax = (kend - k0) < BK ? int(kend - k0) : BK;
     for (int kk = 0; kk < kmax; ++kk) {
       T a[R], b[R];
 #pragma unroll
-      for (int r = 0; r < R; ++r) a[r] = As[kk][tx + 16 * r];
+      for (int r = 0; r < R; ++r) a[r] = As[st][kk][tx + 16 * r];
 #pragma unroll
-      for (int c = 0; c < R; ++c) b[c] = Bs[kk][ty + 16 * c];
+      for (int c = 0; c < R; ++c) b[c] = Bs[st][kk][ty + 16 * c];
 #pragma unroll
       for (int r = 0; r < R; ++r)
 #pragma unroll
         for (int c = 0; c < R; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
     }
+    if (more) stash(st ^ 1);
     __syncthreads();
+    st ^= 1;
   }
   if (t.slot >= 0) {  // split-K partial: the whole tile, raw sums, column-major TILE x TILE
     double* w = ws + int64_t(t.slot) * TILE * TILE;
