@@ -187,6 +187,15 @@ def test_f64tc_long_k_and_alpha_beta():
     assert err < 3e-13
 
 
+def test_f64tc_short_k_many_tiles_without_split():
+    """Outer-product-like list (k = 12, ~1000 output tiles): every tile takes its whole K range, so the plan
+    has no split-K partials and no reduce table."""
+    blocks = [(600, 600, 12, 0, 0), (1000, 1000, 12, 1, 0), (1400, 1400, 12, 0, 1), (1000, 1000, 12, 0, 0)]
+    err = _run(blocks, alpha=1.5, beta=-0.5, seed=25, prec=PREC_F64TC)
+    print("f64tc short-k relative error", err)
+    assert err < 3e-13
+
+
 def test_f64tc_graded_rows_against_the_slice_error_bound():
     """Entries spanning twelve decades within each row and column: every element within the scheme's
     bound 4 k 2^-49 max_k|a_ik| max_k|b_kj| (the slices are taken relative to each row's and column's

@@ -1016,9 +1016,9 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
     for (int g = 0; g < n_groups; ++g) flops += 2.0 * double(descs[g].m) * double(descs[g].n) * double(descs[g].k);
     auto* dd = upload(descs, size_t(n_groups), s);
     auto* dg = upload(op.groups.data(), op.groups.size(), s);
-    auto* dk = upload(op.tasks.data(), std::max<size_t>(op.tasks.size(), 1), s);
+    auto* dk = upload(op.tasks.data(), op.tasks.size(), s);
     auto* dt = upload(op.tiles.data(), op.tiles.size(), s);
-    auto* dr = upload(op.red.data(), std::max<size_t>(op.red.size(), 1), s);
+    auto* dr = upload(op.red.data(), op.red.size(), s);
     auto* rm = static_cast<unsigned long long*>(dev_alloc(sizeof(unsigned long long) * size_t(std::max<int64_t>(op.rowmax, 1))));
     auto* ap = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(op.a_bytes, 16))));
     auto* bp = static_cast<unsigned char*>(dev_alloc(size_t(std::max<int64_t>(op.b_bytes, 16))));
@@ -1039,7 +1039,7 @@ int xgb_grouped_gemm(int precision, int n_groups, const xgb_gemm_desc* descs, co
     for (int g = 0; g < n_groups; ++g) flops += 2.0 * double(descs[g].m) * double(descs[g].n) * double(descs[g].k);
     auto* dd = upload(descs, size_t(n_groups), s);
     auto* dg = upload(tp.groups.data(), tp.groups.size(), s);
-    auto* dk = upload(tp.tasks.data(), std::max<size_t>(tp.tasks.size(), 1), s);
+    auto* dk = upload(tp.tasks.data(), tp.tasks.size(), s);
     auto* dt = upload(tp.tiles.data(), tp.tiles.size(), s);
     auto* ap = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.a_floats, 4))));
     auto* bp = static_cast<float*>(dev_alloc(sizeof(float) * size_t(std::max<int64_t>(tp.b_floats, 4))));
