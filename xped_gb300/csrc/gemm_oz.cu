@@ -260,6 +260,10 @@ __global__ void __launch_bounds__(256) oz_pack_kernel(const xgb_gemm_desc* __res
 }
 
 // ----------------------------------------------------------------------------- gemm
+// the rare cases of scaled_double (subnormal, infinite or out-of-range results), out of line so that
+// the common path is never if-converted into the FP64 conversion and ldexp
+__device__ __noinline__ double scaled_double_slow(float v, int sc) { return ldexp(double(v), sc); }
+
 // v 2^sc as a double, assembled from the FP32 bits (exact; no FP64 arithmetic) while the result is a
 // normal double, else through ldexp
 __device__ __forceinline__ double scaled_double(float v, int sc) {
@@ -267,7 +271,7 @@ __device__ __forceinline__ double scaled_double(float v, int sc) {
   const int e8 = int((b >> 23) & 0xFF);
   if ((b & 0x7FFFFFFFu) == 0u) return __longlong_as_double(static_cast<long long>(uint64_t(b >> 31) << 63));
   const int e = e8 - 127 + 1023 + sc;
-  if (e8 == 0 || e8 == 255 || e <= 0 || e >= 2047) return ldexp(double(v), sc);
+  if (e8 == 0 || e8 == 255 || e <= 0 || e >= 2047) return scaled_double_slow(v, sc);
   return __longlong_as_double(static_cast<long long>((uint64_t(b >> 31) << 63) | (uint64_t(e) << 52) |
                                                      (uint64_t(b & 0x7FFFFFu) << 29)));
 }
@@ -444,17 +448,20 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     const int64_t row = m0 + quarter * 32 + lane;
     if (row < d.m) {
       const int ei = rsc[quarter * 32 + lane];
+      // 0: partial tile to the workspace, 1: C = acc, 2: C = alpha acc, 3: C = alpha acc + beta C
+      const int mode = t.slot >= 0 ? 0 : beta != 0.0 ? 3 : alpha != 1.0 ? 2 : 1;
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const int64_t col = n0 + colg * 32 + j;
         if (col < d.n) {
           const int sc = ei + csc[colg * 32 + j];
           const double acc = scaled_double(hi[j], sc) + scaled_double(lo[j], sc);
-          if (t.slot >= 0) {  // split-K partial: raw sum, tile-local column-major OM x ON
+          if (mode == 0) {  // split-K partial: raw sum, tile-local column-major OM x ON
             ws[int64_t(t.slot) * OM * ON + (quarter * 32 + lane) + int64_t(colg * 32 + j) * OM] = acc;
           } else {
             double* cp = C + d.c_off + row + col * d.ldc;
-            if (beta == 0.0) *cp = alpha == 1.0 ? acc : alpha * acc;
+            if (mode == 1) *cp = acc;
+            else if (mode == 2) *cp = alpha * acc;
             else *cp = fma(alpha, acc, beta * *cp);
           }
         }
@@ -491,10 +498,10 @@ __global__ void __launch_bounds__(256) oz_splitk_reduce_kernel(const xgb_gemm_de
   for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const int64_t i = int64_t(r.tm) * OM + e % OM, j = int64_t(r.tn) * ON + e / OM;
     if (i >= d.m || j >= d.n) continue;
-    double acc = 0.0;
-    for (int p = 0; p < r.count; ++p) acc += ws[(int64_t(r.first) + p) * OM * ON + e];
+    double acc = ws[int64_t(r.first) * OM * ON + e];
+    for (int p = 1; p < r.count; ++p) acc += ws[(int64_t(r.first) + p) * OM * ON + e];
     double* c = C + d.c_off + i + j * d.ldc;
-    *c = beta == 0.0 ? alpha * acc : fma(alpha, acc, beta * *c);
+    *c = beta != 0.0 ? fma(alpha, acc, beta * *c) : alpha == 1.0 ? acc : alpha * acc;
   }
 }
 

@@ -223,6 +223,8 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __r
       for (int c = 0; c < R; ++c) w[(tx + 16 * r) + (ty + 16 * c) * TILE] = double(acc[r][c]);
     return;
   }
+  // FP64 operations go through GB300's narrow FP64 pipe: alpha = 1, beta = 0 stores the sums as they are
+  const bool scaled = alpha != 1.0, accumulate = beta != 0.0;
 #pragma unroll
   for (int r = 0; r < R; ++r)
 #pragma unroll
@@ -230,8 +232,8 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __r
       int64_t i = row0 + tx + 16 * r, j = col0 + ty + 16 * c;
       if (i < d.m && j < d.n) {
         double* p = C + d.c_off + i + j * d.ldc;
-        double v = alpha * double(acc[r][c]);
-        if (beta != 0.0) v += beta * (*p);
+        double v = scaled ? alpha * double(acc[r][c]) : double(acc[r][c]);
+        if (accumulate) v += beta * (*p);
         *p = v;
       }
     }
@@ -258,10 +260,10 @@ __global__ void __launch_bounds__(256) splitk_reduce_kernel(const xgb_gemm_desc*
   for (int64_t e = threadIdx.x; e < tt; e += blockDim.x) {
     const int64_t i = int64_t(r.tm) * tile + e % tile, j = int64_t(r.tn) * tile + e / tile;
     if (i >= d.m || j >= d.n) continue;
-    double acc = 0.0;
-    for (int p = 0; p < r.count; ++p) acc += ws[(int64_t(r.first) + p) * tt + e];
+    double acc = ws[int64_t(r.first) * tt + e];
+    for (int p = 1; p < r.count; ++p) acc += ws[(int64_t(r.first) + p) * tt + e];
     double* c = C + d.c_off + i + j * d.ldc;
-    double v = alpha * acc;
+    double v = alpha == 1.0 ? acc : alpha * acc;
     if (beta != 0.0) v += beta * (*c);
     *c = v;
   }
