@@ -196,6 +196,18 @@ def test_f64tc_short_k_many_tiles_without_split():
     assert err < 3e-13
 
 
+@pytest.mark.parametrize("alpha,beta", [(1.0, 0.0), (2.0, 0.0), (1.5, -0.5)])
+def test_f64tc_wide_outputs_computed_transposed(alpha, beta):
+    """Few rows and many columns: the plan computes C^T = op(B)^T op(A)^T (half the 128 x 64 tiles) and
+    stores it transposed; every store form (C = acc, alpha acc, alpha acc + beta C), a split-K group
+    (k = 2000) whose reduce writes transposed, a k = 0 group and both transposes."""
+    blocks = [(20, 900, 12, 0, 0), (36, 1500, 40, 1, 1), (50, 700, 2000, 0, 1), (10, 300, 0, 0, 0),
+              (130, 70, 64, 1, 0)]
+    err = _run(blocks, alpha=alpha, beta=beta, seed=26, prec=PREC_F64TC)
+    print("f64tc transposed relative error", alpha, beta, err)
+    assert err < 3e-13
+
+
 def test_f64tc_graded_rows_against_the_slice_error_bound():
     """Entries spanning twelve decades within each row and column: every element within the scheme's
     bound 4 k 2^-49 max_k|a_ik| max_k|b_kj| (the slices are taken relative to each row's and column's

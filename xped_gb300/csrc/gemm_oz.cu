@@ -143,11 +143,12 @@ __global__ void __launch_bounds__(256) oz_rowmax_kernel(const xgb_gemm_desc* __r
   const xgb_gemm_desc d = descs[t.g];
   const OzGroup gr = groups[t.g];
   const bool isB = t.which != 0;
-  const double* src = isB ? B : A;
-  const int64_t off = isB ? d.b_off : d.a_off, ld = isB ? d.ldb : d.lda;
-  const int64_t rows = isB ? d.n : d.m;
+  const bool sb = isB != (gr.swap != 0);  // the rows of this role are op(B)^T's (columns of op(B))
+  const double* src = sb ? B : A;
+  const int64_t off = sb ? d.b_off : d.a_off, ld = sb ? d.ldb : d.lda;
+  const int64_t rows = sb ? d.n : d.m;
   const int tr = isB ? ON : OM;
-  const bool rowfast = isB ? d.trans_b != 0 : d.trans_a == 0;
+  const bool rowfast = sb ? d.trans_b != 0 : d.trans_a == 0;
   const int64_t r0 = int64_t(t.tile) * tr, k0 = int64_t(t.slice) * OK;
   for (int e = threadIdx.x; e < tr * OK; e += 256) {
     int r, k;
@@ -219,11 +220,12 @@ __global__ void __launch_bounds__(256) oz_pack_kernel(const xgb_gemm_desc* __res
   const xgb_gemm_desc d = descs[t.g];
   const OzGroup gr = groups[t.g];
   const bool isB = t.which != 0;
-  const double* src = isB ? B : A;
-  const int64_t off = isB ? d.b_off : d.a_off, ld = isB ? d.ldb : d.lda;
-  const int64_t rows = isB ? d.n : d.m;
+  const bool sb = isB != (gr.swap != 0);  // the rows of this role are op(B)^T's (columns of op(B))
+  const double* src = sb ? B : A;
+  const int64_t off = sb ? d.b_off : d.a_off, ld = sb ? d.ldb : d.lda;
+  const int64_t rows = sb ? d.n : d.m;
   const int tr = isB ? ON : OM;
-  const bool rowfast = isB ? d.trans_b != 0 : d.trans_a == 0;
+  const bool rowfast = sb ? d.trans_b != 0 : d.trans_a == 0;
   const int64_t r0 = int64_t(t.tile) * tr, k0 = int64_t(t.slice) * OK;
   for (int e = threadIdx.x; e < tr * OK; e += 256) {
     int r, k;
@@ -293,14 +295,17 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   const xgb_gemm_desc d = descs[t.g];
   const OzGroup gr = groups[t.g];
   const int64_t m0 = int64_t(t.tm) * OM, n0 = int64_t(t.tn) * ON;
+  // extents of the computed product: C, or C^T for a swapped group (element (r, c) of C^T is C[c + r ldc])
+  const bool swp = gr.swap != 0;
+  const int64_t pm = swp ? d.n : d.m, pn = swp ? d.m : d.n;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // split-K: this CTA takes K slices [ks, ks + nk) and, with a slot, stores its raw partial tile
   const int ks = t.k0, nk = (t.k1 < 0 ? gr.slices : t.k1) - t.k0;
   const int nchunks = (nk + kChunk - 1) / kChunk;
 
   for (int i = threadIdx.x; i < OM + ON; i += kOzThreads) {
-    if (i < OM) rsc[i] = m0 + i < d.m ? row_scale(rowmax[gr.a_rowmax + m0 + i]) : 0;
-    else csc[i - OM] = n0 + (i - OM) < d.n ? row_scale(rowmax[gr.b_rowmax + n0 + (i - OM)]) : 0;
+    if (i < OM) rsc[i] = m0 + i < pm ? row_scale(rowmax[gr.a_rowmax + m0 + i]) : 0;
+    else csc[i - OM] = n0 + (i - OM) < pn ? row_scale(rowmax[gr.b_rowmax + n0 + (i - OM)]) : 0;
   }
   if (warp == kOzMma) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s_u32(&tmem_slot)),
@@ -444,16 +449,37 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   ok = __syncthreads_and(ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
+  // 0: partial tile to the workspace, 1: C = acc, 2: C = alpha acc, 3: C = alpha acc + beta C
+  const int mode = t.slot >= 0 ? 0 : beta != 0.0 ? 3 : alpha != 1.0 ? 2 : 1;
   if (ok && nk > 0 && warp < kOzDrainWarps) {
     const int64_t row = m0 + quarter * 32 + lane;
-    if (row < d.m) {
-      const int ei = rsc[quarter * 32 + lane];
-      // 0: partial tile to the workspace, 1: C = acc, 2: C = alpha acc, 3: C = alpha acc + beta C
-      const int mode = t.slot >= 0 ? 0 : beta != 0.0 ? 3 : alpha != 1.0 ? 2 : 1;
+    const int ei = rsc[quarter * 32 + lane];
+    if (mode != 0 && swp) {
+      // transposed store through shared memory (the stages are idle now): thread (r, 32 columns) puts
+      // its values at T[c][r] (row pitch 129 doubles), then each warp writes 32 consecutive rows of C
+      double* T = reinterpret_cast<double*>(smem);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int c = colg * 32 + j;
+        const int sc = ei + csc[c];
+        T[c * (OM + 1) + quarter * 32 + lane] = scaled_double(hi[j], sc) + scaled_double(lo[j], sc);
+      }
+      asm volatile("bar.sync 1, %0;" ::"n"(kOzDrainWarps * 32) : "memory");
+      for (int e = threadIdx.x; e < OM * ON; e += kOzDrainWarps * 32) {
+        const int c = e % ON, r = e / ON;  // C row n0 + c, C column m0 + r
+        if (m0 + r < pm && n0 + c < pn) {
+          const double acc = T[c * (OM + 1) + r];
+          double* cp = C + d.c_off + (n0 + c) + (m0 + r) * d.ldc;
+          if (mode == 1) *cp = acc;
+          else if (mode == 2) *cp = alpha * acc;
+          else *cp = fma(alpha, acc, beta * *cp);
+        }
+      }
+    } else if (row < pm) {
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const int64_t col = n0 + colg * 32 + j;
-        if (col < d.n) {
+        if (col < pn) {
           const int sc = ei + csc[colg * 32 + j];
           const double acc = scaled_double(hi[j], sc) + scaled_double(lo[j], sc);
           if (mode == 0) {  // split-K partial: raw sum, tile-local column-major OM x ON
@@ -470,8 +496,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   } else if (ok && nk == 0) {
     for (int e = threadIdx.x; e < OM * ON; e += kOzThreads) {
       const int64_t row = m0 + e % OM, col = n0 + e / OM;
-      if (row < d.m && col < d.n) {
-        double* cp = C + d.c_off + row + col * d.ldc;
+      if (row < pm && col < pn) {
+        double* cp = C + d.c_off + (swp ? col + row * d.ldc : row + col * d.ldc);
         *cp = beta == 0.0 ? 0.0 : beta * *cp;
       }
     }
@@ -488,19 +514,25 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 
 // C tile = alpha * (the split-K partials of the tile, added in slot order) + beta * C
 __global__ void __launch_bounds__(256) oz_splitk_reduce_kernel(const xgb_gemm_desc* __restrict__ descs,
+                                                                const OzGroup* __restrict__ groups,
                                                                 const SplitReduce* __restrict__ red,
                                                                 const double* __restrict__ ws, double* __restrict__ C,
                                                                 double alpha, double beta) {
   const SplitReduce r = red[blockIdx.x];
   const xgb_gemm_desc d = descs[r.g];
-  // blockIdx.y: a 1024-element part of the tile (eight CTAs per tile keep the sums spread over the SMs)
+  const bool swp = groups[r.g].swap != 0;
+  const int64_t pm = swp ? d.n : d.m, pn = swp ? d.m : d.n;
+  // blockIdx.y: a 1024-element part of the tile (eight CTAs per tile keep the sums spread over the SMs);
+  // consecutive threads take consecutive rows of C (tile rows, or tile columns of a swapped group)
   const int e0 = int(blockIdx.y) * 1024, e1 = e0 + 1024 < OM * ON ? e0 + 1024 : OM * ON;
   for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-    const int64_t i = int64_t(r.tm) * OM + e % OM, j = int64_t(r.tn) * ON + e / OM;
-    if (i >= d.m || j >= d.n) continue;
-    double acc = ws[int64_t(r.first) * OM * ON + e];
-    for (int p = 1; p < r.count; ++p) acc += ws[(int64_t(r.first) + p) * OM * ON + e];
-    double* c = C + d.c_off + i + j * d.ldc;
+    const int li = swp ? e / ON : e % OM, lj = swp ? e % ON : e / OM;  // tile-local row / column
+    const int64_t i = int64_t(r.tm) * OM + li, j = int64_t(r.tn) * ON + lj;
+    if (i >= pm || j >= pn) continue;
+    const int64_t w = li + int64_t(lj) * OM;
+    double acc = ws[int64_t(r.first) * OM * ON + w];
+    for (int p = 1; p < r.count; ++p) acc += ws[(int64_t(r.first) + p) * OM * ON + w];
+    double* c = C + d.c_off + (swp ? j + i * d.ldc : i + j * d.ldc);
     *c = beta != 0.0 ? fma(alpha, acc, beta * *c) : alpha == 1.0 ? acc : alpha * acc;
   }
 }
@@ -509,24 +541,33 @@ bool g_oz_attr = false;
 
 }  // namespace
 
-OzPlanHost build_oz_plan(const xgb_gemm_desc* descs, int n) {
-  // rowmax layout: every group's op(A) rows first, then every group's op(B) columns, so that the
-  // B part can be cleared and recomputed alone when only B changes between products
+OzPlanHost build_oz_plan(const xgb_gemm_desc* descs, int n, bool allow_swap) {
+  // A group is computed transposed (C^T = op(B)^T op(A)^T) when that needs at most 3/4 of the 128 x 64
+  // output tiles (few rows, many columns: the 128-row tile would be mostly padding).
+  auto tiles_of = [](int64_t r, int64_t c) { return ((r + OM - 1) / OM) * ((c + ON - 1) / ON); };
+  std::vector<char> swap(size_t(n), 0);
+  if (allow_swap)
+    for (int g = 0; g < n; ++g) swap[g] = 4 * tiles_of(descs[g].n, descs[g].m) <= 3 * tiles_of(descs[g].m, descs[g].n);
+  // rowmax layout: every group's rows of the "A" role first, then every group's rows of the "B" role
+  // (columns of the product), so that the B part can be cleared and recomputed alone when only B
+  // changes between products
   OzPlanHost p;
-  for (int g = 0; g < n; ++g) p.rowmax_a += descs[g].m;
+  for (int g = 0; g < n; ++g) p.rowmax_a += swap[g] ? descs[g].n : descs[g].m;
   int64_t ra = 0, rb = p.rowmax_a;
   for (int g = 0; g < n; ++g) {
     const xgb_gemm_desc& d = descs[g];
+    const int64_t pm = swap[g] ? d.n : d.m, pn = swap[g] ? d.m : d.n;  // extents of the computed product
     OzGroup gr{};
-    gr.a_tiles = int32_t((d.m + OM - 1) / OM);
-    gr.b_tiles = int32_t((d.n + ON - 1) / ON);
+    gr.swap = swap[g];
+    gr.a_tiles = int32_t((pm + OM - 1) / OM);
+    gr.b_tiles = int32_t((pn + ON - 1) / ON);
     gr.slices = int32_t((d.k + OK - 1) / OK);
     gr.a_pack = p.a_bytes;
     gr.b_pack = p.b_bytes;
     gr.a_rowmax = ra;
     gr.b_rowmax = rb;
-    ra += d.m;
-    rb += d.n;
+    ra += pm;
+    rb += pn;
     p.a_bytes += int64_t(gr.a_tiles) * gr.slices * kPieces * kAPieceBytes;
     p.b_bytes += int64_t(gr.b_tiles) * gr.slices * kPieces * kBPieceBytes;
     for (int32_t s = 0; s < gr.slices; ++s) {
@@ -604,8 +645,8 @@ void launch_oz_gemm(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const
                                                      beta, ws, gemm_tc_error_flag());
   count_launch();
   if (n_red > 0) {
-    oz_splitk_reduce_kernel<<<dim3(unsigned(n_red), (OM * ON + 1023) / 1024), 256, 0, s>>>(d_descs, d_red, ws, C,
-                                                                                            alpha, beta);
+    oz_splitk_reduce_kernel<<<dim3(unsigned(n_red), (OM * ON + 1023) / 1024), 256, 0, s>>>(d_descs, d_groups, d_red,
+                                                                                            ws, C, alpha, beta);
     count_launch();
   }
   if (ws) dev_free(ws);

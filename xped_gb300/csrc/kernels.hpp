@@ -114,9 +114,12 @@ int* gemm_tc_error_flag();      // the device flag itself (allocated on first us
 // FP64-accurate tensor-core grouped GEMM from exact BF16 slices (gemm_oz.cu): 128 x 64 output tiles,
 // 32-K slices, seven BF16 pieces per operand entry; per group the packed A / B slice blocks (bytes)
 // and the offsets of its op(A) rows' / op(B) columns' largest magnitudes in the rowmax array
+// swap != 0: the group is computed as C^T = op(B)^T op(A)^T (the product's "A" role is op(B)^T, read
+// from the B buffer, and the tile is stored transposed), which wastes less of the 128 x 64 output tile
+// when C has few rows and many columns
 struct OzGroup {
   int64_t a_pack, b_pack, a_rowmax, b_rowmax;
-  int32_t a_tiles, b_tiles, slices, pad;
+  int32_t a_tiles, b_tiles, slices, swap;
 };
 struct OzPlanHost {
   std::vector<OzGroup> groups;
@@ -128,7 +131,9 @@ struct OzPlanHost {
   int64_t a_bytes = 0, b_bytes = 0;
   int64_t rowmax = 0, rowmax_a = 0;  // entries in all; the op(A) rows come first
 };
-OzPlanHost build_oz_plan(const xgb_gemm_desc* descs, int n);
+// allow_swap: groups with few rows and many columns may be computed transposed (not for callers that
+// keep one operand's slices across products, whose roles must stay fixed)
+OzPlanHost build_oz_plan(const xgb_gemm_desc* descs, int n, bool allow_swap = true);
 // the row scales and slices of the given chunks (rowmax[clear_from .. + clear_count) zeroed first)
 void launch_oz_pack(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const TcPackTask* d_tasks, int n_tasks,
                     const double* A, const double* B, unsigned long long* rowmax, int64_t clear_from,

@@ -307,6 +307,33 @@ TreePairMap treepair_turn(const Sym& s, int shift, const FusionTree& t1, const F
   return out;
 }
 
+void treepair_permute_abelian(const Sym& s, int shift, const FusionTree& t1, const FusionTree& t2,
+                              const std::vector<int>& p, FusionTree& d, FusionTree& c) {
+  // abelian, non-fermionic symmetries: the permuted pair is unique, with coefficient 1
+  const int R = t1.rank, C = t2.rank;
+  const int newR = R - shift, newC = C + shift;
+  d = FusionTree{};
+  c = FusionTree{};
+  d.rank = newR;
+  c.rank = newC;
+  for (int r = 0; r < newR; ++r) {
+    int src = p[r];
+    if (src < R) { d.qu[r] = t1.qu[src]; d.dims[r] = t1.dims[src]; d.set_dual(r, t1.is_dual(src)); }
+    else { d.qu[r] = s.conj(t2.qu[src - R]); d.dims[r] = t2.dims[src - R]; d.set_dual(r, !t2.is_dual(src - R)); }
+  }
+  for (int k = 0; k < newC; ++k) {
+    int src = p[k + newR];
+    if (src < R) { c.qu[k] = s.conj(t1.qu[src]); c.dims[k] = t1.dims[src]; c.set_dual(k, !t1.is_dual(src)); }
+    else { c.qu[k] = t2.qu[src - R]; c.dims[k] = t2.dims[src - R]; c.set_dual(k, t2.is_dual(src - R)); }
+  }
+  d.qc = s.vacuum();
+  c.qc = s.vacuum();
+  d.compute_dim();
+  c.compute_dim();
+  d = tree_compute_intermediates(s, d);
+  c = tree_compute_intermediates(s, c);
+}
+
 TreePairMap treepair_permute(const Sym& s, int shift, const FusionTree& t1, const FusionTree& t2, const std::vector<int>& p) {
   // treepair::permute<shift> (treepair.cpp:143-217)
   const int R = t1.rank, C = t2.rank;
@@ -314,24 +341,7 @@ TreePairMap treepair_permute(const Sym& s, int shift, const FusionTree& t1, cons
   TreePairMap out;
   if (s.abelian() && !s.fermionic()) {
     FusionTree d, c;
-    d.rank = newR;
-    c.rank = newC;
-    for (int r = 0; r < newR; ++r) {
-      int src = p[r];
-      if (src < R) { d.qu[r] = t1.qu[src]; d.dims[r] = t1.dims[src]; d.set_dual(r, t1.is_dual(src)); }
-      else { d.qu[r] = s.conj(t2.qu[src - R]); d.dims[r] = t2.dims[src - R]; d.set_dual(r, !t2.is_dual(src - R)); }
-    }
-    for (int k = 0; k < newC; ++k) {
-      int src = p[k + newR];
-      if (src < R) { c.qu[k] = s.conj(t1.qu[src]); c.dims[k] = t1.dims[src]; c.set_dual(k, !t1.is_dual(src)); }
-      else { c.qu[k] = t2.qu[src - R]; c.dims[k] = t2.dims[src - R]; c.set_dual(k, t2.is_dual(src - R)); }
-    }
-    d.qc = s.vacuum();
-    c.qc = s.vacuum();
-    d.compute_dim();
-    c.compute_dim();
-    d = tree_compute_intermediates(s, d);
-    c = tree_compute_intermediates(s, c);
+    treepair_permute_abelian(s, shift, t1, t2, p, d, c);
     out.emplace(std::make_pair(d, c), 1.0);
     return out;
   }

@@ -91,6 +91,9 @@ TreeMap tree_permute(const Sym& s, const FusionTree& t, const std::vector<int>& 
 std::vector<int> decompose_permutation(const std::vector<int>& pi);
 TreePairMap treepair_turn(const Sym& s, int shift, const FusionTree& t1, const FusionTree& t2);
 TreePairMap treepair_permute(const Sym& s, int shift, const FusionTree& t1, const FusionTree& t2, const std::vector<int>& p);
+// the same for abelian, non-fermionic symmetries (one result pair, coefficient 1), without a map
+void treepair_permute_abelian(const Sym& s, int shift, const FusionTree& t1, const FusionTree& t2,
+                              const std::vector<int>& p, FusionTree& d, FusionTree& c);
 
 // ------------------------------------------------------------------ Qbasis
 struct Qbasis;

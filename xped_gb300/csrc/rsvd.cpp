@@ -142,7 +142,7 @@ class TcProducts {
 class OzProducts {
  public:
   OzProducts(const std::vector<xgb_gemm_desc>& d, const double* A, cudaStream_t s) {
-    const OzPlanHost op = build_oz_plan(d.data(), int(d.size()));
+    const OzPlanHost op = build_oz_plan(d.data(), int(d.size()), false);  // op(A) keeps the A role
     n_tiles_ = int(op.tiles.size());
     n_red_ = int(op.red.size());
     slots_ = op.slots;

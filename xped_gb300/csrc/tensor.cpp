@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <unordered_map>
 #include <mutex>
 #include <numeric>
 #include <sstream>
@@ -203,15 +204,16 @@ std::unordered_map<std::string, std::shared_ptr<GemmPlan>> g_gemm_plans;
 CacheStats g_stats;
 
 struct TaskBuilder {
-  std::map<int64_t, int> by_dst;  // dst_base -> task
+  // destination sub-block -> task; contributions kept flat in insertion order (no per-task vectors)
+  std::unordered_map<int64_t, int> by_dst;
   std::vector<xgb_perm_task> tasks;
-  std::vector<std::vector<xgb_perm_contrib>> contribs;
+  std::vector<std::pair<int, xgb_perm_contrib>> flat;
 
   void add(int64_t dst_base, int rank, const int32_t* dims, const int64_t* dst_stride, int64_t src_base,
            const int64_t* src_stride, double coeff) {
-    auto it = by_dst.find(dst_base);
-    int ti;
-    if (it == by_dst.end()) {
+    const auto [it, inserted] = by_dst.try_emplace(dst_base, int(tasks.size()));
+    const int ti = it->second;
+    if (inserted) {
       xgb_perm_task t{};
       t.dst_base = dst_base;
       t.rank = rank;
@@ -221,12 +223,8 @@ struct TaskBuilder {
         t.dst_stride[k] = dst_stride[k];
         t.nelem *= dims[k];
       }
-      ti = int(tasks.size());
       tasks.push_back(t);
-      contribs.emplace_back();
-      by_dst.emplace(dst_base, ti);
     } else {
-      ti = it->second;
       for (int k = 0; k < rank; ++k)
         if (tasks[ti].dims[k] != dims[k]) throw std::runtime_error("permute plan: inconsistent sub-block shapes");
     }
@@ -234,21 +232,37 @@ struct TaskBuilder {
     c.src_base = src_base;
     c.coeff = coeff;
     for (int k = 0; k < rank; ++k) c.src_stride[k] = src_stride[k];
-    contribs[ti].push_back(c);
+    flat.emplace_back(ti, c);
   }
 
+  // tasks in ascending destination offset, each task's contributions contiguous in insertion order
   PermTables tables(const MetaPtr& out) const {
     PermTables t;
     t.out = out;
+    const size_t nt = tasks.size();
+    std::vector<int> order(nt);
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return tasks[a].dst_base < tasks[b].dst_base; });
+    std::vector<int32_t> count(nt, 0);
+    for (const auto& fc : flat) ++count[fc.first];
+    std::vector<int64_t> at(nt);
+    int64_t pos = 0;
+    for (int oi : order) {
+      at[oi] = pos;
+      pos += count[oi];
+    }
+    t.tasks.reserve(nt);
+    t.start.reserve(nt + 1);
     t.start.push_back(0);
-    for (const auto& [dst, ti] : by_dst) {
-      xgb_perm_task task = tasks[ti];
-      task.contrib0 = int32_t(t.contribs.size());
-      task.n_contrib = int32_t(contribs[ti].size());
-      for (const auto& c : contribs[ti]) t.contribs.push_back(c);
+    for (int oi : order) {
+      xgb_perm_task task = tasks[oi];
+      task.contrib0 = int32_t(at[oi]);
+      task.n_contrib = count[oi];
       t.tasks.push_back(task);
       t.start.push_back(t.start.back() + task.nelem);
     }
+    t.contribs.resize(flat.size());
+    for (const auto& fc : flat) t.contribs[size_t(at[fc.first]++)] = fc.second;
     t.needs_zero = t.start.back() < out->size;
     return t;
   }
@@ -342,6 +356,10 @@ PermTables build_perm_tables(const TensorMeta& in, uint32_t mask, int shift, con
               if (std::abs(c1 * c2) < kCoeffCut) continue;
               emit(g1, g2, c1 * c2, ptot);
             }
+        } else if (s.abelian() && !s.fermionic()) {
+          FusionTree g1, g2;  // the one permuted pair, coefficient 1
+          treepair_permute_abelian(s, shift, f1, f2, p, g1, g2);
+          emit(g1, g2, 1.0, p);
         } else {
           // permute_impl<shift>(p) (Tensor.cpp:148-214)
           for (const auto& [pr, c] : treepair_permute(s, shift, f1, f2, p)) {
