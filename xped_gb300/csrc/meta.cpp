@@ -489,15 +489,19 @@ static void sort_basis(Qbasis& b) {
   std::sort(idx.begin(), idx.end(), [&](int a, int c) {
     return cj ? s.conj(b.qs[a]) < s.conj(b.qs[c]) : b.qs[a] < b.qs[c];
   });
-  Qbasis o = b;
+  std::vector<int> qs(idx.size());
+  std::vector<int64_t> dims(idx.size());
+  std::vector<std::vector<FusionTree>> trees(idx.size());
   for (size_t i = 0; i < idx.size(); ++i) {
-    o.qs[i] = b.qs[idx[i]];
-    o.dims[i] = b.dims[idx[i]];
-    o.trees[i] = b.trees[idx[i]];
+    qs[i] = b.qs[idx[i]];
+    dims[i] = b.dims[idx[i]];
+    trees[i] = std::move(b.trees[idx[i]]);
   }
-  b.qs.swap(o.qs);
-  b.dims.swap(o.dims);
-  b.trees.swap(o.trees);
+  b.qs.swap(qs);
+  b.dims.swap(dims);
+  b.trees.swap(trees);
+  b.qindex.clear();  // lookup caches follow the new order when next used
+  b.offset_cache.clear();
 }
 
 BasisPtr basis_from_pairs(const Sym& s, const std::vector<std::pair<int, int64_t>>& pairs, bool sort) {
@@ -558,22 +562,33 @@ BasisPtr basis_combine(const BasisPtr& a, const BasisPtr& bb) {
   }
   // Qbasis::combine (Qbasis.cpp:441-495)
   const Sym& s = a->sym;
+  // coupled charges in order of first appearance, each with its trees; a tree is the concatenation of
+  // its two parents, so distinct parent pairs give distinct trees: only non-abelian symmetries (several
+  // channels per pair) keep the membership check of the reference's insertion
   std::vector<int> order;
-  std::unordered_map<int, std::vector<FusionTree>> trees;
-  std::unordered_map<int, std::unordered_set<FusionTree, TreeHash>> seen;  // membership, O(1) per tree
+  std::vector<std::vector<FusionTree>> trees;
+  std::unordered_map<int, int> slot;
+  std::vector<std::unordered_set<FusionTree, TreeHash>> seen;
+  const bool check = !s.abelian();
   int buf[64];
   for (size_t i1 = 0; i1 < a->qs.size(); ++i1) {
     for (size_t i2 = 0; i2 < bb->qs.size(); ++i2) {
       int n = s.combine(a->qs[i1], bb->qs[i2], buf);
       for (int k = 0; k < n; ++k) {
-        int q = buf[k];
+        const int q = buf[k];
+        auto [it, fresh] = slot.try_emplace(q, int(order.size()));
+        if (fresh) {
+          order.push_back(q);
+          trees.emplace_back();
+          if (check) seen.emplace_back();
+        }
+        auto& lst = trees[size_t(it->second)];
+        lst.reserve(lst.size() + a->trees[i1].size() * bb->trees[i2].size());
         for (const auto& t1 : a->trees[i1])
           for (const auto& t2 : bb->trees[i2]) {
             FusionTree tt = tree_enlarge(t1, t2);
             tt.qc = q;
-            auto& lst = trees[q];
-            if (lst.empty()) order.push_back(q);
-            if (seen[q].insert(tt).second) lst.push_back(tt);
+            if (!check || seen[size_t(it->second)].insert(tt).second) lst.push_back(tt);
           }
       }
     }
@@ -581,14 +596,14 @@ BasisPtr basis_combine(const BasisPtr& a, const BasisPtr& bb) {
   Qbasis out;
   out.sym = s;
   out.depth = a->depth + 1;
-  for (int q : order) {
-    auto& lst = trees[q];
+  for (size_t o = 0; o < order.size(); ++o) {
+    auto& lst = trees[o];
     std::sort(lst.begin(), lst.end(), [](const FusionTree& x, const FusionTree& y) { return x.less(y); });
     int64_t d = 0;
     for (const auto& t : lst) d += t.dim;
-    out.qs.push_back(q);
+    out.qs.push_back(order[o]);
     out.dims.push_back(d);
-    out.trees.push_back(lst);
+    out.trees.push_back(std::move(lst));
   }
   sort_basis(out);
   BasisPtr res = intern_basis(std::move(out));

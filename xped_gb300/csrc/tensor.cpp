@@ -204,65 +204,57 @@ std::unordered_map<std::string, std::shared_ptr<GemmPlan>> g_gemm_plans;
 CacheStats g_stats;
 
 struct TaskBuilder {
-  // destination sub-block -> task; contributions kept flat in insertion order (no per-task vectors)
-  std::unordered_map<int64_t, int> by_dst;
+  // one entry per contribution, in insertion order; tables() merges the entries of one destination
+  // sub-block (abelian symmetries have exactly one, so no lookup structure is kept while adding)
   std::vector<xgb_perm_task> tasks;
-  std::vector<std::pair<int, xgb_perm_contrib>> flat;
+  std::vector<xgb_perm_contrib> cons;
 
   void add(int64_t dst_base, int rank, const int32_t* dims, const int64_t* dst_stride, int64_t src_base,
            const int64_t* src_stride, double coeff) {
-    const auto [it, inserted] = by_dst.try_emplace(dst_base, int(tasks.size()));
-    const int ti = it->second;
-    if (inserted) {
-      xgb_perm_task t{};
-      t.dst_base = dst_base;
-      t.rank = rank;
-      t.nelem = 1;
-      for (int k = 0; k < rank; ++k) {
-        t.dims[k] = dims[k];
-        t.dst_stride[k] = dst_stride[k];
-        t.nelem *= dims[k];
-      }
-      tasks.push_back(t);
-    } else {
-      for (int k = 0; k < rank; ++k)
-        if (tasks[ti].dims[k] != dims[k]) throw std::runtime_error("permute plan: inconsistent sub-block shapes");
+    xgb_perm_task t{};
+    t.dst_base = dst_base;
+    t.rank = rank;
+    t.nelem = 1;
+    for (int k = 0; k < rank; ++k) {
+      t.dims[k] = dims[k];
+      t.dst_stride[k] = dst_stride[k];
+      t.nelem *= dims[k];
     }
+    tasks.push_back(t);
     xgb_perm_contrib c{};
     c.src_base = src_base;
     c.coeff = coeff;
     for (int k = 0; k < rank; ++k) c.src_stride[k] = src_stride[k];
-    flat.emplace_back(ti, c);
+    cons.push_back(c);
   }
 
   // tasks in ascending destination offset, each task's contributions contiguous in insertion order
   PermTables tables(const MetaPtr& out) const {
     PermTables t;
     t.out = out;
-    const size_t nt = tasks.size();
-    std::vector<int> order(nt);
+    std::vector<int> order(tasks.size());
     std::iota(order.begin(), order.end(), 0);
-    std::sort(order.begin(), order.end(), [&](int a, int b) { return tasks[a].dst_base < tasks[b].dst_base; });
-    std::vector<int32_t> count(nt, 0);
-    for (const auto& fc : flat) ++count[fc.first];
-    std::vector<int64_t> at(nt);
-    int64_t pos = 0;
-    for (int oi : order) {
-      at[oi] = pos;
-      pos += count[oi];
-    }
-    t.tasks.reserve(nt);
-    t.start.reserve(nt + 1);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return tasks[a].dst_base < tasks[b].dst_base; });
+    t.tasks.reserve(tasks.size());
+    t.contribs.reserve(cons.size());
+    t.start.reserve(tasks.size() + 1);
     t.start.push_back(0);
-    for (int oi : order) {
-      xgb_perm_task task = tasks[oi];
-      task.contrib0 = int32_t(at[oi]);
-      task.n_contrib = count[oi];
+    for (size_t r = 0; r < order.size();) {
+      size_t e = r + 1;
+      while (e < order.size() && tasks[order[e]].dst_base == tasks[order[r]].dst_base) ++e;
+      xgb_perm_task task = tasks[order[r]];
+      for (size_t x = r + 1; x < e; ++x)
+        for (int k = 0; k < task.rank; ++k)
+          if (tasks[order[x]].dims[k] != task.dims[k])
+            throw std::runtime_error("permute plan: inconsistent sub-block shapes");
+      task.contrib0 = int32_t(t.contribs.size());
+      task.n_contrib = int32_t(e - r);
+      for (size_t x = r; x < e; ++x) t.contribs.push_back(cons[order[x]]);
       t.tasks.push_back(task);
       t.start.push_back(t.start.back() + task.nelem);
+      r = e;
     }
-    t.contribs.resize(flat.size());
-    for (const auto& fc : flat) t.contribs[size_t(at[fc.first]++)] = fc.second;
     t.needs_zero = t.start.back() < out->size;
     return t;
   }
