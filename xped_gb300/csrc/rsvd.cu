@@ -233,14 +233,15 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   __syncthreads();
   // Cholesky (right-looking, one column of look-ahead), lower triangle in place.  Iteration j, with
   // column j final (updated by every earlier column and scaled by its pivot's reciprocal):
-  //   warp 0 ("panel") applies column j to column j + 1 only, forms pivot j + 1 and scales column j + 1,
-  //   warps 1.. apply column j to the trailing columns j + 2 .. l - 1,
+  //   warp 0 finishes the diagonal element j + 1 and forms its pivot, warp 1 applies column j to the
+  //   rest of column j + 1 and scales it with the pivot's reciprocal (two-warp barrier in between),
+  //   warps 2.. apply column j to the trailing columns j + 2 .. l - 1,
   // and one barrier ends the iteration.  The pivot chain - on GB300 a dependent FP64 operation takes
   // ~64 cycles, sqrt ~675 and a division ~430, so the pivot is r = rsqrt(d) (~430) with L_jj = d r and
   // 1 / L_jj = r - runs beside the trailing update instead of between two barriers.  Every element sees
   // the same FMAs in the same order as in the unblocked column algorithm.
   const unsigned full_warp = 0xffffffffu;
-  auto panel = [&](int c) {  // warp 0: pivot of column c and its scaling; lane ln owns rows c + ln + 32 r
+  auto panel = [&](int c) {  // warp 0: pivot of column c and its scaling (first column); lane ln owns rows c + ln + 32 r
     double r = 0.0;
     int dd = 0;
     if (lane == 0) {
@@ -259,18 +260,38 @@ __device__ void chol_inv_body(const CholDesc& d, double* __restrict__ Gg, double
   };
   if (warp == 0 && l > 0) panel(0);
   __syncthreads();
+  // warp 0 forms the next pivot (one lane: the diagonal's last FMA, then rsqrt) while warp 1 applies
+  // column j to the rest of column j + 1; a two-warp barrier hands the reciprocal over for the scaling
+  __shared__ double piv_r;
+  __shared__ int piv_dead;
   for (int j = 0; j + 1 < l; ++j) {
+    const int nc = j + 1;  // the next column
     if (warp == 0) {
-      const double ljj = LA(j + 1, j);
-      for (int i = j + 1 + lane; i < l; i += 32) LA(i, j + 1) = fma(-LA(i, j), ljj, LA(i, j + 1));
-      __syncwarp();
-      panel(j + 1);
+      if (lane == 0) {
+        const double ljj = LA(nc, j);
+        const double dj = fma(-ljj, ljj, LA(nc, nc));  // row nc of the column update, as in the unblocked order
+        const int dd = !(dj > dfloor);               // also true for NaN
+        if (dd) atomicAdd(bad, 1);
+        const double v = dd ? dfloor : dj;
+        const double r = rsqrt(v);
+        LA(nc, nc) = v * r;
+        piv_r = r;
+        piv_dead = dd;
+      }
+      asm volatile("bar.sync 1, 64;" ::: "memory");
+    } else if (warp == 1) {
+      const double ljj = LA(nc, j);
+      for (int i = nc + 1 + lane; i < l; i += 32) LA(i, nc) = fma(-LA(i, j), ljj, LA(i, nc));
+      asm volatile("bar.sync 1, 64;" ::: "memory");
+      const double r = piv_r;
+      const bool dd = piv_dead != 0;
+      for (int i = nc + 1 + lane; i < l; i += 32) LA(i, nc) = dd ? 0.0 : LA(i, nc) * r;
     } else {
       // trailing lower triangle (rows i >= k >= j + 2) folded into whole columns: column c and column
       // t-1-c together hold t+1 elements; an odd t leaves the middle column alone
       const int t = l - j - 2, half = t >> 1;
       const int total = (t + 1) * half + ((t & 1) ? (t + 1) >> 1 : 0);
-      for (int e = tid - 32; e < total; e += nt - 32) {
+      for (int e = tid - 64; e < total; e += nt - 64) {
         int i, k;
         if (e < (t + 1) * half) {
           const int r = e % (t + 1), c = e / (t + 1);
