@@ -173,6 +173,12 @@ int xgb_ctm_set_gemm_precision(xgb_ctm c, int precision);
    randomized form: exact FP64 tSVD (on = 0, the default) or a sketch of
    min(chi, min(rows, cols)) + 16 columns (on = 1), for either width rule. */
 int xgb_ctm_set_sketch_unseen(xgb_ctm c, int on);
+/* on != 0 (the default): grow_all runs the left and right moves, then the top and bottom moves, two at
+ * a time on two CUDA streams driven by two host threads (the pairs touch disjoint environment tensors;
+ * results equal the sequential order's).  Only with the randomized projector SVD, and not while
+ * per-launch profiling or autotune measurement is on.  No counterpart in the reference, whose
+ * CTM::grow_all (src/PEPS/CTM.cpp:385-398) runs the four moves one after the other. */
+int xgb_ctm_set_concurrent(xgb_ctm c, int on);
 /* Products of the randomized projector SVD's subspace iterations: fp64_tail >= 0
    runs the first product A Omega and all but the last fp64_tail iterations as
    3xTF32 tensor-core GEMMs (FP32 accumulation), the last fp64_tail iterations, the

@@ -224,3 +224,32 @@ def test_fp64_accurate_tensor_core_products_match_fp64(svd):
     print(svd, "energy fp64", e_ex, "f64tc", e_tc, "diff", abs(e_ex - e_tc), "env diff", err)
     assert abs(e_ex - e_tc) < 1e-12
     assert err < 1e-10
+
+
+@pytest.mark.parametrize("gemm", ["fp64", "f64tc"])
+def test_concurrent_move_pairs_equal_sequential(gemm):
+    """grow_all running the left/right and then the top/bottom moves two at a time on two streams
+    (the default with randomized projectors) gives the same environments bit for bit, the same
+    statistics and the same decomposition log, in the same order, as the four moves one after the
+    other."""
+    aux = [(-1, 2), (0, 2), (1, 2)]
+    _, seq = _setup("u1", aux, [(-1, 1), (1, 1)], 48, 5)
+    _, par = _setup("u1", aux, [(-1, 1), (1, 1)], 48, 5)
+    for c in (seq, par):
+        c.set_svd("randomized", power_iters=3, oversample=16, growth=0.5)
+        c.set_gemm(gemm)
+        c.record(True)
+    seq.set_concurrent(False)
+    par.set_concurrent(True)
+    for _ in range(4):
+        seq.grow_all()
+        par.grow_all()
+    env_s, env_p = seq.env(), par.env()
+    for k in env_s:
+        assert np.array_equal(env_s[k].data(), env_p[k].data()), k
+    assert seq.stats() == par.stats()
+    rs, rp = seq.records(), par.records()
+    assert [r["dir"] for r in rs] == [r["dir"] for r in rp] == [0, 1, 2, 3] * 4
+    for a, b in zip(rs, rp):
+        assert np.array_equal(a["keep"], b["keep"]) and np.array_equal(a["width"], b["width"])
+        assert all(np.array_equal(x, y) for x, y in zip(a["spectrum"], b["spectrum"]))

@@ -121,6 +121,7 @@ PROTOS = [
     ("xgb_ctm_stats", C.c_int, [P, i64p]),
     ("xgb_ctm_set_warm_start", C.c_int, [P, C.c_int]),
     ("xgb_ctm_set_sketch_unseen", C.c_int, [P, C.c_int]),
+    ("xgb_ctm_set_concurrent", C.c_int, [P, C.c_int]),
     ("xgb_ctm_set_sketch_precision", C.c_int, [P, C.c_int]),
     ("xgb_ctm_set_residual_tol", C.c_int, [P, C.c_double]),
     ("xgb_ctm_residual_stats", C.c_int, [P, i64p, dblp]),

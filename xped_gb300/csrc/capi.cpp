@@ -425,6 +425,13 @@ int xgb_ctm_set_gemm_precision(xgb_ctm c, int precision) {
   })
 }
 
+int xgb_ctm_set_concurrent(xgb_ctm c, int on) {
+  GUARD(XGB_E_BADPLAN, {
+    c->c->concurrent = on != 0;
+    return XGB_OK;
+  })
+}
+
 int xgb_ctm_set_sketch_unseen(xgb_ctm c, int on) {
   GUARD(XGB_E_BADPLAN, {
     c->c->sketch_unseen = on != 0;

@@ -42,6 +42,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 
 #include "kernels.hpp"
 
@@ -537,7 +538,7 @@ __global__ void __launch_bounds__(256) oz_splitk_reduce_kernel(const xgb_gemm_de
   }
 }
 
-bool g_oz_attr = false;
+std::once_flag g_oz_attr;
 
 }  // namespace
 
@@ -636,10 +637,9 @@ void launch_oz_gemm(const xgb_gemm_desc* d_descs, const OzGroup* d_groups, const
                     const unsigned char* bpack, const unsigned long long* rowmax, double* C, double alpha, double beta,
                     cudaStream_t s) {
   if (n_tiles <= 0) return;
-  if (!g_oz_attr) {
+  std::call_once(g_oz_attr, [] {
     cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kOzSmem);
-    g_oz_attr = true;
-  }
+  });
   double* ws = slots > 0 ? static_cast<double*>(dev_alloc(sizeof(double) * size_t(slots) * OM * ON)) : nullptr;
   oz_gemm_kernel<<<n_tiles, kOzThreads, kOzSmem, s>>>(d_descs, d_groups, d_tiles, apack, bpack, rowmax, C, alpha,
                                                      beta, ws, gemm_tc_error_flag());

@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "kernels.hpp"
 
@@ -420,7 +421,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemAlloc));
 }
 
-bool g_tc_attr = false;
+std::once_flag g_tc_attr, g_tc_err_once;
 int* g_tc_err = nullptr;
 
 }  // namespace
@@ -455,12 +456,11 @@ void launch_gemm_tc(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const
                     const GemmTile* d_tiles, int n_tiles, const double* A, const double* B, float* apack,
                     float* bpack, double* C, double alpha, double beta, cudaStream_t s, int form) {
   if (n_tiles <= 0) return;
-  if (!g_tc_attr) {
+  std::call_once(g_tc_attr, [] {
     cudaFuncSetAttribute(gemm_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
     cudaFuncSetAttribute(gemm_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-    gemm_tc_error_flag();
-    g_tc_attr = true;
-  }
+  });
+  gemm_tc_error_flag();
   if (form == 1) {
     if (n_tasks > 0) {
       tc_pack_kernel<1><<<n_tasks, 256, 0, s>>>(d_descs, d_groups, d_tasks, A, B, apack, bpack);
@@ -490,10 +490,10 @@ void launch_tc_pack(const xgb_gemm_desc* d_descs, const TcGroup* d_groups, const
 }
 
 int* gemm_tc_error_flag() {
-  if (!g_tc_err) {
+  std::call_once(g_tc_err_once, [] {
     cudaMalloc(&g_tc_err, sizeof(int));
     cudaMemset(g_tc_err, 0, sizeof(int));
-  }
+  });
   return g_tc_err;
 }
 

@@ -13,9 +13,13 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <condition_variable>
 #include <cstring>
+#include <exception>
 #include <map>
 #include <mutex>
+#include <stdexcept>
+#include <thread>
 #include <new>
 #include <string>
 #include <vector>
@@ -30,19 +34,139 @@ struct Runtime {
   bool ready = false;
   int device = 0;
   int sms = 152;
-  cudaStream_t stream = nullptr;
-  double* scratch = nullptr;  // 64 doubles of device scratch
+  cudaStream_t stream = nullptr;  // lane 0
+  double* scratch = nullptr;      // 64 doubles of device scratch per lane
+  cudaStream_t side[kLanes - 1] = {nullptr, nullptr};
+  double* side_scratch[kLanes - 1] = {nullptr, nullptr};
+  cudaEvent_t fork_ev = nullptr, join_ev[kLanes - 1] = {nullptr, nullptr};
 };
 Runtime g_rt;
 std::atomic<int64_t> g_launches{0};
+std::atomic<bool> g_lanes_used{false};
 thread_local std::string g_err;
+thread_local int t_lane = 0;
+
+// The worker host thread of lane 1: runs one task at a time, handed over under a mutex.
+class LaneWorker {
+ public:
+  ~LaneWorker() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    if (th_.joinable()) th_.join();
+  }
+  void start(std::function<void()> f) {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (!th_.joinable()) th_ = std::thread([this] { loop(); });
+    task_ = std::move(f);
+    err_ = nullptr;
+    has_ = true;
+    done_ = false;
+    cv_.notify_all();
+  }
+  void wait() {
+    std::unique_lock<std::mutex> lk(mu_);
+    cv_.wait(lk, [this] { return done_; });
+    if (err_) {
+      std::exception_ptr e = err_;
+      err_ = nullptr;
+      std::rethrow_exception(e);
+    }
+  }
+
+ private:
+  void loop() {
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+      cv_.wait(lk, [this] { return stop_ || has_; });
+      if (stop_) return;
+      std::function<void()> f = std::move(task_);
+      has_ = false;
+      lk.unlock();
+      std::exception_ptr e;
+      try {
+        cudaSetDevice(g_rt.device);  // the current device is per host thread
+        f();
+      } catch (...) {
+        e = std::current_exception();
+      }
+      lk.lock();
+      err_ = e;
+      done_ = true;
+      cv_.notify_all();
+    }
+  }
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::thread th_;
+  std::function<void()> task_;
+  std::exception_ptr err_;
+  bool has_ = false, done_ = true, stop_ = false;
+};
+
+LaneWorker& lane_worker() {
+  static LaneWorker w;
+  return w;
+}
+std::mutex g_pair_mu;  // one fork-join section at a time
 }  // namespace
 
-cudaStream_t stream() { return g_rt.stream; }
+cudaStream_t stream() { return t_lane == 0 ? g_rt.stream : g_rt.side[t_lane - 1]; }
+int lane() { return t_lane; }
+LaneScope::LaneScope(int l) : saved(t_lane) { t_lane = l; }
+LaneScope::~LaneScope() { t_lane = saved; }
+bool lanes_used() { return g_lanes_used.load(); }
 bool runtime_ready() { return g_rt.ready; }
 int num_sms() { return g_rt.sms; }
-double* scalar_scratch() { return g_rt.scratch; }
+double* scalar_scratch() { return t_lane == 0 ? g_rt.scratch : g_rt.side_scratch[t_lane - 1]; }
 void count_launch(int n) { g_launches += n; }
+
+void run_pair(const std::function<void()>& a, const std::function<void()>& b) {
+  if (t_lane != 0) throw std::runtime_error("run_pair: called from a side lane");
+  std::lock_guard<std::mutex> lk(g_pair_mu);
+  g_lanes_used = true;
+  if (cudaEventRecord(g_rt.fork_ev, g_rt.stream) != cudaSuccess ||
+      cudaStreamWaitEvent(g_rt.side[0], g_rt.fork_ev, 0) != cudaSuccess ||
+      cudaStreamWaitEvent(g_rt.side[1], g_rt.fork_ev, 0) != cudaSuccess)
+    throw std::runtime_error("run_pair: fork failed");
+  LaneWorker& w = lane_worker();
+  w.start([&a] {
+    LaneScope ls(1);
+    a();
+  });
+  std::exception_ptr eb, ea;
+  try {
+    LaneScope ls(2);
+    b();
+  } catch (...) {
+    eb = std::current_exception();
+  }
+  try {
+    w.wait();
+  } catch (...) {
+    ea = std::current_exception();
+  }
+  for (int i = 0; i < kLanes - 1; ++i) {
+    cudaEventRecord(g_rt.join_ev[i], g_rt.side[i]);
+    cudaStreamWaitEvent(g_rt.stream, g_rt.join_ev[i], 0);
+  }
+  if (ea) std::rethrow_exception(ea);
+  if (eb) std::rethrow_exception(eb);
+}
+
+void order_after_lanes(cudaStream_t s) {
+  for (int l = 0; l < kLanes; ++l) {
+    cudaStream_t o = l == 0 ? g_rt.stream : g_rt.side[l - 1];
+    if (o == s || !o) continue;
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) continue;
+    cudaEventRecord(e, o);
+    cudaStreamWaitEvent(s, e, 0);
+    cudaEventDestroy(e);  // released once the wait has been satisfied
+  }
+}
 
 int set_error(int code, const std::string& msg) {
   g_err = msg;
@@ -58,7 +182,7 @@ int check_cuda(cudaError_t e, const char* what) {
 void* dev_alloc(size_t bytes) {
   if (bytes == 0) bytes = 8;
   void* p = nullptr;
-  cudaError_t e = cudaMallocAsync(&p, bytes, g_rt.stream);
+  cudaError_t e = cudaMallocAsync(&p, bytes, stream());
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     set_error(XGB_E_OOM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
@@ -68,7 +192,7 @@ void* dev_alloc(size_t bytes) {
 }
 
 void dev_free(void* p) {
-  if (p && g_rt.ready) cudaFreeAsync(p, g_rt.stream);
+  if (p && g_rt.ready) cudaFreeAsync(p, stream());
 }
 
 // ======================================================================= instrumentation
@@ -79,6 +203,7 @@ struct ProfEvent {
   double work;
 };
 bool g_prof_on = false;
+std::mutex g_prof_mu;
 std::vector<ProfEvent> g_prof_events;
 std::vector<cudaEvent_t> g_event_pool;
 int64_t g_prof_launches[K_COUNT] = {0};
@@ -111,6 +236,8 @@ void prof_drain() {
 }
 }  // namespace
 
+bool profiling() { return g_prof_on; }
+
 void prof_begin(int kind, cudaStream_t s) {
   if (!g_prof_on) return;
   g_pending_a[kind] = pool_event();
@@ -118,8 +245,11 @@ void prof_begin(int kind, cudaStream_t s) {
 }
 
 void prof_end(int kind, cudaStream_t s, double work) {
-  g_prof_launches[kind] += 1;
-  g_prof_work[kind] += work;
+  {
+    std::lock_guard<std::mutex> lk(g_prof_mu);  // lanes count concurrently (profiling itself runs on lane 0)
+    g_prof_launches[kind] += 1;
+    g_prof_work[kind] += work;
+  }
   if (!g_prof_on || !g_pending_a[kind]) return;
   cudaEvent_t b = pool_event();
   cudaEventRecord(b, s);
@@ -904,10 +1034,21 @@ int xgb_init(int device) {
   g_rt.sms = prop.multiProcessorCount;
   g_rt.device = device;
   if ((rc = check_cuda(cudaStreamCreateWithFlags(&g_rt.stream, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
+  for (int i = 0; i < kLanes - 1; ++i) {
+    if ((rc = check_cuda(cudaStreamCreateWithFlags(&g_rt.side[i], cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
+    if ((rc = check_cuda(cudaMalloc(&g_rt.side_scratch[i], 64 * sizeof(double)), "cudaMalloc scratch"))) return rc;
+    if ((rc = check_cuda(cudaEventCreateWithFlags(&g_rt.join_ev[i], cudaEventDisableTiming), "cudaEventCreate")))
+      return rc;
+  }
+  if ((rc = check_cuda(cudaEventCreateWithFlags(&g_rt.fork_ev, cudaEventDisableTiming), "cudaEventCreate"))) return rc;
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
     uint64_t thr = ~0ull;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    // memory freed on one lane is not handed to another lane's allocation behind an inserted wait
+    // (that would serialise the lanes); it is reused there once its free has completed
+    int no = 0;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no);
   }
   if ((rc = check_cuda(cudaMalloc(&g_rt.scratch, 64 * sizeof(double)), "cudaMalloc scratch"))) return rc;
   g_rt.ready = true;
@@ -917,9 +1058,17 @@ int xgb_init(int device) {
 int xgb_shutdown(void) {
   if (!g_rt.ready) return XGB_OK;
   cudaStreamSynchronize(g_rt.stream);
+  for (int i = 0; i < kLanes - 1; ++i) {
+    cudaStreamSynchronize(g_rt.side[i]);
+    cudaFree(g_rt.side_scratch[i]);
+    cudaStreamDestroy(g_rt.side[i]);
+    cudaEventDestroy(g_rt.join_ev[i]);
+  }
+  cudaEventDestroy(g_rt.fork_ev);
   cudaFree(g_rt.scratch);
   cudaStreamDestroy(g_rt.stream);
   g_rt = Runtime{};
+  g_lanes_used = false;
   return XGB_OK;
 }
 

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -29,7 +30,28 @@ struct SplitReduce { int32_t g, tm, tn, first, count, pad; };
 void order_tiles_by_work(std::vector<GemmTile>& tiles, const xgb_gemm_desc* descs);
 
 // runtime ------------------------------------------------------------------------
+// The stream of this host thread's lane: lane 0 is the runtime's stream; lanes 1 and 2 are the side
+// streams of a fork-join section (run_pair), each driven by its own host thread.
 cudaStream_t stream();
+constexpr int kLanes = 3;
+int lane();
+struct LaneScope {  // this host thread enqueues on lane `l` until the scope ends
+  int saved;
+  explicit LaneScope(int l);
+  ~LaneScope();
+  LaneScope(const LaneScope&) = delete;
+  LaneScope& operator=(const LaneScope&) = delete;
+};
+// Runs a() on lane 1 (a worker host thread) and b() on lane 2 (the calling thread) at the same time:
+// both lanes first wait for the work enqueued so far on lane 0, and lane 0 then waits for both
+// lanes, so the section is ordered like a() followed by b() on lane 0.  a() and b() must not touch
+// device memory that the other writes or frees.  An exception of either is rethrown (a()'s first)
+// once both have returned.  One section runs at a time; the caller must be on lane 0.
+void run_pair(const std::function<void()>& a, const std::function<void()>& b);
+bool lanes_used();  // a fork-join section has run since xgb_init
+// makes `s` wait for the work enqueued so far on every other lane (device memory that several lanes
+// may have used is freed on `s` after this)
+void order_after_lanes(cudaStream_t s);
 bool runtime_ready();  // xgb_init has run
 int set_error(int code, const std::string& msg);
 int check_cuda(cudaError_t e, const char* what);
@@ -190,6 +212,7 @@ void launch_mlp_reduce_adam(float* params, float* mom, float* vel, const float* 
 // per-kernel-kind instrumentation (CUDA events around each launch when enabled;
 // algorithmic work - flops for GEMMs, bytes for data movement - always counted)
 enum KernelKind { K_GEMM = 0, K_PERMUTE, K_SVD, K_TRUNC, K_QR, K_ABSMAX, K_SCALE, K_COPY2D, K_DIAG, K_GEMM_TC, K_SKETCH, K_MLP, K_GEMM_F32, K_GEMM_OZ, K_COUNT };
+bool profiling();  // per-launch CUDA-event timing is on (it needs the launches of one lane only)
 void prof_begin(int kind, cudaStream_t s);
 void prof_end(int kind, cudaStream_t s, double work);
 

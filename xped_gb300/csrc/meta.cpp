@@ -445,6 +445,18 @@ BasisPtr intern_basis(Qbasis&& b) {
   auto it = g_interned.find(k);
   if (it != g_interned.end()) return it->second;
   b.id = g_next_id++;
+  // the lookup caches are complete before the basis is shared: later lookups (from any host thread)
+  // only read them
+  b.qindex.clear();
+  for (size_t i = 0; i < b.qs.size(); ++i) b.qindex[b.qs[i]] = static_cast<int>(i);
+  b.offset_cache.assign(b.qs.size(), {});
+  for (size_t i = 0; i < b.qs.size(); ++i) {
+    int64_t off = 0;
+    for (const auto& tr : b.trees[i]) {
+      b.offset_cache[i].emplace(tr, off);
+      off += tr.dim;
+    }
+  }
   auto sp = std::make_shared<const Qbasis>(std::move(b));
   g_interned[k] = sp;
   return sp;

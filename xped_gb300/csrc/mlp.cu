@@ -9,6 +9,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 
 #include "kernels.hpp"
 
@@ -201,14 +202,14 @@ __global__ void mlp_reduce_adam_kernel(float* __restrict__ p, float* __restrict_
   p[i] -= lr * (m1 / c1) / (sqrtf(v1 / c2) + eps);
 }
 
-bool g_attr_set = false;
+std::once_flag g_attr_set;
 
 void set_attrs() {
-  if (g_attr_set) return;
-  const int bytes = kSmemFloats * int(sizeof(float));
-  cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  g_attr_set = true;
+  std::call_once(g_attr_set, [] {
+    const int bytes = kSmemFloats * int(sizeof(float));
+    cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(mlp_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  });
 }
 
 int grid_for(int64_t n) {

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "kernels.hpp"
 
@@ -477,7 +478,7 @@ __global__ void __launch_bounds__(32 * kTrinvCols) trinv_kernel(const CholDesc* 
 void launch_chol_inv(const CholDesc* d_descs, int n, int64_t max_l, double* G, double* Rinv, double rel_shift,
                      int* bad, cudaStream_t s) {
   if (n <= 0 || max_l <= 0) return;
-  static bool attr = false;
+  static std::once_flag attr;
   // Cholesky alone: one l x (l | 1) matrix in shared memory up to l = 167 (< 227 KB)
   constexpr int kCapChol = 167;
   // Cholesky and inverse in one CTA (blocks wider than the register-resident inverse allows):
@@ -485,23 +486,21 @@ void launch_chol_inv(const CholDesc* d_descs, int n, int64_t max_l, double* G, d
   constexpr int kCapBoth = 119;
   constexpr int kBytesChol = kCapChol * (kCapChol | 1) * int(sizeof(double));
   constexpr int kBytesBoth = 2 * kCapBoth * (kCapBoth | 1) * int(sizeof(double));
-  if (!attr) {
+  std::call_once(attr, [] {
     cudaFuncSetAttribute(chol_inv_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBytesChol);
     cudaFuncSetAttribute(chol_inv_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kBytesBoth);
-    attr = true;
-  }
+  });
   if (max_l > 64 * 32) {
     chol_inv_kernel<true><<<n, 1024, kBytesBoth, s>>>(d_descs, G, Rinv, rel_shift, bad, kCapBoth);
     count_launch();
     return;
   }
   if (max_l <= kCholWarpL) {
-    static bool wattr = false;
-    if (!wattr) {
+    static std::once_flag wattr;
+    std::call_once(wattr, [] {
       cudaFuncSetAttribute(chol_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kCholWarpL * (kCholWarpL | 1) * int(sizeof(double)));
-      wattr = true;
-    }
+    });
     const int lw = int(max_l);
     chol_warp_kernel<<<n, 32, lw * (lw | 1) * int(sizeof(double)), s>>>(d_descs, G, rel_shift, bad);
   } else {
@@ -514,13 +513,12 @@ void launch_chol_inv(const CholDesc* d_descs, int n, int64_t max_l, double* G, d
   count_launch();
   const int chunks = int((max_l + kTrinvCols - 1) / kTrinvCols);
   if (max_l <= kTrinvStageL) {
-    static bool tattr = false;
-    if (!tattr) {
+    static std::once_flag tattr;
+    std::call_once(tattr, [] {
       for (auto f : {trinv_kernel<4, true>, trinv_kernel<8, true>})
         cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              int(sizeof(double)) * kTrinvStageL * (kTrinvStageL + 1));
-      tattr = true;
-    }
+    });
     const size_t sm = sizeof(double) * size_t(max_l) * size_t(max_l + 1);
     if (max_l <= 128)
       trinv_kernel<4, true><<<n * chunks, 32 * kTrinvCols, sm, s>>>(d_descs, chunks, G, Rinv);

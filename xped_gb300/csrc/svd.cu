@@ -42,6 +42,7 @@
 #include <stdexcept>
 #include <cmath>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "kernels.hpp"
@@ -637,28 +638,35 @@ size_t svd_work_elems(int64_t m, int64_t n) {
 void launch_svd(const xgb_svd_desc* d_descs, const xgb_svd_desc* h_descs, const int64_t* d_work_off, int n,
                 int64_t max_k, const double* A, double* U, double* S, double* Vt, double* work, cudaStream_t s) {
   if (n <= 0) return;
-  if (g_stats_cap < n) {
-    if (g_stats_dev) cudaFree(g_stats_dev);
-    cudaMalloc(&g_stats_dev, sizeof(int) * 6 * n);
-    g_stats_cap = n;
+  // sweep statistics of lane 0's calls only (a side lane records none: the buffer is not shared)
+  int* stats = nullptr;
+  if (lane() == 0) {
+    if (g_stats_cap < n) {
+      if (g_stats_dev) cudaFree(g_stats_dev);
+      cudaMalloc(&g_stats_dev, sizeof(int) * 6 * n);
+      g_stats_cap = n;
+    }
+    g_stats_n = n;
+    stats = g_stats_dev;
   }
-  g_stats_n = n;
   // Every CTA gets the full staging budget (one CTA per SM); each block
   // checks whether its 2b staged columns fit and otherwise rotates in L2.
   (void)max_k;
   const int smem = kSmemLimit;
-  static bool configured = false;
-  if (!configured) {
+  static std::once_flag configured;
+  std::call_once(configured, [] {
     cudaFuncSetAttribute(svd_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
     cudaFuncSetAttribute(svd_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
-    configured = true;
-  }
+  });
+  // Wide blocks run on the grid-wide kernel only from lane 0: a side lane shares the SMs with the
+  // other lane's kernels, and the grid-wide kernel's blocks wait on one another, so there every
+  // block stays on the cluster kernel (which takes any width, rotating in L2).
   std::vector<int> wide;
-  if (h_descs)
+  if (h_descs && lane() == 0)
     for (int i = 0; i < n; ++i)
       if (std::min(h_descs[i].m, h_descs[i].n) >= kSvdGridMin) wide.push_back(i);
   const int64_t grid_min = wide.empty() ? INT64_MAX : kSvdGridMin;
-  svd_cluster_kernel<<<n * kCluster, kThreads, smem, s>>>(d_descs, d_work_off, A, U, S, Vt, work, g_stats_dev, smem,
+  svd_cluster_kernel<<<n * kCluster, kThreads, smem, s>>>(d_descs, d_work_off, A, U, S, Vt, work, stats, smem,
                                                           grid_min);
   count_launch();
   if (wide.empty()) return;
@@ -669,7 +677,7 @@ void launch_svd(const xgb_svd_desc* d_descs, const xgb_svd_desc* h_descs, const 
     const int64_t nn = std::min(h_descs[sector].m, h_descs[sector].n);
     const int ctas = int(std::max<int64_t>(1, std::min<int64_t>(sms, (nn + 2 * kGridCols - 1) / (2 * kGridCols))));
     void* args[] = {const_cast<xgb_svd_desc**>(&d_descs), const_cast<int64_t**>(&d_work_off), &sector,
-                    const_cast<double**>(&A), &U, &S, &Vt, &work, &g_stats_dev, const_cast<int*>(&smem)};
+                    const_cast<double**>(&A), &U, &S, &Vt, &work, &stats, const_cast<int*>(&smem)};
     const cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(svd_grid_kernel), dim3(ctas),
                                                       dim3(kThreads), args, size_t(smem), s);
     if (e != cudaSuccess) throw std::runtime_error(std::string("svd grid launch: ") + cudaGetErrorString(e));

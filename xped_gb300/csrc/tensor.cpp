@@ -29,7 +29,9 @@ static void cuda_ok(cudaError_t e, const char* what) {
 // asynchronous copy, so building a plan neither allocates with cudaMalloc nor waits for the device
 // (both stall a queue that a synchronisation has just drained).  The host tables live as long as the
 // plan, so no copy can read freed host memory; the device memory is released in stream order when
-// the last user drops the plan.
+// the last user drops the plan.  Plans are shared by the lanes of a fork-join section: a side lane
+// waits for its uploads before the plan is published (the other lane may use it at once), and once
+// sections have run the release also waits for the work enqueued on every lane.
 struct PlanMem {
   std::vector<void*> dev;
   std::vector<std::shared_ptr<const void>> host;
@@ -37,6 +39,8 @@ struct PlanMem {
   PlanMem(const PlanMem&) = delete;
   PlanMem& operator=(const PlanMem&) = delete;
   ~PlanMem() {
+    if (dev.empty()) return;
+    if (lanes_used()) order_after_lanes(stream());
     for (void* d : dev) dev_free(d);
   }
   template <class T>
@@ -46,6 +50,7 @@ struct PlanMem {
     dev.push_back(d);
     if (!h->empty())
       cuda_ok(cudaMemcpyAsync(d, h->data(), sizeof(T) * h->size(), cudaMemcpyHostToDevice, stream()), "plan upload");
+    if (lane() != 0) cuda_ok(cudaStreamSynchronize(stream()), "plan upload");
     host.push_back(h);
     return d;
   }
@@ -935,9 +940,9 @@ struct SvdPlan {
   int32_t* d_deg = nullptr;
 };
 std::unordered_map<uint64_t, std::shared_ptr<SvdPlan>> g_svd_plans;
-int32_t* g_keep_host = nullptr;  // pinned
-double* g_out2_host = nullptr;
-int g_keep_cap = 0;
+int32_t* g_keep_host[kLanes] = {nullptr, nullptr, nullptr};  // pinned, one per lane
+double* g_out2_host[kLanes] = {nullptr, nullptr, nullptr};
+int g_keep_cap[kLanes] = {0, 0, 0};
 
 std::shared_ptr<SvdPlan> get_svd_plan(const TensorMeta& m) {
   {
@@ -1007,14 +1012,17 @@ SVDResult truncate_spectra(const TensorMeta& m, const Spectra& sp, int64_t max_k
   prof_begin(K_TRUNC, st);
   launch_truncate(n, d_sb, d_deg, sp.S, s_total, max_keep, eps_svd, preserve_multiplets ? 1 : 0, keep_d, out2_d, st);
   prof_end(K_TRUNC, st, 8.0 * double(s_total));
-  if (g_keep_cap < n) {
-    if (g_keep_host) cudaFreeHost(g_keep_host);
-    cuda_ok(cudaMallocHost(&g_keep_host, sizeof(int32_t) * n), "pinned");
-    g_keep_cap = n;
-    if (!g_out2_host) cuda_ok(cudaMallocHost(&g_out2_host, sizeof(double) * 2), "pinned");
+  const int ln = lane();
+  int32_t*& keep_host = g_keep_host[ln];
+  double*& out2_host = g_out2_host[ln];
+  if (g_keep_cap[ln] < n) {
+    if (keep_host) cudaFreeHost(keep_host);
+    cuda_ok(cudaMallocHost(&keep_host, sizeof(int32_t) * n), "pinned");
+    g_keep_cap[ln] = n;
+    if (!out2_host) cuda_ok(cudaMallocHost(&out2_host, sizeof(double) * 2), "pinned");
   }
-  cuda_ok(cudaMemcpyAsync(g_keep_host, keep_d, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st), "d2h");
-  cuda_ok(cudaMemcpyAsync(g_out2_host, out2_d, sizeof(double) * 2, cudaMemcpyDeviceToHost, st), "d2h");
+  cuda_ok(cudaMemcpyAsync(keep_host, keep_d, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st), "d2h");
+  cuda_ok(cudaMemcpyAsync(out2_host, out2_d, sizeof(double) * 2, cudaMemcpyDeviceToHost, st), "d2h");
   SVDResult res;
   res.spectrum.resize(size_t(s_total));
   res.spec_begin = sp.s_begin;
@@ -1028,9 +1036,9 @@ SVDResult truncate_spectra(const TensorMeta& m, const Spectra& sp, int64_t max_k
     dev_free(d_deg);
   }
 
-  res.trunc_weight = g_out2_host[0];
-  res.entropy = g_out2_host[1];
-  res.keep.assign(g_keep_host, g_keep_host + n);
+  res.trunc_weight = out2_host[0];
+  res.entropy = out2_host[1];
+  res.keep.assign(keep_host, keep_host + n);
   for (int i = 0; i < n; ++i)
     if (res.keep[i] < 0 || res.keep[i] > sp.k[i]) throw std::runtime_error("tSVD: truncation returned an invalid count");
   // truncated basis: charges with kept values in ascending order (std::map, Tensor.cpp:592-598)
@@ -1434,6 +1442,11 @@ std::pair<Tensor, Tensor> CTM::decompose_dir(int d, const Tensor& t1, const Tens
   Tensor prod = matmul(t1, t2);
   const TensorMeta& m = *prod.meta;
   const size_t n = m.sectors.size();
+  // inside a fork-join section the statistics and the record go to this direction's slot and are
+  // committed in the sequential order afterwards; the seed is the one the sequential order gives
+  Deferred* df = defer_[d].on ? &defer_[d] : nullptr;
+  CTMStats& st = df ? df->delta : stats;
+  const int64_t dec_index = df ? df->index : stats.decompositions;
   DecompRecord rec;
   if (record) {
     rec.dir = d;
@@ -1445,7 +1458,7 @@ std::pair<Tensor, Tensor> CTM::decompose_dir(int d, const Tensor& t1, const Tens
   if (svd_mode == 0) {
     r = tsvd(prod, chi, 1.0e-10, false);
     for (size_t i = 0; i < n; ++i) width[i] = std::min(m.rows[i], m.cols[i]);
-    stats.exact_sectors += int64_t(n);
+    st.exact_sectors += int64_t(n);
   } else {
     if (!policy) throw std::runtime_error("CTM: randomized projector SVD without a width policy");
     std::vector<int64_t> want = policy->widths(m, hist[d], chi);
@@ -1455,18 +1468,18 @@ std::pair<Tensor, Tensor> CTM::decompose_dir(int d, const Tensor& t1, const Tens
           want[i] = std::min<int64_t>(chi, std::min(m.rows[i], m.cols[i])) + 16;
     RsvdInfo info;
     const bool warm = warm_iters >= 0 && warm_v[d].valid() && warm_v[d].meta->cod == m.cod;
-    r = tsvd_randomized(prod, chi, 1.0e-10, want, warm ? warm_iters : power_iters,
-                        seed + uint64_t(stats.decompositions), &info, warm ? &warm_v[d] : nullptr, res_tol,
-                        sketch_fp64_tail, exact_tc);
-    stats.refinements += info.refinements;
-    stats.max_residual = info.max_residual;
+    r = tsvd_randomized(prod, chi, 1.0e-10, want, warm ? warm_iters : power_iters, seed + uint64_t(dec_index), &info,
+                        warm ? &warm_v[d] : nullptr, res_tol, sketch_fp64_tail, exact_tc);
+    st.refinements += info.refinements;
+    st.max_residual = info.max_residual;
+    if (df) df->residual_set = true;
     width = info.width;
-    stats.exact_sectors += info.exact_sectors;
-    stats.sketched_sectors += int64_t(n) - info.exact_sectors;
-    stats.redo += int64_t(info.saturated.size());
-    stats.sketch_cols += info.sketch_cols;
+    st.exact_sectors += info.exact_sectors;
+    st.sketched_sectors += int64_t(n) - info.exact_sectors;
+    st.redo += int64_t(info.saturated.size());
+    st.sketch_cols += info.sketch_cols;
   }
-  ++stats.decompositions;
+  ++st.decompositions;
   // history for the next decomposition of this direction
   History h;
   double smax = 0;
@@ -1492,7 +1505,7 @@ std::pair<Tensor, Tensor> CTM::decompose_dir(int d, const Tensor& t1, const Tens
     for (size_t i = 0; i < n; ++i) rec.kmin.push_back(std::min(m.rows[i], m.cols[i]));
     rec.spectrum = r.spectrum;
     rec.spec_begin = r.spec_begin;
-    records.push_back(std::move(rec));
+    (df ? df->records : records).push_back(std::move(rec));
   }
   return projectors_from_svd(r, t1, t2);
 }
@@ -1634,12 +1647,55 @@ void CTM::move(char dir) {
   }
 }
 
+bool CTM::pairs_concurrent() const {
+  // exact projector SVDs keep their wide blocks on the grid-wide kernel of lane 0; per-launch
+  // profiling and autotune measurements time one lane at a time
+  return concurrent && svd_mode != 0 && !profiling() && autotune_mode() != 1;
+}
+
+void CTM::move_pair(char a, char b) {
+  auto dir = [](char c) { return c == 'L' ? 0 : c == 'R' ? 1 : c == 'T' ? 2 : 3; };
+  const int da = dir(a), db = dir(b);
+  defer_[da] = Deferred{};
+  defer_[db] = Deferred{};
+  defer_[da].on = defer_[db].on = true;
+  defer_[da].index = stats.decompositions;
+  defer_[db].index = stats.decompositions + 1;
+  try {
+    run_pair([&] { move(a); }, [&] { move(b); });
+  } catch (...) {
+    defer_[da].on = defer_[db].on = false;
+    throw;
+  }
+  for (int d : {da, db}) {
+    Deferred& f = defer_[d];
+    f.on = false;
+    stats.decompositions += f.delta.decompositions;
+    stats.sketched_sectors += f.delta.sketched_sectors;
+    stats.exact_sectors += f.delta.exact_sectors;
+    stats.redo += f.delta.redo;
+    stats.sketch_cols += f.delta.sketch_cols;
+    stats.refinements += f.delta.refinements;
+    if (f.residual_set) stats.max_residual = f.delta.max_residual;
+    for (auto& r : f.records) records.push_back(std::move(r));
+    f.records.clear();
+  }
+}
+
 void CTM::grow_all() {
-  // CTM::grow_all (src/PEPS/CTM.cpp:385-398)
-  move('L');
-  move('R');
-  move('T');
-  move('B');
+  // CTM::grow_all (src/PEPS/CTM.cpp:385-398): left, right, top, bottom.  The left and right moves
+  // read and replace disjoint environment tensors (C1 T4 C4 and C2 T2 C3; both read T1 and T3), and
+  // so do the top and bottom moves (C1 T1 C2 and C4 T3 C3; both read T2 and T4): each pair runs at
+  // once on two lanes, with the result of the sequential order.
+  if (!pairs_concurrent()) {
+    move('L');
+    move('R');
+    move('T');
+    move('B');
+    return;
+  }
+  move_pair('L', 'R');
+  move_pair('T', 'B');
 }
 
 CTM::SolveResult CTM::solve(const Tensor& H, double tol_E, int max_steps) {

@@ -258,9 +258,23 @@ class CTM {
   CTMStats stats;
   History hist[4];
   Tensor warm_v[4];  // last V^dag per direction (warm start of the randomized SVD)
+  // grow_all runs the left/right and the top/bottom moves two at a time on the runtime's side lanes
+  // (randomized projector SVD only; same results as one after the other)
+  bool concurrent = true;
 
  private:
   std::pair<Tensor, Tensor> decompose_dir(int d, const Tensor& t1, const Tensor& t2);
+  bool pairs_concurrent() const;
+  void move_pair(char a, char b);
+  // a direction's decomposition inside a fork-join section: its seed index, and its statistics and
+  // record, committed in the sequential order once both moves have returned
+  struct Deferred {
+    bool on = false, residual_set = false;
+    int64_t index = 0;
+    CTMStats delta;
+    std::vector<DecompRecord> records;
+  };
+  Deferred defer_[4];
   Tensor A, Ad;
   Tensor C1, C2, C3, C4, T1, T2, T3, T4;
 };

@@ -489,6 +489,12 @@ class CTM:
         check(lib().xgb_ctm_stats(self._h, out), "ctm_stats")
         return dict(zip(("decompositions", "sketched_sectors", "exact_sectors", "redo", "sketch_cols"), out))
 
+    def set_concurrent(self, on: bool = True):
+        """Run the left/right and the top/bottom moves of grow_all two at a time on two streams (the
+        default; randomized projector SVD only).  The result equals the sequential order's."""
+        check(lib().xgb_ctm_set_concurrent(self._h, int(on)), "ctm_set_concurrent")
+        return self
+
     def record(self, on: bool = True):
         check(lib().xgb_ctm_record(self._h, int(on)), "ctm_record")
         return self
