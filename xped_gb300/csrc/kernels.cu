@@ -283,6 +283,15 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __r
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int64_t row0 = int64_t(t.tm) * TILE, col0 = int64_t(t.tn) * TILE;
+  // a warp whose outputs all lie outside the block (an edge tile of a block narrower than the tile)
+  // skips the multiply-adds: GB300's narrow FP64 pipe takes as long for a warp instruction whatever
+  // its active lanes; its share of the staging loads and the barriers stays
+  bool live = false;
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int c = 0; c < R; ++c) live |= row0 + tx + 16 * r < d.m && col0 + ty + 16 * c < d.n;
+  const bool warp_live = __any_sync(0xffffffffu, live);
   T acc[R][R];
 #pragma unroll
   for (int i = 0; i < R; ++i)
@@ -329,7 +338,7 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(const xgb_gemm_desc* __r
   for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
     const bool more = k0 + BK < kend;
     if (more) fetch(k0 + BK);
-    const int kmax = (kend - k0) < BK ? int(kend - k0) : BK;
+    const int kmax = !warp_live ? 0 : (kend - k0) < BK ? int(kend - k0) : BK;
     for (int kk = 0; kk < kmax; ++kk) {
       T a[R], b[R];
 #pragma unroll

@@ -560,18 +560,182 @@ __global__ void __cluster_dims__(kCluster, 1, 1) __launch_bounds__(kThreads)
   }
 }
 
-// Wide blocks: the same one-sided block Jacobi spread over every SM of the GPU (a cooperative launch of
-// one CTA per SM, grid-wide barriers between the rounds) instead of one 8-SM cluster, FP64 throughout
-// (no FP32 preconditioning: with 2 x SMs column blocks of a few columns each, a sweep is ~150x the
-// cluster's FP64 throughput per block).  One launch per block; the cluster kernel takes the narrower
-// blocks of the batch.
+// Wide blocks: QR-preconditioned one-sided Jacobi spread over every SM of the GPU (a cooperative launch
+// of one CTA per SM, grid-wide barriers), FP64 throughout.  One launch per block; the cluster kernel
+// takes the narrower blocks of the batch.
+//   1. Householder QR with column pivoting, op(A) P = Q R (Businger-Golub: the largest remaining column
+//      norm is pivoted in; the norms are downdated and recomputed under cancellation, the rule of
+//      LAPACK's xLAQP2).  Per step CTA 0 picks the pivot, swaps it into place and forms the reflector,
+//      and then every warp applies it to one trailing column.
+//   2. The block Jacobi of the cluster kernel on X = R^T (nn x nn): the rows of a column-pivoted R are
+//      graded, so the columns of X are close to orthogonal and converge in a few sweeps where op(A)
+//      itself took tens (the preconditioning of Drmac and Veselic's one-sided Jacobi SVD).
+//   3. X V = W with W_j = sigma_j u_j gives R = V Sigma U_X^T, so op(A) = (Q V) Sigma (P U_X)^T: each
+//      warp applies the reflectors to one column [V_j; 0] (no barriers), and P U_X is a row scatter.
 constexpr int kMaxSweepsGrid = 80;
+constexpr double kQrRecompute = 1.4901161193847656e-08;  // sqrt(eps): norm downdates below this are recomputed
+
+// sum over the 512 threads of a CTA, the same bits in every thread; red: kWarps doubles of shared memory
+__device__ double block_sum(double v, double* red, const Ctx& c) {
+  v = wsum(v);
+  __syncthreads();  // red is free (an earlier call's readers are done)
+  if (c.lane == 0) red[c.warp] = v;
+  __syncthreads();
+  double t = 0;
+  for (int w = 0; w < kWarps; ++w) t += red[w];
+  return t;
+}
+
+// Householder QR with column pivoting of H (mm x nn column-major, mm >= nn) in place: R on and above
+// the diagonal, the reflectors v_k = (1, H[k+1:, k]) below it, H_k = I - tau_k v_k v_k^T; piv[k] = the
+// column of the input at position k.  vn1 / vn2: partial column norms and their last exact values.
+template <class Group>
+__device__ void qr_pivoted(Group& gg, const Ctx& c, double* H, int64_t mm, int nn, double* tau, int* piv,
+                           double* vn1, double* vn2, double* red, int* redi) {
+  const unsigned full = 0xffffffffu;
+  for (int j = c.gw; j < nn; j += c.gnw) {
+    const double* h = H + int64_t(j) * mm;
+    double a = 0;
+    for (int64_t i = c.lane; i < mm; i += 32) {
+      const double x = ldg(h + i);
+      a = fma(x, x, a);
+    }
+    a = sqrt(wsum(a));
+    if (c.lane == 0) {
+      stg(vn1 + j, a);
+      stg(vn2 + j, a);
+      __stcg(piv + j, j);
+    }
+  }
+  gg.sync();
+  for (int k = 0; k < nn; ++k) {
+    if (c.rank == 0) {
+      // pivot: the largest remaining norm (the first such column on ties)
+      double best = -1.0;
+      int bi = k;
+      for (int j = k + c.tid; j < nn; j += kThreads) {
+        const double v = ldg(vn1 + j);
+        if (v > best) {
+          best = v;
+          bi = j;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(full, best, o);
+        const int oi = __shfl_xor_sync(full, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      __syncthreads();
+      if (c.lane == 0) {
+        red[c.warp] = best;
+        redi[c.warp] = bi;
+      }
+      __syncthreads();
+      best = red[0];
+      bi = redi[0];
+      for (int w = 1; w < kWarps; ++w)
+        if (red[w] > best || (red[w] == best && redi[w] < bi)) {
+          best = red[w];
+          bi = redi[w];
+        }
+      const int p = bi;
+      double* hk = H + int64_t(k) * mm;
+      double* hp = H + int64_t(p) * mm;
+      // swap columns k and p (every row: rows above k hold R's earlier entries), with the sum of squares of
+      // the new column k below row k
+      double ss = 0;
+      for (int64_t i = c.tid; i < mm; i += kThreads) {
+        const double x = ldg(hp + i);
+        if (p != k) {
+          stg(hp + i, ldg(hk + i));
+          stg(hk + i, x);
+        }
+        if (i > k) ss = fma(x, x, ss);
+      }
+      ss = block_sum(ss, red, c);  // its barriers also order the swap before the reads below
+      if (c.tid == 0 && p != k) {
+        const double a1 = ldg(vn1 + k), a2 = ldg(vn2 + k);
+        stg(vn1 + k, ldg(vn1 + p));
+        stg(vn2 + k, ldg(vn2 + p));
+        stg(vn1 + p, a1);
+        stg(vn2 + p, a2);
+        const int q = __ldcg(piv + k);
+        __stcg(piv + k, __ldcg(piv + p));
+        __stcg(piv + p, q);
+      }
+      // reflector: beta = -sign(alpha) |(alpha, x)|, tau = (beta - alpha) / beta, v = x / (alpha - beta)
+      const double alpha = ldg(hk + k);
+      double beta = alpha, t = 0.0, scal = 0.0;
+      if (ss > 0.0) {
+        beta = -copysign(sqrt(fma(alpha, alpha, ss)), alpha);
+        t = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
+        for (int64_t i = k + 1 + c.tid; i < mm; i += kThreads) stg(hk + i, ldg(hk + i) * scal);
+      }
+      if (c.tid == 0) {
+        stg(hk + k, beta);
+        stg(tau + k, t);
+      }
+    }
+    gg.sync();
+    // apply H_k to the trailing columns (one warp each) and downdate their norms
+    const double tk = ldg(tau + k);
+    const double* v = H + int64_t(k) * mm;
+    for (int j = k + 1 + c.gw; j < nn; j += c.gnw) {
+      double* h = H + int64_t(j) * mm;
+      const double hkj = ldg(h + k);
+      double w = 0.0;
+      if (tk != 0.0) {
+        double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        int64_t i = k + 1 + c.lane;
+        for (; i + 96 < mm; i += 128) {
+          a0 = fma(ldg(v + i), ldg(h + i), a0);
+          a1 = fma(ldg(v + i + 32), ldg(h + i + 32), a1);
+          a2 = fma(ldg(v + i + 64), ldg(h + i + 64), a2);
+          a3 = fma(ldg(v + i + 96), ldg(h + i + 96), a3);
+        }
+        for (; i < mm; i += 32) a0 = fma(ldg(v + i), ldg(h + i), a0);
+        w = tk * (hkj + wsum((a0 + a1) + (a2 + a3)));
+        for (int64_t i2 = k + 1 + c.lane; i2 < mm; i2 += 32) stg(h + i2, fma(-w, ldg(v + i2), ldg(h + i2)));
+      }
+      const double rkj = hkj - w;  // R(k, j)
+      if (c.lane == 0) stg(h + k, rkj);
+      const double n1 = ldg(vn1 + j);
+      if (n1 != 0.0) {  // warp-uniform
+        double r = fabs(rkj) / n1;
+        r = fmax(0.0, (1.0 + r) * (1.0 - r));
+        const double q = n1 / ldg(vn2 + j);
+        double n1new;
+        if (r * q * q <= kQrRecompute) {
+          // each lane re-reads the rows it wrote above
+          double a = 0;
+          for (int64_t i2 = k + 1 + c.lane; i2 < mm; i2 += 32) {
+            const double x = ldg(h + i2);
+            a = fma(x, x, a);
+          }
+          n1new = sqrt(wsum(a));
+          if (c.lane == 0) stg(vn2 + j, n1new);
+        } else {
+          n1new = n1 * sqrt(r);
+        }
+        if (c.lane == 0) stg(vn1 + j, n1new);
+      }
+    }
+    gg.sync();
+  }
+}
+
 __global__ void __launch_bounds__(kThreads)
     svd_grid_kernel(const xgb_svd_desc* __restrict__ descs, const int64_t* __restrict__ work_off, int sector,
                     const double* __restrict__ A, double* __restrict__ U, double* __restrict__ S,
                     double* __restrict__ Vt, double* __restrict__ work, int* __restrict__ sweep_stats,
                     int smem_bytes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[kWarps];
+  __shared__ int redi[kWarps];
   cg::grid_group gg = cg::this_grid();
   const xgb_svd_desc d = descs[sector];
   const bool tr = d.m < d.n;
@@ -589,36 +753,121 @@ __global__ void __launch_bounds__(kThreads)
   c.gtid = c.rank * kThreads + c.tid;
   c.gnt = int(gridDim.x) * kThreads;
 
-  // workspace as in the cluster kernel: W64 mm*nn | V64 nn*nn | (2 nn*nn unused) | n64 nn | misc
+  // workspace (doubles): H mm*nn | V nn*nn | T1 nn*nn | X nn*nn | n64 nn | misc 8 | Y mm*nn (svd_work_elems
+  // adds Y for blocks this wide); T1: the Jacobi column order (nn ints), then tau, vn1, vn2 (nn each), piv
   const int64_t nn2 = int64_t(nn) * nn;
-  double* W64 = work + work_off[sector];
-  double* V64 = W64 + mm * nn;
-  double* n64 = V64 + 3 * nn2;
+  double* H = work + work_off[sector];
+  double* V64 = H + mm * nn;
+  double* T1 = V64 + nn2;
+  double* X = T1 + nn2;
+  double* n64 = X + nn2;
   int* flag = reinterpret_cast<int*>(n64 + nn);
+  double* Y = n64 + nn + 8;
+  int* jorder = reinterpret_cast<int*>(T1);
+  double* tau = T1 + nn;
+  double* vn1 = tau + nn;
+  double* vn2 = vn1 + nn;
+  int* piv = reinterpret_cast<int*>(vn2 + nn);
   auto opA = [&](int64_t i, int64_t j) { return tr ? A[d.a_off + j + i * d.m] : A[d.a_off + i + j * d.m]; };
   const long long t0 = clock64();
-  for (int j = c.gw; j < nn; j += c.gnw) {
-    for (int64_t i = c.lane; i < mm; i += 32) stg(W64 + int64_t(j) * mm + i, opA(i, j));
-    for (int i = c.lane; i < nn; i += 32) stg(V64 + int64_t(j) * nn + i, i == j ? 1.0 : 0.0);
-  }
+  for (int j = c.gw; j < nn; j += c.gnw)
+    for (int64_t i = c.lane; i < mm; i += 32) stg(H + int64_t(j) * mm + i, opA(i, j));
   gg.sync();
+  qr_pivoted(gg, c, H, mm, nn, tau, piv, vn1, vn2, red, redi);
+  // X = R^T (lower triangle), V = I
+  for (int j = c.gw; j < nn; j += c.gnw)
+    for (int i = c.lane; i < nn; i += 32) {
+      stg(X + int64_t(j) * nn + i, i >= j ? ldg(H + int64_t(i) * mm + j) : 0.0);
+      stg(V64 + int64_t(j) * nn + i, i == j ? 1.0 : 0.0);
+    }
+  gg.sync();
+  const long long t1 = clock64();
   const int nblocks = 2 * int(gridDim.x);
   const int b = (nn + nblocks - 1) / nblocks;
-  const bool staged = int64_t(2 * b) * (mm + nn + 1) * 8 <= smem_bytes;
-  const int sw = nn > 1 ? block_jacobi<double>(gg, c, W64, V64, n64, flag, mm, nn, 1.0e-13, kFloor64, kMaxSweepsGrid,
-                                               reinterpret_cast<double*>(smem_raw), staged, nblocks,
-                                               reinterpret_cast<int*>(V64 + nn2))
+  const bool staged = int64_t(2 * b) * (nn + nn + 1) * 8 <= smem_bytes;
+  const int sw = nn > 1 ? block_jacobi<double>(gg, c, X, V64, n64, flag, nn, nn, 1.0e-13, kFloor64, kMaxSweepsGrid,
+                                               reinterpret_cast<double*>(smem_raw), staged, nblocks, jorder)
                         : 0;
-  const long long t1 = clock64();
-  finish_svd(gg, c, d, tr, mm, nn, W64, V64, n64, U, S, Vt);
+  const long long t2 = clock64();
+  // sigma_j = |x_j|
+  for (int j = c.gw; j < nn; j += c.gnw) {
+    const double* x = X + int64_t(j) * nn;
+    double a = 0;
+    for (int i = c.lane; i < nn; i += 32) {
+      const double e = ldg(x + i);
+      a = fma(e, e, a);
+    }
+    a = wsum(a);
+    if (c.lane == 0) stg(n64 + j, sqrt(a));
+  }
+  gg.sync();
+  // per Jacobi column j (one warp, no barriers): rank r among the sigmas (descending, ties by column),
+  // Y_j = Q [V_j; 0] (reflectors H_{nn-1} first; lane ln owns rows ln + 32 t throughout), then U, S, V^T of
+  // the block with the sign rule
+  const int64_t kk = nn;
+  for (int j = c.gw; j < nn; j += c.gnw) {
+    const double sj = ldg(n64 + j);
+    int r = 0;
+    for (int i = c.lane; i < nn; i += 32) {
+      const double si = ldg(n64 + i);
+      r += (si > sj) || (si == sj && i < j);
+    }
+    r = wsum(r);
+    const double inv = sj > 0 ? 1.0 / sj : 0.0;
+    double* y = Y + int64_t(j) * mm;
+    for (int64_t i = c.lane; i < mm; i += 32) stg(y + i, i < nn ? ldg(V64 + int64_t(j) * nn + i) : 0.0);
+    for (int k = nn - 1; k >= 0; --k) {
+      const double tk = ldg(tau + k);
+      if (tk == 0.0) continue;  // uniform
+      const double* v = H + int64_t(k) * mm;
+      double a0 = 0, a1 = 0, yk = 0;
+      int64_t i = c.lane;
+      for (; i + 32 < mm; i += 64) {
+        const double y0 = ldg(y + i), y1 = ldg(y + i + 32);
+        if (i > k) a0 = fma(ldg(v + i), y0, a0);
+        else if (i == k) yk = y0;
+        if (i + 32 > k) a1 = fma(ldg(v + i + 32), y1, a1);
+        else if (i + 32 == k) yk = y1;
+      }
+      for (; i < mm; i += 32) {
+        const double y0 = ldg(y + i);
+        if (i > k) a0 = fma(ldg(v + i), y0, a0);
+        else if (i == k) yk = y0;
+      }
+      yk = __shfl_sync(0xffffffffu, yk, k & 31);
+      const double w = tk * (yk + wsum(a0 + a1));
+      for (int64_t i2 = c.lane; i2 < mm; i2 += 32) {
+        if (i2 == k) stg(y + i2, yk - w);
+        else if (i2 > k) stg(y + i2, fma(-w, ldg(v + i2), ldg(y + i2)));
+      }
+    }
+    // op(A) = Y Sigma (P U_X)^T with U_X = X / sigma: column j of P U_X has X[i, j] / sigma_j at row piv[i]
+    double* ucol = U + d.u_off + int64_t(r) * d.m;
+    double sg;
+    if (!tr) {
+      sg = sign_of(y, mm, 1.0, c.lane);
+      for (int64_t i = c.lane; i < mm; i += 32) ucol[i] = sg * ldg(y + i);
+      for (int i = c.lane; i < nn; i += 32)
+        Vt[d.vt_off + r + int64_t(__ldcg(piv + i)) * kk] = sg * inv * ldg(X + int64_t(j) * nn + i);
+    } else {
+      // U = P U_X (nn rows): scattered, then read back for the sign
+      for (int i = c.lane; i < nn; i += 32) stg(ucol + __ldcg(piv + i), inv * ldg(X + int64_t(j) * nn + i));
+      __syncwarp();
+      sg = sign_of(ucol, nn, 1.0, c.lane);
+      if (sg < 0)
+        for (int i = c.lane; i < nn; i += 32) stg(ucol + i, -ldg(ucol + i));
+      for (int64_t cc = c.lane; cc < mm; cc += 32) Vt[d.vt_off + r + cc * kk] = sg * ldg(y + cc);
+    }
+    if (c.lane == 0) S[d.s_off + r] = sj;
+  }
   if (sweep_stats && c.rank == 0 && c.tid == 0) {
     int* st6 = sweep_stats + 6 * sector;
     st6[0] = 0;
     st6[1] = sw;
-    st6[2] = 0;
+    st6[2] = int((t1 - t0) >> 10);  // QR cycles / 1024 on CTA 0's SM
     st6[3] = 0;
-    st6[4] = int((t1 - t0) >> 10);
-    st6[5] = int((clock64() - t1) >> 10);
+    st6[4] = int((t2 - t1) >> 10);
+    st6[5] = int((clock64() - t2) >> 10);
   }
 }
 
@@ -632,7 +881,9 @@ size_t svd_work_elems(int64_t m, int64_t n) {
   const int64_t mm = std::max(m, n), nn = std::min(m, n);
   const int64_t doubles = mm * nn + 3 * nn * nn + nn + 8;
   const int64_t floats = mm * nn + nn * nn + nn;
-  return size_t(doubles + (floats + 1) / 2 + 2);
+  // blocks on the grid-wide kernel also hold Q's columns (mm x nn) behind the misc slots
+  const int64_t grid_extra = nn >= kSvdGridMin ? mm * nn : 0;
+  return size_t(doubles + std::max((floats + 1) / 2 + 2, grid_extra));
 }
 
 void launch_svd(const xgb_svd_desc* d_descs, const xgb_svd_desc* h_descs, const int64_t* d_work_off, int n,
