@@ -184,6 +184,10 @@ def run_gpu(args):
     ctm.record(False)
     if args.autotune:
         L.xgb_autotune_set(2)  # frozen: no measurement inside the timed steps
+    # one more untimed step in the timed configuration: the first step that runs the move pairs on two
+    # streams (not while the autotuner measures) starts the side lane's host thread and its buffers
+    ctm.grow_all()
+    L.xgb_synchronize()
     res["chosen_setup_s"] = time.perf_counter() - t0
     res["autotune"] = autotune_report(L)
 
