@@ -476,9 +476,14 @@ def permute_roofline(degs=(20, 40, 60, 40, 20), reps=5):
     algorithmic = 16.0 * T.size
     gbs = algorithmic / (per_launch * 1e-3) / 1e9
     del T
-    return {"kernel": "permute_rows_kernel", "elements": int(algorithmic // 16), "gbytes_moved": algorithmic / 1e9,
-            "launches": int(n), "ms_per_launch": per_launch, "achieved": gbs, "peak": hbm, "unit": "GB/s",
-            "frac": gbs / hbm, "bound": "hbm",
+    # DRAM read + write of one launch from an ncu capture of the [14, 28, 42, 28, 14] case (42.5 M
+    # doubles: 344.7 MB read, 294.2 MB written, the rest of the output still in L2 at the kernel's end),
+    # scaled by the element count (the traffic grows in proportion)
+    traffic = (344.672e6 + 294.158e6) * (algorithmic / 16.0) / 42526512.0
+    return {"kernel": "permute_rows_wide_kernel", "elements": int(algorithmic // 16),
+            "gbytes_moved": algorithmic / 1e9, "launches": int(n), "ms_per_launch": per_launch, "achieved": gbs,
+            "peak": hbm, "unit": "GB/s", "frac": gbs / hbm, "bound": "hbm", "traffic": traffic,
+            "traffic_source": "ncu capture of the deg [14, 28, 42, 28, 14] case scaled by elements",
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
             "workload": "U(1) Tensor<2,2>, legs q -2..2 deg " + str(list(degs)) + ", permute<0>(0,2,1,3)"}
 

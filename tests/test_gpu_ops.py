@@ -46,6 +46,23 @@ def test_permute_all(symname, pB, pC):
             assert_same(got, ref, rtol=tol, atol=tol)
 
 
+# Larger degeneracies: the runs along output leg 0 are long enough (element-weighted 6-70) that the
+# device takes its wide-row permute kernel (groups of 8-32 lanes) for these single-contribution plans,
+# with rows both shorter than a group and longer than one pass of two elements per lane.
+WIDE_CASES = [
+    ("u1", [(-1, 3), (0, 20), (1, 5)], [(0, 9), (1, 35), (2, 2)]),
+    ("fz2", [(0, 12), (1, 20)], [(0, 3), (1, 17)]),
+]
+
+
+@pytest.mark.parametrize("symname,pB,pC", WIDE_CASES)
+def test_permute_wide_rows(symname, pB, pC):
+    s, ob, nb, ot, nt = _pair_tensors(symname, pB, pC, seed=5)
+    for p in itertools.permutations(range(4)):
+        for shift in range(-2, 3):
+            assert_same(nt.permute(shift, list(p)), ot.permute(shift, list(p)), rtol=0.0, atol=0.0)
+
+
 def test_twist_then_permute():
     s, ob, nb, ot, nt = _pair_tensors("fu1", *CASES[2][1:])
     for mask in range(16):

@@ -637,6 +637,182 @@ __global__ void __launch_bounds__(256) permute_rows_kernel(const xgb_perm_task* 
   }
 }
 
+// Wide-row form (groups of G >= 8 lanes, rows of about G or more elements).  The row cursor above
+// keeps every leg's extent and strides in registers (128 per thread for G = 32: two CTAs per SM),
+// which leaves too few loads in flight to cover HBM latency on large tensors.  Here lane u < 8 of a
+// group decodes row u of the group's 8-row chunk on its own (task by the cached range or a binary
+// search, multi-index by 32-bit division, the per-leg fields read from the L1-resident task table
+// in a loop rather than held in registers), and the row's offsets, strides, length and coefficient
+// reach the other lanes by shuffles.  The loads go through shared memory instead of registers:
+// every lane copies the first 2G elements of each of the chunk's 8 rows (16 elements) with 8-byte
+// cp.async into its own column of the warp's staging buffer, so that in-flight data costs no
+// registers.  Two stages per warp: the next chunk is decoded and its copies issued before the
+// current chunk's copies are awaited, scaled by the coefficient and stored.  Elements past 2G of a
+// long row are copied directly.  It serves plans in which every task has exactly one contribution
+// (every abelian permute); plans with several contributions per task (SU(2) recoupling) take the
+// cursor kernel above.  Loop bounds that contain shuffles are warp-uniform (chunks are taken per
+// warp).
+constexpr int kWideSlots = 2;      // staged elements per row and lane
+constexpr int kWideThreads = 128;  // 4 warps per CTA: 32 KB of staging
+
+__device__ __forceinline__ void find_task(const int64_t* __restrict__ row_start, int n_tasks, int64_t r, int& ti,
+                                          int64_t& lo, int64_t& hi) {
+  if (r >= lo && r < hi) return;
+  int a = 0, b = n_tasks - 1;
+  while (a < b) {
+    const int mid = (a + b + 1) >> 1;
+    if (row_start[mid] <= r) a = mid; else b = mid - 1;
+  }
+  ti = a;
+  lo = row_start[a];
+  hi = row_start[a + 1];
+}
+
+__device__ __forceinline__ int split_index(int64_t& rem, int dk) {
+  if (rem < (int64_t(1) << 31)) {  // 32-bit division for the common case
+    const uint32_t r32 = uint32_t(rem), q = r32 / uint32_t(dk);
+    rem = q;
+    return int(r32 - q * uint32_t(dk));
+  }
+  const int64_t q = rem / dk;
+  const int ik = int(rem - q * dk);
+  rem = q;
+  return ik;
+}
+
+__device__ __forceinline__ void cp_async8(double* smem, const double* gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <typename SI>
+struct WideRow {  // one decoded row (len 0: no row)
+  long long dofs = 0, sofs = 0;
+  double coeff = 0.0;
+  int len = 0;
+  SI ds0 = 0, ss0 = 0;
+};
+
+template <typename SI>
+__device__ __forceinline__ WideRow<SI> wide_decode(const xgb_perm_task* __restrict__ tasks,
+                                                   const int64_t* __restrict__ row_start, int n_tasks,
+                                                   int64_t total_rows, const xgb_perm_contrib* __restrict__ contribs,
+                                                   int64_t r, bool valid, int& ti, int64_t& lo, int64_t& hi) {
+  WideRow<SI> w;
+  if (!valid || r >= total_rows) return w;
+  find_task(row_start, n_tasks, r, ti, lo, hi);
+  const xgb_perm_task& t = tasks[ti];
+  const xgb_perm_contrib& c = contribs[t.contrib0];  // the only contribution
+  const int rank = t.rank;
+  int64_t rem = r - lo;
+  int64_t dofs = t.dst_base, sofs = c.src_base;
+  for (int k = 1; k < rank; ++k) {
+    const int ik = split_index(rem, t.dims[k]);
+    dofs += int64_t(ik) * t.dst_stride[k];
+    sofs += int64_t(ik) * c.src_stride[k];
+  }
+  w.dofs = dofs;
+  w.sofs = sofs;
+  w.coeff = c.coeff;
+  w.len = rank > 0 ? t.dims[0] : 1;
+  w.ds0 = rank > 0 ? SI(t.dst_stride[0]) : SI(0);
+  w.ss0 = rank > 0 ? SI(c.src_stride[0]) : SI(0);
+  return w;
+}
+
+template <int G, typename SI>
+__global__ void __launch_bounds__(kWideThreads, 6) permute_rows_wide_kernel(const xgb_perm_task* __restrict__ tasks,
+                                                                            const int64_t* __restrict__ row_start,
+                                                                            int n_tasks, int64_t total_rows,
+                                                                            const xgb_perm_contrib* __restrict__ contribs,
+                                                                            const double* __restrict__ src,
+                                                                            double* __restrict__ dst) {
+  static_assert(G >= kRowsPerChunk && G <= 32, "one decoding lane per row of the chunk");
+  constexpr int kGroupsPerWarp = 32 / G;
+  constexpr int kHead = kWideSlots * G;  // staged elements per row
+  constexpr unsigned kFull = 0xffffffffu;
+  __shared__ double stage[kWideThreads / 32][2][kRowsPerChunk * kWideSlots][32];
+  const int lane = int(threadIdx.x) & 31;
+  const int wib = int(threadIdx.x) >> 5;
+  const int gl = lane % G;
+  const bool decoder = gl < kRowsPerChunk;
+  const int64_t warp = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+  const int64_t nchunks = (total_rows + kRowsPerChunk - 1) / kRowsPerChunk;
+  const int64_t step = nwarps * kGroupsPerWarp;
+  int ti = 0;
+  int64_t lo = 0, hi = 0;  // rows of task ti (empty: the first row searches)
+
+  // copies of the first kHead elements of the chunk's rows into stage st (one commit group)
+  auto issue = [&](const WideRow<SI>& w, int st) {
+#pragma unroll
+    for (int u = 0; u < kRowsPerChunk; ++u) {
+      const long long so = __shfl_sync(kFull, w.sofs, u, G);
+      const SI ss = __shfl_sync(kFull, w.ss0, u, G);
+      const int lu = __shfl_sync(kFull, w.len, u, G);
+#pragma unroll
+      for (int j = 0; j < kWideSlots; ++j) {
+        const int i = j * G + gl;
+        if (i < lu) cp_async8(&stage[wib][st][u * kWideSlots + j][lane], src + so + int64_t(i) * ss);
+      }
+    }
+    cp_async_commit();
+  };
+  // scaled stores of the staged elements, then the elements past kHead of long rows
+  auto drain = [&](const WideRow<SI>& w, int st) {
+#pragma unroll
+    for (int u = 0; u < kRowsPerChunk; ++u) {
+      const long long dof = __shfl_sync(kFull, w.dofs, u, G);
+      const SI ds = __shfl_sync(kFull, w.ds0, u, G);
+      const int lu = __shfl_sync(kFull, w.len, u, G);
+      const double cf = __shfl_sync(kFull, w.coeff, u, G);
+#pragma unroll
+      for (int j = 0; j < kWideSlots; ++j) {
+        const int i = j * G + gl;
+        if (i < lu) dst[dof + int64_t(i) * ds] = cf * stage[wib][st][u * kWideSlots + j][lane];
+      }
+    }
+    if (__reduce_max_sync(kFull, w.len) > kHead) {
+      for (int u = 0; u < kRowsPerChunk; ++u) {
+        const long long so = __shfl_sync(kFull, w.sofs, u, G);
+        const long long dof = __shfl_sync(kFull, w.dofs, u, G);
+        const SI ss = __shfl_sync(kFull, w.ss0, u, G);
+        const SI ds = __shfl_sync(kFull, w.ds0, u, G);
+        const int lu = __shfl_sync(kFull, w.len, u, G);
+        const double cf = __shfl_sync(kFull, w.coeff, u, G);
+        for (int i = kHead + gl; i < lu; i += G) dst[dof + int64_t(i) * ds] = cf * __ldg(src + so + int64_t(i) * ss);
+      }
+    }
+  };
+
+  int64_t cb = warp * kGroupsPerWarp;
+  if (cb >= nchunks) return;  // warp-uniform
+  int64_t chunk = cb + lane / G;
+  WideRow<SI> cur = wide_decode<SI>(tasks, row_start, n_tasks, total_rows, contribs, chunk * kRowsPerChunk + gl,
+                                    decoder && chunk < nchunks, ti, lo, hi);
+  issue(cur, 0);
+  int st = 0;
+  for (; cb < nchunks; cb += step) {
+    const int64_t nb = cb + step;
+    WideRow<SI> nxt;
+    if (nb < nchunks) {  // warp-uniform
+      chunk = nb + lane / G;
+      nxt = wide_decode<SI>(tasks, row_start, n_tasks, total_rows, contribs, chunk * kRowsPerChunk + gl,
+                            decoder && chunk < nchunks, ti, lo, hi);
+      issue(nxt, st ^ 1);
+      cp_async_wait<1>();  // the current chunk's group has landed
+    } else {
+      cp_async_wait<0>();
+    }
+    drain(cur, st);
+    cur = nxt;
+    st ^= 1;
+  }
+}
+
 PermRows perm_rows(const xgb_perm_task* tasks, int n_tasks, const xgb_perm_contrib* contribs, int n_contrib) {
   PermRows r;
   r.row_start.assign(size_t(n_tasks) + 1, 0);
@@ -649,6 +825,7 @@ PermRows perm_rows(const xgb_perm_task* tasks, int n_tasks, const xgb_perm_contr
     weighted += double(tasks[t].nelem) * double(d0);
   }
   r.total_rows = r.row_start.back();
+  for (int t = 0; t < n_tasks && r.single; ++t) r.single = tasks[t].n_contrib == 1;
   auto wide = [](int64_t v) { return v > INT32_MAX || v < INT32_MIN; };
   for (int t = 0; t < n_tasks && r.narrow; ++t)
     for (int k = 0; k < tasks[t].rank; ++k)
@@ -664,29 +841,39 @@ PermRows perm_rows(const xgb_perm_task* tasks, int n_tasks, const xgb_perm_contr
 
 template <typename SI>
 void launch_permute_t(const xgb_perm_task* d_tasks, const int64_t* d_row_start, int n_tasks, int64_t total_rows,
-                      int group, const xgb_perm_contrib* d_contribs, const double* src, double* dst, cudaStream_t s) {
+                      int group, bool single, const xgb_perm_contrib* d_contribs, const double* src, double* dst,
+                      cudaStream_t s) {
   if (total_rows <= 0 || n_tasks <= 0) return;
   // one group per chunk of kRowsPerChunk rows; enough CTAs to fill the GPU a few times over
   const int64_t groups_needed = (total_rows + kRowsPerChunk - 1) / kRowsPerChunk;
   const int64_t per_block = 256 / group;
   const int64_t cap = int64_t(num_sms() > 0 ? num_sms() : 152) * 16;
   const unsigned blocks = unsigned(std::max<int64_t>(1, std::min<int64_t>(cap, (groups_needed + per_block - 1) / per_block)));
-  switch (group) {
-    case 32: permute_rows_kernel<32, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
-    case 16: permute_rows_kernel<16, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
-    case 8: permute_rows_kernel<8, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+  // wide-row kernel: 128-thread CTAs, about one resident wave (six per SM) looping over the chunks
+  const int64_t wide_per_block = kWideThreads / group;
+  const unsigned wblocks = unsigned(std::max<int64_t>(
+      1, std::min<int64_t>(int64_t(num_sms() > 0 ? num_sms() : 152) * 6, (groups_needed + wide_per_block - 1) / wide_per_block)));
+  // the wide-row kernel for single-contribution plans whose rows fill a group of 8 or more lanes
+  switch (single || group < kRowsPerChunk ? group : -group) {
+    case 32: permute_rows_wide_kernel<32, SI><<<wblocks, kWideThreads, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case 16: permute_rows_wide_kernel<16, SI><<<wblocks, kWideThreads, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case 8: permute_rows_wide_kernel<8, SI><<<wblocks, kWideThreads, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
     case 4: permute_rows_kernel<4, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
     case 2: permute_rows_kernel<2, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case -32: permute_rows_kernel<32, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case -16: permute_rows_kernel<16, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
+    case -8: permute_rows_kernel<8, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
     default: permute_rows_kernel<1, SI><<<blocks, 256, 0, s>>>(d_tasks, d_row_start, n_tasks, total_rows, d_contribs, src, dst); break;
   }
   count_launch();
 }
 
 void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_row_start, int n_tasks, int64_t total_rows,
-                    int group, bool narrow, const xgb_perm_contrib* d_contribs, const double* src, double* dst,
-                    cudaStream_t s) {
-  if (narrow) launch_permute_t<int32_t>(d_tasks, d_row_start, n_tasks, total_rows, group, d_contribs, src, dst, s);
-  else launch_permute_t<int64_t>(d_tasks, d_row_start, n_tasks, total_rows, group, d_contribs, src, dst, s);
+                    int group, bool narrow, bool single, const xgb_perm_contrib* d_contribs, const double* src,
+                    double* dst, cudaStream_t s) {
+  if (narrow)
+    launch_permute_t<int32_t>(d_tasks, d_row_start, n_tasks, total_rows, group, single, d_contribs, src, dst, s);
+  else launch_permute_t<int64_t>(d_tasks, d_row_start, n_tasks, total_rows, group, single, d_contribs, src, dst, s);
 }
 
 // ======================================================================= shared helpers
@@ -1269,7 +1456,7 @@ int xgb_permute(int n_tasks, const xgb_perm_task* tasks, int n_contrib, const xg
   auto* dt = upload(tasks, size_t(n_tasks), s);
   auto* ds = upload(rows.row_start.data(), rows.row_start.size(), s);
   auto* dc = upload(contribs, size_t(n_contrib), s);
-  launch_permute(dt, ds, n_tasks, rows.total_rows, rows.group, rows.narrow, dc, src, dst, s);
+  launch_permute(dt, ds, n_tasks, rows.total_rows, rows.group, rows.narrow, rows.single, dc, src, dst, s);
   dev_free(dt);
   dev_free(ds);
   dev_free(dc);

@@ -86,11 +86,12 @@ struct PermRows {
   int64_t total_rows = 0;
   int group = 1;
   bool narrow = true;  // every stride fits 32 bits (the kernel keeps them in 32-bit registers)
+  bool single = true;  // every task has exactly one contribution (no SU(2) sums)
 };
 PermRows perm_rows(const xgb_perm_task* tasks, int n_tasks, const xgb_perm_contrib* contribs, int n_contrib);
 void launch_permute(const xgb_perm_task* d_tasks, const int64_t* d_row_start, int n_tasks, int64_t total_rows,
-                    int group, bool narrow, const xgb_perm_contrib* d_contribs, const double* src, double* dst,
-                    cudaStream_t s);
+                    int group, bool narrow, bool single, const xgb_perm_contrib* d_contribs, const double* src,
+                    double* dst, cudaStream_t s);
 // h_descs: host copy of the descriptors (blocks at least kSvdGridMin wide run one at a time on a
 // grid-wide Jacobi kernel over all SMs; nullptr keeps every block on the cluster kernel)
 void launch_svd(const xgb_svd_desc* d_descs, const xgb_svd_desc* h_descs, const int64_t* d_work_off, int n,

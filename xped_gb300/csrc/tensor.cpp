@@ -152,6 +152,7 @@ struct PermPlan {
   int64_t total_rows = 0;
   int group = 1;
   bool narrow = true;
+  bool single = true;
   xgb_perm_task* d_tasks = nullptr;
   int64_t* d_row_start = nullptr;
   xgb_perm_contrib* d_contribs = nullptr;
@@ -198,6 +199,7 @@ std::shared_ptr<PermPlan> upload_tables(const PermTables& t) {
   plan->total_rows = rows.total_rows;
   plan->group = rows.group;
   plan->narrow = rows.narrow;
+  plan->single = rows.single;
   plan->d_row_start = plan->mem.table(rows.row_start);
   plan->d_contribs = plan->mem.table(t.contribs);
   for (const auto& task : t.tasks) plan->bytes += 8.0 * double(task.nelem) * (1 + task.n_contrib);
@@ -442,7 +444,7 @@ std::shared_ptr<PermPlan> get_perm_plan(const TensorMeta& m, uint32_t mask, int 
 Tensor run_perm_plan(const PermPlan& plan, const Tensor& src) {
   Tensor out = plan.needs_zero ? zeros(plan.out) : empty_like_meta(plan.out);
   prof_begin(K_PERMUTE, stream());
-  launch_permute(plan.d_tasks, plan.d_row_start, plan.n_tasks, plan.total_rows, plan.group, plan.narrow,
+  launch_permute(plan.d_tasks, plan.d_row_start, plan.n_tasks, plan.total_rows, plan.group, plan.narrow, plan.single,
                  plan.d_contribs, src.data(), out.data(), stream());
   prof_end(K_PERMUTE, stream(), plan.bytes);
   return out;
