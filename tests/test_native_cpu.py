@@ -1,7 +1,8 @@
 """CPU-side checks of the native library: it loads, exports every symbol the
 headers declare, and its host metadata (bases, fusion trees, sector order,
 permute and GEMM plans) matches the oracle bit for bit.  The permute plans
-are executed here by a numpy emulation of the kernel's index arithmetic."""
+are executed here by numpy emulations of the index arithmetic of both permute
+kernels (the row cursor and the wide-row form)."""
 import itertools
 import re
 from pathlib import Path
@@ -153,6 +154,124 @@ def emulate_permute(tasks, contribs, src, n_out, sms=152):
             step(cur, t, contribs[t.contrib0] if single else None)
     assert seen.max() <= 1  # tasks tile disjoint regions of the output
     return dst
+
+
+def _perm_rows(tasks):
+    row_start = [0]
+    elems = weighted = 0.0
+    for t in tasks:
+        d0 = max(t.dims[0], 1) if t.rank > 0 else 1
+        row_start.append(row_start[-1] + t.nelem // d0)
+        elems += t.nelem
+        weighted += t.nelem * d0
+    avg = weighted / elems if elems > 0 else 1.0
+    G = 1
+    while G < 32 and 2.0 * G <= avg * 1.25:
+        G *= 2
+    return row_start, G
+
+
+def emulate_permute_wide(tasks, contribs, src, n_out, sms=152):
+    """The index arithmetic of permute_rows_wide_kernel: 128-thread CTAs (at most six per SM),
+    chunks of 8 rows taken per warp (chunk = warp * (32 / G) + group, stepping by all warps'
+    groups), decoder lane u of a group decoding row 8 * chunk + u from scratch (task by search,
+    multi-index by division), lane gl copying elements j * G + gl (j = 0, 1) of every row of the
+    chunk and the rest of a long row from 2G + gl on in steps of G.  Every chunk must be visited
+    once, every index must lie inside its buffer and every output element is written at most once."""
+    n = len(tasks)
+    row_start, G = _perm_rows(tasks)
+    assert G >= 8 and all(t.n_contrib == 1 for t in tasks)
+    total_rows = row_start[-1]
+    dst = np.zeros(n_out)
+    if total_rows == 0:
+        return dst
+    RPC, SLOTS, THREADS = 8, 2, 128
+    gpw = 32 // G
+    nchunks = (total_rows + RPC - 1) // RPC
+    per_block = THREADS // G
+    blocks = max(1, min(sms * 6, (nchunks + per_block - 1) // per_block))
+    nwarps = blocks * THREADS // 32
+    step = nwarps * gpw
+    seen = np.zeros(n_out, dtype=np.int64)
+    visited = np.zeros(nchunks, dtype=np.int64)
+
+    def decode(r):
+        ti = int(np.searchsorted(row_start, r, side="right") - 1)
+        assert 0 <= ti < n and row_start[ti] <= r < row_start[ti + 1]
+        t, c = tasks[ti], contribs[tasks[ti].contrib0]
+        rem = r - row_start[ti]
+        dofs, sofs = t.dst_base, c.src_base
+        for k in range(1, t.rank):
+            ik = rem % t.dims[k]
+            rem //= t.dims[k]
+            dofs += ik * t.dst_stride[k]
+            sofs += ik * c.src_stride[k]
+        ln = t.dims[0] if t.rank > 0 else 1
+        ds0 = t.dst_stride[0] if t.rank > 0 else 0
+        ss0 = c.src_stride[0] if t.rank > 0 else 0
+        return dofs, sofs, ln, ds0, ss0, c.coeff
+
+    for warp in range(nwarps):
+        cb = warp * gpw
+        while cb < nchunks:
+            for g in range(gpw):
+                chunk = cb + g
+                if chunk >= nchunks:
+                    continue
+                visited[chunk] += 1
+                for u in range(RPC):
+                    r = chunk * RPC + u
+                    if r >= total_rows:
+                        continue
+                    dofs, sofs, ln, ds0, ss0, coeff = decode(r)
+                    head = [j * G + gl for j in range(SLOTS) for gl in range(G)]
+                    tail = [i for gl in range(G) for i in range(SLOTS * G + gl, ln, G)]
+                    i = np.array([x for x in head if x < ln] + tail, dtype=np.int64)
+                    assert sorted(i.tolist()) == list(range(ln))
+                    so, do = sofs + i * ss0, dofs + i * ds0
+                    assert so.min() >= 0 and so.max() < len(src) and do.min() >= 0 and do.max() < n_out
+                    dst[do] = coeff * src[so]
+                    np.add.at(seen, do, 1)
+            cb += step
+    assert (visited == 1).all()
+    assert seen.max() <= 1
+    return dst
+
+
+def run_permute_plan(tasks, contribs, src, n_out):
+    """The kernel launch_permute picks: the wide-row kernel for single-contribution plans whose
+    groups have 8 or more lanes, the cursor kernel otherwise."""
+    _, G = _perm_rows(tasks)
+    if G >= 8 and all(t.n_contrib == 1 for t in tasks):
+        return emulate_permute_wide(tasks, contribs, src, n_out)
+    return emulate_permute(tasks, contribs, src, n_out)
+
+
+# degeneracies large enough that most permute plans take the wide-row kernel
+WIDE_CASES = [
+    ("u1", [(-1, 2), (0, 10), (1, 3)], [(0, 4), (1, 13), (2, 1)]),
+    ("fz2", [(0, 9), (1, 14)], [(0, 2), (1, 11)]),
+]
+
+
+@pytest.mark.parametrize("symname,pB,pC", WIDE_CASES)
+def test_wide_permute_plans_match_oracle(symname, pB, pC):
+    from xped_gb300 import Tensor
+    rng = np.random.default_rng(4)
+    s, oB, nB = pair_basis(symname, pB)
+    _, oC, nC = pair_basis(symname, pC)
+    ot = oracle.Tensor(s, [oB, oC], [oB, oC]).set_random(rng)
+    nt = Tensor.meta([nB, nC], [nB, nC])
+    src = ot.data()
+    wide = 0
+    for p, shift in [((0, 1, 2, 3), 0), ((0, 2, 1, 3), 0), ((1, 0, 3, 2), 1), ((3, 1, 0, 2), -1), ((2, 3, 0, 1), 2),
+                     ((1, 3, 2, 0), -2)]:
+        ref = ot.permute(shift, list(p))
+        tasks, contribs, outm = nt.permute_plan(shift, list(p))
+        wide += _perm_rows(tasks)[1] >= 8
+        got = run_permute_plan(tasks, contribs, src, outm.size)
+        assert np.array_equal(got, ref.data())
+    assert wide >= 3
 
 
 @pytest.mark.parametrize("symname,pB,pC", CASES)
