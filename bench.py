@@ -372,14 +372,26 @@ def profile_step(args):
     from xped_gb300 import ensure_device, lib
     ensure_device(dist_info()[2])
     L = lib()
+    # --autotune-cache: the first run measures and saves its choices, a later run (e.g. under a profiler,
+    # whose launch interception would skew the measurements) loads them, so both profile the same launches
+    cache = args.autotune_cache
+    loaded = 0
     if args.autotune:
-        L.xgb_autotune_set(1)
+        if cache and os.path.exists(cache):
+            loaded = L.xgb_autotune_load(cache.encode())
+            if loaded <= 0:
+                raise RuntimeError(f"autotune cache {cache}: no entries for this GPU")
+            L.xgb_autotune_set(2)
+        else:
+            L.xgb_autotune_set(1)
     A, _ = site_tensor(AUX)
     c = make_ctm(A, CHI, "chosen", args.gemm, args.sketch_tail)
     for _ in range(args.warmup):
         c.grow_all()
     L.xgb_synchronize()
     if args.autotune:
+        if cache and not loaded and L.xgb_autotune_save(cache.encode()) != 0:
+            raise RuntimeError(f"autotune cache {cache} not written")
         L.xgb_autotune_set(2)
     rt = None
     with open("/proc/self/maps") as f:  # the CUDA runtime the library itself loaded
@@ -395,7 +407,7 @@ def profile_step(args):
     L.xgb_synchronize()
     rt.cudaProfilerStop()
     return {"ms": L.xgb_event_elapsed_ms(0, 1), "launches": L.xgb_launch_count() - n0, "gemm": args.gemm,
-            "workload": WORKLOAD}
+            "workload": WORKLOAD, "autotune_cache": cache, "autotune_loaded": int(loaded)}
 
 
 def dtype_label(args):
@@ -1168,6 +1180,9 @@ def main():
     ap.add_argument("--profile-step", action="store_true",
                     help="warm up the chosen form, then run one step between cudaProfilerStart / Stop (for ncu "
                          "--profile-from-start off) and print its CUDA-event time")
+    ap.add_argument("--autotune-cache", default=None, metavar="PATH",
+                    help="with --profile-step: load the autotuner's choices from PATH if it exists, else measure "
+                         "them during the warm-up and save them there")
     ap.add_argument("--permute-only", action="store_true",
                     help="run only the permute HBM roofline case (1.42 GB U(1) Tensor<2,2>) and print it")
     ap.add_argument("--permute-degs", default="20,40,60,40,20",
