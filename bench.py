@@ -219,7 +219,8 @@ def run_gpu(args):
     st1 = ctm.stats()
     res["cols_per_step"] = (st1["sketch_cols"] - st0["sketch_cols"]) / args.steps
     res["redo_per_step"] = (st1["redo"] - st0["redo"]) / args.steps
-    res["launches"] = (L.xgb_launch_count() - launches0) / max(args.steps, 1)
+    res["launches"] = int(L.xgb_launch_count() - launches0)  # this library's kernels in the K timed steps
+    res["launches_per_step"] = res["launches"] / max(args.steps, 1)
     res["clocks"] = sampler.stop()
     res["step_ms"] = float(np.mean(step_ms))
     res["step_ms_all"] = step_ms
@@ -1284,7 +1285,7 @@ def main():
                            gemm=args.gemm, parallelism=f"replicas x{world}"),
             "e2e": {"value": world * 1e3 / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"]},
-            "gpu_launches": r["launches"], "clocks": r["clocks"],
+            "gpu_launches": r["launches"], "gpu_launches_per_step": r["launches_per_step"], "clocks": r["clocks"],
             "roofline": roofline(prof, r["prof_steps"], r.get("fp64_peak")),
             "block_gemm": {"form": args.gemm, "tflops": (g[2] / (g[1] * 1e-3) / 1e12) if g[1] > 0 else None,
                            "ms_per_step": g[1] / r["prof_steps"]},
