@@ -187,7 +187,7 @@ int xgb_batched_svd(int n, const xgb_svd_desc* descs, const double* A, double* U
    one fixed 16 MiB device array per GPU
    (xgb_batched_svd_noalloc_capacity_bytes()) that the library holds until
    exit; batches needing more return XGB_E_UNSUPPORTED (one square block of
-   up to about 580 columns fits).  The array's address is looked up on the
+   up to 647 columns fits: an n x n block needs about 5 n^2 doubles).  The array's address is looked up on the
    first call on each device, so make that first call before any stream
    capture.  All calls share the array: calls that overlap on the GPU
    (different streams or host threads) race and must be serialised by the
